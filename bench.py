@@ -1,0 +1,352 @@
+"""Benchmark of the compressible Newton-Krylov hot path on one GB300.
+
+Workload (the at-scale case of the benchmark definitions): unit cube,
+128^3 hexes x 6 = 12,582,912 linear tets, 2,146,689 stored nodes, periodic in
+y and z, Dirichlet inflow / natural outflow in x, Mach 0.3, Re 1000, gamma 1.4,
+Pr 0.72, uniform flow + seeded 1% Gaussian noise, generalized alpha
+(rho_inf = 0.5) at CFL 1, GMRES Kspace 20, tol 1e-3, 3 Newton iterations per
+time step.  Synthetic data (no mesh files exist for it).
+
+A "step" is one Newton iteration (one flow solve of the itrdrv multi-corrector:
+SolMFG + itrCorrect + itrBC).  Steps run in time steps of 3 iterations.
+``value`` = elements x steps / device time, inputs resident in HBM;
+``e2e`` = the same through the host-buffer C ABI (phgpu_time_step), host<->device
+copies inside the timed region.  The state and mesh (> 300 MB) exceed the
+129 MB L2, so no flush is needed between steps.
+
+``--impl reference`` times the reference algorithm's CPU restatement (the
+oracle) with all host threads on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NEWTON_PER_TIMESTEP = 3
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([s.strip() for s in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[3 + i]})
+        pw = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "power_w_max": max(pw) if pw else None, "samples": len(self.samples)}
+
+
+def make_workload(n: int, precision: str):
+    from phasta_gb300 import _lib as L
+    from phasta_gb300 import mesh
+    from phasta_gb300.solver import make_params
+
+    case, ph = mesh.channel_case(n, mach=0.3, re=1000.0)
+    prec = L.PHGPU_MIXED if precision == "mixed" else L.PHGPU_FP64
+    ap = L.PHGPU_AP_LINEAR if precision == "mixed" else L.PHGPU_AP_FD
+    params = make_params(ph["mu"], ph["dt"], rho_inf=0.5, Kspace=20, etol=1e-3, minIters=1,
+                         precision=prec, ap_mode=ap)
+    y0 = mesh.uniform_state(case, 0.3, sigma=0.01)
+    ac0 = np.zeros_like(y0)
+    return case, params, y0, ac0
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    from phasta_gb300.solver import GpuSolver
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    case, params, y0, ac0 = make_workload(args.n, args.precision)
+    E = case.nelem
+    g = GpuSolver(case, params)
+    stream = torch.cuda.ExternalStream(g.stream())
+
+    def run_steps(k):
+        done = 0
+        while done < k:
+            nitr = min(NEWTON_PER_TIMESTEP, k - done)
+            g.time_step_dev(nitr)
+            done += nitr
+
+    g.upload(y0, ac0, y0, ac0)
+    run_steps(args.warmup)
+    g.upload(y0, ac0, y0, ac0)
+    g.set_params(istep=0, eGMRES=0.0)
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.barrier()
+    torch.cuda.synchronize()
+    l0 = g.kernel_launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        ev0.record(stream)
+        t0 = time.perf_counter()
+        run_steps(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = g.kernel_launches - l0
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        import torch.distributed as tdist
+        t = torch.tensor([ms], device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * E * args.steps / (ms / 1e3)
+
+    # convergence record of one time step (outside the timed region)
+    g.upload(y0, ac0, y0, ac0)
+    g.set_params(istep=0, eGMRES=0.0)
+    r0 = g.residual_norm_dev()
+    iks, rn = [], []
+    for it in range(1, NEWTON_PER_TIMESTEP + 1):
+        g.set_params(iter=it)
+        st = g.newton_dev()
+        iks.append(st.iKs)
+        rn.append(st.rnorm)
+    r_end = g.residual_norm_dev()
+
+    # e2e: host buffers through the reference-facing time-step call
+    yold, acold = y0.copy(), ac0.copy()
+    g.set_params(istep=0, eGMRES=0.0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ksteps = max(1, args.steps // NEWTON_PER_TIMESTEP)
+    for _ in range(ksteps):
+        yold, acold, y, ac, st = g.time_step(yold, acold, NEWTON_PER_TIMESTEP)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_steps = ksteps * NEWTON_PER_TIMESTEP
+    e2e = {"value": world * E * e2e_steps / e2e_s, "unit": "elements/s",
+           "h2d_bytes_per_step": int(2 * 5 * case.nshg * 8 / NEWTON_PER_TIMESTEP),
+           "d2h_bytes_per_step": int(4 * 5 * case.nshg * 8 / NEWTON_PER_TIMESTEP)}
+
+    # dominant kernel: the FP32 linearized residual sweep of the Ap product
+    roof = kernel_roofline(g, case, stream, args)
+    result = {
+        "metric": "Newton-step throughput to 1e-3 relative nonlinear residual (elements/s)",
+        "value": value, "unit": "elements/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 assembly/Ap, f64 residual/dots/Givens/LU" if args.precision == "mixed" else "f64",
+        "data": "synthetic",
+        "config": {"workload": f"channel {args.n}^3x6 tets Mach0.3 Re1000, Kspace20 tol1e-3, 3 Newton/step",
+                   "elements": E, "nodes": case.nshg, "precision": args.precision,
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "e2e": e2e, "gpu_launches": int(launches), "wall_s": wall,
+        "newton": {"krylov_iterations": iks, "residual_before_each": rn, "rel_residual_after_3": r_end / r0},
+        "roofline": roof, "clocks": clk.summary(),
+    }
+    if args.precision == "mixed" and not args.skip_fp64:
+        result["fp64_plain"] = fp64_plain(args, case)
+    g.close()
+    return result
+
+
+def kernel_roofline(g, case, stream, args):
+    import torch
+
+    g.sweep_dev(5)  # FP32 shadows of the state
+    for _ in range(3):
+        g.sweep_dev(2)
+    torch.cuda.synchronize()
+    reps = 10
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        g.sweep_dev(2)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / reps / 1e3
+    E, N = case.nelem, case.nshg
+    # compulsory bytes of one linearized sweep: int4 connectivity per element;
+    # per node the direction (5 f32), base state (5 f32), coordinates (3 f32)
+    # read and the product (5 f32) read and written
+    algo = 16 * E + N * (20 + 20 + 12 + 40)
+    peak, src = peaks()
+    achieved = algo / t / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "lin_sweep_traffic.json"
+    if tp.exists():
+        d = json.loads(tp.read_text())
+        traffic = d["bytes_per_element"] * E
+    return {"kernel": "k_elem_res<float, RM_LIN> (all colours of one sweep)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": f"{src} hbm_gbs", "traffic": traffic, "algorithmic_bytes": algo,
+            "sweep_ms": t * 1e3, "elements_per_s": E / t}
+
+
+def fp64_plain(args, case):
+    """The reference arithmetic on the same GPU: FP64 everywhere, finite-difference Au1MFG."""
+    import torch
+
+    from phasta_gb300.solver import GpuSolver
+
+    case, params, y0, ac0 = make_workload(args.n, "fp64")
+    g = GpuSolver(case, params)
+    g.upload(y0, ac0, y0, ac0)
+    g.set_params(istep=0, eGMRES=0.0)
+    torch.cuda.synchronize()
+    r0 = g.residual_norm_dev()
+    t0 = time.perf_counter()
+    iks = []
+    for it in range(1, NEWTON_PER_TIMESTEP + 1):
+        g.set_params(iter=it)
+        st = g.newton_dev()
+        iks.append(st.iKs)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    r_end = g.residual_norm_dev()
+    g.close()
+    return {"ms_per_step": dt * 1e3 / NEWTON_PER_TIMESTEP,
+            "value": case.nelem * NEWTON_PER_TIMESTEP / dt, "krylov_iterations": iks,
+            "rel_residual_after_3": r_end / r0}
+
+
+def cpu_sample(n_sample: int, steps: int = 1):
+    """The oracle (reference algorithm, FP64, finite-difference Au1MFG) on host threads."""
+    from oracle.pyoracle import Oracle
+
+    case, params, y0, ac0 = make_workload(n_sample, "fp64")
+    threads = os.cpu_count() or 1
+    o = Oracle(case, params, nthreads=threads, grouped=True)
+    t0 = time.perf_counter()
+    y, ac = y0, ac0
+    for it in range(1, steps + 1):
+        o.set_params(iter=it)
+        y, ac, st, _ = o.newton(y, ac, y0, ac0)
+    dt = time.perf_counter() - t0
+    return {"value": case.nelem * steps / dt, "unit": "elements/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} Newton iteration(s) of the channel case at {n_sample}^3x6 = {case.nelem} tets "
+                      f"(FP64, Kspace 20, tol 1e-3), {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return None
+    n_s = args.cpu_sample_n
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(n_s)
+    t0 = time.perf_counter()
+    last = None
+    for _ in range(args.steps):
+        last = cpu_sample(n_s)
+        vals.append(last["value"])
+    wall = time.perf_counter() - t0
+    v = float(np.mean(vals))
+    return {"impl": "reference", "metric": "Newton-step throughput to 1e-3 relative nonlinear residual (elements/s)",
+            "value": v, "unit": "elements/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": wall * 1e3 / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"channel {args.n}^3x6 tets Mach0.3 Re1000, Kspace20 tol1e-3, 3 Newton/step",
+                       "sample_n": n_s},
+            "cpu_baseline": {**last, "value": v},
+            "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-sample-n", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true")
+    args = ap.parse_args()
+    rank, world, _ = _dist()
+    if args.impl == "reference":
+        out = run_reference(args)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    from phasta_gb300 import build
+    if rank == 0:
+        build.build()
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.barrier()
+    res = run_gpu(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            res["cpu_baseline"] = cpu_sample(args.cpu_sample_n)
+        print(json.dumps(res))
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

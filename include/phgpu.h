@@ -1,0 +1,158 @@
+/*
+ * phgpu.h -- C ABI of the GB300-native drop-in for PHASTA's compressible
+ * matrix-free Newton-Krylov hot path (one GPU, sm_103a).
+ *
+ * The entry points replace, with the same argument meaning, these reference
+ * routines (paths within the PHASTA project):
+ *
+ *   phgpu_elmmfg     ElmMFG   phSolver/compressible/elmmfg.f:1-5
+ *                    (interior AsIMFG/e3 + boundary AsBMFG/e3b + bc3Res + bc3BDg)
+ *   phgpu_elmres     ElmMFG with iprec = 0 and no modified residual (res only)
+ *   phgpu_itrres     ItrRes   phSolver/compressible/itrres.f:1-5 (adds into rmes)
+ *   phgpu_i3lu       i3LU     phSolver/compressible/i3lu.f:1
+ *   phgpu_solmfg     SolMFG   phSolver/compressible/solmfg.f:1-7
+ *   phgpu_itrcorrect itrCorrect + itrBC  phSolver/compressible/itrPC.f:128, itrbc.f:1
+ *   phgpu_newton     one flow solve of the itrdrv multi-corrector loop
+ *                    (SolMFG + itrCorrect + itrBC, itrdrv.f:489-506, 596-598)
+ *   phgpu_time_step  itrPredict + itrBC + nitr x phgpu_newton + itrUpdate + itrBC
+ *                    (itrdrv.f:398-399, 427-634, 651-652)
+ *
+ * Host arrays keep the reference layout (Fortran column-major, node index
+ * fastest) and dof orders:
+ *   y, ac, yold, acold (nshg, 5): y[k*nshg + n], k over (u, v, w, p, T)
+ *   res, rmes, Dy      (nshg, 5): r[k*nshg + n], k over (continuity, x-, y-, z-momentum, energy)
+ *                                  = the (p, u, v, w, T) order of the element routines
+ *   BDiag        (nshg, 5, 5)   : bd[(i + 5*j)*nshg + n]
+ *   x            (nshg, 3)      : x[d*nshg + n]
+ * Connectivity is 0-based.  The "_dev" suffix marks entry points that work on
+ * the state already resident in the context's device memory.
+ *
+ * Every entry point returns a status code instead of stopping the program as
+ * the reference's error()/tnanq do (common/error.f, tnanq.f); the message of
+ * the last failure is available from phgpu_last_error().
+ */
+#ifndef PHGPU_H
+#define PHGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    PHGPU_OK = 0,
+    PHGPU_ERR_INVALID = 1,     /* bad argument or size */
+    PHGPU_ERR_CUDA = 2,        /* CUDA runtime failure (no device, launch failure, ...) */
+    PHGPU_ERR_NONFINITE = 3,   /* NaN/Inf in a residual or in the solution update (tnanq.f) */
+    PHGPU_ERR_SINGULAR = 4,    /* zero or non-finite pivot in the 5x5 block LU */
+    PHGPU_ERR_UNSUPPORTED = 5, /* option outside the implemented path */
+    PHGPU_ERR_NOMEM = 6        /* device allocation failed */
+};
+
+enum { PHGPU_FP64 = 0, PHGPU_MIXED = 1 };         /* precision */
+enum { PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1 };     /* Jacobian-vector product */
+enum { PHGPU_LU_FACT = 0, PHGPU_LU_FORWARD = 1, PHGPU_LU_BACKWARD = 2, PHGPU_LU_PRODUCT = 3 };
+
+/* The COMMON-block values the hot path reads (common.h), plus three options
+ * of this implementation.  Field meanings follow the reference names. */
+typedef struct {
+    double Rgas, gamma, gamma1, pr;  /* mmatpar: gas constant, gamma, gamma-1, Prandtl */
+    double rmu;                      /* datmat(1,2,1): constant viscosity (matflg(2)=0) */
+    double Dtgl, almi, alfi, gami;   /* timdat: 1/dt and generalized-alpha factors */
+    double dtsfct, taucfct, temper;  /* Tau Time Constant, Tau C Scale Factor, Temperature scaling */
+    int itau;                        /* 0 (Diagonal-Shakib) is the implemented tau */
+    int ivart;                       /* 2 = SUPG, 1 = Galerkin */
+    int iremoveStabTimeTerm;
+    int Navier;                      /* 1 = Navier-Stokes, 0 = Euler */
+    int ipord;                       /* 1 = linear basis (implemented) */
+    int EntropyPressure;
+    int Kspace, nGMRES, minIters;    /* solpar */
+    double etol;                     /* epstol(1) */
+    double epsM;                     /* sqrt(machine epsilon), input.f:30 */
+    double eGMRES;                   /* finite-difference interval (itrpar), in/out */
+    int iter, istep;                 /* Newton iteration (1-based) and time step (0-based) */
+    /* options of this implementation */
+    int precision;                   /* PHGPU_FP64: reference arithmetic; PHGPU_MIXED: FP32
+                                        assembly and Ap, FP64 outer residual, dots, Givens, LU */
+    int ap_mode;                     /* PHGPU_AP_FD (Au1MFG) or PHGPU_AP_LINEAR */
+    int reserved[6];
+} phgpu_config;
+
+/* Mesh and boundary-condition arrays (what the reference keeps in
+ * pointer_data mien/mienb/miBCB/mBCB and in iBC/BC/iper). */
+typedef struct {
+    int nshg;             /* nodes (periodic slaves are stored, as in the reference) */
+    int nelem;            /* interior linear tets */
+    const int* ien;       /* nelem*4, element-major: ien[4*e + a] */
+    const double* x;      /* (nshg, 3) */
+    int nbelem;           /* boundary tets, boundary face = local nodes 0,1,2 */
+    const int* ienb;      /* nbelem*4 */
+    const int* iBCB;      /* nbelem*2: (flux bits as iBCB(:,1), surface id) */
+    const double* BCB;    /* nbelem*3*6: BCB[(e*3 + n)*6 + k] as BCB(e, n, k) */
+    const int* iBC;       /* nshg: BC bit codes (bit 1 T, bit 2 p, bits 3-5 velocity, bit 10 periodic) */
+    const double* BC;     /* (nshg, 6) column-major, BC(:,k) */
+    const int* iper;      /* nshg: periodic master (== n when not periodic) */
+} phgpu_mesh;
+
+typedef struct {
+    int iKs;              /* Krylov iterations of the last GMRES cycle (solmfg.f:222) */
+    int lGMRES;           /* restarts */
+    int ntotGM;           /* running total of GMRES iterations (in/out) */
+    int status;
+    double unorm0;        /* ||L^-1 R|| before GMRES */
+    double echeck;        /* final |eBrg(iKs+1)| */
+    double eGMRES;        /* finite-difference interval used */
+    double totres;        /* rstat measure: sqrt(sum res^2)/nshg of L^-1 R */
+    double rnorm;         /* unpreconditioned FP64 ||R|| after BCs (nonlinear residual) */
+    double t_assembly_ms, t_gmres_ms; /* device time of the phases, if timing is on */
+} phgpu_stats;
+
+typedef struct phgpu_ctx phgpu_ctx;
+
+/* set-up: copies the mesh to the device, colours the elements; one GPU, one stream */
+int phgpu_create(const phgpu_mesh* mesh, const phgpu_config* cfg, phgpu_ctx** out);
+int phgpu_destroy(phgpu_ctx* ctx);
+int phgpu_set_config(phgpu_ctx* ctx, const phgpu_config* cfg);
+int phgpu_get_config(phgpu_ctx* ctx, phgpu_config* cfg);
+const char* phgpu_last_error(phgpu_ctx* ctx);
+void* phgpu_stream(phgpu_ctx* ctx);        /* the cudaStream_t every kernel runs on */
+int phgpu_num_colors(phgpu_ctx* ctx);
+long long phgpu_kernel_launches(phgpu_ctx* ctx); /* kernels launched since create */
+
+/* ElmMFG: res, rmes, BDiag (BDiag only when iprec != 0) */
+int phgpu_elmmfg(phgpu_ctx* ctx, const double* y, const double* ac,
+                 double* res, double* rmes, double* bdiag, int iprec);
+/* residual only (ires = 1) with boundary faces and bc3Res */
+int phgpu_elmres(phgpu_ctx* ctx, const double* y, const double* ac, double* res);
+/* ItrRes: rmes += Rmod(yp; yc), then bc3Res */
+int phgpu_itrres(phgpu_ctx* ctx, const double* yp, const double* yc, const double* ac,
+                 double* rmes);
+/* i3LU on host arrays */
+int phgpu_i3lu(phgpu_ctx* ctx, double* bdiag, double* r, int code);
+/* SolMFG: outputs res = L^-1 R, bdiag = LU factors, Dy */
+int phgpu_solmfg(phgpu_ctx* ctx, const double* y, const double* ac,
+                 double* res, double* bdiag, double* Dy, phgpu_stats* st);
+/* itrCorrect + itrBC on host arrays */
+int phgpu_itrcorrect(phgpu_ctx* ctx, double* y, double* ac, const double* yold,
+                     const double* acold, const double* Dy);
+/* one multi-corrector flow solve on host arrays (y, ac updated in place) */
+int phgpu_newton(phgpu_ctx* ctx, double* y, double* ac, const double* yold,
+                 const double* acold, phgpu_stats* st);
+/* one time step: yold/acold updated in place, y/ac returned */
+int phgpu_time_step(phgpu_ctx* ctx, double* yold, double* acold, double* y, double* ac,
+                    int nitr, phgpu_stats* st);
+
+/* device-resident state (no host traffic inside) */
+int phgpu_upload_state(phgpu_ctx* ctx, const double* y, const double* ac,
+                       const double* yold, const double* acold);
+int phgpu_download_state(phgpu_ctx* ctx, double* y, double* ac, double* yold, double* acold);
+int phgpu_newton_dev(phgpu_ctx* ctx, phgpu_stats* st);
+int phgpu_time_step_dev(phgpu_ctx* ctx, int nitr, phgpu_stats* st);
+/* nonlinear residual ||R(y)|| (FP64, unpreconditioned, after BCs) of the resident state */
+int phgpu_residual_norm_dev(phgpu_ctx* ctx, double* rnorm);
+/* one FP32/FP64 residual sweep of the resident state (timing probe of the hot kernel) */
+int phgpu_sweep_dev(phgpu_ctx* ctx, int which);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

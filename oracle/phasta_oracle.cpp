@@ -1,0 +1,1290 @@
+// phasta_oracle.cpp -- CPU restatement (FP64) of PHASTA's compressible
+// matrix-free Newton-Krylov hot path.
+//
+// TEST INFRASTRUCTURE ONLY: the parity checker of the GB300 kernels and the
+// timed CPU baseline of the benchmark.  Nothing in the product links it.
+//
+// Every routine below follows the reference routine it names statement by
+// statement, in the same operation order (array statements over the npro
+// element vector become per-element scalar statements, which evaluates the
+// same arithmetic).  Compile with -ffp-contract=off so no multiply-add is
+// fused behind the restatement's back.  Terms the reference leaves out
+// because they multiply structural zeros of the Euler Jacobians are written
+// here as dense sums; adding an exact zero leaves every partial sum unchanged.
+#include "phasta_oracle.h"
+
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+#include <algorithm>
+#include <cstdint>
+
+namespace {
+
+// numeric constants of common.h:281-296
+const double zero = 0.0, one = 1.0, two = 2.0, three = 3.0, four = 4.0;
+const double pt125 = 0.125, pt5 = 0.5;
+const double pt66 = 0.6666666666666666666666666666667;
+
+// ---------------------------------------------------------------------------
+// quadrature and shape functions for linear tets
+//   symtet.c (4-point rule, barycentric (a,b,b,b) permutations, weights 1/4)
+//   genint.f:72-73 (Qwt *= 4/3, Qwtb *= 2)
+//   uniformP.c TetShapeAndDrv (N = L, dN of the vertex modes)
+//   genshp.f:32-35 / genshpb.f (shgl /= 2 for tets)
+//   symtri.c (3-point rule (B,C,C) with weights A)
+// ---------------------------------------------------------------------------
+struct Tables {
+    double shp[4][4];      // [q][a]
+    double shgl[4][3][4];  // [q][i][a]
+    double Qwt[4];
+    double shpb[3][4];
+    double shglb[3][3][4];
+    double Qwtb[3];
+};
+
+void tet_shape(const double par[3], double N[4], double dN[4][3]) {
+    // uniformP.c:8-30 vertex modes
+    double L[4] = {par[0], par[1], par[2], 1.0 - par[0] - par[1] - par[2]};
+    for (int i = 0; i < 4; ++i) {
+        N[i] = L[i];
+        for (int j = 0; j < 3; ++j)
+            dN[i][j] = (i == 3) ? -1.0 : (i == j ? 1.0 : 0.0);
+    }
+}
+
+Tables make_tables() {
+    Tables t;
+    const double a4 = 0.5854101966249685, b4 = 0.1381966011250150;  // symtet.c
+    const double pts[4][4] = {{a4, b4, b4, b4}, {b4, a4, b4, b4}, {b4, b4, a4, b4}, {b4, b4, b4, a4}};
+    for (int q = 0; q < 4; ++q) {
+        double N[4], dN[4][3];
+        tet_shape(pts[q], N, dN);
+        for (int a = 0; a < 4; ++a) {
+            t.shp[q][a] = N[a];
+            for (int i = 0; i < 3; ++i) t.shgl[q][i][a] = dN[a][i] / two;
+        }
+        t.Qwt[q] = (four / three) * 0.25;
+    }
+    const double A = 0.3333333333333330000000000000000000, B = 0.666666666666667,
+                 C = 0.166666666666667;  // symtri.c
+    const double ptb[3][3] = {{B, C, C}, {C, B, C}, {C, C, B}};
+    for (int q = 0; q < 3; ++q) {
+        double N[4], dN[4][3];
+        tet_shape(ptb[q], N, dN);
+        for (int a = 0; a < 4; ++a) {
+            t.shpb[q][a] = N[a];
+            for (int i = 0; i < 3; ++i) t.shglb[q][i][a] = dN[a][i] / two;
+        }
+        t.Qwtb[q] = two * A;
+    }
+    return t;
+}
+
+const Tables& tables() {
+    static const Tables t = make_tables();
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// e3.f for one element (lhs = 0, idiff = 0, iLES = iRANS = iLSet = 0, iDC = 0,
+// no body force, ipord = 1, itau = 0)
+// ---------------------------------------------------------------------------
+void e3_element(const or_common& c, int ires, int iprec, const double (*yl)[5],
+                const double (*ycl)[5], const double (*acl)[5], const double (*xl)[3],
+                double (*rl)[5], double (*rml)[5], double (*bdl)[5][5]) {
+    const Tables& T = tables();
+    const int nshl = 4, nenl = 4, ngauss = 4;
+    const double Rgas = c.Rgas, gamma = c.gamma, gamma1 = c.gamma1;
+
+    for (int intp = 0; intp < ngauss; ++intp) {
+        if (T.Qwt[intp] == zero) continue;  // e3.f:110
+        const double* shape = T.shp[intp];
+        const double (*shgl)[4] = T.shgl[intp];
+        double ri[20] = {0}, rmi[20] = {0};
+
+        // ---------------- e3ivar.f:96-156 ----------------
+        double dui[5] = {0, 0, 0, 0, 0};
+        for (int n = 0; n < nshl; ++n)
+            for (int k = 0; k < 5; ++k) dui[k] = dui[k] + shape[n] * yl[n][k];
+        double rk = pt5 * (dui[1] * dui[1] + dui[2] * dui[2] + dui[3] * dui[3]);
+        {   // getthm ithm=6 (getthm.f:103-148): pres=dui(1), T=dui(5)
+            double rho6 = dui[0] / (Rgas * dui[4]);
+            double ei6 = dui[4] * (Rgas / gamma1);
+            dui[0] = rho6;
+            dui[1] = rho6 * dui[1];
+            dui[2] = rho6 * dui[2];
+            dui[3] = rho6 * dui[3];
+            dui[4] = rho6 * (ei6 + rk);
+        }
+        double pres = 0, u1 = 0, u2 = 0, u3 = 0, Tq = 0;
+        for (int n = 0; n < nshl; ++n) {
+            pres = pres + shape[n] * ycl[n][0];
+            u1 = u1 + shape[n] * ycl[n][1];
+            u2 = u2 + shape[n] * ycl[n][2];
+            u3 = u3 + shape[n] * ycl[n][3];
+            Tq = Tq + shape[n] * ycl[n][4];
+        }
+        double aci[5] = {0, 0, 0, 0, 0};
+        for (int n = 0; n < nshl; ++n)
+            for (int k = 0; k < 5; ++k) aci[k] = aci[k] + shape[n] * acl[n][k];
+        rk = pt5 * (u1 * u1 + u2 * u2 + u3 * u3);
+        // getthm ithm=7 (getthm.f:111, 148, 157-171)
+        const double rho = pres / (Rgas * Tq);
+        const double ei = Tq * (Rgas / gamma1);
+        const double h = Tq * (Rgas * gamma / gamma1);
+        const double cv = Rgas / gamma1;
+        const double cp = Rgas * gamma / gamma1;
+        const double alfap = one / Tq;
+        const double betaT = one / pres;
+        // getDiff (getdiff.f:127, 164, 171, 258-261): constant mu, Stokes, no eddy viscosity
+        double rmu = c.rmu;
+        double rlm = -pt66 * rmu;
+        double con = rmu * cp / c.pr;
+        const double xmut = 0.0;
+        rlm = rlm - pt66 * xmut;
+        rmu = rmu + xmut;
+        const double rlm2mu = rlm + two * rmu;
+        con = con + xmut * cp / c.pr;
+        // e3metric (e3metric.f:22-77)
+        double dxdxi[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int n = 0; n < nenl; ++n)
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) dxdxi[i][j] = dxdxi[i][j] + xl[n][i] * shgl[j][n];
+        double dxidx[3][3];
+        dxidx[0][0] = dxdxi[1][1] * dxdxi[2][2] - dxdxi[2][1] * dxdxi[1][2];
+        dxidx[0][1] = dxdxi[2][1] * dxdxi[0][2] - dxdxi[0][1] * dxdxi[2][2];
+        dxidx[0][2] = dxdxi[0][1] * dxdxi[1][2] - dxdxi[0][2] * dxdxi[1][1];
+        const double tmp = one / (dxidx[0][0] * dxdxi[0][0] + dxidx[0][1] * dxdxi[1][0] +
+                                  dxidx[0][2] * dxdxi[2][0]);
+        dxidx[0][0] = dxidx[0][0] * tmp;
+        dxidx[0][1] = dxidx[0][1] * tmp;
+        dxidx[0][2] = dxidx[0][2] * tmp;
+        dxidx[1][0] = (dxdxi[1][2] * dxdxi[2][0] - dxdxi[1][0] * dxdxi[2][2]) * tmp;
+        dxidx[1][1] = (dxdxi[0][0] * dxdxi[2][2] - dxdxi[2][0] * dxdxi[0][2]) * tmp;
+        dxidx[1][2] = (dxdxi[1][0] * dxdxi[0][2] - dxdxi[0][0] * dxdxi[1][2]) * tmp;
+        dxidx[2][0] = (dxdxi[1][0] * dxdxi[2][1] - dxdxi[1][1] * dxdxi[2][0]) * tmp;
+        dxidx[2][1] = (dxdxi[2][0] * dxdxi[0][1] - dxdxi[0][0] * dxdxi[2][1]) * tmp;
+        dxidx[2][2] = (dxdxi[0][0] * dxdxi[1][1] - dxdxi[0][1] * dxdxi[1][0]) * tmp;
+        const double WdetJ = T.Qwt[intp] / tmp;
+        double shg[4][3];
+        for (int n = 0; n < nshl; ++n)
+            for (int i = 0; i < 3; ++i)
+                shg[n][i] = shgl[0][n] * dxidx[0][i] + shgl[1][n] * dxidx[1][i] +
+                            shgl[2][n] * dxidx[2][i];
+        // global gradients of the (perturbed) yl (e3ivar.f:259-334)
+        double g[3][5] = {{0}};
+        for (int n = 0; n < nshl; ++n)
+            for (int i = 0; i < 3; ++i)
+                for (int k = 0; k < 5; ++k) g[i][k] = g[i][k] + shg[n][i] * yl[n][k];
+
+        // ---------------- e3mtrx.f:79-224 ----------------
+        double A0[5][5] = {{0}}, A[3][5][5] = {{{0}}};
+        const double drdp = rho * betaT;
+        const double drdT = -rho * alfap;
+        A0[4][0] = drdp * (h + rk) - alfap * Tq;
+        const double e2p = A0[4][0] + one;
+        const double e3p = rho * (h + rk);
+        const double e4p = drdT * (h + rk) + rho * cp;
+        A0[0][0] = drdp;
+        A0[0][4] = drdT;
+        A0[1][0] = drdp * u1; A0[1][1] = rho; A0[1][4] = drdT * u1;
+        A0[2][0] = drdp * u2; A0[2][2] = rho; A0[2][4] = drdT * u2;
+        A0[3][0] = drdp * u3; A0[3][3] = rho; A0[3][4] = drdT * u3;
+        A0[4][1] = rho * u1; A0[4][2] = rho * u2; A0[4][3] = rho * u3; A0[4][4] = e4p;
+        double (*A1)[5] = A[0], (*A2)[5] = A[1], (*A3)[5] = A[2];
+        A1[0][0] = drdp * u1; A1[0][1] = rho; A1[0][4] = drdT * u1;
+        A1[1][0] = drdp * u1 * u1 + 1; A1[1][1] = two * rho * u1; A1[1][4] = drdT * u1 * u1;
+        A1[2][0] = drdp * u1 * u2; A1[2][1] = rho * u2; A1[2][2] = rho * u1; A1[2][4] = drdT * u1 * u2;
+        A1[3][0] = drdp * u1 * u3; A1[3][1] = rho * u3; A1[3][3] = rho * u1; A1[3][4] = drdT * u1 * u3;
+        A1[4][0] = u1 * e2p; A1[4][1] = e3p + rho * u1 * u1; A1[4][2] = rho * u1 * u2;
+        A1[4][3] = rho * u1 * u3; A1[4][4] = u1 * e4p;
+        A2[0][0] = drdp * u2; A2[0][2] = rho; A2[0][4] = drdT * u2;
+        A2[1][0] = drdp * u1 * u2; A2[1][1] = rho * u2; A2[1][2] = rho * u1; A2[1][4] = drdT * u1 * u2;
+        A2[2][0] = drdp * u2 * u2 + 1; A2[2][2] = two * rho * u2; A2[2][4] = drdT * u2 * u2;
+        A2[3][0] = drdp * u2 * u3; A2[3][2] = rho * u3; A2[3][3] = rho * u2; A2[3][4] = drdT * u2 * u3;
+        A2[4][0] = u2 * e2p; A2[4][1] = rho * u1 * u2; A2[4][2] = e3p + rho * u2 * u2;
+        A2[4][3] = rho * u2 * u3; A2[4][4] = u2 * e4p;
+        A3[0][0] = drdp * u3; A3[0][3] = rho; A3[0][4] = drdT * u3;
+        A3[1][0] = drdp * u1 * u3; A3[1][1] = rho * u3; A3[1][3] = rho * u1; A3[1][4] = drdT * u1 * u3;
+        A3[2][0] = drdp * u3 * u2; A3[2][2] = rho * u3; A3[2][3] = rho * u2; A3[2][4] = drdT * u3 * u2;
+        A3[3][0] = drdp * u3 * u3 + 1; A3[3][3] = two * rho * u3; A3[3][4] = drdT * u3 * u3;
+        A3[4][0] = u3 * e2p; A3[4][1] = rho * u1 * u3; A3[4][2] = rho * u2 * u3;
+        A3[4][3] = e3p + rho * u3 * u3; A3[4][4] = u3 * e4p;
+
+        // ---------------- e3conv.f:72-184 ----------------
+        if (ires == 1 || ires == 3) {
+            ri[0] = (-u1) * rho;
+            ri[1] = (-u1) * rho * u1 - pres;
+            ri[2] = (-u1) * rho * u2;
+            ri[3] = (-u1) * rho * u3;
+            ri[4] = (-u1) * rho * (ei + rk) - u1 * pres;
+            ri[5] = (-u2) * rho;
+            ri[6] = (-u2) * rho * u1;
+            ri[7] = (-u2) * rho * u2 - pres;
+            ri[8] = (-u2) * rho * u3;
+            ri[9] = (-u2) * rho * (ei + rk) - u2 * pres;
+            ri[10] = (-u3) * rho;
+            ri[11] = (-u3) * rho * u1;
+            ri[12] = (-u3) * rho * u2;
+            ri[13] = (-u3) * rho * u3 - pres;
+            ri[14] = (-u3) * rho * (ei + rk) - u3 * pres;
+        }
+        double rLyi[5];
+        for (int k = 0; k < 5; ++k) {
+            double s = 0.0;
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 5; ++j) s = s + A[i][k][j] * g[i][j];
+            rLyi[k] = s;
+        }
+        if (ires == 2 || ires == 3)
+            for (int k = 0; k < 5; ++k) rmi[15 + k] = rLyi[k];
+
+        // ---------------- e3visc.f:278-368 (Navier == 1, rlsli == 0) ----------------
+        if (c.Navier == 1) {
+            const double (*g1)[5] = &g[0], (*g2)[5] = &g[1], (*g3)[5] = &g[2];
+            (void)g1; (void)g2; (void)g3;
+            const double* G1 = g[0]; const double* G2 = g[1]; const double* G3 = g[2];
+            rmi[1] = rlm2mu * G1[1] + rlm * G2[2] + rlm * G3[3] - 0.0;
+            rmi[2] = rmu * G1[2] + rmu * G2[1] - 0.0;
+            rmi[3] = rmu * G1[3] + rmu * G3[1] - 0.0;
+            rmi[4] = rlm2mu * u1 * G1[1] + rmu * u2 * G1[2] + rmu * u3 * G1[3] +
+                     rmu * u2 * G2[1] + rlm * u1 * G2[2] + rmu * u3 * G3[1] +
+                     rlm * u1 * G3[3] + con * G1[4];
+            for (int k = 1; k < 5; ++k) ri[k] = ri[k] + rmi[k];
+            rmi[6] = rmu * G1[2] + rmu * G2[1] - 0.0;
+            rmi[7] = rlm * G1[1] + rlm2mu * G2[2] + rlm * G3[3] - 0.0;
+            rmi[8] = rmu * G2[3] + rmu * G3[2] - 0.0;
+            rmi[9] = rlm * u2 * G1[1] + rmu * u1 * G1[2] + rmu * u1 * G2[1] +
+                     rlm2mu * u2 * G2[2] + rmu * u3 * G2[3] + rmu * u3 * G3[2] +
+                     rlm * u2 * G3[3] + con * G2[4];
+            for (int k = 6; k < 10; ++k) ri[k] = ri[k] + rmi[k];
+            rmi[11] = rmu * G1[3] + rmu * G3[1] - 0.0;
+            rmi[12] = rmu * G2[3] + rmu * G3[2] - 0.0;
+            rmi[13] = rlm * G1[1] + rlm * G2[2] + rlm2mu * G3[3] - 0.0;
+            rmi[14] = rlm * u3 * G1[1] + rmu * u1 * G1[3] + rlm * u3 * G2[2] +
+                      rmu * u2 * G2[3] + rmu * u1 * G3[1] + rmu * u2 * G3[2] +
+                      rlm2mu * u3 * G3[3] + con * G3[4];
+            for (int k = 11; k < 15; ++k) ri[k] = ri[k] + rmi[k];
+        }
+
+        // ---------------- e3ls.f:96-143 ----------------
+        const double fct1 = c.almi / c.gami / c.alfi * c.Dtgl;
+        double rLymi[5] = {0, 0, 0, 0, 0};
+        if (ires != 1)
+            for (int k = 0; k < 5; ++k) rLymi[k] = rLyi[k] + fct1 * dui[k];
+        if (ires == 1 || ires == 3)
+            for (int k = 0; k < 5; ++k) {
+                double s = rLyi[k];
+                for (int j = 0; j < 5; ++j) s = s + A0[k][j] * aci[j];
+                rLyi[k] = s;
+            }
+
+        // ---------------- e3tau.f:140-181 (itau = 0) + e3gijd tet branch 1440-1470 ----------------
+        double gijd[6];
+        {
+            const double c1 = 1.259921049894873e+00, c2 = 6.299605249474365e-01;
+            double t1, t2, t3;
+            t1 = c1 * dxidx[0][0] + c2 * (dxidx[1][0] + dxidx[2][0]);
+            t2 = c1 * dxidx[1][0] + c2 * (dxidx[0][0] + dxidx[2][0]);
+            t3 = c1 * dxidx[2][0] + c2 * (dxidx[0][0] + dxidx[1][0]);
+            gijd[0] = dxidx[0][0] * t1 + dxidx[1][0] * t2 + dxidx[2][0] * t3;
+            t1 = c1 * dxidx[0][1] + c2 * (dxidx[1][1] + dxidx[2][1]);
+            t2 = c1 * dxidx[1][1] + c2 * (dxidx[0][1] + dxidx[2][1]);
+            t3 = c1 * dxidx[2][1] + c2 * (dxidx[0][1] + dxidx[1][1]);
+            gijd[1] = dxidx[0][0] * t1 + dxidx[1][0] * t2 + dxidx[2][0] * t3;
+            gijd[2] = dxidx[0][1] * t1 + dxidx[1][1] * t2 + dxidx[2][1] * t3;
+            t1 = c1 * dxidx[0][2] + c2 * (dxidx[1][2] + dxidx[2][2]);
+            t2 = c1 * dxidx[1][2] + c2 * (dxidx[0][2] + dxidx[2][2]);
+            t3 = c1 * dxidx[2][2] + c2 * (dxidx[0][2] + dxidx[1][2]);
+            gijd[3] = dxidx[0][0] * t1 + dxidx[1][0] * t2 + dxidx[2][0] * t3;
+            gijd[4] = dxidx[0][1] * t1 + dxidx[1][1] * t2 + dxidx[2][1] * t3;
+            gijd[5] = dxidx[0][2] * t1 + dxidx[1][2] * t2 + dxidx[2][2] * t3;
+        }
+        double tau[3];
+        {
+            const double fff = 36.0;  // ipord == 1
+            const double dts = (c.iremoveStabTimeTerm == 1) ? zero : c.dtsfct * c.Dtgl;
+            double t2 = rho * rho * ((two * dts) * (two * dts) +
+                                     (u1 * (u1 * gijd[0] + two * (u2 * gijd[1] + u3 * gijd[3])) +
+                                      u2 * (u2 * gijd[2] + two * u3 * gijd[4]) + u3 * u3 * gijd[5])) +
+                        fff * (rmu * rmu) *
+                            (gijd[0] * gijd[0] + gijd[2] * gijd[2] + gijd[5] * gijd[5] +
+                             two * (gijd[1] * gijd[1] + gijd[3] * gijd[3] + gijd[4] * gijd[4]));
+            const double fact = std::sqrt(t2);
+            tau[0] = pt125 * fact / (rho * (gijd[0] + gijd[2] + gijd[5])) * c.taucfct;
+            tau[1] = one / fact;
+            tau[2] = tau[1] / cv * c.temper;
+        }
+        const double tauk[5] = {tau[0], tau[1], tau[1], tau[1], tau[2]};
+        if (ires == 1 || ires == 3)
+            for (int k = 0; k < 5; ++k) rLyi[k] = tauk[k] * rLyi[k];
+        if (ires != 1)
+            for (int k = 0; k < 5; ++k) rLymi[k] = tauk[k] * rLymi[k];
+
+        // ---------------- e3ls.f:231-459: A_i (tau L) ----------------
+        if (ires != 1)
+            for (int r = 0; r < 15; ++r) {
+                const int i = r / 5, row = r % 5;
+                double s = 0.0;
+                for (int j = 0; j < 5; ++j) s = s + A[i][row][j] * rLymi[j];
+                rmi[r] = s + rmi[r];
+            }
+        if (ires == 1 || ires == 3)
+            for (int r = 0; r < 15; ++r) {
+                const int i = r / 5, row = r % 5;
+                double s = 0.0;
+                for (int j = 0; j < 5; ++j) s = s + A[i][row][j] * rLyi[j];
+                ri[r] = s + ri[r];
+            }
+
+        // ---------------- e3massr.f:26-88 ----------------
+        if (ires == 1 || ires == 3)
+            for (int k = 0; k < 5; ++k) {
+                double s = ri[15 + k];
+                for (int j = 0; j < 5; ++j) s = s + A0[k][j] * aci[j];
+                ri[15 + k] = s;
+            }
+        if (ires != 1)
+            for (int k = 0; k < 5; ++k) rmi[15 + k] = rmi[15 + k] + fct1 * dui[k];
+
+        // ---------------- e3bdg.f (iprec == 1, lhs != 1, itau < 10) ----------------
+        if (iprec == 1 && bdl) {
+            // convective, non-integrated-by-parts: N_b A_i N_b,i  (e3bdg.f:37-189)
+            for (int j = 0; j < nshl; ++j) {
+                const double t = shape[j] * WdetJ;
+                for (int r = 0; r < 5; ++r)
+                    for (int cc = 0; cc < 5; ++cc)
+                        bdl[j][r][cc] = bdl[j][r][cc] +
+                                        t * (shg[j][0] * A1[r][cc] + shg[j][1] * A2[r][cc] +
+                                             shg[j][2] * A3[r][cc]);
+            }
+            // mass (e3bdg.f:219-246), bcool = 0
+            {
+                const double ff = c.almi / c.gami / c.alfi;
+                const double t = WdetJ * (c.Dtgl * ff + 0.0);
+                for (int j = 0; j < nshl; ++j) {
+                    const double t2 = (shape[j] * shape[j]) * t;
+                    for (int r = 0; r < 5; ++r)
+                        for (int cc = 0; cc < 5; ++cc) bdl[j][r][cc] = bdl[j][r][cc] + t2 * A0[r][cc];
+                }
+            }
+            // least-squares time term N_a,i A_i tau A0 (e3bdg.f:254-342)
+            if (c.ivart >= 2) {
+                double AtA0[3][5][5];
+                for (int i = 0; i < 3; ++i) {
+                    double Atau[5][5];
+                    for (int r = 0; r < 5; ++r)
+                        for (int k = 0; k < 5; ++k) Atau[r][k] = A[i][r][k] * tauk[k];
+                    for (int cc = 0; cc < 5; ++cc)
+                        for (int r = 0; r < 5; ++r)
+                            AtA0[i][r][cc] = Atau[r][0] * A0[0][cc] + Atau[r][1] * A0[1][cc] +
+                                             Atau[r][2] * A0[2][cc] + Atau[r][3] * A0[3][cc] +
+                                             Atau[r][4] * A0[4][cc];
+                }
+                for (int a = 0; a < nshl; ++a) {
+                    const double t1 = shape[a] * WdetJ * c.almi / c.gami / c.alfi * c.Dtgl;
+                    for (int r = 0; r < 5; ++r)
+                        for (int cc = 0; cc < 5; ++cc)
+                            bdl[a][r][cc] = bdl[a][r][cc] +
+                                            t1 * (shg[a][0] * AtA0[0][r][cc] + shg[a][1] * AtA0[1][r][cc] +
+                                                  shg[a][2] * AtA0[2][r][cc]);
+                }
+            }
+            // stiffness: N_a,p (A_p tau A_q + K_pq) N_a,q  (e3bdg.f:346-2590)
+            const int blocks[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+            for (int b = 0; b < 6; ++b) {
+                const int p = blocks[b][0], q = blocks[b][1];
+                const double (*Ap)[5] = A[p];
+                const double (*Aq)[5] = A[q];
+                double M[5][5];
+                if (c.ivart >= 2) {
+                    for (int r = 0; r < 5; ++r)
+                        for (int cc = 0; cc < 5; ++cc) {
+                            if (p == q) {
+                                M[r][cc] = tau[0] * Ap[r][0] * Ap[0][cc] +
+                                           tau[1] * (Ap[r][1] * Ap[1][cc] + Ap[r][2] * Ap[2][cc] +
+                                                     Ap[r][3] * Ap[3][cc]) +
+                                           tau[2] * Ap[r][4] * Ap[4][cc];
+                            } else {
+                                M[r][cc] = tau[0] * (Ap[r][0] * Aq[0][cc] + Aq[r][0] * Ap[0][cc]) +
+                                           tau[1] * (Ap[r][1] * Aq[1][cc] + Ap[r][2] * Aq[2][cc] +
+                                                     Ap[r][3] * Aq[3][cc] + Aq[r][1] * Ap[1][cc] +
+                                                     Aq[r][2] * Ap[2][cc] + Aq[r][3] * Ap[3][cc]) +
+                                           tau[2] * (Ap[r][4] * Aq[4][cc] + Aq[r][4] * Ap[4][cc]);
+                            }
+                        }
+                } else {
+                    std::memset(M, 0, sizeof(M));
+                }
+                if (c.Navier == 1) {
+                    const double uu[3] = {u1, u2, u3};
+                    if (p == q) {
+                        // diagonal: rlm2mu on the p-th momentum row, rmu on the others
+                        for (int d = 0; d < 3; ++d) {
+                            const double coef = (d == p) ? rlm2mu : rmu;
+                            M[1 + d][1 + d] = M[1 + d][1 + d] + coef;
+                        }
+                        for (int d = 0; d < 3; ++d) {
+                            const double coef = (d == p) ? rlm2mu : rmu;
+                            M[4][1 + d] = M[4][1 + d] + coef * uu[d];
+                        }
+                        M[4][4] = M[4][4] + con;
+                    } else {
+                        // off-diagonal pair (p,q): rlm2mu - rmu = rlm + rmu
+                        M[1 + p][1 + q] = M[1 + p][1 + q] + rlm2mu - rmu;
+                        M[1 + q][1 + p] = M[1 + q][1 + p] + rlm2mu - rmu;
+                        M[4][1 + p] = M[4][1 + p] + (rlm2mu - rmu) * uu[q];
+                        M[4][1 + q] = M[4][1 + q] + (rlm2mu - rmu) * uu[p];
+                    }
+                }
+                for (int j = 0; j < nshl; ++j) {
+                    const double t = WdetJ * shg[j][p] * shg[j][q];
+                    for (int r = 0; r < 5; ++r)
+                        for (int cc = 0; cc < 5; ++cc) bdl[j][r][cc] = bdl[j][r][cc] + t * M[r][cc];
+                }
+            }
+        }
+
+        // ---------------- e3wmlt.f:72-145 ----------------
+        if (ires == 1 || ires == 3)
+            for (int i = 0; i < nshl; ++i)
+                for (int k = 0; k < 5; ++k)
+                    rl[i][k] = rl[i][k] + WdetJ * (shg[i][0] * ri[k] + shg[i][1] * ri[5 + k] +
+                                                   shg[i][2] * ri[10 + k]);
+        if (ires == 2 || ires == 3)
+            for (int i = 0; i < nshl; ++i)
+                for (int k = 0; k < 5; ++k)
+                    rml[i][k] = rml[i][k] + WdetJ * (shg[i][0] * rmi[k] + shg[i][1] * rmi[5 + k] +
+                                                     shg[i][2] * rmi[10 + k] + shape[i] * rmi[15 + k]);
+        if (ires == 1 || ires == 3)  // temporal term (adds exact zeros when ires == 2)
+            for (int i = 0; i < nshl; ++i)
+                for (int k = 0; k < 5; ++k) rl[i][k] = rl[i][k] + shape[i] * WdetJ * ri[15 + k];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// e3b.f + e3bvar.f for one boundary tet (face = local nodes 0,1,2), ires 1/3
+// ---------------------------------------------------------------------------
+void e3b_element(const or_common& c, const double (*yl)[5], int iBCB, const double (*BCB)[6],
+                 const double (*xlb)[3], double (*rl)[5]) {
+    const Tables& T = tables();
+    const double Rgas = c.Rgas, gamma = c.gamma, gamma1 = c.gamma1;
+    const int nshlb = 3, nshl = 4, nenl = 4;
+    for (int intp = 0; intp < 3; ++intp) {
+        if (T.Qwtb[intp] == zero) continue;
+        const double* shpb = T.shpb[intp];
+        const double (*shglb)[4] = T.shglb[intp];
+        // e3bvar.f:100-121
+        double pres = 0, u1 = 0, u2 = 0, u3 = 0, Tq = 0;
+        for (int n = 0; n < nshlb; ++n) {
+            pres = pres + shpb[n] * yl[n][0];
+            u1 = u1 + shpb[n] * yl[n][1];
+            u2 = u2 + shpb[n] * yl[n][2];
+            u3 = u3 + shpb[n] * yl[n][3];
+            Tq = Tq + shpb[n] * yl[n][4];
+        }
+        const double rk = pt5 * (u1 * u1 + u2 * u2 + u3 * u3);
+        const double rho = pres / (Rgas * Tq);
+        const double ei = Tq * (Rgas / gamma1);
+        const double cp = Rgas * gamma / gamma1;
+        // metrics (e3bvar.f:139-199)
+        double dx[3][3] = {{0}};
+        for (int n = 0; n < nenl; ++n)
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) dx[i][j] = dx[i][j] + xlb[n][i] * shglb[j][n];
+        double v1[3], v2[3];
+        for (int i = 0; i < 3; ++i) { v1[i] = xlb[1][i] - xlb[0][i]; v2[i] = xlb[2][i] - xlb[0][i]; }
+        const double t1 = v1[1] * v2[2] - v2[1] * v1[2];
+        const double t2 = v2[0] * v1[2] - v1[0] * v2[2];
+        const double t3 = v1[0] * v2[1] - v2[0] * v1[1];
+        double temp = one / std::sqrt(t1 * t1 + t2 * t2 + t3 * t3);
+        const double bn[3] = {t1 * temp, t2 * temp, t3 * temp};
+        const double WdetJb = T.Qwtb[intp] / (four * temp);
+        double g[3][5] = {{0}};
+        if (c.Navier == 1) {
+            double di[3][3];
+            di[0][0] = dx[1][1] * dx[2][2] - dx[2][1] * dx[1][2];
+            di[0][1] = dx[2][1] * dx[0][2] - dx[0][1] * dx[2][2];
+            di[0][2] = dx[0][1] * dx[1][2] - dx[0][2] * dx[1][1];
+            temp = one / (di[0][0] * dx[0][0] + di[0][1] * dx[1][0] + di[0][2] * dx[2][0]);
+            di[0][0] = di[0][0] * temp;
+            di[0][1] = di[0][1] * temp;
+            di[0][2] = di[0][2] * temp;
+            di[1][0] = (dx[1][2] * dx[2][0] - dx[1][0] * dx[2][2]) * temp;
+            di[1][1] = (dx[0][0] * dx[2][2] - dx[2][0] * dx[0][2]) * temp;
+            di[1][2] = (dx[1][0] * dx[0][2] - dx[0][0] * dx[1][2]) * temp;
+            di[2][0] = (dx[1][0] * dx[2][1] - dx[1][1] * dx[2][0]) * temp;
+            di[2][1] = (dx[2][0] * dx[0][1] - dx[0][0] * dx[2][1]) * temp;
+            di[2][2] = (dx[0][0] * dx[1][1] - dx[0][1] * dx[1][0]) * temp;
+            double gl[3][5] = {{0}};
+            for (int n = 0; n < nshl; ++n)
+                for (int i = 0; i < 3; ++i)
+                    for (int k = 0; k < 5; ++k) gl[i][k] = gl[i][k] + shglb[i][n] * yl[n][k];
+            for (int k = 1; k < 5; ++k)
+                for (int i = 0; i < 3; ++i)
+                    g[i][k] = di[0][i] * gl[0][k] + di[1][i] * gl[1][k] + di[2][i] * gl[2][k];
+        }
+        double rou = 0, p = 0;
+        for (int n = 0; n < nshlb; ++n) {
+            rou = rou + shpb[n] * BCB[n][0];
+            p = p + shpb[n] * BCB[n][1];
+        }
+        double Fv2 = 0, Fv3 = 0, Fv4 = 0, Fh5 = 0;
+        if (c.Navier == 1)
+            for (int n = 0; n < nshlb; ++n) {
+                Fv2 = Fv2 + shpb[n] * BCB[n][2];
+                Fv3 = Fv3 + shpb[n] * BCB[n][3];
+                Fv4 = Fv4 + shpb[n] * BCB[n][4];
+                Fh5 = Fh5 + shpb[n] * BCB[n][5];
+            }
+        // e3b.f:134-166
+        double un;
+        if (!(iBCB & 1)) {
+            un = bn[0] * u1 + bn[1] * u2 + bn[2] * u3;
+            rou = rho * (un);
+        } else {
+            un = (rou / rho);
+        }
+        if (!(iBCB & 2)) p = pres;
+        double F1 = rou;
+        double F2 = rou * u1 + bn[0] * p;
+        double F3 = rou * u2 + bn[1] * p;
+        double F4 = rou * u3 + bn[2] * p;
+        double F5 = rou * (ei + rk) + un * p;
+        if (c.Navier == 1) {
+            // getDiff with the boundary T, cp
+            double rmu = c.rmu;
+            double rlm = -pt66 * rmu;
+            double con = rmu * cp / c.pr;
+            const double rlm2mu = rlm + two * rmu;
+            const double* G1 = g[0]; const double* G2 = g[1]; const double* G3 = g[2];
+            const double tau1n = bn[0] * (rlm2mu * G1[1] + rlm * G2[2] + rlm * G3[3]) +
+                                 bn[1] * (rmu * (G2[1] + G1[2])) + bn[2] * (rmu * (G3[1] + G1[3]));
+            const double tau2n = bn[0] * (rmu * (G2[1] + G1[2])) +
+                                 bn[1] * (rlm * G1[1] + rlm2mu * G2[2] + rlm * G3[3]) +
+                                 bn[2] * (rmu * (G3[2] + G2[3]));
+            const double tau3n = bn[0] * (rmu * (G3[1] + G1[3])) + bn[1] * (rmu * (G3[2] + G2[3])) +
+                                 bn[2] * (rlm * G1[1] + rlm * G2[2] + rlm2mu * G3[3]);
+            if (!(iBCB & 4)) { Fv2 = tau1n; Fv3 = tau2n; Fv4 = tau3n; }
+            const double Fv5 = u1 * Fv2 + u2 * Fv3 + u3 * Fv4;
+            const double heat = -con * (bn[0] * G1[4] + bn[1] * G2[4] + bn[2] * G3[4]);
+            if (!(iBCB & 8)) Fh5 = heat;
+            F2 = F2 - Fv2;
+            F3 = F3 - Fv3;
+            F4 = F4 - Fv4;
+            F5 = F5 - Fv5 + Fh5;
+        }
+        // e3b.f:224-241
+        for (int n = 0; n < nshlb; ++n) {
+            const double w = WdetJb * shpb[n];
+            rl[n][0] = rl[n][0] + w * F1;
+            rl[n][1] = rl[n][1] + w * F2;
+            rl[n][2] = rl[n][2] + w * F3;
+            rl[n][3] = rl[n][3] + w * F4;
+            rl[n][4] = rl[n][4] + w * F5;
+        }
+    }
+}
+
+// localy gather (localy.f:48-73): global (u,v,w,p,T) -> local (p,u,v,w,T)
+inline void gather_y(const double* y, int nshg, int node, double out[5]) {
+    out[0] = y[3 * (size_t)nshg + node];
+    out[1] = y[0 * (size_t)nshg + node];
+    out[2] = y[1 * (size_t)nshg + node];
+    out[3] = y[2 * (size_t)nshg + node];
+    out[4] = y[4 * (size_t)nshg + node];
+}
+inline void gather_x(const double* x, int nshg, int node, double out[3]) {
+    for (int d = 0; d < 3; ++d) out[d] = x[d * (size_t)nshg + node];
+}
+
+template <class F>
+void parallel_for(int n, int nthreads, F&& f) {
+    if (nthreads <= 1 || n < 2) {
+        for (int i = 0; i < n; ++i) f(i);
+        return;
+    }
+    nthreads = std::min(nthreads, n);
+    std::vector<std::thread> th;
+    th.reserve(nthreads);
+    for (int t = 0; t < nthreads; ++t)
+        th.emplace_back([&, t]() {
+            for (int i = t; i < n; i += nthreads) f(i);
+        });
+    for (auto& x : th) x.join();
+}
+
+// Interior element loop shared by ElmMFG / ItrRes / residual-only.
+// ires 3: res, rmes, (BDiag if iprec); ires 2: rmes from (yp, yc); ires 1: res.
+void element_sweep(const or_common& c, const or_mesh& m, int ires, int iprec,
+                   const double* yp, const double* yc, const double* ac,
+                   double* res, double* rmes, double* bd, int iabres, int nthreads) {
+    const int nshg = m.nshg;
+    const int ngrp = m.ngrp > 0 ? m.ngrp : 1;
+    for (int gI = 0; gI < ngrp; ++gI) {
+        const int b0 = m.ngrp > 0 ? m.grp_start[gI] : 0;
+        const int b1 = m.ngrp > 0 ? m.grp_start[gI + 1] : m.nblk;
+        // blocks inside a group touch disjoint nodes, so they may run concurrently;
+        // with one thread the block order is the reference's.
+        const int nb = b1 - b0;
+        auto run_block = [&](int bi) {
+            const int blk = b0 + bi;
+            for (int e = m.blk_start[blk]; e < m.blk_start[blk + 1]; ++e) {
+                const int* ie = m.ien + 4 * (size_t)e;
+                double yl[4][5], ycl[4][5], acl[4][5], xl[4][3];
+                for (int a = 0; a < 4; ++a) {
+                    gather_y(yp, nshg, ie[a], yl[a]);
+                    gather_y(yc, nshg, ie[a], ycl[a]);
+                    gather_y(ac, nshg, ie[a], acl[a]);
+                    gather_x(m.x, nshg, ie[a], xl[a]);
+                }
+                double rl[4][5] = {{0}}, rml[4][5] = {{0}}, bdl[4][5][5] = {{{0}}};
+                e3_element(c, ires, iprec, yl, ycl, acl, xl, rl, rml, iprec ? bdl : nullptr);
+                if (iabres == 1)
+                    for (int a = 0; a < 4; ++a)
+                        for (int k = 0; k < 5; ++k) rml[a][k] = std::fabs(rml[a][k]);
+                // local.f:66-80 scatter (res rows in equation order)
+                for (int k = 0; k < 5; ++k)
+                    for (int a = 0; a < 4; ++a) {
+                        if (res && (ires == 1 || ires == 3)) res[k * (size_t)nshg + ie[a]] += rl[a][k];
+                        if (rmes && (ires == 2 || ires == 3)) rmes[k * (size_t)nshg + ie[a]] += rml[a][k];
+                    }
+                if (iprec && bd)
+                    for (int j = 0; j < 5; ++j)
+                        for (int i = 0; i < 5; ++i)
+                            for (int a = 0; a < 4; ++a)
+                                bd[(i + 5 * j) * (size_t)nshg + ie[a]] += bdl[a][i][j];
+            }
+        };
+        parallel_for(nb, nthreads, run_block);
+    }
+}
+
+void boundary_sweep(const or_common& c, const or_mesh& m, const double* y, double* res) {
+    const int nshg = m.nshg;
+    for (int e = 0; e < m.nbelem; ++e) {
+        const int* ie = m.ienb + 4 * (size_t)e;
+        double yl[4][5], xl[4][3];
+        for (int a = 0; a < 4; ++a) {
+            gather_y(y, nshg, ie[a], yl[a]);
+            gather_x(m.x, nshg, ie[a], xl[a]);
+        }
+        double bcb[3][6];
+        for (int n = 0; n < 3; ++n)
+            for (int k = 0; k < 6; ++k) bcb[n][k] = m.BCB ? m.BCB[(e * 3 + n) * 6 + k] : 0.0;
+        double rl[4][5] = {{0}};
+        e3b_element(c, yl, m.iBCB ? m.iBCB[2 * e] : 0, bcb, xl, rl);
+        for (int k = 0; k < 5; ++k)
+            for (int a = 0; a < 4; ++a) res[k * (size_t)nshg + ie[a]] += rl[a][k];
+    }
+}
+
+inline int ibits3(int v) { return (v >> 3) & 7; }
+inline bool btest(int v, int b) { return (v >> b) & 1; }
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+
+// Element groups for the threaded sweep: greedy colouring (no two elements of
+// a group share a node), each colour cut into blocks of at most bksiz
+// elements.  perm[nelem] lists the element order, blk_start[nblk+1] and
+// grp_start[ngrp+1] the blocks and groups; returns ngrp (or -1 on overflow).
+int or_make_groups(int nshg, int nelem, const int* ien, int bksiz, int* perm, int* blk_start,
+                   int* nblk_out, int* grp_start, int max_grp) {
+    std::vector<uint64_t> m0(nshg, 0), m1(nshg, 0);
+    std::vector<int> col(nelem);
+    int ncol = 0;
+    for (int e = 0; e < nelem; ++e) {
+        const int* nd = ien + 4 * (size_t)e;
+        uint64_t f0 = 0, f1 = 0;
+        for (int a = 0; a < 4; ++a) { f0 |= m0[nd[a]]; f1 |= m1[nd[a]]; }
+        int c;
+        if (~f0) c = __builtin_ctzll(~f0);
+        else if (~f1) c = 64 + __builtin_ctzll(~f1);
+        else return -1;
+        col[e] = c;
+        ncol = std::max(ncol, c + 1);
+        for (int a = 0; a < 4; ++a) {
+            if (c < 64) m0[nd[a]] |= 1ull << c;
+            else m1[nd[a]] |= 1ull << (c - 64);
+        }
+    }
+    if (ncol > max_grp) return -1;
+    std::vector<std::vector<int>> cls(ncol);
+    for (int e = 0; e < nelem; ++e) cls[col[e]].push_back(e);
+    int p = 0, nb = 0;
+    grp_start[0] = 0;
+    for (int c = 0; c < ncol; ++c) {
+        for (size_t i = 0; i < cls[c].size(); ++i) {
+            if (i % bksiz == 0) blk_start[nb++] = p;
+            perm[p++] = cls[c][i];
+        }
+        grp_start[c + 1] = nb;
+    }
+    blk_start[nb] = p;
+    *nblk_out = nb;
+    return ncol;
+}
+
+void or_tet_tables(double shp[16], double shgl[48], double Qwt[4], double shpb[12],
+                   double shglb[36], double Qwtb[3]) {
+    const Tables& t = tables();
+    for (int q = 0; q < 4; ++q) {
+        Qwt[q] = t.Qwt[q];
+        for (int a = 0; a < 4; ++a) {
+            shp[q * 4 + a] = t.shp[q][a];
+            for (int i = 0; i < 3; ++i) shgl[(q * 3 + i) * 4 + a] = t.shgl[q][i][a];
+        }
+    }
+    for (int q = 0; q < 3; ++q) {
+        Qwtb[q] = t.Qwtb[q];
+        for (int a = 0; a < 4; ++a) {
+            shpb[q * 4 + a] = t.shpb[q][a];
+            for (int i = 0; i < 3; ++i) shglb[(q * 3 + i) * 4 + a] = t.shglb[q][i][a];
+        }
+    }
+}
+
+void or_e3(const or_common* c, int ires, int iprec, const double* yl, const double* ycl,
+           const double* acl, const double* xl, double* rl, double* rml, double* bdl) {
+    e3_element(*c, ires, iprec, (const double (*)[5])yl, (const double (*)[5])ycl,
+               (const double (*)[5])acl, (const double (*)[3])xl, (double (*)[5])rl,
+               (double (*)[5])rml, iprec ? (double (*)[5][5])bdl : nullptr);
+}
+
+void or_e3b(const or_common* c, int ires, const double* yl, const int* iBCB, const double* BCB,
+            const double* xlb, double* rl) {
+    if (ires == 1 || ires == 3)
+        e3b_element(*c, (const double (*)[5])yl, iBCB ? iBCB[0] : 0, (const double (*)[6])BCB,
+                    (const double (*)[3])xlb, (double (*)[5])rl);
+}
+
+// bc3res.f:23-160 (single rank)
+void or_bc3res(const or_mesh* m, const double* y, double* res, const or_common* c) {
+    const int N = m->nshg;
+    const int* iBC = m->iBC;
+    const double* BC = m->BC;
+    double* r[5];
+    for (int k = 0; k < 5; ++k) r[k] = res + (size_t)k * N;
+    auto bc = [&](int k, int n) { return BC[(size_t)(k - 1) * N + n]; };  // 1-based column
+    for (int n = 0; n < N; ++n) {
+        const int ib = iBC[n];
+        if (btest(ib, 0)) {  // density
+            r[4][n] = r[4][n] + bc(1, n) * c->Rgas * r[0][n];
+            r[0][n] = zero;
+        }
+        if (btest(ib, 2)) {  // pressure
+            if (c->EntropyPressure == 1) {
+                const double* yy[5];
+                for (int k = 0; k < 5; ++k) yy[k] = y + (size_t)k * N;
+                r[1][n] = r[1][n] - yy[0][n] * r[0][n];
+                r[2][n] = r[2][n] - yy[1][n] * r[0][n];
+                r[3][n] = r[3][n] - yy[2][n] * r[0][n];
+                r[4][n] = r[4][n] - (c->gamma * c->Rgas / c->gamma1 * yy[4][n] +
+                                     pt5 * (yy[0][n] * yy[0][n] + yy[1][n] * yy[1][n] + yy[2][n] * yy[2][n])) *
+                                        r[0][n];
+            }
+            r[0][n] = zero;
+        }
+        const int v = ibits3(ib);
+        switch (v) {
+            case 1:
+                r[2][n] = r[2][n] - bc(4, n) * r[1][n];
+                r[3][n] = r[3][n] - bc(5, n) * r[1][n];
+                r[1][n] = zero;
+                break;
+            case 2:
+                r[1][n] = r[1][n] - bc(4, n) * r[2][n];
+                r[3][n] = r[3][n] - bc(5, n) * r[2][n];
+                r[2][n] = zero;
+                break;
+            case 3:
+                r[3][n] = r[3][n] - bc(4, n) * r[1][n] - bc(6, n) * r[2][n];
+                r[1][n] = zero;
+                r[2][n] = zero;
+                break;
+            case 4:
+                r[1][n] = r[1][n] - bc(4, n) * r[3][n];
+                r[2][n] = r[2][n] - bc(5, n) * r[3][n];
+                r[3][n] = zero;
+                break;
+            case 5:
+                r[2][n] = r[2][n] - bc(4, n) * r[1][n] - bc(6, n) * r[3][n];
+                r[1][n] = zero;
+                r[3][n] = zero;
+                break;
+            case 6:
+                r[1][n] = r[1][n] - bc(4, n) * r[2][n] - bc(6, n) * r[3][n];
+                r[2][n] = zero;
+                r[3][n] = zero;
+                break;
+            case 7:
+                r[1][n] = zero;
+                r[2][n] = zero;
+                r[3][n] = zero;
+                break;
+            default:
+                break;
+        }
+        if (btest(ib, 1)) r[4][n] = zero;  // temperature
+    }
+    // local periodic (bc3res.f:155-160), sequential as in the reference
+    for (int j = 0; j < N; ++j)
+        if (btest(iBC[j], 10)) {
+            const int i = m->iper[j];
+            for (int k = 0; k < 5; ++k) {
+                r[k][i] = r[k][i] + r[k][j];
+                r[k][j] = zero;
+            }
+        }
+}
+
+// bc3bdg.f:23-322 (single rank)
+void or_bc3bdg(const or_mesh* m, const double* y, double* bdiag, const or_common* c) {
+    const int N = m->nshg;
+    const int* iBC = m->iBC;
+    const double* BC = m->BC;
+    auto B = [&](int i, int j, int n) -> double& {  // 1-based (i,j)
+        return bdiag[((size_t)(i - 1) + 5 * (size_t)(j - 1)) * N + n];
+    };
+    auto bc = [&](int k, int n) { return BC[(size_t)(k - 1) * N + n]; };
+    for (int n = 0; n < N; ++n) {
+        const int ib = iBC[n];
+        const double a5 = -y[4 * (size_t)N + n] * (c->Rgas * c->gamma / c->gamma1);
+        if (btest(ib, 0)) {
+            B(5, 5, n) = B(5, 5, n) + a5 * a5 * B(1, 1, n) + a5 * B(1, 5, n) + a5 * B(5, 1, n);
+            B(4, 5, n) = B(4, 5, n) + a5 * B(4, 1, n);
+            B(3, 5, n) = B(3, 5, n) + a5 * B(3, 1, n);
+            B(2, 5, n) = B(2, 5, n) + a5 * B(2, 1, n);
+            B(5, 4, n) = B(5, 4, n) + a5 * B(1, 4, n);
+            B(5, 3, n) = B(5, 3, n) + a5 * B(1, 3, n);
+            B(5, 2, n) = B(5, 2, n) + a5 * B(1, 2, n);
+            B(1, 2, n) = zero; B(1, 3, n) = zero; B(1, 4, n) = zero; B(1, 5, n) = zero;
+            B(2, 1, n) = zero; B(3, 1, n) = zero; B(4, 1, n) = zero; B(5, 1, n) = zero;
+            B(1, 1, n) = one;
+        }
+        if (btest(ib, 2)) {
+            B(1, 2, n) = zero; B(1, 3, n) = zero; B(1, 4, n) = zero; B(1, 5, n) = zero;
+            B(2, 1, n) = zero; B(3, 1, n) = zero; B(4, 1, n) = zero; B(5, 1, n) = zero;
+            B(1, 1, n) = one;
+        }
+        const int v = ibits3(ib);
+        // a single constrained velocity component d (1-based dof 1+d) with the
+        // two coefficients of the others (bc3bdg.f:71-155)
+        auto single = [&](int dc, int o1, int o2) {  // dc: constrained dof row, o1/o2: the others
+            const double b4 = bc(4, n), b5 = bc(5, n);
+            B(5, o2, n) = B(5, o2, n) - b5 * B(5, dc, n);
+            B(5, o1, n) = B(5, o1, n) - b4 * B(5, dc, n);
+            B(o2, 5, n) = B(o2, 5, n) - b5 * B(dc, 5, n);
+            B(o1, 5, n) = B(o1, 5, n) - b4 * B(dc, 5, n);
+            B(o2, 1, n) = B(o2, 1, n) - b5 * B(dc, 1, n);
+            B(o1, 1, n) = B(o1, 1, n) - b4 * B(dc, 1, n);
+            B(1, o2, n) = B(1, o2, n) - b5 * B(1, dc, n);
+            B(1, o1, n) = B(1, o1, n) - b4 * B(1, dc, n);
+            B(o2, o2, n) = B(o2, o2, n) + b5 * b5 * B(dc, dc, n) - b5 * B(dc, o2, n) - b5 * B(o2, dc, n);
+            B(o1, o2, n) = B(o1, o2, n) + b4 * b5 * B(dc, dc, n) - b5 * B(o1, dc, n) - b4 * B(dc, o2, n);
+            B(o2, o1, n) = B(o2, o1, n) + b4 * b5 * B(dc, dc, n) - b5 * B(dc, o1, n) - b4 * B(o2, dc, n);
+            B(o1, o1, n) = B(o1, o1, n) + b4 * b4 * B(dc, dc, n) - b4 * B(dc, o1, n) - b4 * B(o1, dc, n);
+            for (int k = 1; k <= 5; ++k)
+                if (k != dc) { B(dc, k, n) = zero; B(k, dc, n) = zero; }
+            B(dc, dc, n) = one;
+        };
+        auto dbl = [&](int d1, int d2, int o) {  // two constrained components, one free (o)
+            const double b4 = bc(4, n), b6 = bc(6, n);
+            B(o, o, n) = B(o, o, n) + b4 * b4 * B(d1, d1, n) + b6 * b6 * B(d2, d2, n) +
+                         b4 * b6 * (B(d1, d2, n) + B(d2, d1, n)) - b4 * (B(d1, o, n) + B(o, d1, n)) -
+                         b6 * (B(d2, o, n) + B(o, d2, n));
+            B(o, 1, n) = B(o, 1, n) - b4 * B(d1, 1, n) - b6 * B(d2, 1, n);
+            B(o, 5, n) = B(o, 5, n) - b4 * B(d1, 5, n) - b6 * B(d2, 5, n);
+            B(1, o, n) = B(1, o, n) - b4 * B(1, d1, n) - b6 * B(1, d2, n);
+            B(5, o, n) = B(5, o, n) - b4 * B(5, d1, n) - b6 * B(5, d2, n);
+            for (int k = 1; k <= 5; ++k) {
+                if (k != d1) { B(d1, k, n) = zero; B(k, d1, n) = zero; }
+                if (k != d2) { B(d2, k, n) = zero; B(k, d2, n) = zero; }
+            }
+            B(d1, d1, n) = one;
+            B(d2, d2, n) = one;
+        };
+        switch (v) {
+            case 1: single(2, 3, 4); break;
+            case 2: single(3, 2, 4); break;
+            case 3: {  // bc3bdg.f:139-168, written with products of entries as in the reference
+                const double b4 = bc(4, n), b6 = bc(6, n);
+                B(4, 4, n) = B(4, 4, n) + b4 * b4 * B(2, 2, n) + b6 * b6 * B(3, 3, n) +
+                             b4 * b6 * (B(2, 3, n) * B(3, 2, n)) - b6 * (B(4, 3, n) * B(3, 4, n)) -
+                             b4 * (B(4, 2, n) * B(2, 4, n));
+                B(1, 4, n) = B(1, 4, n) - b4 * B(1, 2, n) - b6 * B(1, 3, n);
+                B(4, 1, n) = B(4, 1, n) - b4 * B(2, 1, n) - b6 * B(3, 1, n);
+                B(5, 4, n) = B(5, 4, n) - b4 * B(5, 2, n) - b6 * B(5, 3, n);
+                B(4, 5, n) = B(4, 5, n) - b4 * B(2, 5, n) - b6 * B(3, 5, n);
+                for (int k = 1; k <= 5; ++k) {
+                    if (k != 2) { B(2, k, n) = zero; B(k, 2, n) = zero; }
+                    if (k != 3) { B(3, k, n) = zero; B(k, 3, n) = zero; }
+                }
+                B(3, 3, n) = one;
+                B(2, 2, n) = one;
+                break;
+            }
+            case 4: single(4, 2, 3); break;
+            case 5: dbl(2, 4, 3); break;
+            case 6: dbl(3, 4, 2); break;
+            case 7:
+                for (int a = 2; a <= 4; ++a)
+                    for (int k = 1; k <= 5; ++k)
+                        if (k != a) { B(a, k, n) = zero; B(k, a, n) = zero; }
+                B(2, 2, n) = one; B(3, 3, n) = one; B(4, 4, n) = one;
+                break;
+            default: break;
+        }
+        if (btest(ib, 1)) {
+            B(5, 5, n) = one;
+            for (int k = 1; k <= 4; ++k) { B(k, 5, n) = zero; B(5, k, n) = zero; }
+        }
+    }
+    for (int j = 0; j < N; ++j)
+        if (btest(iBC[j], 10)) {
+            const int i = m->iper[j];
+            for (int a = 1; a <= 5; ++a)
+                for (int b = 1; b <= 5; ++b) B(a, b, i) = B(a, b, i) + B(a, b, j);
+        }
+    for (int j = 0; j < N; ++j)
+        if (btest(iBC[j], 10)) {
+            const int i = m->iper[j];
+            for (int a = 1; a <= 5; ++a)
+                for (int b = 1; b <= 5; ++b) B(a, b, j) = B(a, b, i);
+        }
+}
+
+// itrbc.f:54-176 (no limiting, single rank); y in global order (u,v,w,p,T)
+void or_itrbc(const or_mesh* m, double* y, double* ac, int ires, double Rgas) {
+    const int N = m->nshg;
+    const int* iBC = m->iBC;
+    const double* BC = m->BC;
+    auto bc = [&](int k, int n) { return BC[(size_t)(k - 1) * N + n]; };
+    auto Y = [&](int k, int n) -> double& { return y[(size_t)(k - 1) * N + n]; };
+    for (int n = 0; n < N; ++n) {
+        const int ib = iBC[n];
+        if (btest(ib, 1)) Y(5, n) = bc(2, n);
+        switch (ibits3(ib)) {
+            case 1: Y(1, n) = bc(3, n) - bc(4, n) * Y(2, n) - bc(5, n) * Y(3, n); break;
+            case 2: Y(2, n) = bc(3, n) - bc(4, n) * Y(1, n) - bc(5, n) * Y(3, n); break;
+            case 3: Y(1, n) = bc(3, n) - bc(4, n) * Y(3, n); Y(2, n) = bc(5, n) - bc(6, n) * Y(3, n); break;
+            case 4: Y(3, n) = bc(3, n) - bc(4, n) * Y(1, n) - bc(5, n) * Y(2, n); break;
+            case 5: Y(1, n) = bc(3, n) - bc(4, n) * Y(2, n); Y(3, n) = bc(5, n) - bc(6, n) * Y(2, n); break;
+            case 6: Y(2, n) = bc(3, n) - bc(4, n) * Y(1, n); Y(3, n) = bc(5, n) - bc(6, n) * Y(1, n); break;
+            case 7: Y(1, n) = bc(3, n); Y(2, n) = bc(4, n); Y(3, n) = bc(5, n); break;
+            default: break;
+        }
+    }
+    // density (itrbc.f:124-143): getthm ithm=2 gives pres = Rgas*rho*T, which the
+    // reference stores into y(:,1); pressure (itrbc.f:146-151) into y(:,4)
+    for (int n = 0; n < N; ++n)
+        if (btest(iBC[n], 0)) Y(1, n) = Rgas * bc(1, n) * Y(5, n);
+    for (int n = 0; n < N; ++n)
+        if (btest(iBC[n], 2)) Y(4, n) = bc(1, n);
+    for (int k = 1; k <= 5; ++k) {
+        for (int n = 0; n < N; ++n) Y(k, n) = Y(k, m->iper[n]);
+        if (ires != 2 && ac)
+            for (int n = 0; n < N; ++n) ac[(size_t)(k - 1) * N + n] = ac[(size_t)(k - 1) * N + m->iper[n]];
+    }
+}
+
+// i3lu.f:39-171
+void or_i3lu(int N, double* bd, double* r, int code) {
+    auto D = [&](int i, int j, int n) -> double& { return bd[((size_t)(i - 1) + 5 * (size_t)(j - 1)) * N + n]; };
+    auto R = [&](int k, int n) -> double& { return r[(size_t)(k - 1) * N + n]; };
+    for (int n = 0; n < N; ++n) {
+        if (code == 0) {
+            D(1, 1, n) = one / D(1, 1, n);
+            D(2, 1, n) = D(1, 1, n) * D(2, 1, n);
+            D(3, 1, n) = D(1, 1, n) * D(3, 1, n);
+            D(4, 1, n) = D(1, 1, n) * D(4, 1, n);
+            D(5, 1, n) = D(1, 1, n) * D(5, 1, n);
+            D(2, 2, n) = D(2, 2, n) - D(2, 1, n) * D(1, 2, n);
+            D(2, 3, n) = D(2, 3, n) - D(2, 1, n) * D(1, 3, n);
+            D(2, 4, n) = D(2, 4, n) - D(2, 1, n) * D(1, 4, n);
+            D(2, 5, n) = D(2, 5, n) - D(2, 1, n) * D(1, 5, n);
+            D(2, 2, n) = one / D(2, 2, n);
+            D(3, 2, n) = D(2, 2, n) * (D(3, 2, n) - D(3, 1, n) * D(1, 2, n));
+            D(4, 2, n) = D(2, 2, n) * (D(4, 2, n) - D(4, 1, n) * D(1, 2, n));
+            D(5, 2, n) = D(2, 2, n) * (D(5, 2, n) - D(5, 1, n) * D(1, 2, n));
+            D(3, 3, n) = D(3, 3, n) - D(3, 1, n) * D(1, 3, n) - D(3, 2, n) * D(2, 3, n);
+            D(3, 4, n) = D(3, 4, n) - D(3, 1, n) * D(1, 4, n) - D(3, 2, n) * D(2, 4, n);
+            D(3, 5, n) = D(3, 5, n) - D(3, 1, n) * D(1, 5, n) - D(3, 2, n) * D(2, 5, n);
+            D(3, 3, n) = one / D(3, 3, n);
+            D(4, 3, n) = D(3, 3, n) * (D(4, 3, n) - D(4, 1, n) * D(1, 3, n) - D(4, 2, n) * D(2, 3, n));
+            D(5, 3, n) = D(3, 3, n) * (D(5, 3, n) - D(5, 1, n) * D(1, 3, n) - D(5, 2, n) * D(2, 3, n));
+            D(4, 4, n) = D(4, 4, n) - D(4, 1, n) * D(1, 4, n) - D(4, 2, n) * D(2, 4, n) -
+                         D(4, 3, n) * D(3, 4, n);
+            D(4, 4, n) = one / D(4, 4, n);
+            D(5, 4, n) = D(4, 4, n) * (D(5, 4, n) - D(5, 1, n) * D(1, 4, n) - D(5, 2, n) * D(2, 4, n) -
+                                       D(5, 3, n) * D(3, 4, n));
+            D(5, 5, n) = D(5, 5, n) - D(5, 1, n) * D(1, 5, n) - D(5, 2, n) * D(2, 5, n) -
+                         D(5, 3, n) * D(3, 5, n) - D(5, 4, n) * D(4, 5, n);
+            D(5, 5, n) = one / D(5, 5, n);
+        } else if (code == 1) {
+            R(2, n) = R(2, n) - D(2, 1, n) * R(1, n);
+            R(3, n) = R(3, n) - D(3, 1, n) * R(1, n) - D(3, 2, n) * R(2, n);
+            R(4, n) = R(4, n) - D(4, 1, n) * R(1, n) - D(4, 2, n) * R(2, n) - D(4, 3, n) * R(3, n);
+            R(5, n) = R(5, n) - D(5, 1, n) * R(1, n) - D(5, 2, n) * R(2, n) - D(5, 3, n) * R(3, n) -
+                      D(5, 4, n) * R(4, n);
+        } else if (code == 2) {
+            R(5, n) = D(5, 5, n) * R(5, n);
+            R(4, n) = D(4, 4, n) * (R(4, n) - R(5, n) * D(4, 5, n));
+            R(3, n) = D(3, 3, n) * (R(3, n) - R(5, n) * D(3, 5, n) - R(4, n) * D(3, 4, n));
+            R(2, n) = D(2, 2, n) * (R(2, n) - R(5, n) * D(2, 5, n) - R(4, n) * D(2, 4, n) -
+                                    R(3, n) * D(2, 3, n));
+            R(1, n) = D(1, 1, n) * (R(1, n) - R(5, n) * D(1, 5, n) - R(4, n) * D(1, 4, n) -
+                                    R(3, n) * D(1, 3, n) - R(2, n) * D(1, 2, n));
+        } else if (code == 3) {
+            R(1, n) = R(1, n) / D(1, 1, n) + R(2, n) * D(1, 2, n) + R(3, n) * D(1, 3, n) +
+                      R(4, n) * D(1, 4, n) + R(5, n) * D(1, 5, n);
+            R(2, n) = R(2, n) / D(2, 2, n) + R(3, n) * D(2, 3, n) + R(4, n) * D(2, 4, n) +
+                      R(5, n) * D(2, 5, n);
+            R(3, n) = R(3, n) / D(3, 3, n) + R(4, n) * D(3, 4, n) + R(5, n) * D(3, 5, n);
+            R(4, n) = R(4, n) / D(4, 4, n) + R(5, n) * D(4, 5, n);
+            R(5, n) = R(5, n) / D(5, 5, n);
+        }
+    }
+}
+
+// shuffle.f:11-29
+void or_yshuffle(int N, double* r, int code) {
+    std::vector<double> t((size_t)5 * N);
+    std::memcpy(t.data(), r, sizeof(double) * 5 * (size_t)N);
+    if (code == 0) {  // old2new: (p,u,v,w,T) -> (u,v,w,p,T)
+        for (int k = 0; k < 3; ++k) std::memcpy(r + (size_t)k * N, t.data() + (size_t)(k + 1) * N, sizeof(double) * N);
+        std::memcpy(r + (size_t)3 * N, t.data(), sizeof(double) * N);
+    } else {  // new2old: (u,v,w,p,T) -> (p,u,v,w,T)
+        for (int k = 0; k < 3; ++k) std::memcpy(r + (size_t)(k + 1) * N, t.data() + (size_t)k * N, sizeof(double) * N);
+        std::memcpy(r, t.data() + (size_t)3 * N, sizeof(double) * N);
+    }
+}
+
+void or_elmmfg(const or_common* c, const or_mesh* m, const double* y, const double* ac,
+               double* res, double* rmes, double* bdiag, int iprec, int nthreads) {
+    const size_t N = m->nshg;
+    std::memset(res, 0, sizeof(double) * 5 * N);
+    std::memset(rmes, 0, sizeof(double) * 5 * N);
+    if (iprec) std::memset(bdiag, 0, sizeof(double) * 25 * N);
+    element_sweep(*c, *m, 3, iprec, y, y, ac, res, rmes, iprec ? bdiag : nullptr, 0, nthreads);
+    boundary_sweep(*c, *m, y, res);  // AsBMFG: rml is zero while Jactyp == 0 (e3b.f:244-246)
+    or_bc3res(m, y, res, c);
+    or_bc3res(m, y, rmes, c);
+    if (iprec) or_bc3bdg(m, y, bdiag, c);
+}
+
+void or_itrres(const or_common* c, const or_mesh* m, const double* yp, const double* yc,
+               const double* ac, double* rmes, int iabres, int nthreads) {
+    element_sweep(*c, *m, 2, 0, yp, yc, ac, nullptr, rmes, nullptr, iabres, nthreads);
+    // boundary elements are skipped while Jactyp == 0 (itrres.f:95)
+    or_bc3res(m, yc, rmes, c);
+}
+
+void or_elmres(const or_common* c, const or_mesh* m, const double* y, const double* ac,
+               double* res, int nthreads) {
+    const size_t N = m->nshg;
+    std::memset(res, 0, sizeof(double) * 5 * N);
+    element_sweep(*c, *m, 1, 0, y, y, ac, res, nullptr, nullptr, 0, nthreads);
+    boundary_sweep(*c, *m, y, res);
+    or_bc3res(m, y, res, c);
+}
+
+// au1mfg.f:57-83: uBrg <- (L^-1 Rmod(P U^-1 (ypre + eps u)) - rmes) / eps
+static void au1mfg(const or_common& c, const or_mesh& m, const double* ypre, const double* y,
+                   const double* ac, const double* rmes, const double* bd, double* u,
+                   int nthreads) {
+    const size_t n5 = 5 * (size_t)m.nshg;
+    std::vector<double> ub(n5, 0.0), ut(n5);
+    for (size_t i = 0; i < n5; ++i) ut[i] = ypre[i] + c.eGMRES * u[i];
+    or_i3lu(m.nshg, const_cast<double*>(bd), ut.data(), 2);
+    or_yshuffle(m.nshg, ut.data(), 0);
+    or_itrbc(&m, ut.data(), ut.data(), 2, c.Rgas);
+    or_itrres(&c, &m, ut.data(), y, ac, ub.data(), 0, nthreads);
+    or_i3lu(m.nshg, const_cast<double*>(bd), ub.data(), 1);
+    for (size_t i = 0; i < n5; ++i) u[i] = (ub[i] - rmes[i]) / c.eGMRES;
+}
+
+static double sumsq(const double* a, size_t n) {
+    double s = 0.0;
+    for (size_t i = 0; i < n; ++i) s += a[i] * a[i];
+    return s;
+}
+static double dot(const double* a, const double* b, size_t n) {
+    double s = 0.0;
+    for (size_t i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+}
+
+// itrfdi.f:45-139
+static void itrfdi(or_common& c, const or_mesh& m, const double* ypre, const double* y,
+                   const double* ac, const double* rmes, const double* ubrg, const double* bd,
+                   int nthreads) {
+    const size_t n5 = 5 * (size_t)m.nshg;
+    double* bdm = const_cast<double*>(bd);
+    std::vector<double> rtmp(n5, 0.0), ytmp(ypre, ypre + n5);
+    or_i3lu(m.nshg, bdm, ytmp.data(), 2);
+    or_yshuffle(m.nshg, ytmp.data(), 0);
+    or_itrres(&c, &m, ytmp.data(), y, ac, rtmp.data(), 1, nthreads);
+    or_i3lu(m.nshg, bdm, rtmp.data(), 1);
+    const double epsA = (c.epsM * c.epsM) * std::sqrt(sumsq(rtmp.data(), n5));
+    const double epsSD = std::sqrt(c.epsM);
+    std::fill(rtmp.begin(), rtmp.end(), 0.0);
+    for (size_t i = 0; i < n5; ++i) ytmp[i] = ypre[i] + epsSD * ubrg[i];
+    or_i3lu(m.nshg, bdm, ytmp.data(), 2);
+    or_yshuffle(m.nshg, ytmp.data(), 0);
+    or_itrres(&c, &m, ytmp.data(), y, ac, rtmp.data(), 0, nthreads);
+    for (size_t i = 0; i < n5; ++i) ytmp[i] = ypre[i] - epsSD * ubrg[i];
+    or_i3lu(m.nshg, bdm, ytmp.data(), 2);
+    or_yshuffle(m.nshg, ytmp.data(), 0);
+    or_itrres(&c, &m, ytmp.data(), y, ac, rtmp.data(), 0, nthreads);
+    or_i3lu(m.nshg, bdm, rtmp.data(), 1);
+    for (size_t i = 0; i < n5; ++i) {
+        const double d = (rtmp[i] - two * rmes[i]) / c.epsM;
+        rtmp[i] = d * d;
+    }
+    double s = 0.0;
+    for (size_t i = 0; i < n5; ++i) s += rtmp[i];
+    const double SDnrm = std::sqrt(s);
+    c.eGMRES = two * std::sqrt(epsA / SDnrm);
+}
+
+void or_solmfg(or_common* c, const or_mesh* m, const double* y, const double* ac, double* res,
+               double* bdiag, double* Dy, or_solve_stats* st, int nthreads) {
+    const int N = m->nshg;
+    const size_t n5 = 5 * (size_t)N;
+    const int K = c->Kspace;
+    std::vector<double> rmes(n5), ypre(n5), temp(n5);
+    std::vector<double> uB(n5 * (K + 1));
+    std::vector<double> H((K + 1) * K, 0.0), eB(K + 1, 0.0), yB(K, 0.0), Rc(K, 0.0), Rs(K, 0.0);
+    auto Hm = [&](int i, int j) -> double& { return H[(size_t)(i - 1) + (size_t)(K + 1) * (j - 1)]; };
+    auto U = [&](int j) { return uB.data() + n5 * (size_t)(j - 1); };
+
+    or_elmmfg(c, m, y, ac, res, rmes.data(), bdiag, 1, nthreads);
+    or_i3lu(N, bdiag, nullptr, 0);
+    or_i3lu(N, bdiag, res, 1);
+    or_i3lu(N, bdiag, rmes.data(), 1);
+    std::memcpy(U(1), res, sizeof(double) * n5);
+    std::fill(Dy, Dy + n5, 0.0);
+    std::memcpy(ypre.data(), y, sizeof(double) * n5);
+    or_yshuffle(N, ypre.data(), 1);
+    or_i3lu(N, bdiag, ypre.data(), 3);
+    double unorm = std::sqrt(sumsq(res, n5));
+    st->unorm0 = unorm;
+    int iKs = 0, lGMRES = 0;
+    double echeck = 0.0;
+    if (!(unorm < 100. * c->epsM * c->epsM)) {
+        const double epsnrm = c->etol * unorm;
+        if (c->iter == 1 && (c->istep % 20) == 0)
+            itrfdi(*c, *m, ypre.data(), y, ac, rmes.data(), res, bdiag, nthreads);
+        for (int mG = 1; mG <= c->nGMRES; ++mG) {
+            lGMRES = mG - 1;
+            if (lGMRES > 0) {
+                // Au2MFG restart (R - J Dy); not used by nGMRES = 1 configurations
+                std::vector<double> t(Dy, Dy + n5);
+                au1mfg(*c, *m, ypre.data(), y, ac, rmes.data(), bdiag, t.data(), nthreads);
+                for (size_t i = 0; i < n5; ++i) temp[i] = res[i] - t[i];
+                std::memcpy(U(1), temp.data(), sizeof(double) * n5);
+                unorm = std::sqrt(sumsq(temp.data(), n5));
+            }
+            std::fill(eB.begin(), eB.end(), 0.0);
+            eB[0] = unorm;
+            for (size_t i = 0; i < n5; ++i) U(1)[i] = U(1)[i] / unorm;
+            for (int iK = 1; iK <= K; ++iK) {
+                iKs = iK;
+                std::memcpy(temp.data(), U(iKs), sizeof(double) * n5);
+                au1mfg(*c, *m, ypre.data(), y, ac, rmes.data(), bdiag, temp.data(), nthreads);
+                std::memcpy(U(iKs + 1), temp.data(), sizeof(double) * n5);
+                double beta = 0.0;
+                for (int jK = 1; jK <= iKs + 1; ++jK) {
+                    double* w = U(iKs + 1);
+                    if (jK == 1) {
+                        beta = dot(w, U(1), n5);
+                    } else {
+                        const double* up = U(jK - 1);
+                        for (size_t i = 0; i < n5; ++i) w[i] = w[i] - beta * up[i];
+                        beta = dot(w, U(jK), n5);
+                    }
+                    Hm(jK, iKs) = beta;
+                }
+                unorm = std::sqrt(beta);
+                Hm(iKs + 1, iKs) = unorm;
+                for (size_t i = 0; i < n5; ++i) U(iKs + 1)[i] = U(iKs + 1)[i] / unorm;
+                for (int jK = 1; jK <= iKs - 1; ++jK) {
+                    const double t = Rc[jK - 1] * Hm(jK, iKs) + Rs[jK - 1] * Hm(jK + 1, iKs);
+                    Hm(jK + 1, iKs) = -Rs[jK - 1] * Hm(jK, iKs) + Rc[jK - 1] * Hm(jK + 1, iKs);
+                    Hm(jK, iKs) = t;
+                }
+                const double t = std::sqrt(Hm(iKs, iKs) * Hm(iKs, iKs) + Hm(iKs + 1, iKs) * Hm(iKs + 1, iKs));
+                Rc[iKs - 1] = Hm(iKs, iKs) / t;
+                Rs[iKs - 1] = Hm(iKs + 1, iKs) / t;
+                Hm(iKs, iKs) = t;
+                Hm(iKs + 1, iKs) = zero;
+                const double te = Rc[iKs - 1] * eB[iKs - 1] + Rs[iKs - 1] * eB[iKs];
+                eB[iKs] = -Rs[iKs - 1] * eB[iKs - 1] + Rc[iKs - 1] * eB[iKs];
+                eB[iKs - 1] = te;
+                st->ntotGM += 1;
+                echeck = std::fabs(eB[iKs]);
+                if (echeck <= epsnrm && iKs >= c->minIters) break;
+            }
+            for (int jK = iKs; jK >= 1; --jK) {
+                yB[jK - 1] = eB[jK - 1] / Hm(jK, jK);
+                for (int lK = 1; lK <= jK - 1; ++lK) eB[lK - 1] = eB[lK - 1] - yB[jK - 1] * Hm(lK, jK);
+            }
+            for (int jK = 1; jK <= iKs; ++jK) {
+                const double* uj = U(jK);
+                for (size_t i = 0; i < n5; ++i) Dy[i] = Dy[i] + yB[jK - 1] * uj[i];
+            }
+            if (std::fabs(eB[iKs]) <= epsnrm) break;
+        }
+    }
+    or_i3lu(N, bdiag, Dy, 2);
+    st->iKs = iKs;
+    st->lGMRES = lGMRES;
+    st->echeck = echeck;
+    st->eGMRES = c->eGMRES;
+    st->totres = std::sqrt(sumsq(res, n5)) / (double)N;
+}
+
+void or_itrpredict(const or_common* c, int N, const double* yold, const double* acold, double* y,
+                   double* ac) {
+    const size_t n5 = 5 * (size_t)N;
+    for (size_t i = 0; i < n5; ++i) {
+        y[i] = yold[i];
+        ac[i] = acold[i] * (one - c->almi / c->gami);
+    }
+}
+
+void or_itrcorrect(const or_common* c, int N, double* y, double* ac, const double* yold,
+                   const double* acold, const double* Dy) {
+    auto Y = [&](int k, int n) -> double& { return y[(size_t)(k - 1) * N + n]; };
+    auto D = [&](int k, int n) { return Dy[(size_t)(k - 1) * N + n]; };
+    for (int n = 0; n < N; ++n) {
+        Y(1, n) = Y(1, n) - D(2, n);
+        Y(2, n) = Y(2, n) - D(3, n);
+        Y(3, n) = Y(3, n) - D(4, n);
+        Y(4, n) = Y(4, n) - D(1, n);
+        Y(5, n) = Y(5, n) - D(5, n);
+    }
+    const double fct1 = (one - c->almi / c->gami);
+    const double fct2 = c->almi * c->Dtgl / c->gami / c->alfi;
+    for (size_t i = 0; i < 5 * (size_t)N; ++i) ac[i] = acold[i] * fct1 + (y[i] - yold[i]) * fct2;
+}
+
+void or_itrupdate(const or_common* c, int N, double* yold, double* acold, const double* y,
+                  const double* ac) {
+    const double fct2 = one / c->almi, fct3 = one / c->alfi;
+    for (size_t i = 0; i < 5 * (size_t)N; ++i) {
+        acold[i] = acold[i] + (ac[i] - acold[i]) * fct2;
+        yold[i] = yold[i] + (y[i] - yold[i]) * fct3;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,263 @@
+"""ctypes wrapper of the oracle (libphoracle.so) -- test infrastructure only.
+
+The same method names and array layouts as phasta_gb300.solver.GpuSolver, so
+parity tests compare the two call for call.  Only tests/, the smoke check and
+the CPU-baseline leg of bench.py use this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class Common(C.Structure):
+    _fields_ = [
+        ("Rgas", C.c_double), ("gamma", C.c_double), ("gamma1", C.c_double), ("pr", C.c_double),
+        ("rmu", C.c_double), ("Dtgl", C.c_double), ("almi", C.c_double), ("alfi", C.c_double),
+        ("gami", C.c_double), ("dtsfct", C.c_double), ("taucfct", C.c_double), ("temper", C.c_double),
+        ("itau", C.c_int), ("ivart", C.c_int), ("iremoveStabTimeTerm", C.c_int), ("Navier", C.c_int),
+        ("ipord", C.c_int), ("EntropyPressure", C.c_int), ("Kspace", C.c_int), ("nGMRES", C.c_int),
+        ("minIters", C.c_int), ("etol", C.c_double), ("epsM", C.c_double), ("eGMRES", C.c_double),
+        ("iter", C.c_int), ("istep", C.c_int),
+    ]
+
+
+class OMesh(C.Structure):
+    _fields_ = [
+        ("nshg", C.c_int), ("nelem", C.c_int), ("ien", _ip), ("nblk", C.c_int), ("blk_start", _ip),
+        ("ngrp", C.c_int), ("grp_start", _ip), ("x", _dp), ("nbelem", C.c_int), ("ienb", _ip),
+        ("iBCB", _ip), ("BCB", _dp), ("iBC", _ip), ("BC", _dp), ("iper", _ip),
+    ]
+
+
+class OStats(C.Structure):
+    _fields_ = [("iKs", C.c_int), ("lGMRES", C.c_int), ("ntotGM", C.c_int), ("unorm0", C.c_double),
+                ("echeck", C.c_double), ("eGMRES", C.c_double), ("totres", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        from .build_oracle import build_oracle  # noqa: WPS433
+        build_oracle()
+        L = C.CDLL(str(HERE / "libphoracle.so"))
+        cp, mp, vp = C.POINTER(Common), C.POINTER(OMesh), None
+        sig = {
+            "or_make_groups": ([C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, _ip, _ip, C.c_int], C.c_int),
+            "or_tet_tables": ([_dp] * 6, None),
+            "or_e3": ([cp, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp], None),
+            "or_e3b": ([cp, C.c_int, _dp, _ip, _dp, _dp, _dp], None),
+            "or_elmmfg": ([cp, mp, _dp, _dp, _dp, _dp, _dp, C.c_int, C.c_int], None),
+            "or_itrres": ([cp, mp, _dp, _dp, _dp, _dp, C.c_int, C.c_int], None),
+            "or_elmres": ([cp, mp, _dp, _dp, _dp, C.c_int], None),
+            "or_bc3res": ([mp, _dp, _dp, cp], None),
+            "or_bc3bdg": ([mp, _dp, _dp, cp], None),
+            "or_itrbc": ([mp, _dp, _dp, C.c_int, C.c_double], None),
+            "or_i3lu": ([C.c_int, _dp, _dp, C.c_int], None),
+            "or_yshuffle": ([C.c_int, _dp, C.c_int], None),
+            "or_solmfg": ([cp, mp, _dp, _dp, _dp, _dp, _dp, C.POINTER(OStats), C.c_int], None),
+            "or_itrpredict": ([cp, C.c_int, _dp, _dp, _dp, _dp], None),
+            "or_itrcorrect": ([cp, C.c_int, _dp, _dp, _dp, _dp, _dp], None),
+            "or_itrupdate": ([cp, C.c_int, _dp, _dp, _dp, _dp], None),
+        }
+        for name, (a, r) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = a
+            f.restype = r
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_ip)
+
+
+def common(params: dict) -> Common:
+    c = Common()
+    for name, _ in Common._fields_:
+        if name in params:
+            setattr(c, name, params[name])
+    return c
+
+
+@dataclass
+class OracleStats:
+    iKs: int
+    lGMRES: int
+    ntotGM: int
+    unorm0: float
+    echeck: float
+    eGMRES: float
+    totres: float
+
+
+def tet_tables():
+    L = lib()
+    shp, shgl, qwt = np.zeros(16), np.zeros(48), np.zeros(4)
+    shpb, shglb, qwtb = np.zeros(12), np.zeros(36), np.zeros(3)
+    L.or_tet_tables(_d(shp), _d(shgl), _d(qwt), _d(shpb), _d(shglb), _d(qwtb))
+    return {"shp": shp.reshape(4, 4), "shgl": shgl.reshape(4, 3, 4), "Qwt": qwt,
+            "shpb": shpb.reshape(3, 4), "shglb": shglb.reshape(3, 3, 4), "Qwtb": qwtb}
+
+
+def e3(params: dict, yl, ycl, acl, xl, ires=3, iprec=1):
+    """One element (e3.f). yl/ycl/acl (4,5) in element order (p,u,v,w,T), xl (4,3)."""
+    L = lib()
+    c = common(params)
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+    rl, rml, bd = np.zeros((4, 5)), np.zeros((4, 5)), np.zeros((4, 5, 5))
+    L.or_e3(C.byref(c), ires, iprec, _d(f(yl)), _d(f(ycl)), _d(f(acl)), _d(f(xl)), _d(rl), _d(rml), _d(bd))
+    return rl, rml, bd
+
+
+class Oracle:
+    """The whole-mesh routines on a Case (phasta_gb300.mesh.Case)."""
+
+    def __init__(self, case, params: dict, nthreads: int = 1, grouped: bool | None = None, bksiz: int = 64):
+        self.L = lib()
+        self.case = case
+        self.params = dict(params)
+        self.nthreads = nthreads
+        self.nshg = case.nshg
+        grouped = nthreads > 1 if grouped is None else grouped
+        ien = np.ascontiguousarray(case.ien, dtype=np.int32)
+        E = ien.shape[0]
+        if grouped:
+            perm = np.zeros(E, np.int32)
+            blk = np.zeros(E + 2, np.int32)
+            grp = np.zeros(1025, np.int32)
+            nb = C.c_int()
+            ng = self.L.or_make_groups(self.nshg, E, _i(ien.reshape(-1)), bksiz, _i(perm), _i(blk), C.byref(nb),
+                                       _i(grp), 1024)
+            assert ng > 0
+            ien = np.ascontiguousarray(ien[perm])
+            self._blk = np.ascontiguousarray(blk[: nb.value + 1])
+            self._grp = np.ascontiguousarray(grp[: ng + 1])
+            ngrp = ng
+        else:
+            nb = (E + bksiz - 1) // bksiz
+            self._blk = np.minimum(np.arange(nb + 1, dtype=np.int32) * bksiz, E).astype(np.int32)
+            self._grp = np.zeros(1, np.int32)
+            ngrp = 0
+        self._ien = ien.reshape(-1)
+        self._x = case.x_ref()
+        self._ienb = np.ascontiguousarray(case.ienb, dtype=np.int32).reshape(-1)
+        self._iBCB = np.ascontiguousarray(case.iBCB, dtype=np.int32).reshape(-1)
+        self._BCB = np.ascontiguousarray(case.BCB, dtype=np.float64).reshape(-1)
+        self._iBC = np.ascontiguousarray(case.iBC, dtype=np.int32)
+        self._BC = np.ascontiguousarray(case.BC, dtype=np.float64).reshape(-1)
+        self._iper = np.ascontiguousarray(case.iper, dtype=np.int32)
+        self.m = OMesh(self.nshg, E, _i(self._ien), len(self._blk) - 1, _i(self._blk), ngrp, _i(self._grp),
+                       _d(self._x), case.nbelem, _i(self._ienb), _i(self._iBCB), _d(self._BCB), _i(self._iBC),
+                       _d(self._BC), _i(self._iper))
+        self.c = common(self.params)
+        self.ntotGM = 0
+
+    def set_params(self, **kw):
+        self.params.update(kw)
+        self.c = common(self.params)
+
+    def _v(self, k=5):
+        return np.zeros(k * self.nshg)
+
+    def ElmMFG(self, y, ac, iprec=1):
+        res, rmes, bd = self._v(), self._v(), self._v(25)
+        self.L.or_elmmfg(C.byref(self.c), C.byref(self.m), _d(y), _d(ac), _d(res), _d(rmes), _d(bd), iprec,
+                         self.nthreads)
+        return res, rmes, (bd if iprec else None)
+
+    def ElmRes(self, y, ac):
+        res = self._v()
+        self.L.or_elmres(C.byref(self.c), C.byref(self.m), _d(y), _d(ac), _d(res), self.nthreads)
+        return res
+
+    def ItrRes(self, yp, yc, ac, rmes=None, iabres=0):
+        rmes = self._v() if rmes is None else np.array(rmes, dtype=np.float64)
+        self.L.or_itrres(C.byref(self.c), C.byref(self.m), _d(yp), _d(yc), _d(ac), _d(rmes), iabres, self.nthreads)
+        return rmes
+
+    def i3LU(self, bd, r, code):
+        bd = np.array(bd, dtype=np.float64)
+        r = None if r is None else np.array(r, dtype=np.float64)
+        self.L.or_i3lu(self.nshg, _d(bd), _d(r), code)
+        return bd, r
+
+    def bc3Res(self, y, res):
+        res = np.array(res, dtype=np.float64)
+        self.L.or_bc3res(C.byref(self.m), _d(y), _d(res), C.byref(self.c))
+        return res
+
+    def bc3BDg(self, y, bd):
+        bd = np.array(bd, dtype=np.float64)
+        self.L.or_bc3bdg(C.byref(self.m), _d(y), _d(bd), C.byref(self.c))
+        return bd
+
+    def itrBC(self, y, ac=None, ires=3):
+        y = np.array(y, dtype=np.float64)
+        ac = None if ac is None else np.array(ac, dtype=np.float64)
+        self.L.or_itrbc(C.byref(self.m), _d(y), _d(ac), ires, self.params["Rgas"])
+        return y, ac
+
+    def SolMFG(self, y, ac):
+        res, bd, Dy = self._v(), self._v(25), self._v()
+        st = OStats()
+        st.ntotGM = self.ntotGM
+        self.L.or_solmfg(C.byref(self.c), C.byref(self.m), _d(y), _d(ac), _d(res), _d(bd), _d(Dy), C.byref(st),
+                         self.nthreads)
+        self.ntotGM = st.ntotGM
+        self.params["eGMRES"] = self.c.eGMRES
+        return res, bd, Dy, OracleStats(st.iKs, st.lGMRES, st.ntotGM, st.unorm0, st.echeck, st.eGMRES, st.totres)
+
+    def itrPredict(self, yold, acold):
+        y, ac = self._v(), self._v()
+        self.L.or_itrpredict(C.byref(self.c), self.nshg, _d(yold), _d(acold), _d(y), _d(ac))
+        return y, ac
+
+    def itrCorrect(self, y, ac, yold, acold, Dy):
+        y, ac = np.array(y, dtype=np.float64), np.array(ac, dtype=np.float64)
+        self.L.or_itrcorrect(C.byref(self.c), self.nshg, _d(y), _d(ac), _d(yold), _d(acold), _d(Dy))
+        y, ac = self.itrBC(y, ac, ires=3)
+        return y, ac
+
+    def itrUpdate(self, yold, acold, y, ac):
+        yold, acold = np.array(yold, dtype=np.float64), np.array(acold, dtype=np.float64)
+        self.L.or_itrupdate(C.byref(self.c), self.nshg, _d(yold), _d(acold), _d(y), _d(ac))
+        return self.itrBC(yold, acold, ires=3)
+
+    def newton(self, y, ac, yold, acold):
+        """SolMFG + itrCorrect + itrBC (itrdrv.f:489-598)."""
+        res, bd, Dy, st = self.SolMFG(y, ac)
+        y, ac = self.itrCorrect(y, ac, yold, acold, Dy)
+        return y, ac, st, Dy
+
+    def time_step(self, yold, acold, nitr):
+        y, ac = self.itrPredict(yold, acold)
+        y, ac = self.itrBC(y, ac, ires=3)
+        stats = []
+        for it in range(1, nitr + 1):
+            self.set_params(iter=it)
+            y, ac, st, _ = self.newton(y, ac, yold, acold)
+            stats.append(st)
+        yold, acold = self.itrUpdate(yold, acold, y, ac)
+        self.set_params(istep=self.params["istep"] + 1)
+        return yold, acold, y, ac, stats

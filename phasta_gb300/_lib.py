@@ -1,0 +1,118 @@
+"""ctypes binding of ``include/phgpu.h`` (the C ABI of the GPU hot path).
+
+Loading fails loudly when ``libphgpu.so`` has not been built: there is no CPU
+fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libphgpu.so"
+
+PHGPU_OK = 0
+STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NONFINITE", 4: "SINGULAR", 5: "UNSUPPORTED", 6: "NOMEM"}
+PHGPU_FP64, PHGPU_MIXED = 0, 1
+PHGPU_AP_FD, PHGPU_AP_LINEAR = 0, 1
+LU_FACT, LU_FORWARD, LU_BACKWARD, LU_PRODUCT = 0, 1, 2, 3
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("Rgas", C.c_double), ("gamma", C.c_double), ("gamma1", C.c_double), ("pr", C.c_double),
+        ("rmu", C.c_double),
+        ("Dtgl", C.c_double), ("almi", C.c_double), ("alfi", C.c_double), ("gami", C.c_double),
+        ("dtsfct", C.c_double), ("taucfct", C.c_double), ("temper", C.c_double),
+        ("itau", C.c_int), ("ivart", C.c_int), ("iremoveStabTimeTerm", C.c_int), ("Navier", C.c_int),
+        ("ipord", C.c_int), ("EntropyPressure", C.c_int),
+        ("Kspace", C.c_int), ("nGMRES", C.c_int), ("minIters", C.c_int),
+        ("etol", C.c_double), ("epsM", C.c_double), ("eGMRES", C.c_double),
+        ("iter", C.c_int), ("istep", C.c_int),
+        ("precision", C.c_int), ("ap_mode", C.c_int), ("reserved", C.c_int * 6),
+    ]
+
+
+class Mesh(C.Structure):
+    _fields_ = [
+        ("nshg", C.c_int), ("nelem", C.c_int), ("ien", _ip), ("x", _dp),
+        ("nbelem", C.c_int), ("ienb", _ip), ("iBCB", _ip), ("BCB", _dp),
+        ("iBC", _ip), ("BC", _dp), ("iper", _ip),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("iKs", C.c_int), ("lGMRES", C.c_int), ("ntotGM", C.c_int), ("status", C.c_int),
+        ("unorm0", C.c_double), ("echeck", C.c_double), ("eGMRES", C.c_double), ("totres", C.c_double),
+        ("rnorm", C.c_double), ("t_assembly_ms", C.c_double), ("t_gmres_ms", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    """Load libphgpu.so (raises if it is missing: build it with phasta_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing; run phasta_gb300.build.build() (needs nvcc)")
+    L = C.CDLL(str(LIB_PATH))
+    vp = C.c_void_p
+    sig = {
+        "phgpu_create": ([C.POINTER(Mesh), C.POINTER(Config), C.POINTER(vp)], C.c_int),
+        "phgpu_destroy": ([vp], C.c_int),
+        "phgpu_set_config": ([vp, C.POINTER(Config)], C.c_int),
+        "phgpu_get_config": ([vp, C.POINTER(Config)], C.c_int),
+        "phgpu_last_error": ([vp], C.c_char_p),
+        "phgpu_stream": ([vp], vp),
+        "phgpu_num_colors": ([vp], C.c_int),
+        "phgpu_kernel_launches": ([vp], C.c_longlong),
+        "phgpu_elmmfg": ([vp, _dp, _dp, _dp, _dp, _dp, C.c_int], C.c_int),
+        "phgpu_elmres": ([vp, _dp, _dp, _dp], C.c_int),
+        "phgpu_itrres": ([vp, _dp, _dp, _dp, _dp], C.c_int),
+        "phgpu_i3lu": ([vp, _dp, _dp, C.c_int], C.c_int),
+        "phgpu_solmfg": ([vp, _dp, _dp, _dp, _dp, _dp, C.POINTER(Stats)], C.c_int),
+        "phgpu_itrcorrect": ([vp, _dp, _dp, _dp, _dp, _dp], C.c_int),
+        "phgpu_newton": ([vp, _dp, _dp, _dp, _dp, C.POINTER(Stats)], C.c_int),
+        "phgpu_time_step": ([vp, _dp, _dp, _dp, _dp, C.c_int, C.POINTER(Stats)], C.c_int),
+        "phgpu_upload_state": ([vp, _dp, _dp, _dp, _dp], C.c_int),
+        "phgpu_download_state": ([vp, _dp, _dp, _dp, _dp], C.c_int),
+        "phgpu_newton_dev": ([vp, C.POINTER(Stats)], C.c_int),
+        "phgpu_time_step_dev": ([vp, C.c_int, C.POINTER(Stats)], C.c_int),
+        "phgpu_residual_norm_dev": ([vp, _dp], C.c_int),
+        "phgpu_sweep_dev": ([vp, C.c_int], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def exported_symbols() -> list[str]:
+    """Names declared in include/phgpu.h (used to check the library's exports)."""
+    hdr = (Path(__file__).resolve().parent.parent / "include" / "phgpu.h").read_text()
+    import re
+    return sorted(set(re.findall(r"\b(phgpu_[a-z0-9_]+)\s*\(", hdr)))
+
+
+def dptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous, "expected a contiguous float64 array"
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags.c_contiguous, "expected a contiguous int32 array"
+    return a.ctypes.data_as(_ip)

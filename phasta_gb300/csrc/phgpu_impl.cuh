@@ -1,0 +1,152 @@
+// phgpu_impl.cuh -- internal declarations of the GB300 implementation of the
+// compressible Newton-Krylov hot path.  Device data layout:
+//   nodal vectors  [node][5] in element dof order (p, u, v, w, T) / equation order
+//   BDiag          [node][25], row-major 5x5 block (bd[n*25 + 5*i + j] = BDiag(n, i, j))
+//   coordinates    [node][3]
+//   connectivity   int4 per element, elements sorted by colour (no two elements
+//                  of one colour share a stored node, so scatters are plain
+//                  read-modify-writes, deterministic and atomic-free)
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/phgpu.h"
+
+namespace phgpu {
+
+constexpr int kBlock = 128;          // threads per block of the element kernels
+constexpr int kRedBlocks = 4 * 152;  // fixed grid of the reductions (deterministic order)
+constexpr int kRedThreads = 256;
+
+// Physics constants of one assembly, derived from phgpu_config (passed by value).
+template <typename R>
+struct Phys {
+    R Rgas, rRgas;       // R and 1/R
+    R cv, cp;            // R/(gamma-1), R*gamma/(gamma-1)
+    R rmu, rlm, rlm2mu, con, rlmpmu;  // viscosity, lambda, lambda+2mu, conductivity, lambda+mu
+    R fct1;              // almi/gami/alfi*Dtgl
+    R dts2;              // (2*dtsfct*Dtgl)^2  (0 if the time term is removed)
+    R fmu2;              // 36*mu^2
+    R taucfct, rtempcv;  // tau_C scale, temper/cv
+    int navier, supg;
+};
+
+// quadrature/shape tables for linear tets (host-computed, read-only in constant memory)
+struct TetTables {
+    double shp[4][4];    // [q][a]
+    double Qwt[4];
+    double shpb[3][4];
+    double Qwtb[3];
+};
+
+struct Ctx {
+    int N = 0, E = 0, Eb = 0;
+    phgpu_config cfg{};
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    std::string err;
+    long long launches = 0;
+
+    // element colouring
+    std::vector<int> col_start;   // ncol+1 (interior)
+    std::vector<int> bcol_start;  // boundary
+    int4* d_ien = nullptr;        // E
+    int4* d_ienb = nullptr;       // Eb (face nodes first)
+    int* d_iBCB = nullptr;        // Eb
+    double* d_BCB = nullptr;      // Eb*18  [e][n][6]
+    std::vector<int> perm_e;      // colour-sorted position -> input element id
+
+    double* d_x = nullptr;        // N*3
+    float* d_xf = nullptr;        // N*3
+    int* d_iBC = nullptr;         // N
+    double* d_BC = nullptr;       // N*6  [n][6]
+    float* d_BCf = nullptr;
+    int* d_iper = nullptr;        // N
+    int nmaster = 0;              // masters with slaves
+    int* d_mst = nullptr;         // masters
+    int* d_slv_start = nullptr;   // nmaster+1
+    int* d_slv = nullptr;         // slaves (ascending)
+    int nslave = 0;
+    int* d_slaves = nullptr;      // all slave nodes
+    int nbcn = 0;                 // nodes with a Dirichlet/flux bit
+    int* d_bcn = nullptr;
+
+    // state (FP64 master copies + FP32 shadows)
+    double *d_y = nullptr, *d_ac = nullptr, *d_yold = nullptr, *d_acold = nullptr;
+    float *d_yf = nullptr, *d_acf = nullptr;
+
+    // work arrays
+    double *d_res = nullptr, *d_rmes = nullptr, *d_bd = nullptr, *d_Dy = nullptr, *d_bdstage = nullptr;
+    double *d_ypre = nullptr, *d_t64 = nullptr, *d_t64b = nullptr;
+    float *d_resf = nullptr, *d_rmesf = nullptr, *d_bdf = nullptr, *d_t32 = nullptr, *d_t32b = nullptr;
+    void* d_U = nullptr;          // Krylov basis (Kspace+1) x 5N, double or float
+    int Ucap = 0;
+    double* d_scal = nullptr;     // device scalars (see Scal below)
+    double* d_part = nullptr;     // reduction partials
+    unsigned int* d_count = nullptr;
+    int* d_flag = nullptr;        // [0] converged, [1] error bits
+    double* h_scal = nullptr;     // pinned mirror
+    int* h_flag = nullptr;
+
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool timing = true;
+};
+
+// device scalar slots (d_scal)
+enum Scal : int {
+    S_BETA = 0,        // running MGS beta
+    S_UNORM = 1,
+    S_EPSNRM = 2,
+    S_ECHECK = 3,
+    S_TMP0 = 4, S_TMP1 = 5, S_TMP2 = 6, S_TMP3 = 7,
+    S_EB = 8,          // eBrg[K+1]
+    S_RC = 8 + 64,     // Rcos[K]
+    S_RS = 8 + 128,    // Rsin[K]
+    S_YB = 8 + 192,    // yBrg[K]
+    S_H = 8 + 256,     // H (K+1) x K, column-major
+    S_TOTAL = 8 + 256 + 65 * 64
+};
+constexpr int kMaxK = 63;
+
+template <typename R> Phys<R> make_phys(const phgpu_config& c);
+
+// ---- element kernels (elements.cu) ----
+enum ResMode : int { RM_RES = 1, RM_MODRES = 2, RM_LIN = 3 };
+template <typename R>
+void launch_elem_res(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R* ac,
+                     R* out, int iabres, const int* skip);
+template <typename R>
+void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rmes, R* bd);
+void launch_boundary(Ctx& C, const double* y, double* res);
+void upload_tables(Ctx& C);
+
+// ---- nodal kernels (nodal.cu) ----
+template <typename R> void bc3res(Ctx& C, R* r);
+template <typename R> void bc3bdg(Ctx& C, const double* y, R* bd);
+template <typename R> void itrbc_pert(Ctx& C, R* v, bool zero_dirichlet);
+void itrbc_state(Ctx& C, double* y, double* ac, bool with_ac);
+template <typename R> void lu_fact(Ctx& C, R* bd, int* flag);
+template <typename R, typename V> void lu_apply(Ctx& C, const R* bd, V* r, int code);
+void ref_to_dev_state(Ctx& C, const double* h_ref, double* d_tmp_host_layout, double* d_out);
+void dev_to_ref_state(Ctx& C, const double* d_in, double* d_tmp, double* h_ref);
+void ref_to_dev_res(Ctx& C, const double* h_ref, double* d_tmp, double* d_out);
+void dev_to_ref_res(Ctx& C, const double* d_in, double* d_tmp, double* h_ref);
+void ref_to_dev_bd(Ctx& C, const double* h_ref, double* d_tmp, double* d_out);
+void dev_to_ref_bd(Ctx& C, const double* d_in, double* d_tmp, double* h_ref);
+void to_f32(Ctx& C, const double* a, float* b, size_t n);
+void to_f64(Ctx& C, const float* a, double* b, size_t n);
+void fill0(Ctx& C, void* p, size_t bytes);
+
+// reductions with FP64 accumulation into d_scal[slot] (deterministic)
+template <typename V> void dot(Ctx& C, const V* a, const V* b, size_t n, int slot, const int* skip);
+// MGS step: w -= d_scal[S_H + (jprev)]*uprev (if uprev), then H[...] = w.uj
+template <typename V>
+void mgs_step(Ctx& C, V* w, const V* uprev, const double* beta_prev, const V* uj, size_t n,
+              double* beta_out, const int* skip);
+template <typename V> void scale_by(Ctx& C, V* w, const double* s, int mode, size_t n, const int* skip);
+
+int check(Ctx& C, cudaError_t e, const char* what);
+
+}  // namespace phgpu

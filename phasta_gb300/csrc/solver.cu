@@ -1,0 +1,959 @@
+// solver.cu -- set-up (colouring, device mirrors) and the drivers of the hot
+// path: ElmMFG (elmmfg.f), ItrRes (itrres.f), SolMFG (solmfg.f: block-LU
+// preconditioning, finite-difference or linearized Au1MFG, MGS Arnoldi,
+// Givens least squares), itrFDI (itrfdi.f), itrCorrect/itrBC/itrUpdate
+// (itrPC.f, itrbc.f) and the C ABI of include/phgpu.h.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <type_traits>
+
+#include "phgpu_impl.cuh"
+
+namespace phgpu {
+
+int check(Ctx& C, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return PHGPU_OK;
+    if (C.err.empty()) C.err = std::string(what) + ": " + cudaGetErrorString(e);
+    return PHGPU_ERR_CUDA;
+}
+
+namespace {
+
+#define PH_TRY(x)                          \
+    do {                                   \
+        int _s = (x);                      \
+        if (_s != PHGPU_OK) return _s;     \
+    } while (0)
+
+int fail(Ctx& C, int code, const std::string& msg) {
+    C.err = msg;
+    return code;
+}
+
+template <typename T>
+int dalloc(Ctx& C, T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * n);
+    if (e != cudaSuccess) {
+        C.err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return PHGPU_ERR_NOMEM;
+    }
+    return PHGPU_OK;
+}
+
+int sync(Ctx& C) {
+    PH_TRY(check(C, cudaGetLastError(), "kernel launch"));
+    return check(C, cudaStreamSynchronize(C.stream), "stream synchronize");
+}
+
+// greedy first-fit colouring: no two elements of a colour share a node
+int colour(Ctx& C, int n_nodes, const int* ien4, int ne, std::vector<int>& order, std::vector<int>& start) {
+    std::vector<uint64_t> m0(n_nodes, 0), m1(n_nodes, 0);
+    std::vector<int> col(ne);
+    int ncol = 0;
+    for (int e = 0; e < ne; ++e) {
+        const int* nd = ien4 + 4 * (size_t)e;
+        uint64_t f0 = 0, f1 = 0;
+        for (int a = 0; a < 4; ++a) {
+            f0 |= m0[nd[a]];
+            f1 |= m1[nd[a]];
+        }
+        int c;
+        if (~f0) c = __builtin_ctzll(~f0);
+        else if (~f1) c = 64 + __builtin_ctzll(~f1);
+        else return fail(C, PHGPU_ERR_UNSUPPORTED, "element colouring needs more than 128 colours");
+        col[e] = c;
+        ncol = std::max(ncol, c + 1);
+        for (int a = 0; a < 4; ++a) {
+            if (c < 64) m0[nd[a]] |= (1ull << c);
+            else m1[nd[a]] |= (1ull << (c - 64));
+        }
+    }
+    start.assign(ncol + 1, 0);
+    for (int e = 0; e < ne; ++e) start[col[e] + 1]++;
+    for (int c = 0; c < ncol; ++c) start[c + 1] += start[c];
+    std::vector<int> pos(start.begin(), start.end() - 1);
+    order.resize(ne);
+    for (int e = 0; e < ne; ++e) order[pos[col[e]]++] = e;
+    return PHGPU_OK;
+}
+
+// ------------------------------------------------------------------------
+// small device kernels of the driver
+// ------------------------------------------------------------------------
+template <typename V>
+__global__ void k_axpy_pre(const double* __restrict__ ypre, const V* __restrict__ u, double e, V* __restrict__ t,
+                           size_t n, const int* skip) {
+    if (skip && *skip) return;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        t[i] = (V)(ypre[i] + e * (double)u[i]);
+}
+template <typename V>
+__global__ void k_fd_diff(const V* __restrict__ ub, const V* __restrict__ rmes, double e, V* __restrict__ u,
+                          size_t n, const int* skip) {
+    if (skip && *skip) return;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        u[i] = (ub[i] - rmes[i]) / (V)e;
+}
+template <typename V>
+__global__ void k_copy(const V* __restrict__ a, V* __restrict__ b, size_t n, const int* skip) {
+    if (skip && *skip) return;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = a[i];
+}
+__global__ void k_fdi_combine(double* __restrict__ r, const double* __restrict__ rmes, double epsM, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double d = (r[i] - 2.0 * rmes[i]) / epsM;
+        r[i] = d;
+    }
+}
+__global__ void k_axpby(const double* __restrict__ a, double alpha, const double* __restrict__ b, double beta,
+                        double* __restrict__ o, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        o[i] = alpha * a[i] + beta * b[i];
+}
+
+// Givens update of column iKs (solmfg.f:274-317); also sets H(iKs+1,iKs) = sqrt(beta)
+__global__ void k_givens(double* __restrict__ s, int K, int iKs, int minIters, int* __restrict__ flag) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (flag[0]) return;
+    auto H = [&](int i, int j) -> double& { return s[S_H + (i - 1) + (K + 1) * (j - 1)]; };
+    double* eB = s + S_EB;
+    double* Rc = s + S_RC;
+    double* Rs = s + S_RS;
+    const double unorm = sqrt(H(iKs + 1, iKs));
+    H(iKs + 1, iKs) = unorm;
+    for (int jK = 1; jK <= iKs - 1; ++jK) {
+        const double t = Rc[jK - 1] * H(jK, iKs) + Rs[jK - 1] * H(jK + 1, iKs);
+        H(jK + 1, iKs) = -Rs[jK - 1] * H(jK, iKs) + Rc[jK - 1] * H(jK + 1, iKs);
+        H(jK, iKs) = t;
+    }
+    const double t = sqrt(H(iKs, iKs) * H(iKs, iKs) + H(iKs + 1, iKs) * H(iKs + 1, iKs));
+    Rc[iKs - 1] = H(iKs, iKs) / t;
+    Rs[iKs - 1] = H(iKs + 1, iKs) / t;
+    H(iKs, iKs) = t;
+    H(iKs + 1, iKs) = 0.0;
+    const double te = Rc[iKs - 1] * eB[iKs - 1] + Rs[iKs - 1] * eB[iKs];
+    eB[iKs] = -Rs[iKs - 1] * eB[iKs - 1] + Rc[iKs - 1] * eB[iKs];
+    eB[iKs - 1] = te;
+    const double echeck = fabs(eB[iKs]);
+    s[S_ECHECK] = echeck;
+    if (!(echeck == echeck)) flag[1] |= 2;
+    if (echeck <= s[S_EPSNRM] && iKs >= minIters) flag[0] = 1;
+}
+
+// back substitution H y = e (solmfg.f:329-334)
+__global__ void k_backsolve(double* __restrict__ s, int K, int iKs) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    auto H = [&](int i, int j) -> double { return s[S_H + (i - 1) + (K + 1) * (j - 1)]; };
+    double* eB = s + S_EB;
+    double* yB = s + S_YB;
+    for (int jK = iKs; jK >= 1; --jK) {
+        yB[jK - 1] = eB[jK - 1] / H(jK, jK);
+        for (int lK = 1; lK <= jK - 1; ++lK) eB[lK - 1] = eB[lK - 1] - yB[jK - 1] * H(lK, jK);
+    }
+}
+
+// Dy = Dy + sum_j yBrg(j) u_j (solmfg.f:338-340)
+template <typename V>
+__global__ void k_update_dy(double* __restrict__ Dy, const V* __restrict__ U, size_t ld, int iKs,
+                            const double* __restrict__ s, size_t n) {
+    const double* yB = s + S_YB;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double d = Dy[i];
+        for (int j = 0; j < iKs; ++j) d = d + yB[j] * (double)U[(size_t)j * ld + i];
+        Dy[i] = d;
+    }
+}
+
+__global__ void k_init_cycle(double* __restrict__ s, int K, double unorm, double epsnrm, int* flag) {
+    const int t = threadIdx.x;
+    for (int i = t; i < K + 1; i += blockDim.x) s[S_EB + i] = 0.0;
+    for (int i = t; i < (K + 1) * K; i += blockDim.x) s[S_H + i] = 0.0;
+    if (t == 0) {
+        s[S_EB] = unorm;
+        s[S_UNORM] = unorm;
+        s[S_EPSNRM] = epsnrm;
+        s[S_ECHECK] = 0.0;
+        flag[0] = 0;
+    }
+}
+
+// itrCorrect (itrPC.f:128-148) in the device's local dof order
+__global__ void k_correct(double* __restrict__ y, double* __restrict__ ac, const double* __restrict__ yold,
+                          const double* __restrict__ acold, const double* __restrict__ Dy, double fct1,
+                          double fct2, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double yi = y[i] - Dy[i];
+        y[i] = yi;
+        ac[i] = acold[i] * fct1 + (yi - yold[i]) * fct2;
+    }
+}
+__global__ void k_predict(const double* __restrict__ yold, const double* __restrict__ acold, double* __restrict__ y,
+                          double* __restrict__ ac, double f, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        y[i] = yold[i];
+        ac[i] = acold[i] * f;
+    }
+}
+__global__ void k_update(double* __restrict__ yold, double* __restrict__ acold, const double* __restrict__ y,
+                         const double* __restrict__ ac, double fct2, double fct3, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        acold[i] = acold[i] + (ac[i] - acold[i]) * fct2;
+        yold[i] = yold[i] + (y[i] - yold[i]) * fct3;
+    }
+}
+
+constexpr int kVG = kRedBlocks, kVT = 256;
+
+// ------------------------------------------------------------------------
+// ElmMFG / residual drivers on resident device data
+// ------------------------------------------------------------------------
+int elmres64(Ctx& C, const double* y, const double* ac, double* res) {
+    fill0(C, res, sizeof(double) * 5 * (size_t)C.N);
+    launch_elem_res<double>(C, RM_RES, C.d_x, y, nullptr, ac, res, 0, nullptr);
+    if (C.Eb > 0) launch_boundary(C, y, res);
+    bc3res<double>(C, res);
+    return check(C, cudaGetLastError(), "elmres");
+}
+
+int elmmfg64(Ctx& C, const double* y, const double* ac, double* res, double* rmes, double* bd, int iprec) {
+    const size_t N = C.N;
+    fill0(C, res, sizeof(double) * 5 * N);
+    fill0(C, rmes, sizeof(double) * 5 * N);
+    if (iprec) {
+        fill0(C, bd, sizeof(double) * 25 * N);
+        launch_elem_full<double>(C, C.d_x, y, ac, res, rmes, bd);
+    } else {
+        launch_elem_res<double>(C, RM_RES, C.d_x, y, nullptr, ac, res, 0, nullptr);
+        launch_elem_res<double>(C, RM_MODRES, C.d_x, y, y, ac, rmes, 0, nullptr);
+    }
+    if (C.Eb > 0) launch_boundary(C, y, res);
+    bc3res<double>(C, res);
+    bc3res<double>(C, rmes);
+    if (iprec) bc3bdg<double>(C, y, bd);
+    return check(C, cudaGetLastError(), "elmmfg");
+}
+
+// rmes += Rmod(yp; yc) then bc3Res (itrres.f)
+template <typename R>
+int itrres_dev(Ctx& C, const R* x, const R* yp, const R* yc, R* rmes, int iabres, const int* skip) {
+    launch_elem_res<R>(C, RM_MODRES, x, yp, yc, nullptr, rmes, iabres, skip);
+    bc3res<R>(C, rmes);
+    return PHGPU_OK;
+}
+
+// ------------------------------------------------------------------------
+// SolMFG
+// ------------------------------------------------------------------------
+template <typename V>
+struct KrylovOps;
+
+// Jacobian-vector product u <- L^-1 J U^-1 u (Au1MFG, au1mfg.f:57-83)
+int ap_fd64(Ctx& C, double* u, const double* rmes, const int* skip) {
+    const size_t n5 = 5 * (size_t)C.N;
+    double* t = C.d_t64;
+    double* ub = C.d_t64b;
+    k_axpy_pre<double><<<kVG, kVT, 0, C.stream>>>(C.d_ypre, u, C.cfg.eGMRES, t, n5, skip);
+    ++C.launches;
+    lu_apply<double, double>(C, C.d_bd, t, PHGPU_LU_BACKWARD);
+    itrbc_pert<double>(C, t, false);
+    fill0(C, ub, sizeof(double) * n5);
+    itrres_dev<double>(C, C.d_x, t, C.d_y, ub, 0, skip);
+    lu_apply<double, double>(C, C.d_bd, ub, PHGPU_LU_FORWARD);
+    k_fd_diff<double><<<kVG, kVT, 0, C.stream>>>(ub, rmes, C.cfg.eGMRES, u, n5, skip);
+    ++C.launches;
+    return PHGPU_OK;
+}
+
+template <typename V>
+int ap_lin(Ctx& C, V* u, const int* skip);
+
+template <>
+int ap_lin<double>(Ctx& C, double* u, const int* skip) {
+    const size_t n5 = 5 * (size_t)C.N;
+    double* v = C.d_t64;
+    k_copy<double><<<kVG, kVT, 0, C.stream>>>(u, v, n5, skip);
+    ++C.launches;
+    lu_apply<double, double>(C, C.d_bd, v, PHGPU_LU_BACKWARD);
+    itrbc_pert<double>(C, v, true);
+    fill0(C, u, sizeof(double) * n5);
+    launch_elem_res<double>(C, RM_LIN, C.d_x, v, C.d_y, nullptr, u, 0, skip);
+    bc3res<double>(C, u);
+    lu_apply<double, double>(C, C.d_bd, u, PHGPU_LU_FORWARD);
+    return PHGPU_OK;
+}
+
+template <>
+int ap_lin<float>(Ctx& C, float* u, const int* skip) {
+    const size_t n5 = 5 * (size_t)C.N;
+    float* v = C.d_t32;
+    k_copy<float><<<kVG, kVT, 0, C.stream>>>(u, v, n5, skip);
+    ++C.launches;
+    lu_apply<float, float>(C, C.d_bdf, v, PHGPU_LU_BACKWARD);
+    itrbc_pert<float>(C, v, true);
+    fill0(C, u, sizeof(float) * n5);
+    launch_elem_res<float>(C, RM_LIN, C.d_xf, v, C.d_yf, nullptr, u, 0, skip);
+    bc3res<float>(C, u);
+    lu_apply<float, float>(C, C.d_bdf, u, PHGPU_LU_FORWARD);
+    return PHGPU_OK;
+}
+
+// itrFDI (itrfdi.f:45-139), FP64
+int itrfdi_dev(Ctx& C, const double* rmes, const double* ubrg) {
+    const size_t n5 = 5 * (size_t)C.N;
+    double* rt = C.d_t64b;
+    double* yt = C.d_t64;
+    // cancellation error epsA
+    fill0(C, rt, sizeof(double) * n5);
+    k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_ypre, yt, n5, nullptr);
+    ++C.launches;
+    lu_apply<double, double>(C, C.d_bd, yt, PHGPU_LU_BACKWARD);
+    itrres_dev<double>(C, C.d_x, yt, C.d_y, rt, 1, nullptr);
+    lu_apply<double, double>(C, C.d_bd, rt, PHGPU_LU_FORWARD);
+    dot<double>(C, rt, rt, n5, S_TMP0, nullptr);
+    // second derivative
+    const double epsSD = std::sqrt(C.cfg.epsM);
+    fill0(C, rt, sizeof(double) * n5);
+    k_axpy_pre<double><<<kVG, kVT, 0, C.stream>>>(C.d_ypre, ubrg, epsSD, yt, n5, nullptr);
+    ++C.launches;
+    lu_apply<double, double>(C, C.d_bd, yt, PHGPU_LU_BACKWARD);
+    itrres_dev<double>(C, C.d_x, yt, C.d_y, rt, 0, nullptr);
+    k_axpy_pre<double><<<kVG, kVT, 0, C.stream>>>(C.d_ypre, ubrg, -epsSD, yt, n5, nullptr);
+    ++C.launches;
+    lu_apply<double, double>(C, C.d_bd, yt, PHGPU_LU_BACKWARD);
+    itrres_dev<double>(C, C.d_x, yt, C.d_y, rt, 0, nullptr);
+    lu_apply<double, double>(C, C.d_bd, rt, PHGPU_LU_FORWARD);
+    k_fdi_combine<<<kVG, kVT, 0, C.stream>>>(rt, rmes, C.cfg.epsM, n5);
+    ++C.launches;
+    dot<double>(C, rt, rt, n5, S_TMP1, nullptr);
+    PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, C.d_scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "fdi"));
+    PH_TRY(sync(C));
+    const double epsA = (C.cfg.epsM * C.cfg.epsM) * std::sqrt(C.h_scal[S_TMP0]);
+    const double SDnrm = std::sqrt(C.h_scal[S_TMP1]);
+    C.cfg.eGMRES = 2.0 * std::sqrt(epsA / SDnrm);
+    if (!std::isfinite(C.cfg.eGMRES) || C.cfg.eGMRES <= 0.0)
+        return fail(C, PHGPU_ERR_NONFINITE, "itrFDI produced a non-finite finite-difference interval");
+    return PHGPU_OK;
+}
+
+// GMRES cycles on V-typed Krylov vectors; b (= L^-1 R, FP64) in d_res, output Dy (FP64, before U^-1)
+template <typename V>
+int gmres(Ctx& C, phgpu_stats* st) {
+    const size_t n5 = 5 * (size_t)C.N;
+    const int K = C.cfg.Kspace;
+    V* U = (V*)C.d_U;
+    auto Uj = [&](int j) { return U + (size_t)(j - 1) * n5; };  // 1-based
+    double* s = C.d_scal;
+    const int* done = C.d_flag;
+    // ||b||
+    dot<double>(C, C.d_res, C.d_res, n5, S_TMP0, nullptr);
+    PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "unorm"));
+    PH_TRY(sync(C));
+    double unorm = std::sqrt(C.h_scal[S_TMP0]);
+    st->unorm0 = unorm;
+    st->totres = unorm / (double)C.N;
+    fill0(C, C.d_Dy, sizeof(double) * n5);
+    st->iKs = 0;
+    st->lGMRES = 0;
+    if (!std::isfinite(unorm)) return fail(C, PHGPU_ERR_NONFINITE, "non-finite residual (tnanq)");
+    if (unorm < 100. * C.cfg.epsM * C.cfg.epsM) return PHGPU_OK;
+    const double epsnrm = C.cfg.etol * unorm;
+    if (C.cfg.ap_mode == PHGPU_AP_FD && C.cfg.iter == 1 && (C.cfg.istep % 20) == 0) PH_TRY(itrfdi_dev(C, C.d_rmes, C.d_res));
+    st->eGMRES = C.cfg.eGMRES;
+    if constexpr (std::is_same<V, double>::value) {
+        k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_res, Uj(1), n5, nullptr);
+        ++C.launches;
+    } else {
+        to_f32(C, C.d_res, Uj(1), n5);
+    }
+    int iKs = 0;
+    for (int mG = 1; mG <= C.cfg.nGMRES; ++mG) {
+        st->lGMRES = mG - 1;
+        if (mG > 1) {
+            // restart: uBrg(1) = R - A Dy (Au2MFG is a central difference; the
+            // one-sided/linearized product is used here)
+            V* t = Uj(1);
+            if constexpr (std::is_same<V, double>::value) {
+                k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, t, n5, nullptr);
+                ++C.launches;
+                if (C.cfg.ap_mode == PHGPU_AP_FD) PH_TRY(ap_fd64(C, t, C.d_rmes, nullptr));
+                else PH_TRY(ap_lin<V>(C, t, nullptr));
+                k_axpby<<<kVG, kVT, 0, C.stream>>>(C.d_res, 1.0, t, -1.0, t, n5);  // t = b - A Dy
+                ++C.launches;
+            } else {
+                to_f32(C, C.d_Dy, t, n5);
+                PH_TRY(ap_lin<V>(C, t, nullptr));
+                to_f64(C, t, C.d_t64b, n5);
+                k_axpby<<<kVG, kVT, 0, C.stream>>>(C.d_res, 1.0, C.d_t64b, -1.0, C.d_t64b, n5);
+                ++C.launches;
+                to_f32(C, C.d_t64b, t, n5);
+            }
+            dot<V>(C, t, t, n5, S_TMP0, nullptr);
+            PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "unorm"));
+            PH_TRY(sync(C));
+            unorm = std::sqrt(C.h_scal[S_TMP0]);
+        }
+        k_init_cycle<<<1, 256, 0, C.stream>>>(s, K, unorm, epsnrm, C.d_flag);
+        ++C.launches;
+        // uBrg(1) /= unorm
+        scale_by<V>(C, Uj(1), s + S_UNORM, 0, n5, nullptr);
+        for (int iK = 1; iK <= K; ++iK) {
+            iKs = iK;
+            V* w = Uj(iKs + 1);
+            k_copy<V><<<kVG, kVT, 0, C.stream>>>(Uj(iKs), w, n5, nullptr);
+            ++C.launches;
+            if constexpr (std::is_same<V, double>::value) {
+                if (C.cfg.ap_mode == PHGPU_AP_FD) PH_TRY(ap_fd64(C, w, C.d_rmes, nullptr));
+                else PH_TRY(ap_lin<V>(C, w, nullptr));
+            } else {
+                PH_TRY(ap_lin<V>(C, w, nullptr));
+            }
+            // modified Gram-Schmidt (solmfg.f:247-267)
+            double* Hcol = s + S_H + (size_t)(K + 1) * (iKs - 1);
+            for (int jK = 1; jK <= iKs + 1; ++jK) {
+                const V* up = (jK == 1) ? nullptr : Uj(jK - 1);
+                const double* bprev = (jK == 1) ? nullptr : Hcol + (jK - 2);
+                mgs_step<V>(C, w, up, bprev, Uj(jK), n5, Hcol + (jK - 1), nullptr);
+            }
+            scale_by<V>(C, w, Hcol + iKs, 1, n5, nullptr);
+            k_givens<<<1, 1, 0, C.stream>>>(s, K, iKs, C.cfg.minIters, C.d_flag);
+            ++C.launches;
+            st->ntotGM += 1;
+            PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
+            PH_TRY(sync(C));
+            if (C.h_flag[1]) return fail(C, PHGPU_ERR_NONFINITE, "non-finite Hessenberg entry in GMRES");
+            if (C.h_flag[0]) break;
+        }
+        k_backsolve<<<1, 1, 0, C.stream>>>(s, K, iKs);
+        k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, U, n5, iKs, s, n5);
+        C.launches += 2;
+        PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "echeck"));
+        PH_TRY(sync(C));
+        st->echeck = C.h_scal[S_ECHECK];
+        if (C.h_scal[S_ECHECK] <= epsnrm) break;
+    }
+    st->iKs = iKs;
+    (void)done;
+    return PHGPU_OK;
+}
+
+int solmfg_dev(Ctx& C, phgpu_stats* st) {
+    const size_t N = C.N, n5 = 5 * N;
+    cudaEventRecord(C.ev[0], C.stream);
+    if (C.cfg.precision == PHGPU_FP64) {
+        PH_TRY(elmmfg64(C, C.d_y, C.d_ac, C.d_res, C.d_rmes, C.d_bd, 1));
+    } else {
+        if (C.cfg.ap_mode != PHGPU_AP_LINEAR)
+            return fail(C, PHGPU_ERR_UNSUPPORTED, "mixed precision needs the linearized Jacobian-vector product");
+        // FP64 outer residual; FP32 block-diagonal tangent
+        PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
+        to_f32(C, C.d_y, C.d_yf, n5);
+        to_f32(C, C.d_ac, C.d_acf, n5);
+        fill0(C, C.d_bdf, sizeof(float) * 25 * N);
+        launch_elem_full<float>(C, C.d_xf, C.d_yf, C.d_acf, nullptr, nullptr, C.d_bdf);
+        bc3bdg<float>(C, C.d_y, C.d_bdf);
+        to_f64(C, C.d_bdf, C.d_bd, 25 * N);
+    }
+    // nonlinear residual ||R|| (FP64, unpreconditioned)
+    dot<double>(C, C.d_res, C.d_res, n5, S_TMP3, nullptr);
+    fill0(C, C.d_flag, sizeof(int) * 2);
+    lu_fact<double>(C, C.d_bd, C.d_flag);
+    if (C.cfg.precision == PHGPU_MIXED) to_f32(C, C.d_bd, C.d_bdf, 25 * N);
+    lu_apply<double, double>(C, C.d_bd, C.d_res, PHGPU_LU_FORWARD);
+    if (C.cfg.precision == PHGPU_FP64) lu_apply<double, double>(C, C.d_bd, C.d_rmes, PHGPU_LU_FORWARD);
+    // ypre = U . y (local order is already the "old" order)
+    k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_y, C.d_ypre, n5, nullptr);
+    ++C.launches;
+    lu_apply<double, double>(C, C.d_bd, C.d_ypre, PHGPU_LU_PRODUCT);
+    PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
+    PH_TRY(check(C, cudaMemcpyAsync(C.h_scal + 8, C.d_scal + S_TMP3, sizeof(double), cudaMemcpyDeviceToHost, C.stream), "rn"));
+    PH_TRY(sync(C));
+    st->rnorm = std::sqrt(C.h_scal[8]);
+    if (C.h_flag[1]) return fail(C, PHGPU_ERR_SINGULAR, "zero or non-finite pivot in the block-diagonal LU");
+    cudaEventRecord(C.ev[1], C.stream);
+    int rc;
+    if (C.cfg.precision == PHGPU_FP64) rc = gmres<double>(C, st);
+    else rc = gmres<float>(C, st);
+    if (rc != PHGPU_OK) return rc;
+    lu_apply<double, double>(C, C.d_bd, C.d_Dy, PHGPU_LU_BACKWARD);
+    cudaEventRecord(C.ev[2], C.stream);
+    PH_TRY(sync(C));
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, C.ev[0], C.ev[1]);
+    cudaEventElapsedTime(&b, C.ev[1], C.ev[2]);
+    st->t_assembly_ms = a;
+    st->t_gmres_ms = b;
+    st->status = PHGPU_OK;
+    return PHGPU_OK;
+}
+
+int correct_dev(Ctx& C) {
+    const size_t n5 = 5 * (size_t)C.N;
+    const phgpu_config& c = C.cfg;
+    k_correct<<<kVG, kVT, 0, C.stream>>>(C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_Dy, 1.0 - c.almi / c.gami,
+                                         c.almi * c.Dtgl / c.gami / c.alfi, n5);
+    ++C.launches;
+    itrbc_state(C, C.d_y, C.d_ac, true);
+    return check(C, cudaGetLastError(), "itrCorrect");
+}
+
+int newton_dev(Ctx& C, phgpu_stats* st) {
+    PH_TRY(solmfg_dev(C, st));
+    PH_TRY(correct_dev(C));
+    return PHGPU_OK;
+}
+
+int time_step_dev(Ctx& C, int nitr, phgpu_stats* st) {
+    const size_t n5 = 5 * (size_t)C.N;
+    const phgpu_config& c = C.cfg;
+    k_predict<<<kVG, kVT, 0, C.stream>>>(C.d_yold, C.d_acold, C.d_y, C.d_ac, 1.0 - c.almi / c.gami, n5);
+    ++C.launches;
+    itrbc_state(C, C.d_y, C.d_ac, true);
+    for (int it = 1; it <= nitr; ++it) {
+        C.cfg.iter = it;
+        PH_TRY(newton_dev(C, st));
+    }
+    k_update<<<kVG, kVT, 0, C.stream>>>(C.d_yold, C.d_acold, C.d_y, C.d_ac, 1.0 / c.almi, 1.0 / c.alfi, n5);
+    ++C.launches;
+    itrbc_state(C, C.d_yold, C.d_acold, true);
+    C.cfg.istep += 1;
+    return sync(C);
+}
+
+}  // namespace
+}  // namespace phgpu
+
+// ============================================================================
+// C ABI
+// ============================================================================
+using phgpu::Ctx;
+
+struct phgpu_ctx {
+    Ctx c;
+};
+
+extern "C" {
+
+int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) {
+    using namespace phgpu;
+    if (!out) return PHGPU_ERR_INVALID;
+    *out = nullptr;
+    if (!m || !cfg || m->nshg <= 0 || m->nelem <= 0 || !m->ien || !m->x || !m->iBC || !m->BC || !m->iper)
+        return PHGPU_ERR_INVALID;
+    if (m->nbelem < 0 || (m->nbelem > 0 && !m->ienb)) return PHGPU_ERR_INVALID;
+    if (cfg->Kspace < 1 || cfg->Kspace > kMaxK || cfg->nGMRES < 1) return PHGPU_ERR_INVALID;
+    if (cfg->itau != 0 || cfg->ipord != 1 || cfg->EntropyPressure != 0) return PHGPU_ERR_UNSUPPORTED;
+    phgpu_ctx* h = new (std::nothrow) phgpu_ctx();
+    if (!h) return PHGPU_ERR_NOMEM;
+    Ctx& C = h->c;
+    C.N = m->nshg;
+    C.E = m->nelem;
+    C.Eb = m->nbelem;
+    C.cfg = *cfg;
+    const int N = C.N;
+    // validate connectivity and periodic masters
+    for (size_t i = 0; i < 4 * (size_t)C.E; ++i)
+        if (m->ien[i] < 0 || m->ien[i] >= N) { delete h; return PHGPU_ERR_INVALID; }
+    for (size_t i = 0; i < 4 * (size_t)C.Eb; ++i)
+        if (m->ienb[i] < 0 || m->ienb[i] >= N) { delete h; return PHGPU_ERR_INVALID; }
+    for (int n = 0; n < N; ++n) {
+        const int p = m->iper[n];
+        if (p < 0 || p >= N) { delete h; return PHGPU_ERR_INVALID; }
+        if (p != n && m->iper[p] != p) { delete h; return PHGPU_ERR_UNSUPPORTED; }  // chains
+        if (((m->iBC[n] >> 10) & 1) != (p != n ? 1 : 0)) { delete h; return PHGPU_ERR_INVALID; }
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { delete h; return PHGPU_ERR_CUDA; }
+    C.device = dev;
+    if (cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking) != cudaSuccess) { delete h; return PHGPU_ERR_CUDA; }
+    for (auto& e : C.ev) cudaEventCreate(&e);
+    int rc = PHGPU_OK;
+    auto T = [&](int s) { if (rc == PHGPU_OK) rc = s; };
+    // colouring
+    std::vector<int> order, border;
+    T(colour(C, N, m->ien, C.E, order, C.col_start));
+    if (C.Eb > 0) T(colour(C, N, m->ienb, C.Eb, border, C.bcol_start));
+    if (rc != PHGPU_OK) { phgpu_destroy(h); return rc; }
+    C.perm_e = order;
+    std::vector<int4> ien(C.E);
+    for (int i = 0; i < C.E; ++i) {
+        const int* p = m->ien + 4 * (size_t)order[i];
+        ien[i] = make_int4(p[0], p[1], p[2], p[3]);
+    }
+    std::vector<int4> ienb(std::max(C.Eb, 1));
+    std::vector<int> ibcb(std::max(C.Eb, 1), 0);
+    std::vector<double> bcb(18 * (size_t)std::max(C.Eb, 1), 0.0);
+    for (int i = 0; i < C.Eb; ++i) {
+        const int e = border[i];
+        const int* p = m->ienb + 4 * (size_t)e;
+        ienb[i] = make_int4(p[0], p[1], p[2], p[3]);
+        ibcb[i] = m->iBCB ? m->iBCB[2 * (size_t)e] : 0;
+        if (m->BCB)
+            for (int k = 0; k < 18; ++k) bcb[18 * (size_t)i + k] = m->BCB[18 * (size_t)e + k];
+    }
+    // node arrays
+    std::vector<double> x(3 * (size_t)N), bc(6 * (size_t)N);
+    std::vector<float> xf(3 * (size_t)N);
+    for (int n = 0; n < N; ++n) {
+        for (int d = 0; d < 3; ++d) {
+            x[3 * (size_t)n + d] = m->x[(size_t)d * N + n];
+            xf[3 * (size_t)n + d] = (float)x[3 * (size_t)n + d];
+        }
+        for (int k = 0; k < 6; ++k) bc[6 * (size_t)n + k] = m->BC[(size_t)k * N + n];
+    }
+    std::vector<int> bcn, slaves, mst, sstart, slv;
+    for (int n = 0; n < N; ++n) {
+        if (m->iBC[n] & 0x3F) bcn.push_back(n);
+        if (m->iper[n] != n) slaves.push_back(n);
+    }
+    {
+        std::vector<int> cnt(N, 0);
+        for (int s : slaves) cnt[m->iper[s]]++;
+        std::vector<int> pos(N, -1);
+        sstart.push_back(0);
+        for (int n = 0; n < N; ++n)
+            if (cnt[n] > 0) {
+                pos[n] = (int)mst.size();
+                mst.push_back(n);
+                sstart.push_back(sstart.back() + cnt[n]);
+            }
+        slv.assign(slaves.size(), 0);
+        std::vector<int> fillp(sstart.begin(), sstart.end() - 1);
+        for (int s : slaves) slv[fillp[pos[m->iper[s]]]++] = s;  // ascending slave order
+    }
+    C.nbcn = (int)bcn.size();
+    C.nslave = (int)slaves.size();
+    C.nmaster = (int)mst.size();
+    const size_t n5 = 5 * (size_t)N;
+    const int K = cfg->Kspace;
+    T(dalloc(C, &C.d_ien, C.E));
+    T(dalloc(C, &C.d_ienb, std::max(C.Eb, 1)));
+    T(dalloc(C, &C.d_iBCB, std::max(C.Eb, 1)));
+    T(dalloc(C, &C.d_BCB, 18 * (size_t)std::max(C.Eb, 1)));
+    T(dalloc(C, &C.d_x, 3 * (size_t)N));
+    T(dalloc(C, &C.d_xf, 3 * (size_t)N));
+    T(dalloc(C, &C.d_iBC, N));
+    T(dalloc(C, &C.d_BC, 6 * (size_t)N));
+    T(dalloc(C, &C.d_iper, N));
+    T(dalloc(C, &C.d_bcn, std::max(C.nbcn, 1)));
+    T(dalloc(C, &C.d_slaves, std::max(C.nslave, 1)));
+    T(dalloc(C, &C.d_mst, std::max(C.nmaster, 1)));
+    T(dalloc(C, &C.d_slv_start, C.nmaster + 1));
+    T(dalloc(C, &C.d_slv, std::max(C.nslave, 1)));
+    for (double** p : {&C.d_y, &C.d_ac, &C.d_yold, &C.d_acold, &C.d_res, &C.d_rmes, &C.d_Dy, &C.d_ypre, &C.d_t64, &C.d_t64b})
+        T(dalloc(C, p, n5));
+    T(dalloc(C, &C.d_bd, 25 * (size_t)N));
+    T(dalloc(C, &C.d_bdstage, 25 * (size_t)N));
+    for (float** p : {&C.d_yf, &C.d_acf, &C.d_resf, &C.d_rmesf, &C.d_t32, &C.d_t32b}) T(dalloc(C, p, n5));
+    T(dalloc(C, &C.d_bdf, 25 * (size_t)N));
+    {
+        const size_t vb = (cfg->precision == PHGPU_FP64) ? sizeof(double) : sizeof(float);
+        char* p = nullptr;
+        T(dalloc(C, &p, vb * n5 * (size_t)(K + 1)));
+        C.d_U = p;
+        C.Ucap = K;
+    }
+    T(dalloc(C, &C.d_scal, S_TOTAL));
+    T(dalloc(C, &C.d_part, kRedBlocks));
+    T(dalloc(C, &C.d_count, 1));
+    T(dalloc(C, &C.d_flag, 2));
+    if (rc == PHGPU_OK && cudaMallocHost((void**)&C.h_scal, sizeof(double) * 16) != cudaSuccess) rc = PHGPU_ERR_NOMEM;
+    if (rc == PHGPU_OK && cudaMallocHost((void**)&C.h_flag, sizeof(int) * 2) != cudaSuccess) rc = PHGPU_ERR_NOMEM;
+    if (rc != PHGPU_OK) {
+        phgpu_destroy(h);
+        return rc;
+    }
+    auto up = [&](void* d, const void* s, size_t bytes) {
+        T(check(C, cudaMemcpy(d, s, bytes, cudaMemcpyHostToDevice), "upload mesh"));
+    };
+    up(C.d_ien, ien.data(), sizeof(int4) * C.E);
+    up(C.d_ienb, ienb.data(), sizeof(int4) * ienb.size());
+    up(C.d_iBCB, ibcb.data(), sizeof(int) * ibcb.size());
+    up(C.d_BCB, bcb.data(), sizeof(double) * bcb.size());
+    up(C.d_x, x.data(), sizeof(double) * x.size());
+    up(C.d_xf, xf.data(), sizeof(float) * xf.size());
+    up(C.d_iBC, m->iBC, sizeof(int) * N);
+    up(C.d_BC, bc.data(), sizeof(double) * bc.size());
+    up(C.d_iper, m->iper, sizeof(int) * N);
+    if (C.nbcn) up(C.d_bcn, bcn.data(), sizeof(int) * C.nbcn);
+    if (C.nslave) up(C.d_slaves, slaves.data(), sizeof(int) * C.nslave);
+    if (C.nmaster) up(C.d_mst, mst.data(), sizeof(int) * C.nmaster);
+    up(C.d_slv_start, sstart.data(), sizeof(int) * sstart.size());
+    if (C.nslave) up(C.d_slv, slv.data(), sizeof(int) * C.nslave);
+    T(check(C, cudaDeviceSynchronize(), "upload mesh"));
+    T(check(C, cudaMemsetAsync(C.d_count, 0, sizeof(unsigned int), C.stream), "memset"));
+    T(check(C, cudaMemsetAsync(C.d_scal, 0, sizeof(double) * S_TOTAL, C.stream), "memset"));
+    for (double* p : {C.d_y, C.d_ac, C.d_yold, C.d_acold})
+        T(check(C, cudaMemsetAsync(p, 0, sizeof(double) * n5, C.stream), "memset"));
+    upload_tables(C);
+    T(sync(C));
+    if (rc != PHGPU_OK) {
+        phgpu_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return PHGPU_OK;
+}
+
+int phgpu_destroy(phgpu_ctx* h) {
+    if (!h) return PHGPU_OK;
+    Ctx& C = h->c;
+    if (C.stream) cudaStreamSynchronize(C.stream);
+    void* ptrs[] = {C.d_bdstage, C.d_ien, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
+                    C.d_slaves, C.d_mst, C.d_slv_start, C.d_slv, C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_res,
+                    C.d_rmes, C.d_Dy, C.d_ypre, C.d_t64, C.d_t64b, C.d_bd, C.d_yf, C.d_acf, C.d_resf, C.d_rmesf,
+                    C.d_t32, C.d_t32b, C.d_bdf, C.d_U, C.d_scal, C.d_part, C.d_count, C.d_flag};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (C.h_scal) cudaFreeHost(C.h_scal);
+    if (C.h_flag) cudaFreeHost(C.h_flag);
+    for (auto& e : C.ev)
+        if (e) cudaEventDestroy(e);
+    if (C.stream) cudaStreamDestroy(C.stream);
+    delete h;
+    return PHGPU_OK;
+}
+
+int phgpu_set_config(phgpu_ctx* h, const phgpu_config* cfg) {
+    if (!h || !cfg) return PHGPU_ERR_INVALID;
+    if (cfg->Kspace < 1 || cfg->Kspace > h->c.Ucap || cfg->nGMRES < 1) return PHGPU_ERR_INVALID;
+    if (cfg->itau != 0 || cfg->ipord != 1 || cfg->EntropyPressure != 0) return PHGPU_ERR_UNSUPPORTED;
+    const bool was64 = h->c.cfg.precision == PHGPU_FP64;
+    const bool is64 = cfg->precision == PHGPU_FP64;
+    if (was64 != is64 && !was64) return PHGPU_ERR_UNSUPPORTED;  // basis was allocated as FP32
+    h->c.cfg = *cfg;
+    return PHGPU_OK;
+}
+int phgpu_get_config(phgpu_ctx* h, phgpu_config* cfg) {
+    if (!h || !cfg) return PHGPU_ERR_INVALID;
+    *cfg = h->c.cfg;
+    return PHGPU_OK;
+}
+const char* phgpu_last_error(phgpu_ctx* h) { return h ? h->c.err.c_str() : "null context"; }
+void* phgpu_stream(phgpu_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
+int phgpu_num_colors(phgpu_ctx* h) { return h ? (int)h->c.col_start.size() - 1 : 0; }
+long long phgpu_kernel_launches(phgpu_ctx* h) { return h ? h->c.launches : 0; }
+
+int phgpu_elmmfg(phgpu_ctx* h, const double* y, const double* ac, double* res, double* rmes, double* bdiag,
+                 int iprec) {
+    using namespace phgpu;
+    if (!h || !y || !ac || !res || !rmes || (iprec && !bdiag)) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    ref_to_dev_state(C, y, C.d_t64, C.d_y);
+    ref_to_dev_state(C, ac, C.d_t64b, C.d_ac);
+    PH_TRY(elmmfg64(C, C.d_y, C.d_ac, C.d_res, C.d_rmes, C.d_bd, iprec));
+    dev_to_ref_res(C, C.d_res, C.d_t64, res);
+    dev_to_ref_res(C, C.d_rmes, C.d_t64b, rmes);
+    if (iprec) {
+        dev_to_ref_bd(C, C.d_bd, C.d_bdstage, bdiag);
+        return sync(C);
+    }
+    return sync(C);
+}
+
+int phgpu_elmres(phgpu_ctx* h, const double* y, const double* ac, double* res) {
+    using namespace phgpu;
+    if (!h || !y || !ac || !res) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    ref_to_dev_state(C, y, C.d_t64, C.d_y);
+    ref_to_dev_state(C, ac, C.d_t64b, C.d_ac);
+    PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
+    dev_to_ref_res(C, C.d_res, C.d_t64, res);
+    return sync(C);
+}
+
+int phgpu_itrres(phgpu_ctx* h, const double* yp, const double* yc, const double* ac, double* rmes) {
+    using namespace phgpu;
+    if (!h || !yp || !yc || !rmes) return PHGPU_ERR_INVALID;
+    (void)ac;  // the modified residual (ires = 2) does not read the acceleration
+    Ctx& C = h->c;
+    C.err.clear();
+    ref_to_dev_state(C, yp, C.d_t64, C.d_ypre);
+    ref_to_dev_state(C, yc, C.d_t64b, C.d_y);
+    ref_to_dev_res(C, rmes, C.d_t64, C.d_rmes);
+    PH_TRY(itrres_dev<double>(C, C.d_x, C.d_ypre, C.d_y, C.d_rmes, 0, nullptr));
+    dev_to_ref_res(C, C.d_rmes, C.d_t64b, rmes);
+    return sync(C);
+}
+
+int phgpu_i3lu(phgpu_ctx* h, double* bdiag, double* r, int code) {
+    using namespace phgpu;
+    if (!h || !bdiag || (code != PHGPU_LU_FACT && !r) || code < 0 || code > 3) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    double* tmp = C.d_bdstage;
+    ref_to_dev_bd(C, bdiag, tmp, C.d_bd);
+    int rc = PHGPU_OK;
+    if (code == PHGPU_LU_FACT) {
+        fill0(C, C.d_flag, sizeof(int) * 2);
+        lu_fact<double>(C, C.d_bd, C.d_flag);
+        dev_to_ref_bd(C, C.d_bd, tmp, bdiag);
+        cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream);
+        rc = sync(C);
+        if (rc == PHGPU_OK && C.h_flag[1]) rc = fail(C, PHGPU_ERR_SINGULAR, "zero pivot in i3LU");
+    } else {
+        ref_to_dev_res(C, r, C.d_t64, C.d_res);
+        lu_apply<double, double>(C, C.d_bd, C.d_res, code);
+        dev_to_ref_res(C, C.d_res, C.d_t64, r);
+        rc = sync(C);
+    }
+    return rc;
+}
+
+int phgpu_upload_state(phgpu_ctx* h, const double* y, const double* ac, const double* yold, const double* acold) {
+    using namespace phgpu;
+    if (!h) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    if (y) ref_to_dev_state(C, y, C.d_t64, C.d_y);
+    if (ac) ref_to_dev_state(C, ac, C.d_t64b, C.d_ac);
+    PH_TRY(sync(C));
+    if (yold) ref_to_dev_state(C, yold, C.d_t64, C.d_yold);
+    if (acold) ref_to_dev_state(C, acold, C.d_t64b, C.d_acold);
+    return sync(C);
+}
+
+int phgpu_download_state(phgpu_ctx* h, double* y, double* ac, double* yold, double* acold) {
+    using namespace phgpu;
+    if (!h) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    if (y) dev_to_ref_state(C, C.d_y, C.d_t64, y);
+    if (ac) dev_to_ref_state(C, C.d_ac, C.d_t64b, ac);
+    PH_TRY(sync(C));
+    if (yold) dev_to_ref_state(C, C.d_yold, C.d_t64, yold);
+    if (acold) dev_to_ref_state(C, C.d_acold, C.d_t64b, acold);
+    return sync(C);
+}
+
+int phgpu_solmfg(phgpu_ctx* h, const double* y, const double* ac, double* res, double* bdiag, double* Dy,
+                 phgpu_stats* st) {
+    using namespace phgpu;
+    if (!h || !y || !ac || !st) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    ref_to_dev_state(C, y, C.d_t64, C.d_y);
+    ref_to_dev_state(C, ac, C.d_t64b, C.d_ac);
+    PH_TRY(sync(C));
+    int ntot = st->ntotGM;
+    *st = phgpu_stats{};
+    st->ntotGM = ntot;
+    PH_TRY(solmfg_dev(C, st));
+    if (res) dev_to_ref_res(C, C.d_res, C.d_t64, res);
+    if (Dy) dev_to_ref_res(C, C.d_Dy, C.d_t64b, Dy);
+    PH_TRY(sync(C));
+    if (bdiag) {
+        dev_to_ref_bd(C, C.d_bd, C.d_bdstage, bdiag);
+        return sync(C);
+    }
+    return PHGPU_OK;
+}
+
+int phgpu_itrcorrect(phgpu_ctx* h, double* y, double* ac, const double* yold, const double* acold, const double* Dy) {
+    using namespace phgpu;
+    if (!h || !y || !ac || !yold || !acold || !Dy) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    ref_to_dev_state(C, y, C.d_t64, C.d_y);
+    ref_to_dev_state(C, ac, C.d_t64b, C.d_ac);
+    PH_TRY(sync(C));
+    ref_to_dev_state(C, yold, C.d_t64, C.d_yold);
+    ref_to_dev_state(C, acold, C.d_t64b, C.d_acold);
+    PH_TRY(sync(C));
+    ref_to_dev_res(C, Dy, C.d_t64, C.d_Dy);
+    PH_TRY(correct_dev(C));
+    dev_to_ref_state(C, C.d_y, C.d_t64, y);
+    dev_to_ref_state(C, C.d_ac, C.d_t64b, ac);
+    return sync(C);
+}
+
+int phgpu_newton_dev(phgpu_ctx* h, phgpu_stats* st) {
+    if (!h || !st) return PHGPU_ERR_INVALID;
+    h->c.err.clear();
+    int ntot = st->ntotGM;
+    *st = phgpu_stats{};
+    st->ntotGM = ntot;
+    int rc = phgpu::newton_dev(h->c, st);
+    st->status = rc;
+    return rc;
+}
+
+int phgpu_newton(phgpu_ctx* h, double* y, double* ac, const double* yold, const double* acold, phgpu_stats* st) {
+    if (!h || !y || !ac || !yold || !acold || !st) return PHGPU_ERR_INVALID;
+    int rc = phgpu_upload_state(h, y, ac, yold, acold);
+    if (rc != PHGPU_OK) return rc;
+    rc = phgpu_newton_dev(h, st);
+    if (rc != PHGPU_OK) return rc;
+    return phgpu_download_state(h, y, ac, nullptr, nullptr);
+}
+
+int phgpu_time_step_dev(phgpu_ctx* h, int nitr, phgpu_stats* st) {
+    if (!h || !st || nitr < 1) return PHGPU_ERR_INVALID;
+    h->c.err.clear();
+    int ntot = st->ntotGM;
+    *st = phgpu_stats{};
+    st->ntotGM = ntot;
+    int rc = phgpu::time_step_dev(h->c, nitr, st);
+    st->status = rc;
+    return rc;
+}
+
+int phgpu_time_step(phgpu_ctx* h, double* yold, double* acold, double* y, double* ac, int nitr, phgpu_stats* st) {
+    if (!h || !yold || !acold || !y || !ac || !st) return PHGPU_ERR_INVALID;
+    int rc = phgpu_upload_state(h, nullptr, nullptr, yold, acold);
+    if (rc != PHGPU_OK) return rc;
+    rc = phgpu_time_step_dev(h, nitr, st);
+    if (rc != PHGPU_OK) return rc;
+    return phgpu_download_state(h, y, ac, yold, acold);
+}
+
+int phgpu_residual_norm_dev(phgpu_ctx* h, double* rnorm) {
+    using namespace phgpu;
+    if (!h || !rnorm) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
+    dot<double>(C, C.d_res, C.d_res, 5 * (size_t)C.N, S_TMP2, nullptr);
+    PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, C.d_scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "rnorm"));
+    PH_TRY(sync(C));
+    *rnorm = std::sqrt(C.h_scal[S_TMP2]);
+    return PHGPU_OK;
+}
+
+int phgpu_sweep_dev(phgpu_ctx* h, int which) {
+    using namespace phgpu;
+    if (!h) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    const size_t n5 = 5 * (size_t)C.N;
+    switch (which) {
+        case 0:  // FP64 residual
+            launch_elem_res<double>(C, RM_RES, C.d_x, C.d_y, nullptr, C.d_ac, C.d_res, 0, nullptr);
+            break;
+        case 1:  // FP64 modified residual
+            launch_elem_res<double>(C, RM_MODRES, C.d_x, C.d_y, C.d_y, nullptr, C.d_rmes, 0, nullptr);
+            break;
+        case 2:  // FP32 linearized product in direction y
+            launch_elem_res<float>(C, RM_LIN, C.d_xf, C.d_yf, C.d_yf, nullptr, C.d_t32, 0, nullptr);
+            break;
+        case 3:  // FP32 block diagonal
+            launch_elem_full<float>(C, C.d_xf, C.d_yf, C.d_acf, nullptr, nullptr, C.d_bdf);
+            break;
+        case 4:  // FP64 block diagonal + residuals
+            launch_elem_full<double>(C, C.d_x, C.d_y, C.d_ac, C.d_res, C.d_rmes, C.d_bd);
+            break;
+        case 5:
+            to_f32(C, C.d_y, C.d_yf, n5);
+            to_f32(C, C.d_ac, C.d_acf, n5);
+            break;
+        default:
+            return PHGPU_ERR_INVALID;
+    }
+    return check(C, cudaGetLastError(), "sweep");
+}
+
+}  // extern "C"

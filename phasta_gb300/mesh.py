@@ -1,0 +1,255 @@
+"""Synthetic meshes, boundary conditions and states of the benchmark cases.
+
+The reference reads partitioned meshes written by its preprocessor; the
+benchmark cases here are generated in process with the same data model
+(``x(nshg,3)``, tet connectivity, boundary tets with the boundary face first,
+``iBC``/``BC``/``iper`` and ``iBCB``/``BCB``):
+
+* a box of n^3 hexahedra, each split into 6 tets along its main diagonal
+  (Kuhn/Freudenthal split; conforming across hexes and across periodic
+  faces), nodes (n+1)^3 with the periodic slaves stored as in the reference;
+* periodic directions identify the last node layer with the first
+  (``iper`` points at the ultimate master, ``iBC`` bit 10 marks slaves);
+* an inflow face at x = x0 with Dirichlet velocity and temperature
+  (iBC bits 1, 3, 4, 5) and natural (flux-computed) boundary faces at x = x0
+  and x = x1 (``iBCB`` = 0);
+* states: uniform flow along x at a Mach number plus seeded Gaussian noise,
+  or the decaying-vortex field of the 42.5M-tet case.
+
+Tet node order follows the reference's convention: det(dx/dxi) > 0 with
+N1..N3 = barycentric coordinates 1..3 and N4 = 1 - N1 - N2 - N3, so the
+right-handed normal of face (1,2,3) points out of the element (e3bvar.f:161-171).
+"""
+from __future__ import annotations
+
+import itertools
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# gas properties of the reference (common.f:101-108, input.f:164-182)
+RH = 8.31441
+MSH = (2.8e-2, 3.2e-2)
+XN2, XO2 = 0.79, 0.21
+GAMMA, GAMMA1 = 1.4, 0.4
+
+
+def rgas() -> float:
+    rs1, rs2 = RH / MSH[0], RH / MSH[1]
+    return 1.0 / (XN2 / rs1 + XO2 / rs2)
+
+
+@dataclass
+class Case:
+    """A mesh with its boundary conditions (0-based, reference layouts)."""
+    nshg: int
+    x: np.ndarray            # (nshg, 3) float64, stored column-major as x(nshg,3) -> x.T contiguous
+    ien: np.ndarray          # (nelem, 4) int32
+    ienb: np.ndarray         # (nbelem, 4) int32, boundary face first
+    iBCB: np.ndarray         # (nbelem, 2) int32
+    BCB: np.ndarray          # (nbelem, 3, 6) float64
+    iBC: np.ndarray          # (nshg,) int32
+    BC: np.ndarray           # (6, nshg) float64  == BC(nshg,6) column-major
+    iper: np.ndarray         # (nshg,) int32
+    h: float                 # smallest edge
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def nelem(self) -> int:
+        return int(self.ien.shape[0])
+
+    @property
+    def nbelem(self) -> int:
+        return int(self.ienb.shape[0])
+
+    def x_ref(self) -> np.ndarray:
+        """x(nshg,3) in the reference's column-major layout, as a flat array."""
+        return np.ascontiguousarray(self.x.T).reshape(-1)
+
+
+def _kuhn_tets(n: tuple[int, int, int]) -> np.ndarray:
+    nx, ny, nz = n
+    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    ii, jj, kk = (a.reshape(-1) for a in (ii, jj, kk))
+
+    def nid(i, j, k):
+        return i + (nx + 1) * (j + (ny + 1) * k)
+
+    tets = []
+    for perm in itertools.permutations(range(3)):
+        off = np.zeros(3, dtype=np.int64)
+        verts = [nid(ii, jj, kk)]
+        for ax in perm:
+            off[ax] += 1
+            verts.append(nid(ii + off[0], jj + off[1], kk + off[2]))
+        tets.append(np.stack(verts, axis=1))
+    # interleave so the 6 tets of one hex are consecutive (spatial locality)
+    return np.stack(tets, axis=1).reshape(-1, 4)
+
+
+def _orient(ien: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """Reorder each tet so that det[x1-x4, x2-x4, x3-x4] > 0."""
+    a, b, c, d = (x[ien[:, k]] for k in range(4))
+    det = np.einsum("ij,ij->i", a - d, np.cross(b - d, c - d))
+    out = ien.copy()
+    neg = det < 0
+    out[neg, 0], out[neg, 1] = ien[neg, 1], ien[neg, 0]
+    return out
+
+
+def box(n: int | tuple[int, int, int], lengths=(1.0, 1.0, 1.0), periodic=(False, True, True),
+        inflow=None, boundary_faces=True) -> Case:
+    """n^3 hexes x 6 tets on [0,Lx]x[0,Ly]x[0,Lz].
+
+    ``inflow``: dict(T=..., u=(u,v,w)) for a Dirichlet inflow at x = 0, or None.
+    Non-periodic x faces get boundary tets with natural (computed) fluxes.
+    """
+    if isinstance(n, int):
+        n = (n, n, n)
+    nx, ny, nz = n
+    npts = (nx + 1, ny + 1, nz + 1)
+    nshg = npts[0] * npts[1] * npts[2]
+    gx = [np.linspace(0.0, lengths[d], npts[d]) for d in range(3)]
+    X, Y, Z = np.meshgrid(*gx, indexing="ij")
+    # node id = i + (nx+1)*(j + (ny+1)*k): store in that order
+    x = np.stack([X.transpose(2, 1, 0).reshape(-1), Y.transpose(2, 1, 0).reshape(-1),
+                  Z.transpose(2, 1, 0).reshape(-1)], axis=1).astype(np.float64)
+    ien = _orient(_kuhn_tets(n), x).astype(np.int32)
+
+    idx = np.arange(nshg)
+    i = idx % npts[0]
+    j = (idx // npts[0]) % npts[1]
+    k = idx // (npts[0] * npts[1])
+    mi, mj, mk = i.copy(), j.copy(), k.copy()
+    if periodic[0]:
+        mi[i == nx] = 0
+    if periodic[1]:
+        mj[j == ny] = 0
+    if periodic[2]:
+        mk[k == nz] = 0
+    iper = (mi + npts[0] * (mj + npts[1] * mk)).astype(np.int32)
+    iBC = np.zeros(nshg, dtype=np.int32)
+    iBC[iper != idx] |= 1 << 10
+    BC = np.zeros((6, nshg), dtype=np.float64)
+    if inflow is not None and not periodic[0]:
+        m = i == 0
+        iBC[m] |= (1 << 1) | (7 << 3)
+        BC[1, m] = inflow["T"]
+        BC[2, m], BC[3, m], BC[4, m] = inflow["u"]
+
+    ienb = np.zeros((0, 4), dtype=np.int32)
+    if boundary_faces and not periodic[0]:
+        xs = x[:, 0]
+        blist = []
+        for plane in (0.0, lengths[0]):
+            on = np.isclose(xs[ien], plane)
+            sel = np.where(on.sum(axis=1) == 3)[0]
+            for e in sel:
+                face = [ien[e, a] for a in range(4) if on[e, a]]
+                inner = [ien[e, a] for a in range(4) if not on[e, a]]
+                blist.append(face + inner)
+        if blist:
+            ienb = _orient(np.array(blist, dtype=np.int64), x)
+            # orientation swaps nodes 0/1 only, so the face stays first
+            ienb = ienb.astype(np.int32)
+    nb = ienb.shape[0]
+    h = min(lengths[d] / n[d] for d in range(3))
+    return Case(nshg=nshg, x=x, ien=ien, ienb=ienb, iBCB=np.zeros((nb, 2), np.int32),
+                BCB=np.zeros((nb, 3, 6), np.float64), iBC=iBC, BC=BC, iper=iper, h=h,
+                meta={"n": n, "lengths": lengths, "periodic": periodic})
+
+
+# ---------------------------------------------------------------------------
+# seeded states (counter-based: the value of (node, dof) does not depend on
+# the mesh size or traversal order)
+# ---------------------------------------------------------------------------
+def _noise(seed: int, nshg: int, ndof: int = 5) -> np.ndarray:
+    """Standard normals from a Philox counter generator keyed by seed; row k = dof k."""
+    g = np.random.Generator(np.random.Philox(key=seed))
+    return g.standard_normal((ndof, nshg))
+
+
+def freestream(mach: float, u: float = 1.0, rho: float = 1.0) -> dict:
+    R = rgas()
+    c = u / mach
+    T = c * c / (GAMMA * R)
+    p = rho * R * T
+    return {"u": u, "T": T, "p": p, "c": c, "rho": rho}
+
+
+def uniform_state(case: Case, mach: float, sigma: float = 0.01, seed: int = 20261203) -> np.ndarray:
+    """y(nshg,5) in the reference order (u,v,w,p,T), column-major flat (5*nshg)."""
+    fs = freestream(mach)
+    y = np.empty((5, case.nshg))
+    y[0], y[1], y[2], y[3], y[4] = fs["u"], 0.0, 0.0, fs["p"], fs["T"]
+    if sigma > 0:
+        z = _noise(seed, case.nshg)
+        scale = np.array([fs["u"], fs["u"], fs["u"], fs["p"], fs["T"]])[:, None]
+        y += sigma * scale * z
+    return apply_bc_state(case, y.reshape(-1))
+
+
+def vortex_state(case: Case, mach: float = 0.1, noise: float = 1e-3, seed: int = 20261203) -> np.ndarray:
+    """u = U0 sin x cos y cos z, v = -U0 cos x sin y cos z, w = 0, uniform p and T, + noise."""
+    fs = freestream(mach)
+    X, Yc, Z = case.x[:, 0], case.x[:, 1], case.x[:, 2]
+    y = np.empty((5, case.nshg))
+    y[0] = np.sin(X) * np.cos(Yc) * np.cos(Z)
+    y[1] = -np.cos(X) * np.sin(Yc) * np.cos(Z)
+    y[2] = 0.0
+    y[3], y[4] = fs["p"], fs["T"]
+    if noise > 0:
+        z = _noise(seed, case.nshg)
+        scale = np.array([1.0, 1.0, 1.0, fs["p"], fs["T"]])[:, None]
+        y += noise * scale * z
+    return apply_bc_state(case, y.reshape(-1))
+
+
+def apply_bc_state(case: Case, y: np.ndarray) -> np.ndarray:
+    """itrBC for Dirichlet T/velocity and the periodic master->slave copy (itrbc.f:54-176)."""
+    y = y.reshape(5, case.nshg).copy()
+    ib = case.iBC
+    t = (ib >> 1) & 1 == 1
+    y[4, t] = case.BC[1, t]
+    v7 = ((ib >> 3) & 7) == 7
+    y[0, v7], y[1, v7], y[2, v7] = case.BC[2, v7], case.BC[3, v7], case.BC[4, v7]
+    y = y[:, case.iper]
+    return np.ascontiguousarray(y).reshape(-1)
+
+
+def time_params(rho_inf: float, dt: float) -> dict:
+    """Generalized-alpha parameters of itrSetup (itrPC.f:16-24, 42)."""
+    if rho_inf < 0 or rho_inf > 1:
+        almi = alfi = gami = 1.0
+    else:
+        almi = (3.0 - rho_inf) / (1.0 + rho_inf) / 2.0
+        alfi = 1.0 / (1.0 + rho_inf)
+        gami = 0.5 + almi - alfi
+    return {"Dtgl": 1.0 / dt, "almi": almi, "alfi": alfi, "gami": gami}
+
+
+def cfl_dt(case: Case, mach: float, cfl: float = 1.0, umax: float = 1.0) -> float:
+    fs = freestream(mach, u=umax)
+    return cfl * case.h / (umax + fs["c"])
+
+
+# ---------------------------------------------------------------------------
+# benchmark cases (sizes of the reference's benchmark definitions)
+# ---------------------------------------------------------------------------
+def channel_case(n: int, mach: float = 0.3, re: float = 1000.0):
+    """Unit cube, periodic y/z, Dirichlet inflow at x=0, natural outflow at x=1."""
+    fs = freestream(mach)
+    case = box(n, periodic=(False, True, True), inflow={"T": fs["T"], "u": (fs["u"], 0.0, 0.0)})
+    mu = fs["rho"] * fs["u"] * 1.0 / re
+    dt = cfl_dt(case, mach)
+    return case, {"mach": mach, "re": re, "mu": mu, "dt": dt, "fs": fs}
+
+
+def periodic_vortex_case(n: int, mach: float = 0.1, re: float = 1600.0):
+    L = 2.0 * math.pi
+    case = box(n, lengths=(L, L, L), periodic=(True, True, True), inflow=None)
+    fs = freestream(mach)
+    mu = fs["rho"] * 1.0 * 1.0 / re
+    dt = cfl_dt(case, mach)
+    return case, {"mach": mach, "re": re, "mu": mu, "dt": dt, "fs": fs}

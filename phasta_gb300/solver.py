@@ -1,0 +1,229 @@
+"""Host-side mirror of PHASTA's compressible hot-path routines on the GPU.
+
+``GpuSolver`` owns one GPU context (``phgpu_ctx``) created from a mesh and the
+COMMON-block parameters; its methods carry the reference routine names and
+argument meaning (arrays in the reference layout, see include/phgpu.h):
+
+    ElmMFG(y, ac)                -> res, rmes, BDiag          elmmfg.f:1
+    ElmRes(y, ac)                -> res                       (ElmMFG with ires = 1)
+    ItrRes(yp, yc, ac, rmes)     -> rmes (accumulated)        itrres.f:1
+    i3LU(BDiag, r, code)                                      i3lu.f:1
+    SolMFG(y, ac)                -> res, BDiag, Dy, stats     solmfg.f:1
+    itrCorrect(y, ac, yold, acold, Dy)                        itrPC.f:128 + itrbc.f
+    newton(y, ac, yold, acold)   one flow solve of itrdrv      itrdrv.f:489-598
+    time_step(yold, acold, nitr) itrPredict + nitr solves + itrUpdate
+
+Every call runs on the GPU; a non-zero status from the library raises
+``PhgpuError`` (the reference would stop in error()/tnanq).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from .mesh import GAMMA, GAMMA1, Case, rgas, time_params
+
+
+class PhgpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"phgpu status {code} ({L.STATUS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+def make_params(mu: float, dt: float, rho_inf: float = 0.5, Kspace: int = 10, etol: float = 1e-3,
+                minIters: int = 1, nGMRES: int = 1, pr: float = 0.72, precision: int = L.PHGPU_FP64,
+                ap_mode: int = L.PHGPU_AP_FD, navier: int = 1, ivart: int = 2) -> dict:
+    """The COMMON-block values of the hot path (input.config defaults otherwise)."""
+    p = {"Rgas": rgas(), "gamma": GAMMA, "gamma1": GAMMA1, "pr": pr, "rmu": mu,
+         "dtsfct": 1.0, "taucfct": 1.0, "temper": 1.0, "itau": 0, "ivart": ivart,
+         "iremoveStabTimeTerm": 0, "Navier": navier, "ipord": 1, "EntropyPressure": 0,
+         "Kspace": Kspace, "nGMRES": nGMRES, "minIters": minIters, "etol": etol,
+         "epsM": float(np.sqrt(np.finfo(np.float64).eps)), "eGMRES": 0.0, "iter": 1, "istep": 0,
+         "precision": precision, "ap_mode": ap_mode}
+    p.update(time_params(rho_inf, dt))
+    return p
+
+
+def _config(p: dict) -> L.Config:
+    c = L.Config()
+    for name, _ in L.Config._fields_:
+        if name in p:
+            setattr(c, name, p[name])
+    return c
+
+
+@dataclass
+class SolveStats:
+    iKs: int
+    lGMRES: int
+    ntotGM: int
+    unorm0: float
+    echeck: float
+    eGMRES: float
+    totres: float
+    rnorm: float
+    t_assembly_ms: float
+    t_gmres_ms: float
+
+
+def _stats(s: L.Stats) -> SolveStats:
+    return SolveStats(s.iKs, s.lGMRES, s.ntotGM, s.unorm0, s.echeck, s.eGMRES, s.totres, s.rnorm,
+                      s.t_assembly_ms, s.t_gmres_ms)
+
+
+class GpuSolver:
+    def __init__(self, case: Case, params: dict):
+        self.lib = L.lib()
+        self.case = case
+        self.params = dict(params)
+        self.nshg = case.nshg
+        # keep the host arrays alive for the duration of create
+        self._x = case.x_ref()
+        self._ien = np.ascontiguousarray(case.ien, dtype=np.int32).reshape(-1)
+        self._ienb = np.ascontiguousarray(case.ienb, dtype=np.int32).reshape(-1)
+        self._iBCB = np.ascontiguousarray(case.iBCB, dtype=np.int32).reshape(-1)
+        self._BCB = np.ascontiguousarray(case.BCB, dtype=np.float64).reshape(-1)
+        self._iBC = np.ascontiguousarray(case.iBC, dtype=np.int32)
+        self._BC = np.ascontiguousarray(case.BC, dtype=np.float64).reshape(-1)
+        self._iper = np.ascontiguousarray(case.iper, dtype=np.int32)
+        m = L.Mesh(self.nshg, case.nelem, L.iptr(self._ien), L.dptr(self._x), case.nbelem,
+                   L.iptr(self._ienb) if case.nbelem else None, L.iptr(self._iBCB) if case.nbelem else None,
+                   L.dptr(self._BCB) if case.nbelem else None, L.iptr(self._iBC), L.dptr(self._BC),
+                   L.iptr(self._iper))
+        self._cfg = _config(self.params)
+        h = C.c_void_p()
+        rc = self.lib.phgpu_create(C.byref(m), C.byref(self._cfg), C.byref(h))
+        if rc != 0:
+            raise PhgpuError(rc, "phgpu_create failed")
+        self.h = h
+        self.ntotGM = 0
+
+    # -- helpers --
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.phgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise PhgpuError(rc, self.lib.phgpu_last_error(self.h).decode())
+
+    def set_params(self, **kw):
+        self.params.update(kw)
+        self._cfg = _config(self.params)
+        self._check(self.lib.phgpu_set_config(self.h, C.byref(self._cfg)))
+
+    def get_params(self) -> dict:
+        c = L.Config()
+        self._check(self.lib.phgpu_get_config(self.h, C.byref(c)))
+        return {name: getattr(c, name) for name, _ in L.Config._fields_ if name != "reserved"}
+
+    def _v(self, k: int = 5) -> np.ndarray:
+        return np.zeros(k * self.nshg, dtype=np.float64)
+
+    @property
+    def num_colors(self) -> int:
+        return self.lib.phgpu_num_colors(self.h)
+
+    @property
+    def kernel_launches(self) -> int:
+        return self.lib.phgpu_kernel_launches(self.h)
+
+    def stream(self) -> int:
+        return self.lib.phgpu_stream(self.h)
+
+    # -- reference routines --
+    def ElmMFG(self, y, ac, iprec: int = 1):
+        res, rmes = self._v(), self._v()
+        bd = self._v(25) if iprec else None
+        self._check(self.lib.phgpu_elmmfg(self.h, L.dptr(y), L.dptr(ac), L.dptr(res), L.dptr(rmes),
+                                          L.dptr(bd), iprec))
+        return res, rmes, bd
+
+    def ElmRes(self, y, ac):
+        res = self._v()
+        self._check(self.lib.phgpu_elmres(self.h, L.dptr(y), L.dptr(ac), L.dptr(res)))
+        return res
+
+    def ItrRes(self, yp, yc, ac, rmes=None):
+        rmes = self._v() if rmes is None else np.array(rmes, dtype=np.float64)
+        self._check(self.lib.phgpu_itrres(self.h, L.dptr(yp), L.dptr(yc), L.dptr(ac), L.dptr(rmes)))
+        return rmes
+
+    def i3LU(self, bdiag, r, code):
+        bdiag = np.array(bdiag, dtype=np.float64)
+        r = None if r is None else np.array(r, dtype=np.float64)
+        self._check(self.lib.phgpu_i3lu(self.h, L.dptr(bdiag), L.dptr(r), code))
+        return bdiag, r
+
+    def SolMFG(self, y, ac):
+        res, bd, Dy = self._v(), self._v(25), self._v()
+        st = L.Stats()
+        st.ntotGM = self.ntotGM
+        self._check(self.lib.phgpu_solmfg(self.h, L.dptr(y), L.dptr(ac), L.dptr(res), L.dptr(bd), L.dptr(Dy),
+                                          C.byref(st)))
+        self.ntotGM = st.ntotGM
+        return res, bd, Dy, _stats(st)
+
+    def itrCorrect(self, y, ac, yold, acold, Dy):
+        y, ac = np.array(y, dtype=np.float64), np.array(ac, dtype=np.float64)
+        self._check(self.lib.phgpu_itrcorrect(self.h, L.dptr(y), L.dptr(ac), L.dptr(yold), L.dptr(acold), L.dptr(Dy)))
+        return y, ac
+
+    def newton(self, y, ac, yold, acold):
+        y, ac = np.array(y, dtype=np.float64), np.array(ac, dtype=np.float64)
+        st = L.Stats()
+        st.ntotGM = self.ntotGM
+        self._check(self.lib.phgpu_newton(self.h, L.dptr(y), L.dptr(ac), L.dptr(yold), L.dptr(acold), C.byref(st)))
+        self.ntotGM = st.ntotGM
+        return y, ac, _stats(st)
+
+    def time_step(self, yold, acold, nitr: int):
+        yold, acold = np.array(yold, dtype=np.float64), np.array(acold, dtype=np.float64)
+        y, ac = self._v(), self._v()
+        st = L.Stats()
+        st.ntotGM = self.ntotGM
+        self._check(self.lib.phgpu_time_step(self.h, L.dptr(yold), L.dptr(acold), L.dptr(y), L.dptr(ac), nitr,
+                                             C.byref(st)))
+        self.ntotGM = st.ntotGM
+        return yold, acold, y, ac, _stats(st)
+
+    # -- device-resident path (benchmarks) --
+    def upload(self, y=None, ac=None, yold=None, acold=None):
+        self._check(self.lib.phgpu_upload_state(self.h, L.dptr(y), L.dptr(ac), L.dptr(yold), L.dptr(acold)))
+
+    def download(self):
+        y, ac, yo, ao = self._v(), self._v(), self._v(), self._v()
+        self._check(self.lib.phgpu_download_state(self.h, L.dptr(y), L.dptr(ac), L.dptr(yo), L.dptr(ao)))
+        return y, ac, yo, ao
+
+    def newton_dev(self) -> SolveStats:
+        st = L.Stats()
+        st.ntotGM = self.ntotGM
+        self._check(self.lib.phgpu_newton_dev(self.h, C.byref(st)))
+        self.ntotGM = st.ntotGM
+        return _stats(st)
+
+    def time_step_dev(self, nitr: int) -> SolveStats:
+        st = L.Stats()
+        st.ntotGM = self.ntotGM
+        self._check(self.lib.phgpu_time_step_dev(self.h, nitr, C.byref(st)))
+        self.ntotGM = st.ntotGM
+        return _stats(st)
+
+    def residual_norm_dev(self) -> float:
+        r = C.c_double()
+        self._check(self.lib.phgpu_residual_norm_dev(self.h, C.byref(r)))
+        return r.value
+
+    def sweep_dev(self, which: int):
+        self._check(self.lib.phgpu_sweep_dev(self.h, which))

@@ -1,0 +1,65 @@
+"""Generate tests/golden/tet_tables.json from the reference's own C sources.
+
+Runs in a container that holds the reference tree: oracle/build_oracle.py
+compiles symtet.c, symtri.c and shapeFunction/src/*.c of the reference in
+place into oracle/_ref/libphref_shape.so; this script calls
+symtet/symtri (the quadrature rules genint.f uses) and TetShapeAndDrv (the
+shape functions genshp.f/genshpb.f tabulate), applies genint.f:72-73 and
+genshp.f:32-35, and writes the tables the element routines read.
+
+    python tests/golden/make_tables.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle.build_oracle import build_reference_shape  # noqa: E402
+
+
+def main():
+    so = build_reference_shape()
+    if so is None:
+        raise SystemExit("reference sources not found")
+    L = C.CDLL(str(so))
+    D = C.c_double
+    out = {}
+    # interior: 4-point tet rule
+    n, err = C.c_int(4), C.c_int(0)
+    pt, wt = (D * 16)(), (D * 4)()
+    L.symtet_(C.byref(n), pt, wt, C.byref(err))
+    shp, shgl, qwt = [], [], []
+    for q in range(4):
+        par = (D * 3)(pt[4 * q], pt[4 * q + 1], pt[4 * q + 2])
+        N, dN = (D * 4)(), (D * 12)()
+        L.TetShapeAndDrv(1, par, N, dN)
+        shp.append([N[a] for a in range(4)])
+        shgl.append([[dN[3 * a + i] / 2.0 for a in range(4)] for i in range(3)])
+        qwt.append((4.0 / 3.0) * wt[q])
+    out["shp"], out["shgl"], out["Qwt"] = shp, shgl, qwt
+    # boundary: 3-point triangle rule on the tet face
+    n = C.c_int(3)
+    pt, wt = (D * 12)(), (D * 3)()
+    L.symtri_(C.byref(n), pt, wt, C.byref(err))
+    shpb, shglb, qwtb = [], [], []
+    for q in range(3):
+        par = (D * 3)(pt[4 * q], pt[4 * q + 1], pt[4 * q + 2])
+        N, dN = (D * 4)(), (D * 12)()
+        L.TetShapeAndDrv(1, par, N, dN)
+        shpb.append([N[a] for a in range(4)])
+        shglb.append([[dN[3 * a + i] / 2.0 for a in range(4)] for i in range(3)])
+        qwtb.append(2.0 * wt[q])
+    out["shpb"], out["shglb"], out["Qwtb"] = shpb, shglb, qwtb
+    out["source"] = "reference symtet.c, symtri.c, shapeFunction/src (TetShapeAndDrv), genint.f:72-73, genshp.f:32-35"
+    p = Path(__file__).resolve().parent / "tet_tables.json"
+    p.write_text(json.dumps(out, indent=1))
+    print(p)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,191 @@
+"""GPU parity: the sm_103a kernels (through the C ABI) against the CPU oracle.
+
+Tolerances (relative, in the 2-norm over the whole array):
+  * FP64 residual, modified residual, BDiag: 1e-10
+  * FP64 i3LU factors and solves:            1e-12
+  * FP32 block diagonal (mixed mode):        1e-5
+  * finite-difference GMRES (FP64): the same Krylov iteration count, Dy within 1e-6
+    (Au1MFG amplifies rounding by 1/eGMRES, so bitwise-different sums move Dy at ~1e-9)
+  * mixed-precision Newton step: the nonlinear residual after the step within
+    the Krylov tolerance of the FP64 step's
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import channel, rel, vortex
+from oracle import pyoracle
+from phasta_gb300 import _lib as L
+from phasta_gb300 import mesh
+from phasta_gb300.solver import GpuSolver, PhgpuError
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def c8(gpu_lib):
+    case, p, y, ac = channel(8, ac_scale=0.05)
+    return case, p, y, ac, GpuSolver(case, p), pyoracle.Oracle(case, p)
+
+
+@pytest.fixture(scope="module")
+def c16(gpu_lib):
+    case, p, y, ac = channel(16, ac_scale=0.05)
+    return case, p, y, ac, GpuSolver(case, p), pyoracle.Oracle(case, p, nthreads=4)
+
+
+@pytest.mark.parametrize("which", ["c8", "c16"])
+def test_elmmfg_fp64(which, request):
+    case, p, y, ac, g, o = request.getfixturevalue(which)
+    rg, mg, bg = g.ElmMFG(y, ac)
+    ro, mo, bo = o.ElmMFG(y, ac)
+    assert rel(rg, ro) < 1e-10
+    assert rel(mg, mo) < 1e-10
+    assert rel(bg, bo) < 1e-10
+
+
+def test_elmres_and_elmmfg_without_preconditioner(c8):
+    case, p, y, ac, g, o = c8
+    assert rel(g.ElmRes(y, ac), o.ElmRes(y, ac)) < 1e-10
+    rg, mg, _ = g.ElmMFG(y, ac, iprec=0)
+    ro, mo, _ = o.ElmMFG(y, ac, iprec=0)
+    assert rel(rg, ro) < 1e-10 and rel(mg, mo) < 1e-10
+
+
+def test_itrres_perturbed_state(c8):
+    case, p, y, ac, g, o = c8
+    rng = np.random.default_rng(11)
+    yp = y * (1.0 + 1e-3 * rng.standard_normal(y.shape))
+    r0 = rng.standard_normal(y.shape)
+    assert rel(g.ItrRes(yp, y, ac, r0), o.ItrRes(yp, y, ac, r0)) < 1e-10
+
+
+def test_i3lu_all_codes(c8):
+    case, p, y, ac, g, o = c8
+    _, _, bd = o.ElmMFG(y, ac)
+    lug, _ = g.i3LU(bd, None, L.LU_FACT)
+    luo, _ = o.i3LU(bd, None, 0)
+    assert rel(lug, luo) < 1e-12
+    r = np.random.default_rng(3).standard_normal(5 * case.nshg)
+    for code in (L.LU_FORWARD, L.LU_BACKWARD, L.LU_PRODUCT):
+        _, a = g.i3LU(luo, r, code)
+        _, b = o.i3LU(luo, r.copy(), code)
+        assert rel(a, b) < 1e-12, code
+
+
+def test_i3lu_singular_block_reports_status(c8):
+    case, p, y, ac, g, o = c8
+    bd = np.zeros(25 * case.nshg)
+    with pytest.raises(PhgpuError) as e:
+        g.i3LU(bd, None, L.LU_FACT)
+    assert e.value.code == 4  # PHGPU_ERR_SINGULAR
+    # the context stays usable
+    assert rel(g.ElmRes(y, ac), o.ElmRes(y, ac)) < 1e-10
+
+
+def test_periodic_vortex_residual(gpu_lib):
+    case, p, y, ac = vortex(8)
+    g, o = GpuSolver(case, p), pyoracle.Oracle(case, p)
+    rg, mg, bg = g.ElmMFG(y, ac)
+    ro, mo, bo = o.ElmMFG(y, ac)
+    assert rel(rg, ro) < 1e-10 and rel(mg, mo) < 1e-10 and rel(bg, bo) < 1e-10
+
+
+def test_solmfg_fd_matches_oracle(c8):
+    case, p, y, ac, g, o = c8
+    rg, bg, Dg, sg = g.SolMFG(y, ac)
+    ro, bo, Do, so = o.SolMFG(y, ac)
+    assert rel(rg, ro) < 1e-10
+    assert rel(bg, bo) < 1e-10
+    assert abs(sg.eGMRES - so.eGMRES) <= 1e-6 * so.eGMRES
+    assert sg.iKs == so.iKs
+    assert rel(Dg, Do) < 1e-6
+    assert sg.echeck <= p["etol"] * sg.unorm0
+
+
+def test_newton_step_fp64_matches_oracle(c16):
+    case, p, y, ac, g, o = c16
+    yg, acg, sg = g.newton(y, ac, y, ac)
+    yo, aco, so, _ = o.newton(y, ac, y, ac)
+    assert rel(yg, yo) < 1e-9
+    assert rel(acg, aco) < 1e-6
+    r0 = np.linalg.norm(o.ElmRes(y, ac))
+    assert np.linalg.norm(o.ElmRes(yg, acg)) < 0.05 * r0
+
+
+def test_linearized_product_agrees_with_finite_difference(gpu_lib):
+    """The linearized Jacobian-vector product is the eps -> 0 limit of Au1MFG."""
+    case, p, y, ac = channel(8)
+    p_lin = dict(p, ap_mode=L.PHGPU_AP_LINEAR)
+    g_fd, g_lin = GpuSolver(case, p), GpuSolver(case, p_lin)
+    _, _, Dfd, sfd = g_fd.SolMFG(y, ac)
+    _, _, Dlin, slin = g_lin.SolMFG(y, ac)
+    assert abs(sfd.iKs - slin.iKs) <= 1
+    # both solve J Dy = R to the Krylov tolerance; they differ by O(eGMRES) and the tolerance
+    assert rel(Dlin, Dfd) < 5 * p["etol"]
+
+
+def test_mixed_precision_newton_step(gpu_lib):
+    case, p, y, ac = channel(16)
+    p64 = dict(p, ap_mode=L.PHGPU_AP_LINEAR)
+    pmx = dict(p, ap_mode=L.PHGPU_AP_LINEAR, precision=L.PHGPU_MIXED)
+    o = pyoracle.Oracle(case, p, nthreads=4)
+    g64, gmx = GpuSolver(case, p64), GpuSolver(case, pmx)
+    r0 = np.linalg.norm(o.ElmRes(y, ac))
+    y64, a64, s64 = g64.newton(y, ac, y, ac)
+    ymx, amx, smx = gmx.newton(y, ac, y, ac)
+    r64 = np.linalg.norm(o.ElmRes(y64, a64))
+    rmx = np.linalg.norm(o.ElmRes(ymx, amx))
+    assert abs(smx.iKs - s64.iKs) <= 2
+    # the correction agrees to the Krylov tolerance, so do the new residuals
+    assert rel(ymx - y, y64 - y) < 10 * p["etol"]
+    assert rmx < r64 + 10 * p["etol"] * r0
+    assert s64.rnorm == pytest.approx(r0, rel=1e-10)
+    assert smx.rnorm == pytest.approx(r0, rel=1e-10)  # the outer residual is FP64 in both modes
+
+
+def test_time_step_matches_oracle(gpu_lib):
+    case, p, y, ac = channel(8)
+    g, o = GpuSolver(case, p), pyoracle.Oracle(case, p)
+    yog, aog, yg, acg, sg = g.time_step(y, ac, 2)
+    yoo, aoo, yo, aco, so = o.time_step(y, ac, 2)
+    assert rel(yg, yo) < 1e-8
+    assert rel(yog, yoo) < 1e-8
+    assert rel(aog, aoo) < 1e-5
+
+
+def test_nan_state_reports_nonfinite_and_context_survives(c8):
+    case, p, y, ac, g, o = c8
+    bad = y.copy()
+    bad[5] = np.nan
+    with pytest.raises(PhgpuError) as e:
+        g.SolMFG(bad, ac)
+    assert e.value.code in (3, 4)
+    assert rel(g.ElmRes(y, ac), o.ElmRes(y, ac)) < 1e-10
+
+
+def test_deterministic_repeat(c16):
+    case, p, y, ac, g, o = c16
+    a = g.ElmMFG(y, ac)
+    b = g.ElmMFG(y, ac)
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+
+
+@pytest.mark.parametrize("n", [48])
+def test_large_mesh_properties(gpu_lib, n):
+    """Size-independent properties at a mesh the oracle is not run on."""
+    case, ph = mesh.channel_case(n)
+    from phasta_gb300.solver import make_params
+    p = make_params(ph["mu"], ph["dt"], Kspace=20, ap_mode=L.PHGPU_AP_LINEAR, precision=L.PHGPU_MIXED)
+    g = GpuSolver(case, p)
+    y0 = mesh.uniform_state(case, 0.3, sigma=0.0)
+    ac = np.zeros_like(y0)
+    r = g.ElmRes(y0, ac)
+    assert np.abs(r).max() < 1e-11  # free stream
+    y = mesh.uniform_state(case, 0.3)
+    r0 = np.linalg.norm(g.ElmRes(y, ac))
+    y1, a1, st = g.newton(y, ac, y, ac)
+    assert st.echeck <= p["etol"] * st.unorm0
+    assert np.linalg.norm(g.ElmRes(y1, a1)) < 0.1 * r0
