@@ -84,7 +84,7 @@ class ClockSampler:
         sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
         mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[3 + i]})
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].strip() == "Active"})
         pw = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "power_w_max": max(pw) if pw else None, "samples": len(self.samples)}
@@ -98,8 +98,9 @@ def make_workload(n: int, precision: str):
     case, ph = mesh.channel_case(n, mach=0.3, re=1000.0)
     prec = L.PHGPU_MIXED if precision == "mixed" else L.PHGPU_FP64
     ap = L.PHGPU_AP_LINEAR if precision == "mixed" else L.PHGPU_AP_FD
+    res = L.PHGPU_RES_GALERKIN64 if precision == "mixed" else L.PHGPU_RES_FP64
     params = make_params(ph["mu"], ph["dt"], rho_inf=0.5, Kspace=20, etol=1e-3, minIters=1,
-                         precision=prec, ap_mode=ap)
+                         precision=prec, ap_mode=ap, outer_residual=res)
     y0 = mesh.uniform_state(case, 0.3, sigma=0.01)
     ac0 = np.zeros_like(y0)
     return case, params, y0, ac0
@@ -193,7 +194,8 @@ def run_gpu(args, rank, world):
         "metric": "Newton-step throughput to 1e-3 relative nonlinear residual (elements/s)",
         "value": value, "unit": "elements/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 assembly/Ap, f64 residual/dots/Givens/LU" if args.precision == "mixed" else "f64",
+        "dtype": ("f32 assembly/Ap/stabilization; f64 Galerkin residual, dots, Givens, LU"
+                  if args.precision == "mixed" else "f64"),
         "data": "synthetic",
         "config": {"workload": f"channel {args.n}^3x6 tets Mach0.3 Re1000, Kspace20 tol1e-3, 3 Newton/step",
                    "elements": E, "nodes": case.nshg, "precision": args.precision,

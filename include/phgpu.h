@@ -50,6 +50,7 @@ enum {
 
 enum { PHGPU_FP64 = 0, PHGPU_MIXED = 1 };         /* precision */
 enum { PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1 };     /* Jacobian-vector product */
+enum { PHGPU_RES_FP64 = 0, PHGPU_RES_GALERKIN64 = 1 }; /* outer residual in mixed precision */
 enum { PHGPU_LU_FACT = 0, PHGPU_LU_FORWARD = 1, PHGPU_LU_BACKWARD = 2, PHGPU_LU_PRODUCT = 3 };
 
 /* The COMMON-block values the hot path reads (common.h), plus three options
@@ -74,7 +75,10 @@ typedef struct {
     int precision;                   /* PHGPU_FP64: reference arithmetic; PHGPU_MIXED: FP32
                                         assembly and Ap, FP64 outer residual, dots, Givens, LU */
     int ap_mode;                     /* PHGPU_AP_FD (Au1MFG) or PHGPU_AP_LINEAR */
-    int reserved[6];
+    int outer_residual;              /* mixed precision only: PHGPU_RES_FP64 (every term FP64) or
+                                        PHGPU_RES_GALERKIN64 (metrics, Euler flux and time term FP64;
+                                        least-squares and viscous terms FP32) */
+    int reserved[5];
 } phgpu_config;
 
 /* Mesh and boundary-condition arrays (what the reference keeps in

@@ -16,6 +16,7 @@ PHGPU_OK = 0
 STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NONFINITE", 4: "SINGULAR", 5: "UNSUPPORTED", 6: "NOMEM"}
 PHGPU_FP64, PHGPU_MIXED = 0, 1
 PHGPU_AP_FD, PHGPU_AP_LINEAR = 0, 1
+PHGPU_RES_FP64, PHGPU_RES_GALERKIN64 = 0, 1
 LU_FACT, LU_FORWARD, LU_BACKWARD, LU_PRODUCT = 0, 1, 2, 3
 
 _dp = C.POINTER(C.c_double)
@@ -33,7 +34,7 @@ class Config(C.Structure):
         ("Kspace", C.c_int), ("nGMRES", C.c_int), ("minIters", C.c_int),
         ("etol", C.c_double), ("epsM", C.c_double), ("eGMRES", C.c_double),
         ("iter", C.c_int), ("istep", C.c_int),
-        ("precision", C.c_int), ("ap_mode", C.c_int), ("reserved", C.c_int * 6),
+        ("precision", C.c_int), ("ap_mode", C.c_int), ("outer_residual", C.c_int), ("reserved", C.c_int * 5),
     ]
 
 

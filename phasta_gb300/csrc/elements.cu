@@ -21,6 +21,8 @@
 namespace phgpu {
 
 __constant__ TetTables c_tab;
+__constant__ float c_shpf[4][4];   // single-precision copies (no conversions in FP32 kernels)
+__constant__ float c_qwtf;
 
 void upload_tables(Ctx& C) {
     TetTables t;
@@ -45,6 +47,15 @@ void upload_tables(Ctx& C) {
         t.Qwtb[q] = 2.0 * A;
     }
     check(C, cudaMemcpyToSymbolAsync(c_tab, &t, sizeof(t), 0, cudaMemcpyHostToDevice, C.stream),
+          "upload tables");
+    float sf[4][4];
+    for (int q = 0; q < 4; ++q)
+        for (int a = 0; a < 4; ++a) sf[q][a] = (float)t.shp[q][a];
+    check(C, cudaMemcpyToSymbolAsync(c_shpf, sf, sizeof(sf), 0, cudaMemcpyHostToDevice, C.stream),
+          "upload tables");
+    static float qf;
+    qf = (float)t.Qwt[0];
+    check(C, cudaMemcpyToSymbolAsync(c_qwtf, &qf, sizeof(qf), 0, cudaMemcpyHostToDevice, C.stream),
           "upload tables");
 }
 
@@ -80,6 +91,13 @@ namespace {
 __device__ __forceinline__ float rsqrt_(float v) { return rsqrtf(v); }
 __device__ __forceinline__ double rsqrt_(double v) { return rsqrt(v); }
 
+template <typename R> __device__ __forceinline__ R shp(int q, int a);
+template <> __device__ __forceinline__ double shp<double>(int q, int a) { return c_tab.shp[q][a]; }
+template <> __device__ __forceinline__ float shp<float>(int q, int a) { return c_shpf[q][a]; }
+template <typename R> __device__ __forceinline__ R qwt();
+template <> __device__ __forceinline__ double qwt<double>() { return c_tab.Qwt[0]; }
+template <> __device__ __forceinline__ float qwt<float>() { return c_qwtf; }
+
 template <typename R>
 struct Geo {
     R WdetJ;
@@ -110,7 +128,7 @@ __device__ __forceinline__ void geometry(const R (&xl)[4][3], Geo<R>& g) {
     di[2][0] = (d[1][0] * d[2][1] - d[1][1] * d[2][0]) * rdet;
     di[2][1] = (d[2][0] * d[0][1] - d[0][0] * d[2][1]) * rdet;
     di[2][2] = (d[0][0] * d[1][1] - d[0][1] * d[1][0]) * rdet;
-    g.WdetJ = R(c_tab.Qwt[0]) * det;
+    g.WdetJ = qwt<R>() * det;
     R s[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -260,38 +278,38 @@ __device__ __forceinline__ void load5(const R* __restrict__ a, int n, R (&o)[5])
 }
 
 // --------------------------------------------------------------------------
-// residual family, one thread per element
-//   RM_RES    : ires = 1 residual (Euler + viscous + SUPG + time term)
-//   RM_MODRES : ires = 2 modified residual of (ya = perturbed, yb = base)
-//   RM_LIN    : d/d eps of the modified residual at yb in direction ya
+// chunk kernels: one CTA per chunk of <= kChunk elements
+//   phase 1  the chunk's nodes are staged in shared memory
+//   phase 2  each element's contributions go to shared-memory slots
+//   phase 3  each chunk node sums its slots (ascending (element, corner)
+//            order) and adds the sum to the global array; chunks that run
+//            concurrently share no node
 // --------------------------------------------------------------------------
+struct ChunkArgs {
+    const int* elem;     // nchunk+1
+    const int* node;     // nchunk+1
+    const int* nodes;    // global node of each chunk-local node
+    const int* cstart;   // slot-list offsets per chunk-local node (+1)
+    const unsigned short* csr;  // slot = element*4 + corner
+    const ushort4* lien; // local node indices per element
+};
+
+template <typename R>
+__device__ __forceinline__ void lds5(const R* __restrict__ s, int l, R (&o)[5]) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) o[k] = s[5 * l + k];
+}
+
+// residual family for one element (node data already gathered):
+//   RM_RES    : ires = 1 residual of state va with acceleration vb
+//   RM_MODRES : ires = 2 modified residual of (va = perturbed, vb = base)
+//   RM_LIN    : d/d eps of the modified residual at vb in direction va
+// writes the four nodal contributions (already weighted) to o[a][k]
 template <typename R, int MODE>
-__global__ void __launch_bounds__(kBlock)
-k_elem_res(const int4* __restrict__ ien, int ne, const R* __restrict__ x, const R* __restrict__ ya,
-           const R* __restrict__ yb, const R* __restrict__ ac, R* __restrict__ out, Phys<R> P,
-           int iabres, const int* __restrict__ skip) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
-    if (skip && *skip) return;
-    const int4 nd4 = ien[e];
-    const int nd[4] = {nd4.x, nd4.y, nd4.z, nd4.w};
+__device__ __forceinline__ void elem_res(const Phys<R>& P, const R (&xl)[4][3], const R (&va)[4][5],
+                                         const R (&vb)[4][5], R (&o)[4][5]) {
     Geo<R> geo;
-    {
-        R xl[4][3];
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int d = 0; d < 3; ++d) xl[a][d] = ldg(x + 3 * (size_t)nd[a] + d);
-        geometry(xl, geo);
-    }
-    // RM_RES: va = state, vb = acceleration; otherwise va = perturbed state or
-    // direction and vb = base state
-    R va[4][5], vb[4][5];
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        load5(ya, nd[a], va[a]);
-        load5(MODE == RM_RES ? ac : yb, nd[a], vb[a]);
-    }
+    geometry(xl, geo);
     const R (&base)[4][5] = (MODE == RM_RES) ? va : vb;
     R g[3][5];
     gradients(geo, va, g);
@@ -312,7 +330,7 @@ k_elem_res(const int4* __restrict__ ien, int ne, const R* __restrict__ x, const 
     for (int q = 0; q < 4; ++q) {
         R N[4];
 #pragma unroll
-        for (int a = 0; a < 4; ++a) N[a] = R(c_tab.shp[q][a]);
+        for (int a = 0; a < 4; ++a) N[a] = shp<R>(q, a);
         R bq[5];
 #pragma unroll
         for (int k = 0; k < 5; ++k) bq[k] = N[0] * base[0][k] + N[1] * base[1][k] + N[2] * base[2][k] + N[3] * base[3][k];
@@ -349,11 +367,11 @@ k_elem_res(const int4* __restrict__ ien, int ne, const R* __restrict__ x, const 
 #pragma unroll
                 for (int k = 0; k < 5; ++k) F[i][k] = R(0);
             R du[5];
+            R pv[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) pv[k] = N[0] * va[0][k] + N[1] * va[1][k] + N[2] * va[2][k] + N[3] * va[3][k];
             if (MODE == RM_MODRES) {
                 // conservative variables of the perturbed state (e3ivar.f:96-131)
-                R pv[5];
-#pragma unroll
-                for (int k = 0; k < 5; ++k) pv[k] = N[0] * va[0][k] + N[1] * va[1][k] + N[2] * va[2][k] + N[3] * va[3][k];
                 const R rho6 = pv[0] / (P.Rgas * pv[4]);
                 const R rk6 = R(0.5) * (pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3]);
                 du[0] = rho6;
@@ -362,10 +380,7 @@ k_elem_res(const int4* __restrict__ ien, int ne, const R* __restrict__ x, const 
                 du[3] = rho6 * pv[3];
                 du[4] = rho6 * (pv[4] * P.cv + rk6);
             } else {
-                R vq[5];
-#pragma unroll
-                for (int k = 0; k < 5; ++k) vq[k] = N[0] * va[0][k] + N[1] * va[1][k] + N[2] * va[2][k] + N[3] * va[3][k];
-                a0_v(b, vq, du);
+                a0_v(b, pv, du);
             }
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
@@ -398,78 +413,305 @@ k_elem_res(const int4* __restrict__ ien, int ne, const R* __restrict__ x, const 
 #pragma unroll
             for (int k = 0; k < 5; ++k) Tn[a][k] += N[a] * r16[k];
     }
-    // e3wmlt.f + local.f scatter (colour-exclusive read-modify-write)
+    // e3wmlt.f weights
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        R* o = out + 5 * (size_t)nd[a];
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+            o[a][k] = geo.WdetJ * (geo.shg[a][0] * S[0][k] + geo.shg[a][1] * S[1][k] + geo.shg[a][2] * S[2][k] + Tn[a][k]);
+}
+
+template <typename R, int MODE>
+__global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? 4 : 2)
+k_chunk_res(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restrict__ ya,
+            const R* __restrict__ yb, const R* __restrict__ ac, R* __restrict__ out, Phys<R> P, int iabres,
+            const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* sm = reinterpret_cast<R*>(smem_raw);
+    const int c = chunk0 + blockIdx.x;
+    const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
+    const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+    R* sx = sm;
+    R* sa = sx + 3 * nn;
+    R* sb = sa + 5 * nn;
+    R* slot = sb + 5 * nn;
+    const R* bsrc = (MODE == RM_RES) ? ac : yb;
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const int gn = ca.nodes[n0 + l];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) sx[3 * l + d] = ldg(x + 3 * (size_t)gn + d);
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-            R v = geo.WdetJ * (geo.shg[a][0] * S[0][k] + geo.shg[a][1] * S[1][k] + geo.shg[a][2] * S[2][k] + Tn[a][k]);
-            if (iabres) v = fabs(v);
-            o[k] += v;
+            sa[5 * l + k] = ldg(ya + 5 * (size_t)gn + k);
+            sb[5 * l + k] = ldg(bsrc + 5 * (size_t)gn + k);
         }
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < ne) {
+        const ushort4 ln = ca.lien[e0 + threadIdx.x];
+        const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
+        R xl[4][3], va[4][5], vb[4][5];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) xl[a][d] = sx[3 * nd[a] + d];
+            lds5(sa, nd[a], va[a]);
+            lds5(sb, nd[a], vb[a]);
+        }
+        R o[4][5];
+        elem_res<R, MODE>(P, xl, va, vb, o);
+        R* sl = slot + 20 * threadIdx.x;
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) sl[5 * a + k] = iabres ? fabs(o[a][k]) : o[a][k];
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        R acc[5] = {R(0), R(0), R(0), R(0), R(0)};
+        const int s0 = ca.cstart[n0 + l], s1 = ca.cstart[n0 + l + 1];
+        for (int s = s0; s < s1; ++s) {
+            const R* sl = slot + 5 * (int)ca.csr[s];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) acc[k] += sl[k];
+        }
+        R* og = out + 5 * (size_t)ca.nodes[n0 + l];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) og[k] += acc[k];
     }
 }
 
 // --------------------------------------------------------------------------
-// ElmMFG interior (ires = 3, iprec = 1): res, rmes and BDiag.
-// One thread per (element, node a); the quadrature-point state is evaluated
-// by each of the four threads of an element.
+// outer residual (ires = 1) with FP64 Galerkin terms and FP32 stabilization:
+// the element metrics and weights, the Euler flux (e3conv.f:72-96) and the
+// time term N_a A0 Y,t (e3massr.f:26-58) -- the large terms that cancel
+// between elements -- are FP64; the least-squares term A_i tau L (e3ls.f) and
+// the viscous flux (e3visc.f), which are small in comparison, are FP32.
 // --------------------------------------------------------------------------
-template <typename R>
-__global__ void __launch_bounds__(kBlock)
-k_elem_full(const int4* __restrict__ ien, int ne, const R* __restrict__ x, const R* __restrict__ y,
-            const R* __restrict__ ac, R* __restrict__ res, R* __restrict__ rmes, R* __restrict__ bd,
-            Phys<R> P) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int e = t >> 2, a = t & 3;
-    if (e >= ne) return;
-    const int4 nd4 = ien[e];
-    const int nd[4] = {nd4.x, nd4.y, nd4.z, nd4.w};
-    Geo<R> geo;
-    {
-        R xl[4][3];
+__global__ void __launch_bounds__(kChunk, 2)
+k_chunk_resh(ChunkArgs ca, int chunk0, const double* __restrict__ x, const double* __restrict__ y,
+             const double* __restrict__ ac, const float* __restrict__ xf, const float* __restrict__ yf,
+             const float* __restrict__ acf, double* __restrict__ out, Phys<double> P, Phys<float> Pf) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* sm = reinterpret_cast<double*>(smem_raw);
+    const int c = chunk0 + blockIdx.x;
+    const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
+    const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+    double* sx = sm;
+    double* sy = sx + 3 * nn;
+    double* sa = sy + 5 * nn;
+    double* slot = sa + 5 * nn;
+    float* fsm = reinterpret_cast<float*>(slot + 20 * kChunk);
+    float* fx = fsm;
+    float* fy = fx + 3 * nn;
+    float* fa = fy + 5 * nn;
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const size_t gn = ca.nodes[n0 + l];
 #pragma unroll
-        for (int n = 0; n < 4; ++n)
+        for (int d = 0; d < 3; ++d) {
+            sx[3 * l + d] = __ldg(x + 3 * gn + d);
+            fx[3 * l + d] = __ldg(xf + 3 * gn + d);
+        }
 #pragma unroll
-            for (int d = 0; d < 3; ++d) xl[n][d] = ldg(x + 3 * (size_t)nd[n] + d);
+        for (int k = 0; k < 5; ++k) {
+            sy[5 * l + k] = __ldg(y + 5 * gn + k);
+            sa[5 * l + k] = __ldg(ac + 5 * gn + k);
+            fy[5 * l + k] = __ldg(yf + 5 * gn + k);
+            fa[5 * l + k] = __ldg(acf + 5 * gn + k);
+        }
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < ne) {
+        const ushort4 ln = ca.lien[e0 + threadIdx.x];
+        const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
+        // ---- FP32: viscous flux and least-squares term, summed over the points ----
+        float S32[3][5];
+        {
+            float xl[4][3], yl[4][5], al[4][5];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) xl[a][d] = fx[3 * nd[a] + d];
+                lds5(fy, nd[a], yl[a]);
+                lds5(fa, nd[a], al[a]);
+            }
+            Geo<float> geo;
+            geometry(xl, geo);
+            float g[3][5];
+            gradients(geo, yl, g);
+            Visc<float> vs;
+            if (Pf.navier) viscous(Pf, g, vs);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 5; ++k) S32[i][k] = 0.f;
+#pragma unroll 1
+            for (int q = 0; q < 4; ++q) {
+                float N[4];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) N[a] = shp<float>(q, a);
+                float bq[5], aq[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    bq[k] = N[0] * yl[0][k] + N[1] * yl[1][k] + N[2] * yl[2][k] + N[3] * yl[3][k];
+                    aq[k] = N[0] * al[0][k] + N[1] * al[1][k] + N[2] * al[2][k] + N[3] * al[3][k];
+                }
+                Qp<float> b;
+                qp_state(Pf, bq[0], bq[1], bq[2], bq[3], bq[4], b);
+                qp_tau(Pf, geo, b);
+                float aig[5], a0a[5];
+                ai_gi(b, g, aig);
+                a0_v(b, aq, a0a);
+                float tl[5];
+                tl[0] = b.tau[0] * (aig[0] + a0a[0]);
+                tl[1] = b.tau[1] * (aig[1] + a0a[1]);
+                tl[2] = b.tau[1] * (aig[2] + a0a[2]);
+                tl[3] = b.tau[1] * (aig[3] + a0a[3]);
+                tl[4] = b.tau[2] * (aig[4] + a0a[4]);
+                float F[3][5];
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) F[i][k] = 0.f;
+                if (Pf.navier) {
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+                        for (int j = 0; j < 3; ++j) F[i][1 + j] = vs.t[i][j];
+                        F[i][4] = b.u[0] * vs.t[i][0] + b.u[1] * vs.t[i][1] + b.u[2] * vs.t[i][2] + vs.q[i];
+                    }
+                }
+                add_ai_v(b, tl, F);
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) S32[i][k] += F[i][k];
+            }
+        }
+        // ---- FP64: metrics, Euler flux and time term ----
+        double xl[4][3], yl[4][5];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) xl[a][d] = sx[3 * nd[a] + d];
+            lds5(sy, nd[a], yl[a]);
+        }
+        Geo<double> geo;
         geometry(xl, geo);
-    }
-    R yl[4][5], al[4][5];
+        double S[3][5], Tn[4][5];
 #pragma unroll
-    for (int n = 0; n < 4; ++n) {
-        load5(y, nd[n], yl[n]);
-        load5(ac, nd[n], al[n]);
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) S[i][k] = (double)S32[i][k];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) Tn[a][k] = 0.0;
+#pragma unroll 1
+        for (int q = 0; q < 4; ++q) {
+            double N[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) N[a] = shp<double>(q, a);
+            double bq[5], aq[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                bq[k] = N[0] * yl[0][k] + N[1] * yl[1][k] + N[2] * yl[2][k] + N[3] * yl[3][k];
+                aq[k] = N[0] * sa[5 * nd[0] + k] + N[1] * sa[5 * nd[1] + k] + N[2] * sa[5 * nd[2] + k] +
+                        N[3] * sa[5 * nd[3] + k];
+            }
+            const double p = bq[0], u0 = bq[1], u1 = bq[2], u2 = bq[3], T = bq[4];
+            const double rT = 1.0 / T;
+            const double drdp = P.rRgas * rT;
+            const double rho = p * drdp;
+            const double drdT = -rho * rT;
+            const double rk = 0.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+            const double hk = T * P.cp + rk;
+            const double ek = T * P.cv + rk;
+            const double e1p = drdp * hk - rT * T;
+            const double e4p = drdT * hk + rho * P.cp;
+            const double uu[3] = {u0, u1, u2};
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const double m = -uu[i] * rho;
+                S[i][0] += m;
+#pragma unroll
+                for (int j = 0; j < 3; ++j) S[i][1 + j] += m * uu[j] - (i == j ? p : 0.0);
+                S[i][4] += m * ek - uu[i] * p;
+            }
+            // A0 Y,t
+            const double sA = drdp * aq[0] + drdT * aq[4];
+            double a0a[5];
+            a0a[0] = sA;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) a0a[1 + j] = uu[j] * sA + rho * aq[1 + j];
+            a0a[4] = e1p * aq[0] + rho * (u0 * aq[1] + u1 * aq[2] + u2 * aq[3]) + e4p * aq[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int k = 0; k < 5; ++k) Tn[a][k] += N[a] * a0a[k];
+        }
+        double* sl = slot + 20 * threadIdx.x;
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                sl[5 * a + k] = geo.WdetJ * (geo.shg[a][0] * S[0][k] + geo.shg[a][1] * S[1][k] +
+                                             geo.shg[a][2] * S[2][k] + Tn[a][k]);
     }
+    __syncthreads();
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        const int s0 = ca.cstart[n0 + l], s1 = ca.cstart[n0 + l + 1];
+        for (int s = s0; s < s1; ++s) {
+            const double* sl = slot + 5 * (int)ca.csr[s];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) acc[k] += sl[k];
+        }
+        double* og = out + 5 * (size_t)ca.nodes[n0 + l];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) og[k] += acc[k];
+    }
+}
+
+// --------------------------------------------------------------------------
+// ElmMFG interior (ires = 3, iprec = 1): res, rmes and BDiag of node a of one
+// element; the quadrature-point state is evaluated by each of the four
+// threads of an element.  35 outputs: res 0-4, rmes 5-9, BDiag 10-34.
+// --------------------------------------------------------------------------
+constexpr int kFullOut = 35;
+constexpr int kFullSub = kChunk / 4;  // elements per sub-batch (4 threads each)
+template <typename R> constexpr int full_nsub() { return sizeof(R) == 4 ? 4 : 1; }
+
+// Lanes 4e..4e+3 of a warp hold one element; lane a evaluates quadrature
+// point q = a once and the four lanes exchange the point data by shuffles.
+constexpr int kQpVals = 25;  // u(3) p rho ek drdp drdT e1p e2p e3p e4p tau(3) A_i Y,i (5) A0 Y,t (5)
+
+template <typename R>
+__device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R (&xl)[4][3], const R (&yl)[4][5],
+                                               const R (&al)[4][5], R* __restrict__ out35) {
+    Geo<R> geo;
+    geometry(xl, geo);
     R g[3][5];
     gradients(geo, yl, g);
     Visc<R> vs;
     if (P.navier) viscous(P, g, vs);
     R s[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) s[i] = geo.shg[a][i];
+    for (int i = 0; i < 3; ++i) s[i] = (a == 0) ? geo.shg[0][i] : (a == 1) ? geo.shg[1][i] : (a == 2) ? geo.shg[2][i] : geo.shg[3][i];
     const R ss = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
-    R rl[5], rml[5], B_[5][5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-        rl[k] = R(0);
-        rml[k] = R(0);
-#pragma unroll
-        for (int j = 0; j < 5; ++j) B_[k][j] = R(0);
-    }
-    // viscous part of the weighted flux sum_i s_i F_i (element constant momentum part)
     R sv[3] = {R(0), R(0), R(0)}, sq = R(0);
     if (P.navier) {
 #pragma unroll
         for (int j = 0; j < 3; ++j) sv[j] = s[0] * vs.t[0][j] + s[1] * vs.t[1][j] + s[2] * vs.t[2][j];
         sq = s[0] * vs.q[0] + s[1] * vs.q[1] + s[2] * vs.q[2];
     }
-#pragma unroll 1
-    for (int q = 0; q < 4; ++q) {
+    // this lane's quadrature point (q = a)
+    R own[kQpVals];
+    {
         R N[4];
 #pragma unroll
-        for (int n = 0; n < 4; ++n) N[n] = R(c_tab.shp[q][n]);
-        const R Na = N[a];
+        for (int n = 0; n < 4; ++n) N[n] = shp<R>(a, n);
         R yq[5], aq[5];
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
@@ -479,58 +721,67 @@ k_elem_full(const int4* __restrict__ ien, int ne, const R* __restrict__ x, const
         Qp<R> b;
         qp_state(P, yq[0], yq[1], yq[2], yq[3], yq[4], b);
         qp_tau(P, geo, b);
-        const R u0 = b.u[0], u1 = b.u[1], u2 = b.u[2];
-        R aig[5], a0a[5], du[5];
+        R aig[5], a0a[5];
         ai_gi(b, g, aig);
         a0_v(b, aq, a0a);
-        const R ek = b.ei + b.rk;
-        du[0] = b.rho;
-        du[1] = b.rho * u0;
-        du[2] = b.rho * u1;
-        du[3] = b.rho * u2;
-        du[4] = b.rho * ek;
-        R lt[5], lm[5];  // tau (A_i Y,i + A0 Y,t)  and  tau (A_i Y,i + fct U)
+        own[0] = b.u[0]; own[1] = b.u[1]; own[2] = b.u[2]; own[3] = b.p; own[4] = b.rho; own[5] = b.ei + b.rk;
+        own[6] = b.drdp; own[7] = b.drdT; own[8] = b.e1p; own[9] = b.e2p; own[10] = b.e3p; own[11] = b.e4p;
+        own[12] = b.tau[0]; own[13] = b.tau[1]; own[14] = b.tau[2];
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-            lt[k] = aig[k] + a0a[k];
-            lm[k] = aig[k] + P.fct1 * du[k];
+            own[15 + k] = aig[k];
+            own[20 + k] = a0a[k];
         }
-        const R tk[5] = {b.tau[0], b.tau[1], b.tau[1], b.tau[1], b.tau[2]};
-        R rm16[5];
+    }
+    R rl[5], rml[5], B_[5][5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        rl[k] = R(0);
+        rml[k] = R(0);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) B_[k][j] = R(0);
+    }
+    const int base_lane = (threadIdx.x & 31) & ~3;
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        R v[kQpVals];
+#pragma unroll
+        for (int i = 0; i < kQpVals; ++i) v[i] = __shfl_sync(0xffffffffu, own[i], base_lane + q);
+        const R Na = shp<R>(q, a);
+        const R u0 = v[0], u1 = v[1], u2 = v[2], p = v[3], rho = v[4], ek = v[5];
+        const R drdp = v[6], drdT = v[7], e1p = v[8], e2p = v[9], e3p = v[10], e4p = v[11];
+        const R tk[5] = {v[12], v[13], v[13], v[13], v[14]};
+        const R uu[3] = {u0, u1, u2};
+        R lt[5], lm[5], rm16[5];
+        const R du[5] = {rho, rho * u0, rho * u1, rho * u2, rho * ek};
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-            rm16[k] = lm[k];
-            lt[k] *= tk[k];
-            lm[k] *= tk[k];
+            rm16[k] = v[15 + k] + P.fct1 * du[k];
+            lt[k] = tk[k] * (v[15 + k] + v[20 + k]);
+            lm[k] = tk[k] * rm16[k];
         }
-        // B_a = sum_i s_i A_i
         const R Us = s[0] * u0 + s[1] * u1 + s[2] * u2;
         R Bm[5][5];
-        Bm[0][0] = b.drdp * Us;
-        Bm[0][4] = b.drdT * Us;
+        Bm[0][0] = drdp * Us;
+        Bm[0][4] = drdT * Us;
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            Bm[0][1 + j] = b.rho * s[j];
-            Bm[1 + j][0] = b.drdp * Us * b.u[j] + s[j];
-            Bm[1 + j][4] = b.drdT * Us * b.u[j];
+            Bm[0][1 + j] = rho * s[j];
+            Bm[1 + j][0] = drdp * Us * uu[j] + s[j];
+            Bm[1 + j][4] = drdT * Us * uu[j];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) Bm[1 + j][1 + k] = b.rho * (b.u[j] * s[k] + (j == k ? Us : R(0)));
-            Bm[4][1 + j] = b.e3p * s[j] + b.rho * Us * b.u[j];
+            for (int k = 0; k < 3; ++k) Bm[1 + j][1 + k] = rho * (uu[j] * s[k] + (j == k ? Us : R(0)));
+            Bm[4][1 + j] = e3p * s[j] + rho * Us * uu[j];
         }
-        Bm[4][0] = b.e2p * Us;
-        Bm[4][4] = b.e4p * Us;
-        // residual: sum_i s_i (Euler_i + visc_i) + B_a tau L + N_a A0 Y,t
+        Bm[4][0] = e2p * Us;
+        Bm[4][4] = e4p * Us;
         R fe[5];
-        const R m = -b.rho * Us;
+        const R m = -rho * Us;
         fe[0] = m;
 #pragma unroll
-        for (int j = 0; j < 3; ++j) fe[1 + j] = m * b.u[j] - s[j] * b.p + sv[j];
-        fe[4] = m * ek - Us * b.p + (u0 * sv[0] + u1 * sv[1] + u2 * sv[2]) + sq;
-        R fm[5];
-        fm[0] = R(0);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) fm[1 + j] = sv[j];
-        fm[4] = (u0 * sv[0] + u1 * sv[1] + u2 * sv[2]) + sq;
+        for (int j = 0; j < 3; ++j) fe[1 + j] = m * uu[j] - s[j] * p + sv[j];
+        const R usv = u0 * sv[0] + u1 * sv[1] + u2 * sv[2] + sq;
+        fe[4] = m * ek - Us * p + usv;
 #pragma unroll
         for (int r = 0; r < 5; ++r) {
             R bt = R(0), bm = R(0);
@@ -539,27 +790,28 @@ k_elem_full(const int4* __restrict__ ien, int ne, const R* __restrict__ x, const
                 bt += Bm[r][k] * lt[k];
                 bm += Bm[r][k] * lm[k];
             }
-            rl[r] += fe[r] + bt + Na * a0a[r];
-            rml[r] += fm[r] + bm + Na * rm16[r];
+            const R fm = (r == 0) ? R(0) : (r == 4) ? usv : sv[r - 1];
+            rl[r] += fe[r] + bt + Na * v[20 + r];
+            rml[r] += fm + bm + Na * rm16[r];
         }
         // BDiag: (N_a I + B_a tau)(B_a + fct N_a A0) + K_a
+        const R fN = P.fct1 * Na;
         R Cm[5][5];
 #pragma unroll
         for (int r = 0; r < 5; ++r)
 #pragma unroll
             for (int k = 0; k < 5; ++k) Cm[r][k] = Bm[r][k];
-        const R fN = P.fct1 * Na;
-        Cm[0][0] += fN * b.drdp;
-        Cm[0][4] += fN * b.drdT;
+        Cm[0][0] += fN * drdp;
+        Cm[0][4] += fN * drdT;
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            Cm[1 + j][0] += fN * b.drdp * b.u[j];
-            Cm[1 + j][1 + j] += fN * b.rho;
-            Cm[1 + j][4] += fN * b.drdT * b.u[j];
-            Cm[4][1 + j] += fN * b.rho * b.u[j];
+            Cm[1 + j][0] += fN * drdp * uu[j];
+            Cm[1 + j][1 + j] += fN * rho;
+            Cm[1 + j][4] += fN * drdT * uu[j];
+            Cm[4][1 + j] += fN * rho * uu[j];
         }
-        Cm[4][0] += fN * b.e1p;
-        Cm[4][4] += fN * b.e4p;
+        Cm[4][0] += fN * e1p;
+        Cm[4][4] += fN * e4p;
         if (P.supg) {
 #pragma unroll
             for (int r = 0; r < 5; ++r) {
@@ -567,21 +819,20 @@ k_elem_full(const int4* __restrict__ ien, int ne, const R* __restrict__ x, const
 #pragma unroll
                 for (int k = 0; k < 5; ++k) D[k] = Bm[r][k] * tk[k] + (r == k ? Na : R(0));
 #pragma unroll
-                for (int c = 0; c < 5; ++c) {
+                for (int cc = 0; cc < 5; ++cc) {
                     R acc = R(0);
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) acc += D[k] * Cm[k][c];
-                    B_[r][c] += acc;
+                    for (int k = 0; k < 5; ++k) acc += D[k] * Cm[k][cc];
+                    B_[r][cc] += acc;
                 }
             }
         } else {
 #pragma unroll
             for (int r = 0; r < 5; ++r)
 #pragma unroll
-                for (int c = 0; c < 5; ++c) B_[r][c] += Na * Cm[r][c];
+                for (int cc = 0; cc < 5; ++cc) B_[r][cc] += Na * Cm[r][cc];
         }
         if (P.navier) {
-            // K_a = sum_pq s_p s_q K_pq: momentum rmu|s|^2 I + (lambda+mu) s s^T, energy row K u, con |s|^2
             R km[3][3];
 #pragma unroll
             for (int j = 0; j < 3; ++j)
@@ -597,22 +848,130 @@ k_elem_full(const int4* __restrict__ ien, int ne, const R* __restrict__ x, const
         }
     }
     const R w = geo.WdetJ;
-    if (res) {
-        R* o = res + 5 * (size_t)nd[a];
 #pragma unroll
-        for (int k = 0; k < 5; ++k) o[k] += w * rl[k];
+    for (int k = 0; k < 5; ++k) {
+        out35[k] = w * rl[k];
+        out35[5 + k] = w * rml[k];
     }
-    if (rmes) {
-        R* o = rmes + 5 * (size_t)nd[a];
 #pragma unroll
-        for (int k = 0; k < 5; ++k) o[k] += w * rml[k];
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 5; ++cc) out35[10 + 5 * r + cc] = w * B_[r][cc];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? 3 : 2)
+k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restrict__ y, const R* __restrict__ ac,
+             R* __restrict__ res, R* __restrict__ rmes, R* __restrict__ bd, Phys<R> P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* sm = reinterpret_cast<R*>(smem_raw);
+    const int c = chunk0 + blockIdx.x;
+    const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
+    const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+    R* sx = sm;
+    R* sy = sx + 3 * nn;
+    R* sa = sy + 5 * nn;
+    constexpr bool single = kFullSub * full_nsub<R>() >= kChunk;
+    R* acc = sa + 5 * nn;                         // nn x 35 (multi-round only)
+    R* slot = acc + (single ? 0 : kFullOut * nn); // (kChunk * nsub) x 35
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const int gn = ca.nodes[n0 + l];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) sx[3 * l + d] = ldg(x + 3 * (size_t)gn + d);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            sy[5 * l + k] = ldg(y + 5 * (size_t)gn + k);
+            sa[5 * l + k] = ldg(ac + 5 * (size_t)gn + k);
+        }
     }
-    if (bd) {
-        R* o = bd + 25 * (size_t)nd[a];
+    if (!single)
+        for (int i = threadIdx.x; i < kFullOut * nn; i += blockDim.x) acc[i] = R(0);
+    // FP32: the whole chunk is computed before one accumulation round;
+    // FP64: one sub-batch per round (bounded shared memory)
+    constexpr int nsub = full_nsub<R>();
+    for (int b0 = 0; b0 < ne; b0 += kFullSub * nsub) {
+        __syncthreads();
+#pragma unroll 1
+        for (int sb = 0; sb < nsub; ++sb) {
+            const int el_raw = b0 + sb * kFullSub + (threadIdx.x >> 2), a = threadIdx.x & 3;
+            const bool valid = el_raw < ne;
+            const int el = valid ? el_raw : ne - 1;  // every lane takes part in the shuffles
+            const ushort4 ln = ca.lien[e0 + el];
+            const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
+            R xl[4][3], yl[4][5], al[4][5];
 #pragma unroll
-        for (int r = 0; r < 5; ++r)
+            for (int n = 0; n < 4; ++n) {
 #pragma unroll
-            for (int c = 0; c < 5; ++c) o[5 * r + c] += w * B_[r][c];
+                for (int d = 0; d < 3; ++d) xl[n][d] = sx[3 * nd[n] + d];
+                lds5(sy, nd[n], yl[n]);
+                lds5(sa, nd[n], al[n]);
+            }
+            R o35[kFullOut];
+            elem_full_node<R>(P, a, xl, yl, al, o35);
+            if (valid) {
+                R* sl = slot + kFullOut * (sb * kChunk + threadIdx.x);
+#pragma unroll
+                for (int k = 0; k < kFullOut; ++k) sl[k] = o35[k];
+            }
+        }
+        __syncthreads();
+        const int lo = 4 * b0, hi = 4 * (b0 + kFullSub * nsub);
+        if (kFullSub * nsub >= kChunk) {
+            // single round: sum the slots straight into the global arrays
+            for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+                const int s0 = ca.cstart[n0 + l], s1 = ca.cstart[n0 + l + 1];
+                R t[kFullOut];
+#pragma unroll
+                for (int k = 0; k < kFullOut; ++k) t[k] = R(0);
+                for (int s = s0; s < s1; ++s) {
+                    const R* sl = slot + kFullOut * (int)ca.csr[s];
+#pragma unroll
+                    for (int k = 0; k < kFullOut; ++k) t[k] += sl[k];
+                }
+                const size_t gn = ca.nodes[n0 + l];
+                if (res) {
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) res[5 * gn + k] += t[k];
+                }
+                if (rmes) {
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) rmes[5 * gn + k] += t[5 + k];
+                }
+                if (bd) {
+#pragma unroll
+                    for (int k = 0; k < 25; ++k) bd[25 * gn + k] += t[10 + k];
+                }
+            }
+            return;
+        }
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            const int s0 = ca.cstart[n0 + l], s1 = ca.cstart[n0 + l + 1];
+            R* ac_ = acc + kFullOut * l;
+            for (int s = s0; s < s1; ++s) {
+                const int j = ca.csr[s];
+                if (j < lo || j >= hi) continue;
+                const R* sl = slot + kFullOut * (j - lo);
+#pragma unroll
+                for (int k = 0; k < kFullOut; ++k) ac_[k] += sl[k];
+            }
+        }
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const size_t gn = ca.nodes[n0 + l];
+        const R* ac_ = acc + kFullOut * l;
+        if (res) {
+#pragma unroll
+            for (int k = 0; k < 5; ++k) res[5 * gn + k] += ac_[k];
+        }
+        if (rmes) {
+#pragma unroll
+            for (int k = 0; k < 5; ++k) rmes[5 * gn + k] += ac_[5 + k];
+        }
+        if (bd) {
+#pragma unroll
+            for (int k = 0; k < 25; ++k) bd[25 * gn + k] += ac_[10 + k];
+        }
     }
 }
 
@@ -720,22 +1079,62 @@ k_boundary(const int4* __restrict__ ienb, const int* __restrict__ iBCB, const do
 
 }  // namespace
 
+static ChunkArgs chunk_args(const Ctx& C) {
+    return ChunkArgs{C.d_ch_elem, C.d_ch_node, C.d_ch_nodes, C.d_ch_cstart, C.d_ch_csr, C.d_ch_lien};
+}
+
+template <typename R>
+size_t res_smem(const Ctx& C) { return sizeof(R) * ((size_t)C.chunk_lmax * 13 + (size_t)kChunk * 20); }
+template <typename R>
+size_t full_smem(const Ctx& C) {
+    const bool single = kFullSub * full_nsub<R>() >= kChunk;
+    return sizeof(R) * ((size_t)C.chunk_lmax * (13 + (single ? 0 : kFullOut)) + (size_t)kChunk * full_nsub<R>() * kFullOut);
+}
+
+size_t resh_smem(const Ctx& C) {
+    return sizeof(double) * ((size_t)C.chunk_lmax * 13 + (size_t)kChunk * 20) + sizeof(float) * (size_t)C.chunk_lmax * 13;
+}
+
+template <typename R>
+int configure_chunk_kernels(Ctx& C) {
+    const int rs = (int)res_smem<R>(C), fs = (int)full_smem<R>(C);
+    int rc = PHGPU_OK;
+    auto T = [&](cudaError_t e) { if (rc == PHGPU_OK) rc = check(C, e, "cudaFuncSetAttribute"); };
+    T(cudaFuncSetAttribute(k_chunk_res<R, RM_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
+    T(cudaFuncSetAttribute(k_chunk_res<R, RM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
+    T(cudaFuncSetAttribute(k_chunk_res<R, RM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
+    T(cudaFuncSetAttribute(k_chunk_full<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, fs));
+    return rc;
+}
+int configure_element_kernels(Ctx& C) {
+    if (full_smem<double>(C) > 227 * 1024) {
+        C.err = "a mesh chunk has too many distinct nodes for shared memory";
+        return PHGPU_ERR_UNSUPPORTED;
+    }
+    int rc = configure_chunk_kernels<double>(C);
+    if (rc == PHGPU_OK) rc = configure_chunk_kernels<float>(C);
+    if (rc == PHGPU_OK)
+        rc = check(C, cudaFuncSetAttribute(k_chunk_resh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)resh_smem(C)),
+                   "cudaFuncSetAttribute");
+    return rc;
+}
+
 template <typename R>
 void launch_elem_res(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R* ac, R* out,
                      int iabres, const int* skip) {
     const Phys<R> P = make_phys<R>(C.cfg);
-    const int ncol = (int)C.col_start.size() - 1;
+    const ChunkArgs ca = chunk_args(C);
+    const size_t sm = res_smem<R>(C);
+    const int ncol = (int)C.chunk_col_start.size() - 1;
     for (int c = 0; c < ncol; ++c) {
-        const int e0 = C.col_start[c], ne = C.col_start[c + 1] - e0;
-        if (ne <= 0) continue;
-        const int grid = (ne + kBlock - 1) / kBlock;
-        const int4* ien = C.d_ien + e0;
+        const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
+        if (nc <= 0) continue;
         if (mode == RM_RES)
-            k_elem_res<R, RM_RES><<<grid, kBlock, 0, C.stream>>>(ien, ne, x, ya, yb, ac, out, P, iabres, skip);
+            k_chunk_res<R, RM_RES><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
         else if (mode == RM_MODRES)
-            k_elem_res<R, RM_MODRES><<<grid, kBlock, 0, C.stream>>>(ien, ne, x, ya, yb, ac, out, P, iabres, skip);
+            k_chunk_res<R, RM_MODRES><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
         else
-            k_elem_res<R, RM_LIN><<<grid, kBlock, 0, C.stream>>>(ien, ne, x, ya, yb, ac, out, P, iabres, skip);
+            k_chunk_res<R, RM_LIN><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
         ++C.launches;
     }
 }
@@ -744,15 +1143,30 @@ template void launch_elem_res<double>(Ctx&, int, const double*, const double*, c
 template void launch_elem_res<float>(Ctx&, int, const float*, const float*, const float*, const float*, float*,
                                      int, const int*);
 
+void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf, const float* acf, double* out) {
+    const Phys<double> P = make_phys<double>(C.cfg);
+    const Phys<float> Pf = make_phys<float>(C.cfg);
+    const ChunkArgs ca = chunk_args(C);
+    const size_t sm = resh_smem(C);
+    const int ncol = (int)C.chunk_col_start.size() - 1;
+    for (int c = 0; c < ncol; ++c) {
+        const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
+        if (nc <= 0) continue;
+        k_chunk_resh<<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_x, y, ac, C.d_xf, yf, acf, out, P, Pf);
+        ++C.launches;
+    }
+}
+
 template <typename R>
 void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rmes, R* bd) {
     const Phys<R> P = make_phys<R>(C.cfg);
-    const int ncol = (int)C.col_start.size() - 1;
+    const ChunkArgs ca = chunk_args(C);
+    const size_t sm = full_smem<R>(C);
+    const int ncol = (int)C.chunk_col_start.size() - 1;
     for (int c = 0; c < ncol; ++c) {
-        const int e0 = C.col_start[c], ne = C.col_start[c + 1] - e0;
-        if (ne <= 0) continue;
-        const int grid = (4 * ne + kBlock - 1) / kBlock;
-        k_elem_full<R><<<grid, kBlock, 0, C.stream>>>(C.d_ien + e0, ne, x, y, ac, res, rmes, bd, P);
+        const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
+        if (nc <= 0) continue;
+        k_chunk_full<R><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, ac, res, rmes, bd, P);
         ++C.launches;
     }
 }

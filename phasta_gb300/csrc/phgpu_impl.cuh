@@ -16,7 +16,8 @@
 
 namespace phgpu {
 
-constexpr int kBlock = 128;          // threads per block of the element kernels
+constexpr int kBlock = 128;          // threads per block of the boundary kernel
+constexpr int kChunk = 128;          // elements per chunk (one CTA per chunk)
 constexpr int kRedBlocks = 4 * 152;  // fixed grid of the reductions (deterministic order)
 constexpr int kRedThreads = 256;
 
@@ -52,7 +53,16 @@ struct Ctx {
     // element colouring
     std::vector<int> col_start;   // ncol+1 (interior)
     std::vector<int> bcol_start;  // boundary
-    int4* d_ien = nullptr;        // E
+    int4* d_ien = nullptr;        // E (chunk order)
+    // chunks (chunks.cu)
+    int nchunk = 0, chunk_lmax = 0;
+    std::vector<int> chunk_col_start;  // chunk colours
+    int* d_ch_elem = nullptr;     // nchunk+1
+    int* d_ch_node = nullptr;     // nchunk+1
+    int* d_ch_nodes = nullptr;    // chunk-local -> global node
+    int* d_ch_cstart = nullptr;   // slot-list offsets (+1)
+    unsigned short* d_ch_csr = nullptr;
+    ushort4* d_ch_lien = nullptr;
     int4* d_ienb = nullptr;       // Eb (face nodes first)
     int* d_iBCB = nullptr;        // Eb
     double* d_BCB = nullptr;      // Eb*18  [e][n][6]
@@ -120,7 +130,10 @@ void launch_elem_res(Ctx& C, int mode, const R* x, const R* ya, const R* yb, con
 template <typename R>
 void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rmes, R* bd);
 void launch_boundary(Ctx& C, const double* y, double* res);
+void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf, const float* acf, double* out);
 void upload_tables(Ctx& C);
+int build_chunks(Ctx& C, const int* ien, const double* x_ref);
+int configure_element_kernels(Ctx& C);
 
 // ---- nodal kernels (nodal.cu) ----
 template <typename R> void bc3res(Ctx& C, R* r);

@@ -450,10 +450,17 @@ int solmfg_dev(Ctx& C, phgpu_stats* st) {
     } else {
         if (C.cfg.ap_mode != PHGPU_AP_LINEAR)
             return fail(C, PHGPU_ERR_UNSUPPORTED, "mixed precision needs the linearized Jacobian-vector product");
-        // FP64 outer residual; FP32 block-diagonal tangent
-        PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
+        // outer residual (FP64, or FP64 Galerkin + FP32 stabilization); FP32 block-diagonal tangent
         to_f32(C, C.d_y, C.d_yf, n5);
         to_f32(C, C.d_ac, C.d_acf, n5);
+        if (C.cfg.outer_residual == PHGPU_RES_GALERKIN64) {
+            fill0(C, C.d_res, sizeof(double) * n5);
+            launch_elem_resh(C, C.d_y, C.d_ac, C.d_yf, C.d_acf, C.d_res);
+            if (C.Eb > 0) launch_boundary(C, C.d_y, C.d_res);
+            bc3res<double>(C, C.d_res);
+        } else {
+            PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
+        }
         fill0(C, C.d_bdf, sizeof(float) * 25 * N);
         launch_elem_full<float>(C, C.d_xf, C.d_yf, C.d_acf, nullptr, nullptr, C.d_bdf);
         bc3bdg<float>(C, C.d_y, C.d_bdf);
@@ -575,16 +582,12 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     int rc = PHGPU_OK;
     auto T = [&](int s) { if (rc == PHGPU_OK) rc = s; };
     // colouring
-    std::vector<int> order, border;
-    T(colour(C, N, m->ien, C.E, order, C.col_start));
+    std::vector<int> border;
     if (C.Eb > 0) T(colour(C, N, m->ienb, C.Eb, border, C.bcol_start));
     if (rc != PHGPU_OK) { phgpu_destroy(h); return rc; }
-    C.perm_e = order;
-    std::vector<int4> ien(C.E);
-    for (int i = 0; i < C.E; ++i) {
-        const int* p = m->ien + 4 * (size_t)order[i];
-        ien[i] = make_int4(p[0], p[1], p[2], p[3]);
-    }
+    T(build_chunks(C, m->ien, m->x));
+    if (rc == PHGPU_OK) T(configure_element_kernels(C));
+    if (rc != PHGPU_OK) { phgpu_destroy(h); return rc; }
     std::vector<int4> ienb(std::max(C.Eb, 1));
     std::vector<int> ibcb(std::max(C.Eb, 1), 0);
     std::vector<double> bcb(18 * (size_t)std::max(C.Eb, 1), 0.0);
@@ -631,7 +634,6 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     C.nmaster = (int)mst.size();
     const size_t n5 = 5 * (size_t)N;
     const int K = cfg->Kspace;
-    T(dalloc(C, &C.d_ien, C.E));
     T(dalloc(C, &C.d_ienb, std::max(C.Eb, 1)));
     T(dalloc(C, &C.d_iBCB, std::max(C.Eb, 1)));
     T(dalloc(C, &C.d_BCB, 18 * (size_t)std::max(C.Eb, 1)));
@@ -671,7 +673,6 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     auto up = [&](void* d, const void* s, size_t bytes) {
         T(check(C, cudaMemcpy(d, s, bytes, cudaMemcpyHostToDevice), "upload mesh"));
     };
-    up(C.d_ien, ien.data(), sizeof(int4) * C.E);
     up(C.d_ienb, ienb.data(), sizeof(int4) * ienb.size());
     up(C.d_iBCB, ibcb.data(), sizeof(int) * ibcb.size());
     up(C.d_BCB, bcb.data(), sizeof(double) * bcb.size());
@@ -704,7 +705,8 @@ int phgpu_destroy(phgpu_ctx* h) {
     if (!h) return PHGPU_OK;
     Ctx& C = h->c;
     if (C.stream) cudaStreamSynchronize(C.stream);
-    void* ptrs[] = {C.d_bdstage, C.d_ien, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
+    void* ptrs[] = {C.d_ch_elem, C.d_ch_node, C.d_ch_nodes, C.d_ch_cstart, C.d_ch_csr, C.d_ch_lien,
+                    C.d_bdstage, C.d_ien, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
                     C.d_slaves, C.d_mst, C.d_slv_start, C.d_slv, C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_res,
                     C.d_rmes, C.d_Dy, C.d_ypre, C.d_t64, C.d_t64b, C.d_bd, C.d_yf, C.d_acf, C.d_resf, C.d_rmesf,
                     C.d_t32, C.d_t32b, C.d_bdf, C.d_U, C.d_scal, C.d_part, C.d_count, C.d_flag};
@@ -736,7 +738,7 @@ int phgpu_get_config(phgpu_ctx* h, phgpu_config* cfg) {
 }
 const char* phgpu_last_error(phgpu_ctx* h) { return h ? h->c.err.c_str() : "null context"; }
 void* phgpu_stream(phgpu_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
-int phgpu_num_colors(phgpu_ctx* h) { return h ? (int)h->c.col_start.size() - 1 : 0; }
+int phgpu_num_colors(phgpu_ctx* h) { return h ? (int)h->c.chunk_col_start.size() - 1 : 0; }
 long long phgpu_kernel_launches(phgpu_ctx* h) { return h ? h->c.launches : 0; }
 
 int phgpu_elmmfg(phgpu_ctx* h, const double* y, const double* ac, double* res, double* rmes, double* bdiag,
@@ -949,6 +951,9 @@ int phgpu_sweep_dev(phgpu_ctx* h, int which) {
         case 5:
             to_f32(C, C.d_y, C.d_yf, n5);
             to_f32(C, C.d_ac, C.d_acf, n5);
+            break;
+        case 6:  // FP64-Galerkin / FP32-stabilization residual
+            launch_elem_resh(C, C.d_y, C.d_ac, C.d_yf, C.d_acf, C.d_res);
             break;
         default:
             return PHGPU_ERR_INVALID;
