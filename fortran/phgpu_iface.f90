@@ -1,0 +1,84 @@
+! phgpu_iface.f90 -- ISO_C_BINDING interface of include/phgpu.h for a PHASTA
+! build (compressible solver).  Compiled only by a Fortran compiler; the
+! wrappers keep the argument lists of the routines they replace.
+module phgpu_iface
+  use iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: PHGPU_OK = 0
+  integer(c_int), parameter :: PHGPU_FP64 = 0, PHGPU_MIXED = 1
+  integer(c_int), parameter :: PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1
+  integer(c_int), parameter :: PHGPU_RES_FP64 = 0, PHGPU_RES_GALERKIN64 = 1
+
+  type, bind(C) :: phgpu_config
+     real(c_double) :: Rgas, gamma, gamma1, pr, rmu
+     real(c_double) :: Dtgl, almi, alfi, gami
+     real(c_double) :: dtsfct, taucfct, temper
+     integer(c_int) :: itau, ivart, iremoveStabTimeTerm, Navier, ipord, EntropyPressure
+     integer(c_int) :: Kspace, nGMRES, minIters
+     real(c_double) :: etol, epsM, eGMRES
+     integer(c_int) :: iter, istep
+     integer(c_int) :: precision, ap_mode, outer_residual
+     integer(c_int) :: reserved(5)
+  end type
+
+  type, bind(C) :: phgpu_mesh
+     integer(c_int) :: nshg, nelem
+     type(c_ptr)    :: ien, x
+     integer(c_int) :: nbelem
+     type(c_ptr)    :: ienb, iBCB, BCB, iBC, BC, iper
+  end type
+
+  type, bind(C) :: phgpu_stats
+     integer(c_int) :: iKs, lGMRES, ntotGM, status
+     real(c_double) :: unorm0, echeck, eGMRES, totres, rnorm, t_assembly_ms, t_gmres_ms
+  end type
+
+  interface
+     integer(c_int) function phgpu_create(mesh, cfg, ctx) bind(C, name="phgpu_create")
+       import :: c_int, c_ptr, phgpu_mesh, phgpu_config
+       type(phgpu_mesh), intent(in) :: mesh
+       type(phgpu_config), intent(in) :: cfg
+       type(c_ptr), intent(out) :: ctx
+     end function
+     integer(c_int) function phgpu_set_config(ctx, cfg) bind(C, name="phgpu_set_config")
+       import :: c_int, c_ptr, phgpu_config
+       type(c_ptr), value :: ctx
+       type(phgpu_config), intent(in) :: cfg
+     end function
+     integer(c_int) function phgpu_elmmfg(ctx, y, ac, res, rmes, bdiag, iprec) bind(C, name="phgpu_elmmfg")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: y(*), ac(*)
+       real(c_double), intent(out) :: res(*), rmes(*), bdiag(*)
+       integer(c_int), value :: iprec
+     end function
+     integer(c_int) function phgpu_itrres(ctx, yp, yc, ac, rmes) bind(C, name="phgpu_itrres")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: yp(*), yc(*), ac(*)
+       real(c_double), intent(inout) :: rmes(*)
+     end function
+     integer(c_int) function phgpu_solmfg(ctx, y, ac, res, bdiag, Dy, st) bind(C, name="phgpu_solmfg")
+       import :: c_int, c_double, c_ptr, phgpu_stats
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: y(*), ac(*)
+       real(c_double), intent(out) :: res(*), bdiag(*), Dy(*)
+       type(phgpu_stats), intent(inout) :: st
+     end function
+     integer(c_int) function phgpu_time_step(ctx, yold, acold, y, ac, nitr, st) bind(C, name="phgpu_time_step")
+       import :: c_int, c_double, c_ptr, phgpu_stats
+       type(c_ptr), value :: ctx
+       real(c_double), intent(inout) :: yold(*), acold(*)
+       real(c_double), intent(out) :: y(*), ac(*)
+       integer(c_int), value :: nitr
+       type(phgpu_stats), intent(inout) :: st
+     end function
+     type(c_ptr) function phgpu_last_error(ctx) bind(C, name="phgpu_last_error")
+       import :: c_ptr
+       type(c_ptr), value :: ctx
+     end function
+  end interface
+
+  type(c_ptr), save :: phgpu_ctx = c_null_ptr
+end module phgpu_iface
