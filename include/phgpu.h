@@ -45,7 +45,8 @@ enum {
     PHGPU_ERR_NONFINITE = 3,   /* NaN/Inf in a residual or in the solution update (tnanq.f) */
     PHGPU_ERR_SINGULAR = 4,    /* zero or non-finite pivot in the 5x5 block LU */
     PHGPU_ERR_UNSUPPORTED = 5, /* option outside the implemented path */
-    PHGPU_ERR_NOMEM = 6        /* device allocation failed */
+    PHGPU_ERR_NOMEM = 6,       /* device allocation failed */
+    PHGPU_ERR_TOO_LARGE = 7    /* input larger than a fixed-size entry point accepts */
 };
 
 enum { PHGPU_FP64 = 0, PHGPU_MIXED = 1 };         /* precision */
@@ -155,6 +156,33 @@ int phgpu_time_step_dev(phgpu_ctx* ctx, int nitr, phgpu_stats* st);
 int phgpu_residual_norm_dev(phgpu_ctx* ctx, double* rnorm);
 /* one FP32/FP64 residual sweep of the resident state (timing probe of the hot kernel) */
 int phgpu_sweep_dev(phgpu_ctx* ctx, int which);
+
+/* Largest 5*nshg that phgpu_rstat_noalloc accepts (33,554,432 values, nshg <= 6,710,886). */
+#define PHGPU_RSTAT_NOALLOC_MAX_N 33554432
+/* No counterpart in the reference: an allocation-free form of the residual
+ * statistic that phgpu_solmfg reports as phgpu_stats.totres,
+ * *totres = sqrt(sum_k res[k]^2) / nshg over the 5*nshg values of res.
+ *
+ * For callers that cannot allocate device memory -- a host code whose device
+ * memory is all owned by its own pool or another framework's allocator, or a
+ * phase that must not grow the device footprint or take the device-wide
+ * synchronisation that cudaMalloc/cudaFree can imply.  It needs no context.
+ * res and totres are DEVICE pointers owned by the caller; the call is
+ * asynchronous on `stream` (a cudaStream_t, NULL = legacy default stream).
+ * Its working storage is a fixed 128 KiB static device array inside the
+ * library, held by every GPU that loads the library until the process exits;
+ * it calls no cudaMalloc, cudaFree or other allocating routine.
+ *   - The first call on a device looks up that array's device address
+ *     (cudaGetSymbolAddress, with that device current) and caches it; make
+ *     that first call before any stream capture.
+ *   - Returns PHGPU_ERR_TOO_LARGE when 5*nshg > PHGPU_RSTAT_NOALLOC_MAX_N,
+ *     PHGPU_ERR_INVALID for null pointers or nshg <= 0, PHGPU_ERR_CUDA when
+ *     the address look-up or the launch fails.
+ *   - Every call shares the one array: calls that can overlap on the GPU
+ *     (concurrent streams, several host threads) race and give wrong results;
+ *     serialise them on one stream.  Each call clears the array's completion
+ *     counter itself, so no zeroing is required of the caller. */
+int phgpu_rstat_noalloc(const double* res, int nshg, double* totres, void* stream);
 
 #ifdef __cplusplus
 }

@@ -13,10 +13,12 @@ import numpy as np
 LIB_PATH = Path(__file__).resolve().parent / "libphgpu.so"
 
 PHGPU_OK = 0
-STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NONFINITE", 4: "SINGULAR", 5: "UNSUPPORTED", 6: "NOMEM"}
+STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NONFINITE", 4: "SINGULAR", 5: "UNSUPPORTED", 6: "NOMEM", 7: "TOO_LARGE"}
 PHGPU_FP64, PHGPU_MIXED = 0, 1
 PHGPU_AP_FD, PHGPU_AP_LINEAR = 0, 1
 PHGPU_RES_FP64, PHGPU_RES_GALERKIN64 = 0, 1
+PHGPU_ERR_INVALID, PHGPU_ERR_TOO_LARGE = 1, 7
+PHGPU_RSTAT_NOALLOC_MAX_N = 33554432
 LU_FACT, LU_FORWARD, LU_BACKWARD, LU_PRODUCT = 0, 1, 2, 3
 
 _dp = C.POINTER(C.c_double)
@@ -89,6 +91,7 @@ def lib():
         "phgpu_time_step_dev": ([vp, C.c_int, C.POINTER(Stats)], C.c_int),
         "phgpu_residual_norm_dev": ([vp, _dp], C.c_int),
         "phgpu_sweep_dev": ([vp, C.c_int], C.c_int),
+        "phgpu_rstat_noalloc": ([vp, C.c_int, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
