@@ -11,6 +11,11 @@
 // fused behind the restatement's back.  Terms the reference leaves out
 // because they multiply structural zeros of the Euler Jacobians are written
 // here as dense sums; adding an exact zero leaves every partial sum unchanged.
+//
+// Pinned against the reference itself: tests/golden/ref_*.npz hold outputs of
+// the reference's own Fortran routines (executed from its sources by
+// tests/golden/make_ref_golden.py), and tests/test_ref_golden.py checks this
+// file against them.
 #include "phasta_oracle.h"
 
 #include <cmath>
@@ -1117,6 +1122,30 @@ static double sumsq(const double* a, size_t n) {
     for (size_t i = 0; i < n; ++i) s += a[i] * a[i];
     return s;
 }
+
+// au2mfg.f:55-108: restart residual R - J Dy by a central difference of ItrRes
+// with eps = epsM^(2/3) / ||Dy||; u receives the new first Krylov vector
+static void au2mfg(const or_common& c, const or_mesh& m, const double* ypre, const double* y,
+                   const double* ac, const double* res, const double* Dy, const double* bd,
+                   double* u, int nthreads) {
+    const size_t n5 = 5 * (size_t)m.nshg;
+    double* bdm = const_cast<double*>(bd);
+    const double eps = std::pow(c.epsM, 2.0 / 3.0) / std::sqrt(sumsq(Dy, n5));
+    std::vector<double> ub1(n5, 0.0), ub2(n5, 0.0), ut(n5);
+    for (size_t i = 0; i < n5; ++i) ut[i] = ypre[i] + eps * Dy[i];
+    or_i3lu(m.nshg, bdm, ut.data(), 2);
+    or_yshuffle(m.nshg, ut.data(), 0);
+    or_itrbc(&m, ut.data(), ut.data(), 2, c.Rgas);
+    or_itrres(&c, &m, ut.data(), y, ac, ub1.data(), 0, nthreads);
+    or_i3lu(m.nshg, bdm, ub1.data(), 1);
+    for (size_t i = 0; i < n5; ++i) ut[i] = ypre[i] - eps * Dy[i];
+    or_i3lu(m.nshg, bdm, ut.data(), 2);
+    or_yshuffle(m.nshg, ut.data(), 0);
+    or_itrbc(&m, ut.data(), ut.data(), 2, c.Rgas);
+    or_itrres(&c, &m, ut.data(), y, ac, ub2.data(), 0, nthreads);
+    or_i3lu(m.nshg, bdm, ub2.data(), 1);
+    for (size_t i = 0; i < n5; ++i) u[i] = res[i] - (ub1[i] - ub2[i]) / (two * eps);
+}
 static double dot(const double* a, const double* b, size_t n) {
     double s = 0.0;
     for (size_t i = 0; i < n; ++i) s += a[i] * b[i];
@@ -1187,10 +1216,8 @@ void or_solmfg(or_common* c, const or_mesh* m, const double* y, const double* ac
         for (int mG = 1; mG <= c->nGMRES; ++mG) {
             lGMRES = mG - 1;
             if (lGMRES > 0) {
-                // Au2MFG restart (R - J Dy); not used by nGMRES = 1 configurations
-                std::vector<double> t(Dy, Dy + n5);
-                au1mfg(*c, *m, ypre.data(), y, ac, rmes.data(), bdiag, t.data(), nthreads);
-                for (size_t i = 0; i < n5; ++i) temp[i] = res[i] - t[i];
+                // solmfg.f:186-203: restart from R - J Dy (Au2MFG)
+                au2mfg(*c, *m, ypre.data(), y, ac, res, Dy, bdiag, temp.data(), nthreads);
                 std::memcpy(U(1), temp.data(), sizeof(double) * n5);
                 unorm = std::sqrt(sumsq(temp.data(), n5));
             }

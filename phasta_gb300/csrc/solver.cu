@@ -99,6 +99,12 @@ __global__ void k_fd_diff(const V* __restrict__ ub, const V* __restrict__ rmes, 
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         u[i] = (ub[i] - rmes[i]) / (V)e;
 }
+// u = res - (ub1 - ub2) / (2 eps)  (au2mfg.f:104)
+__global__ void k_cd_diff(const double* __restrict__ res, const double* ub1, const double* __restrict__ ub2,
+                          double two_eps, double* u, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        u[i] = res[i] - (ub1[i] - ub2[i]) / two_eps;
+}
 template <typename V>
 __global__ void k_copy(const V* __restrict__ a, V* __restrict__ b, size_t n, const int* skip) {
     if (skip && *skip) return;
@@ -270,6 +276,33 @@ int ap_fd64(Ctx& C, double* u, const double* rmes, const int* skip) {
     return PHGPU_OK;
 }
 
+// restart vector R - J Dy by a central difference of ItrRes (Au2MFG, au2mfg.f:55-104):
+// eps = epsM^(2/3) / ||Dy||, out = res - (R(ypre + eps Dy) - R(ypre - eps Dy)) / (2 eps)
+int au2_fd64(Ctx& C, double* out) {
+    const size_t n5 = 5 * (size_t)C.N;
+    dot<double>(C, C.d_Dy, C.d_Dy, n5, S_TMP0, nullptr);
+    PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, C.d_scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream),
+                 "Au2MFG norm"));
+    PH_TRY(sync(C));
+    const double eps = std::pow(C.cfg.epsM, 2.0 / 3.0) / std::sqrt(C.h_scal[S_TMP0]);
+    if (!std::isfinite(eps)) return fail(C, PHGPU_ERR_NONFINITE, "Au2MFG: zero or non-finite restart step");
+    double* t = C.d_t64;
+    double* ub2 = C.d_t64b;
+    for (int side = 0; side < 2; ++side) {
+        double* ub = side == 0 ? out : ub2;
+        k_axpy_pre<double><<<kVG, kVT, 0, C.stream>>>(C.d_ypre, C.d_Dy, side == 0 ? eps : -eps, t, n5, nullptr);
+        ++C.launches;
+        lu_apply<double, double>(C, C.d_bd, t, PHGPU_LU_BACKWARD);
+        itrbc_pert<double>(C, t, false);
+        fill0(C, ub, sizeof(double) * n5);
+        itrres_dev<double>(C, C.d_x, t, C.d_y, ub, 0, nullptr);
+        lu_apply<double, double>(C, C.d_bd, ub, PHGPU_LU_FORWARD);
+    }
+    k_cd_diff<<<kVG, kVT, 0, C.stream>>>(C.d_res, out, ub2, 2.0 * eps, out, n5);
+    ++C.launches;
+    return PHGPU_OK;
+}
+
 template <typename V>
 int ap_lin(Ctx& C, V* u, const int* skip);
 
@@ -375,16 +408,19 @@ int gmres(Ctx& C, phgpu_stats* st) {
     for (int mG = 1; mG <= C.cfg.nGMRES; ++mG) {
         st->lGMRES = mG - 1;
         if (mG > 1) {
-            // restart: uBrg(1) = R - A Dy (Au2MFG is a central difference; the
-            // one-sided/linearized product is used here)
+            // restart: uBrg(1) = R - A Dy, by Au2MFG's central difference when the
+            // product is finite-differenced, else with the linearized product
             V* t = Uj(1);
             if constexpr (std::is_same<V, double>::value) {
-                k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, t, n5, nullptr);
-                ++C.launches;
-                if (C.cfg.ap_mode == PHGPU_AP_FD) PH_TRY(ap_fd64(C, t, C.d_rmes, nullptr));
-                else PH_TRY(ap_lin<V>(C, t, nullptr));
-                k_axpby<<<kVG, kVT, 0, C.stream>>>(C.d_res, 1.0, t, -1.0, t, n5);  // t = b - A Dy
-                ++C.launches;
+                if (C.cfg.ap_mode == PHGPU_AP_FD) {
+                    PH_TRY(au2_fd64(C, t));
+                } else {
+                    k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, t, n5, nullptr);
+                    ++C.launches;
+                    PH_TRY(ap_lin<V>(C, t, nullptr));
+                    k_axpby<<<kVG, kVT, 0, C.stream>>>(C.d_res, 1.0, t, -1.0, t, n5);  // t = b - A Dy
+                    ++C.launches;
+                }
             } else {
                 to_f32(C, C.d_Dy, t, n5);
                 PH_TRY(ap_lin<V>(C, t, nullptr));

@@ -1,0 +1,90 @@
+"""Generate tests/golden/ref_*.npz: outputs of the reference's own Fortran routines.
+
+Runs where the reference tree is present (it reads the Fortran sources from
+there).  fexec.py translates the reference's fixed-form sources of the hot
+path into numpy code in memory and refrun.py sets the COMMON blocks, so the
+arrays written here are what ElmMFG, ItrRes, i3LU, itrBC, SolMFG, itrSetup,
+itrPredict, itrCorrect and itrUpdate of the reference compute for the seeded
+inputs, which are stored beside the outputs.
+
+    python tests/golden/make_ref_golden.py [reference phSolver directory]
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path[:0] = [str(HERE), str(ROOT), str(ROOT / "tests")]
+
+from helpers import channel, vortex  # noqa: E402
+from refrun import RefPhasta  # noqa: E402
+
+DEFAULT_REF = Path("/root/reference/phSolver")
+
+# (name, case builder, parts): "elm" ElmMFG; "pieces" ItrRes, i3LU, itrBC; "solve" SolMFG;
+# "step" itrSetup and one two-iteration time step
+ALL = ("elm", "pieces", "solve", "step")
+CASES = [
+    ("channel4", lambda: channel(4, ac_scale=0.05), ALL),
+    ("vortex4", lambda: vortex(4), ALL),
+    ("channel3_euler", lambda: channel(3, ac_scale=0.05, navier=0), ("elm",)),
+    ("channel3_galerkin", lambda: channel(3, ac_scale=0.05, ivart=1), ("elm",)),
+    # Kspace 3 with two cycles: the second cycle restarts from Au2MFG's R - J Dy
+    ("channel4_restart", lambda: channel(4, ac_scale=0.05, Kspace=3, nGMRES=2), ("elm", "solve")),
+]
+
+
+def _params_json(p):
+    return json.dumps({k: (float(v) if isinstance(v, float) else v) for k, v in p.items()}, sort_keys=True)
+
+
+def make(name, build, parts, ref_root):
+    case, p, y, ac = build()
+    R = RefPhasta(case, p, ref_root)
+    out = {"params": np.array(_params_json(p)), "nshg": np.array(case.nshg), "nelem": np.array(case.nelem),
+           "ien": case.ien.astype(np.int32), "x": case.x_ref(), "y": y, "ac": ac}
+    res, rmes, bd = R.ElmMFG(y, ac)
+    out.update(elm_res=res, elm_rmes=rmes, elm_bd=bd)
+    if "pieces" in parts:
+        rng = np.random.default_rng(7)
+        yp = y * (1.0 + 1e-3 * rng.standard_normal(y.shape))
+        r0 = rng.standard_normal(y.shape)
+        out.update(yp=yp, r0=r0, itrres_rmes=R.ItrRes(yp, y, ac, r0))
+        lu, _ = R.i3LU(bd, None, 0)
+        out["lu_fact"] = lu
+        for code, key in ((1, "lu_forward"), (2, "lu_backward"), (3, "lu_product")):
+            out[key] = R.i3LU(lu, r0, code)[1]
+        yb, ab = R.itrBC(yp, ac)
+        out.update(itrbc_y=yb, itrbc_ac=ab)
+    if "solve" in parts:
+        sres, sbd, sDy, st = R.SolMFG(y, ac, y, ac)
+        out.update(sol_res=sres, sol_bd=sbd, sol_Dy=sDy, sol_iKs=np.array(st["iKs"]),
+                   sol_lGMRES=np.array(st["lGMRES"]), sol_ntotGM=np.array(st["ntotGM"]),
+                   sol_eGMRES=np.array(st["eGMRES"]))
+    if "step" in parts:
+        rho_inf = 0.5
+        setup = R.itrSetup(rho_inf, 1.0 / p["Dtgl"])
+        out["setup"] = np.array([setup[k] for k in ("almi", "alfi", "gami", "Dtgl")])
+        R2 = RefPhasta(case, p, ref_root)
+        yold, acold, y1, ac1, iks = R2.time_step(y, ac, 2)
+        out.update(step_yold=yold, step_acold=acold, step_y=y1, step_ac=ac1, step_iks=np.array(iks))
+    path = HERE / f"ref_{name}.npz"
+    np.savez_compressed(path, **out)
+    print(f"{path.name}: {path.stat().st_size // 1024} KiB, nshg {case.nshg}, nelem {case.nelem}")
+
+
+def main():
+    ref_root = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REF
+    if not (ref_root / "compressible" / "e3.f").exists():
+        raise SystemExit(f"reference sources not found under {ref_root}")
+    for name, build, parts in CASES:
+        make(name, build, parts, ref_root)
+
+
+if __name__ == "__main__":
+    main()

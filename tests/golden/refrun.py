@@ -1,0 +1,227 @@
+"""The reference's own Fortran routines of the hot path, run through fexec.
+
+``RefPhasta(case, params, root)`` loads the reference sources below from the
+reference tree ``root`` (its ``phSolver`` directory), sets the COMMON blocks a
+single-rank PHASTA run would hold for one linear-tet interior block and one
+boundary block, and exposes the routines with host arrays in the layouts of
+``include/phgpu.h`` (``y[k*nshg + n]``, ``bd[(i + 5j)*nshg + n]``).  It only
+runs where the reference tree is present; ``make_ref_golden.py`` uses it to
+write the committed golden vectors.
+"""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+
+try:
+    from . import fexec
+except ImportError:  # run as a script from tests/golden
+    import fexec
+
+HERE = Path(__file__).resolve().parent
+
+SOURCES = [
+    # ElmMFG chain
+    "compressible/elmmfg.f", "compressible/asimfg.f", "common/local.f", "common/localy.f",
+    "compressible/e3.f", "common/hierarchic.f", "compressible/e3ivar.f", "compressible/getthm.f",
+    "compressible/getdiff.f", "common/e3metric.f", "compressible/e3mtrx.f", "compressible/e3conv.f",
+    "compressible/e3visc.f", "compressible/e3ls.f", "compressible/e3tau.f", "compressible/e3massr.f",
+    "compressible/e3bdg.f", "compressible/e3wmlt.f",
+    # boundary elements and boundary conditions
+    "compressible/asbmfg.f", "compressible/e3b.f", "compressible/e3bvar.f", "compressible/bc3res.f",
+    "compressible/bc3bdg.f", "compressible/bc3per.f", "compressible/itrbc.f",
+    # solver
+    "compressible/itrres.f", "compressible/asires.f", "compressible/i3lu.f", "compressible/solmfg.f",
+    "compressible/au1mfg.f", "compressible/au2mfg.f", "compressible/itrfdi.f", "compressible/shuffle.f",
+    "compressible/itrPC.f", "common/mpitools.f", "common/clear.f",
+]
+# rstat.f only prints statistics, and SolMFG calls it with two of its three
+# arguments (solmfg.f:367 vs rstat.f:1); its totres (rstat.f:108) is computed
+# from the returned residual instead.
+
+MODULES = ["rlssave", "turbsa", "specialbc", "turbke", "spat_var_eps", "timedata", "machcontrol",
+           "blowingcontrol", "mod_timedata", "dtnmod", "periodicity", "pvsqbc", "convolimpflow",
+           "convolrcrflow", "incpbc", "lapackfuncs", "stats"]
+
+_LU = {0: "LU_Fact ", 1: "forward ", 2: "backward", 3: "product "}
+
+
+class _Obj:
+    def __init__(self, p):
+        self.p = p
+
+
+def _F(flat, shape):
+    """flat reference-layout array -> Fortran-ordered view of shape."""
+    return np.asarray(flat, dtype=np.float64).reshape(shape, order="F")
+
+
+class RefPhasta:
+    def __init__(self, case, params: dict, root):
+        root = Path(root)
+        P = fexec.Program([root / "common", root / "compressible"])
+        for f in SOURCES:
+            P.load(root / f)
+        P.stubs.update(timer=lambda *a: None, secs=lambda *a: 0.0, tmr=lambda *a: 0.0,
+                       tmrc=lambda *a: 0.0, tnanq=lambda *a: None, rstat=lambda *a: None)
+        N, E, Eb = case.nshg, case.nelem, case.nbelem
+        self.N, self.case, self.params = N, case, dict(params)
+        ien = np.asfortranarray(case.ien.astype(np.int64) + 1)
+        ienb = np.asfortranarray(case.ienb.astype(np.int64) + 1)
+        P.module("pointer_data", {
+            "mien": [_Obj(ien)], "mmat": [_Obj(np.ones(E, np.int64))],
+            "mxmudmi": [_Obj(np.zeros((E, 4), order="F"))],
+            "mienb": [_Obj(ienb)], "mmatb": [_Obj(np.ones(max(Eb, 1), np.int64))],
+            "mibcb": [_Obj(np.asfortranarray(case.iBCB.astype(np.int64)))],
+            "mbcb": [_Obj(np.asfortranarray(case.BCB))]})
+        for m in MODULES:
+            P.module(m, {})
+        P.function("elmmfg")  # declares the COMMON blocks of common.h
+        G = P.G
+        T = json.loads((HERE / "tet_tables.json").read_text())
+        p = self.params
+        G.numpe, G.myrank, G.master = 1, 0, 0
+        G.numnp = G.nshg = N
+        G.nshgt = N
+        G.numel, G.numelb = E, Eb
+        G.nen, G.ndof, G.nflow, G.nedof = 4, 5, 5, 20
+        G.ndofbc, G.ndibcb, G.ndbcb = 6, 2, 6
+        G.nelblk, G.nelblb = 1, (1 if Eb else 0)
+        # lcblk(:,iblk): iel, lelCat, lcsyst, iorder, nenl, -, mattyp, ndofl, nsymdl, nshl
+        G.lcblk[:, 0] = [1, 1, 1, 1, 4, 0, 1, 5, 0, 4]
+        G.lcblk[0, 1] = E + 1
+        # lcblkb(:,iblk): iel, lelCat, lcsyst, iorder, nenl, nenbl, mattyp, ndofl, nshl, nshlb
+        G.lcblkb[:, 0] = [1, 1, 1, 1, 4, 3, 1, 5, 4, 3]
+        G.lcblkb[0, 1] = Eb + 1
+        G.nint[0], G.nintb[0] = 4, 3
+        G.qwt[0, :4] = T["Qwt"]
+        G.qwtb[0, :3] = T["Qwtb"]
+        G.datmat[0, 1, 0] = p["rmu"]
+        G.pr, G.rgas, G.gamma, G.gamma1 = p["pr"], p["Rgas"], p["gamma"], p["gamma1"]
+        G.dtgl, G.almi, G.alfi, G.gami = p["Dtgl"], p["almi"], p["alfi"], p["gami"]
+        G.lhs, G.itau, G.ipord, G.idiff, G.isurf = 0, p["itau"], p["ipord"], 0, 0
+        G.dtsfct, G.taucfct, G.temper = p["dtsfct"], p["taucfct"], p["temper"]
+        G.ivart, G.navier, G.jactyp, G.idc = p["ivart"], p["Navier"], 0, 0
+        G.iremovestabtimeterm, G.entropypressure, G.idflx = p["iremoveStabTimeTerm"], p["EntropyPressure"], 0
+        G.kspace, G.ngmres, G.miniters = p["Kspace"], p["nGMRES"], p["minIters"]
+        G.epstol[0] = p["etol"]
+        G.etol = p["etol"]  # itrdrv.f:433
+        G.epsm = p["epsM"]
+        G.egmres = p["eGMRES"]
+        G.iter, G.istep = p["iter"], p["istep"]
+        G.iprec = 1
+        G.ipred = 1  # input.config: Predictor at Start of Step = Same Velocity
+        G.ntotgm = 0
+        self.P, self.G = P, G
+        self.shp = np.zeros((6, 32, 125), order="F")
+        self.shgl = np.zeros((6, 3, 32, 125), order="F")
+        self.shpb = np.zeros((6, 32, 125), order="F")
+        self.shglb = np.zeros((6, 3, 32, 125), order="F")
+        for q in range(4):
+            self.shp[0, :4, q] = T["shp"][q]
+            self.shgl[0, :, :4, q] = T["shgl"][q]
+        for q in range(3):
+            self.shpb[0, :4, q] = T["shpb"][q]
+            self.shglb[0, :, :4, q] = T["shglb"][q]
+        self.iBC = case.iBC.astype(np.int64)
+        self.BC = np.asfortranarray(case.BC.T)
+        self.iper = case.iper.astype(np.int64) + 1
+        self.x = np.asfortranarray(case.x)
+        self.ilwork = np.zeros(1, np.int64)
+        self.rerr = np.zeros((N, 10), order="F")
+
+    # ---- routines (flat reference layouts in and out)
+    def ElmMFG(self, y, ac, iprec=1):
+        N = self.N
+        self.G.iprec = iprec
+        yF, acF = _F(np.array(y), (N, 5)), _F(np.array(ac), (N, 5))
+        res, rmes = np.zeros((N, 5), order="F"), np.zeros((N, 5), order="F")
+        bd = np.zeros((N, 5, 5), order="F")
+        self.P.call("elmmfg", yF, acF, self.x, self.shp, self.shgl, self.iBC, self.BC, self.shpb, self.shglb,
+                    res, rmes, bd, self.iper, self.ilwork, self.rerr)
+        self.G.iprec = 1
+        return res.reshape(-1, order="F"), rmes.reshape(-1, order="F"), bd.reshape(-1, order="F")
+
+    def ItrRes(self, yp, yc, ac, rmes):
+        N = self.N
+        rm = _F(np.array(rmes), (N, 5)).copy(order="F")
+        self.P.call("itrres", _F(np.array(yp), (N, 5)), _F(np.array(yc), (N, 5)), self.x, self.shp, self.shgl,
+                    self.iBC, self.BC, self.shpb, self.shglb, rm, self.iper, self.ilwork, _F(np.array(ac), (N, 5)))
+        return rm.reshape(-1, order="F")
+
+    def i3LU(self, bd, r, code):
+        N = self.N
+        bdF = _F(np.array(bd), (N, 5, 5)).copy(order="F")
+        rF = _F(np.array(r), (N, 5)).copy(order="F") if r is not None else np.zeros((N, 5), order="F")
+        self.P.call("i3lu", bdF, rF, _LU[code])
+        return bdF.reshape(-1, order="F"), rF.reshape(-1, order="F")
+
+    def itrBC(self, y, ac):
+        N = self.N
+        yF = _F(np.array(y), (N, 5)).copy(order="F")
+        acF = _F(np.array(ac), (N, 5)).copy(order="F")
+        self.P.call("itrbc", yF, acF, self.iBC, self.BC, self.iper, self.ilwork)
+        return yF.reshape(-1, order="F"), acF.reshape(-1, order="F")
+
+    def SolMFG(self, y, ac, yold, acold):
+        N, K = self.N, self.params["Kspace"]
+        G = self.G
+        res = np.zeros((N, 5), order="F")
+        bd = np.zeros((N, 5, 5), order="F")
+        Dy = np.zeros((N, 5), order="F")
+        HBrg = np.zeros((K + 1, K), order="F")
+        eBrg, yBrg = np.zeros(K + 1), np.zeros(K)
+        Rcos, Rsin = np.zeros(K), np.zeros(K)
+        G.iprec = 1  # itrdrv.f:494 with LHSupd(1) = 1: the block diagonal is rebuilt every solve
+        self.P.call("solmfg", _F(np.array(y), (N, 5)), _F(np.array(ac), (N, 5)), _F(np.array(yold), (N, 5)),
+                    _F(np.array(acold), (N, 5)), self.x, self.iBC, self.BC, res, bd, HBrg, eBrg, yBrg, Rcos, Rsin,
+                    self.iper, self.ilwork, self.shp, self.shgl, self.shpb, self.shglb, Dy, self.rerr)
+        stats = {"iKs": int(G.iks), "lGMRES": int(G.lgmres), "ntotGM": int(G.ntotgm), "eGMRES": float(G.egmres),
+                 "eBrg": eBrg.tolist()}
+        return res.reshape(-1, order="F"), bd.reshape(-1, order="F"), Dy.reshape(-1, order="F"), stats
+
+    def itrSetup(self, rho_inf: float, dt: float):
+        """almi, alfi, gami, Dtgl of itrSetup (itrPC.f:6-46) for one time-sequence entry."""
+        G = self.G
+        G.itseq = 1
+        G.rhoinf[0] = rho_inf
+        G.delt[0] = dt
+        y = np.zeros((self.N, 5), order="F")
+        self.P.call("itrsetup", y, y.copy(order="F"))
+        return {"almi": float(G.almi), "alfi": float(G.alfi), "gami": float(G.gami), "Dtgl": float(G.dtgl)}
+
+    def itrPredict(self, yold, acold):
+        N = self.N
+        y, ac = np.zeros((N, 5), order="F"), np.zeros((N, 5), order="F")
+        self.P.call("itrpredict", _F(np.array(yold), (N, 5)), _F(np.array(acold), (N, 5)), y, ac)
+        return y.reshape(-1, order="F"), ac.reshape(-1, order="F")
+
+    def itrCorrect(self, y, ac, yold, acold, Dy):
+        N = self.N
+        yF, acF = _F(np.array(y), (N, 5)).copy(order="F"), _F(np.array(ac), (N, 5)).copy(order="F")
+        self.P.call("itrcorrect", yF, acF, _F(np.array(yold), (N, 5)), _F(np.array(acold), (N, 5)),
+                    _F(np.array(Dy), (N, 5)))
+        return yF.reshape(-1, order="F"), acF.reshape(-1, order="F")
+
+    def itrUpdate(self, yold, acold, y, ac):
+        N = self.N
+        yoF, aoF = _F(np.array(yold), (N, 5)).copy(order="F"), _F(np.array(acold), (N, 5)).copy(order="F")
+        self.P.call("itrupdate", yoF, aoF, _F(np.array(y), (N, 5)), _F(np.array(ac), (N, 5)))
+        return yoF.reshape(-1, order="F"), aoF.reshape(-1, order="F")
+
+    def time_step(self, yold, acold, nitr: int):
+        """One step in the order of itrdrv.f:398-399, 427-634, 651-652 (matrix-free solve)."""
+        y, ac = self.itrPredict(yold, acold)
+        y, ac = self.itrBC(y, ac)
+        iks = []
+        for it in range(1, nitr + 1):
+            self.G.iter = it
+            _, _, Dy, st = self.SolMFG(y, ac, yold, acold)
+            iks.append(st["iKs"])
+            y, ac = self.itrCorrect(y, ac, yold, acold, Dy)
+            y, ac = self.itrBC(y, ac)
+        yold, acold = self.itrUpdate(yold, acold, y, ac)
+        yold, acold = self.itrBC(yold, acold)
+        return yold, acold, y, ac, iks

@@ -1,0 +1,97 @@
+"""The CPU oracle against golden vectors computed by the reference's own Fortran.
+
+tests/golden/ref_*.npz hold the outputs of the reference routines (ElmMFG,
+ItrRes, i3LU, itrBC, SolMFG, itrSetup, itrPredict/itrCorrect/itrUpdate and one
+two-iteration time step in the order of itrdrv.f), executed from the reference
+sources by tests/golden/make_ref_golden.py, with the seeded inputs they were
+run on.  Tolerances (relative 2-norm):
+  * element routines, LU, boundary conditions: 1e-12 (operation order differs
+    from the Fortran array syntax only in the last bits);
+  * SolMFG: the same Krylov iteration count, eGMRES within 1e-2 and Dy within
+    1e-5: itrFDI divides a second difference of residuals by epsM, so a one-ulp
+    change of the state moves eGMRES by up to ~0.4% and, through Au1MFG, Dy by
+    ~2e-6 on these cases;
+  * time step: y within 1e-9, ac within 1e-7 (the state moves by the
+    finite-difference Dy above, ac by Dtgl/gami times it).
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from helpers import rel
+from oracle import pyoracle
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+sys.path.insert(0, str(GOLDEN))
+from make_ref_golden import CASES  # noqa: E402
+
+FIXTURES = {name: (build, parts) for name, build, parts in CASES}
+
+
+def having(part):
+    return [n for n, (_, parts) in FIXTURES.items() if part in parts]
+
+
+def load(name):
+    path = GOLDEN / f"ref_{name}.npz"
+    d = dict(np.load(path, allow_pickle=False))
+    build, _parts = FIXTURES[name]
+    case, p, y, ac = build()
+    assert np.array_equal(d["ien"], case.ien.astype(np.int32)), "mesh generator changed"
+    assert np.array_equal(d["x"], case.x_ref())
+    assert np.array_equal(d["y"], y) and np.array_equal(d["ac"], ac), "seeded state changed"
+    assert json.loads(str(d["params"])) == json.loads(json.dumps(p, sort_keys=True))
+    return d, case, p
+
+
+@pytest.mark.parametrize("name", list(FIXTURES))
+def test_oracle_elmmfg_matches_reference(name):
+    d, case, p = load(name)
+    o = pyoracle.Oracle(case, p)
+    r, m, b = o.ElmMFG(d["y"], d["ac"])
+    assert rel(r, d["elm_res"]) < 1e-12
+    assert rel(m, d["elm_rmes"]) < 1e-12
+    assert rel(b, d["elm_bd"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", having("pieces"))
+def test_oracle_itrres_lu_itrbc_match_reference(name):
+    d, case, p = load(name)
+    o = pyoracle.Oracle(case, p)
+    assert rel(o.ItrRes(d["yp"], d["y"], d["ac"], d["r0"]), d["itrres_rmes"]) < 1e-12
+    lu, _ = o.i3LU(d["elm_bd"], None, 0)
+    assert rel(lu, d["lu_fact"]) < 1e-12
+    for code, key in ((1, "lu_forward"), (2, "lu_backward"), (3, "lu_product")):
+        assert rel(o.i3LU(d["lu_fact"], d["r0"], code)[1], d[key]) < 1e-12, key
+    yb, ab = o.itrBC(d["yp"], d["ac"])
+    assert rel(yb, d["itrbc_y"]) < 1e-15 and rel(ab, d["itrbc_ac"]) < 1e-15
+
+
+@pytest.mark.parametrize("name", having("solve"))
+def test_oracle_solmfg_matches_reference(name):
+    d, case, p = load(name)
+    o = pyoracle.Oracle(case, p)
+    res, bd, Dy, st = o.SolMFG(d["y"], d["ac"])
+    assert rel(res, d["sol_res"]) < 1e-12
+    assert rel(bd, d["sol_bd"]) < 1e-12
+    assert st.iKs == int(d["sol_iKs"]) and st.lGMRES == int(d["sol_lGMRES"])
+    assert st.ntotGM == int(d["sol_ntotGM"])
+    assert abs(st.eGMRES / float(d["sol_eGMRES"]) - 1.0) < 1e-2
+    assert rel(Dy, d["sol_Dy"]) < 1e-5
+
+
+@pytest.mark.parametrize("name", having("step"))
+def test_oracle_time_step_matches_reference(name):
+    d, case, p = load(name)
+    almi, alfi, gami, Dtgl = d["setup"]
+    assert (p["almi"], p["alfi"], p["gami"], p["Dtgl"]) == (almi, alfi, gami, Dtgl)
+    o = pyoracle.Oracle(case, p)
+    yold, acold, y, ac, stats = o.time_step(d["y"], d["ac"], 2)
+    assert [s.iKs for s in stats] == list(d["step_iks"])
+    assert rel(y, d["step_y"]) < 1e-9 and rel(yold, d["step_yold"]) < 1e-9
+    assert rel(ac, d["step_ac"]) < 1e-7 and rel(acold, d["step_acold"]) < 1e-7
