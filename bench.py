@@ -115,7 +115,7 @@ def make_workload(n: int, precision: str):
     case, ph = mesh.channel_case(n, mach=0.3, re=1000.0)
     prec = L.PHGPU_MIXED if precision == "mixed" else L.PHGPU_FP64
     ap = L.PHGPU_AP_LINEAR if precision == "mixed" else L.PHGPU_AP_FD
-    res = L.PHGPU_RES_GALERKIN64 if precision == "mixed" else L.PHGPU_RES_FP64
+    res = L.PHGPU_RES_SPLITDF if precision == "mixed" else L.PHGPU_RES_FP64
     params = make_params(ph["mu"], ph["dt"], rho_inf=0.5, Kspace=20, etol=1e-3, minIters=1,
                          precision=prec, ap_mode=ap, outer_residual=res)
     y0 = mesh.uniform_state(case, 0.3, sigma=0.01)
@@ -205,7 +205,7 @@ def run_gpu(args, rank, world):
         "metric": "Newton-step throughput to 1e-3 relative nonlinear residual (elements/s)",
         "value": value, "unit": "elements/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": ("f32 assembly/Ap/stabilization; f64 Galerkin residual, dots, Givens, LU"
+        "dtype": ("f32 assembly/Ap/stabilization; double-float Galerkin flux; f64 dots, Givens, LU"
                   if args.precision == "mixed" else "f64"),
         "data": "synthetic",
         "config": {"workload": f"channel {args.n}^3x6 tets Mach0.3 Re1000, Kspace20 tol1e-3, 3 Newton/step",
@@ -237,11 +237,12 @@ def _time_sweep(g, stream, which, reps=10):
 
 # The element sweeps of one mixed-precision Newton iteration and their compulsory
 # HBM bytes (int4 connectivity per element; per node what the sweep must read and write):
-#   resh: FP64-Galerkin outer residual, reads y, ac (f64) and x (f64), writes res (f64)
+#   ress: outer residual, reads y, ac (f64) and x (f64), writes res (f64)
 #   full: FP32 block diagonal, reads y, ac, x (f32), writes BDiag (25 f32)
 #   lin:  FP32 linearized product, reads the direction, base state, x (f32), reads and writes the product
 SWEEPS = {
-    "resh": (6, "k_chunk_resh (FP64 Galerkin + FP32 stabilization residual)", lambda E, N: 16 * E + N * (40 + 40 + 24 + 40)),
+    "ress": (7, "k_chunk_ress (double-float constant flux + FP32 increment residual)",
+             lambda E, N: 16 * E + N * (40 + 40 + 24 + 40)),
     "full": (3, "k_chunk_full<float> (FP32 block diagonal)", lambda E, N: 16 * E + N * (20 + 20 + 12 + 100)),
     "lin": (2, "k_chunk_res<float, RM_LIN> (FP32 linearized Ap sweep)", lambda E, N: 16 * E + N * (20 + 20 + 12 + 40)),
 }
@@ -249,10 +250,11 @@ SWEEPS = {
 
 def kernel_roofline(g, case, stream, args, krylov_per_newton):
     """Time each element sweep alone; the roofline object is the one with the largest share of a Newton iteration."""
-    g.sweep_dev(5)  # FP32 shadows of the state
+    g.sweep_dev(5)  # FP32 copies of the state
+    g.sweep_dev(8)  # hi/lo copies for the split residual
     E, N = case.nelem, case.nshg
     peak, src = peaks()
-    calls = {"resh": 1.0, "full": 1.0, "lin": krylov_per_newton}
+    calls = {"ress": 1.0, "full": 1.0, "lin": krylov_per_newton}
     kernels = {}
     for key, (which, name, algo_f) in SWEEPS.items():
         t = _time_sweep(g, stream, which)

@@ -51,7 +51,7 @@ enum {
 
 enum { PHGPU_FP64 = 0, PHGPU_MIXED = 1 };         /* precision */
 enum { PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1 };     /* Jacobian-vector product */
-enum { PHGPU_RES_FP64 = 0, PHGPU_RES_GALERKIN64 = 1 }; /* outer residual in mixed precision */
+enum { PHGPU_RES_FP64 = 0, PHGPU_RES_GALERKIN64 = 1, PHGPU_RES_SPLITDF = 2 }; /* outer residual in mixed precision */
 enum { PHGPU_LU_FACT = 0, PHGPU_LU_FORWARD = 1, PHGPU_LU_BACKWARD = 2, PHGPU_LU_PRODUCT = 3 };
 
 /* The COMMON-block values the hot path reads (common.h), plus three options
@@ -76,9 +76,12 @@ typedef struct {
     int precision;                   /* PHGPU_FP64: reference arithmetic; PHGPU_MIXED: FP32
                                         assembly and Ap, FP64 outer residual, dots, Givens, LU */
     int ap_mode;                     /* PHGPU_AP_FD (Au1MFG) or PHGPU_AP_LINEAR */
-    int outer_residual;              /* mixed precision only: PHGPU_RES_FP64 (every term FP64) or
+    int outer_residual;              /* mixed precision only: PHGPU_RES_FP64 (every term FP64),
                                         PHGPU_RES_GALERKIN64 (metrics, Euler flux and time term FP64;
-                                        least-squares and viscous terms FP32) */
+                                        least-squares and viscous terms FP32) or PHGPU_RES_SPLITDF
+                                        (no FP64 arithmetic: the Euler flux of each element's node-3
+                                        state in double-float, its increment over the element and
+                                        the other terms in FP32) */
     int reserved[5];
 } phgpu_config;
 
@@ -154,7 +157,10 @@ int phgpu_newton_dev(phgpu_ctx* ctx, phgpu_stats* st);
 int phgpu_time_step_dev(phgpu_ctx* ctx, int nitr, phgpu_stats* st);
 /* nonlinear residual ||R(y)|| (FP64, unpreconditioned, after BCs) of the resident state */
 int phgpu_residual_norm_dev(phgpu_ctx* ctx, double* rnorm);
-/* one FP32/FP64 residual sweep of the resident state (timing probe of the hot kernel) */
+/* one element sweep of the resident state (timing probe of the hot kernels): 0 FP64 residual,
+ * 1 FP64 modified residual, 2 FP32 linearized product, 3 FP32 block diagonal, 4 FP64 block
+ * diagonal + residuals, 5 FP32 copies of the state, 6 FP64-Galerkin residual, 7 double-float
+ * split residual, 8 hi/lo float copies of the state */
 int phgpu_sweep_dev(phgpu_ctx* ctx, int which);
 
 /* Largest 5*nshg that phgpu_rstat_noalloc accepts (33,554,432 values, nshg <= 6,710,886). */

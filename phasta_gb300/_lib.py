@@ -16,7 +16,7 @@ PHGPU_OK = 0
 STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NONFINITE", 4: "SINGULAR", 5: "UNSUPPORTED", 6: "NOMEM", 7: "TOO_LARGE"}
 PHGPU_FP64, PHGPU_MIXED = 0, 1
 PHGPU_AP_FD, PHGPU_AP_LINEAR = 0, 1
-PHGPU_RES_FP64, PHGPU_RES_GALERKIN64 = 0, 1
+PHGPU_RES_FP64, PHGPU_RES_GALERKIN64, PHGPU_RES_SPLITDF = 0, 1, 2
 PHGPU_ERR_INVALID, PHGPU_ERR_TOO_LARGE = 1, 7
 PHGPU_RSTAT_NOALLOC_MAX_N = 33554432
 LU_FACT, LU_FORWARD, LU_BACKWARD, LU_PRODUCT = 0, 1, 2, 3

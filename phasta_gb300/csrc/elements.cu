@@ -17,12 +17,16 @@
 //    quadrature sum (WdetJ is the same at every point of a linear tet).
 // Results agree with the statement-by-statement restatement to rounding.
 #include "phgpu_impl.cuh"
+#include "df64.cuh"
 
 namespace phgpu {
 
 __constant__ TetTables c_tab;
 __constant__ float c_shpf[4][4];   // single-precision copies (no conversions in FP32 kernels)
 __constant__ float c_qwtf;
+
+// tet point weight: symtet.c's 1/4 scaled by 4/3 (genint.f:72)
+constexpr double kTetQwt = (4.0 / 3.0) * 0.25;
 
 void upload_tables(Ctx& C) {
     TetTables t;
@@ -34,7 +38,7 @@ void upload_tables(Ctx& C) {
         t.shp[q][1] = pts[q][1];
         t.shp[q][2] = pts[q][2];
         t.shp[q][3] = 1.0 - pts[q][0] - pts[q][1] - pts[q][2];
-        t.Qwt[q] = (4.0 / 3.0) * 0.25;
+        t.Qwt[q] = kTetQwt;
     }
     // symtri.c 3-point rule, genint.f:73 Qwtb *= 2
     const double A = 0.333333333333333, B = 0.666666666666667, Cc = 0.166666666666667;
@@ -675,6 +679,260 @@ k_chunk_resh(ChunkArgs ca, int chunk0, const double* __restrict__ x, const doubl
 }
 
 // --------------------------------------------------------------------------
+// outer residual (ires = 1) without FP64 arithmetic.  The Euler flux at a
+// quadrature point is split exactly as F(y_q) = F(y_r) + [F(y_q) - F(y_r)],
+// y_r the state of the element's local node 3:
+//   * F(y_r) is constant over the element, so its weighted sum over the four
+//     points is 4 F(y_r) WdetJ shg_a = (Qwt/2) cof'_a F(y_r), cof'_a the
+//     cofactors of the edge matrix x_j - x_3.  These terms are large and cancel
+//     between the elements around a node; they are formed in double-float
+//     arithmetic (df64.cuh) from hi/lo float copies of x and y.
+//   * the increment is written with the exact expansions
+//       rho - rho_r = (dp T_r - p_r dT) / (R T T_r),  m_i - m_ri = drho u_i + rho_r du_i,
+//       m_i u_j - m_ri u_rj = dm_i u_j + m_ri du_j, ...
+//     of increments dy = y_q - y_r formed from the hi/lo copies, so FP32
+//     evaluates it to FP32 accuracy relative to its own (small) size.
+// The time term (e3massr.f:26-58), the least-squares term (e3ls.f) and the
+// viscous flux (e3visc.f) are FP32, as in k_chunk_resh.  Slots and node sums
+// are double-float; each node's sum is added to the FP64 output.
+// --------------------------------------------------------------------------
+struct DfConst {
+    float rRgas_hi, rRgas_lo, cv_hi, cv_lo, wq_hi, wq_lo;  // 1/R, R/(gamma-1), Qwt/2
+};
+
+constexpr int kSplitSlot = 40;  // per element: 20 hi then 20 lo
+
+__device__ __forceinline__ df64 df_diff(float ah, float al, float bh, float bl) {
+    float s, e;
+    two_sum(ah, -bh, s, e);
+    e = __fadd_rn(e, __fsub_rn(al, bl));
+    return quick_two_sum(s, e);
+}
+
+__global__ void __launch_bounds__(kChunk, 3)
+k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float* __restrict__ xlo,
+             const float* __restrict__ yh, const float* __restrict__ ylo, const float* __restrict__ acf,
+             double* __restrict__ out, Phys<float> Pf, DfConst K) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sm = reinterpret_cast<float*>(smem_raw);
+    const int c = chunk0 + blockIdx.x;
+    const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
+    const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+    float* sxh = sm;
+    float* sxl = sxh + 3 * nn;
+    float* syh = sxl + 3 * nn;
+    float* syl = syh + 5 * nn;
+    float* sa = syl + 5 * nn;
+    float* slot = sa + 5 * nn;
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const size_t gn = ca.nodes[n0 + l];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            sxh[3 * l + d] = __ldg(xh + 3 * gn + d);
+            sxl[3 * l + d] = __ldg(xlo + 3 * gn + d);
+        }
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            syh[5 * l + k] = __ldg(yh + 5 * gn + k);
+            syl[5 * l + k] = __ldg(ylo + 5 * gn + k);
+            sa[5 * l + k] = __ldg(acf + 5 * gn + k);
+        }
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < ne) {
+        const ushort4 ln = ca.lien[e0 + threadIdx.x];
+        const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
+        float o32[4][5];
+        {
+            float xl[4][3], yl[4][5], al[4][5], dl[3][5];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) xl[a][d] = sxh[3 * nd[a] + d];
+                lds5(syh, nd[a], yl[a]);
+                lds5(sa, nd[a], al[a]);
+            }
+            // increments from local node 3, from the hi and lo parts
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int k = 0; k < 5; ++k)
+                    dl[a][k] = (yl[a][k] - yl[3][k]) + (syl[5 * nd[a] + k] - syl[5 * nd[3] + k]);
+            Geo<float> geo;
+            geometry(xl, geo);
+            // gradients from the increments (sum_a shg_a = 0): differences of nearby nodal
+            // values keep their own FP32 accuracy instead of that of the values
+            float g[3][5];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 5; ++k)
+                    g[i][k] = geo.shg[0][i] * dl[0][k] + geo.shg[1][i] * dl[1][k] + geo.shg[2][i] * dl[2][k];
+            Visc<float> vs;
+            if (Pf.navier) viscous(Pf, g, vs);
+            const float pr = yl[3][0], Tr = yl[3][4];
+            const float ur[3] = {yl[3][1], yl[3][2], yl[3][3]};
+            const float rhor = pr * Pf.rRgas / Tr;
+            const float mr[3] = {rhor * ur[0], rhor * ur[1], rhor * ur[2]};
+            float S32[3][5], T32[4][5];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 5; ++k) S32[i][k] = 0.f;
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int k = 0; k < 5; ++k) T32[a][k] = 0.f;
+#pragma unroll 1
+            for (int q = 0; q < 4; ++q) {
+                float N[4];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) N[a] = shp<float>(q, a);
+                float bq[5], aq[5], dq[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    bq[k] = N[0] * yl[0][k] + N[1] * yl[1][k] + N[2] * yl[2][k] + N[3] * yl[3][k];
+                    aq[k] = N[0] * al[0][k] + N[1] * al[1][k] + N[2] * al[2][k] + N[3] * al[3][k];
+                    dq[k] = N[0] * dl[0][k] + N[1] * dl[1][k] + N[2] * dl[2][k];
+                }
+                Qp<float> b;
+                qp_state(Pf, bq[0], bq[1], bq[2], bq[3], bq[4], b);
+                qp_tau(Pf, geo, b);
+                float aig[5], a0a[5];
+                ai_gi(b, g, aig);
+                a0_v(b, aq, a0a);
+                float tl[5];
+                tl[0] = b.tau[0] * (aig[0] + a0a[0]);
+                tl[1] = b.tau[1] * (aig[1] + a0a[1]);
+                tl[2] = b.tau[1] * (aig[2] + a0a[2]);
+                tl[3] = b.tau[1] * (aig[3] + a0a[3]);
+                tl[4] = b.tau[2] * (aig[4] + a0a[4]);
+                float F[3][5];
+                // Euler-flux increment F(y_q) - F(y_r) (flux sign of e3conv.f:72-96)
+                const float drho = (dq[0] * Tr - pr * dq[4]) * Pf.rRgas / (Tr * b.T);
+                const float dek = Pf.cv * dq[4] + (ur[0] * dq[1] + ur[1] * dq[2] + ur[2] * dq[3]) +
+                                  0.5f * (dq[1] * dq[1] + dq[2] * dq[2] + dq[3] * dq[3]);
+                const float ek = b.ei + b.rk;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const float dm = drho * b.u[i] + rhor * dq[1 + i];
+                    F[i][0] = -dm;
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) F[i][1 + j] = -(dm * b.u[j] + mr[i] * dq[1 + j]) - (i == j ? dq[0] : 0.f);
+                    F[i][4] = -(dm * ek + mr[i] * dek) - (dq[1 + i] * b.p + ur[i] * dq[0]);
+                }
+                if (Pf.navier) {
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+                        for (int j = 0; j < 3; ++j) F[i][1 + j] += vs.t[i][j];
+                        F[i][4] += b.u[0] * vs.t[i][0] + b.u[1] * vs.t[i][1] + b.u[2] * vs.t[i][2] + vs.q[i];
+                    }
+                }
+                add_ai_v(b, tl, F);
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) S32[i][k] += F[i][k];
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) T32[a][k] += N[a] * a0a[k];
+            }
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int k = 0; k < 5; ++k)
+                    o32[a][k] = geo.WdetJ * (geo.shg[a][0] * S32[0][k] + geo.shg[a][1] * S32[1][k] +
+                                             geo.shg[a][2] * S32[2][k] + T32[a][k]);
+        }
+        // ---- element-constant flux F(y_r) (double-float) ----
+        const int r = nd[3];
+        const df64 p = df_make(syh[5 * r + 0], syl[5 * r + 0]);
+        const df64 u[3] = {df_make(syh[5 * r + 1], syl[5 * r + 1]), df_make(syh[5 * r + 2], syl[5 * r + 2]),
+                           df_make(syh[5 * r + 3], syl[5 * r + 3])};
+        const df64 T = df_make(syh[5 * r + 4], syl[5 * r + 4]);
+        const df64 rho = df_mul(p, df_mul(df_make(K.rRgas_hi, K.rRgas_lo), df_rcp(T)));
+        df64 rk = df_add(df_add(df_mul(u[0], u[0]), df_mul(u[1], u[1])), df_mul(u[2], u[2]));
+        rk.hi *= 0.5f;
+        rk.lo *= 0.5f;
+        const df64 ek = df_add(df_mul(df_make(K.cv_hi, K.cv_lo), T), rk);
+        df64 F[3][5];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const df64 m = df_mul(rho, u[i]);
+            F[i][0] = df_neg(m);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                F[i][1 + j] = df_neg(df_mul(m, u[j]));
+                if (i == j) F[i][1 + j] = df_sub(F[i][1 + j], p);
+            }
+            F[i][4] = df_neg(df_add(df_mul(m, ek), df_mul(u[i], p)));
+        }
+        // cofactors of the edge matrix d'[i][j] = x_j,i - x_3,i (the geometry() layout)
+        df64 d[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                d[i][j] = df_diff(sxh[3 * nd[j] + i], sxl[3 * nd[j] + i], sxh[3 * r + i], sxl[3 * r + i]);
+        auto minor2 = [](df64 a, df64 b, df64 c2, df64 e) { return df_sub(df_mul(a, b), df_mul(c2, e)); };
+        df64 cof[3][3];
+        cof[0][0] = minor2(d[1][1], d[2][2], d[2][1], d[1][2]);
+        cof[0][1] = minor2(d[2][1], d[0][2], d[0][1], d[2][2]);
+        cof[0][2] = minor2(d[0][1], d[1][2], d[0][2], d[1][1]);
+        cof[1][0] = minor2(d[1][2], d[2][0], d[1][0], d[2][2]);
+        cof[1][1] = minor2(d[0][0], d[2][2], d[2][0], d[0][2]);
+        cof[1][2] = minor2(d[1][0], d[0][2], d[0][0], d[1][2]);
+        cof[2][0] = minor2(d[1][0], d[2][1], d[1][1], d[2][0]);
+        cof[2][1] = minor2(d[2][0], d[0][1], d[0][0], d[2][1]);
+        cof[2][2] = minor2(d[0][0], d[1][1], d[0][1], d[1][0]);
+        const df64 wq = df_make(K.wq_hi, K.wq_lo);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) cof[a][i] = df_mul(cof[a][i], wq);
+        float* sl = slot + kSplitSlot * threadIdx.x;
+        df64 s3[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s3[k] = df_make(0.f, 0.f);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                const df64 g64 = df_add(df_add(df_mul(cof[a][0], F[0][k]), df_mul(cof[a][1], F[1][k])),
+                                        df_mul(cof[a][2], F[2][k]));
+                s3[k] = df_add(s3[k], g64);
+                const df64 v = df_add(g64, o32[a][k]);
+                sl[5 * a + k] = v.hi;
+                sl[20 + 5 * a + k] = v.lo;
+            }
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const df64 v = df_add(df_neg(s3[k]), o32[3][k]);  // shg_3 = -(shg_0 + shg_1 + shg_2)
+            sl[15 + k] = v.hi;
+            sl[35 + k] = v.lo;
+        }
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        df64 acc[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) acc[k] = df_make(0.f, 0.f);
+        const int s0 = ca.cstart[n0 + l], s1 = ca.cstart[n0 + l + 1];
+        for (int s = s0; s < s1; ++s) {
+            const int sid = (int)ca.csr[s];
+            const float* sl = slot + kSplitSlot * (sid >> 2) + 5 * (sid & 3);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) acc[k] = df_add(acc[k], df_make(sl[k], sl[20 + k]));
+        }
+        double* og = out + 5 * (size_t)ca.nodes[n0 + l];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) og[k] += df_to_double(acc[k]);
+    }
+}
+
+// --------------------------------------------------------------------------
 // ElmMFG interior (ires = 3, iprec = 1): res, rmes and BDiag of node a of one
 // element; the quadrature-point state is evaluated by each of the four
 // threads of an element.  35 outputs: res 0-4, rmes 5-9, BDiag 10-34.
@@ -1094,6 +1352,12 @@ size_t full_smem(const Ctx& C) {
 size_t resh_smem(const Ctx& C) {
     return sizeof(double) * ((size_t)C.chunk_lmax * 13 + (size_t)kChunk * 20) + sizeof(float) * (size_t)C.chunk_lmax * 13;
 }
+size_t ress_smem(const Ctx& C) { return sizeof(float) * ((size_t)C.chunk_lmax * 21 + (size_t)kChunk * kSplitSlot); }
+
+static void split(double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
 
 template <typename R>
 int configure_chunk_kernels(Ctx& C) {
@@ -1115,6 +1379,9 @@ int configure_element_kernels(Ctx& C) {
     if (rc == PHGPU_OK) rc = configure_chunk_kernels<float>(C);
     if (rc == PHGPU_OK)
         rc = check(C, cudaFuncSetAttribute(k_chunk_resh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)resh_smem(C)),
+                   "cudaFuncSetAttribute");
+    if (rc == PHGPU_OK)
+        rc = check(C, cudaFuncSetAttribute(k_chunk_ress, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ress_smem(C)),
                    "cudaFuncSetAttribute");
     return rc;
 }
@@ -1153,6 +1420,23 @@ void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf
         const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
         if (nc <= 0) continue;
         k_chunk_resh<<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_x, y, ac, C.d_xf, yf, acf, out, P, Pf);
+        ++C.launches;
+    }
+}
+
+void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* acf, double* out) {
+    const Phys<float> Pf = make_phys<float>(C.cfg);
+    DfConst K;
+    split(1.0 / C.cfg.Rgas, K.rRgas_hi, K.rRgas_lo);
+    split(C.cfg.Rgas / C.cfg.gamma1, K.cv_hi, K.cv_lo);
+    split(0.5 * kTetQwt, K.wq_hi, K.wq_lo);
+    const ChunkArgs ca = chunk_args(C);
+    const size_t sm = ress_smem(C);
+    const int ncol = (int)C.chunk_col_start.size() - 1;
+    for (int c = 0; c < ncol; ++c) {
+        const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
+        if (nc <= 0) continue;
+        k_chunk_ress<<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K);
         ++C.launches;
     }
 }

@@ -70,6 +70,7 @@ struct Ctx {
 
     double* d_x = nullptr;        // N*3
     float* d_xf = nullptr;        // N*3
+    float* d_xlo = nullptr;       // N*3: x - (double)d_xf, rounded to float
     int* d_iBC = nullptr;         // N
     double* d_BC = nullptr;       // N*6  [n][6]
     float* d_BCf = nullptr;
@@ -86,6 +87,7 @@ struct Ctx {
     // state (FP64 master copies + FP32 shadows)
     double *d_y = nullptr, *d_ac = nullptr, *d_yold = nullptr, *d_acold = nullptr;
     float *d_yf = nullptr, *d_acf = nullptr;
+    float* d_ylo = nullptr;       // y - (double)d_yf, rounded to float (double-float residual)
 
     // work arrays
     double *d_res = nullptr, *d_rmes = nullptr, *d_bd = nullptr, *d_Dy = nullptr, *d_bdstage = nullptr;
@@ -131,6 +133,8 @@ template <typename R>
 void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rmes, R* bd);
 void launch_boundary(Ctx& C, const double* y, double* res);
 void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf, const float* acf, double* out);
+// outer residual with no FP64 arithmetic: double-float element-constant flux + FP32 increments
+void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* acf, double* out);
 void upload_tables(Ctx& C);
 int build_chunks(Ctx& C, const int* ien, const double* x_ref);
 int configure_element_kernels(Ctx& C);
@@ -149,6 +153,8 @@ void dev_to_ref_res(Ctx& C, const double* d_in, double* d_tmp, double* h_ref);
 void ref_to_dev_bd(Ctx& C, const double* h_ref, double* d_tmp, double* d_out);
 void dev_to_ref_bd(Ctx& C, const double* d_in, double* d_tmp, double* h_ref);
 void to_f32(Ctx& C, const double* a, float* b, size_t n);
+// hi = (float)a, lo = (float)(a - hi): the double-float pair of each value
+void split_f32(Ctx& C, const double* a, float* hi, float* lo, size_t n);
 void to_f64(Ctx& C, const float* a, double* b, size_t n);
 void fill0(Ctx& C, void* p, size_t bytes);
 

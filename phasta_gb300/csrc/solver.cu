@@ -11,6 +11,7 @@
 #include <type_traits>
 
 #include "phgpu_impl.cuh"
+#include "df64.cuh"
 
 namespace phgpu {
 
@@ -164,15 +165,30 @@ __global__ void k_backsolve(double* __restrict__ s, int K, int iKs) {
     }
 }
 
-// Dy = Dy + sum_j yBrg(j) u_j (solmfg.f:338-340)
+// Dy = Dy + sum_j yBrg(j) u_j (solmfg.f:338-340).  FP32 Krylov vectors: the sum over j
+// runs in double-float (coefficients split once per block), then one FP64 add per entry.
 template <typename V>
 __global__ void k_update_dy(double* __restrict__ Dy, const V* __restrict__ U, size_t ld, int iKs,
                             const double* __restrict__ s, size_t n) {
     const double* yB = s + S_YB;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        double d = Dy[i];
-        for (int j = 0; j < iKs; ++j) d = d + yB[j] * (double)U[(size_t)j * ld + i];
-        Dy[i] = d;
+    if constexpr (std::is_same<V, float>::value) {
+        __shared__ float ch[kMaxK], cl[kMaxK];
+        for (int j = threadIdx.x; j < iKs; j += blockDim.x) {
+            ch[j] = (float)yB[j];
+            cl[j] = (float)(yB[j] - (double)ch[j]);
+        }
+        __syncthreads();
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+            df64 acc{0.f, 0.f};
+            for (int j = 0; j < iKs; ++j) acc = df_add(acc, df_mul(df_make(ch[j], cl[j]), U[(size_t)j * ld + i]));
+            Dy[i] = Dy[i] + df_to_double(acc);
+        }
+    } else {
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+            double d = Dy[i];
+            for (int j = 0; j < iKs; ++j) d = d + yB[j] * (double)U[(size_t)j * ld + i];
+            Dy[i] = d;
+        }
     }
 }
 
@@ -487,11 +503,13 @@ int solmfg_dev(Ctx& C, phgpu_stats* st) {
         if (C.cfg.ap_mode != PHGPU_AP_LINEAR)
             return fail(C, PHGPU_ERR_UNSUPPORTED, "mixed precision needs the linearized Jacobian-vector product");
         // outer residual (FP64, or FP64 Galerkin + FP32 stabilization); FP32 block-diagonal tangent
-        to_f32(C, C.d_y, C.d_yf, n5);
+        if (C.cfg.outer_residual == PHGPU_RES_SPLITDF) split_f32(C, C.d_y, C.d_yf, C.d_ylo, n5);
+        else to_f32(C, C.d_y, C.d_yf, n5);
         to_f32(C, C.d_ac, C.d_acf, n5);
-        if (C.cfg.outer_residual == PHGPU_RES_GALERKIN64) {
+        if (C.cfg.outer_residual == PHGPU_RES_GALERKIN64 || C.cfg.outer_residual == PHGPU_RES_SPLITDF) {
             fill0(C, C.d_res, sizeof(double) * n5);
-            launch_elem_resh(C, C.d_y, C.d_ac, C.d_yf, C.d_acf, C.d_res);
+            if (C.cfg.outer_residual == PHGPU_RES_SPLITDF) launch_elem_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res);
+            else launch_elem_resh(C, C.d_y, C.d_ac, C.d_yf, C.d_acf, C.d_res);
             if (C.Eb > 0) launch_boundary(C, C.d_y, C.d_res);
             bc3res<double>(C, C.d_res);
         } else {
@@ -637,11 +655,15 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     }
     // node arrays
     std::vector<double> x(3 * (size_t)N), bc(6 * (size_t)N);
-    std::vector<float> xf(3 * (size_t)N);
+    std::vector<float> xf(3 * (size_t)N), xlo(3 * (size_t)N);
     for (int n = 0; n < N; ++n) {
         for (int d = 0; d < 3; ++d) {
             x[3 * (size_t)n + d] = m->x[(size_t)d * N + n];
-            xf[3 * (size_t)n + d] = (float)x[3 * (size_t)n + d];
+        {
+            const size_t i = 3 * (size_t)n + d;
+            xf[i] = (float)x[i];
+            xlo[i] = (float)(x[i] - (double)xf[i]);
+        }
         }
         for (int k = 0; k < 6; ++k) bc[6 * (size_t)n + k] = m->BC[(size_t)k * N + n];
     }
@@ -675,6 +697,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     T(dalloc(C, &C.d_BCB, 18 * (size_t)std::max(C.Eb, 1)));
     T(dalloc(C, &C.d_x, 3 * (size_t)N));
     T(dalloc(C, &C.d_xf, 3 * (size_t)N));
+    T(dalloc(C, &C.d_xlo, 3 * (size_t)N));
     T(dalloc(C, &C.d_iBC, N));
     T(dalloc(C, &C.d_BC, 6 * (size_t)N));
     T(dalloc(C, &C.d_iper, N));
@@ -687,7 +710,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
         T(dalloc(C, p, n5));
     T(dalloc(C, &C.d_bd, 25 * (size_t)N));
     T(dalloc(C, &C.d_bdstage, 25 * (size_t)N));
-    for (float** p : {&C.d_yf, &C.d_acf, &C.d_resf, &C.d_rmesf, &C.d_t32, &C.d_t32b}) T(dalloc(C, p, n5));
+    for (float** p : {&C.d_yf, &C.d_ylo, &C.d_acf, &C.d_resf, &C.d_rmesf, &C.d_t32, &C.d_t32b}) T(dalloc(C, p, n5));
     T(dalloc(C, &C.d_bdf, 25 * (size_t)N));
     {
         const size_t vb = (cfg->precision == PHGPU_FP64) ? sizeof(double) : sizeof(float);
@@ -714,6 +737,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     up(C.d_BCB, bcb.data(), sizeof(double) * bcb.size());
     up(C.d_x, x.data(), sizeof(double) * x.size());
     up(C.d_xf, xf.data(), sizeof(float) * xf.size());
+    up(C.d_xlo, xlo.data(), sizeof(float) * xlo.size());
     up(C.d_iBC, m->iBC, sizeof(int) * N);
     up(C.d_BC, bc.data(), sizeof(double) * bc.size());
     up(C.d_iper, m->iper, sizeof(int) * N);
@@ -742,9 +766,9 @@ int phgpu_destroy(phgpu_ctx* h) {
     Ctx& C = h->c;
     if (C.stream) cudaStreamSynchronize(C.stream);
     void* ptrs[] = {C.d_ch_elem, C.d_ch_node, C.d_ch_nodes, C.d_ch_cstart, C.d_ch_csr, C.d_ch_lien,
-                    C.d_bdstage, C.d_ien, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
+                    C.d_bdstage, C.d_ien, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_xlo, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
                     C.d_slaves, C.d_mst, C.d_slv_start, C.d_slv, C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_res,
-                    C.d_rmes, C.d_Dy, C.d_ypre, C.d_t64, C.d_t64b, C.d_bd, C.d_yf, C.d_acf, C.d_resf, C.d_rmesf,
+                    C.d_rmes, C.d_Dy, C.d_ypre, C.d_t64, C.d_t64b, C.d_bd, C.d_yf, C.d_ylo, C.d_acf, C.d_resf, C.d_rmesf,
                     C.d_t32, C.d_t32b, C.d_bdf, C.d_U, C.d_scal, C.d_part, C.d_count, C.d_flag};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -990,6 +1014,13 @@ int phgpu_sweep_dev(phgpu_ctx* h, int which) {
             break;
         case 6:  // FP64-Galerkin / FP32-stabilization residual
             launch_elem_resh(C, C.d_y, C.d_ac, C.d_yf, C.d_acf, C.d_res);
+            break;
+        case 7:  // double-float constant flux + FP32 increments (needs the hi/lo split of case 8)
+            launch_elem_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res);
+            break;
+        case 8:
+            split_f32(C, C.d_y, C.d_yf, C.d_ylo, n5);
+            to_f32(C, C.d_ac, C.d_acf, n5);
             break;
         default:
             return PHGPU_ERR_INVALID;

@@ -206,3 +206,25 @@ def test_galerkin64_outer_residual_against_fp64(gpu_lib):
     assert st.rnorm == pytest.approx(r64, rel=1e-5)
     y1, a1, st1 = g.newton(y, ac, y, ac)
     assert np.linalg.norm(o.ElmRes(y1, a1)) < 0.05 * r64
+
+
+@pytest.mark.parametrize("which", ["channel", "vortex"])
+def test_split_double_float_outer_residual(gpu_lib, which):
+    """Outer residual with no FP64 arithmetic (double-float element-constant Euler flux, FP32
+    increments and stabilization) against the FP64 outer residual of the same mixed solve.
+
+    The runs share the FP32 block diagonal, so res = L^-1 R differs only through R.  The
+    gradients come from double-float node differences, so the FP32 stabilization, viscous
+    and time terms carry FP32 accuracy relative to their own size, as does the flux
+    increment over an element.  Tolerances: 1e-6 relative on the channel (observed 2e-7);
+    1e-5 on the 8^3 vortex (observed 4e-6), whose elements span 2 pi / 8, so the increments
+    are as large as the flux itself; in both cases at least 3x closer to FP64 than the
+    FP64-Galerkin hybrid, whose FP32 gradients of rounded nodal values are less accurate."""
+    case, p, y, ac = channel(16, ac_scale=0.05) if which == "channel" else vortex(8)
+    base = dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR)
+    r64, _, _, s64 = GpuSolver(case, dict(base, outer_residual=L.PHGPU_RES_FP64)).SolMFG(y, ac)
+    rdf, _, _, sdf = GpuSolver(case, dict(base, outer_residual=L.PHGPU_RES_SPLITDF)).SolMFG(y, ac)
+    rgl, _, _, sgl = GpuSolver(case, dict(base, outer_residual=L.PHGPU_RES_GALERKIN64)).SolMFG(y, ac)
+    assert rel(rdf, r64) < (1e-6 if which == "channel" else 1e-5)
+    assert sdf.rnorm == pytest.approx(s64.rnorm, rel=1e-7)
+    assert rel(rdf, r64) < rel(rgl, r64) / 3
