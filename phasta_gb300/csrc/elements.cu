@@ -19,6 +19,22 @@
 #include "phgpu_impl.cuh"
 #include "df64.cuh"
 
+// occupancy targets (resident CTAs per SM) of the FP32 chunk kernels
+#ifndef PHGPU_RES32_MINB
+#define PHGPU_RES32_MINB 4
+#endif
+#ifndef PHGPU_FULL32_MINB
+#define PHGPU_FULL32_MINB 3
+#endif
+#ifndef PHGPU_RESS_MINB
+#define PHGPU_RESS_MINB 3
+#endif
+#ifndef PHGPU_RES_QUNROLL
+#define PHGPU_RES_QUNROLL 1
+#endif
+#define PH_STR(x) #x
+#define PH_UNROLL(n) _Pragma(PH_STR(unroll n))
+
 namespace phgpu {
 
 __constant__ TetTables c_tab;
@@ -330,7 +346,7 @@ __device__ __forceinline__ void elem_res(const Phys<R>& P, const R (&xl)[4][3], 
 #pragma unroll
         for (int k = 0; k < 5; ++k) Tn[a][k] = R(0);
 
-#pragma unroll 1
+    PH_UNROLL(PHGPU_RES_QUNROLL)
     for (int q = 0; q < 4; ++q) {
         R N[4];
 #pragma unroll
@@ -426,7 +442,7 @@ __device__ __forceinline__ void elem_res(const Phys<R>& P, const R (&xl)[4][3], 
 }
 
 template <typename R, int MODE>
-__global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? PHGPU_RES32_MINB : 2)
 k_chunk_res(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restrict__ ya,
             const R* __restrict__ yb, const R* __restrict__ ac, R* __restrict__ out, Phys<R> P, int iabres,
             const int* __restrict__ skip) {
@@ -709,7 +725,7 @@ __device__ __forceinline__ df64 df_diff(float ah, float al, float bh, float bl) 
     return quick_two_sum(s, e);
 }
 
-__global__ void __launch_bounds__(kChunk, 3)
+__global__ void __launch_bounds__(kChunk, PHGPU_RESS_MINB)
 k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float* __restrict__ xlo,
              const float* __restrict__ yh, const float* __restrict__ ylo, const float* __restrict__ acf,
              double* __restrict__ out, Phys<float> Pf, DfConst K) {
@@ -1118,7 +1134,7 @@ __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R 
 }
 
 template <typename R>
-__global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? PHGPU_FULL32_MINB : 2)
 k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restrict__ y, const R* __restrict__ ac,
              R* __restrict__ res, R* __restrict__ rmes, R* __restrict__ bd, Phys<R> P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
