@@ -46,7 +46,7 @@ def build_reference_shape(force: bool = False) -> Path | None:
     shapesrc = REFERENCE / "shapeFunction" / "src"
     if not (common / "symtet.c").exists() or not shapesrc.exists():
         return None
-    if REF_LIB.exists() and not force:
+    if REF_LIB.exists() and not force and REF_LIB.stat().st_mtime >= Path(__file__).stat().st_mtime:
         return REF_LIB
     inc = REF_DIR / "include"
     inc.mkdir(parents=True, exist_ok=True)
@@ -54,14 +54,20 @@ def build_reference_shape(force: bool = False) -> Path | None:
     (inc / "FCMangle.h").write_text(
         "#define FortranCInterface_GLOBAL(name,NAME) name##_\n"
         "#define FortranCInterface_GLOBAL_(name,NAME) name##_\n")
-    srcs = [common / "symtet.c", common / "symtri.c"]
+    # tet/triangle rules and shapes; hex, wedge and quadrilateral rules (symhex.c, symwdg.c,
+    # symquad.c, symquadw.c) with the hex/wedge shapes (shphex.c, shp6w.c -> newshape.cc)
+    srcs = [common / n for n in ("symtet.c", "symtri.c", "symhex.c", "symwdg.c", "symquad.c", "symquadw.c",
+                                 "shphex.c", "shp6w.c")]
     srcs += sorted(p for p in shapesrc.glob("*.c"))
     objs = []
     for s in srcs:
         o = REF_DIR / (s.stem + ".o")
         _run(["gcc", "-O2", "-fPIC", "-I", str(inc), "-I", str(shapesrc), "-c", str(s), "-o", str(o)])
         objs.append(o)
-    _run(["gcc", "-shared", "-o", str(REF_LIB), *map(str, objs), "-lm"])
+    o = REF_DIR / "newshape.o"
+    _run(["g++", "-O2", "-fPIC", "-I", str(common), "-c", str(common / "newshape.cc"), "-o", str(o)])
+    objs.append(o)
+    _run(["g++", "-shared", "-o", str(REF_LIB), *map(str, objs), "-lm"])
     return REF_LIB
 
 

@@ -92,21 +92,97 @@ const Tables& tables() {
     return t;
 }
 
+// interior element topologies (lcsyst 1 tet, 2 hex, 3 wedge), linear basis (ipord = 1)
+struct Topo {
+    int lcsyst, nshl, ngauss;
+    double shp[8][8];      // [q][a]
+    double shgl[8][3][8];  // [q][i][a]
+    double Qwt[8];
+};
+
+Topo make_topo(int lcsyst) {
+    Topo t{};
+    t.lcsyst = lcsyst;
+    if (lcsyst == 1) {
+        const Tables& T = tables();
+        t.nshl = 4;
+        t.ngauss = 4;
+        for (int q = 0; q < 4; ++q) {
+            t.Qwt[q] = T.Qwt[q];
+            for (int a = 0; a < 4; ++a) {
+                t.shp[q][a] = T.shp[q][a];
+                for (int i = 0; i < 3; ++i) t.shgl[q][i][a] = T.shgl[q][i][a];
+            }
+        }
+    } else if (lcsyst == 2) {
+        // symhex.c 2-point Gauss rule per direction (xi fastest), weights 1 (genint.f: no scaling);
+        // HexShapeAndDrv (newshape.cc) p = 1: trilinear vertex modes, node order
+        // (-,-,-), (+,-,-), (+,+,-), (-,+,-), then zeta = +1
+        const double g = 0.577350269189626;
+        const double sgn[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                  {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+        t.nshl = 8;
+        t.ngauss = 8;
+        for (int q = 0; q < 8; ++q) {
+            const double par[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
+            t.Qwt[q] = 1.0;
+            for (int a = 0; a < 8; ++a) {
+                const double f[3] = {(1.0 + sgn[a][0] * par[0]) / 2.0, (1.0 + sgn[a][1] * par[1]) / 2.0,
+                                     (1.0 + sgn[a][2] * par[2]) / 2.0};
+                t.shp[q][a] = f[0] * f[1] * f[2];
+                t.shgl[q][0][a] = sgn[a][0] / 2.0 * f[1] * f[2];
+                t.shgl[q][1][a] = f[0] * sgn[a][1] / 2.0 * f[2];
+                t.shgl[q][2][a] = f[0] * f[1] * sgn[a][2] / 2.0;
+            }
+        }
+    } else {
+        // symwdg.c 2-point rule: triangle points (1/6,1/6), (2/3,1/6), (1/6,2/3) x zeta = -+1/sqrt(3),
+        // weight 2/3 each; WedgeShapeAndDrv p = 1: N = L_a (1 -+ zeta)/2, L = (1-r-s, r, s), with the
+        // in-plane derivatives taken on a parent triangle of area 2 (half of d/dr, d/ds; the weights
+        // sum to 4)
+        const double P3 = 0.166666666666667, P4 = 0.666666666666667, Q = 0.577350269189626;
+        const double W = 0.666666666666667;
+        const double tri[3][2] = {{P3, P3}, {P4, P3}, {P3, P4}};
+        t.nshl = 6;
+        t.ngauss = 6;
+        for (int q = 0; q < 6; ++q) {
+            const double r = tri[q % 3][0], s2 = tri[q % 3][1], z = q < 3 ? -Q : Q;
+            const double L[3] = {1.0 - r - s2, r, s2};
+            const double dLr[3] = {-1.0, 1.0, 0.0}, dLs[3] = {-1.0, 0.0, 1.0};
+            t.Qwt[q] = W;
+            for (int a = 0; a < 6; ++a) {
+                const int v = a % 3;
+                const double zs = a < 3 ? -1.0 : 1.0;
+                const double fz = (1.0 + zs * z) / 2.0;
+                t.shp[q][a] = L[v] * fz;
+                t.shgl[q][0][a] = dLr[v] * fz / 2.0;
+                t.shgl[q][1][a] = dLs[v] * fz / 2.0;
+                t.shgl[q][2][a] = L[v] * zs / 2.0;
+            }
+        }
+    }
+    return t;
+}
+
+const Topo& topo(int lcsyst) {
+    static const Topo t[3] = {make_topo(1), make_topo(2), make_topo(3)};
+    return t[lcsyst - 1];
+}
+
 // ---------------------------------------------------------------------------
 // e3.f for one element (lhs = 0, idiff = 0, iLES = iRANS = iLSet = 0, iDC = 0,
 // no body force, ipord = 1, itau = 0)
 // ---------------------------------------------------------------------------
-void e3_element(const or_common& c, int ires, int iprec, const double (*yl)[5],
+void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const double (*yl)[5],
                 const double (*ycl)[5], const double (*acl)[5], const double (*xl)[3],
                 double (*rl)[5], double (*rml)[5], double (*bdl)[5][5]) {
-    const Tables& T = tables();
-    const int nshl = 4, nenl = 4, ngauss = 4;
+    const int nshl = tp.nshl, nenl = tp.nshl, ngauss = tp.ngauss;
     const double Rgas = c.Rgas, gamma = c.gamma, gamma1 = c.gamma1;
 
     for (int intp = 0; intp < ngauss; ++intp) {
-        if (T.Qwt[intp] == zero) continue;  // e3.f:110
-        const double* shape = T.shp[intp];
-        const double (*shgl)[4] = T.shgl[intp];
+        if (tp.Qwt[intp] == zero) continue;  // e3.f:110
+        const double* shape = tp.shp[intp];
+        const double (*shgl)[8] = tp.shgl[intp];
         double ri[20] = {0}, rmi[20] = {0};
 
         // ---------------- e3ivar.f:96-156 ----------------
@@ -172,8 +248,8 @@ void e3_element(const or_common& c, int ires, int iprec, const double (*yl)[5],
         dxidx[2][0] = (dxdxi[1][0] * dxdxi[2][1] - dxdxi[1][1] * dxdxi[2][0]) * tmp;
         dxidx[2][1] = (dxdxi[2][0] * dxdxi[0][1] - dxdxi[0][0] * dxdxi[2][1]) * tmp;
         dxidx[2][2] = (dxdxi[0][0] * dxdxi[1][1] - dxdxi[0][1] * dxdxi[1][0]) * tmp;
-        const double WdetJ = T.Qwt[intp] / tmp;
-        double shg[4][3];
+        const double WdetJ = tp.Qwt[intp] / tmp;
+        double shg[8][3];
         for (int n = 0; n < nshl; ++n)
             for (int i = 0; i < 3; ++i)
                 shg[n][i] = shgl[0][n] * dxidx[0][i] + shgl[1][n] * dxidx[1][i] +
@@ -286,9 +362,20 @@ void e3_element(const or_common& c, int ires, int iprec, const double (*yl)[5],
                 rLyi[k] = s;
             }
 
-        // ---------------- e3tau.f:140-181 (itau = 0) + e3gijd tet branch 1440-1470 ----------------
+        // ---------------- e3tau.f:140-181 (itau = 0) + e3gijd (e3tau.f:1397-1508) ----------------
         double gijd[6];
-        {
+        if (tp.lcsyst >= 2) {
+            // hexes and wedges: dxidx^T dxidx (e3tau.f:1408-1425)
+            auto col = [&](int i, int j) {
+                return dxidx[0][i] * dxidx[0][j] + dxidx[1][i] * dxidx[1][j] + dxidx[2][i] * dxidx[2][j];
+            };
+            gijd[0] = col(0, 0);
+            gijd[1] = col(0, 1);
+            gijd[2] = col(1, 1);
+            gijd[3] = col(0, 2);
+            gijd[4] = col(1, 2);
+            gijd[5] = col(2, 2);
+        } else {
             const double c1 = 1.259921049894873e+00, c2 = 6.299605249474365e-01;
             double t1, t2, t3;
             t1 = c1 * dxidx[0][0] + c2 * (dxidx[1][0] + dxidx[2][0]);
@@ -621,6 +708,35 @@ void parallel_for(int n, int nthreads, F&& f) {
     for (auto& x : th) x.join();
 }
 
+// gather (localy.f, localx.f), e3, scatter (local.f:66-80) of one interior element
+void one_element(const or_common& c, const Topo& tp, const or_mesh& m, const int* ie, int ires, int iprec,
+                 const double* yp, const double* yc, const double* ac, double* res, double* rmes, double* bd,
+                 int iabres) {
+    const int nshg = m.nshg, nen = tp.nshl;
+    double yl[8][5], ycl[8][5], acl[8][5], xl[8][3];
+    for (int a = 0; a < nen; ++a) {
+        gather_y(yp, nshg, ie[a], yl[a]);
+        gather_y(yc, nshg, ie[a], ycl[a]);
+        gather_y(ac, nshg, ie[a], acl[a]);
+        gather_x(m.x, nshg, ie[a], xl[a]);
+    }
+    double rl[8][5] = {{0}}, rml[8][5] = {{0}}, bdl[8][5][5] = {{{0}}};
+    e3_element(c, tp, ires, iprec, yl, ycl, acl, xl, rl, rml, iprec ? bdl : nullptr);
+    if (iabres == 1)
+        for (int a = 0; a < nen; ++a)
+            for (int k = 0; k < 5; ++k) rml[a][k] = std::fabs(rml[a][k]);
+    // res rows in equation order
+    for (int k = 0; k < 5; ++k)
+        for (int a = 0; a < nen; ++a) {
+            if (res && (ires == 1 || ires == 3)) res[k * (size_t)nshg + ie[a]] += rl[a][k];
+            if (rmes && (ires == 2 || ires == 3)) rmes[k * (size_t)nshg + ie[a]] += rml[a][k];
+        }
+    if (iprec && bd)
+        for (int j = 0; j < 5; ++j)
+            for (int i = 0; i < 5; ++i)
+                for (int a = 0; a < nen; ++a) bd[(i + 5 * j) * (size_t)nshg + ie[a]] += bdl[a][i][j];
+}
+
 // Interior element loop shared by ElmMFG / ItrRes / residual-only.
 // ires 3: res, rmes, (BDiag if iprec); ires 2: rmes from (yp, yc); ires 1: res.
 void element_sweep(const or_common& c, const or_mesh& m, int ires, int iprec,
@@ -636,35 +752,16 @@ void element_sweep(const or_common& c, const or_mesh& m, int ires, int iprec,
         const int nb = b1 - b0;
         auto run_block = [&](int bi) {
             const int blk = b0 + bi;
-            for (int e = m.blk_start[blk]; e < m.blk_start[blk + 1]; ++e) {
-                const int* ie = m.ien + 4 * (size_t)e;
-                double yl[4][5], ycl[4][5], acl[4][5], xl[4][3];
-                for (int a = 0; a < 4; ++a) {
-                    gather_y(yp, nshg, ie[a], yl[a]);
-                    gather_y(yc, nshg, ie[a], ycl[a]);
-                    gather_y(ac, nshg, ie[a], acl[a]);
-                    gather_x(m.x, nshg, ie[a], xl[a]);
-                }
-                double rl[4][5] = {{0}}, rml[4][5] = {{0}}, bdl[4][5][5] = {{{0}}};
-                e3_element(c, ires, iprec, yl, ycl, acl, xl, rl, rml, iprec ? bdl : nullptr);
-                if (iabres == 1)
-                    for (int a = 0; a < 4; ++a)
-                        for (int k = 0; k < 5; ++k) rml[a][k] = std::fabs(rml[a][k]);
-                // local.f:66-80 scatter (res rows in equation order)
-                for (int k = 0; k < 5; ++k)
-                    for (int a = 0; a < 4; ++a) {
-                        if (res && (ires == 1 || ires == 3)) res[k * (size_t)nshg + ie[a]] += rl[a][k];
-                        if (rmes && (ires == 2 || ires == 3)) rmes[k * (size_t)nshg + ie[a]] += rml[a][k];
-                    }
-                if (iprec && bd)
-                    for (int j = 0; j < 5; ++j)
-                        for (int i = 0; i < 5; ++i)
-                            for (int a = 0; a < 4; ++a)
-                                bd[(i + 5 * j) * (size_t)nshg + ie[a]] += bdl[a][i][j];
-            }
+            for (int e = m.blk_start[blk]; e < m.blk_start[blk + 1]; ++e)
+                one_element(c, topo(1), m, m.ien + 4 * (size_t)e, ires, iprec, yp, yc, ac, res, rmes, bd, iabres);
         };
         parallel_for(nb, nthreads, run_block);
     }
+    // hex and wedge blocks (elmmfg.f:113-146 block loop), element by element
+    for (int e = 0; e < m.nhex; ++e)
+        one_element(c, topo(2), m, m.ienh + 8 * (size_t)e, ires, iprec, yp, yc, ac, res, rmes, bd, iabres);
+    for (int e = 0; e < m.nwedge; ++e)
+        one_element(c, topo(3), m, m.ienw + 6 * (size_t)e, ires, iprec, yp, yc, ac, res, rmes, bd, iabres);
 }
 
 void boundary_sweep(const or_common& c, const or_mesh& m, const double* y, double* res) {
@@ -759,9 +856,29 @@ void or_tet_tables(double shp[16], double shgl[48], double Qwt[4], double shpb[1
 
 void or_e3(const or_common* c, int ires, int iprec, const double* yl, const double* ycl,
            const double* acl, const double* xl, double* rl, double* rml, double* bdl) {
-    e3_element(*c, ires, iprec, (const double (*)[5])yl, (const double (*)[5])ycl,
+    e3_element(*c, topo(1), ires, iprec, (const double (*)[5])yl, (const double (*)[5])ycl,
                (const double (*)[5])acl, (const double (*)[3])xl, (double (*)[5])rl,
                (double (*)[5])rml, iprec ? (double (*)[5][5])bdl : nullptr);
+}
+
+void or_topo_tables(int lcsyst, double shp[64], double shgl[192], double Qwt[8], int* nshl, int* ngauss) {
+    const Topo& t = topo(lcsyst);
+    *nshl = t.nshl;
+    *ngauss = t.ngauss;
+    for (int q = 0; q < t.ngauss; ++q) {
+        Qwt[q] = t.Qwt[q];
+        for (int a = 0; a < t.nshl; ++a) {
+            shp[q * t.nshl + a] = t.shp[q][a];
+            for (int i = 0; i < 3; ++i) shgl[(q * 3 + i) * t.nshl + a] = t.shgl[q][i][a];
+        }
+    }
+}
+
+void or_e3_topo(const or_common* c, int lcsyst, int ires, int iprec, const double* yl, const double* ycl,
+                const double* acl, const double* xl, double* rl, double* rml, double* bdl) {
+    e3_element(*c, topo(lcsyst), ires, iprec, (const double (*)[5])yl, (const double (*)[5])ycl,
+               (const double (*)[5])acl, (const double (*)[3])xl, (double (*)[5])rl, (double (*)[5])rml,
+               (double (*)[5][5])bdl);
 }
 
 void or_e3b(const or_common* c, int ires, const double* yl, const int* iBCB, const double* BCB,

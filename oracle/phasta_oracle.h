@@ -7,12 +7,10 @@
  * (phasta_gb300) never links, loads or calls it.
  *
  * Parity status: the quadrature and shape-function tables are pinned against
- * the reference's own C sources (symtet.c, symtri.c, uniformP.c) compiled in
- * place; the Fortran element routines cannot be compiled in this image (no
- * Fortran compiler), so the element-level restatement is pinned only by the
- * golden vectors produced by executing the reference Fortran source through
- * the Fortran-subset interpreter in tests/golden (where present) and by the
- * invariant tests.
+ * the reference's own C sources (symtet.c, symtri.c, symhex.c, symwdg.c,
+ * uniformP.c, newshape.cc) compiled in place; the Fortran routines are pinned
+ * by golden vectors computed by the reference's own Fortran source, executed
+ * through the Fortran-to-numpy translator in tests/golden.
  *
  * Array layouts are the reference's (Fortran column-major, node index
  * fastest):
@@ -59,6 +57,10 @@ typedef struct {
     const int* iBC;           /* nshg */
     const double* BC;         /* (nshg, ndofBC=6) column-major: BC[k*nshg + n] */
     const int* iper;          /* nshg, 0-based master (== n for non-periodic) */
+    int nhex;                 /* interior linear hexes (lcsyst 2) */
+    const int* ienh;          /* nhex*8, reference local node order */
+    int nwedge;               /* interior linear wedges (lcsyst 3) */
+    const int* ienw;          /* nwedge*6 */
 } or_mesh;
 
 typedef struct {
@@ -84,6 +86,13 @@ void or_tet_tables(double shp[16], double shgl[48], double Qwt[4],
 void or_e3(const or_common* c, int ires, int iprec,
            const double* yl, const double* ycl, const double* acl,
            const double* xl, double* rl, double* rml, double* bdl);
+
+/* quadrature/shape tables of topology lcsyst (1 tet, 2 hex, 3 wedge):
+ * shp[q*nshl+a], shgl[(q*3+i)*nshl+a], Qwt[q] */
+void or_topo_tables(int lcsyst, double shp[64], double shgl[192], double Qwt[8], int* nshl, int* ngauss);
+/* one element of topology lcsyst, arrays (nshl,5)/(nshl,3)/(nshl,5,5) as in or_e3 */
+void or_e3_topo(const or_common* c, int lcsyst, int ires, int iprec, const double* yl, const double* ycl,
+                const double* acl, const double* xl, double* rl, double* rml, double* bdl);
 
 /* one boundary element, e3b.f (ires in {1,3} adds rl) */
 void or_e3b(const or_common* c, int ires, const double* yl, const int* iBCB,

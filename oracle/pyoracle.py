@@ -34,6 +34,7 @@ class OMesh(C.Structure):
         ("nshg", C.c_int), ("nelem", C.c_int), ("ien", _ip), ("nblk", C.c_int), ("blk_start", _ip),
         ("ngrp", C.c_int), ("grp_start", _ip), ("x", _dp), ("nbelem", C.c_int), ("ienb", _ip),
         ("iBCB", _ip), ("BCB", _dp), ("iBC", _ip), ("BC", _dp), ("iper", _ip),
+        ("nhex", C.c_int), ("ienh", _ip), ("nwedge", C.c_int), ("ienw", _ip),
     ]
 
 
@@ -55,6 +56,7 @@ def lib():
         sig = {
             "or_make_groups": ([C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, _ip, _ip, C.c_int], C.c_int),
             "or_tet_tables": ([_dp] * 6, None),
+            "or_topo_tables": ([C.c_int, _dp, _dp, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int)], None),
             "or_e3": ([cp, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp], None),
             "or_e3b": ([cp, C.c_int, _dp, _ip, _dp, _dp, _dp], None),
             "or_elmmfg": ([cp, mp, _dp, _dp, _dp, _dp, _dp, C.c_int, C.c_int], None),
@@ -167,9 +169,12 @@ class Oracle:
         self._iBC = np.ascontiguousarray(case.iBC, dtype=np.int32)
         self._BC = np.ascontiguousarray(case.BC, dtype=np.float64).reshape(-1)
         self._iper = np.ascontiguousarray(case.iper, dtype=np.int32)
+        self._ienh = np.ascontiguousarray(getattr(case, "ienh", np.zeros((0, 8))), dtype=np.int32).reshape(-1)
+        self._ienw = np.ascontiguousarray(getattr(case, "ienw", np.zeros((0, 6))), dtype=np.int32).reshape(-1)
         self.m = OMesh(self.nshg, E, _i(self._ien), len(self._blk) - 1, _i(self._blk), ngrp, _i(self._grp),
                        _d(self._x), case.nbelem, _i(self._ienb), _i(self._iBCB), _d(self._BCB), _i(self._iBC),
-                       _d(self._BC), _i(self._iper))
+                       _d(self._BC), _i(self._iper), len(self._ienh) // 8, _i(self._ienh), len(self._ienw) // 6,
+                       _i(self._ienw))
         self.c = common(self.params)
         self.ntotGM = 0
 
@@ -261,3 +266,13 @@ class Oracle:
         yold, acold = self.itrUpdate(yold, acold, y, ac)
         self.set_params(istep=self.params["istep"] + 1)
         return yold, acold, y, ac, stats
+
+
+def topo_tables(lcsyst: int) -> dict:
+    """Quadrature/shape tables of topology lcsyst (1 tet, 2 hex, 3 wedge): shp[q][a], shgl[q][i][a], Qwt[q]."""
+    L = lib()
+    shp, shgl, qwt = np.zeros(64), np.zeros(192), np.zeros(8)
+    nshl, ng = C.c_int(), C.c_int()
+    L.or_topo_tables(lcsyst, _d(shp), _d(shgl), _d(qwt), C.byref(nshl), C.byref(ng))
+    n, q = nshl.value, ng.value
+    return {"shp": shp[: q * n].reshape(q, n), "shgl": shgl[: 3 * q * n].reshape(q, 3, n), "Qwt": qwt[:q]}

@@ -54,6 +54,17 @@ class Case:
     iper: np.ndarray         # (nshg,) int32
     h: float                 # smallest edge
     meta: dict = field(default_factory=dict)
+    # further interior blocks (linear hexes and wedges, the reference's lcsyst 2 and 3)
+    ienh: np.ndarray = field(default_factory=lambda: np.zeros((0, 8), np.int32))
+    ienw: np.ndarray = field(default_factory=lambda: np.zeros((0, 6), np.int32))
+
+    @property
+    def nhex(self) -> int:
+        return int(self.ienh.shape[0])
+
+    @property
+    def nwedge(self) -> int:
+        return int(self.ienw.shape[0])
 
     @property
     def nelem(self) -> int:
@@ -160,6 +171,95 @@ def box(n: int | tuple[int, int, int], lengths=(1.0, 1.0, 1.0), periodic=(False,
                 meta={"n": n, "lengths": lengths, "periodic": periodic})
 
 
+def _grid(n, lengths, periodic):
+    """Nodes of an (n+1)^3 lattice (slaves of periodic faces stored, as in the reference)."""
+    nx, ny, nz = n
+    npts = (nx + 1, ny + 1, nz + 1)
+    nshg = npts[0] * npts[1] * npts[2]
+    gx = [np.linspace(0.0, lengths[d], npts[d]) for d in range(3)]
+    X, Y, Z = np.meshgrid(*gx, indexing="ij")
+    x = np.stack([X.transpose(2, 1, 0).reshape(-1), Y.transpose(2, 1, 0).reshape(-1),
+                  Z.transpose(2, 1, 0).reshape(-1)], axis=1).astype(np.float64)
+    idx = np.arange(nshg)
+    i = idx % npts[0]
+    j = (idx // npts[0]) % npts[1]
+    k = idx // (npts[0] * npts[1])
+    mi, mj, mk = i.copy(), j.copy(), k.copy()
+    for d, (m, c, nd) in enumerate(((mi, i, nx), (mj, j, ny), (mk, k, nz))):
+        if periodic[d]:
+            m[c == nd] = 0
+    iper = (mi + npts[0] * (mj + npts[1] * mk)).astype(np.int32)
+    iBC = np.zeros(nshg, dtype=np.int32)
+    iBC[iper != idx] |= 1 << 10
+    return x, iper, iBC, (lambda a, b, c: a + npts[0] * (b + npts[1] * c))
+
+
+def hex_box(n, lengths=(1.0, 1.0, 1.0)) -> Case:
+    """Fully periodic box of n^3 linear hexes.
+
+    Local node order of the reference's hex (HexShapeAndDrv in newshape.cc): parent
+    (xi, eta, zeta) corners (-,-,-), (+,-,-), (+,+,-), (-,+,-), then the same at zeta = +1;
+    xi, eta, zeta run along x, y, z."""
+    if isinstance(n, int):
+        n = (n, n, n)
+    x, iper, iBC, nid = _grid(n, lengths, (True, True, True))
+    ii, jj, kk = (a.reshape(-1) for a in np.meshgrid(*(np.arange(m) for m in n), indexing="ij"))
+    corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    ienh = np.stack([nid(ii + a, jj + b, kk + c) for a, b, c in corners], axis=1).astype(np.int32)
+    h = min(lengths[d] / n[d] for d in range(3))
+    return Case(nshg=x.shape[0], x=x, ien=np.zeros((0, 4), np.int32), ienb=np.zeros((0, 4), np.int32),
+                iBCB=np.zeros((0, 2), np.int32), BCB=np.zeros((0, 3, 6)), iBC=iBC,
+                BC=np.zeros((6, x.shape[0])), iper=iper, h=h, ienh=ienh,
+                meta={"n": n, "lengths": lengths, "periodic": (True, True, True)})
+
+
+def wedge_box(n, lengths=(1.0, 1.0, 1.0)) -> Case:
+    """Fully periodic box of n^3 cubes, each split along its x = y diagonal into two prisms
+    with triangles in the xy planes.
+
+    Local node order of the reference's wedge (WedgeShapeAndDrv): the triangle at
+    zeta = -1 with parent (r, s) = (0, 0), (1, 0), (0, 1), then the triangle at zeta = +1."""
+    if isinstance(n, int):
+        n = (n, n, n)
+    x, iper, iBC, nid = _grid(n, lengths, (True, True, True))
+    ii, jj, kk = (a.reshape(-1) for a in np.meshgrid(*(np.arange(m) for m in n), indexing="ij"))
+    tris = ([(0, 0), (1, 0), (1, 1)], [(0, 0), (1, 1), (0, 1)])  # counter-clockwise seen from +z
+    prisms = []
+    for tri in tris:
+        bot = [nid(ii + a, jj + b, kk) for a, b in tri]
+        top = [nid(ii + a, jj + b, kk + 1) for a, b in tri]
+        prisms.append(np.stack(bot + top, axis=1))
+    ienw = np.stack(prisms, axis=1).reshape(-1, 6).astype(np.int32)
+    h = min(lengths[d] / n[d] for d in range(3))
+    return Case(nshg=x.shape[0], x=x, ien=np.zeros((0, 4), np.int32), ienb=np.zeros((0, 4), np.int32),
+                iBCB=np.zeros((0, 2), np.int32), BCB=np.zeros((0, 3, 6)), iBC=iBC,
+                BC=np.zeros((6, x.shape[0])), iper=iper, h=h, ienw=ienw,
+                meta={"n": n, "lengths": lengths, "periodic": (True, True, True)})
+
+
+def concat(*cases: Case) -> Case:
+    """Disjoint union of meshes (node numbers of each part offset by the nodes before it)."""
+    off = 0
+    parts = {k: [] for k in ("x", "ien", "ienb", "iBCB", "BCB", "iBC", "BC", "iper", "ienh", "ienw")}
+    for c in cases:
+        parts["x"].append(c.x)
+        parts["ien"].append(c.ien + off)
+        parts["ienb"].append(c.ienb + off)
+        parts["iBCB"].append(c.iBCB)
+        parts["BCB"].append(c.BCB)
+        parts["iBC"].append(c.iBC)
+        parts["BC"].append(c.BC)
+        parts["iper"].append(c.iper + off)
+        parts["ienh"].append(c.ienh + off)
+        parts["ienw"].append(c.ienw + off)
+        off += c.nshg
+    cat = {k: np.concatenate(v, axis=(1 if k == "BC" else 0)) for k, v in parts.items()}
+    return Case(nshg=off, x=cat["x"], ien=cat["ien"].astype(np.int32), ienb=cat["ienb"].astype(np.int32),
+                iBCB=cat["iBCB"].astype(np.int32), BCB=cat["BCB"], iBC=cat["iBC"].astype(np.int32), BC=cat["BC"],
+                iper=cat["iper"].astype(np.int32), h=min(c.h for c in cases), ienh=cat["ienh"].astype(np.int32),
+                ienw=cat["ienw"].astype(np.int32), meta={"parts": [c.meta for c in cases]})
+
+
 # ---------------------------------------------------------------------------
 # seeded states (counter-based: the value of (node, dof) does not depend on
 # the mesh size or traversal order)
@@ -251,5 +351,22 @@ def periodic_vortex_case(n: int, mach: float = 0.1, re: float = 1600.0):
     case = box(n, lengths=(L, L, L), periodic=(True, True, True), inflow=None)
     fs = freestream(mach)
     mu = fs["rho"] * 1.0 * 1.0 / re
+    dt = cfl_dt(case, mach)
+    return case, {"mach": mach, "re": re, "mu": mu, "dt": dt, "fs": fs}
+
+
+def mixed_case(n_tet=4, n_hex=4, n_wedge=(4, 4, 2), mach: float = 0.3, re: float = 1000.0):
+    """Three disjoint periodic unit boxes: n_tet^3 x 6 tets, n_hex^3 hexes and 2 x prod(n_wedge)
+    wedges -- the element blocks of a mixed-topology mesh (each block conforming)."""
+    parts = []
+    if n_tet:
+        parts.append(box(n_tet, periodic=(True, True, True), inflow=None))
+    if n_hex:
+        parts.append(hex_box(n_hex))
+    if n_wedge:
+        parts.append(wedge_box(n_wedge))
+    case = concat(*parts)
+    fs = freestream(mach)
+    mu = fs["rho"] * fs["u"] * 1.0 / re
     dt = cfl_dt(case, mach)
     return case, {"mach": mach, "re": re, "mu": mu, "dt": dt, "fs": fs}

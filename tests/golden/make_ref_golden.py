@@ -21,7 +21,7 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 sys.path[:0] = [str(HERE), str(ROOT), str(ROOT / "tests")]
 
-from helpers import channel, vortex  # noqa: E402
+from helpers import channel, mixed, vortex  # noqa: E402
 from refrun import RefPhasta  # noqa: E402
 
 DEFAULT_REF = Path("/root/reference/phSolver")
@@ -36,6 +36,8 @@ CASES = [
     ("channel3_galerkin", lambda: channel(3, ac_scale=0.05, ivart=1), ("elm",)),
     # Kspace 3 with two cycles: the second cycle restarts from Au2MFG's R - J Dy
     ("channel4_restart", lambda: channel(4, ac_scale=0.05, Kspace=3, nGMRES=2), ("elm", "solve")),
+    # tet, hex (lcsyst 2) and wedge (lcsyst 3) blocks
+    ("mixed3", lambda: mixed(3, 3, (3, 3, 2)), ALL),
 ]
 
 

@@ -59,6 +59,27 @@ def main():
     p = Path(__file__).resolve().parent / "tet_tables.json"
     p.write_text(json.dumps(out, indent=1))
     print(p)
+    topo = {}
+    # hex: 8-point rule of symhex.c (genint.f:86-99, no weight scaling), shapes of shphex.c (genshp.f)
+    # wedge: 6-point rule of symwdg.c (genint.f:312-317), shapes of shp6w.c; no gradient scaling for either
+    for name, rule, shape, nq, nen in (("hex", L.symhex_, L.shphex_, 8, 8), ("wedge", L.symwdg_, L.shp6w_, 6, 6)):
+        n = C.c_int(nq)
+        pt, wt = (D * (4 * nq))(), (D * nq)()
+        rule(C.byref(n), pt, wt, C.byref(err))
+        shp, shgl, qwt, pts = [], [], [], []
+        for q in range(nq):
+            par = (D * 3)(pt[4 * q], pt[4 * q + 1], pt[4 * q + 2])
+            N, dN = (D * nen)(), (D * (3 * nen))()
+            shape(C.byref(C.c_int(1)), par, N, dN)
+            shp.append([N[a] for a in range(nen)])
+            shgl.append([[dN[3 * a + i] for a in range(nen)] for i in range(3)])
+            qwt.append(wt[q])
+            pts.append([pt[4 * q + k] for k in range(4)])
+        topo[name] = {"shp": shp, "shgl": shgl, "Qwt": qwt, "Qpt": pts}
+    topo["source"] = "reference symhex.c, symwdg.c, shphex.c, shp6w.c -> newshape.cc; genint.f, genshp.f"
+    p2 = Path(__file__).resolve().parent / "topo_tables.json"
+    p2.write_text(json.dumps(topo, indent=1))
+    print(p2)
 
 
 if __name__ == "__main__":

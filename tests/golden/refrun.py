@@ -68,11 +68,15 @@ class RefPhasta:
                        tmrc=lambda *a: 0.0, tnanq=lambda *a: None, rstat=lambda *a: None)
         N, E, Eb = case.nshg, case.nelem, case.nbelem
         self.N, self.case, self.params = N, case, dict(params)
-        ien = np.asfortranarray(case.ien.astype(np.int64) + 1)
+        # interior blocks by topology: (connectivity, lcsyst, nshl, points)
+        blocks = [(case.ien, 1, 4, 4), (getattr(case, "ienh", np.zeros((0, 8))), 2, 8, 8),
+                  (getattr(case, "ienw", np.zeros((0, 6))), 3, 6, 6)]
+        blocks = [b for b in blocks if len(b[0])]
         ienb = np.asfortranarray(case.ienb.astype(np.int64) + 1)
         P.module("pointer_data", {
-            "mien": [_Obj(ien)], "mmat": [_Obj(np.ones(E, np.int64))],
-            "mxmudmi": [_Obj(np.zeros((E, 4), order="F"))],
+            "mien": [_Obj(np.asfortranarray(np.asarray(b[0]).astype(np.int64) + 1)) for b in blocks],
+            "mmat": [_Obj(np.ones(len(b[0]), np.int64)) for b in blocks],
+            "mxmudmi": [_Obj(np.zeros((len(b[0]), b[3]), order="F")) for b in blocks],
             "mienb": [_Obj(ienb)], "mmatb": [_Obj(np.ones(max(Eb, 1), np.int64))],
             "mibcb": [_Obj(np.asfortranarray(case.iBCB.astype(np.int64)))],
             "mbcb": [_Obj(np.asfortranarray(case.BCB))]})
@@ -81,6 +85,7 @@ class RefPhasta:
         P.function("elmmfg")  # declares the COMMON blocks of common.h
         G = P.G
         T = json.loads((HERE / "tet_tables.json").read_text())
+        TT = json.loads((HERE / "topo_tables.json").read_text())
         p = self.params
         G.numpe, G.myrank, G.master = 1, 0, 0
         G.numnp = G.nshg = N
@@ -88,15 +93,21 @@ class RefPhasta:
         G.numel, G.numelb = E, Eb
         G.nen, G.ndof, G.nflow, G.nedof = 4, 5, 5, 20
         G.ndofbc, G.ndibcb, G.ndbcb = 6, 2, 6
-        G.nelblk, G.nelblb = 1, (1 if Eb else 0)
+        G.nelblk, G.nelblb = len(blocks), (1 if Eb else 0)
         # lcblk(:,iblk): iel, lelCat, lcsyst, iorder, nenl, -, mattyp, ndofl, nsymdl, nshl
-        G.lcblk[:, 0] = [1, 1, 1, 1, 4, 0, 1, 5, 0, 4]
-        G.lcblk[0, 1] = E + 1
+        iel = 1
+        for ib, (con, lcsyst, nshl, _nq) in enumerate(blocks):
+            G.lcblk[:, ib] = [iel, lcsyst, lcsyst, 1, nshl, 0, 1, 5, 0, nshl]
+            iel += len(con)
+        G.lcblk[0, len(blocks)] = iel
         # lcblkb(:,iblk): iel, lelCat, lcsyst, iorder, nenl, nenbl, mattyp, ndofl, nshl, nshlb
         G.lcblkb[:, 0] = [1, 1, 1, 1, 4, 3, 1, 5, 4, 3]
         G.lcblkb[0, 1] = Eb + 1
         G.nint[0], G.nintb[0] = 4, 3
+        G.nint[1], G.nint[2] = 8, 6
         G.qwt[0, :4] = T["Qwt"]
+        G.qwt[1, :8] = TT["hex"]["Qwt"]
+        G.qwt[2, :6] = TT["wedge"]["Qwt"]
         G.qwtb[0, :3] = T["Qwtb"]
         G.datmat[0, 1, 0] = p["rmu"]
         G.pr, G.rgas, G.gamma, G.gamma1 = p["pr"], p["Rgas"], p["gamma"], p["gamma1"]
@@ -125,6 +136,10 @@ class RefPhasta:
         for q in range(3):
             self.shpb[0, :4, q] = T["shpb"][q]
             self.shglb[0, :, :4, q] = T["shglb"][q]
+        for top, (name, nq, nen) in ((1, ("hex", 8, 8)), (2, ("wedge", 6, 6))):
+            for q in range(nq):
+                self.shp[top, :nen, q] = TT[name]["shp"][q]
+                self.shgl[top, :, :nen, q] = TT[name]["shgl"][q]
         self.iBC = case.iBC.astype(np.int64)
         self.BC = np.asfortranarray(case.BC.T)
         self.iper = case.iper.astype(np.int64) + 1

@@ -211,3 +211,13 @@ def test_yshuffle_roundtrip(code):
     L.or_yshuffle(N, a.ctypes.data_as(C.POINTER(C.c_double)), code)
     L.or_yshuffle(N, a.ctypes.data_as(C.POINTER(C.c_double)), 1 - code)
     assert np.array_equal(a, r)
+
+
+def test_hex_and_wedge_tables_match_reference_c_sources():
+    """Oracle restatement of symhex.c/symwdg.c and the hex/wedge shapes vs tests/golden/topo_tables.json."""
+    import json
+    d = json.loads((Path(__file__).resolve().parent / "golden" / "topo_tables.json").read_text())
+    for name, lcsyst in (("hex", 2), ("wedge", 3)):
+        t = pyoracle.topo_tables(lcsyst)
+        for k in ("shp", "shgl", "Qwt"):
+            assert np.array_equal(t[k], np.array(d[name][k])), (name, k)
