@@ -27,6 +27,10 @@ module phgpu_iface
      type(c_ptr)    :: ien, x
      integer(c_int) :: nbelem
      type(c_ptr)    :: ienb, iBCB, BCB, iBC, BC, iper
+     integer(c_int) :: nhex          ! blocks with lcsyst 2 (mien(iblk)%p of nshl = 8)
+     type(c_ptr)    :: ienh
+     integer(c_int) :: nwedge        ! blocks with lcsyst 3 (nshl = 6)
+     type(c_ptr)    :: ienw
   end type
 
   type, bind(C) :: phgpu_stats

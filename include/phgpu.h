@@ -89,7 +89,7 @@ typedef struct {
  * pointer_data mien/mienb/miBCB/mBCB and in iBC/BC/iper). */
 typedef struct {
     int nshg;             /* nodes (periodic slaves are stored, as in the reference) */
-    int nelem;            /* interior linear tets */
+    int nelem;            /* interior linear tets (lcsyst 1) */
     const int* ien;       /* nelem*4, element-major: ien[4*e + a] */
     const double* x;      /* (nshg, 3) */
     int nbelem;           /* boundary tets, boundary face = local nodes 0,1,2 */
@@ -99,6 +99,11 @@ typedef struct {
     const int* iBC;       /* nshg: BC bit codes (bit 1 T, bit 2 p, bits 3-5 velocity, bit 10 periodic) */
     const double* BC;     /* (nshg, 6) column-major, BC(:,k) */
     const int* iper;      /* nshg: periodic master (== n when not periodic) */
+    /* further interior blocks (linear hexes and wedges, lcsyst 2 and 3), reference local node order */
+    int nhex;             /* hexes */
+    const int* ienh;      /* nhex*8 */
+    int nwedge;           /* wedges */
+    const int* ienw;      /* nwedge*6 */
 } phgpu_mesh;
 
 typedef struct {

@@ -45,6 +45,7 @@ class Mesh(C.Structure):
         ("nshg", C.c_int), ("nelem", C.c_int), ("ien", _ip), ("x", _dp),
         ("nbelem", C.c_int), ("ienb", _ip), ("iBCB", _ip), ("BCB", _dp),
         ("iBC", _ip), ("BC", _dp), ("iper", _ip),
+        ("nhex", C.c_int), ("ienh", _ip), ("nwedge", C.c_int), ("ienw", _ip),
     ]
 
 

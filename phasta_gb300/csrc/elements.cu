@@ -41,6 +41,8 @@ __constant__ TetTables c_tab;
 __constant__ float c_shpf[4][4];   // single-precision copies (no conversions in FP32 kernels)
 __constant__ float c_qwtf;
 
+void upload_topo_tables(Ctx& C);
+
 // tet point weight: symtet.c's 1/4 scaled by 4/3 (genint.f:72)
 constexpr double kTetQwt = (4.0 / 3.0) * 0.25;
 
@@ -77,6 +79,7 @@ void upload_tables(Ctx& C) {
     qf = (float)t.Qwt[0];
     check(C, cudaMemcpyToSymbolAsync(c_qwtf, &qf, sizeof(qf), 0, cudaMemcpyHostToDevice, C.stream),
           "upload tables");
+    upload_topo_tables(C);
 }
 
 template <typename R>
@@ -1351,7 +1354,479 @@ k_boundary(const int4* __restrict__ ienb, const int* __restrict__ iBCB, const do
     }
 }
 
+// --------------------------------------------------------------------------
+// hex and wedge blocks (lcsyst 2 and 3, linear basis).  One thread per
+// (element, node); the linear rules have as many points as nodes, so thread a
+// of an element evaluates quadrature point q = a (metric e3metric.f, state
+// e3ivar.f/getthm.f, tau e3tau.f with the dxidx^T dxidx metric of
+// e3tau.f:1408-1425) and shares it in shared memory; then each thread sums
+// its node's weighted terms over the points (e3wmlt.f, e3bdg.f) and adds
+// them to the node.  Elements of one colour share no node.
+// --------------------------------------------------------------------------
+struct TopoTabD {
+    double shp[8][8];      // [q][a]
+    double shgl[8][3][8];  // [q][i][a]
+    double qwt[8];
+};
+struct TopoTabF {
+    float shp[8][8];
+    float shgl[8][3][8];
+    float qwt[8];
+};
+__constant__ TopoTabD c_topo[2];   // 0 hex, 1 wedge
+__constant__ TopoTabF c_topof[2];
+
+template <typename R> __device__ __forceinline__ R tshp(int t, int q, int a);
+template <> __device__ __forceinline__ double tshp<double>(int t, int q, int a) { return c_topo[t].shp[q][a]; }
+template <> __device__ __forceinline__ float tshp<float>(int t, int q, int a) { return c_topof[t].shp[q][a]; }
+template <typename R> __device__ __forceinline__ R tshgl(int t, int q, int i, int a);
+template <> __device__ __forceinline__ double tshgl<double>(int t, int q, int i, int a) { return c_topo[t].shgl[q][i][a]; }
+template <> __device__ __forceinline__ float tshgl<float>(int t, int q, int i, int a) { return c_topof[t].shgl[q][i][a]; }
+template <typename R> __device__ __forceinline__ R tqwt(int t, int q);
+template <> __device__ __forceinline__ double tqwt<double>(int t, int q) { return c_topo[t].qwt[q]; }
+template <> __device__ __forceinline__ float tqwt<float>(int t, int q) { return c_topof[t].qwt[q]; }
+
+constexpr int kTopoThreads = 128;
+enum TopoMode : int { TM_RES = RM_RES, TM_MODRES = RM_MODRES, TM_LIN = RM_LIN, TM_FULL = 4 };
+
+// shared values of one quadrature point
+template <int NEN>
+struct TopoQp {
+    static constexpr int kShg = 0;                  // shg[b][i], NEN*3
+    static constexpr int kW = NEN * 3;              // WdetJ
+    static constexpr int kU = kW + 1;               // u(3) p rho ek drdp drdT e1p e2p e3p e4p tau(3) = 15
+    static constexpr int kAig = kU + 15;            // A_i Y,i (5)
+    static constexpr int kA0 = kAig + 5;            // A0 Y,t (res) / dU (modified, linear) (5)
+    static constexpr int kVt = kA0 + 5;             // viscous stress t[i][j] (9)
+    static constexpr int kVq = kVt + 9;             // heat flux (3)
+    static constexpr int kDu = kVq + 3;             // conservative variables (full mode) (5)
+    static constexpr int kN = kDu + 5;
+};
+
+template <typename R, int NEN, int TOPO, int MODE>
+__global__ void __launch_bounds__(kTopoThreads)
+k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __restrict__ ya,
+       const R* __restrict__ yb, const R* __restrict__ ac, R* __restrict__ res, R* __restrict__ rmes,
+       R* __restrict__ bd, Phys<R> P, int iabres, const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    using Q = TopoQp<NEN>;
+    constexpr int EPB = kTopoThreads / NEN;  // elements per CTA
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* sm = reinterpret_cast<R*>(smem_raw);
+    const int le = threadIdx.x / NEN, a = threadIdx.x % NEN;
+    const int e = blockIdx.x * EPB + le;
+    const bool active = le < EPB && e < ne;
+    R* sx = sm + (size_t)le * NEN * 13;   // x(3) ya(5) yb(5) per node
+    R* sq = sm + (size_t)EPB * NEN * 13 + (size_t)le * NEN * Q::kN;
+    int node = 0;
+    if (active) {
+        node = ien[(size_t)e * NEN + a];
+        R* s = sx + 13 * a;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) s[d] = ldg(x + 3 * (size_t)node + d);
+        const R* bsrc = (MODE == TM_RES || MODE == TM_FULL) ? ac : yb;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            s[3 + k] = ldg(ya + 5 * (size_t)node + k);
+            s[8 + k] = ldg(bsrc + 5 * (size_t)node + k);
+        }
+    }
+    __syncthreads();
+    if (active) {
+        // ---- quadrature point q = a: metric (e3metric.f:22-77) ----
+        const int q = a;
+        R dxdxi[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                R acc = R(0);
+#pragma unroll
+                for (int b = 0; b < NEN; ++b) acc += sx[13 * b + i] * tshgl<R>(TOPO, q, j, b);
+                dxdxi[i][j] = acc;
+            }
+        R di[3][3];
+        di[0][0] = dxdxi[1][1] * dxdxi[2][2] - dxdxi[2][1] * dxdxi[1][2];
+        di[0][1] = dxdxi[2][1] * dxdxi[0][2] - dxdxi[0][1] * dxdxi[2][2];
+        di[0][2] = dxdxi[0][1] * dxdxi[1][2] - dxdxi[0][2] * dxdxi[1][1];
+        const R tmp = R(1) / (di[0][0] * dxdxi[0][0] + di[0][1] * dxdxi[1][0] + di[0][2] * dxdxi[2][0]);
+        di[0][0] *= tmp;
+        di[0][1] *= tmp;
+        di[0][2] *= tmp;
+        di[1][0] = (dxdxi[1][2] * dxdxi[2][0] - dxdxi[1][0] * dxdxi[2][2]) * tmp;
+        di[1][1] = (dxdxi[0][0] * dxdxi[2][2] - dxdxi[2][0] * dxdxi[0][2]) * tmp;
+        di[1][2] = (dxdxi[1][0] * dxdxi[0][2] - dxdxi[0][0] * dxdxi[1][2]) * tmp;
+        di[2][0] = (dxdxi[1][0] * dxdxi[2][1] - dxdxi[1][1] * dxdxi[2][0]) * tmp;
+        di[2][1] = (dxdxi[2][0] * dxdxi[0][1] - dxdxi[0][0] * dxdxi[2][1]) * tmp;
+        di[2][2] = (dxdxi[0][0] * dxdxi[1][1] - dxdxi[0][1] * dxdxi[1][0]) * tmp;
+        R* o = sq + Q::kN * q;
+        o[Q::kW] = tqwt<R>(TOPO, q) / tmp;
+        R g[3][5];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) g[i][k] = R(0);
+        R bq[5], pv[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) bq[k] = pv[k] = R(0);
+        R aq[5] = {R(0), R(0), R(0), R(0), R(0)};
+#pragma unroll
+        for (int b = 0; b < NEN; ++b) {
+            R sh[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                sh[i] = tshgl<R>(TOPO, q, 0, b) * di[0][i] + tshgl<R>(TOPO, q, 1, b) * di[1][i] +
+                        tshgl<R>(TOPO, q, 2, b) * di[2][i];
+                o[Q::kShg + 3 * b + i] = sh[i];
+            }
+            const R Nb = tshp<R>(TOPO, q, b);
+            const R* s = sx + 13 * b;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                const R va = s[3 + k];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) g[i][k] += sh[i] * va;
+                pv[k] += Nb * va;
+                if (MODE == TM_RES || MODE == TM_FULL) aq[k] += Nb * s[8 + k];
+                else bq[k] += Nb * s[8 + k];
+            }
+        }
+        if (MODE == TM_RES || MODE == TM_FULL) {
+#pragma unroll
+            for (int k = 0; k < 5; ++k) bq[k] = pv[k];
+        }
+        Qp<R> st;
+        qp_state(P, bq[0], bq[1], bq[2], bq[3], bq[4], st);
+        Geo<R> gm;  // only the metric of tau (e3tau.f:1408-1425)
+        {
+            auto gij = [&](int i, int j) { return di[0][i] * di[0][j] + di[1][i] * di[1][j] + di[2][i] * di[2][j]; };
+            gm.G[0] = gij(0, 0);
+            gm.G[1] = gij(0, 1);
+            gm.G[2] = gij(1, 1);
+            gm.G[3] = gij(0, 2);
+            gm.G[4] = gij(1, 2);
+            gm.G[5] = gij(2, 2);
+            gm.GG = gm.G[0] * gm.G[0] + gm.G[2] * gm.G[2] + gm.G[5] * gm.G[5] +
+                    R(2) * (gm.G[1] * gm.G[1] + gm.G[3] * gm.G[3] + gm.G[4] * gm.G[4]);
+            gm.trG = gm.G[0] + gm.G[2] + gm.G[5];
+        }
+        qp_tau(P, gm, st);
+        R aig[5], a0x[5];
+        ai_gi(st, g, aig);
+        if (MODE == TM_RES || MODE == TM_FULL) {
+            a0_v(st, aq, a0x);
+        } else if (MODE == TM_MODRES) {
+            // conservative variables of the perturbed state (e3ivar.f:96-131)
+            const R rho6 = pv[0] / (P.Rgas * pv[4]);
+            const R rk6 = R(0.5) * (pv[1] * pv[1] + pv[2] * pv[2] + pv[3] * pv[3]);
+            a0x[0] = rho6;
+            a0x[1] = rho6 * pv[1];
+            a0x[2] = rho6 * pv[2];
+            a0x[3] = rho6 * pv[3];
+            a0x[4] = rho6 * (pv[4] * P.cv + rk6);
+        } else {
+            a0_v(st, pv, a0x);
+        }
+        Visc<R> vs;
+        if (P.navier) viscous(P, g, vs);
+        else {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                vs.q[i] = R(0);
+#pragma unroll
+                for (int j = 0; j < 3; ++j) vs.t[i][j] = R(0);
+            }
+        }
+        R* ov = o + Q::kU;
+        ov[0] = st.u[0];
+        ov[1] = st.u[1];
+        ov[2] = st.u[2];
+        ov[3] = st.p;
+        ov[4] = st.rho;
+        ov[5] = st.ei + st.rk;
+        ov[6] = st.drdp;
+        ov[7] = st.drdT;
+        ov[8] = st.e1p;
+        ov[9] = st.e2p;
+        ov[10] = st.e3p;
+        ov[11] = st.e4p;
+        ov[12] = st.tau[0];
+        ov[13] = st.tau[1];
+        ov[14] = st.tau[2];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            o[Q::kAig + k] = aig[k];
+            o[Q::kA0 + k] = a0x[k];
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+#pragma unroll
+            for (int j = 0; j < 3; ++j) o[Q::kVt + 3 * i + j] = vs.t[i][j];
+            o[Q::kVq + i] = vs.q[i];
+        }
+        const R du[5] = {st.rho, st.rho * st.u[0], st.rho * st.u[1], st.rho * st.u[2], st.rho * (st.ei + st.rk)};
+#pragma unroll
+        for (int k = 0; k < 5; ++k) o[Q::kDu + k] = du[k];
+    }
+    __syncthreads();
+    if (!active) return;
+    // ---- node a: weighted terms summed over the points ----
+    R rl[5], rml[5], B_[5][5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        rl[k] = rml[k] = R(0);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) B_[k][j] = R(0);
+    }
+#pragma unroll 1
+    for (int q = 0; q < NEN; ++q) {
+        const R* v = sq + Q::kN * q;
+        const R w = v[Q::kW];
+        const R s[3] = {v[Q::kShg + 3 * a], v[Q::kShg + 3 * a + 1], v[Q::kShg + 3 * a + 2]};
+        const R Na = tshp<R>(TOPO, q, a);
+        const R* u = v + Q::kU;
+        const R u0 = u[0], u1 = u[1], u2 = u[2], p = u[3], rho = u[4], ek = u[5];
+        const R drdp = u[6], drdT = u[7], e1p = u[8], e2p = u[9], e3p = u[10], e4p = u[11];
+        const R tk[5] = {u[12], u[13], u[13], u[13], u[14]};
+        const R uu[3] = {u0, u1, u2};
+        R sv[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) sv[j] = s[0] * v[Q::kVt + j] + s[1] * v[Q::kVt + 3 + j] + s[2] * v[Q::kVt + 6 + j];
+        const R sqh = s[0] * v[Q::kVq] + s[1] * v[Q::kVq + 1] + s[2] * v[Q::kVq + 2];
+        const R usv = u0 * sv[0] + u1 * sv[1] + u2 * sv[2] + sqh;
+        const R Us = s[0] * u0 + s[1] * u1 + s[2] * u2;
+        // B = sum_i s_i A_i (e3mtrx.f closed form)
+        R Bm[5][5];
+        Bm[0][0] = drdp * Us;
+        Bm[0][4] = drdT * Us;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            Bm[0][1 + j] = rho * s[j];
+            Bm[1 + j][0] = drdp * Us * uu[j] + s[j];
+            Bm[1 + j][4] = drdT * Us * uu[j];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) Bm[1 + j][1 + k] = rho * (uu[j] * s[k] + (j == k ? Us : R(0)));
+            Bm[4][1 + j] = e3p * s[j] + rho * Us * uu[j];
+        }
+        Bm[4][0] = e2p * Us;
+        Bm[4][4] = e4p * Us;
+        if (MODE == TM_RES || MODE == TM_FULL) {
+            R lt[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) lt[k] = tk[k] * (v[Q::kAig + k] + v[Q::kA0 + k]);
+            R fe[5];
+            const R m = -rho * Us;
+            fe[0] = m;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) fe[1 + j] = m * uu[j] - s[j] * p + sv[j];
+            fe[4] = m * ek - Us * p + usv;
+#pragma unroll
+            for (int r = 0; r < 5; ++r) {
+                R bt = R(0);
+#pragma unroll
+                for (int k = 0; k < 5; ++k) bt += Bm[r][k] * lt[k];
+                rl[r] += w * (fe[r] + bt + Na * v[Q::kA0 + r]);
+            }
+        }
+        if (MODE != TM_RES) {
+            R rm16[5], lm[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                const R dk = (MODE == TM_FULL) ? v[Q::kDu + k] : v[Q::kA0 + k];
+                rm16[k] = v[Q::kAig + k] + P.fct1 * dk;
+                lm[k] = tk[k] * rm16[k];
+            }
+#pragma unroll
+            for (int r = 0; r < 5; ++r) {
+                R bm = R(0);
+#pragma unroll
+                for (int k = 0; k < 5; ++k) bm += Bm[r][k] * lm[k];
+                const R fm = (r == 0) ? R(0) : (r == 4) ? usv : sv[r - 1];
+                rml[r] += w * (fm + bm + Na * rm16[r]);
+            }
+        }
+        if (MODE == TM_FULL && bd) {
+            // (N_a I + B tau)(B + fct N_a A0) + K_a (e3bdg.f)
+            const R fN = P.fct1 * Na;
+            R Cm[5][5];
+#pragma unroll
+            for (int r = 0; r < 5; ++r)
+#pragma unroll
+                for (int k = 0; k < 5; ++k) Cm[r][k] = Bm[r][k];
+            Cm[0][0] += fN * drdp;
+            Cm[0][4] += fN * drdT;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                Cm[1 + j][0] += fN * drdp * uu[j];
+                Cm[1 + j][1 + j] += fN * rho;
+                Cm[1 + j][4] += fN * drdT * uu[j];
+                Cm[4][1 + j] += fN * rho * uu[j];
+            }
+            Cm[4][0] += fN * e1p;
+            Cm[4][4] += fN * e4p;
+#pragma unroll
+            for (int r = 0; r < 5; ++r) {
+                R D[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) D[k] = (P.supg ? Bm[r][k] * tk[k] : R(0)) + (r == k ? Na : R(0));
+#pragma unroll
+                for (int cc = 0; cc < 5; ++cc) {
+                    R acc = R(0);
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) acc += D[k] * Cm[k][cc];
+                    B_[r][cc] += w * acc;
+                }
+            }
+            if (P.navier) {
+                const R ss = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
+                R km[3][3];
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) km[j][k] = P.rlmpmu * s[j] * s[k] + (j == k ? P.rmu * ss : R(0));
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) B_[1 + j][1 + k] += w * km[j][k];
+                    B_[4][1 + j] += w * (km[j][0] * u0 + km[j][1] * u1 + km[j][2] * u2);
+                }
+                B_[4][4] += w * P.con * ss;
+            }
+        }
+    }
+    if ((MODE == TM_RES || MODE == TM_FULL) && res) {
+        R* og = res + 5 * (size_t)node;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) og[k] += rl[k];
+    }
+    if (MODE != TM_RES && rmes) {
+        R* og = rmes + 5 * (size_t)node;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) og[k] += iabres ? fabs(rml[k]) : rml[k];
+    }
+    if (MODE == TM_FULL && bd) {
+        R* ob = bd + 25 * (size_t)node;
+#pragma unroll
+        for (int r = 0; r < 5; ++r)
+#pragma unroll
+            for (int cc = 0; cc < 5; ++cc) ob[5 * r + cc] += B_[r][cc];
+    }
+}
+
 }  // namespace
+
+// hex and wedge tables: the rules and linear shapes of symhex.c/symwdg.c and
+// HexShapeAndDrv/WedgeShapeAndDrv (wedge in-plane derivatives on the area-2 parent)
+void upload_topo_tables(Ctx& C) {
+    TopoTabD t[2] = {};
+    const double g = 0.577350269189626;
+    const double sgn[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                              {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+    for (int q = 0; q < 8; ++q) {
+        const double par[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
+        t[0].qwt[q] = 1.0;
+        for (int a = 0; a < 8; ++a) {
+            const double f[3] = {(1.0 + sgn[a][0] * par[0]) / 2.0, (1.0 + sgn[a][1] * par[1]) / 2.0,
+                                 (1.0 + sgn[a][2] * par[2]) / 2.0};
+            t[0].shp[q][a] = f[0] * f[1] * f[2];
+            t[0].shgl[q][0][a] = sgn[a][0] / 2.0 * f[1] * f[2];
+            t[0].shgl[q][1][a] = f[0] * sgn[a][1] / 2.0 * f[2];
+            t[0].shgl[q][2][a] = f[0] * f[1] * sgn[a][2] / 2.0;
+        }
+    }
+    const double P3 = 0.166666666666667, P4 = 0.666666666666667, Qz = 0.577350269189626, W = 0.666666666666667;
+    const double tri[3][2] = {{P3, P3}, {P4, P3}, {P3, P4}};
+    const double dLr[3] = {-1.0, 1.0, 0.0}, dLs[3] = {-1.0, 0.0, 1.0};
+    for (int q = 0; q < 6; ++q) {
+        const double r = tri[q % 3][0], s2 = tri[q % 3][1], z = q < 3 ? -Qz : Qz;
+        const double L[3] = {1.0 - r - s2, r, s2};
+        t[1].qwt[q] = W;
+        for (int a = 0; a < 6; ++a) {
+            const int v = a % 3;
+            const double zs = a < 3 ? -1.0 : 1.0;
+            const double fz = (1.0 + zs * z) / 2.0;
+            t[1].shp[q][a] = L[v] * fz;
+            t[1].shgl[q][0][a] = dLr[v] * fz / 2.0;
+            t[1].shgl[q][1][a] = dLs[v] * fz / 2.0;
+            t[1].shgl[q][2][a] = L[v] * zs / 2.0;
+        }
+    }
+    static TopoTabD td[2];
+    static TopoTabF tf[2];
+    for (int k = 0; k < 2; ++k) {
+        td[k] = t[k];
+        for (int q = 0; q < 8; ++q) {
+            tf[k].qwt[q] = (float)t[k].qwt[q];
+            for (int a = 0; a < 8; ++a) {
+                tf[k].shp[q][a] = (float)t[k].shp[q][a];
+                for (int i = 0; i < 3; ++i) tf[k].shgl[q][i][a] = (float)t[k].shgl[q][i][a];
+            }
+        }
+    }
+    check(C, cudaMemcpyToSymbolAsync(c_topo, td, sizeof(td), 0, cudaMemcpyHostToDevice, C.stream), "upload tables");
+    check(C, cudaMemcpyToSymbolAsync(c_topof, tf, sizeof(tf), 0, cudaMemcpyHostToDevice, C.stream), "upload tables");
+}
+
+template <typename R, int NEN>
+constexpr size_t topo_smem() {
+    return sizeof(R) * (size_t)(kTopoThreads / NEN) * NEN * (13 + TopoQp<NEN>::kN);
+}
+
+template <typename R, int NEN, int TOPO>
+int configure_topo_kernels(Ctx& C) {
+    const int sm = (int)topo_smem<R, NEN>();
+    int rc = PHGPU_OK;
+    auto T = [&](cudaError_t e) { if (rc == PHGPU_OK) rc = check(C, e, "cudaFuncSetAttribute"); };
+    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    return rc;
+}
+
+template <typename R, int NEN, int TOPO>
+static void launch_topo_one(Ctx& C, int mode, const int* d_ien, const std::vector<int>& col, const R* x,
+                            const R* ya, const R* yb, const R* ac, R* res, R* rmes, R* bd, int iabres,
+                            const int* skip) {
+    const Phys<R> P = make_phys<R>(C.cfg);
+    constexpr int EPB = kTopoThreads / NEN;
+    const size_t sm = topo_smem<R, NEN>();
+    const int ncol = (int)col.size() - 1;
+    for (int c = 0; c < ncol; ++c) {
+        const int e0 = col[c], ne = col[c + 1] - e0;
+        if (ne <= 0) continue;
+        const int grid = (ne + EPB - 1) / EPB;
+        const int* ie = d_ien + (size_t)NEN * e0;
+        switch (mode) {
+            case TM_RES:
+                k_topo<R, NEN, TOPO, TM_RES><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip);
+                break;
+            case TM_MODRES:
+                k_topo<R, NEN, TOPO, TM_MODRES><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip);
+                break;
+            case TM_LIN:
+                k_topo<R, NEN, TOPO, TM_LIN><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip);
+                break;
+            default:
+                k_topo<R, NEN, TOPO, TM_FULL><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip);
+                break;
+        }
+        ++C.launches;
+    }
+}
+
+template <typename R>
+void launch_topo(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R* ac, R* res, R* rmes, R* bd,
+                 int iabres, const int* skip) {
+    if (C.nhex > 0)
+        launch_topo_one<R, 8, 0>(C, mode, C.d_ienh, C.hcol_start, x, ya, yb, ac, res, rmes, bd, iabres, skip);
+    if (C.nwedge > 0)
+        launch_topo_one<R, 6, 1>(C, mode, C.d_ienw, C.wcol_start, x, ya, yb, ac, res, rmes, bd, iabres, skip);
+}
+template void launch_topo<double>(Ctx&, int, const double*, const double*, const double*, const double*, double*,
+                                  double*, double*, int, const int*);
+template void launch_topo<float>(Ctx&, int, const float*, const float*, const float*, const float*, float*, float*,
+                                 float*, int, const int*);
 
 static ChunkArgs chunk_args(const Ctx& C) {
     return ChunkArgs{C.d_ch_elem, C.d_ch_node, C.d_ch_nodes, C.d_ch_cstart, C.d_ch_csr, C.d_ch_lien};
@@ -1399,6 +1874,10 @@ int configure_element_kernels(Ctx& C) {
     if (rc == PHGPU_OK)
         rc = check(C, cudaFuncSetAttribute(k_chunk_ress, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ress_smem(C)),
                    "cudaFuncSetAttribute");
+    if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 8, 0>(C);
+    if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 6, 1>(C);
+    if (rc == PHGPU_OK) rc = configure_topo_kernels<float, 8, 0>(C);
+    if (rc == PHGPU_OK) rc = configure_topo_kernels<float, 6, 1>(C);
     return rc;
 }
 
@@ -1420,6 +1899,9 @@ void launch_elem_res(Ctx& C, int mode, const R* x, const R* ya, const R* yb, con
             k_chunk_res<R, RM_LIN><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
         ++C.launches;
     }
+    // hex and wedge blocks: ires = 1 writes res, ires = 2 (and the linearized form) rmes
+    if (mode == RM_RES) launch_topo<R>(C, TM_RES, x, ya, yb, ac, out, nullptr, nullptr, iabres, skip);
+    else launch_topo<R>(C, mode, x, ya, yb, ac, nullptr, out, nullptr, iabres, skip);
 }
 template void launch_elem_res<double>(Ctx&, int, const double*, const double*, const double*, const double*,
                                       double*, int, const int*);
@@ -1469,6 +1951,7 @@ void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rm
         k_chunk_full<R><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, ac, res, rmes, bd, P);
         ++C.launches;
     }
+    launch_topo<R>(C, TM_FULL, x, y, nullptr, ac, res, rmes, bd, 0, nullptr);
 }
 template void launch_elem_full<double>(Ctx&, const double*, const double*, const double*, double*, double*,
                                        double*);

@@ -54,6 +54,11 @@ struct Ctx {
     std::vector<int> col_start;   // ncol+1 (interior)
     std::vector<int> bcol_start;  // boundary
     int4* d_ien = nullptr;        // E (chunk order)
+    // hex and wedge blocks (colour order)
+    int nhex = 0, nwedge = 0;
+    int* d_ienh = nullptr;        // nhex*8
+    int* d_ienw = nullptr;        // nwedge*6
+    std::vector<int> hcol_start, wcol_start;
     // chunks (chunks.cu)
     int nchunk = 0, chunk_lmax = 0;
     std::vector<int> chunk_col_start;  // chunk colours
@@ -135,6 +140,10 @@ void launch_boundary(Ctx& C, const double* y, double* res);
 void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf, const float* acf, double* out);
 // outer residual with no FP64 arithmetic: double-float element-constant flux + FP32 increments
 void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* acf, double* out);
+// hex and wedge blocks; mode RM_RES/RM_MODRES/RM_LIN or 4 (ires = 3 + block diagonal)
+template <typename R>
+void launch_topo(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R* ac, R* res, R* rmes, R* bd,
+                 int iabres, const int* skip);
 void upload_tables(Ctx& C);
 int build_chunks(Ctx& C, const int* ien, const double* x_ref);
 int configure_element_kernels(Ctx& C);

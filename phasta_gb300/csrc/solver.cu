@@ -52,14 +52,14 @@ int sync(Ctx& C) {
 }
 
 // greedy first-fit colouring: no two elements of a colour share a node
-int colour(Ctx& C, int n_nodes, const int* ien4, int ne, std::vector<int>& order, std::vector<int>& start) {
+int colour(Ctx& C, int n_nodes, const int* ien, int nen, int ne, std::vector<int>& order, std::vector<int>& start) {
     std::vector<uint64_t> m0(n_nodes, 0), m1(n_nodes, 0);
     std::vector<int> col(ne);
     int ncol = 0;
     for (int e = 0; e < ne; ++e) {
-        const int* nd = ien4 + 4 * (size_t)e;
+        const int* nd = ien + nen * (size_t)e;
         uint64_t f0 = 0, f1 = 0;
-        for (int a = 0; a < 4; ++a) {
+        for (int a = 0; a < nen; ++a) {
             f0 |= m0[nd[a]];
             f1 |= m1[nd[a]];
         }
@@ -69,7 +69,7 @@ int colour(Ctx& C, int n_nodes, const int* ien4, int ne, std::vector<int>& order
         else return fail(C, PHGPU_ERR_UNSUPPORTED, "element colouring needs more than 128 colours");
         col[e] = c;
         ncol = std::max(ncol, c + 1);
-        for (int a = 0; a < 4; ++a) {
+        for (int a = 0; a < nen; ++a) {
             if (c < 64) m0[nd[a]] |= (1ull << c);
             else m1[nd[a]] |= (1ull << (c - 64));
         }
@@ -510,6 +510,8 @@ int solmfg_dev(Ctx& C, phgpu_stats* st) {
             fill0(C, C.d_res, sizeof(double) * n5);
             if (C.cfg.outer_residual == PHGPU_RES_SPLITDF) launch_elem_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res);
             else launch_elem_resh(C, C.d_y, C.d_ac, C.d_yf, C.d_acf, C.d_res);
+            // hex and wedge blocks: FP64 outer residual
+            launch_topo<double>(C, RM_RES, C.d_x, C.d_y, nullptr, C.d_ac, C.d_res, nullptr, nullptr, 0, nullptr);
             if (C.Eb > 0) launch_boundary(C, C.d_y, C.d_res);
             bc3res<double>(C, C.d_res);
         } else {
@@ -604,7 +606,10 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     using namespace phgpu;
     if (!out) return PHGPU_ERR_INVALID;
     *out = nullptr;
-    if (!m || !cfg || m->nshg <= 0 || m->nelem <= 0 || !m->ien || !m->x || !m->iBC || !m->BC || !m->iper)
+    if (!m || !cfg || m->nshg <= 0 || m->nelem < 0 || !m->x || !m->iBC || !m->BC || !m->iper)
+        return PHGPU_ERR_INVALID;
+    if (m->nhex < 0 || m->nwedge < 0 || (m->nelem > 0 && !m->ien) || (m->nhex > 0 && !m->ienh) ||
+        (m->nwedge > 0 && !m->ienw) || m->nelem + m->nhex + m->nwedge <= 0)
         return PHGPU_ERR_INVALID;
     if (m->nbelem < 0 || (m->nbelem > 0 && !m->ienb)) return PHGPU_ERR_INVALID;
     if (cfg->Kspace < 1 || cfg->Kspace > kMaxK || cfg->nGMRES < 1) return PHGPU_ERR_INVALID;
@@ -622,6 +627,12 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
         if (m->ien[i] < 0 || m->ien[i] >= N) { delete h; return PHGPU_ERR_INVALID; }
     for (size_t i = 0; i < 4 * (size_t)C.Eb; ++i)
         if (m->ienb[i] < 0 || m->ienb[i] >= N) { delete h; return PHGPU_ERR_INVALID; }
+    for (size_t i = 0; i < 8 * (size_t)m->nhex; ++i)
+        if (m->ienh[i] < 0 || m->ienh[i] >= N) { delete h; return PHGPU_ERR_INVALID; }
+    for (size_t i = 0; i < 6 * (size_t)m->nwedge; ++i)
+        if (m->ienw[i] < 0 || m->ienw[i] >= N) { delete h; return PHGPU_ERR_INVALID; }
+    C.nhex = m->nhex;
+    C.nwedge = m->nwedge;
     for (int n = 0; n < N; ++n) {
         const int p = m->iper[n];
         if (p < 0 || p >= N) { delete h; return PHGPU_ERR_INVALID; }
@@ -636,10 +647,12 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     int rc = PHGPU_OK;
     auto T = [&](int s) { if (rc == PHGPU_OK) rc = s; };
     // colouring
-    std::vector<int> border;
-    if (C.Eb > 0) T(colour(C, N, m->ienb, C.Eb, border, C.bcol_start));
+    std::vector<int> border, horder, worder;
+    if (C.Eb > 0) T(colour(C, N, m->ienb, 4, C.Eb, border, C.bcol_start));
+    if (C.nhex > 0) T(colour(C, N, m->ienh, 8, C.nhex, horder, C.hcol_start));
+    if (C.nwedge > 0) T(colour(C, N, m->ienw, 6, C.nwedge, worder, C.wcol_start));
     if (rc != PHGPU_OK) { phgpu_destroy(h); return rc; }
-    T(build_chunks(C, m->ien, m->x));
+    if (C.E > 0) T(build_chunks(C, m->ien, m->x));
     if (rc == PHGPU_OK) T(configure_element_kernels(C));
     if (rc != PHGPU_OK) { phgpu_destroy(h); return rc; }
     std::vector<int4> ienb(std::max(C.Eb, 1));
@@ -658,12 +671,10 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     std::vector<float> xf(3 * (size_t)N), xlo(3 * (size_t)N);
     for (int n = 0; n < N; ++n) {
         for (int d = 0; d < 3; ++d) {
-            x[3 * (size_t)n + d] = m->x[(size_t)d * N + n];
-        {
             const size_t i = 3 * (size_t)n + d;
+            x[i] = m->x[(size_t)d * N + n];
             xf[i] = (float)x[i];
             xlo[i] = (float)(x[i] - (double)xf[i]);
-        }
         }
         for (int k = 0; k < 6; ++k) bc[6 * (size_t)n + k] = m->BC[(size_t)k * N + n];
     }
@@ -695,6 +706,8 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     T(dalloc(C, &C.d_ienb, std::max(C.Eb, 1)));
     T(dalloc(C, &C.d_iBCB, std::max(C.Eb, 1)));
     T(dalloc(C, &C.d_BCB, 18 * (size_t)std::max(C.Eb, 1)));
+    T(dalloc(C, &C.d_ienh, 8 * (size_t)std::max(C.nhex, 1)));
+    T(dalloc(C, &C.d_ienw, 6 * (size_t)std::max(C.nwedge, 1)));
     T(dalloc(C, &C.d_x, 3 * (size_t)N));
     T(dalloc(C, &C.d_xf, 3 * (size_t)N));
     T(dalloc(C, &C.d_xlo, 3 * (size_t)N));
@@ -733,6 +746,18 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
         T(check(C, cudaMemcpy(d, s, bytes, cudaMemcpyHostToDevice), "upload mesh"));
     };
     up(C.d_ienb, ienb.data(), sizeof(int4) * ienb.size());
+    if (C.nhex > 0) {
+        std::vector<int> v(8 * (size_t)C.nhex);
+        for (int i = 0; i < C.nhex; ++i)
+            for (int a = 0; a < 8; ++a) v[8 * (size_t)i + a] = m->ienh[8 * (size_t)horder[i] + a];
+        up(C.d_ienh, v.data(), sizeof(int) * v.size());
+    }
+    if (C.nwedge > 0) {
+        std::vector<int> v(6 * (size_t)C.nwedge);
+        for (int i = 0; i < C.nwedge; ++i)
+            for (int a = 0; a < 6; ++a) v[6 * (size_t)i + a] = m->ienw[6 * (size_t)worder[i] + a];
+        up(C.d_ienw, v.data(), sizeof(int) * v.size());
+    }
     up(C.d_iBCB, ibcb.data(), sizeof(int) * ibcb.size());
     up(C.d_BCB, bcb.data(), sizeof(double) * bcb.size());
     up(C.d_x, x.data(), sizeof(double) * x.size());
@@ -766,7 +791,7 @@ int phgpu_destroy(phgpu_ctx* h) {
     Ctx& C = h->c;
     if (C.stream) cudaStreamSynchronize(C.stream);
     void* ptrs[] = {C.d_ch_elem, C.d_ch_node, C.d_ch_nodes, C.d_ch_cstart, C.d_ch_csr, C.d_ch_lien,
-                    C.d_bdstage, C.d_ien, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_xlo, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
+                    C.d_bdstage, C.d_ien, C.d_ienh, C.d_ienw, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_xlo, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
                     C.d_slaves, C.d_mst, C.d_slv_start, C.d_slv, C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_res,
                     C.d_rmes, C.d_Dy, C.d_ypre, C.d_t64, C.d_t64b, C.d_bd, C.d_yf, C.d_ylo, C.d_acf, C.d_resf, C.d_rmesf,
                     C.d_t32, C.d_t32b, C.d_bdf, C.d_U, C.d_scal, C.d_part, C.d_count, C.d_flag};

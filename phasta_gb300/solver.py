@@ -90,10 +90,13 @@ class GpuSolver:
         self._iBC = np.ascontiguousarray(case.iBC, dtype=np.int32)
         self._BC = np.ascontiguousarray(case.BC, dtype=np.float64).reshape(-1)
         self._iper = np.ascontiguousarray(case.iper, dtype=np.int32)
-        m = L.Mesh(self.nshg, case.nelem, L.iptr(self._ien), L.dptr(self._x), case.nbelem,
+        self._ienh = np.ascontiguousarray(case.ienh, dtype=np.int32).reshape(-1)
+        self._ienw = np.ascontiguousarray(case.ienw, dtype=np.int32).reshape(-1)
+        m = L.Mesh(self.nshg, case.nelem, L.iptr(self._ien) if case.nelem else None, L.dptr(self._x), case.nbelem,
                    L.iptr(self._ienb) if case.nbelem else None, L.iptr(self._iBCB) if case.nbelem else None,
                    L.dptr(self._BCB) if case.nbelem else None, L.iptr(self._iBC), L.dptr(self._BC),
-                   L.iptr(self._iper))
+                   L.iptr(self._iper), case.nhex, L.iptr(self._ienh) if case.nhex else None, case.nwedge,
+                   L.iptr(self._ienw) if case.nwedge else None)
         self._cfg = _config(self.params)
         h = C.c_void_p()
         rc = self.lib.phgpu_create(C.byref(m), C.byref(self._cfg), C.byref(h))
