@@ -57,24 +57,37 @@ class ClockSampler:
         self._t = None
 
     def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                     timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([s.strip() for s in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        # one nvidia-smi process streaming a sample every 50 ms (-lms), started before the timed region
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                           "--format=csv,noheader,nounits", "-lms", "50"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            return
+        for line in self._proc.stdout:
+            if self._stop.is_set():
+                break
+            line = line.strip()
+            if line:
+                self.samples.append([s.strip() for s in line.split(",")])
 
     def __enter__(self):
+        self._proc = None
         self._t = threading.Thread(target=self._run, daemon=True)
         self._t.start()
+        time.sleep(0.15)  # the sampling process is up before the timed region starts
+        self.samples.clear()
         return self
 
     def __exit__(self, *a):
+        time.sleep(0.06)
         self._stop.set()
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
         if self._t:
             self._t.join(timeout=10)
 

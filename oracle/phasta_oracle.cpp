@@ -175,7 +175,7 @@ const Topo& topo(int lcsyst) {
 // ---------------------------------------------------------------------------
 void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const double (*yl)[5],
                 const double (*ycl)[5], const double (*acl)[5], const double (*xl)[3],
-                double (*rl)[5], double (*rml)[5], double (*bdl)[5][5]) {
+                double (*rl)[5], double (*rml)[5], double (*bdl)[5][5], const double (*ql)[12] = nullptr) {
     const int nshl = tp.nshl, nenl = tp.nshl, ngauss = tp.ngauss;
     const double Rgas = c.Rgas, gamma = c.gamma, gamma1 = c.gamma1;
 
@@ -361,6 +361,15 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
                 for (int j = 0; j < 5; ++j) s = s + A0[k][j] * aci[j];
                 rLyi[k] = s;
             }
+        // idiff >= 1: divergence of the reconstructed diffusive flux (e3ivar.f:363-395),
+        // subtracted from the least-squares term (e3ls.f:147-156)
+        if (ql && c.idiff >= 1 && (ires == 1 || ires == 3)) {
+            double divqi[4] = {0, 0, 0, 0};
+            for (int n = 0; n < nshl; ++n)
+                for (int k = 0; k < 4; ++k)
+                    divqi[k] = divqi[k] + shg[n][0] * ql[n][k] + shg[n][1] * ql[n][4 + k] + shg[n][2] * ql[n][8 + k];
+            for (int k = 0; k < 4; ++k) rLyi[1 + k] = rLyi[1 + k] - divqi[k];
+        }
 
         // ---------------- e3tau.f:140-181 (itau = 0) + e3gijd (e3tau.f:1397-1508) ----------------
         double gijd[6];
@@ -708,20 +717,133 @@ void parallel_for(int n, int nthreads, F&& f) {
     for (auto& x : th) x.join();
 }
 
+// e3q.f:54-191 with e3qvar.f (idiff = 1) for one element: ql(a,1:12) += N_a WdetJ qdi,
+// rmassl(a) += N_a WdetJ, qdi the viscous flux at the point
+void e3q_element(const or_common& c, const Topo& tp, const double (*ycl)[5], const double (*xl)[3],
+                 double (*ql)[12], double* rmassl) {
+    const int nshl = tp.nshl, nenl = tp.nshl;
+    for (int intp = 0; intp < tp.ngauss; ++intp) {
+        if (tp.Qwt[intp] == zero) continue;
+        const double* shape = tp.shp[intp];
+        const double (*shgl)[8] = tp.shgl[intp];
+        double u1 = 0, u2 = 0, u3 = 0;
+        for (int n = 0; n < nshl; ++n) {
+            u1 = u1 + shape[n] * ycl[n][1];
+            u2 = u2 + shape[n] * ycl[n][2];
+            u3 = u3 + shape[n] * ycl[n][3];
+        }
+        // getthm ithm = 7: cp; getDiff: constant mu, Stokes (getdiff.f:127,164,171)
+        const double cp = c.Rgas * c.gamma / c.gamma1;
+        const double rmu = c.rmu, rlm = -pt66 * rmu, rlm2mu = rlm + two * rmu, con = rmu * cp / c.pr;
+        // e3metric.f:22-77
+        double dxdxi[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int n = 0; n < nenl; ++n)
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) dxdxi[i][j] = dxdxi[i][j] + xl[n][i] * shgl[j][n];
+        double dxidx[3][3];
+        dxidx[0][0] = dxdxi[1][1] * dxdxi[2][2] - dxdxi[2][1] * dxdxi[1][2];
+        dxidx[0][1] = dxdxi[2][1] * dxdxi[0][2] - dxdxi[0][1] * dxdxi[2][2];
+        dxidx[0][2] = dxdxi[0][1] * dxdxi[1][2] - dxdxi[0][2] * dxdxi[1][1];
+        const double tmp = one / (dxidx[0][0] * dxdxi[0][0] + dxidx[0][1] * dxdxi[1][0] +
+                                  dxidx[0][2] * dxdxi[2][0]);
+        dxidx[0][0] = dxidx[0][0] * tmp;
+        dxidx[0][1] = dxidx[0][1] * tmp;
+        dxidx[0][2] = dxidx[0][2] * tmp;
+        dxidx[1][0] = (dxdxi[1][2] * dxdxi[2][0] - dxdxi[1][0] * dxdxi[2][2]) * tmp;
+        dxidx[1][1] = (dxdxi[0][0] * dxdxi[2][2] - dxdxi[2][0] * dxdxi[0][2]) * tmp;
+        dxidx[1][2] = (dxdxi[1][0] * dxdxi[0][2] - dxdxi[0][0] * dxdxi[1][2]) * tmp;
+        dxidx[2][0] = (dxdxi[1][0] * dxdxi[2][1] - dxdxi[1][1] * dxdxi[2][0]) * tmp;
+        dxidx[2][1] = (dxdxi[2][0] * dxdxi[0][1] - dxdxi[0][0] * dxdxi[2][1]) * tmp;
+        dxidx[2][2] = (dxdxi[0][0] * dxdxi[1][1] - dxdxi[0][1] * dxdxi[1][0]) * tmp;
+        const double WdetJ = tp.Qwt[intp] / tmp;
+        double shg[8][3];
+        for (int n = 0; n < nshl; ++n)
+            for (int i = 0; i < 3; ++i)
+                shg[n][i] = shgl[0][n] * dxidx[0][i] + shgl[1][n] * dxidx[1][i] + shgl[2][n] * dxidx[2][i];
+        double g[3][5] = {{0}};
+        for (int n = 0; n < nshl; ++n)
+            for (int i = 0; i < 3; ++i)
+                for (int k = 0; k < 5; ++k) g[i][k] = g[i][k] + shg[n][i] * ycl[n][k];
+        const double* g1 = g[0];
+        const double* g2 = g[1];
+        const double* g3 = g[2];
+        double qdi[12];
+        qdi[0] = rlm2mu * g1[1] + rlm * g2[2] + rlm * g3[3];
+        qdi[1] = rmu * g1[2] + rmu * g2[1];
+        qdi[2] = rmu * g1[3] + rmu * g3[1];
+        qdi[3] = rlm2mu * u1 * g1[1] + rmu * u2 * g1[2] + rmu * u3 * g1[3] + rmu * u2 * g2[1] +
+                 rlm * u1 * g2[2] + rmu * u3 * g3[1] + rlm * u1 * g3[3] + con * g1[4];
+        qdi[4] = rmu * g1[2] + rmu * g2[1];
+        qdi[5] = rlm * g1[1] + rlm2mu * g2[2] + rlm * g3[3];
+        qdi[6] = rmu * g2[3] + rmu * g3[2];
+        qdi[7] = rlm * u2 * g1[1] + rmu * u1 * g1[2] + rmu * u1 * g2[1] + rlm2mu * u2 * g2[2] +
+                 rmu * u3 * g2[3] + rmu * u3 * g3[2] + rlm * u2 * g3[3] + con * g2[4];
+        qdi[8] = rmu * g1[3] + rmu * g3[1];
+        qdi[9] = rmu * g2[3] + rmu * g3[2];
+        qdi[10] = rlm * g1[1] + rlm * g2[2] + rlm2mu * g3[3];
+        qdi[11] = rlm * u3 * g1[1] + rmu * u1 * g1[3] + rlm * u3 * g2[2] + rmu * u2 * g2[3] +
+                  rmu * u1 * g3[1] + rmu * u2 * g3[2] + rlm2mu * u3 * g3[3] + con * g3[4];
+        for (int i = 0; i < nshl; ++i)
+            for (int k = 0; k < 12; ++k) ql[i][k] = ql[i][k] + shape[i] * WdetJ * qdi[k];
+        for (int i = 0; i < nshl; ++i) rmassl[i] = rmassl[i] + shape[i] * WdetJ;
+    }
+}
+
+// AsIq (asiq.f) over every block + qpbc (qpbc.f): the lumped L2 reconstruction of the
+// diffusive flux, qres(nshg,12) column-major
+void reconstruct_q(const or_common& c, const or_mesh& m, const double* y, double* qres) {
+    const int nshg = m.nshg;
+    std::vector<double> rmass(nshg, 0.0);
+    std::fill(qres, qres + 12 * (size_t)nshg, 0.0);
+    auto run = [&](const Topo& tp, const int* ie) {
+        double ycl[8][5], xl[8][3], ql[8][12] = {{0}}, rm[8] = {0};
+        for (int a = 0; a < tp.nshl; ++a) {
+            gather_y(y, nshg, ie[a], ycl[a]);
+            gather_x(m.x, nshg, ie[a], xl[a]);
+        }
+        e3q_element(c, tp, ycl, xl, ql, rm);
+        for (int k = 0; k < 12; ++k)
+            for (int a = 0; a < tp.nshl; ++a) qres[k * (size_t)nshg + ie[a]] += ql[a][k];
+        for (int a = 0; a < tp.nshl; ++a) rmass[ie[a]] += rm[a];
+    };
+    for (int b = 0; b < m.nblk; ++b)
+        for (int e = m.blk_start[b]; e < m.blk_start[b + 1]; ++e) run(topo(1), m.ien + 4 * (size_t)e);
+    for (int e = 0; e < m.nhex; ++e) run(topo(2), m.ienh + 8 * (size_t)e);
+    for (int e = 0; e < m.nwedge; ++e) run(topo(3), m.ienw + 6 * (size_t)e);
+    // qpbc.f: periodic slaves summed into masters, then copied back; lumped mass inverted
+    for (int j = 0; j < nshg; ++j)
+        if ((m.iBC[j] >> 10) & 1) {
+            const int i = m.iper[j];
+            rmass[i] = rmass[i] + rmass[j];
+            for (int k = 0; k < 12; ++k) qres[k * (size_t)nshg + i] += qres[k * (size_t)nshg + j];
+        }
+    for (int j = 0; j < nshg; ++j)
+        if ((m.iBC[j] >> 10) & 1) {
+            const int i = m.iper[j];
+            rmass[j] = rmass[i];
+            for (int k = 0; k < 12; ++k) qres[k * (size_t)nshg + j] = qres[k * (size_t)nshg + i];
+        }
+    for (int j = 0; j < nshg; ++j) rmass[j] = one / rmass[j];
+    for (int k = 0; k < 12; ++k)
+        for (int j = 0; j < nshg; ++j) qres[k * (size_t)nshg + j] = rmass[j] * qres[k * (size_t)nshg + j];
+}
+
 // gather (localy.f, localx.f), e3, scatter (local.f:66-80) of one interior element
 void one_element(const or_common& c, const Topo& tp, const or_mesh& m, const int* ie, int ires, int iprec,
                  const double* yp, const double* yc, const double* ac, double* res, double* rmes, double* bd,
-                 int iabres) {
+                 int iabres, const double* qres) {
     const int nshg = m.nshg, nen = tp.nshl;
-    double yl[8][5], ycl[8][5], acl[8][5], xl[8][3];
+    double yl[8][5], ycl[8][5], acl[8][5], xl[8][3], ql[8][12];
     for (int a = 0; a < nen; ++a) {
         gather_y(yp, nshg, ie[a], yl[a]);
         gather_y(yc, nshg, ie[a], ycl[a]);
         gather_y(ac, nshg, ie[a], acl[a]);
         gather_x(m.x, nshg, ie[a], xl[a]);
+        if (qres)
+            for (int k = 0; k < 12; ++k) ql[a][k] = qres[k * (size_t)nshg + ie[a]];
     }
     double rl[8][5] = {{0}}, rml[8][5] = {{0}}, bdl[8][5][5] = {{{0}}};
-    e3_element(c, tp, ires, iprec, yl, ycl, acl, xl, rl, rml, iprec ? bdl : nullptr);
+    e3_element(c, tp, ires, iprec, yl, ycl, acl, xl, rl, rml, iprec ? bdl : nullptr, qres ? ql : nullptr);
     if (iabres == 1)
         for (int a = 0; a < nen; ++a)
             for (int k = 0; k < 5; ++k) rml[a][k] = std::fabs(rml[a][k]);
@@ -741,7 +863,8 @@ void one_element(const or_common& c, const Topo& tp, const or_mesh& m, const int
 // ires 3: res, rmes, (BDiag if iprec); ires 2: rmes from (yp, yc); ires 1: res.
 void element_sweep(const or_common& c, const or_mesh& m, int ires, int iprec,
                    const double* yp, const double* yc, const double* ac,
-                   double* res, double* rmes, double* bd, int iabres, int nthreads) {
+                   double* res, double* rmes, double* bd, int iabres, int nthreads,
+                   const double* qres = nullptr) {
     const int nshg = m.nshg;
     const int ngrp = m.ngrp > 0 ? m.ngrp : 1;
     for (int gI = 0; gI < ngrp; ++gI) {
@@ -753,15 +876,16 @@ void element_sweep(const or_common& c, const or_mesh& m, int ires, int iprec,
         auto run_block = [&](int bi) {
             const int blk = b0 + bi;
             for (int e = m.blk_start[blk]; e < m.blk_start[blk + 1]; ++e)
-                one_element(c, topo(1), m, m.ien + 4 * (size_t)e, ires, iprec, yp, yc, ac, res, rmes, bd, iabres);
+                one_element(c, topo(1), m, m.ien + 4 * (size_t)e, ires, iprec, yp, yc, ac, res, rmes, bd, iabres,
+                            qres);
         };
         parallel_for(nb, nthreads, run_block);
     }
     // hex and wedge blocks (elmmfg.f:113-146 block loop), element by element
     for (int e = 0; e < m.nhex; ++e)
-        one_element(c, topo(2), m, m.ienh + 8 * (size_t)e, ires, iprec, yp, yc, ac, res, rmes, bd, iabres);
+        one_element(c, topo(2), m, m.ienh + 8 * (size_t)e, ires, iprec, yp, yc, ac, res, rmes, bd, iabres, qres);
     for (int e = 0; e < m.nwedge; ++e)
-        one_element(c, topo(3), m, m.ienw + 6 * (size_t)e, ires, iprec, yp, yc, ac, res, rmes, bd, iabres);
+        one_element(c, topo(3), m, m.ienw + 6 * (size_t)e, ires, iprec, yp, yc, ac, res, rmes, bd, iabres, qres);
 }
 
 void boundary_sweep(const or_common& c, const or_mesh& m, const double* y, double* res) {
@@ -1196,7 +1320,13 @@ void or_elmmfg(const or_common* c, const or_mesh* m, const double* y, const doub
     std::memset(res, 0, sizeof(double) * 5 * N);
     std::memset(rmes, 0, sizeof(double) * 5 * N);
     if (iprec) std::memset(bdiag, 0, sizeof(double) * 25 * N);
-    element_sweep(*c, *m, 3, iprec, y, y, ac, res, rmes, iprec ? bdiag : nullptr, 0, nthreads);
+    std::vector<double> qres;
+    if (c->idiff == 1) {
+        qres.resize(12 * N);
+        reconstruct_q(*c, *m, y, qres.data());
+    }
+    element_sweep(*c, *m, 3, iprec, y, y, ac, res, rmes, iprec ? bdiag : nullptr, 0, nthreads,
+                  qres.empty() ? nullptr : qres.data());
     boundary_sweep(*c, *m, y, res);  // AsBMFG: rml is zero while Jactyp == 0 (e3b.f:244-246)
     or_bc3res(m, y, res, c);
     or_bc3res(m, y, rmes, c);
@@ -1214,7 +1344,12 @@ void or_elmres(const or_common* c, const or_mesh* m, const double* y, const doub
                double* res, int nthreads) {
     const size_t N = m->nshg;
     std::memset(res, 0, sizeof(double) * 5 * N);
-    element_sweep(*c, *m, 1, 0, y, y, ac, res, nullptr, nullptr, 0, nthreads);
+    std::vector<double> qres;
+    if (c->idiff == 1) {
+        qres.resize(12 * N);
+        reconstruct_q(*c, *m, y, qres.data());
+    }
+    element_sweep(*c, *m, 1, 0, y, y, ac, res, nullptr, nullptr, 0, nthreads, qres.empty() ? nullptr : qres.data());
     boundary_sweep(*c, *m, y, res);
     or_bc3res(m, y, res, c);
 }

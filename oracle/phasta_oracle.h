@@ -39,6 +39,7 @@ typedef struct {
     double etol, epsM;                /* Krylov tolerance, sqrt(machine eps) */
     double eGMRES;                    /* finite-difference interval (in/out) */
     int    iter, istep;               /* Newton iteration (1-based) and time step (0-based) */
+    int    idiff;                     /* 0, or 1: global reconstruction of the diffusive flux */
 } or_common;
 
 typedef struct {

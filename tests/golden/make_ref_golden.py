@@ -38,6 +38,9 @@ CASES = [
     ("channel4_restart", lambda: channel(4, ac_scale=0.05, Kspace=3, nGMRES=2), ("elm", "solve")),
     # tet, hex (lcsyst 2) and wedge (lcsyst 3) blocks
     ("mixed3", lambda: mixed(3, 3, (3, 3, 2)), ALL),
+    # idiff = 1: the diffusive flux reconstructed (AsIq/e3q/qpbc) and its divergence in e3LS
+    ("channel4_idiff", lambda: channel(4, ac_scale=0.05, idiff=1), ALL),
+    ("mixed3_idiff", lambda: mixed(3, 3, (3, 3, 2), idiff=1), ("elm", "solve")),
 ]
 
 

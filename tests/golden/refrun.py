@@ -36,6 +36,8 @@ SOURCES = [
     "compressible/itrres.f", "compressible/asires.f", "compressible/i3lu.f", "compressible/solmfg.f",
     "compressible/au1mfg.f", "compressible/au2mfg.f", "compressible/itrfdi.f", "compressible/shuffle.f",
     "compressible/itrPC.f", "common/mpitools.f", "common/clear.f",
+    # idiff = 1: global reconstruction of the diffusive flux
+    "compressible/asiq.f", "compressible/e3q.f", "compressible/e3qvar.f", "common/qpbc.f",
 ]
 # rstat.f only prints statistics, and SolMFG calls it with two of its three
 # arguments (solmfg.f:367 vs rstat.f:1); its totres (rstat.f:108) is computed
@@ -112,10 +114,11 @@ class RefPhasta:
         G.datmat[0, 1, 0] = p["rmu"]
         G.pr, G.rgas, G.gamma, G.gamma1 = p["pr"], p["Rgas"], p["gamma"], p["gamma1"]
         G.dtgl, G.almi, G.alfi, G.gami = p["Dtgl"], p["almi"], p["alfi"], p["gami"]
-        G.lhs, G.itau, G.ipord, G.idiff, G.isurf = 0, p["itau"], p["ipord"], 0, 0
+        G.lhs, G.itau, G.ipord, G.idiff, G.isurf = 0, p["itau"], p["ipord"], p.get("idiff", 0), 0
         G.dtsfct, G.taucfct, G.temper = p["dtsfct"], p["taucfct"], p["temper"]
         G.ivart, G.navier, G.jactyp, G.idc = p["ivart"], p["Navier"], 0, 0
-        G.iremovestabtimeterm, G.entropypressure, G.idflx = p["iremoveStabTimeTerm"], p["EntropyPressure"], 0
+        G.iremovestabtimeterm, G.entropypressure = p["iremoveStabTimeTerm"], p["EntropyPressure"]
+        G.idflx = 12 if p.get("idiff", 0) >= 1 else 0  # (nflow-1)*nsd, solmfg.f:61-63
         G.kspace, G.ngmres, G.miniters = p["Kspace"], p["nGMRES"], p["minIters"]
         G.epstol[0] = p["etol"]
         G.etol = p["etol"]  # itrdrv.f:433
