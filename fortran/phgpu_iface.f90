@@ -19,7 +19,8 @@ module phgpu_iface
      real(c_double) :: etol, epsM, eGMRES
      integer(c_int) :: iter, istep
      integer(c_int) :: precision, ap_mode, outer_residual
-     integer(c_int) :: reserved(5)
+     integer(c_int) :: idiff         ! 0 or 1 (global diffusive-flux reconstruction)
+     integer(c_int) :: reserved(4)
   end type
 
   type, bind(C) :: phgpu_mesh

@@ -82,7 +82,10 @@ typedef struct {
                                         (no FP64 arithmetic: the Euler flux of each element's node-3
                                         state in double-float, its increment over the element and
                                         the other terms in FP32) */
-    int reserved[5];
+    int idiff;                       /* 0, or 1: global reconstruction of the diffusive flux
+                                        (elmmfg.f:56-111) whose divergence enters the residual's
+                                        least-squares term */
+    int reserved[4];
 } phgpu_config;
 
 /* Mesh and boundary-condition arrays (what the reference keeps in

@@ -36,7 +36,8 @@ class Config(C.Structure):
         ("Kspace", C.c_int), ("nGMRES", C.c_int), ("minIters", C.c_int),
         ("etol", C.c_double), ("epsM", C.c_double), ("eGMRES", C.c_double),
         ("iter", C.c_int), ("istep", C.c_int),
-        ("precision", C.c_int), ("ap_mode", C.c_int), ("outer_residual", C.c_int), ("reserved", C.c_int * 5),
+        ("precision", C.c_int), ("ap_mode", C.c_int), ("outer_residual", C.c_int), ("idiff", C.c_int),
+        ("reserved", C.c_int * 4),
     ]
 
 

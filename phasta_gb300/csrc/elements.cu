@@ -330,7 +330,7 @@ __device__ __forceinline__ void lds5(const R* __restrict__ s, int l, R (&o)[5]) 
 // writes the four nodal contributions (already weighted) to o[a][k]
 template <typename R, int MODE>
 __device__ __forceinline__ void elem_res(const Phys<R>& P, const R (&xl)[4][3], const R (&va)[4][5],
-                                         const R (&vb)[4][5], R (&o)[4][5]) {
+                                         const R (&vb)[4][5], R (&o)[4][5], const R* divq = nullptr) {
     Geo<R> geo;
     geometry(xl, geo);
     const R (&base)[4][5] = (MODE == RM_RES) ? va : vb;
@@ -383,6 +383,10 @@ __device__ __forceinline__ void elem_res(const Phys<R>& P, const R (&xl)[4][3], 
             for (int k = 0; k < 5; ++k) {
                 r16[k] = a0a[k];
                 aig[k] = aig[k] + a0a[k];  // rLyi += A0 aci (e3ls.f:105-143)
+            }
+            if (divq) {  // idiff = 1: rLyi -= div q (e3ls.f:147-156)
+#pragma unroll
+                for (int k = 0; k < 4; ++k) aig[1 + k] -= divq[k];
             }
         } else {
 #pragma unroll
@@ -444,21 +448,42 @@ __device__ __forceinline__ void elem_res(const Phys<R>& P, const R (&xl)[4][3], 
             o[a][k] = geo.WdetJ * (geo.shg[a][0] * S[0][k] + geo.shg[a][1] * S[1][k] + geo.shg[a][2] * S[2][k] + Tn[a][k]);
 }
 
+// div q of the reconstructed nodal diffusive flux (e3ivar.f:374-395): q staged as 12 values
+// per chunk node (row-major 3 x 4: flux direction i, component k)
+template <typename R>
+__device__ __forceinline__ void tet_divq(const R (&xl)[4][3], const R* __restrict__ sq, const int (&nd)[4],
+                                         R (&divq)[4]) {
+    Geo<R> geo;
+    geometry(xl, geo);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        R acc = R(0);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const R* q = sq + 12 * nd[a];
+            acc += geo.shg[a][0] * q[k] + geo.shg[a][1] * q[4 + k] + geo.shg[a][2] * q[8 + k];
+        }
+        divq[k] = acc;
+    }
+}
+
 template <typename R, int MODE>
 __global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? PHGPU_RES32_MINB : 2)
 k_chunk_res(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restrict__ ya,
             const R* __restrict__ yb, const R* __restrict__ ac, R* __restrict__ out, Phys<R> P, int iabres,
-            const int* __restrict__ skip) {
+            const int* __restrict__ skip, const R* __restrict__ ql = nullptr) {
     if (skip && *skip) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* sm = reinterpret_cast<R*>(smem_raw);
     const int c = chunk0 + blockIdx.x;
     const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
     const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+    const bool with_q = (MODE == RM_RES) && ql != nullptr;
     R* sx = sm;
     R* sa = sx + 3 * nn;
     R* sb = sa + 5 * nn;
-    R* slot = sb + 5 * nn;
+    R* sq = sb + 5 * nn;                  // idiff = 1: reconstructed flux, 12 per node
+    R* slot = sq + (with_q ? 12 * nn : 0);
     const R* bsrc = (MODE == RM_RES) ? ac : yb;
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
         const int gn = ca.nodes[n0 + l];
@@ -469,6 +494,8 @@ k_chunk_res(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restri
             sa[5 * l + k] = ldg(ya + 5 * (size_t)gn + k);
             sb[5 * l + k] = ldg(bsrc + 5 * (size_t)gn + k);
         }
+        if (with_q)
+            for (int k = 0; k < 12; ++k) sq[12 * l + k] = ldg(ql + 13 * (size_t)gn + k);
     }
     __syncthreads();
     if ((int)threadIdx.x < ne) {
@@ -483,7 +510,13 @@ k_chunk_res(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restri
             lds5(sb, nd[a], vb[a]);
         }
         R o[4][5];
-        elem_res<R, MODE>(P, xl, va, vb, o);
+        if (with_q) {
+            R divq[4];
+            tet_divq(xl, sq, nd, divq);
+            elem_res<R, MODE>(P, xl, va, vb, o, divq);
+        } else {
+            elem_res<R, MODE>(P, xl, va, vb, o);
+        }
         R* sl = slot + 20 * threadIdx.x;
 #pragma unroll
         for (int a = 0; a < 4; ++a)
@@ -502,6 +535,105 @@ k_chunk_res(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restri
         R* og = out + 5 * (size_t)ca.nodes[n0 + l];
 #pragma unroll
         for (int k = 0; k < 5; ++k) og[k] += acc[k];
+    }
+}
+
+// --------------------------------------------------------------------------
+// idiff = 1: lumped L2 reconstruction of the diffusive flux (AsIq/e3q.f:54-191).
+// Per element and node a: sum_q N_a WdetJ qdi(q) (12 values, qdi the viscous
+// flux of e3q.f at point q) and sum_q N_a WdetJ (lumped mass); out holds 13
+// values per node (flux row-major (direction, component), then the mass).
+// --------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void visc_flux12(const Phys<R>& P, const Visc<R>& vs, R u0, R u1, R u2, R (&q)[12]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        q[4 * i + 0] = vs.t[i][0];
+        q[4 * i + 1] = vs.t[i][1];
+        q[4 * i + 2] = vs.t[i][2];
+        q[4 * i + 3] = u0 * vs.t[i][0] + u1 * vs.t[i][1] + u2 * vs.t[i][2] + vs.q[i];
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kChunk)
+k_chunk_qrec(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restrict__ y, R* __restrict__ out,
+             Phys<R> P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* sm = reinterpret_cast<R*>(smem_raw);
+    const int c = chunk0 + blockIdx.x;
+    const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
+    const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+    R* sx = sm;
+    R* sy = sx + 3 * nn;
+    R* slot = sy + 5 * nn;  // 13 per (element, corner)
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        const int gn = ca.nodes[n0 + l];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) sx[3 * l + d] = ldg(x + 3 * (size_t)gn + d);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) sy[5 * l + k] = ldg(y + 5 * (size_t)gn + k);
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < ne) {
+        const ushort4 ln = ca.lien[e0 + threadIdx.x];
+        const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
+        R xl[4][3], yl[4][5];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) xl[a][d] = sx[3 * nd[a] + d];
+            lds5(sy, nd[a], yl[a]);
+        }
+        Geo<R> geo;
+        geometry(xl, geo);
+        R g[3][5];
+        gradients(geo, yl, g);
+        Visc<R> vs;
+        viscous(P, g, vs);
+        R ql[4][13];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int k = 0; k < 13; ++k) ql[a][k] = R(0);
+#pragma unroll 1
+        for (int q = 0; q < 4; ++q) {
+            R N[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) N[a] = shp<R>(q, a);
+            const R u0 = N[0] * yl[0][1] + N[1] * yl[1][1] + N[2] * yl[2][1] + N[3] * yl[3][1];
+            const R u1 = N[0] * yl[0][2] + N[1] * yl[1][2] + N[2] * yl[2][2] + N[3] * yl[3][2];
+            const R u2 = N[0] * yl[0][3] + N[1] * yl[1][3] + N[2] * yl[2][3] + N[3] * yl[3][3];
+            R qd[12];
+            visc_flux12(P, vs, u0, u1, u2, qd);
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const R w = N[a] * geo.WdetJ;
+#pragma unroll
+                for (int k = 0; k < 12; ++k) ql[a][k] += w * qd[k];
+                ql[a][12] += w;
+            }
+        }
+        R* sl = slot + 52 * threadIdx.x;
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int k = 0; k < 13; ++k) sl[13 * a + k] = ql[a][k];
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+        R acc[13];
+#pragma unroll
+        for (int k = 0; k < 13; ++k) acc[k] = R(0);
+        const int s0 = ca.cstart[n0 + l], s1 = ca.cstart[n0 + l + 1];
+        for (int s = s0; s < s1; ++s) {
+            const R* sl = slot + 13 * (int)ca.csr[s];
+#pragma unroll
+            for (int k = 0; k < 13; ++k) acc[k] += sl[k];
+        }
+        R* og = out + 13 * (size_t)ca.nodes[n0 + l];
+#pragma unroll
+        for (int k = 0; k < 13; ++k) og[k] += acc[k];
     }
 }
 
@@ -731,7 +863,7 @@ __device__ __forceinline__ df64 df_diff(float ah, float al, float bh, float bl) 
 __global__ void __launch_bounds__(kChunk, PHGPU_RESS_MINB)
 k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float* __restrict__ xlo,
              const float* __restrict__ yh, const float* __restrict__ ylo, const float* __restrict__ acf,
-             double* __restrict__ out, Phys<float> Pf, DfConst K) {
+             double* __restrict__ out, Phys<float> Pf, DfConst K, const float* __restrict__ ql) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sm = reinterpret_cast<float*>(smem_raw);
     const int c = chunk0 + blockIdx.x;
@@ -742,7 +874,8 @@ k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float
     float* syh = sxl + 3 * nn;
     float* syl = syh + 5 * nn;
     float* sa = syl + 5 * nn;
-    float* slot = sa + 5 * nn;
+    float* sq = sa + 5 * nn;              // idiff = 1: reconstructed flux, 12 per node
+    float* slot = sq + (ql ? 12 * nn : 0);
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
         const size_t gn = ca.nodes[n0 + l];
 #pragma unroll
@@ -756,6 +889,8 @@ k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float
             syl[5 * l + k] = __ldg(ylo + 5 * gn + k);
             sa[5 * l + k] = __ldg(acf + 5 * gn + k);
         }
+        if (ql)
+            for (int k = 0; k < 12; ++k) sq[12 * l + k] = __ldg(ql + 13 * gn + k);
     }
     __syncthreads();
     if ((int)threadIdx.x < ne) {
@@ -789,6 +924,19 @@ k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float
                     g[i][k] = geo.shg[0][i] * dl[0][k] + geo.shg[1][i] * dl[1][k] + geo.shg[2][i] * dl[2][k];
             Visc<float> vs;
             if (Pf.navier) viscous(Pf, g, vs);
+            float divq[4] = {0.f, 0.f, 0.f, 0.f};  // idiff = 1 (e3ivar.f:374-395)
+            if (ql) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        const float* q = sq + 12 * nd[a];
+                        acc += geo.shg[a][0] * q[k] + geo.shg[a][1] * q[4 + k] + geo.shg[a][2] * q[8 + k];
+                    }
+                    divq[k] = acc;
+                }
+            }
             const float pr = yl[3][0], Tr = yl[3][4];
             const float ur[3] = {yl[3][1], yl[3][2], yl[3][3]};
             const float rhor = pr * Pf.rRgas / Tr;
@@ -822,10 +970,10 @@ k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float
                 a0_v(b, aq, a0a);
                 float tl[5];
                 tl[0] = b.tau[0] * (aig[0] + a0a[0]);
-                tl[1] = b.tau[1] * (aig[1] + a0a[1]);
-                tl[2] = b.tau[1] * (aig[2] + a0a[2]);
-                tl[3] = b.tau[1] * (aig[3] + a0a[3]);
-                tl[4] = b.tau[2] * (aig[4] + a0a[4]);
+                tl[1] = b.tau[1] * (aig[1] + a0a[1] - divq[0]);
+                tl[2] = b.tau[1] * (aig[2] + a0a[2] - divq[1]);
+                tl[3] = b.tau[1] * (aig[3] + a0a[3] - divq[2]);
+                tl[4] = b.tau[2] * (aig[4] + a0a[4] - divq[3]);
                 float F[3][5];
                 // Euler-flux increment F(y_q) - F(y_r) (flux sign of e3conv.f:72-96)
                 const float drho = (dq[0] * Tr - pr * dq[4]) * Pf.rRgas / (Tr * b.T);
@@ -966,7 +1114,8 @@ constexpr int kQpVals = 25;  // u(3) p rho ek drdp drdT e1p e2p e3p e4p tau(3) A
 
 template <typename R>
 __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R (&xl)[4][3], const R (&yl)[4][5],
-                                               const R (&al)[4][5], R* __restrict__ out35) {
+                                               const R (&al)[4][5], R* __restrict__ out35,
+                                               const R* divq = nullptr) {
     Geo<R> geo;
     geometry(xl, geo);
     R g[3][5];
@@ -1034,7 +1183,8 @@ __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R 
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             rm16[k] = v[15 + k] + P.fct1 * du[k];
-            lt[k] = tk[k] * (v[15 + k] + v[20 + k]);
+            const R dq = (divq && k > 0) ? divq[k - 1] : R(0);  // idiff = 1 (e3ls.f:147-156)
+            lt[k] = tk[k] * (v[15 + k] + v[20 + k] - dq);
             lm[k] = tk[k] * rm16[k];
         }
         const R Us = s[0] * u0 + s[1] * u1 + s[2] * u2;
@@ -1139,17 +1289,20 @@ __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R 
 template <typename R>
 __global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? PHGPU_FULL32_MINB : 2)
 k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restrict__ y, const R* __restrict__ ac,
-             R* __restrict__ res, R* __restrict__ rmes, R* __restrict__ bd, Phys<R> P) {
+             R* __restrict__ res, R* __restrict__ rmes, R* __restrict__ bd, Phys<R> P,
+             const R* __restrict__ ql = nullptr) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* sm = reinterpret_cast<R*>(smem_raw);
     const int c = chunk0 + blockIdx.x;
     const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
     const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+    const bool with_q = ql != nullptr && res != nullptr;
     R* sx = sm;
     R* sy = sx + 3 * nn;
     R* sa = sy + 5 * nn;
+    R* sq = sa + 5 * nn;                          // idiff = 1: 12 per node
     constexpr bool single = kFullSub * full_nsub<R>() >= kChunk;
-    R* acc = sa + 5 * nn;                         // nn x 35 (multi-round only)
+    R* acc = sq + (with_q ? 12 * nn : 0);         // nn x 35 (multi-round only)
     R* slot = acc + (single ? 0 : kFullOut * nn); // (kChunk * nsub) x 35
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
         const int gn = ca.nodes[n0 + l];
@@ -1160,6 +1313,8 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
             sy[5 * l + k] = ldg(y + 5 * (size_t)gn + k);
             sa[5 * l + k] = ldg(ac + 5 * (size_t)gn + k);
         }
+        if (with_q)
+            for (int k = 0; k < 12; ++k) sq[12 * l + k] = ldg(ql + 13 * (size_t)gn + k);
     }
     if (!single)
         for (int i = threadIdx.x; i < kFullOut * nn; i += blockDim.x) acc[i] = R(0);
@@ -1184,7 +1339,13 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
                 lds5(sa, nd[n], al[n]);
             }
             R o35[kFullOut];
-            elem_full_node<R>(P, a, xl, yl, al, o35);
+            if (with_q) {
+                R divq[4];
+                tet_divq(xl, sq, nd, divq);
+                elem_full_node<R>(P, a, xl, yl, al, o35, divq);
+            } else {
+                elem_full_node<R>(P, a, xl, yl, al, o35);
+            }
             if (valid) {
                 R* sl = slot + kFullOut * (sb * kChunk + threadIdx.x);
 #pragma unroll
@@ -1387,7 +1548,8 @@ template <> __device__ __forceinline__ double tqwt<double>(int t, int q) { retur
 template <> __device__ __forceinline__ float tqwt<float>(int t, int q) { return c_topof[t].qwt[q]; }
 
 constexpr int kTopoThreads = 128;
-enum TopoMode : int { TM_RES = RM_RES, TM_MODRES = RM_MODRES, TM_LIN = RM_LIN, TM_FULL = 4 };
+enum TopoMode : int { TM_RES = RM_RES, TM_MODRES = RM_MODRES, TM_LIN = RM_LIN, TM_FULL = 4, TM_QREC = 5 };
+constexpr int kTopoNode = 25;  // staged per node: x(3) ya(5) yb(5) reconstructed flux(12)
 
 // shared values of one quadrature point
 template <int NEN>
@@ -1400,14 +1562,15 @@ struct TopoQp {
     static constexpr int kVt = kA0 + 5;             // viscous stress t[i][j] (9)
     static constexpr int kVq = kVt + 9;             // heat flux (3)
     static constexpr int kDu = kVq + 3;             // conservative variables (full mode) (5)
-    static constexpr int kN = kDu + 5;
+    static constexpr int kDq = kDu + 5;             // div of the reconstructed flux (4)
+    static constexpr int kN = kDq + 4;
 };
 
 template <typename R, int NEN, int TOPO, int MODE>
 __global__ void __launch_bounds__(kTopoThreads)
 k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __restrict__ ya,
        const R* __restrict__ yb, const R* __restrict__ ac, R* __restrict__ res, R* __restrict__ rmes,
-       R* __restrict__ bd, Phys<R> P, int iabres, const int* __restrict__ skip) {
+       R* __restrict__ bd, Phys<R> P, int iabres, const int* __restrict__ skip, const R* __restrict__ ql) {
     if (skip && *skip) return;
     using Q = TopoQp<NEN>;
     constexpr int EPB = kTopoThreads / NEN;  // elements per CTA
@@ -1416,20 +1579,23 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
     const int le = threadIdx.x / NEN, a = threadIdx.x % NEN;
     const int e = blockIdx.x * EPB + le;
     const bool active = le < EPB && e < ne;
-    R* sx = sm + (size_t)le * NEN * 13;   // x(3) ya(5) yb(5) per node
-    R* sq = sm + (size_t)EPB * NEN * 13 + (size_t)le * NEN * Q::kN;
+    R* sx = sm + (size_t)le * NEN * kTopoNode;
+    R* sq = sm + (size_t)EPB * NEN * kTopoNode + (size_t)le * NEN * Q::kN;
+    const bool with_q = (MODE == TM_RES || MODE == TM_FULL) && ql != nullptr;
     int node = 0;
     if (active) {
         node = ien[(size_t)e * NEN + a];
-        R* s = sx + 13 * a;
+        R* s = sx + kTopoNode * a;
 #pragma unroll
         for (int d = 0; d < 3; ++d) s[d] = ldg(x + 3 * (size_t)node + d);
         const R* bsrc = (MODE == TM_RES || MODE == TM_FULL) ? ac : yb;
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             s[3 + k] = ldg(ya + 5 * (size_t)node + k);
-            s[8 + k] = ldg(bsrc + 5 * (size_t)node + k);
+            if (MODE != TM_QREC) s[8 + k] = ldg(bsrc + 5 * (size_t)node + k);
         }
+        if (with_q)
+            for (int k = 0; k < 12; ++k) s[13 + k] = ldg(ql + 13 * (size_t)node + k);
     }
     __syncthreads();
     if (active) {
@@ -1442,7 +1608,7 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
             for (int j = 0; j < 3; ++j) {
                 R acc = R(0);
 #pragma unroll
-                for (int b = 0; b < NEN; ++b) acc += sx[13 * b + i] * tshgl<R>(TOPO, q, j, b);
+                for (int b = 0; b < NEN; ++b) acc += sx[kTopoNode * b + i] * tshgl<R>(TOPO, q, j, b);
                 dxdxi[i][j] = acc;
             }
         R di[3][3];
@@ -1480,7 +1646,7 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
                 o[Q::kShg + 3 * b + i] = sh[i];
             }
             const R Nb = tshp<R>(TOPO, q, b);
-            const R* s = sx + 13 * b;
+            const R* s = sx + kTopoNode * b;
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
                 const R va = s[3 + k];
@@ -1488,9 +1654,23 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
                 for (int i = 0; i < 3; ++i) g[i][k] += sh[i] * va;
                 pv[k] += Nb * va;
                 if (MODE == TM_RES || MODE == TM_FULL) aq[k] += Nb * s[8 + k];
-                else bq[k] += Nb * s[8 + k];
+                else if (MODE != TM_QREC) bq[k] += Nb * s[8 + k];
             }
+            if (with_q)  // div q at this point (e3ivar.f:374-395)
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    o[Q::kDq + k] = (b == 0 ? R(0) : o[Q::kDq + k]) + sh[0] * s[13 + k] + sh[1] * s[17 + k] +
+                                    sh[2] * s[21 + k];
         }
+        if (MODE == TM_QREC) {
+            // viscous flux of e3q.f at this point (the point's velocity enters the energy row)
+            Visc<R> vq;
+            viscous(P, g, vq);
+            R qd[12];
+            visc_flux12(P, vq, pv[1], pv[2], pv[3], qd);
+#pragma unroll
+            for (int k = 0; k < 12; ++k) o[Q::kVt + k] = qd[k];
+        } else {
         if (MODE == TM_RES || MODE == TM_FULL) {
 #pragma unroll
             for (int k = 0; k < 5; ++k) bq[k] = pv[k];
@@ -1567,9 +1747,28 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
         const R du[5] = {st.rho, st.rho * st.u[0], st.rho * st.u[1], st.rho * st.u[2], st.rho * (st.ei + st.rk)};
 #pragma unroll
         for (int k = 0; k < 5; ++k) o[Q::kDu + k] = du[k];
+        }
     }
     __syncthreads();
     if (!active) return;
+    if (MODE == TM_QREC) {
+        // node a: sum_q N_a WdetJ qdi and the lumped mass (e3q.f:160-177)
+        R qa[13];
+#pragma unroll
+        for (int k = 0; k < 13; ++k) qa[k] = R(0);
+#pragma unroll 1
+        for (int q = 0; q < NEN; ++q) {
+            const R* v = sq + Q::kN * q;
+            const R w = tshp<R>(TOPO, q, a) * v[Q::kW];
+#pragma unroll
+            for (int k = 0; k < 12; ++k) qa[k] += w * v[Q::kVt + k];
+            qa[12] += w;
+        }
+        R* og = res + 13 * (size_t)node;
+#pragma unroll
+        for (int k = 0; k < 13; ++k) og[k] += qa[k];
+        return;
+    }
     // ---- node a: weighted terms summed over the points ----
     R rl[5], rml[5], B_[5][5];
 #pragma unroll
@@ -1613,7 +1812,10 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
         if (MODE == TM_RES || MODE == TM_FULL) {
             R lt[5];
 #pragma unroll
-            for (int k = 0; k < 5; ++k) lt[k] = tk[k] * (v[Q::kAig + k] + v[Q::kA0 + k]);
+            for (int k = 0; k < 5; ++k) {
+                const R dq = (with_q && k > 0) ? v[Q::kDq + k - 1] : R(0);  // e3ls.f:147-156
+                lt[k] = tk[k] * (v[Q::kAig + k] + v[Q::kA0 + k] - dq);
+            }
             R fe[5];
             const R m = -rho * Us;
             fe[0] = m;
@@ -1769,7 +1971,7 @@ void upload_topo_tables(Ctx& C) {
 
 template <typename R, int NEN>
 constexpr size_t topo_smem() {
-    return sizeof(R) * (size_t)(kTopoThreads / NEN) * NEN * (13 + TopoQp<NEN>::kN);
+    return sizeof(R) * (size_t)(kTopoThreads / NEN) * NEN * (kTopoNode + TopoQp<NEN>::kN);
 }
 
 template <typename R, int NEN, int TOPO>
@@ -1781,13 +1983,14 @@ int configure_topo_kernels(Ctx& C) {
     T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_QREC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     return rc;
 }
 
 template <typename R, int NEN, int TOPO>
 static void launch_topo_one(Ctx& C, int mode, const int* d_ien, const std::vector<int>& col, const R* x,
                             const R* ya, const R* yb, const R* ac, R* res, R* rmes, R* bd, int iabres,
-                            const int* skip) {
+                            const int* skip, const R* ql) {
     const Phys<R> P = make_phys<R>(C.cfg);
     constexpr int EPB = kTopoThreads / NEN;
     const size_t sm = topo_smem<R, NEN>();
@@ -1799,16 +2002,19 @@ static void launch_topo_one(Ctx& C, int mode, const int* d_ien, const std::vecto
         const int* ie = d_ien + (size_t)NEN * e0;
         switch (mode) {
             case TM_RES:
-                k_topo<R, NEN, TOPO, TM_RES><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip);
+                k_topo<R, NEN, TOPO, TM_RES><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
                 break;
             case TM_MODRES:
-                k_topo<R, NEN, TOPO, TM_MODRES><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip);
+                k_topo<R, NEN, TOPO, TM_MODRES><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
                 break;
             case TM_LIN:
-                k_topo<R, NEN, TOPO, TM_LIN><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip);
+                k_topo<R, NEN, TOPO, TM_LIN><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
+                break;
+            case TM_QREC:
+                k_topo<R, NEN, TOPO, TM_QREC><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
                 break;
             default:
-                k_topo<R, NEN, TOPO, TM_FULL><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip);
+                k_topo<R, NEN, TOPO, TM_FULL><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
                 break;
         }
         ++C.launches;
@@ -1817,16 +2023,16 @@ static void launch_topo_one(Ctx& C, int mode, const int* d_ien, const std::vecto
 
 template <typename R>
 void launch_topo(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R* ac, R* res, R* rmes, R* bd,
-                 int iabres, const int* skip) {
+                 int iabres, const int* skip, const R* ql) {
     if (C.nhex > 0)
-        launch_topo_one<R, 8, 0>(C, mode, C.d_ienh, C.hcol_start, x, ya, yb, ac, res, rmes, bd, iabres, skip);
+        launch_topo_one<R, 8, 0>(C, mode, C.d_ienh, C.hcol_start, x, ya, yb, ac, res, rmes, bd, iabres, skip, ql);
     if (C.nwedge > 0)
-        launch_topo_one<R, 6, 1>(C, mode, C.d_ienw, C.wcol_start, x, ya, yb, ac, res, rmes, bd, iabres, skip);
+        launch_topo_one<R, 6, 1>(C, mode, C.d_ienw, C.wcol_start, x, ya, yb, ac, res, rmes, bd, iabres, skip, ql);
 }
 template void launch_topo<double>(Ctx&, int, const double*, const double*, const double*, const double*, double*,
-                                  double*, double*, int, const int*);
+                                  double*, double*, int, const int*, const double*);
 template void launch_topo<float>(Ctx&, int, const float*, const float*, const float*, const float*, float*, float*,
-                                 float*, int, const int*);
+                                 float*, int, const int*, const float*);
 
 static ChunkArgs chunk_args(const Ctx& C) {
     return ChunkArgs{C.d_ch_elem, C.d_ch_node, C.d_ch_nodes, C.d_ch_cstart, C.d_ch_csr, C.d_ch_lien};
@@ -1834,6 +2040,11 @@ static ChunkArgs chunk_args(const Ctx& C) {
 
 template <typename R>
 size_t res_smem(const Ctx& C) { return sizeof(R) * ((size_t)C.chunk_lmax * 13 + (size_t)kChunk * 20); }
+// extra shared memory of the reconstructed flux (idiff = 1): 12 per chunk node
+template <typename R>
+size_t q_smem(const Ctx& C) { return sizeof(R) * (size_t)C.chunk_lmax * 12; }
+template <typename R>
+size_t qrec_smem(const Ctx& C) { return sizeof(R) * ((size_t)C.chunk_lmax * 8 + (size_t)kChunk * 52); }
 template <typename R>
 size_t full_smem(const Ctx& C) {
     const bool single = kFullSub * full_nsub<R>() >= kChunk;
@@ -1855,14 +2066,16 @@ int configure_chunk_kernels(Ctx& C) {
     const int rs = (int)res_smem<R>(C), fs = (int)full_smem<R>(C);
     int rc = PHGPU_OK;
     auto T = [&](cudaError_t e) { if (rc == PHGPU_OK) rc = check(C, e, "cudaFuncSetAttribute"); };
-    T(cudaFuncSetAttribute(k_chunk_res<R, RM_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
+    T(cudaFuncSetAttribute(k_chunk_res<R, RM_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           rs + (int)q_smem<R>(C)));
+    T(cudaFuncSetAttribute(k_chunk_qrec<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qrec_smem<R>(C)));
     T(cudaFuncSetAttribute(k_chunk_res<R, RM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
     T(cudaFuncSetAttribute(k_chunk_res<R, RM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
-    T(cudaFuncSetAttribute(k_chunk_full<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, fs));
+    T(cudaFuncSetAttribute(k_chunk_full<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, fs + (int)q_smem<R>(C)));
     return rc;
 }
 int configure_element_kernels(Ctx& C) {
-    if (full_smem<double>(C) > 227 * 1024) {
+    if (full_smem<double>(C) + q_smem<double>(C) > 227 * 1024) {
         C.err = "a mesh chunk has too many distinct nodes for shared memory";
         return PHGPU_ERR_UNSUPPORTED;
     }
@@ -1872,7 +2085,8 @@ int configure_element_kernels(Ctx& C) {
         rc = check(C, cudaFuncSetAttribute(k_chunk_resh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)resh_smem(C)),
                    "cudaFuncSetAttribute");
     if (rc == PHGPU_OK)
-        rc = check(C, cudaFuncSetAttribute(k_chunk_ress, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ress_smem(C)),
+        rc = check(C, cudaFuncSetAttribute(k_chunk_ress, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(ress_smem(C) + q_smem<float>(C))),
                    "cudaFuncSetAttribute");
     if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 8, 0>(C);
     if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 6, 1>(C);
@@ -1883,16 +2097,16 @@ int configure_element_kernels(Ctx& C) {
 
 template <typename R>
 void launch_elem_res(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R* ac, R* out,
-                     int iabres, const int* skip) {
+                     int iabres, const int* skip, const R* ql) {
     const Phys<R> P = make_phys<R>(C.cfg);
     const ChunkArgs ca = chunk_args(C);
-    const size_t sm = res_smem<R>(C);
+    const size_t sm = res_smem<R>(C) + ((mode == RM_RES && ql) ? q_smem<R>(C) : 0);
     const int ncol = (int)C.chunk_col_start.size() - 1;
     for (int c = 0; c < ncol; ++c) {
         const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
         if (nc <= 0) continue;
         if (mode == RM_RES)
-            k_chunk_res<R, RM_RES><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
+            k_chunk_res<R, RM_RES><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip, ql);
         else if (mode == RM_MODRES)
             k_chunk_res<R, RM_MODRES><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
         else
@@ -1900,13 +2114,31 @@ void launch_elem_res(Ctx& C, int mode, const R* x, const R* ya, const R* yb, con
         ++C.launches;
     }
     // hex and wedge blocks: ires = 1 writes res, ires = 2 (and the linearized form) rmes
-    if (mode == RM_RES) launch_topo<R>(C, TM_RES, x, ya, yb, ac, out, nullptr, nullptr, iabres, skip);
-    else launch_topo<R>(C, mode, x, ya, yb, ac, nullptr, out, nullptr, iabres, skip);
+    if (mode == RM_RES) launch_topo<R>(C, TM_RES, x, ya, yb, ac, out, nullptr, nullptr, iabres, skip, ql);
+    else launch_topo<R>(C, mode, x, ya, yb, ac, nullptr, out, nullptr, iabres, skip, nullptr);
 }
 template void launch_elem_res<double>(Ctx&, int, const double*, const double*, const double*, const double*,
-                                      double*, int, const int*);
+                                      double*, int, const int*, const double*);
 template void launch_elem_res<float>(Ctx&, int, const float*, const float*, const float*, const float*, float*,
-                                     int, const int*);
+                                     int, const int*, const float*);
+
+// lumped L2 reconstruction of the diffusive flux into out (13 per node, zeroed by the caller)
+template <typename R>
+void launch_qrec(Ctx& C, const R* x, const R* y, R* out) {
+    const Phys<R> P = make_phys<R>(C.cfg);
+    const ChunkArgs ca = chunk_args(C);
+    const size_t sm = qrec_smem<R>(C);
+    const int ncol = (int)C.chunk_col_start.size() - 1;
+    for (int c = 0; c < ncol; ++c) {
+        const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
+        if (nc <= 0) continue;
+        k_chunk_qrec<R><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, out, P);
+        ++C.launches;
+    }
+    launch_topo<R>(C, TM_QREC, x, y, nullptr, nullptr, out, nullptr, nullptr, 0, nullptr, nullptr);
+}
+template void launch_qrec<double>(Ctx&, const double*, const double*, double*);
+template void launch_qrec<float>(Ctx&, const float*, const float*, float*);
 
 void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf, const float* acf, double* out) {
     const Phys<double> P = make_phys<double>(C.cfg);
@@ -1922,40 +2154,41 @@ void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf
     }
 }
 
-void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* acf, double* out) {
+void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* acf, double* out, const float* ql) {
     const Phys<float> Pf = make_phys<float>(C.cfg);
     DfConst K;
     split(1.0 / C.cfg.Rgas, K.rRgas_hi, K.rRgas_lo);
     split(C.cfg.Rgas / C.cfg.gamma1, K.cv_hi, K.cv_lo);
     split(0.5 * kTetQwt, K.wq_hi, K.wq_lo);
     const ChunkArgs ca = chunk_args(C);
-    const size_t sm = ress_smem(C);
+    const size_t sm = ress_smem(C) + (ql ? q_smem<float>(C) : 0);
     const int ncol = (int)C.chunk_col_start.size() - 1;
     for (int c = 0; c < ncol; ++c) {
         const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
         if (nc <= 0) continue;
-        k_chunk_ress<<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K);
+        k_chunk_ress<<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql);
         ++C.launches;
     }
 }
 
 template <typename R>
-void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rmes, R* bd) {
+void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rmes, R* bd, const R* ql) {
     const Phys<R> P = make_phys<R>(C.cfg);
     const ChunkArgs ca = chunk_args(C);
-    const size_t sm = full_smem<R>(C);
+    const size_t sm = full_smem<R>(C) + ((ql && res) ? q_smem<R>(C) : 0);
     const int ncol = (int)C.chunk_col_start.size() - 1;
     for (int c = 0; c < ncol; ++c) {
         const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
         if (nc <= 0) continue;
-        k_chunk_full<R><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, ac, res, rmes, bd, P);
+        k_chunk_full<R><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, ac, res, rmes, bd, P, (ql && res) ? ql : nullptr);
         ++C.launches;
     }
-    launch_topo<R>(C, TM_FULL, x, y, nullptr, ac, res, rmes, bd, 0, nullptr);
+    launch_topo<R>(C, TM_FULL, x, y, nullptr, ac, res, rmes, bd, 0, nullptr, (ql && res) ? ql : nullptr);
 }
 template void launch_elem_full<double>(Ctx&, const double*, const double*, const double*, double*, double*,
-                                       double*);
-template void launch_elem_full<float>(Ctx&, const float*, const float*, const float*, float*, float*, float*);
+                                       double*, const double*);
+template void launch_elem_full<float>(Ctx&, const float*, const float*, const float*, float*, float*, float*,
+                                      const float*);
 
 void launch_boundary(Ctx& C, const double* y, double* res) {
     const Phys<double> P = make_phys<double>(C.cfg);

@@ -555,6 +555,30 @@ __global__ void k_split(const double* __restrict__ a, float* __restrict__ hi, fl
         lo[i] = (float)(v - (double)h);
     }
 }
+// qpbc.f: 1/rmass scaling of the 12 flux values of each node (the 13th value is the mass)
+template <typename R>
+__global__ void k_qscale(R* __restrict__ q, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    R* v = q + 13 * (size_t)i;
+    const R r = R(1) / v[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) v[k] = r * v[k];
+}
+template <typename R>
+void qpbc(Ctx& C, R* q13) {
+    // periodic slaves summed into their master, the master's values copied back (qpbc.f)
+    if (C.nmaster > 0) {
+        k_periodic_sum<R, 13><<<nblocks(C.nmaster), kT, 0, C.stream>>>(C.d_mst, C.d_slv_start, C.d_slv, C.nmaster,
+                                                                       q13, 1);
+        ++C.launches;
+    }
+    k_qscale<R><<<nblocks(C.N), kT, 0, C.stream>>>(q13, C.N);
+    ++C.launches;
+}
+template void qpbc<double>(Ctx&, double*);
+template void qpbc<float>(Ctx&, float*);
+
 void split_f32(Ctx& C, const double* a, float* hi, float* lo, size_t n) {
     k_split<<<kRedBlocks, kT, 0, C.stream>>>(a, hi, lo, n);
     ++C.launches;

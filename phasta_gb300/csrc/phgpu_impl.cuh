@@ -93,6 +93,8 @@ struct Ctx {
     double *d_y = nullptr, *d_ac = nullptr, *d_yold = nullptr, *d_acold = nullptr;
     float *d_yf = nullptr, *d_acf = nullptr;
     float* d_ylo = nullptr;       // y - (double)d_yf, rounded to float (double-float residual)
+    double* d_qres = nullptr;     // idiff = 1: reconstructed diffusive flux, 13 per node (12 + lumped mass)
+    float* d_qresf = nullptr;     //   its FP32 copy for the mixed outer residual
 
     // work arrays
     double *d_res = nullptr, *d_rmes = nullptr, *d_bd = nullptr, *d_Dy = nullptr, *d_bdstage = nullptr;
@@ -133,17 +135,23 @@ template <typename R> Phys<R> make_phys(const phgpu_config& c);
 enum ResMode : int { RM_RES = 1, RM_MODRES = 2, RM_LIN = 3 };
 template <typename R>
 void launch_elem_res(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R* ac,
-                     R* out, int iabres, const int* skip);
+                     R* out, int iabres, const int* skip, const R* ql = nullptr);
 template <typename R>
-void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rmes, R* bd);
+void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rmes, R* bd, const R* ql = nullptr);
+// idiff = 1: lumped L2 reconstruction of the diffusive flux (13 per node: 12 flux, 1 mass), then qpbc
+template <typename R>
+void launch_qrec(Ctx& C, const R* x, const R* y, R* out);
+template <typename R>
+void qpbc(Ctx& C, R* q13);
 void launch_boundary(Ctx& C, const double* y, double* res);
 void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf, const float* acf, double* out);
 // outer residual with no FP64 arithmetic: double-float element-constant flux + FP32 increments
-void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* acf, double* out);
+void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* acf, double* out,
+                      const float* ql = nullptr);
 // hex and wedge blocks; mode RM_RES/RM_MODRES/RM_LIN or 4 (ires = 3 + block diagonal)
 template <typename R>
 void launch_topo(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R* ac, R* res, R* rmes, R* bd,
-                 int iabres, const int* skip);
+                 int iabres, const int* skip, const R* ql = nullptr);
 void upload_tables(Ctx& C);
 int build_chunks(Ctx& C, const int* ien, const double* x_ref);
 int configure_element_kernels(Ctx& C);

@@ -235,9 +235,19 @@ constexpr int kVG = kRedBlocks, kVT = 256;
 // ------------------------------------------------------------------------
 // ElmMFG / residual drivers on resident device data
 // ------------------------------------------------------------------------
+// idiff = 1: the reconstructed diffusive flux of state y in d_qres (elmmfg.f:56-111)
+const double* reconstruct_q(Ctx& C, const double* y) {
+    if (C.cfg.idiff != 1) return nullptr;
+    fill0(C, C.d_qres, sizeof(double) * 13 * (size_t)C.N);
+    launch_qrec<double>(C, C.d_x, y, C.d_qres);
+    qpbc<double>(C, C.d_qres);
+    return C.d_qres;
+}
+
 int elmres64(Ctx& C, const double* y, const double* ac, double* res) {
+    const double* ql = reconstruct_q(C, y);
     fill0(C, res, sizeof(double) * 5 * (size_t)C.N);
-    launch_elem_res<double>(C, RM_RES, C.d_x, y, nullptr, ac, res, 0, nullptr);
+    launch_elem_res<double>(C, RM_RES, C.d_x, y, nullptr, ac, res, 0, nullptr, ql);
     if (C.Eb > 0) launch_boundary(C, y, res);
     bc3res<double>(C, res);
     return check(C, cudaGetLastError(), "elmres");
@@ -245,13 +255,14 @@ int elmres64(Ctx& C, const double* y, const double* ac, double* res) {
 
 int elmmfg64(Ctx& C, const double* y, const double* ac, double* res, double* rmes, double* bd, int iprec) {
     const size_t N = C.N;
+    const double* ql = reconstruct_q(C, y);
     fill0(C, res, sizeof(double) * 5 * N);
     fill0(C, rmes, sizeof(double) * 5 * N);
     if (iprec) {
         fill0(C, bd, sizeof(double) * 25 * N);
-        launch_elem_full<double>(C, C.d_x, y, ac, res, rmes, bd);
+        launch_elem_full<double>(C, C.d_x, y, ac, res, rmes, bd, ql);
     } else {
-        launch_elem_res<double>(C, RM_RES, C.d_x, y, nullptr, ac, res, 0, nullptr);
+        launch_elem_res<double>(C, RM_RES, C.d_x, y, nullptr, ac, res, 0, nullptr, ql);
         launch_elem_res<double>(C, RM_MODRES, C.d_x, y, y, ac, rmes, 0, nullptr);
     }
     if (C.Eb > 0) launch_boundary(C, y, res);
@@ -507,11 +518,16 @@ int solmfg_dev(Ctx& C, phgpu_stats* st) {
         else to_f32(C, C.d_y, C.d_yf, n5);
         to_f32(C, C.d_ac, C.d_acf, n5);
         if (C.cfg.outer_residual == PHGPU_RES_GALERKIN64 || C.cfg.outer_residual == PHGPU_RES_SPLITDF) {
+            if (C.cfg.idiff == 1 && C.cfg.outer_residual == PHGPU_RES_GALERKIN64)
+                return fail(C, PHGPU_ERR_UNSUPPORTED, "idiff = 1 needs the FP64 or the double-float outer residual");
+            const double* ql = reconstruct_q(C, C.d_y);
+            if (ql) to_f32(C, C.d_qres, C.d_qresf, 13 * N);
             fill0(C, C.d_res, sizeof(double) * n5);
-            if (C.cfg.outer_residual == PHGPU_RES_SPLITDF) launch_elem_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res);
+            if (C.cfg.outer_residual == PHGPU_RES_SPLITDF)
+                launch_elem_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res, ql ? C.d_qresf : nullptr);
             else launch_elem_resh(C, C.d_y, C.d_ac, C.d_yf, C.d_acf, C.d_res);
             // hex and wedge blocks: FP64 outer residual
-            launch_topo<double>(C, RM_RES, C.d_x, C.d_y, nullptr, C.d_ac, C.d_res, nullptr, nullptr, 0, nullptr);
+            launch_topo<double>(C, RM_RES, C.d_x, C.d_y, nullptr, C.d_ac, C.d_res, nullptr, nullptr, 0, nullptr, ql);
             if (C.Eb > 0) launch_boundary(C, C.d_y, C.d_res);
             bc3res<double>(C, C.d_res);
         } else {
@@ -614,6 +630,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     if (m->nbelem < 0 || (m->nbelem > 0 && !m->ienb)) return PHGPU_ERR_INVALID;
     if (cfg->Kspace < 1 || cfg->Kspace > kMaxK || cfg->nGMRES < 1) return PHGPU_ERR_INVALID;
     if (cfg->itau != 0 || cfg->ipord != 1 || cfg->EntropyPressure != 0) return PHGPU_ERR_UNSUPPORTED;
+    if (cfg->idiff != 0 && cfg->idiff != 1) return PHGPU_ERR_UNSUPPORTED;
     phgpu_ctx* h = new (std::nothrow) phgpu_ctx();
     if (!h) return PHGPU_ERR_NOMEM;
     Ctx& C = h->c;
@@ -725,6 +742,8 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     T(dalloc(C, &C.d_bdstage, 25 * (size_t)N));
     for (float** p : {&C.d_yf, &C.d_ylo, &C.d_acf, &C.d_resf, &C.d_rmesf, &C.d_t32, &C.d_t32b}) T(dalloc(C, p, n5));
     T(dalloc(C, &C.d_bdf, 25 * (size_t)N));
+    T(dalloc(C, &C.d_qres, 13 * (size_t)N));
+    T(dalloc(C, &C.d_qresf, 13 * (size_t)N));
     {
         const size_t vb = (cfg->precision == PHGPU_FP64) ? sizeof(double) : sizeof(float);
         char* p = nullptr;
@@ -794,7 +813,7 @@ int phgpu_destroy(phgpu_ctx* h) {
                     C.d_bdstage, C.d_ien, C.d_ienh, C.d_ienw, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_xlo, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
                     C.d_slaves, C.d_mst, C.d_slv_start, C.d_slv, C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_res,
                     C.d_rmes, C.d_Dy, C.d_ypre, C.d_t64, C.d_t64b, C.d_bd, C.d_yf, C.d_ylo, C.d_acf, C.d_resf, C.d_rmesf,
-                    C.d_t32, C.d_t32b, C.d_bdf, C.d_U, C.d_scal, C.d_part, C.d_count, C.d_flag};
+                    C.d_t32, C.d_t32b, C.d_bdf, C.d_qres, C.d_qresf, C.d_U, C.d_scal, C.d_part, C.d_count, C.d_flag};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (C.h_scal) cudaFreeHost(C.h_scal);
@@ -810,6 +829,7 @@ int phgpu_set_config(phgpu_ctx* h, const phgpu_config* cfg) {
     if (!h || !cfg) return PHGPU_ERR_INVALID;
     if (cfg->Kspace < 1 || cfg->Kspace > h->c.Ucap || cfg->nGMRES < 1) return PHGPU_ERR_INVALID;
     if (cfg->itau != 0 || cfg->ipord != 1 || cfg->EntropyPressure != 0) return PHGPU_ERR_UNSUPPORTED;
+    if (cfg->idiff != 0 && cfg->idiff != 1) return PHGPU_ERR_UNSUPPORTED;
     const bool was64 = h->c.cfg.precision == PHGPU_FP64;
     const bool is64 = cfg->precision == PHGPU_FP64;
     if (was64 != is64 && !was64) return PHGPU_ERR_UNSUPPORTED;  // basis was allocated as FP32
