@@ -860,6 +860,7 @@ __device__ __forceinline__ df64 df_diff(float ah, float al, float bh, float bl) 
     return quick_two_sum(s, e);
 }
 
+template <bool WITH_Q>
 __global__ void __launch_bounds__(kChunk, PHGPU_RESS_MINB)
 k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float* __restrict__ xlo,
              const float* __restrict__ yh, const float* __restrict__ ylo, const float* __restrict__ acf,
@@ -875,7 +876,7 @@ k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float
     float* syl = syh + 5 * nn;
     float* sa = syl + 5 * nn;
     float* sq = sa + 5 * nn;              // idiff = 1: reconstructed flux, 12 per node
-    float* slot = sq + (ql ? 12 * nn : 0);
+    float* slot = sq + (WITH_Q ? 12 * nn : 0);
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
         const size_t gn = ca.nodes[n0 + l];
 #pragma unroll
@@ -889,7 +890,7 @@ k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float
             syl[5 * l + k] = __ldg(ylo + 5 * gn + k);
             sa[5 * l + k] = __ldg(acf + 5 * gn + k);
         }
-        if (ql)
+        if (WITH_Q)
             for (int k = 0; k < 12; ++k) sq[12 * l + k] = __ldg(ql + 13 * gn + k);
     }
     __syncthreads();
@@ -925,7 +926,7 @@ k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float
             Visc<float> vs;
             if (Pf.navier) viscous(Pf, g, vs);
             float divq[4] = {0.f, 0.f, 0.f, 0.f};  // idiff = 1 (e3ivar.f:374-395)
-            if (ql) {
+            if (WITH_Q) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     float acc = 0.f;
@@ -2085,7 +2086,11 @@ int configure_element_kernels(Ctx& C) {
         rc = check(C, cudaFuncSetAttribute(k_chunk_resh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)resh_smem(C)),
                    "cudaFuncSetAttribute");
     if (rc == PHGPU_OK)
-        rc = check(C, cudaFuncSetAttribute(k_chunk_ress, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        rc = check(C, cudaFuncSetAttribute(k_chunk_ress<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)ress_smem(C)),
+                   "cudaFuncSetAttribute");
+    if (rc == PHGPU_OK)
+        rc = check(C, cudaFuncSetAttribute(k_chunk_ress<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)(ress_smem(C) + q_smem<float>(C))),
                    "cudaFuncSetAttribute");
     if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 8, 0>(C);
@@ -2166,7 +2171,8 @@ void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* ac
     for (int c = 0; c < ncol; ++c) {
         const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
         if (nc <= 0) continue;
-        k_chunk_ress<<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql);
+        if (ql) k_chunk_ress<true><<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql);
+        else k_chunk_ress<false><<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql);
         ++C.launches;
     }
 }
