@@ -175,7 +175,8 @@ const Topo& topo(int lcsyst) {
 // ---------------------------------------------------------------------------
 void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const double (*yl)[5],
                 const double (*ycl)[5], const double (*acl)[5], const double (*xl)[3],
-                double (*rl)[5], double (*rml)[5], double (*bdl)[5][5], const double (*ql)[12] = nullptr) {
+                double (*rl)[5], double (*rml)[5], double (*bdl)[5][5], const double (*ql)[12] = nullptr,
+                double* EG = nullptr) {
     const int nshl = tp.nshl, nenl = tp.nshl, ngauss = tp.ngauss;
     const double Rgas = c.Rgas, gamma = c.gamma, gamma1 = c.gamma1;
 
@@ -450,8 +451,105 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
         if (ires != 1)
             for (int k = 0; k < 5; ++k) rmi[15 + k] = rmi[15 + k] + fct1 * dui[k];
 
+        // ---------------- lhs = 1: element tangent EG[nedof][nedof], nedof = 5 nshl ----------------
+        if (EG) {
+            const int nedof = 5 * nshl;
+            auto E = [&](int r, int cc) -> double& { return EG[(size_t)r * nedof + cc]; };
+            // e3conv.f:186-260: N_a (A_i N_b,i)
+            for (int j = 0; j < nshl; ++j) {
+                const double f1 = WdetJ * shg[j][0], f2 = WdetJ * shg[j][1], f3 = WdetJ * shg[j][2];
+                double AiNbi[5][5];
+                for (int r = 0; r < 5; ++r)
+                    for (int cc = 0; cc < 5; ++cc) AiNbi[r][cc] = f1 * A1[r][cc] + f2 * A2[r][cc] + f3 * A3[r][cc];
+                for (int i = 0; i < nshl; ++i)
+                    for (int cc = 0; cc < 5; ++cc)
+                        for (int r = 0; r < 5; ++r) E(5 * i + r, 5 * j + cc) = E(5 * i + r, 5 * j + cc) + shape[i] * AiNbi[r][cc];
+            }
+            // stiff(15,15): e3visc.f:65-127 (diffusivity K_ij), then e3ls.f:464-702 (A_i tau A_j)
+            double stiff[15][15] = {{0}};
+            if (c.Navier == 1) {
+                const double uu[3] = {u1, u2, u3};
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) {
+                        double (*K)[15] = stiff;
+                        const int ri = 5 * i, cj = 5 * j;
+                        for (int m = 0; m < 3; ++m)
+                            for (int n = 0; n < 3; ++n) {
+                                double v = 0.0;
+                                if (i == j && m == n) v = (m == i) ? rlm2mu : rmu;
+                                else if (i != j && m == i && n == j) v = rlm;
+                                else if (i != j && m == j && n == i) v = rmu;
+                                if (v != 0.0) K[ri + 1 + m][cj + 1 + n] = v;
+                            }
+                        // energy row: u_m times the momentum rows
+                        for (int n = 0; n < 3; ++n) {
+                            double v = 0.0;
+                            if (i == j) v = ((n == i) ? rlm2mu : rmu) * uu[n];
+                            else if (n == j) v = rlm * uu[i];
+                            else if (n == i) v = rmu * uu[j];
+                            if (i == j || n == j || n == i) K[ri + 4][cj + 1 + n] = v;
+                        }
+                        if (i == j) K[ri + 4][cj + 4] = con;
+                    }
+            }
+            double AtA0[3][5][5];
+            for (int i = 0; i < 3; ++i) {
+                double Atau[5][5];
+                for (int r = 0; r < 5; ++r)
+                    for (int k = 0; k < 5; ++k) Atau[r][k] = A[i][r][k] * tauk[k];
+                for (int cc = 0; cc < 5; ++cc)
+                    for (int r = 0; r < 5; ++r)
+                        AtA0[i][r][cc] = Atau[r][0] * A0[0][cc] + Atau[r][1] * A0[1][cc] + Atau[r][2] * A0[2][cc] +
+                                         Atau[r][3] * A0[3][cc] + Atau[r][4] * A0[4][cc];
+                for (int j = 0; j < 3; ++j)
+                    for (int cc = 0; cc < 5; ++cc)
+                        for (int r = 0; r < 5; ++r)
+                            stiff[5 * i + r][5 * j + cc] =
+                                stiff[5 * i + r][5 * j + cc] +
+                                (Atau[r][0] * A[j][0][cc] + Atau[r][1] * A[j][1][cc] + Atau[r][2] * A[j][2][cc] +
+                                 Atau[r][3] * A[j][3][cc] + Atau[r][4] * A[j][4][cc]);
+            }
+            // e3ls.f:703-766: least-squares time term N_a,i A_i tau A0 N_b
+            for (int i = 0; i < nshl; ++i) {
+                double At[5][5];
+                for (int r = 0; r < 5; ++r)
+                    for (int cc = 0; cc < 5; ++cc)
+                        At[r][cc] = shg[i][0] * AtA0[0][r][cc] + shg[i][1] * AtA0[1][r][cc] + shg[i][2] * AtA0[2][r][cc];
+                for (int j = 0; j < nshl; ++j) {
+                    const double fact = shape[j] * WdetJ * c.almi / c.gami / c.alfi * c.Dtgl;
+                    for (int r = 0; r < 5; ++r)
+                        for (int cc = 0; cc < 5; ++cc) E(5 * i + r, 5 * j + cc) = E(5 * i + r, 5 * j + cc) + fact * At[r][cc];
+                }
+            }
+            // e3massl.f:1-75 (bcool = 0): N_a N_b fct A0
+            {
+                const double temp = WdetJ * c.almi / c.gami / c.alfi * c.Dtgl;
+                for (int j = 0; j < nshl; ++j)
+                    for (int i = 0; i < nshl; ++i) {
+                        const double f = (shape[i] * shape[j]) * (temp + 0.0);
+                        for (int cc = 0; cc < 5; ++cc)
+                            for (int r = 0; r < 5; ++r) E(5 * i + r, 5 * j + cc) = E(5 * i + r, 5 * j + cc) + f * A0[r][cc];
+                    }
+            }
+            // e3wmlt.f (lhs part): N_a,i stiff_ij N_b,j
+            for (int j = 0; j < nshl; ++j) {
+                const double g1 = WdetJ * shg[j][0], g2 = WdetJ * shg[j][1], g3 = WdetJ * shg[j][2];
+                double st[3][5][5];
+                for (int cc = 0; cc < 5; ++cc)
+                    for (int r = 0; r < 5; ++r)
+                        for (int b = 0; b < 3; ++b)
+                            st[b][r][cc] = g1 * stiff[5 * b + r][cc] + g2 * stiff[5 * b + r][5 + cc] +
+                                           g3 * stiff[5 * b + r][10 + cc];
+                for (int i = 0; i < nshl; ++i)
+                    for (int cc = 0; cc < 5; ++cc)
+                        for (int r = 0; r < 5; ++r)
+                            E(5 * i + r, 5 * j + cc) = E(5 * i + r, 5 * j + cc) + shg[i][0] * st[0][r][cc] +
+                                                       shg[i][1] * st[1][r][cc] + shg[i][2] * st[2][r][cc];
+            }
+        }
+
         // ---------------- e3bdg.f (iprec == 1, lhs != 1, itau < 10) ----------------
-        if (iprec == 1 && bdl) {
+        if (iprec == 1 && bdl && !EG) {
             // convective, non-integrated-by-parts: N_b A_i N_b,i  (e3bdg.f:37-189)
             for (int j = 0; j < nshl; ++j) {
                 const double t = shape[j] * WdetJ;
@@ -909,6 +1007,142 @@ void boundary_sweep(const or_common& c, const or_mesh& m, const double* y, doubl
 
 inline int ibits3(int v) { return (v >> 3) & 7; }
 inline bool btest(int v, int b) { return (v >> b) & 1; }
+
+// bc3lhs.f:1-198 on one element tangent EG[nedof][nedof] (intpres = 0): per node with
+// a Dirichlet bit, its rows and columns are combined, zeroed and given a unit diagonal
+void bc3lhs_element(const or_mesh& m, const int* ie, int nshl, double* EG) {
+    const int N = m.nshg, nedof = 5 * nshl;
+    auto E = [&](int r, int cc) -> double& { return EG[(size_t)r * nedof + cc]; };
+    auto zero_rc = [&](int d) {
+        for (int i = 0; i < nedof; ++i) {
+            E(i, d) = zero;
+            E(d, i) = zero;
+        }
+    };
+    for (int inod = 0; inod < nshl; ++inod) {
+        const int in = ie[inod];
+        const int ib = m.iBC[in];
+        if (ib == 0) continue;
+        const int i1 = 5 * inod, i2 = i1 + 1, i3 = i1 + 2, i4 = i1 + 3, i5 = i1 + 4;
+        const double b4 = m.BC[3 * (size_t)N + in], b5 = m.BC[4 * (size_t)N + in], b6 = m.BC[5 * (size_t)N + in];
+        if (btest(ib, 2)) {
+            zero_rc(i1);
+            E(i1, i1) = one;
+        }
+        // velocity: (target row/col t1 [, t2]) -= coefficient * source, then the source is constrained
+        auto combine1 = [&](int src, int ta, double ca, int tb, double cb) {
+            for (int i = 0; i < nedof; ++i) {
+                E(ta, i) = E(ta, i) - ca * E(src, i);
+                E(tb, i) = E(tb, i) - cb * E(src, i);
+            }
+            for (int i = 0; i < nedof; ++i) {
+                E(i, ta) = E(i, ta) - ca * E(i, src);
+                E(i, tb) = E(i, tb) - cb * E(i, src);
+            }
+            zero_rc(src);
+            E(src, src) = one;
+        };
+        auto combine2 = [&](int s1, int s2, int t) {
+            for (int i = 0; i < nedof; ++i) E(t, i) = E(t, i) - b4 * E(s1, i) - b6 * E(s2, i);
+            for (int i = 0; i < nedof; ++i) E(i, t) = E(i, t) - b4 * E(i, s1) - b6 * E(i, s2);
+            for (int i = 0; i < nedof; ++i) {
+                E(i, s1) = zero;
+                E(s1, i) = zero;
+                E(i, s2) = zero;
+                E(s2, i) = zero;
+            }
+            E(s1, s1) = one;
+            E(s2, s2) = one;
+        };
+        switch (ibits3(ib)) {
+            case 1: combine1(i2, i3, b4, i4, b5); break;
+            case 2: combine1(i3, i2, b4, i4, b5); break;
+            case 3: combine2(i2, i3, i4); break;
+            case 4: combine1(i4, i2, b4, i3, b5); break;
+            case 5: combine2(i2, i4, i3); break;
+            case 6: combine2(i3, i4, i2); break;
+            case 7:
+                for (int i = 0; i < nedof; ++i) {
+                    E(i, i2) = zero; E(i2, i) = zero;
+                    E(i, i3) = zero; E(i3, i) = zero;
+                    E(i, i4) = zero; E(i4, i) = zero;
+                }
+                E(i2, i2) = one;
+                E(i3, i3) = one;
+                E(i4, i4) = one;
+                break;
+            default: break;
+        }
+        if (btest(ib, 1)) {
+            zero_rc(i5);
+            E(i5, i5) = one;
+        }
+        if (btest(ib, 11)) {  // intpres = 0: the continuity row stays
+            for (int i = 0; i < nedof; ++i) {
+                E(i, i2) = zero; E(i2, i) = zero;
+                E(i, i3) = zero; E(i3, i) = zero;
+                E(i, i4) = zero; E(i4, i) = zero;
+                E(i, i5) = zero; E(i5, i) = zero;
+            }
+            E(i2, i2) = one;
+            E(i3, i3) = one;
+            E(i4, i4) = one;
+            E(i5, i5) = one;
+        }
+    }
+}
+
+// fillsparse.f:1-52 (fillsparseC): EG blocks added to lhsK(25, nnz_tot) at the block of
+// (row ien(a), column ien(b)), found by sparseloc's search of the sorted row (1-based colm/rowp)
+void fillsparse_element(const int* ie, int nshl, const double* EG, const int* colm, const int* rowp, double* lhsK) {
+    const int nedof = 5 * nshl;
+    for (int aa = 0; aa < nshl; ++aa) {
+        const int i = ie[aa];
+        const int c0 = colm[i] - 1, n = colm[i + 1] - colm[i];
+        for (int b = 0; b < nshl; ++b) {
+            const int want = ie[b] + 1;
+            int lo = 0, hi = n - 1, k = -1;
+            while (lo <= hi) {
+                const int mid = (lo + hi) / 2;
+                if (rowp[c0 + mid] == want) { k = c0 + mid; break; }
+                if (rowp[c0 + mid] < want) lo = mid + 1;
+                else hi = mid - 1;
+            }
+            if (k < 0) continue;  // cannot happen for an adjacency built from the same mesh
+            double* blk = lhsK + 25 * (size_t)k;
+            for (int g = 0; g < 5; ++g)
+                for (int f = 0; f < 5; ++f)
+                    blk[5 * g + f] = blk[5 * g + f] + EG[(size_t)(5 * aa + f) * nedof + 5 * b + g];
+        }
+    }
+}
+
+// AsIGMR (asigmr.f:1-105) + bc3LHS + fillsparseC for one interior element (elmgmr.f:429-466)
+void one_element_lhs(const or_common& c, const Topo& tp, const or_mesh& m, const int* ie, const double* y,
+                     const double* ac, double* res, double* bd, const int* colm, const int* rowp, double* lhsK,
+                     const double* qres) {
+    const int nshg = m.nshg, nen = tp.nshl, nedof = 5 * nen;
+    double yl[8][5], acl[8][5], xl[8][3], ql[8][12];
+    for (int a = 0; a < nen; ++a) {
+        gather_y(y, nshg, ie[a], yl[a]);
+        gather_y(ac, nshg, ie[a], acl[a]);
+        gather_x(m.x, nshg, ie[a], xl[a]);
+        if (qres)
+            for (int k = 0; k < 12; ++k) ql[a][k] = qres[k * (size_t)nshg + ie[a]];
+    }
+    double rl[8][5] = {{0}}, rml[8][5] = {{0}};
+    std::vector<double> EG((size_t)nedof * nedof, 0.0);
+    e3_element(c, tp, 3, 1, yl, yl, acl, xl, rl, rml, nullptr, qres ? ql : nullptr, EG.data());
+    for (int k = 0; k < 5; ++k)
+        for (int a = 0; a < nen; ++a) res[k * (size_t)nshg + ie[a]] += rl[a][k];
+    // block diagonal from the tangent before its boundary conditions (asigmr.f:92-103)
+    for (int j = 0; j < 5; ++j)
+        for (int i = 0; i < 5; ++i)
+            for (int a = 0; a < nen; ++a)
+                bd[(i + 5 * j) * (size_t)nshg + ie[a]] += EG[(size_t)(5 * a + i) * nedof + 5 * a + j];
+    bc3lhs_element(m, ie, nen, EG.data());
+    fillsparse_element(ie, nen, EG.data(), colm, rowp, lhsK);
+}
 
 }  // namespace
 
@@ -1527,6 +1761,223 @@ void or_solmfg(or_common* c, const or_mesh* m, const double* y, const double* ac
     or_i3lu(N, bdiag, Dy, 2);
     st->iKs = iKs;
     st->lGMRES = lGMRES;
+    st->echeck = echeck;
+    st->eGMRES = c->eGMRES;
+    st->totres = std::sqrt(sumsq(res, n5)) / (double)N;
+}
+
+// genadj.f:1-76 with Asadj (asadj.f): every node's unique neighbours over all element blocks,
+// listed in ascending order; colm (nshg+1) and rowp are 1-based.  -1 when a row would
+// exceed 15*nnz entries or the total nnz*nshg (where the reference stops).
+int or_genadj(const or_mesh* m, int nnz, int* colm, int* rowp, int* icnt) {
+    const int N = m->nshg;
+    std::vector<std::vector<int>> rows(N);
+    auto add = [&](const int* ien, int nshl, int ne) {
+        for (int e = 0; e < ne; ++e) {
+            const int* nd = ien + (size_t)nshl * e;
+            for (int j = 0; j < nshl; ++j) {
+                std::vector<int>& r = rows[nd[j]];
+                for (int k = 0; k < nshl; ++k)
+                    if (std::find(r.begin(), r.end(), nd[k]) == r.end()) r.push_back(nd[k]);
+            }
+        }
+    };
+    add(m->ien, 4, m->nelem);
+    add(m->ienh, 8, m->nhex);
+    add(m->ienw, 6, m->nwedge);
+    colm[0] = 1;
+    int cnt = 0;
+    for (int i = 0; i < N; ++i) {
+        if ((int)rows[i].size() > 15 * nnz) return -1;
+        colm[i + 1] = colm[i] + (int)rows[i].size();
+        std::sort(rows[i].begin(), rows[i].end());
+        for (int v : rows[i]) {
+            if (cnt >= nnz * N) return -1;
+            rowp[cnt++] = v + 1;
+        }
+    }
+    *icnt = cnt;
+    return 0;
+}
+
+// ElmGMRs (elmgmr.f:280-613) with lhs = 1, iprec = 1: res, BDiag and the assembled
+// tangent lhsK(25, nnz_tot) (column-major 5x5 blocks, lhsK[25 k + 5 g + f] = (f, g))
+void or_elmgmrs(const or_common* c, const or_mesh* m, const double* y, const double* ac, const int* colm,
+                const int* rowp, int nnz_tot, double* res, double* bdiag, double* lhsK, int nthreads) {
+    const size_t N = m->nshg;
+    std::memset(res, 0, sizeof(double) * 5 * N);
+    std::memset(bdiag, 0, sizeof(double) * 25 * N);
+    std::memset(lhsK, 0, sizeof(double) * 25 * (size_t)nnz_tot);
+    std::vector<double> qres;
+    if (c->idiff == 1) {
+        qres.resize(12 * N);
+        reconstruct_q(*c, *m, y, qres.data());
+    }
+    const double* q = qres.empty() ? nullptr : qres.data();
+    const int ngrp = m->ngrp > 0 ? m->ngrp : 1;
+    for (int gI = 0; gI < ngrp; ++gI) {
+        const int b0 = m->ngrp > 0 ? m->grp_start[gI] : 0;
+        const int b1 = m->ngrp > 0 ? m->grp_start[gI + 1] : m->nblk;
+        parallel_for(b1 - b0, nthreads, [&](int bi) {
+            const int blk = b0 + bi;
+            for (int e = m->blk_start[blk]; e < m->blk_start[blk + 1]; ++e)
+                one_element_lhs(*c, topo(1), *m, m->ien + 4 * (size_t)e, y, ac, res, bdiag, colm, rowp, lhsK, q);
+        });
+    }
+    for (int e = 0; e < m->nhex; ++e)
+        one_element_lhs(*c, topo(2), *m, m->ienh + 8 * (size_t)e, y, ac, res, bdiag, colm, rowp, lhsK, q);
+    for (int e = 0; e < m->nwedge; ++e)
+        one_element_lhs(*c, topo(3), *m, m->ienw + 6 * (size_t)e, y, ac, res, bdiag, colm, rowp, lhsK, q);
+    boundary_sweep(*c, *m, y, res);
+    or_bc3res(m, y, res, c);
+    or_bc3bdg(m, y, bdiag, c);
+}
+
+// Spsi3pre (spsi3pre.f:1-196): lhsK(i, j) <- L_i^-1 lhsK(i, j) U_j^-1 with the i3LU factors
+// (unit lower L below the diagonal, U above it, reciprocal pivots on it)
+void or_spsi3pre(int N, const int* colm, const int* rowp, const double* bd, double* lhsK) {
+    auto B = [&](int n, int r, int cc) { return bd[(size_t)(r + 5 * cc) * N + n]; };
+    for (int i = 0; i < N; ++i)
+        for (int k = colm[i] - 1; k < colm[i + 1] - 1; ++k) {
+            double* a = lhsK + 25 * (size_t)k;
+            for (int r = 1; r < 5; ++r)
+                for (int g = 0; g < 5; ++g) {
+                    double v = a[5 * g + r];
+                    for (int cc = 0; cc < r; ++cc) v = v - B(i, r, cc) * a[5 * g + cc];
+                    a[5 * g + r] = v;
+                }
+        }
+    for (int i = 0; i < N; ++i)
+        for (int k = colm[i] - 1; k < colm[i + 1] - 1; ++k) {
+            const int j = rowp[k] - 1;
+            double* a = lhsK + 25 * (size_t)k;
+            for (int g = 0; g < 5; ++g)
+                for (int f = 0; f < 5; ++f) {
+                    double v = a[5 * g + f];
+                    for (int cc = 0; cc < g; ++cc) v = v - B(j, cc, g) * a[5 * cc + f];
+                    a[5 * g + f] = B(j, g, g) * v;
+                }
+        }
+}
+
+// SparseAp (sparseap.f:1-104) then bc3per (bc3per.f:1-20): p <- lhsK p with the periodic
+// gather p(:) = p(iper(:)) first and the slave rows summed into their masters after
+void or_sparseap(const or_mesh* m, const int* colm, const int* rowp, const double* lhsK, double* p) {
+    const int N = m->nshg;
+    std::vector<double> pg(5 * (size_t)N), q(5 * (size_t)N, 0.0);
+    for (int k = 0; k < 5; ++k)
+        for (int n = 0; n < N; ++n) pg[(size_t)k * N + n] = p[(size_t)k * N + m->iper[n]];
+    for (int i = 0; i < N; ++i) {
+        double t[5] = {0, 0, 0, 0, 0};
+        for (int k = colm[i] - 1; k < colm[i + 1] - 1; ++k) {
+            const int j = rowp[k] - 1;
+            const double* a = lhsK + 25 * (size_t)k;
+            for (int f = 0; f < 5; ++f)
+                t[f] = t[f] + a[f] * pg[j] + a[5 + f] * pg[(size_t)N + j] + a[10 + f] * pg[2 * (size_t)N + j] +
+                       a[15 + f] * pg[3 * (size_t)N + j] + a[20 + f] * pg[4 * (size_t)N + j];
+        }
+        for (int f = 0; f < 5; ++f) q[(size_t)f * N + i] = q[(size_t)f * N + i] + t[f];
+    }
+    for (int j = 0; j < N; ++j)
+        if (btest(m->iBC[j], 10)) {
+            const int i = m->iper[j];
+            for (int k = 0; k < 5; ++k) {
+                q[(size_t)k * N + i] = q[(size_t)k * N + i] + q[(size_t)k * N + j];
+                q[(size_t)k * N + j] = zero;
+            }
+        }
+    std::memcpy(p, q.data(), sizeof(double) * 5 * N);
+}
+
+// SolGMRs (solgmr.f:480-700): ElmGMRs, i3LU, Spsi3pre and GMRES on the preconditioned
+// assembled tangent.  st->lGMRES is read on entry as the COMMON lGMRES that the restart
+// test of solgmr.f:528 reads (SolGMRs itself counts in lGMRESs); it returns lGMRESs.
+void or_solgmrs(or_common* c, const or_mesh* m, const int* colm, const int* rowp, int nnz_tot, const double* y,
+                const double* ac, double* res, double* bdiag, double* Dy, double* lhsK, or_solve_stats* st,
+                int nthreads) {
+    const int N = m->nshg;
+    const size_t n5 = 5 * (size_t)N;
+    const int K = c->Kspace;
+    const int lGMRES_common = st->lGMRES;
+    std::vector<double> temp(n5), uB(n5 * (K + 1));
+    std::vector<double> H((K + 1) * K, 0.0), eB(K + 1, 0.0), yB(K, 0.0), Rc(K, 0.0), Rs(K, 0.0);
+    auto Hm = [&](int i, int j) -> double& { return H[(size_t)(i - 1) + (size_t)(K + 1) * (j - 1)]; };
+    auto U = [&](int j) { return uB.data() + n5 * (size_t)(j - 1); };
+    or_elmgmrs(c, m, y, ac, colm, rowp, nnz_tot, res, bdiag, lhsK, nthreads);
+    or_i3lu(N, bdiag, nullptr, 0);
+    or_i3lu(N, bdiag, res, 1);
+    std::fill(Dy, Dy + n5, 0.0);
+    or_spsi3pre(N, colm, rowp, bdiag, lhsK);
+    std::memcpy(U(1), res, sizeof(double) * n5);
+    double unorm = std::sqrt(sumsq(res, n5));
+    st->unorm0 = unorm;
+    int iKs = 0, lGMRESs = 0;
+    double echeck = 0.0;
+    if (!(unorm < 100. * c->epsM * c->epsM)) {
+        const double epsnrm = c->etol * unorm;
+        for (int mG = 1; mG <= c->nGMRES; ++mG) {
+            lGMRESs = mG - 1;
+            if (lGMRES_common > 0) {
+                std::memcpy(temp.data(), Dy, sizeof(double) * n5);
+                or_sparseap(m, colm, rowp, lhsK, temp.data());
+                for (size_t i = 0; i < n5; ++i) temp[i] = res[i] - temp[i];
+                std::memcpy(U(1), temp.data(), sizeof(double) * n5);
+                unorm = std::sqrt(sumsq(temp.data(), n5));
+            }
+            std::fill(eB.begin(), eB.end(), 0.0);
+            eB[0] = unorm;
+            for (size_t i = 0; i < n5; ++i) U(1)[i] = U(1)[i] / unorm;
+            for (int iK = 1; iK <= K; ++iK) {
+                iKs = iK;
+                std::memcpy(U(iKs + 1), U(iKs), sizeof(double) * n5);
+                or_sparseap(m, colm, rowp, lhsK, U(iKs + 1));
+                double beta = 0.0;
+                for (int jK = 1; jK <= iKs + 1; ++jK) {
+                    double* w = U(iKs + 1);
+                    if (jK == 1) {
+                        beta = dot(w, U(1), n5);
+                    } else {
+                        const double* up = U(jK - 1);
+                        for (size_t i = 0; i < n5; ++i) w[i] = w[i] - beta * up[i];
+                        beta = dot(w, U(jK), n5);
+                    }
+                    Hm(jK, iKs) = beta;
+                }
+                unorm = std::sqrt(beta);
+                Hm(iKs + 1, iKs) = unorm;
+                for (size_t i = 0; i < n5; ++i) U(iKs + 1)[i] = U(iKs + 1)[i] / unorm;
+                for (int jK = 1; jK <= iKs - 1; ++jK) {
+                    const double t = Rc[jK - 1] * Hm(jK, iKs) + Rs[jK - 1] * Hm(jK + 1, iKs);
+                    Hm(jK + 1, iKs) = -Rs[jK - 1] * Hm(jK, iKs) + Rc[jK - 1] * Hm(jK + 1, iKs);
+                    Hm(jK, iKs) = t;
+                }
+                const double t = std::sqrt(Hm(iKs, iKs) * Hm(iKs, iKs) + Hm(iKs + 1, iKs) * Hm(iKs + 1, iKs));
+                Rc[iKs - 1] = Hm(iKs, iKs) / t;
+                Rs[iKs - 1] = Hm(iKs + 1, iKs) / t;
+                Hm(iKs, iKs) = t;
+                Hm(iKs + 1, iKs) = zero;
+                const double te = Rc[iKs - 1] * eB[iKs - 1] + Rs[iKs - 1] * eB[iKs];
+                eB[iKs] = -Rs[iKs - 1] * eB[iKs - 1] + Rc[iKs - 1] * eB[iKs];
+                eB[iKs - 1] = te;
+                st->ntotGM += 1;
+                echeck = std::fabs(eB[iKs]);
+                if (echeck <= epsnrm && iKs >= c->minIters) break;
+            }
+            for (int jK = iKs; jK >= 1; --jK) {
+                yB[jK - 1] = eB[jK - 1] / Hm(jK, jK);
+                for (int lK = 1; lK <= jK - 1; ++lK) eB[lK - 1] = eB[lK - 1] - yB[jK - 1] * Hm(lK, jK);
+            }
+            for (int jK = 1; jK <= iKs; ++jK) {
+                const double* uj = U(jK);
+                for (size_t i = 0; i < n5; ++i) Dy[i] = Dy[i] + yB[jK - 1] * uj[i];
+            }
+            echeck = std::fabs(eB[iKs]);
+            if (echeck <= epsnrm) break;
+        }
+    }
+    or_i3lu(N, bdiag, Dy, 2);
+    st->iKs = iKs;
+    st->lGMRES = lGMRESs;
     st->echeck = echeck;
     st->eGMRES = c->eGMRES;
     st->totres = std::sqrt(sumsq(res, n5)) / (double)N;

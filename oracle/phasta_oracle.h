@@ -124,6 +124,23 @@ void or_yshuffle(int nshg, double* r, int code);
 void or_solmfg(or_common* c, const or_mesh* m, const double* y, const double* ac,
                double* res, double* bdiag, double* Dy, or_solve_stats* st, int nthreads);
 
+/* sparse solver (lhs = 1).  colm (nshg+1), rowp (nnz_tot) are 1-based as in the
+ * reference; lhsK (25, nnz_tot) column-major: lhsK[25*k + 5*g + f] is entry (f, g)
+ * of block k. */
+/* genadj.f + asadj.f; returns -1 where the reference stops ("increase nnz") */
+int or_genadj(const or_mesh* m, int nnz, int* colm, int* rowp, int* icnt);
+/* ElmGMRs (elmgmr.f:280) with lhs = iprec = 1 */
+void or_elmgmrs(const or_common* c, const or_mesh* m, const double* y, const double* ac, const int* colm,
+                const int* rowp, int nnz_tot, double* res, double* bdiag, double* lhsK, int nthreads);
+/* Spsi3pre (spsi3pre.f) with the i3LU factors in bd */
+void or_spsi3pre(int nshg, const int* colm, const int* rowp, const double* bd, double* lhsK);
+/* SparseAp (sparseap.f) then bc3per (bc3per.f): p <- lhsK p */
+void or_sparseap(const or_mesh* m, const int* colm, const int* rowp, const double* lhsK, double* p);
+/* SolGMRs (solgmr.f:480); st->lGMRES in: the COMMON lGMRES of the restart test */
+void or_solgmrs(or_common* c, const or_mesh* m, const int* colm, const int* rowp, int nnz_tot,
+                const double* y, const double* ac, double* res, double* bdiag, double* Dy, double* lhsK,
+                or_solve_stats* st, int nthreads);
+
 /* itrPC.f */
 void or_itrpredict(const or_common* c, int nshg, const double* yold, const double* acold,
                    double* y, double* ac);

@@ -68,6 +68,12 @@ def lib():
             "or_i3lu": ([C.c_int, _dp, _dp, C.c_int], None),
             "or_yshuffle": ([C.c_int, _dp, C.c_int], None),
             "or_solmfg": ([cp, mp, _dp, _dp, _dp, _dp, _dp, C.POINTER(OStats), C.c_int], None),
+            "or_genadj": ([mp, C.c_int, _ip, _ip, C.POINTER(C.c_int)], C.c_int),
+            "or_elmgmrs": ([cp, mp, _dp, _dp, _ip, _ip, C.c_int, _dp, _dp, _dp, C.c_int], None),
+            "or_spsi3pre": ([C.c_int, _ip, _ip, _dp, _dp], None),
+            "or_sparseap": ([mp, _ip, _ip, _dp, _dp], None),
+            "or_solgmrs": ([cp, mp, _ip, _ip, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(OStats), C.c_int],
+                           None),
             "or_itrpredict": ([cp, C.c_int, _dp, _dp, _dp, _dp], None),
             "or_itrcorrect": ([cp, C.c_int, _dp, _dp, _dp, _dp, _dp], None),
             "or_itrupdate": ([cp, C.c_int, _dp, _dp, _dp, _dp], None),
@@ -232,6 +238,55 @@ class Oracle:
         self.ntotGM = st.ntotGM
         self.params["eGMRES"] = self.c.eGMRES
         return res, bd, Dy, OracleStats(st.iKs, st.lGMRES, st.ntotGM, st.unorm0, st.echeck, st.eGMRES, st.totres)
+
+    # ---- sparse solver (lhs = 1): colm/rowp 1-based, lhsK (nnz_tot, 25) = the reference's lhsK(25, nnz_tot)
+    def genadj(self, nnz: int = 40):
+        colm = np.zeros(self.nshg + 1, np.int32)
+        rowp = np.zeros(self.nshg * nnz, np.int32)
+        icnt = C.c_int()
+        if self.L.or_genadj(C.byref(self.m), nnz, _i(colm), _i(rowp), C.byref(icnt)) != 0:
+            raise ValueError("genadj: more than nnz blocks in a row")
+        self.colm, self.rowp = colm, np.ascontiguousarray(rowp[: icnt.value])
+        return self.colm.copy(), self.rowp.copy()
+
+    def _adj(self):
+        if not hasattr(self, "colm"):
+            self.genadj()
+        return self.colm, self.rowp
+
+    def ElmGMRs(self, y, ac):
+        colm, rowp = self._adj()
+        res, bd = self._v(), self._v(25)
+        lhsK = np.zeros((len(rowp), 25))
+        self.L.or_elmgmrs(C.byref(self.c), C.byref(self.m), _d(y), _d(ac), _i(colm), _i(rowp), len(rowp), _d(res),
+                          _d(bd), _d(lhsK), self.nthreads)
+        return res, bd, lhsK
+
+    def Spsi3pre(self, lu, lhsK):
+        colm, rowp = self._adj()
+        out = np.array(lhsK, dtype=np.float64, order="C")
+        self.L.or_spsi3pre(self.nshg, _i(colm), _i(rowp), _d(np.ascontiguousarray(lu, dtype=np.float64)), _d(out))
+        return out
+
+    def SparseAp(self, lhsK, p):
+        colm, rowp = self._adj()
+        p = np.array(p, dtype=np.float64)
+        self.L.or_sparseap(C.byref(self.m), _i(colm), _i(rowp), _d(np.ascontiguousarray(lhsK, dtype=np.float64)),
+                           _d(p))
+        return p
+
+    def SolGMRs(self, y, ac, lGMRES_common: int = 0):
+        colm, rowp = self._adj()
+        res, bd, Dy = self._v(), self._v(25), self._v()
+        lhsK = np.zeros((len(rowp), 25))
+        st = OStats()
+        st.ntotGM = self.ntotGM
+        st.lGMRES = lGMRES_common
+        self.L.or_solgmrs(C.byref(self.c), C.byref(self.m), _i(colm), _i(rowp), len(rowp), _d(y), _d(ac), _d(res),
+                          _d(bd), _d(Dy), _d(lhsK), C.byref(st), self.nthreads)
+        self.ntotGM = st.ntotGM
+        return res, bd, Dy, lhsK, OracleStats(st.iKs, st.lGMRES, st.ntotGM, st.unorm0, st.echeck, st.eGMRES,
+                                              st.totres)
 
     def itrPredict(self, yold, acold):
         y, ac = self._v(), self._v()

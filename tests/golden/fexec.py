@@ -912,6 +912,20 @@ def _pow(a, b):
     return np.power(a, b)
 
 
+def _minloc(a):
+    a = np.asarray(a)
+    if a.ndim != 1:
+        raise FortranUnsupported("minloc of a multi-dimensional array")
+    return np.array([int(np.argmin(a)) + 1])
+
+
+def _maxloc(a):
+    a = np.asarray(a)
+    if a.ndim != 1:
+        raise FortranUnsupported("maxloc of a multi-dimensional array")
+    return np.array([int(np.argmax(a)) + 1])
+
+
 def _btest(i, pos):
     r = (np.right_shift(np.asarray(i, dtype=np.int64), int(pos)) & 1) != 0
     return bool(r) if r.ndim == 0 else r
@@ -960,7 +974,7 @@ _INTRINSIC = {
     "tiny": ("(lambda x: float(np.finfo(np.float64).tiny))", "r"),
     "floor": ("(lambda x: np.floor(x).astype(np.int64) if isinstance(x, np.ndarray) else int(np.floor(x)))", "i"),
     "trim": ("(lambda s: str(s).rstrip())", "c"), "len": ("len", "i"),
-    "btest": ("_btest", "l"), "ibits": ("_ibits", "i"), "ibset": ("_ibset", "i"), "ibclr": ("_ibclr", "i"),
+    "btest": ("_btest", "l"), "ibits": ("_ibits", "i"), "minloc": ("_minloc", "i"), "maxloc": ("_maxloc", "i"), "ibset": ("_ibset", "i"), "ibclr": ("_ibclr", "i"),
     "iand": ("np.bitwise_and", "i"), "ior": ("np.bitwise_or", "i"), "ieor": ("np.bitwise_xor", "i"),
 }
 
@@ -977,6 +991,7 @@ class _Gen:
         self.lines: list[str] = []
         self.ind = 1
         self.tmp = 0
+        self.cycle_labels, self.while_heads, self.while_gotos = set(), set(), set()
 
     # ---- names
     def var(self, name) -> Var:
@@ -1231,8 +1246,37 @@ class _Gen:
         self.ret = self._ret_code()
         known = set(u.syms)
         init_at = len(self.lines)
+        # labels of a loop's last statement ("L continue" right before the loop's end):
+        # a forward goto there is a cycle of that loop
+        self.cycle_labels = set()
+        body = u.body
+        for i, (lab, text, _w) in enumerate(body):
+            if lab is None or text != "continue":
+                continue
+            nxt = body[i + 1][1] if i + 1 < len(body) else ""
+            if re.match(r"^end\s*do$", nxt) or any(re.match(rf"^do\s+{lab}\b", t) for _l, t, _x in body[:i]):
+                self.cycle_labels.add(lab)
+        # "L if (c) then ... goto L endif" is a while loop
+        self.while_heads, self.while_gotos = set(), set()
+        for i, (lab, text, _w) in enumerate(body):
+            if lab is None or not re.match(r"^if\s*\(.*\)\s*then$", text):
+                continue
+            depth, j = 0, i
+            for j in range(i, len(body)):
+                t = body[j][1]
+                if re.match(r"^if\s*\(.*\)\s*then$", t) and self._balanced_if(t):
+                    depth += 1
+                elif re.match(r"^end\s*if$", t):
+                    depth -= 1
+                    if depth == 0:
+                        break
+            prev = body[j - 1][1] if j - 1 > i else ""
+            if re.match(rf"^go\s*to\s+{lab}$", prev):
+                self.while_heads.add(i)
+                self.while_gotos.add(j - 1)
         stack = []  # ('if'|'do'|'dolab', label)
-        for lab, text, where in u.body:
+        for idx, (lab, text, where) in enumerate(u.body):
+            self.cur = idx
             try:
                 self.stmt(text, stack, where)
             except FortranUnsupported as exc:
@@ -1309,7 +1353,7 @@ class _Gen:
         m = re.match(r"^if\s*\((.*)\)\s*then$", t)
         if m and self._balanced_if(t):
             c = self.cond_code(m.group(1), where)
-            self.emit(f"if _cond({c}):")
+            self.emit(f"{'while' if getattr(self, 'cur', -1) in self.while_heads else 'if'} _cond({c}):")
             self.ind += 1
             self.emit("pass")
             stack.append(("if", None))
@@ -1394,6 +1438,13 @@ class _Gen:
             return
         if re.match(r"^(write|print|format|flush|open|close|read)\b", t):
             self.emit("pass")
+            return
+        m = re.match(r"^go\s*to\s+(\d+)$", t)
+        if m and getattr(self, "cur", -1) in self.while_gotos:
+            self.emit("continue")
+            return
+        if m and int(m.group(1)) in self.cycle_labels and any(k in ("do", "dolab") for k, _ in stack):
+            self.emit("continue")
             return
         if re.match(r"^(go\s*to)\b", t):
             raise FortranUnsupported("goto")

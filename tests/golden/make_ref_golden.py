@@ -5,7 +5,8 @@ there).  fexec.py translates the reference's fixed-form sources of the hot
 path into numpy code in memory and refrun.py sets the COMMON blocks, so the
 arrays written here are what ElmMFG, ItrRes, i3LU, itrBC, SolMFG, itrSetup,
 itrPredict, itrCorrect and itrUpdate of the reference compute for the seeded
-inputs, which are stored beside the outputs.
+inputs, which are stored beside the outputs; for the sparse solver (lhs = 1)
+also genadj, ElmGMRs, Spsi3pre, SparseAp (with bc3per) and SolGMRs.
 
     python tests/golden/make_ref_golden.py [reference phSolver directory]
 """
@@ -27,17 +28,19 @@ from refrun import RefPhasta  # noqa: E402
 DEFAULT_REF = Path("/root/reference/phSolver")
 
 # (name, case builder, parts): "elm" ElmMFG; "pieces" ItrRes, i3LU, itrBC; "solve" SolMFG;
-# "step" itrSetup and one two-iteration time step
+# "step" itrSetup and one two-iteration time step; "sparse" genadj, ElmGMRs (assembled
+# tangent lhsK), Spsi3pre, SparseAp and SolGMRs
 ALL = ("elm", "pieces", "solve", "step")
 CASES = [
-    ("channel4", lambda: channel(4, ac_scale=0.05), ALL),
-    ("vortex4", lambda: vortex(4), ALL),
+    ("channel4", lambda: channel(4, ac_scale=0.05), ALL + ("sparse",)),
+    ("vortex4", lambda: vortex(4), ALL + ("sparse",)),
     ("channel3_euler", lambda: channel(3, ac_scale=0.05, navier=0), ("elm",)),
     ("channel3_galerkin", lambda: channel(3, ac_scale=0.05, ivart=1), ("elm",)),
     # Kspace 3 with two cycles: the second cycle restarts from Au2MFG's R - J Dy
-    ("channel4_restart", lambda: channel(4, ac_scale=0.05, Kspace=3, nGMRES=2), ("elm", "solve")),
+    # (SolGMRs restarts from its stale first vector: its test reads lGMRES, solgmr.f:528)
+    ("channel4_restart", lambda: channel(4, ac_scale=0.05, Kspace=3, nGMRES=2), ("elm", "solve", "sparse")),
     # tet, hex (lcsyst 2) and wedge (lcsyst 3) blocks
-    ("mixed3", lambda: mixed(3, 3, (3, 3, 2)), ALL),
+    ("mixed3", lambda: mixed(3, 3, (3, 3, 2)), ALL + ("sparse",)),
     # idiff = 1: the diffusive flux reconstructed (AsIq/e3q/qpbc) and its divergence in e3LS
     ("channel4_idiff", lambda: channel(4, ac_scale=0.05, idiff=1), ALL),
     ("mixed3_idiff", lambda: mixed(3, 3, (3, 3, 2), idiff=1), ("elm", "solve")),
@@ -78,6 +81,24 @@ def make(name, build, parts, ref_root):
         R2 = RefPhasta(case, p, ref_root)
         yold, acold, y1, ac1, iks = R2.time_step(y, ac, 2)
         out.update(step_yold=yold, step_acold=acold, step_y=y1, step_ac=ac1, step_iks=np.array(iks))
+    if "sparse" in parts:
+        R3 = RefPhasta(case, p, ref_root)  # fresh COMMON: lGMRES = ntotGM = 0
+        colm, rowp = R3.genadj()
+        gres, gbd, lhsK = R3.ElmGMRs(y, ac)
+        out.update(sp_colm=colm.astype(np.int32), sp_rowp=rowp.astype(np.int32), sp_lhsK=lhsK, sp_res=gres,
+                   sp_bd=gbd)
+        # Spsi3pre with the LU factors of the golden BDiag, then SparseAp on a seeded vector
+        lu, _ = R3.i3LU(gbd, None, 0)
+        pre = R3.Spsi3pre(lu, lhsK)
+        rng = np.random.default_rng(11)
+        pv = rng.standard_normal(5 * case.nshg)
+        out.update(sp_lu=lu, sp_pre=pre, sp_p=pv, sp_ap=R3.SparseAp(pre, pv))
+        R4 = RefPhasta(case, p, ref_root)
+        R4.genadj()
+        # (its preconditioned lhsK equals sp_pre bit for bit, so it is not stored again)
+        sres, sbd, sDy, _, st = R4.SolGMRs(y, ac, y, ac)
+        out.update(sps_res=sres, sps_bd=sbd, sps_Dy=sDy, sps_iKs=np.array(st["iKs"]),
+                   sps_lGMRES=np.array(st["lGMRES"]), sps_ntotGM=np.array(st["ntotGM"]))
     path = HERE / f"ref_{name}.npz"
     np.savez_compressed(path, **out)
     print(f"{path.name}: {path.stat().st_size // 1024} KiB, nshg {case.nshg}, nelem {case.nelem}")

@@ -38,6 +38,11 @@ SOURCES = [
     "compressible/itrPC.f", "common/mpitools.f", "common/clear.f",
     # idiff = 1: global reconstruction of the diffusive flux
     "compressible/asiq.f", "compressible/e3q.f", "compressible/e3qvar.f", "common/qpbc.f",
+    # assembled tangent: ElmGMRs, AsIGMR, e3massl, bc3LHS, fillsparseC, genadj/Asadj,
+    # Spsi3pre, SparseAp, SolGMRs
+    "compressible/elmgmr.f", "compressible/asigmr.f", "compressible/e3massl.f", "compressible/bc3lhs.f",
+    "common/fillsparse.f", "common/genadj.f", "common/asadj.f", "compressible/spsi3pre.f",
+    "compressible/sparseap.f", "compressible/solgmr.f",
 ]
 # rstat.f only prints statistics, and SolMFG calls it with two of its three
 # arguments (solmfg.f:367 vs rstat.f:1); its totres (rstat.f:108) is computed
@@ -67,7 +72,8 @@ class RefPhasta:
         for f in SOURCES:
             P.load(root / f)
         P.stubs.update(timer=lambda *a: None, secs=lambda *a: 0.0, tmr=lambda *a: 0.0,
-                       tmrc=lambda *a: 0.0, tnanq=lambda *a: None, rstat=lambda *a: None)
+                       tmrc=lambda *a: 0.0, tnanq=lambda *a: None, rstat=lambda *a: None,
+                       rstatcheck=lambda *a: None)
         N, E, Eb = case.nshg, case.nelem, case.nbelem
         self.N, self.case, self.params = N, case, dict(params)
         # interior blocks by topology: (connectivity, lcsyst, nshl, points)
@@ -93,7 +99,9 @@ class RefPhasta:
         G.numnp = G.nshg = N
         G.nshgt = N
         G.numel, G.numelb = E, Eb
-        G.nen, G.ndof, G.nflow, G.nedof = 4, 5, 5, 20
+        # nen is the largest element of the mesh (readnblk.f) and nedof = nflow*nshape (itrdrv.f:458)
+        nenmax = max(nshl for _c, _l, nshl, _q in blocks)
+        G.nen, G.ndof, G.nflow, G.nedof = nenmax, 5, 5, 5 * nenmax
         G.ndofbc, G.ndibcb, G.ndbcb = 6, 2, 6
         G.nelblk, G.nelblb = len(blocks), (1 if Eb else 0)
         # lcblk(:,iblk): iel, lelCat, lcsyst, iorder, nenl, -, mattyp, ndofl, nsymdl, nshl
@@ -243,3 +251,75 @@ class RefPhasta:
         yold, acold = self.itrUpdate(yold, acold, y, ac)
         yold, acold = self.itrBC(yold, acold)
         return yold, acold, y, ac, iks
+
+    # ---- assembled tangent (lhs = 1): the reference's default sparse solver
+    def genadj(self, nnz: int = 40):
+        """colm (nshg+1), rowp (icnt) of genadj.f: 1-based block CSR of the node adjacency."""
+        N = self.N
+        G = self.G
+        G.nnz = nnz
+        colm = np.zeros(N + 1, np.int64)
+        rowp = np.zeros(N * nnz, np.int64)
+        r = self.P.call("genadj", colm, rowp, 0)
+        icnt = int(r[0])
+        G.nnz_tot = icnt
+        self.colm, self.rowp = colm, rowp
+        return colm.copy(), rowp[:icnt].copy()
+
+    def ElmGMRs(self, y, ac):
+        """res, BDiag (from the tangent's diagonal blocks) and lhsK(25, nnz_tot) of ElmGMRs (lhs = 1)."""
+        N = self.N
+        G = self.G
+        if not hasattr(self, "colm"):
+            self.genadj()
+        G.lhs, G.iprec = 1, 1
+        lhsK = np.zeros((25, int(G.nnz_tot)), order="F")
+        res, rmes = np.zeros((N, 5), order="F"), np.zeros((N, 5), order="F")
+        bd = np.zeros((N, 5, 5), order="F")
+        self.P.call("elmgmrs", _F(np.array(y), (N, 5)), _F(np.array(ac), (N, 5)), self.x, self.shp, self.shgl,
+                    self.iBC, self.BC, self.shpb, self.shglb, res, rmes, bd, self.iper, self.ilwork, lhsK,
+                    self.colm, self.rowp, self.rerr)
+        G.lhs = 0
+        return res.reshape(-1, order="F"), bd.reshape(-1, order="F"), lhsK
+
+    def SolGMRs(self, y, ac, yold, acold):
+        N, K = self.N, self.params["Kspace"]
+        G = self.G
+        if not hasattr(self, "colm"):
+            self.genadj()
+        G.lhs, G.iprec = 1, 1
+        lhsK = np.zeros((25, int(G.nnz_tot)), order="F")
+        res = np.zeros((N, 5), order="F")
+        bd = np.zeros((N, 5, 5), order="F")
+        Dy = np.zeros((N, 5), order="F")
+        HBrg = np.zeros((K + 1, K), order="F")
+        eBrg, yBrg = np.zeros(K + 1), np.zeros(K)
+        Rcos, Rsin = np.zeros(K), np.zeros(K)
+        self.P.call("solgmrs", _F(np.array(y), (N, 5)), _F(np.array(ac), (N, 5)), _F(np.array(yold), (N, 5)),
+                    _F(np.array(acold), (N, 5)), self.x, self.iBC, self.BC, self.colm, self.rowp, lhsK, res, bd,
+                    HBrg, eBrg, yBrg, Rcos, Rsin, self.iper, self.ilwork, self.shp, self.shgl, self.shpb,
+                    self.shglb, Dy, self.rerr)
+        G.lhs = 0
+        # SolGMRs counts its cycles in lGMRESs (solgmr.f:511,526)
+        stats = {"iKs": int(G.iks), "lGMRES": int(G.lgmress), "ntotGM": int(G.ntotgm)}
+        return res.reshape(-1, order="F"), bd.reshape(-1, order="F"), Dy.reshape(-1, order="F"), lhsK, stats
+
+    def Spsi3pre(self, lu, lhsK):
+        """lhsK after Spsi3pre (spsi3pre.f:1) with the LU factors lu of i3LU."""
+        N = self.N
+        if not hasattr(self, "colm"):
+            self.genadj()
+        bdF = _F(np.array(lu), (N, 5, 5)).copy(order="F")
+        out = np.array(lhsK, order="F", copy=True)
+        self.P.call("spsi3pre", bdF, out, self.colm, self.rowp)
+        return out
+
+    def SparseAp(self, lhsK, p):
+        """lhsK p of SparseAp (sparseap.f:1) with the periodic gather of p, then bc3per (solgmr.f:566)."""
+        N = self.N
+        if not hasattr(self, "colm"):
+            self.genadj()
+        pF = _F(np.array(p), (N, 5)).copy(order="F")
+        self.P.call("sparseap", self.iper, self.ilwork, self.iBC, self.colm, self.rowp, np.asfortranarray(lhsK), pF)
+        self.P.call("bc3per", self.iBC, pF, self.iper, self.ilwork, 5)
+        return pF.reshape(-1, order="F")

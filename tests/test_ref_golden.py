@@ -95,3 +95,41 @@ def test_oracle_time_step_matches_reference(name):
     assert [s.iKs for s in stats] == list(d["step_iks"])
     assert rel(y, d["step_y"]) < 1e-9 and rel(yold, d["step_yold"]) < 1e-9
     assert rel(ac, d["step_ac"]) < 1e-7 and rel(acold, d["step_acold"]) < 1e-7
+
+
+# ---- sparse solver (lhs = 1): the reference's lhsK(25, nnz_tot) is stored as a (25, nnz) array
+@pytest.mark.parametrize("name", having("sparse"))
+def test_oracle_genadj_matches_reference(name):
+    d, case, p = load(name)
+    colm, rowp = pyoracle.Oracle(case, p).genadj()
+    assert np.array_equal(colm, d["sp_colm"]) and np.array_equal(rowp, d["sp_rowp"])
+
+
+@pytest.mark.parametrize("name", having("sparse"))
+def test_oracle_elmgmrs_matches_reference(name):
+    d, case, p = load(name)
+    res, bd, lhsK = pyoracle.Oracle(case, p).ElmGMRs(d["y"], d["ac"])
+    assert rel(res, d["sp_res"]) < 1e-12
+    assert rel(bd, d["sp_bd"]) < 1e-12
+    assert rel(lhsK, d["sp_lhsK"].T) < 1e-12
+
+
+@pytest.mark.parametrize("name", having("sparse"))
+def test_oracle_spsi3pre_sparseap_match_reference(name):
+    d, case, p = load(name)
+    o = pyoracle.Oracle(case, p)
+    pre = o.Spsi3pre(d["sp_lu"], d["sp_lhsK"].T)
+    assert rel(pre, d["sp_pre"].T) < 1e-12
+    assert rel(o.SparseAp(d["sp_pre"].T, d["sp_p"]), d["sp_ap"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", having("sparse"))
+def test_oracle_solgmrs_matches_reference(name):
+    d, case, p = load(name)
+    o = pyoracle.Oracle(case, p)
+    res, bd, Dy, lhsK, st = o.SolGMRs(d["y"], d["ac"])
+    assert rel(res, d["sps_res"]) < 1e-12
+    assert rel(bd, d["sps_bd"]) < 1e-12
+    assert rel(lhsK, d["sp_pre"].T) < 1e-12
+    assert (st.iKs, st.lGMRES, st.ntotGM) == (int(d["sps_iKs"]), int(d["sps_lGMRES"]), int(d["sps_ntotGM"]))
+    assert rel(Dy, d["sps_Dy"]) < 1e-9
