@@ -50,7 +50,9 @@ enum {
 };
 
 enum { PHGPU_FP64 = 0, PHGPU_MIXED = 1 };         /* precision */
-enum { PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1 };     /* Jacobian-vector product */
+/* Jacobian-vector product: finite-differenced (Au1MFG), linearized, or the assembled
+ * tangent of the sparse solver (SolGMRs, solgmr.f:480) */
+enum { PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1, PHGPU_AP_SPARSE = 2 };
 enum { PHGPU_RES_FP64 = 0, PHGPU_RES_GALERKIN64 = 1, PHGPU_RES_SPLITDF = 2 }; /* outer residual in mixed precision */
 enum { PHGPU_LU_FACT = 0, PHGPU_LU_FORWARD = 1, PHGPU_LU_BACKWARD = 2, PHGPU_LU_PRODUCT = 3 };
 
@@ -75,7 +77,8 @@ typedef struct {
     /* options of this implementation */
     int precision;                   /* PHGPU_FP64: reference arithmetic; PHGPU_MIXED: FP32
                                         assembly and Ap, FP64 outer residual, dots, Givens, LU */
-    int ap_mode;                     /* PHGPU_AP_FD (Au1MFG) or PHGPU_AP_LINEAR */
+    int ap_mode;                     /* PHGPU_AP_FD (Au1MFG), PHGPU_AP_LINEAR or PHGPU_AP_SPARSE
+                                        (the drivers then solve with SolGMRs, lhs = 1) */
     int outer_residual;              /* mixed precision only: PHGPU_RES_FP64 (every term FP64),
                                         PHGPU_RES_GALERKIN64 (metrics, Euler flux and time term FP64;
                                         least-squares and viscous terms FP32) or PHGPU_RES_SPLITDF
@@ -156,6 +159,33 @@ int phgpu_newton(phgpu_ctx* ctx, double* y, double* ac, const double* yold,
 /* one time step: yold/acold updated in place, y/ac returned */
 int phgpu_time_step(phgpu_ctx* ctx, double* yold, double* acold, double* y, double* ac,
                     int nitr, phgpu_stats* st);
+
+/* ---- sparse solver: the reference's impl = 1x path (lhs = 1, itrdrv.f:452-488) ----
+ * lhsK is the reference's lhsK(25, nnz_tot) (FP64): block k is 25 contiguous values with
+ * entry (f, g) of the 5x5 block at 25*k + 5*g + f (row f = equation, column g = dof);
+ * the blocks follow genadj's colm/rowp, rows by node and columns ascending. */
+/* genadj (genadj.f:1, asadj.f:1) on the host, no context or GPU needed: colm (nshg+1) and
+ * rowp (room for nnz*nshg) 1-based as in the reference, *icnt = nnz_tot.  Returns
+ * PHGPU_ERR_TOO_LARGE where the reference stops (a row of more than 15*nnz nodes, or more
+ * than nnz*nshg blocks), PHGPU_ERR_INVALID for a node index out of range. */
+int phgpu_genadj(const phgpu_mesh* mesh, int nnz, int* colm, int* rowp, int* icnt);
+/* nnz_tot of the context's mesh (the first sparse call builds the device structure) */
+int phgpu_nnz_tot(phgpu_ctx* ctx, int* nnz_tot);
+/* ElmGMRs (elmgmr.f:280) with lhs = 1, iprec = 1, FP64: res, BDiag and lhsK */
+int phgpu_elmgmrs(phgpu_ctx* ctx, const double* y, const double* ac, double* res, double* bdiag,
+                  double* lhsK);
+/* Spsi3pre (spsi3pre.f:1) on host arrays; bdiag holds the i3LU factors */
+int phgpu_spsi3pre(phgpu_ctx* ctx, const double* bdiag, double* lhsK);
+/* SparseAp (sparseap.f:1) then bc3per (bc3per.f:1), as SolGMRs applies them: p <- lhsK p */
+int phgpu_sparseap(phgpu_ctx* ctx, const double* lhsK, double* p);
+/* SolGMRs (solgmr.f:480) in the configured precision: lhs = 1 assembles BDiag and the tangent
+ * (iprec = lhs, itrdrv.f:456-457); lhs = 0 reuses the factored BDiag and the preconditioned
+ * tangent of the last lhs = 1 call (PHGPU_ERR_INVALID if there is none).  Outputs as
+ * phgpu_solmfg, plus the preconditioned tangent in lhsK (FP64 solves; may be NULL).
+ * st->lGMRES on entry is the COMMON lGMRES that SolGMRs' restart test reads
+ * (solgmr.f:528, never set by SolGMRs itself); on return, the cycles done less one. */
+int phgpu_solgmrs(phgpu_ctx* ctx, const double* y, const double* ac, int lhs, double* res,
+                  double* bdiag, double* Dy, double* lhsK, phgpu_stats* st);
 
 /* device-resident state (no host traffic inside) */
 int phgpu_upload_state(phgpu_ctx* ctx, const double* y, const double* ac,

@@ -15,7 +15,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libphgpu.so"
 PHGPU_OK = 0
 STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NONFINITE", 4: "SINGULAR", 5: "UNSUPPORTED", 6: "NOMEM", 7: "TOO_LARGE"}
 PHGPU_FP64, PHGPU_MIXED = 0, 1
-PHGPU_AP_FD, PHGPU_AP_LINEAR = 0, 1
+PHGPU_AP_FD, PHGPU_AP_LINEAR, PHGPU_AP_SPARSE = 0, 1, 2
 PHGPU_RES_FP64, PHGPU_RES_GALERKIN64, PHGPU_RES_SPLITDF = 0, 1, 2
 PHGPU_ERR_INVALID, PHGPU_ERR_TOO_LARGE = 1, 7
 PHGPU_RSTAT_NOALLOC_MAX_N = 33554432
@@ -94,6 +94,12 @@ def lib():
         "phgpu_residual_norm_dev": ([vp, _dp], C.c_int),
         "phgpu_sweep_dev": ([vp, C.c_int], C.c_int),
         "phgpu_rstat_noalloc": ([vp, C.c_int, vp, vp], C.c_int),
+        "phgpu_genadj": ([C.POINTER(Mesh), C.c_int, _ip, _ip, C.POINTER(C.c_int)], C.c_int),
+        "phgpu_nnz_tot": ([vp, C.POINTER(C.c_int)], C.c_int),
+        "phgpu_elmgmrs": ([vp, _dp, _dp, _dp, _dp, _dp], C.c_int),
+        "phgpu_spsi3pre": ([vp, _dp, _dp], C.c_int),
+        "phgpu_sparseap": ([vp, _dp, _dp], C.c_int),
+        "phgpu_solgmrs": ([vp, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(Stats)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

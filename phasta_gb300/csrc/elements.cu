@@ -18,6 +18,7 @@
 // Results agree with the statement-by-statement restatement to rounding.
 #include "phgpu_impl.cuh"
 #include "df64.cuh"
+#include "qpoint.cuh"
 
 // occupancy targets (resident CTAs per SM) of the FP32 chunk kernels
 #ifndef PHGPU_RES32_MINB
@@ -111,23 +112,12 @@ template Phys<float> make_phys<float>(const phgpu_config&);
 
 namespace {
 
-__device__ __forceinline__ float rsqrt_(float v) { return rsqrtf(v); }
-__device__ __forceinline__ double rsqrt_(double v) { return rsqrt(v); }
-
 template <typename R> __device__ __forceinline__ R shp(int q, int a);
 template <> __device__ __forceinline__ double shp<double>(int q, int a) { return c_tab.shp[q][a]; }
 template <> __device__ __forceinline__ float shp<float>(int q, int a) { return c_shpf[q][a]; }
 template <typename R> __device__ __forceinline__ R qwt();
 template <> __device__ __forceinline__ double qwt<double>() { return c_tab.Qwt[0]; }
 template <> __device__ __forceinline__ float qwt<float>() { return c_qwtf; }
-
-template <typename R>
-struct Geo {
-    R WdetJ;
-    R shg[4][3];
-    R G[6];  // tet-invariant metric, order (11, 12, 22, 13, 23, 33)
-    R GG, trG;
-};
 
 template <typename R>
 __device__ __forceinline__ void geometry(const R (&xl)[4][3], Geo<R>& g) {
@@ -206,49 +196,6 @@ __device__ __forceinline__ void viscous(const Phys<R>& P, const R (&g)[3][5], Vi
     }
 }
 
-template <typename R>
-struct Qp {
-    R u[3], p, T;
-    R rho, rk, ei, drdp, drdT, e1p, e2p, e3p, e4p;
-    R tau[3];
-};
-
-// thermodynamics and the scalars that define A0..A3 (getthm.f ipress=0, e3mtrx.f)
-template <typename R>
-__device__ __forceinline__ void qp_state(const Phys<R>& P, R p, R u0, R u1, R u2, R T, Qp<R>& b) {
-    b.p = p;
-    b.u[0] = u0;
-    b.u[1] = u1;
-    b.u[2] = u2;
-    b.T = T;
-    const R rT = R(1) / T;
-    b.drdp = P.rRgas * rT;            // rho * betaT = 1/(R T)
-    b.rho = p * b.drdp;
-    b.drdT = -b.rho * rT;             // -rho * alfap
-    b.rk = R(0.5) * (u0 * u0 + u1 * u1 + u2 * u2);
-    b.ei = T * P.cv;
-    const R hk = T * P.cp + b.rk;
-    b.e1p = b.drdp * hk - rT * T;
-    b.e2p = b.e1p + R(1);
-    b.e3p = b.rho * hk;
-    b.e4p = b.drdT * hk + b.rho * P.cp;
-}
-
-// diagonal tau (e3tau.f:140-181, itau = 0)
-template <typename R>
-__device__ __forceinline__ void qp_tau(const Phys<R>& P, const Geo<R>& geo, Qp<R>& b) {
-    const R* G = geo.G;
-    const R u0 = b.u[0], u1 = b.u[1], u2 = b.u[2];
-    const R uGu = u0 * (u0 * G[0] + R(2) * (u1 * G[1] + u2 * G[3])) + u1 * (u1 * G[2] + R(2) * u2 * G[4]) +
-                  u2 * u2 * G[5];
-    const R t2 = b.rho * b.rho * (P.dts2 + uGu) + P.fmu2 * geo.GG;
-    const R rfact = rsqrt_(t2);
-    const R fact = t2 * rfact;
-    b.tau[0] = R(0.125) * fact / (b.rho * geo.trG) * P.taucfct;
-    b.tau[1] = rfact;
-    b.tau[2] = rfact * P.rtempcv;
-}
-
 // sum_i A_i Y,i (e3conv.f:100-179) in closed form
 template <typename R>
 __device__ __forceinline__ void ai_gi(const Qp<R>& b, const R (&g)[3][5], R (&o)[5]) {
@@ -290,8 +237,6 @@ __device__ __forceinline__ void add_ai_v(const Qp<R>& b, const R (&v)[5], R (&F)
         F[i][4] += b.u[i] * t + b.e3p * v[1 + i];
     }
 }
-
-template <typename R> __device__ __forceinline__ R ldg(const R* p) { return __ldg(p); }
 
 template <typename R>
 __device__ __forceinline__ void load5(const R* __restrict__ a, int n, R (&o)[5]) {
@@ -1525,16 +1470,6 @@ k_boundary(const int4* __restrict__ ienb, const int* __restrict__ iBCB, const do
 // its node's weighted terms over the points (e3wmlt.f, e3bdg.f) and adds
 // them to the node.  Elements of one colour share no node.
 // --------------------------------------------------------------------------
-struct TopoTabD {
-    double shp[8][8];      // [q][a]
-    double shgl[8][3][8];  // [q][i][a]
-    double qwt[8];
-};
-struct TopoTabF {
-    float shp[8][8];
-    float shgl[8][3][8];
-    float qwt[8];
-};
 __constant__ TopoTabD c_topo[2];   // 0 hex, 1 wedge
 __constant__ TopoTabF c_topof[2];
 
@@ -1919,9 +1854,10 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
 }  // namespace
 
 // hex and wedge tables: the rules and linear shapes of symhex.c/symwdg.c and
-// HexShapeAndDrv/WedgeShapeAndDrv (wedge in-plane derivatives on the area-2 parent)
-void upload_topo_tables(Ctx& C) {
-    TopoTabD t[2] = {};
+// HexShapeAndDrv/WedgeShapeAndDrv (wedge in-plane derivatives on the area-2 parent);
+// tet: the 4-point rule of symtet.c with the halved vertex-mode gradients of genshp.f:32-35
+void topo_tables_host(TopoTabD* t) {
+    for (int k = 0; k < 3; ++k) t[k] = TopoTabD{};
     const double g = 0.577350269189626;
     const double sgn[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
                               {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
@@ -1954,6 +1890,22 @@ void upload_topo_tables(Ctx& C) {
             t[1].shgl[q][2][a] = L[v] * zs / 2.0;
         }
     }
+    const double a4 = 0.5854101966249685, b4 = 0.1381966011250150;
+    const double pts[4][3] = {{a4, b4, b4}, {b4, a4, b4}, {b4, b4, a4}, {b4, b4, b4}};
+    for (int q = 0; q < 4; ++q) {
+        t[2].qwt[q] = kTetQwt;
+        for (int a = 0; a < 3; ++a) t[2].shp[q][a] = pts[q][a];
+        t[2].shp[q][3] = 1.0 - pts[q][0] - pts[q][1] - pts[q][2];
+        for (int i = 0; i < 3; ++i) {
+            for (int a = 0; a < 3; ++a) t[2].shgl[q][i][a] = (i == a) ? 0.5 : 0.0;
+            t[2].shgl[q][i][3] = -0.5;
+        }
+    }
+}
+
+void upload_topo_tables(Ctx& C) {
+    TopoTabD t[3];
+    topo_tables_host(t);
     static TopoTabD td[2];
     static TopoTabF tf[2];
     for (int k = 0; k < 2; ++k) {

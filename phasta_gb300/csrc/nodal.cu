@@ -459,6 +459,17 @@ void bc3res(Ctx& C, R* r) {
 template void bc3res<double>(Ctx&, double*);
 template void bc3res<float>(Ctx&, float*);
 
+// bc3per (bc3per.f:1-20): the periodic part of bc3Res alone
+template <typename R>
+void bc3per(Ctx& C, R* r) {
+    if (C.nmaster > 0) {
+        k_periodic_sum<R, 5><<<nblocks(C.nmaster), kT, 0, C.stream>>>(C.d_mst, C.d_slv_start, C.d_slv, C.nmaster, r, 0);
+        ++C.launches;
+    }
+}
+template void bc3per<double>(Ctx&, double*);
+template void bc3per<float>(Ctx&, float*);
+
 template <typename R>
 void bc3bdg(Ctx& C, const double* y, R* bd) {
     if (C.nbcn > 0) {

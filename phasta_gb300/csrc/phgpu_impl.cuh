@@ -42,6 +42,39 @@ struct TetTables {
     double Qwtb[3];
 };
 
+// quadrature and shape tables of one element topology (linear basis, up to 8 points/nodes)
+struct TopoTabD {
+    double shp[8][8];      // [q][a]
+    double shgl[8][3][8];  // [q][i][a] parent-coordinate derivatives
+    double qwt[8];
+};
+struct TopoTabF {
+    float shp[8][8];
+    float shgl[8][3][8];
+    float qwt[8];
+};
+// t[0] hex (lcsyst 2), t[1] wedge (lcsyst 3), t[2] tet (lcsyst 1)
+void topo_tables_host(TopoTabD* t);
+
+// block-sparse tangent of the sparse solver (lhs = 1), built on the first call that needs it
+struct SparseCtx {
+    bool ready = false;
+    int nnzb = 0;                 // nnz_tot: 5x5 blocks
+    std::vector<int> colm, rowp;  // the reference's genadj arrays (1-based)
+    int* d_rs = nullptr;          // N+1 row starts (0-based)
+    int* d_bcol = nullptr;        // nnzb column node
+    int* d_bcolp = nullptr;       // nnzb iper(column node): SparseAp's periodic gather
+    int* d_brow = nullptr;        // nnzb row node
+    int* d_ient = nullptr;        // tets in tangent colour order (4 per element)
+    std::vector<int> tcol_start;  // tet colours of the tangent
+    int* d_tmap = nullptr;        // block index of (element, a, b): 16 per tet
+    int* d_hmap = nullptr;        // 64 per hex (d_ienh order)
+    int* d_wmap = nullptr;        // 36 per wedge (d_ienw order)
+    double* d_lhsK = nullptr;     // 25 * nnzb, the reference's lhsK(25, nnz_tot) layout
+    float* d_lhsKf = nullptr;     // FP32 tangent of the mixed-precision solve
+    int have = -1;                // precision of the preconditioned tangent kept from the last lhs = 1 solve
+};
+
 struct Ctx {
     int N = 0, E = 0, Eb = 0;
     phgpu_config cfg{};
@@ -72,6 +105,10 @@ struct Ctx {
     int* d_iBCB = nullptr;        // Eb
     double* d_BCB = nullptr;      // Eb*18  [e][n][6]
     std::vector<int> perm_e;      // colour-sorted position -> input element id
+    // host connectivity for the sparse solver's adjacency: tets in input order,
+    // hexes and wedges in the colour order of d_ienh / d_ienw
+    std::vector<int> h_ien, h_ienh, h_ienw;
+    SparseCtx sp;
 
     double* d_x = nullptr;        // N*3
     float* d_xf = nullptr;        // N*3
@@ -158,6 +195,7 @@ int configure_element_kernels(Ctx& C);
 
 // ---- nodal kernels (nodal.cu) ----
 template <typename R> void bc3res(Ctx& C, R* r);
+template <typename R> void bc3per(Ctx& C, R* r);
 template <typename R> void bc3bdg(Ctx& C, const double* y, R* bd);
 template <typename R> void itrbc_pert(Ctx& C, R* v, bool zero_dirichlet);
 void itrbc_state(Ctx& C, double* y, double* ac, bool with_ac);
@@ -182,6 +220,21 @@ template <typename V>
 void mgs_step(Ctx& C, V* w, const V* uprev, const double* beta_prev, const V* uj, size_t n,
               double* beta_out, const int* skip);
 template <typename V> void scale_by(Ctx& C, V* w, const double* s, int mode, size_t n, const int* skip);
+
+// ---- sparse solver (sparse.cu, tangent.cu) ----
+// genadj.f: the unique neighbours of every node over all element blocks, ascending (1-based)
+void block_adjacency(int N, const int* ien, int ne, const int* ienh, int nh, const int* ienw, int nw,
+                     std::vector<int>& colm, std::vector<int>& rowp);
+int sparse_setup(Ctx& C);
+template <typename R> void launch_tangent(Ctx& C, const R* x, const R* y, R* lhsK);
+void upload_tangent_tables(Ctx& C);
+int configure_tangent_kernels(Ctx& C);
+// Spsi3pre: lhsK <- L_i^-1 lhsK U_j^-1 with the i3LU factors bd (device layouts)
+template <typename R> void spsi3pre(Ctx& C, const R* bd, R* lhsK);
+// SparseAp + bc3per: q = lhsK p(iper), slaves summed into masters
+template <typename M, typename V> void sparse_ap(Ctx& C, const M* lhsK, const V* p, V* q);
+// greedy first-fit element colouring (solver.cu)
+int colour(Ctx& C, int n_nodes, const int* ien, int nen, int ne, std::vector<int>& order, std::vector<int>& start);
 
 int check(Ctx& C, cudaError_t e, const char* what);
 

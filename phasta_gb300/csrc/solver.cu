@@ -51,6 +51,8 @@ int sync(Ctx& C) {
     return check(C, cudaStreamSynchronize(C.stream), "stream synchronize");
 }
 
+}  // namespace
+
 // greedy first-fit colouring: no two elements of a colour share a node
 int colour(Ctx& C, int n_nodes, const int* ien, int nen, int ne, std::vector<int>& order, std::vector<int>& start) {
     std::vector<uint64_t> m0(n_nodes, 0), m1(n_nodes, 0);
@@ -82,6 +84,8 @@ int colour(Ctx& C, int n_nodes, const int* ien, int nen, int ne, std::vector<int
     for (int e = 0; e < ne; ++e) order[pos[col[e]]++] = e;
     return PHGPU_OK;
 }
+
+namespace {
 
 // ------------------------------------------------------------------------
 // small device kernels of the driver
@@ -134,6 +138,7 @@ __global__ void k_givens(double* __restrict__ s, int K, int iKs, int minIters, i
     double* Rs = s + S_RS;
     const double unorm = sqrt(H(iKs + 1, iKs));
     H(iKs + 1, iKs) = unorm;
+    s[S_TMP2] = unorm;  // the last norm of the cycle (a sparse-solver restart without a new residual)
     for (int jK = 1; jK <= iKs - 1; ++jK) {
         const double t = Rc[jK - 1] * H(jK, iKs) + Rs[jK - 1] * H(jK + 1, iKs);
         H(jK + 1, iKs) = -Rs[jK - 1] * H(jK, iKs) + Rc[jK - 1] * H(jK + 1, iKs);
@@ -401,9 +406,16 @@ int itrfdi_dev(Ctx& C, const double* rmes, const double* ubrg) {
     return PHGPU_OK;
 }
 
-// GMRES cycles on V-typed Krylov vectors; b (= L^-1 R, FP64) in d_res, output Dy (FP64, before U^-1)
+template <typename V> V* sparse_lhs(Ctx& C);
+template <> double* sparse_lhs<double>(Ctx& C) { return C.sp.d_lhsK; }
+template <> float* sparse_lhs<float>(Ctx& C) { return C.sp.d_lhsKf; }
+
+// GMRES cycles on V-typed Krylov vectors; b (= L^-1 R, FP64) in d_res, output Dy (FP64, before U^-1).
+// ap_mode PHGPU_AP_SPARSE: the product is SparseAp + bc3per on the preconditioned tangent, and a
+// new cycle recomputes R - A Dy only when lgmres_common > 0 (SolGMRs, solgmr.f:526-537)
 template <typename V>
-int gmres(Ctx& C, phgpu_stats* st) {
+int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
+    const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE;
     const size_t n5 = 5 * (size_t)C.N;
     const int K = C.cfg.Kspace;
     V* U = (V*)C.d_U;
@@ -434,7 +446,29 @@ int gmres(Ctx& C, phgpu_stats* st) {
     int iKs = 0;
     for (int mG = 1; mG <= C.cfg.nGMRES; ++mG) {
         st->lGMRES = mG - 1;
-        if (mG > 1) {
+        if (mG > 1 && sparse && lgmres_common <= 0) {
+            // SolGMRs tests the COMMON lGMRES, which it never sets (solgmr.f:528): the cycle
+            // starts again from its first vector, scaled by the last norm of the previous cycle
+            unorm = C.h_scal[S_TMP2];
+        } else if (mG > 1 && sparse) {
+            V* t = Uj(1);
+            if constexpr (std::is_same<V, double>::value) {
+                sparse_ap<double, double>(C, C.sp.d_lhsK, C.d_Dy, t);
+                k_axpby<<<kVG, kVT, 0, C.stream>>>(C.d_res, 1.0, t, -1.0, t, n5);
+                ++C.launches;
+            } else {
+                to_f32(C, C.d_Dy, C.d_t32b, n5);
+                sparse_ap<float, float>(C, C.sp.d_lhsKf, C.d_t32b, C.d_t32);
+                to_f64(C, C.d_t32, C.d_t64b, n5);
+                k_axpby<<<kVG, kVT, 0, C.stream>>>(C.d_res, 1.0, C.d_t64b, -1.0, C.d_t64b, n5);
+                ++C.launches;
+                to_f32(C, C.d_t64b, t, n5);
+            }
+            dot<V>(C, t, t, n5, S_TMP0, nullptr);
+            PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "unorm"));
+            PH_TRY(sync(C));
+            unorm = std::sqrt(C.h_scal[S_TMP0]);
+        } else if (mG > 1) {
             // restart: uBrg(1) = R - A Dy, by Au2MFG's central difference when the
             // product is finite-differenced, else with the linearized product
             V* t = Uj(1);
@@ -468,13 +502,17 @@ int gmres(Ctx& C, phgpu_stats* st) {
         for (int iK = 1; iK <= K; ++iK) {
             iKs = iK;
             V* w = Uj(iKs + 1);
-            k_copy<V><<<kVG, kVT, 0, C.stream>>>(Uj(iKs), w, n5, nullptr);
-            ++C.launches;
-            if constexpr (std::is_same<V, double>::value) {
-                if (C.cfg.ap_mode == PHGPU_AP_FD) PH_TRY(ap_fd64(C, w, C.d_rmes, nullptr));
-                else PH_TRY(ap_lin<V>(C, w, nullptr));
+            if (sparse) {
+                sparse_ap<V, V>(C, sparse_lhs<V>(C), Uj(iKs), w);
             } else {
-                PH_TRY(ap_lin<V>(C, w, nullptr));
+                k_copy<V><<<kVG, kVT, 0, C.stream>>>(Uj(iKs), w, n5, nullptr);
+                ++C.launches;
+                if constexpr (std::is_same<V, double>::value) {
+                    if (C.cfg.ap_mode == PHGPU_AP_FD) PH_TRY(ap_fd64(C, w, C.d_rmes, nullptr));
+                    else PH_TRY(ap_lin<V>(C, w, nullptr));
+                } else {
+                    PH_TRY(ap_lin<V>(C, w, nullptr));
+                }
             }
             // modified Gram-Schmidt (solmfg.f:247-267)
             double* Hcol = s + S_H + (size_t)(K + 1) * (iKs - 1);
@@ -505,14 +543,29 @@ int gmres(Ctx& C, phgpu_stats* st) {
     return PHGPU_OK;
 }
 
-int solmfg_dev(Ctx& C, phgpu_stats* st) {
+// SolMFG (solmfg.f) or, with ap_mode PHGPU_AP_SPARSE, SolGMRs (solgmr.f:480): lhs = 1 forms
+// BDiag and the tangent (iprec = lhs, itrdrv.f:456-457); lhs = 0 reuses the factored BDiag
+// and the preconditioned tangent of the last lhs = 1 solve
+int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
     const size_t N = C.N, n5 = 5 * N;
+    const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE;
+    if (sparse) {
+        PH_TRY(sparse_setup(C));
+        if (!lhs && C.sp.have != C.cfg.precision)
+            return fail(C, PHGPU_ERR_INVALID, "lhs = 0 needs the tangent of an earlier lhs = 1 solve");
+    }
+    const bool asm_bd = !sparse || lhs;
     cudaEventRecord(C.ev[0], C.stream);
     if (C.cfg.precision == PHGPU_FP64) {
-        PH_TRY(elmmfg64(C, C.d_y, C.d_ac, C.d_res, C.d_rmes, C.d_bd, 1));
+        if (asm_bd) PH_TRY(elmmfg64(C, C.d_y, C.d_ac, C.d_res, C.d_rmes, C.d_bd, 1));
+        else PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
+        if (sparse && lhs) {
+            fill0(C, C.sp.d_lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb);
+            launch_tangent<double>(C, C.d_x, C.d_y, C.sp.d_lhsK);
+        }
     } else {
-        if (C.cfg.ap_mode != PHGPU_AP_LINEAR)
-            return fail(C, PHGPU_ERR_UNSUPPORTED, "mixed precision needs the linearized Jacobian-vector product");
+        if (C.cfg.ap_mode == PHGPU_AP_FD)
+            return fail(C, PHGPU_ERR_UNSUPPORTED, "mixed precision needs the linearized or the assembled product");
         // outer residual (FP64, or FP64 Galerkin + FP32 stabilization); FP32 block-diagonal tangent
         if (C.cfg.outer_residual == PHGPU_RES_SPLITDF) split_f32(C, C.d_y, C.d_yf, C.d_ylo, n5);
         else to_f32(C, C.d_y, C.d_yf, n5);
@@ -533,22 +586,38 @@ int solmfg_dev(Ctx& C, phgpu_stats* st) {
         } else {
             PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
         }
-        fill0(C, C.d_bdf, sizeof(float) * 25 * N);
-        launch_elem_full<float>(C, C.d_xf, C.d_yf, C.d_acf, nullptr, nullptr, C.d_bdf);
-        bc3bdg<float>(C, C.d_y, C.d_bdf);
-        to_f64(C, C.d_bdf, C.d_bd, 25 * N);
+        if (asm_bd) {
+            fill0(C, C.d_bdf, sizeof(float) * 25 * N);
+            launch_elem_full<float>(C, C.d_xf, C.d_yf, C.d_acf, nullptr, nullptr, C.d_bdf);
+            bc3bdg<float>(C, C.d_y, C.d_bdf);
+            to_f64(C, C.d_bdf, C.d_bd, 25 * N);
+        }
+        if (sparse && lhs) {
+            fill0(C, C.sp.d_lhsKf, sizeof(float) * 25 * (size_t)C.sp.nnzb);
+            launch_tangent<float>(C, C.d_xf, C.d_yf, C.sp.d_lhsKf);
+        }
     }
     // nonlinear residual ||R|| (FP64, unpreconditioned)
     dot<double>(C, C.d_res, C.d_res, n5, S_TMP3, nullptr);
     fill0(C, C.d_flag, sizeof(int) * 2);
-    lu_fact<double>(C, C.d_bd, C.d_flag);
-    if (C.cfg.precision == PHGPU_MIXED) to_f32(C, C.d_bd, C.d_bdf, 25 * N);
+    if (asm_bd) {
+        lu_fact<double>(C, C.d_bd, C.d_flag);
+        if (C.cfg.precision == PHGPU_MIXED) to_f32(C, C.d_bd, C.d_bdf, 25 * N);
+    }
     lu_apply<double, double>(C, C.d_bd, C.d_res, PHGPU_LU_FORWARD);
-    if (C.cfg.precision == PHGPU_FP64) lu_apply<double, double>(C, C.d_bd, C.d_rmes, PHGPU_LU_FORWARD);
-    // ypre = U . y (local order is already the "old" order)
-    k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_y, C.d_ypre, n5, nullptr);
-    ++C.launches;
-    lu_apply<double, double>(C, C.d_bd, C.d_ypre, PHGPU_LU_PRODUCT);
+    if (sparse) {
+        if (lhs) {
+            if (C.cfg.precision == PHGPU_FP64) spsi3pre<double>(C, C.d_bd, C.sp.d_lhsK);
+            else spsi3pre<float>(C, C.d_bdf, C.sp.d_lhsKf);
+            C.sp.have = C.cfg.precision;
+        }
+    } else {
+        if (C.cfg.precision == PHGPU_FP64) lu_apply<double, double>(C, C.d_bd, C.d_rmes, PHGPU_LU_FORWARD);
+        // ypre = U . y (local order is already the "old" order)
+        k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_y, C.d_ypre, n5, nullptr);
+        ++C.launches;
+        lu_apply<double, double>(C, C.d_bd, C.d_ypre, PHGPU_LU_PRODUCT);
+    }
     PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
     PH_TRY(check(C, cudaMemcpyAsync(C.h_scal + 8, C.d_scal + S_TMP3, sizeof(double), cudaMemcpyDeviceToHost, C.stream), "rn"));
     PH_TRY(sync(C));
@@ -556,8 +625,8 @@ int solmfg_dev(Ctx& C, phgpu_stats* st) {
     if (C.h_flag[1]) return fail(C, PHGPU_ERR_SINGULAR, "zero or non-finite pivot in the block-diagonal LU");
     cudaEventRecord(C.ev[1], C.stream);
     int rc;
-    if (C.cfg.precision == PHGPU_FP64) rc = gmres<double>(C, st);
-    else rc = gmres<float>(C, st);
+    if (C.cfg.precision == PHGPU_FP64) rc = gmres<double>(C, st, lgmres_common);
+    else rc = gmres<float>(C, st, lgmres_common);
     if (rc != PHGPU_OK) return rc;
     lu_apply<double, double>(C, C.d_bd, C.d_Dy, PHGPU_LU_BACKWARD);
     cudaEventRecord(C.ev[2], C.stream);
@@ -570,6 +639,8 @@ int solmfg_dev(Ctx& C, phgpu_stats* st) {
     st->status = PHGPU_OK;
     return PHGPU_OK;
 }
+
+int solmfg_dev(Ctx& C, phgpu_stats* st) { return solve_dev(C, st, 1, 0); }
 
 int correct_dev(Ctx& C) {
     const size_t n5 = 5 * (size_t)C.N;
@@ -655,6 +726,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
         if (p < 0 || p >= N) { delete h; return PHGPU_ERR_INVALID; }
         if (p != n && m->iper[p] != p) { delete h; return PHGPU_ERR_UNSUPPORTED; }  // chains
         if (((m->iBC[n] >> 10) & 1) != (p != n ? 1 : 0)) { delete h; return PHGPU_ERR_INVALID; }
+        if ((m->iBC[n] >> 11) & 1) { delete h; return PHGPU_ERR_UNSUPPORTED; }  // scaled-plane extraction (irscale)
     }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { delete h; return PHGPU_ERR_CUDA; }
@@ -670,6 +742,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     if (C.nwedge > 0) T(colour(C, N, m->ienw, 6, C.nwedge, worder, C.wcol_start));
     if (rc != PHGPU_OK) { phgpu_destroy(h); return rc; }
     if (C.E > 0) T(build_chunks(C, m->ien, m->x));
+    C.h_ien.assign(m->ien, m->ien + 4 * (size_t)C.E);
     if (rc == PHGPU_OK) T(configure_element_kernels(C));
     if (rc != PHGPU_OK) { phgpu_destroy(h); return rc; }
     std::vector<int4> ienb(std::max(C.Eb, 1));
@@ -770,12 +843,14 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
         for (int i = 0; i < C.nhex; ++i)
             for (int a = 0; a < 8; ++a) v[8 * (size_t)i + a] = m->ienh[8 * (size_t)horder[i] + a];
         up(C.d_ienh, v.data(), sizeof(int) * v.size());
+        C.h_ienh = v;
     }
     if (C.nwedge > 0) {
         std::vector<int> v(6 * (size_t)C.nwedge);
         for (int i = 0; i < C.nwedge; ++i)
             for (int a = 0; a < 6; ++a) v[6 * (size_t)i + a] = m->ienw[6 * (size_t)worder[i] + a];
         up(C.d_ienw, v.data(), sizeof(int) * v.size());
+        C.h_ienw = v;
     }
     up(C.d_iBCB, ibcb.data(), sizeof(int) * ibcb.size());
     up(C.d_BCB, bcb.data(), sizeof(double) * bcb.size());
@@ -813,7 +888,9 @@ int phgpu_destroy(phgpu_ctx* h) {
                     C.d_bdstage, C.d_ien, C.d_ienh, C.d_ienw, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_xlo, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
                     C.d_slaves, C.d_mst, C.d_slv_start, C.d_slv, C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_res,
                     C.d_rmes, C.d_Dy, C.d_ypre, C.d_t64, C.d_t64b, C.d_bd, C.d_yf, C.d_ylo, C.d_acf, C.d_resf, C.d_rmesf,
-                    C.d_t32, C.d_t32b, C.d_bdf, C.d_qres, C.d_qresf, C.d_U, C.d_scal, C.d_part, C.d_count, C.d_flag};
+                    C.d_t32, C.d_t32b, C.d_bdf, C.d_qres, C.d_qresf, C.d_U, C.d_scal, C.d_part, C.d_count, C.d_flag,
+                    C.sp.d_rs, C.sp.d_bcol, C.sp.d_bcolp, C.sp.d_brow, C.sp.d_ient, C.sp.d_tmap, C.sp.d_hmap,
+                    C.sp.d_wmap, C.sp.d_lhsK, C.sp.d_lhsKf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (C.h_scal) cudaFreeHost(C.h_scal);
@@ -960,6 +1037,112 @@ int phgpu_solmfg(phgpu_ctx* h, const double* y, const double* ac, double* res, d
         return sync(C);
     }
     return PHGPU_OK;
+}
+
+int phgpu_genadj(const phgpu_mesh* m, int nnz, int* colm, int* rowp, int* icnt) {
+    using namespace phgpu;
+    if (!m || !colm || !rowp || !icnt || nnz <= 0 || m->nshg <= 0 || m->nelem < 0 || m->nhex < 0 || m->nwedge < 0)
+        return PHGPU_ERR_INVALID;
+    if ((m->nelem > 0 && !m->ien) || (m->nhex > 0 && !m->ienh) || (m->nwedge > 0 && !m->ienw)) return PHGPU_ERR_INVALID;
+    const int N = m->nshg;
+    const int* blk[3] = {m->ien, m->ienh, m->ienw};
+    const size_t len[3] = {4 * (size_t)m->nelem, 8 * (size_t)m->nhex, 6 * (size_t)m->nwedge};
+    for (int b = 0; b < 3; ++b)
+        for (size_t i = 0; i < len[b]; ++i)
+            if (blk[b][i] < 0 || blk[b][i] >= N) return PHGPU_ERR_INVALID;
+    std::vector<int> cm, rp;
+    block_adjacency(N, m->ien, m->nelem, m->ienh, m->nhex, m->ienw, m->nwedge, cm, rp);
+    for (int n = 0; n < N; ++n)
+        if (cm[n + 1] - cm[n] > 15 * nnz) return PHGPU_ERR_TOO_LARGE;  // genadj.f: "increase overflow factor"
+    if (rp.size() > (size_t)nnz * N) return PHGPU_ERR_TOO_LARGE;        // genadj.f: "increase nnz"
+    std::copy(cm.begin(), cm.end(), colm);
+    std::copy(rp.begin(), rp.end(), rowp);
+    *icnt = (int)rp.size();
+    return PHGPU_OK;
+}
+
+int phgpu_nnz_tot(phgpu_ctx* h, int* nnz_tot) {
+    using namespace phgpu;
+    if (!h || !nnz_tot) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    PH_TRY(sparse_setup(C));
+    *nnz_tot = C.sp.nnzb;
+    return PHGPU_OK;
+}
+
+int phgpu_elmgmrs(phgpu_ctx* h, const double* y, const double* ac, double* res, double* bdiag, double* lhsK) {
+    using namespace phgpu;
+    if (!h || !y || !ac || !res || !bdiag || !lhsK) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    PH_TRY(sparse_setup(C));
+    C.sp.have = -1;
+    ref_to_dev_state(C, y, C.d_t64, C.d_y);
+    ref_to_dev_state(C, ac, C.d_t64b, C.d_ac);
+    PH_TRY(elmmfg64(C, C.d_y, C.d_ac, C.d_res, C.d_rmes, C.d_bd, 1));
+    fill0(C, C.sp.d_lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb);
+    launch_tangent<double>(C, C.d_x, C.d_y, C.sp.d_lhsK);
+    dev_to_ref_res(C, C.d_res, C.d_t64, res);
+    dev_to_ref_bd(C, C.d_bd, C.d_bdstage, bdiag);
+    PH_TRY(check(C, cudaMemcpyAsync(lhsK, C.sp.d_lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb,
+                                    cudaMemcpyDeviceToHost, C.stream), "download lhsK"));
+    return sync(C);
+}
+
+int phgpu_spsi3pre(phgpu_ctx* h, const double* bdiag, double* lhsK) {
+    using namespace phgpu;
+    if (!h || !bdiag || !lhsK) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    PH_TRY(sparse_setup(C));
+    C.sp.have = -1;
+    const size_t nb = 25 * (size_t)C.sp.nnzb;
+    ref_to_dev_bd(C, bdiag, C.d_bdstage, C.d_bd);
+    PH_TRY(check(C, cudaMemcpyAsync(C.sp.d_lhsK, lhsK, sizeof(double) * nb, cudaMemcpyHostToDevice, C.stream), "upload lhsK"));
+    spsi3pre<double>(C, C.d_bd, C.sp.d_lhsK);
+    PH_TRY(check(C, cudaMemcpyAsync(lhsK, C.sp.d_lhsK, sizeof(double) * nb, cudaMemcpyDeviceToHost, C.stream), "download lhsK"));
+    return sync(C);
+}
+
+int phgpu_sparseap(phgpu_ctx* h, const double* lhsK, double* p) {
+    using namespace phgpu;
+    if (!h || !lhsK || !p) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    PH_TRY(sparse_setup(C));
+    C.sp.have = -1;
+    const size_t nb = 25 * (size_t)C.sp.nnzb;
+    PH_TRY(check(C, cudaMemcpyAsync(C.sp.d_lhsK, lhsK, sizeof(double) * nb, cudaMemcpyHostToDevice, C.stream), "upload lhsK"));
+    ref_to_dev_res(C, p, C.d_t64, C.d_t64b);
+    sparse_ap<double, double>(C, C.sp.d_lhsK, C.d_t64b, C.d_Dy);
+    dev_to_ref_res(C, C.d_Dy, C.d_t64, p);
+    return sync(C);
+}
+
+int phgpu_solgmrs(phgpu_ctx* h, const double* y, const double* ac, int lhs, double* res, double* bdiag, double* Dy,
+                  double* lhsK, phgpu_stats* st) {
+    using namespace phgpu;
+    if (!h || !y || !ac || !st || (lhs != 0 && lhs != 1)) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    ref_to_dev_state(C, y, C.d_t64, C.d_y);
+    ref_to_dev_state(C, ac, C.d_t64b, C.d_ac);
+    PH_TRY(sync(C));
+    const int ntot = st->ntotGM, lg = st->lGMRES;
+    *st = phgpu_stats{};
+    st->ntotGM = ntot;
+    const int ap = C.cfg.ap_mode;
+    C.cfg.ap_mode = PHGPU_AP_SPARSE;
+    const int rc = solve_dev(C, st, lhs, lg);
+    C.cfg.ap_mode = ap;
+    PH_TRY(rc);
+    if (res) dev_to_ref_res(C, C.d_res, C.d_t64, res);
+    if (Dy) dev_to_ref_res(C, C.d_Dy, C.d_t64b, Dy);
+    if (bdiag) dev_to_ref_bd(C, C.d_bd, C.d_bdstage, bdiag);
+    if (lhsK && C.cfg.precision == PHGPU_FP64)
+        PH_TRY(check(C, cudaMemcpyAsync(lhsK, C.sp.d_lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb,
+                                        cudaMemcpyDeviceToHost, C.stream), "download lhsK"));
+    return sync(C);
 }
 
 int phgpu_itrcorrect(phgpu_ctx* h, double* y, double* ac, const double* yold, const double* acold, const double* Dy) {

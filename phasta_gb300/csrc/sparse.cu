@@ -1,0 +1,249 @@
+// sparse.cu -- the block-sparse side of the sparse solver (impl = 1x, lhs = 1):
+//   * the node adjacency of genadj.f/asadj.f (host; rows sorted ascending),
+//   * per-element block maps replacing fillsparseC's sparseloc search
+//     (fillsparse.f) by one host-side search at set-up,
+//   * Spsi3pre (spsi3pre.f): lhsK(i,j) <- L_i^-1 lhsK(i,j) U_j^-1,
+//   * SparseAp (sparseap.f) with the periodic gather and bc3per (bc3per.f).
+//
+// lhsK lives in the reference's layout, lhsK(25, nnz_tot) column-major: block
+// k is 25 contiguous values with entry (f, g) at 5 g + f, blocks of a row are
+// contiguous and ordered by column node.  The product streams each row's
+// 25 * nnz_row values with one warp (coalesced), gathers p through the
+// iper-mapped column list and reduces the five row sums across the warp.
+#include <algorithm>
+
+#include "phgpu_impl.cuh"
+
+namespace phgpu {
+
+void block_adjacency(int N, const int* ien, int ne, const int* ienh, int nh, const int* ienw, int nw,
+                     std::vector<int>& colm, std::vector<int>& rowp) {
+    // node -> incident elements (all blocks), then each row = sorted unique nodes of those elements
+    struct Blk { const int* ien; int nen, ne; };
+    const Blk blks[3] = {{ien, 4, ne}, {ienh, 8, nh}, {ienw, 6, nw}};
+    std::vector<int> deg(N + 1, 0);
+    for (const Blk& b : blks)
+        for (size_t i = 0; i < (size_t)b.nen * b.ne; ++i) deg[b.ien[i] + 1]++;
+    for (int n = 0; n < N; ++n) deg[n + 1] += deg[n];
+    std::vector<long long> inc(deg[N]);  // (block << 40) | element
+    std::vector<int> fillp(deg.begin(), deg.end() - 1);
+    for (int bi = 0; bi < 3; ++bi) {
+        const Blk& b = blks[bi];
+        for (int e = 0; e < b.ne; ++e)
+            for (int a = 0; a < b.nen; ++a) inc[fillp[b.ien[(size_t)b.nen * e + a]]++] = ((long long)bi << 40) | e;
+    }
+    colm.assign(N + 1, 1);
+    rowp.clear();
+    std::vector<int> row;
+    for (int n = 0; n < N; ++n) {
+        row.clear();
+        for (int t = deg[n]; t < deg[n + 1]; ++t) {
+            const Blk& b = blks[inc[t] >> 40];
+            const int e = (int)(inc[t] & ((1ll << 40) - 1));
+            for (int a = 0; a < b.nen; ++a) row.push_back(b.ien[(size_t)b.nen * e + a]);
+        }
+        std::sort(row.begin(), row.end());
+        row.erase(std::unique(row.begin(), row.end()), row.end());
+        for (int v : row) rowp.push_back(v + 1);
+        colm[n + 1] = colm[n] + (int)row.size();
+    }
+}
+
+namespace {
+
+template <typename T>
+int dcopy(Ctx& C, T** d, const T* h, size_t n) {
+    if (cudaMalloc((void**)d, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) {
+        C.err = "cudaMalloc (sparse tangent)";
+        return PHGPU_ERR_NOMEM;
+    }
+    if (n == 0) return PHGPU_OK;
+    return check(C, cudaMemcpy(*d, h, sizeof(T) * n, cudaMemcpyHostToDevice), "upload sparse structure");
+}
+
+// block index of (element, a, b) for every element of a block (element-major, a-major)
+void block_map(const std::vector<int>& colm, const std::vector<int>& rowp, const int* ien, int nen, int ne,
+               std::vector<int>& map) {
+    map.resize((size_t)nen * nen * ne);
+    for (int e = 0; e < ne; ++e)
+        for (int a = 0; a < nen; ++a) {
+            const int i = ien[(size_t)nen * e + a];
+            const int* r0 = rowp.data() + (colm[i] - 1);
+            const int* r1 = rowp.data() + (colm[i + 1] - 1);
+            for (int b = 0; b < nen; ++b) {
+                const int* f = std::lower_bound(r0, r1, ien[(size_t)nen * e + b] + 1);
+                map[((size_t)e * nen + a) * nen + b] = (int)(f - rowp.data());
+            }
+        }
+}
+
+// ---- Spsi3pre: one thread per block ----
+template <typename R>
+__global__ void k_spsi3pre(const int* __restrict__ brow, const int* __restrict__ bcol, const R* __restrict__ bd,
+                           R* __restrict__ A, int nnzb) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnzb) return;
+    const R* Li = bd + 25 * (size_t)brow[k];  // row-major: Li[5 r + c] = BDiag(i, r, c)
+    const R* Uj = bd + 25 * (size_t)bcol[k];
+    R* a = A + 25 * (size_t)k;                // a[5 g + f] = entry (f, g)
+    R m[5][5];
+#pragma unroll
+    for (int g = 0; g < 5; ++g)
+#pragma unroll
+        for (int f = 0; f < 5; ++f) m[f][g] = a[5 * g + f];
+    // forward substitution with the unit lower factor of row node i, column by column
+#pragma unroll
+    for (int r = 1; r < 5; ++r)
+#pragma unroll
+        for (int g = 0; g < 5; ++g) {
+            R v = m[r][g];
+#pragma unroll
+            for (int c = 0; c < r; ++c) v = v - Li[5 * r + c] * m[c][g];
+            m[r][g] = v;
+        }
+    // right solve with the upper factor of column node j (reciprocal pivots on its diagonal)
+#pragma unroll
+    for (int g = 0; g < 5; ++g)
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            R v = m[f][g];
+#pragma unroll
+            for (int c = 0; c < g; ++c) v = v - Uj[5 * c + g] * m[f][c];
+            m[f][g] = Uj[5 * g + g] * v;
+        }
+#pragma unroll
+    for (int g = 0; g < 5; ++g)
+#pragma unroll
+        for (int f = 0; f < 5; ++f) a[5 * g + f] = m[f][g];
+}
+
+// ---- SparseAp: one warp per block row ----
+constexpr int kSpThreads = 256;
+
+template <typename M, typename V>
+__global__ void __launch_bounds__(kSpThreads)
+k_bsr_spmv(const int* __restrict__ rs, const int* __restrict__ bcolp, const M* __restrict__ A,
+           const V* __restrict__ p, V* __restrict__ q, int N) {
+    const int lane = threadIdx.x & 31;
+    const int row = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (row >= N) return;
+    const int k0 = rs[row], k1 = rs[row + 1];
+    const int nv = 25 * (k1 - k0);
+    const M* a = A + 25 * (size_t)k0;
+    V acc[5] = {V(0), V(0), V(0), V(0), V(0)};
+    // value index v = 25 kb + 5 g + f; lanes stride by 32 = 25 + 7
+    int kb = lane / 25, e = lane - 25 * (lane / 25);
+    for (int v = lane; v < nv; v += 32) {
+        const int g = e / 5, f = e - 5 * g;
+        const V t = (V)a[v] * p[5 * (size_t)bcolp[k0 + kb] + g];
+#pragma unroll
+        for (int r = 0; r < 5; ++r) acc[r] += (r == f) ? t : V(0);
+        e += 7;
+        kb += 1;
+        if (e >= 25) {
+            e -= 25;
+            kb += 1;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+    if (lane < 5) {
+        V out = acc[0];
+#pragma unroll
+        for (int r = 1; r < 5; ++r) out = (lane == r) ? acc[r] : out;
+        q[5 * (size_t)row + lane] = out;
+    }
+}
+
+}  // namespace
+
+// the FP32 tangent is allocated the first time a mixed-precision solve needs it
+static int ensure_f32(Ctx& C) {
+    SparseCtx& S = C.sp;
+    if (C.cfg.precision != PHGPU_MIXED || S.d_lhsKf) return PHGPU_OK;
+    if (cudaMalloc((void**)&S.d_lhsKf, sizeof(float) * 25 * (size_t)std::max(S.nnzb, 1)) != cudaSuccess) {
+        C.err = "cudaMalloc (FP32 sparse tangent)";
+        return PHGPU_ERR_NOMEM;
+    }
+    return PHGPU_OK;
+}
+
+int sparse_setup(Ctx& C) {
+    SparseCtx& S = C.sp;
+    if (S.ready) return ensure_f32(C);
+    const int N = C.N;
+    block_adjacency(N, C.h_ien.data(), C.E, C.h_ienh.data(), C.nhex, C.h_ienw.data(), C.nwedge, S.colm, S.rowp);
+    S.nnzb = (int)S.rowp.size();
+    std::vector<int> rs(N + 1), bcol(S.nnzb), bcolp(S.nnzb), brow(S.nnzb);
+    std::vector<int> iper(N);
+    {
+        const int rci = check(C, cudaMemcpy(iper.data(), C.d_iper, sizeof(int) * N, cudaMemcpyDeviceToHost), "download iper");
+        if (rci != PHGPU_OK) return rci;
+    }
+    for (int n = 0; n <= N; ++n) rs[n] = S.colm[n] - 1;
+    for (int n = 0; n < N; ++n)
+        for (int k = rs[n]; k < rs[n + 1]; ++k) {
+            brow[k] = n;
+            bcol[k] = S.rowp[k] - 1;
+            bcolp[k] = iper[bcol[k]];
+        }
+    // tets: their own colouring (the chunk order of the residual kernels groups elements that share nodes)
+    std::vector<int> torder, tien(4 * (size_t)C.E), tmap, hmap, wmap;
+    if (C.E > 0) {
+        const int rcc = colour(C, N, C.h_ien.data(), 4, C.E, torder, S.tcol_start);
+        if (rcc != PHGPU_OK) return rcc;
+        for (int i = 0; i < C.E; ++i)
+            for (int a = 0; a < 4; ++a) tien[4 * (size_t)i + a] = C.h_ien[4 * (size_t)torder[i] + a];
+        block_map(S.colm, S.rowp, tien.data(), 4, C.E, tmap);
+    }
+    if (C.nhex > 0) block_map(S.colm, S.rowp, C.h_ienh.data(), 8, C.nhex, hmap);
+    if (C.nwedge > 0) block_map(S.colm, S.rowp, C.h_ienw.data(), 6, C.nwedge, wmap);
+    int rc = PHGPU_OK;
+    auto T = [&](int s) { if (rc == PHGPU_OK) rc = s; };
+    T(dcopy(C, &S.d_rs, rs.data(), rs.size()));
+    T(dcopy(C, &S.d_bcol, bcol.data(), bcol.size()));
+    T(dcopy(C, &S.d_bcolp, bcolp.data(), bcolp.size()));
+    T(dcopy(C, &S.d_brow, brow.data(), brow.size()));
+    T(dcopy(C, &S.d_ient, tien.data(), tien.size()));
+    T(dcopy(C, &S.d_tmap, tmap.data(), tmap.size()));
+    T(dcopy(C, &S.d_hmap, hmap.data(), hmap.size()));
+    T(dcopy(C, &S.d_wmap, wmap.data(), wmap.size()));
+    if (rc == PHGPU_OK && cudaMalloc((void**)&S.d_lhsK, sizeof(double) * 25 * (size_t)std::max(S.nnzb, 1)) != cudaSuccess)
+        rc = PHGPU_ERR_NOMEM;
+    if (rc == PHGPU_OK) rc = ensure_f32(C);
+    if (rc == PHGPU_OK) upload_tangent_tables(C);
+    if (rc == PHGPU_OK) rc = configure_tangent_kernels(C);
+    if (rc == PHGPU_OK) rc = check(C, cudaStreamSynchronize(C.stream), "sparse set-up");
+    if (rc != PHGPU_OK) {
+        if (C.err.empty()) C.err = "sparse set-up failed";
+        return rc;
+    }
+    S.ready = true;
+    return PHGPU_OK;
+}
+
+template <typename R>
+void spsi3pre(Ctx& C, const R* bd, R* lhsK) {
+    const int n = C.sp.nnzb;
+    if (n == 0) return;
+    k_spsi3pre<R><<<(n + 127) / 128, 128, 0, C.stream>>>(C.sp.d_brow, C.sp.d_bcol, bd, lhsK, n);
+    ++C.launches;
+}
+template void spsi3pre<double>(Ctx&, const double*, double*);
+template void spsi3pre<float>(Ctx&, const float*, float*);
+
+template <typename M, typename V>
+void sparse_ap(Ctx& C, const M* lhsK, const V* p, V* q) {
+    const int N = C.N;
+    const size_t threads = 32 * (size_t)N;
+    k_bsr_spmv<M, V><<<(unsigned)((threads + kSpThreads - 1) / kSpThreads), kSpThreads, 0, C.stream>>>(
+        C.sp.d_rs, C.sp.d_bcolp, lhsK, p, q, N);
+    ++C.launches;
+    bc3per<V>(C, q);
+}
+template void sparse_ap<double, double>(Ctx&, const double*, const double*, double*);
+template void sparse_ap<float, float>(Ctx&, const float*, const float*, float*);
+
+}  // namespace phgpu

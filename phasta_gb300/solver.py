@@ -13,6 +13,16 @@ argument meaning (arrays in the reference layout, see include/phgpu.h):
     newton(y, ac, yold, acold)   one flow solve of itrdrv      itrdrv.f:489-598
     time_step(yold, acold, nitr) itrPredict + nitr solves + itrUpdate
 
+and the sparse solver of the reference's impl = 1x path (lhs = 1):
+
+    genadj(case, nnz)            -> colm, rowp (1-based)      genadj.f:1 (host only)
+    ElmGMRs(y, ac)               -> res, BDiag, lhsK          elmgmr.f:280
+    Spsi3pre(lu, lhsK)           -> lhsK                      spsi3pre.f:1
+    SparseAp(lhsK, p)            -> lhsK p (+ bc3per)         sparseap.f:1, bc3per.f:1
+    SolGMRs(y, ac, lhs)          -> res, BDiag, Dy, lhsK, st  solgmr.f:480
+
+lhsK is returned as an (nnz_tot, 25) array: row k is the reference's lhsK(:, k).
+
 Every call runs on the GPU; a non-zero status from the library raises
 ``PhgpuError`` (the reference would stop in error()/tnanq).
 """
@@ -75,28 +85,49 @@ def _stats(s: L.Stats) -> SolveStats:
                       s.t_assembly_ms, s.t_gmres_ms)
 
 
+class _MeshArrays:
+    """The phgpu_mesh of a Case, with the host arrays it points to kept alive."""
+
+    def __init__(self, case: Case):
+        self.x = case.x_ref()
+        self.ien = np.ascontiguousarray(case.ien, dtype=np.int32).reshape(-1)
+        self.ienb = np.ascontiguousarray(case.ienb, dtype=np.int32).reshape(-1)
+        self.iBCB = np.ascontiguousarray(case.iBCB, dtype=np.int32).reshape(-1)
+        self.BCB = np.ascontiguousarray(case.BCB, dtype=np.float64).reshape(-1)
+        self.iBC = np.ascontiguousarray(case.iBC, dtype=np.int32)
+        self.BC = np.ascontiguousarray(case.BC, dtype=np.float64).reshape(-1)
+        self.iper = np.ascontiguousarray(case.iper, dtype=np.int32)
+        self.ienh = np.ascontiguousarray(case.ienh, dtype=np.int32).reshape(-1)
+        self.ienw = np.ascontiguousarray(case.ienw, dtype=np.int32).reshape(-1)
+        nb = case.nbelem
+        self.m = L.Mesh(case.nshg, case.nelem, L.iptr(self.ien) if case.nelem else None, L.dptr(self.x), nb,
+                        L.iptr(self.ienb) if nb else None, L.iptr(self.iBCB) if nb else None,
+                        L.dptr(self.BCB) if nb else None, L.iptr(self.iBC), L.dptr(self.BC), L.iptr(self.iper),
+                        case.nhex, L.iptr(self.ienh) if case.nhex else None, case.nwedge,
+                        L.iptr(self.ienw) if case.nwedge else None)
+
+
+def genadj(case: Case, nnz: int = 40):
+    """genadj.f: colm (nshg+1) and rowp (nnz_tot), 1-based; runs on the host (no GPU)."""
+    lib = L.lib()
+    ma = _MeshArrays(case)
+    colm = np.zeros(case.nshg + 1, np.int32)
+    rowp = np.zeros(case.nshg * nnz, np.int32)
+    icnt = C.c_int()
+    rc = lib.phgpu_genadj(C.byref(ma.m), nnz, L.iptr(colm), L.iptr(rowp), C.byref(icnt))
+    if rc != 0:
+        raise PhgpuError(rc, "genadj: more than nnz blocks in a row" if rc == L.PHGPU_ERR_TOO_LARGE else "genadj")
+    return colm, rowp[: icnt.value].copy()
+
+
 class GpuSolver:
     def __init__(self, case: Case, params: dict):
         self.lib = L.lib()
         self.case = case
         self.params = dict(params)
         self.nshg = case.nshg
-        # keep the host arrays alive for the duration of create
-        self._x = case.x_ref()
-        self._ien = np.ascontiguousarray(case.ien, dtype=np.int32).reshape(-1)
-        self._ienb = np.ascontiguousarray(case.ienb, dtype=np.int32).reshape(-1)
-        self._iBCB = np.ascontiguousarray(case.iBCB, dtype=np.int32).reshape(-1)
-        self._BCB = np.ascontiguousarray(case.BCB, dtype=np.float64).reshape(-1)
-        self._iBC = np.ascontiguousarray(case.iBC, dtype=np.int32)
-        self._BC = np.ascontiguousarray(case.BC, dtype=np.float64).reshape(-1)
-        self._iper = np.ascontiguousarray(case.iper, dtype=np.int32)
-        self._ienh = np.ascontiguousarray(case.ienh, dtype=np.int32).reshape(-1)
-        self._ienw = np.ascontiguousarray(case.ienw, dtype=np.int32).reshape(-1)
-        m = L.Mesh(self.nshg, case.nelem, L.iptr(self._ien) if case.nelem else None, L.dptr(self._x), case.nbelem,
-                   L.iptr(self._ienb) if case.nbelem else None, L.iptr(self._iBCB) if case.nbelem else None,
-                   L.dptr(self._BCB) if case.nbelem else None, L.iptr(self._iBC), L.dptr(self._BC),
-                   L.iptr(self._iper), case.nhex, L.iptr(self._ienh) if case.nhex else None, case.nwedge,
-                   L.iptr(self._ienw) if case.nwedge else None)
+        self._mesh = _MeshArrays(case)  # kept alive for the duration of create
+        m = self._mesh.m
         self._cfg = _config(self.params)
         h = C.c_void_p()
         rc = self.lib.phgpu_create(C.byref(m), C.byref(self._cfg), C.byref(h))
@@ -204,6 +235,41 @@ class GpuSolver:
                                              C.byref(st)))
         self.ntotGM = st.ntotGM
         return yold, acold, y, ac, _stats(st)
+
+    # -- sparse solver (lhs = 1) --
+    @property
+    def nnz_tot(self) -> int:
+        n = C.c_int()
+        self._check(self.lib.phgpu_nnz_tot(self.h, C.byref(n)))
+        return n.value
+
+    def ElmGMRs(self, y, ac):
+        res, bd = self._v(), self._v(25)
+        lhsK = np.zeros((self.nnz_tot, 25))
+        self._check(self.lib.phgpu_elmgmrs(self.h, L.dptr(y), L.dptr(ac), L.dptr(res), L.dptr(bd), L.dptr(lhsK)))
+        return res, bd, lhsK
+
+    def Spsi3pre(self, lu, lhsK):
+        out = np.array(lhsK, dtype=np.float64, order="C")
+        self._check(self.lib.phgpu_spsi3pre(self.h, L.dptr(np.ascontiguousarray(lu, dtype=np.float64)), L.dptr(out)))
+        return out
+
+    def SparseAp(self, lhsK, p):
+        p = np.array(p, dtype=np.float64)
+        self._check(self.lib.phgpu_sparseap(self.h, L.dptr(np.ascontiguousarray(lhsK, dtype=np.float64)), L.dptr(p)))
+        return p
+
+    def SolGMRs(self, y, ac, lhs: int = 1, lGMRES_common: int = 0):
+        """SolGMRs; lGMRES_common is the COMMON lGMRES its restart test reads (solgmr.f:528)."""
+        res, bd, Dy = self._v(), self._v(25), self._v()
+        lhsK = np.zeros((self.nnz_tot, 25)) if self.params.get("precision", L.PHGPU_FP64) == L.PHGPU_FP64 else None
+        st = L.Stats()
+        st.ntotGM = self.ntotGM
+        st.lGMRES = lGMRES_common
+        self._check(self.lib.phgpu_solgmrs(self.h, L.dptr(y), L.dptr(ac), lhs, L.dptr(res), L.dptr(bd), L.dptr(Dy),
+                                           L.dptr(lhsK), C.byref(st)))
+        self.ntotGM = st.ntotGM
+        return res, bd, Dy, lhsK, _stats(st)
 
     # -- device-resident path (benchmarks) --
     def upload(self, y=None, ac=None, yold=None, acold=None):
