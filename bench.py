@@ -230,6 +230,8 @@ def run_gpu(args, rank, world):
     }
     if args.precision == "mixed" and not args.skip_fp64:
         result["fp64_plain"] = fp64_plain(args, case)
+    if not args.skip_sparse:
+        result["sparse_solver"] = sparse_solver(args)
     g.close()
     return result
 
@@ -286,6 +288,51 @@ def kernel_roofline(g, case, stream, args, krylov_per_newton):
     return {"kernel": k["kernel"], "bound": "hbm", "achieved": k["achieved_gbs"], "peak": peak, "unit": "GB/s",
             "frac": k["achieved_gbs"] / peak, "peak_source": f"{src} hbm_gbs", "traffic": traffic,
             "algorithmic_bytes": k["algorithmic_bytes"], "launch_ms": k["ms"], "sweeps": kernels}
+
+
+def sparse_solver(args):
+    """The reference's sparse solver (SolGMRs on the assembled tangent) on the same workload:
+    FP32 tangent and Krylov vectors in mixed precision, FP64 throughout otherwise."""
+    import torch
+
+    from phasta_gb300 import _lib as L
+    from phasta_gb300.solver import GpuSolver
+
+    case, params, y0, ac0 = make_workload(args.n, args.precision)
+    params = dict(params, ap_mode=L.PHGPU_AP_SPARSE)
+    g = GpuSolver(case, params)
+    stream = torch.cuda.ExternalStream(g.stream())
+    g.upload(y0, ac0, y0, ac0)
+    g.time_step_dev(NEWTON_PER_TIMESTEP)  # warm-up (builds the block structure)
+    g.upload(y0, ac0, y0, ac0)
+    g.set_params(istep=0, eGMRES=0.0)
+    torch.cuda.synchronize()
+    r0 = g.residual_norm_dev()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    iks = []
+    for it in range(1, NEWTON_PER_TIMESTEP + 1):
+        g.set_params(iter=it)
+        iks.append(g.newton_dev().iKs)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / NEWTON_PER_TIMESTEP
+    r_end = g.residual_norm_dev()
+    E, N, nnzb = case.nelem, case.nshg, g.nnz_tot
+    vb = 4 if args.precision == "mixed" else 8
+    tan, spmv = (9, 10) if args.precision == "mixed" else (11, 12)
+    t_tan = _time_sweep(g, stream, tan, reps=3)
+    t_spmv = _time_sweep(g, stream, spmv, reps=10)
+    # compulsory bytes: the tangent writes lhsK once and reads x, y, connectivity and block maps;
+    # the product reads lhsK, its column list and the vector once and writes the result
+    tan_bytes = 25 * vb * nnzb + N * 8 * vb + E * (16 + 64)
+    spmv_bytes = nnzb * (25 * vb + 4) + 4 * (N + 1) + 2 * 5 * vb * N
+    g.close()
+    return {"ms_per_newton": ms, "value": E / ms * 1e3, "krylov_iterations": iks,
+            "rel_residual_after_3": r_end / r0, "nnz_blocks": nnzb,
+            "tangent": {"ms": t_tan * 1e3, "algorithmic_bytes": tan_bytes, "achieved_gbs": tan_bytes / t_tan / 1e9},
+            "spmv": {"ms": t_spmv * 1e3, "algorithmic_bytes": spmv_bytes,
+                     "achieved_gbs": spmv_bytes / t_spmv / 1e9}}
 
 
 def fp64_plain(args, case):
@@ -369,6 +416,7 @@ def main():
     ap.add_argument("--cpu-sample-n", type=int, default=96)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-sparse", action="store_true", help="leave out the assembled-tangent solver line")
     args = ap.parse_args()
     rank, world, _ = _dist()
     if args.impl == "reference":

@@ -226,7 +226,7 @@ template <typename V> void scale_by(Ctx& C, V* w, const double* s, int mode, siz
 void block_adjacency(int N, const int* ien, int ne, const int* ienh, int nh, const int* ienw, int nw,
                      std::vector<int>& colm, std::vector<int>& rowp);
 int sparse_setup(Ctx& C);
-template <typename R> void launch_tangent(Ctx& C, const R* x, const R* y, R* lhsK);
+template <typename R> void launch_tangent(Ctx& C, const R* x, const R* y, R* lhsK, R* bd = nullptr);
 void upload_tangent_tables(Ctx& C);
 int configure_tangent_kernels(Ctx& C);
 // Spsi3pre: lhsK <- L_i^-1 lhsK U_j^-1 with the i3LU factors bd (device layouts)

@@ -277,6 +277,15 @@ int elmmfg64(Ctx& C, const double* y, const double* ac, double* res, double* rme
     return check(C, cudaGetLastError(), "elmmfg");
 }
 
+// the FP64 tangent of ElmGMRs (lhs = 1): lhsK, and BDiag from its diagonal blocks + bc3BDg
+int tangent64(Ctx& C, const double* y, double* lhsK, double* bd) {
+    fill0(C, lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb);
+    fill0(C, bd, sizeof(double) * 25 * (size_t)C.N);
+    launch_tangent<double>(C, C.d_x, y, lhsK, bd);
+    bc3bdg<double>(C, y, bd);
+    return check(C, cudaGetLastError(), "tangent");
+}
+
 // rmes += Rmod(yp; yc) then bc3Res (itrres.f)
 template <typename R>
 int itrres_dev(Ctx& C, const R* x, const R* yp, const R* yc, R* rmes, int iabres, const int* skip) {
@@ -557,11 +566,12 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
     const bool asm_bd = !sparse || lhs;
     cudaEventRecord(C.ev[0], C.stream);
     if (C.cfg.precision == PHGPU_FP64) {
-        if (asm_bd) PH_TRY(elmmfg64(C, C.d_y, C.d_ac, C.d_res, C.d_rmes, C.d_bd, 1));
-        else PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
-        if (sparse && lhs) {
-            fill0(C, C.sp.d_lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb);
-            launch_tangent<double>(C, C.d_x, C.d_y, C.sp.d_lhsK);
+        if (sparse) {
+            // ElmGMRs: the residual, and BDiag from the tangent's diagonal blocks
+            PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
+            if (lhs) PH_TRY(tangent64(C, C.d_y, C.sp.d_lhsK, C.d_bd));
+        } else {
+            PH_TRY(elmmfg64(C, C.d_y, C.d_ac, C.d_res, C.d_rmes, C.d_bd, 1));
         }
     } else {
         if (C.cfg.ap_mode == PHGPU_AP_FD)
@@ -588,13 +598,15 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
         }
         if (asm_bd) {
             fill0(C, C.d_bdf, sizeof(float) * 25 * N);
-            launch_elem_full<float>(C, C.d_xf, C.d_yf, C.d_acf, nullptr, nullptr, C.d_bdf);
+            if (sparse) {
+                // FP32 tangent; its diagonal blocks are the block diagonal
+                fill0(C, C.sp.d_lhsKf, sizeof(float) * 25 * (size_t)C.sp.nnzb);
+                launch_tangent<float>(C, C.d_xf, C.d_yf, C.sp.d_lhsKf, C.d_bdf);
+            } else {
+                launch_elem_full<float>(C, C.d_xf, C.d_yf, C.d_acf, nullptr, nullptr, C.d_bdf);
+            }
             bc3bdg<float>(C, C.d_y, C.d_bdf);
             to_f64(C, C.d_bdf, C.d_bd, 25 * N);
-        }
-        if (sparse && lhs) {
-            fill0(C, C.sp.d_lhsKf, sizeof(float) * 25 * (size_t)C.sp.nnzb);
-            launch_tangent<float>(C, C.d_xf, C.d_yf, C.sp.d_lhsKf);
         }
     }
     // nonlinear residual ||R|| (FP64, unpreconditioned)
@@ -1079,9 +1091,8 @@ int phgpu_elmgmrs(phgpu_ctx* h, const double* y, const double* ac, double* res, 
     C.sp.have = -1;
     ref_to_dev_state(C, y, C.d_t64, C.d_y);
     ref_to_dev_state(C, ac, C.d_t64b, C.d_ac);
-    PH_TRY(elmmfg64(C, C.d_y, C.d_ac, C.d_res, C.d_rmes, C.d_bd, 1));
-    fill0(C, C.sp.d_lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb);
-    launch_tangent<double>(C, C.d_x, C.d_y, C.sp.d_lhsK);
+    PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
+    PH_TRY(tangent64(C, C.d_y, C.sp.d_lhsK, C.d_bd));
     dev_to_ref_res(C, C.d_res, C.d_t64, res);
     dev_to_ref_bd(C, C.d_bd, C.d_bdstage, bdiag);
     PH_TRY(check(C, cudaMemcpyAsync(lhsK, C.sp.d_lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb,
@@ -1249,6 +1260,26 @@ int phgpu_sweep_dev(phgpu_ctx* h, int which) {
         case 8:
             split_f32(C, C.d_y, C.d_yf, C.d_ylo, n5);
             to_f32(C, C.d_ac, C.d_acf, n5);
+            break;
+        case 9:   // FP32 assembled tangent (zero fill + element sweep)
+        case 11:  // FP64 assembled tangent
+            PH_TRY(sparse_setup(C));
+            C.sp.have = -1;
+            if (which == 9) {
+                fill0(C, C.sp.d_lhsKf, sizeof(float) * 25 * (size_t)C.sp.nnzb);
+                launch_tangent<float>(C, C.d_xf, C.d_yf, C.sp.d_lhsKf);
+            } else {
+                fill0(C, C.sp.d_lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb);
+                launch_tangent<double>(C, C.d_x, C.d_y, C.sp.d_lhsK);
+            }
+            break;
+        case 10:  // FP32 block-sparse product (SparseAp + bc3per) of the state
+            PH_TRY(sparse_setup(C));
+            sparse_ap<float, float>(C, C.sp.d_lhsKf, C.d_yf, C.d_t32);
+            break;
+        case 12:  // FP64 block-sparse product
+            PH_TRY(sparse_setup(C));
+            sparse_ap<double, double>(C, C.sp.d_lhsK, C.d_y, C.d_t64);
             break;
         default:
             return PHGPU_ERR_INVALID;

@@ -7,9 +7,9 @@
 //
 // lhsK lives in the reference's layout, lhsK(25, nnz_tot) column-major: block
 // k is 25 contiguous values with entry (f, g) at 5 g + f, blocks of a row are
-// contiguous and ordered by column node.  The product streams each row's
-// 25 * nnz_row values with one warp (coalesced), gathers p through the
-// iper-mapped column list and reduces the five row sums across the warp.
+// contiguous and ordered by column node.  The product gives each (row,
+// equation) pair one thread, which reads its five entries of every block of the
+// row and gathers p through the iper-mapped column list.
 #include <algorithm>
 
 #include "phgpu_impl.cuh"
@@ -117,44 +117,28 @@ __global__ void k_spsi3pre(const int* __restrict__ brow, const int* __restrict__
         for (int f = 0; f < 5; ++f) a[5 * g + f] = m[f][g];
 }
 
-// ---- SparseAp: one warp per block row ----
-constexpr int kSpThreads = 256;
+// ---- SparseAp: one thread per (block row, equation) ----
+// Thread (i, f) forms q(i, f) = sum_k sum_g lhsK(k)(f, g) p(iper(col k), g) over the blocks
+// of row i: five strided values of each block (the row's segment is read in full by its
+// five threads), one gathered node of p, and no reduction across threads.
+constexpr int kSpThreads = 160;  // 32 block rows
 
 template <typename M, typename V>
 __global__ void __launch_bounds__(kSpThreads)
 k_bsr_spmv(const int* __restrict__ rs, const int* __restrict__ bcolp, const M* __restrict__ A,
            const V* __restrict__ p, V* __restrict__ q, int N) {
-    const int lane = threadIdx.x & 31;
-    const int row = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = t / 5, f = t - 5 * (t / 5);
     if (row >= N) return;
     const int k0 = rs[row], k1 = rs[row + 1];
-    const int nv = 25 * (k1 - k0);
-    const M* a = A + 25 * (size_t)k0;
-    V acc[5] = {V(0), V(0), V(0), V(0), V(0)};
-    // value index v = 25 kb + 5 g + f; lanes stride by 32 = 25 + 7
-    int kb = lane / 25, e = lane - 25 * (lane / 25);
-    for (int v = lane; v < nv; v += 32) {
-        const int g = e / 5, f = e - 5 * g;
-        const V t = (V)a[v] * p[5 * (size_t)bcolp[k0 + kb] + g];
-#pragma unroll
-        for (int r = 0; r < 5; ++r) acc[r] += (r == f) ? t : V(0);
-        e += 7;
-        kb += 1;
-        if (e >= 25) {
-            e -= 25;
-            kb += 1;
-        }
+    V acc = V(0);
+#pragma unroll 2
+    for (int k = k0; k < k1; ++k) {
+        const M* a = A + 25 * (size_t)k + f;
+        const V* pj = p + 5 * (size_t)bcolp[k];
+        acc += (V)a[0] * pj[0] + (V)a[5] * pj[1] + (V)a[10] * pj[2] + (V)a[15] * pj[3] + (V)a[20] * pj[4];
     }
-#pragma unroll
-    for (int r = 0; r < 5; ++r)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
-    if (lane < 5) {
-        V out = acc[0];
-#pragma unroll
-        for (int r = 1; r < 5; ++r) out = (lane == r) ? acc[r] : out;
-        q[5 * (size_t)row + lane] = out;
-    }
+    q[5 * (size_t)row + f] = acc;
 }
 
 }  // namespace
@@ -237,7 +221,7 @@ template void spsi3pre<float>(Ctx&, const float*, float*);
 template <typename M, typename V>
 void sparse_ap(Ctx& C, const M* lhsK, const V* p, V* q) {
     const int N = C.N;
-    const size_t threads = 32 * (size_t)N;
+    const size_t threads = 5 * (size_t)N;
     k_bsr_spmv<M, V><<<(unsigned)((threads + kSpThreads - 1) / kSpThreads), kSpThreads, 0, C.stream>>>(
         C.sp.d_rs, C.sp.d_bcolp, lhsK, p, q, N);
     ++C.launches;

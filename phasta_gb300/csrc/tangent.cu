@@ -22,6 +22,11 @@
 #include "phgpu_impl.cuh"
 #include "qpoint.cuh"
 
+// resident CTAs per SM of the FP32 tangent (register budget 65536 / (128 x this))
+#ifndef PHGPU_TAN32_MINB
+#define PHGPU_TAN32_MINB 6
+#endif
+
 namespace phgpu {
 namespace {
 
@@ -144,10 +149,10 @@ __device__ __forceinline__ void bc3lhs_block(R (&M)[5][5], int ia, const double*
 }
 
 template <typename R, int NEN, int TOPO>
-__global__ void __launch_bounds__(kTanThreads)
+__global__ void __launch_bounds__(kTanThreads, sizeof(R) == 4 ? PHGPU_TAN32_MINB : 2)
 k_tangent(const int* __restrict__ ien, const int* __restrict__ bmap, int ne, const R* __restrict__ x,
           const R* __restrict__ y, const int* __restrict__ iBC, const double* __restrict__ BC,
-          R* __restrict__ lhsK, Phys<R> P) {
+          R* __restrict__ lhsK, R* __restrict__ bd, Phys<R> P) {
     using Q = TanQp<NEN>;
     constexpr int EPB = tan_epb<NEN>();
     constexpr int NB = NEN * NEN;
@@ -317,6 +322,14 @@ k_tangent(const int* __restrict__ ien, const int* __restrict__ bmap, int ne, con
     }
     const int* ids = sid + NEN * le;
     const int na = ids[a], nb = ids[b];
+    // the block diagonal is the tangent's diagonal blocks before bc3LHS (asigmr.f:92-103)
+    if (bd && a == b) {
+        R* ob = bd + 25 * (size_t)na;  // row-major BDiag(n, r, c)
+#pragma unroll
+        for (int r = 0; r < 5; ++r)
+#pragma unroll
+            for (int c = 0; c < 5; ++c) ob[5 * r + c] += M[r][c];
+    }
     const int ia = iBC[na], ib = iBC[nb];
     if (ia | ib) bc3lhs_block(M, ia, BC + 6 * (size_t)na, ib, BC + 6 * (size_t)nb, a == b);
     R* o = lhsK + 25 * (size_t)bmap[(size_t)e * NB + ab];
@@ -328,7 +341,7 @@ k_tangent(const int* __restrict__ ien, const int* __restrict__ bmap, int ne, con
 
 template <typename R, int NEN, int TOPO>
 void launch_one(Ctx& C, const int* d_ien, const int* d_map, const std::vector<int>& col, const R* x, const R* y,
-                R* lhsK) {
+                R* lhsK, R* bd) {
     const Phys<R> P = make_phys<R>(C.cfg);
     constexpr int EPB = tan_epb<NEN>();
     const size_t sm = tan_smem<R, NEN>();
@@ -337,7 +350,7 @@ void launch_one(Ctx& C, const int* d_ien, const int* d_map, const std::vector<in
         const int e0 = col[c], ne = col[c + 1] - e0;
         if (ne <= 0) continue;
         k_tangent<R, NEN, TOPO><<<(ne + EPB - 1) / EPB, kTanThreads, sm, C.stream>>>(
-            d_ien + (size_t)NEN * e0, d_map + (size_t)NEN * NEN * e0, ne, x, y, C.d_iBC, C.d_BC, lhsK, P);
+            d_ien + (size_t)NEN * e0, d_map + (size_t)NEN * NEN * e0, ne, x, y, C.d_iBC, C.d_BC, lhsK, bd, P);
         ++C.launches;
     }
 }
@@ -372,15 +385,16 @@ int configure_tangent_kernels(Ctx& C) {
     return rc;
 }
 
-// lhsK += the element tangents of every block (tets, hexes, wedges), colour by colour
+// lhsK += the element tangents of every block (tets, hexes, wedges), colour by colour;
+// bd (optional, device layout) += their diagonal blocks before the boundary conditions
 template <typename R>
-void launch_tangent(Ctx& C, const R* x, const R* y, R* lhsK) {
+void launch_tangent(Ctx& C, const R* x, const R* y, R* lhsK, R* bd) {
     const SparseCtx& S = C.sp;
-    if (C.E > 0) launch_one<R, 4, 2>(C, S.d_ient, S.d_tmap, S.tcol_start, x, y, lhsK);
-    if (C.nhex > 0) launch_one<R, 8, 0>(C, C.d_ienh, S.d_hmap, C.hcol_start, x, y, lhsK);
-    if (C.nwedge > 0) launch_one<R, 6, 1>(C, C.d_ienw, S.d_wmap, C.wcol_start, x, y, lhsK);
+    if (C.E > 0) launch_one<R, 4, 2>(C, S.d_ient, S.d_tmap, S.tcol_start, x, y, lhsK, bd);
+    if (C.nhex > 0) launch_one<R, 8, 0>(C, C.d_ienh, S.d_hmap, C.hcol_start, x, y, lhsK, bd);
+    if (C.nwedge > 0) launch_one<R, 6, 1>(C, C.d_ienw, S.d_wmap, C.wcol_start, x, y, lhsK, bd);
 }
-template void launch_tangent<double>(Ctx&, const double*, const double*, double*);
-template void launch_tangent<float>(Ctx&, const float*, const float*, float*);
+template void launch_tangent<double>(Ctx&, const double*, const double*, double*, double*);
+template void launch_tangent<float>(Ctx&, const float*, const float*, float*, float*);
 
 }  // namespace phgpu
