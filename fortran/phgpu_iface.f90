@@ -7,7 +7,7 @@ module phgpu_iface
 
   integer(c_int), parameter :: PHGPU_OK = 0
   integer(c_int), parameter :: PHGPU_FP64 = 0, PHGPU_MIXED = 1
-  integer(c_int), parameter :: PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1
+  integer(c_int), parameter :: PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1, PHGPU_AP_SPARSE = 2
   integer(c_int), parameter :: PHGPU_RES_FP64 = 0, PHGPU_RES_GALERKIN64 = 1
 
   type, bind(C) :: phgpu_config
@@ -77,6 +77,38 @@ module phgpu_iface
        real(c_double), intent(inout) :: yold(*), acold(*)
        real(c_double), intent(out) :: y(*), ac(*)
        integer(c_int), value :: nitr
+       type(phgpu_stats), intent(inout) :: st
+     end function
+     integer(c_int) function phgpu_genadj(mesh, nnz, colm, rowp, icnt) bind(C, name="phgpu_genadj")
+       import :: c_int, phgpu_mesh
+       type(phgpu_mesh), intent(in) :: mesh
+       integer(c_int), value :: nnz
+       integer(c_int), intent(out) :: colm(*), rowp(*), icnt
+     end function
+     integer(c_int) function phgpu_elmgmrs(ctx, y, ac, res, bdiag, lhsK) bind(C, name="phgpu_elmgmrs")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: y(*), ac(*)
+       real(c_double), intent(out) :: res(*), bdiag(*), lhsK(*)
+     end function
+     integer(c_int) function phgpu_spsi3pre(ctx, bdiag, lhsK) bind(C, name="phgpu_spsi3pre")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: bdiag(*)
+       real(c_double), intent(inout) :: lhsK(*)
+     end function
+     integer(c_int) function phgpu_sparseap(ctx, lhsK, p) bind(C, name="phgpu_sparseap")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: lhsK(*)
+       real(c_double), intent(inout) :: p(*)
+     end function
+     integer(c_int) function phgpu_solgmrs(ctx, y, ac, lhs, res, bdiag, Dy, lhsK, st) bind(C, name="phgpu_solgmrs")
+       import :: c_int, c_double, c_ptr, phgpu_stats
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: y(*), ac(*)
+       integer(c_int), value :: lhs
+       real(c_double), intent(out) :: res(*), bdiag(*), Dy(*), lhsK(*)
        type(phgpu_stats), intent(inout) :: st
      end function
      type(c_ptr) function phgpu_last_error(ctx) bind(C, name="phgpu_last_error")
