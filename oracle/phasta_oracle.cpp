@@ -1118,9 +1118,17 @@ void fillsparse_element(const int* ie, int nshl, const double* EG, const int* co
 }
 
 // AsIGMR (asigmr.f:1-105) + bc3LHS + fillsparseC for one interior element (elmgmr.f:429-466)
+// EBE store (ElmGMRe, elmgmr.f:1-275): EGmass(numel, nedof, nedof) column-major, element eidx
+struct EbeStore {
+    double* EG;
+    size_t numel;
+    int nedof;
+    size_t eidx;
+};
+
 void one_element_lhs(const or_common& c, const Topo& tp, const or_mesh& m, const int* ie, const double* y,
                      const double* ac, double* res, double* bd, const int* colm, const int* rowp, double* lhsK,
-                     const double* qres) {
+                     const double* qres, const EbeStore* ebe = nullptr) {
     const int nshg = m.nshg, nen = tp.nshl, nedof = 5 * nen;
     double yl[8][5], acl[8][5], xl[8][3], ql[8][12];
     for (int a = 0; a < nen; ++a) {
@@ -1141,7 +1149,13 @@ void one_element_lhs(const or_common& c, const Topo& tp, const or_mesh& m, const
             for (int a = 0; a < nen; ++a)
                 bd[(i + 5 * j) * (size_t)nshg + ie[a]] += EG[(size_t)(5 * a + i) * nedof + 5 * a + j];
     bc3lhs_element(m, ie, nen, EG.data());
-    fillsparse_element(ie, nen, EG.data(), colm, rowp, lhsK);
+    if (ebe) {
+        for (int j = 0; j < nedof; ++j)
+            for (int i = 0; i < nedof; ++i)
+                ebe->EG[ebe->eidx + ebe->numel * ((size_t)i + (size_t)ebe->nedof * j)] = EG[(size_t)i * nedof + j];
+    } else {
+        fillsparse_element(ie, nen, EG.data(), colm, rowp, lhsK);
+    }
 }
 
 }  // namespace
@@ -1978,6 +1992,226 @@ void or_solgmrs(or_common* c, const or_mesh* m, const int* colm, const int* rowp
     or_i3lu(N, bdiag, Dy, 2);
     st->iKs = iKs;
     st->lGMRES = lGMRESs;
+    st->echeck = echeck;
+    st->eGMRES = c->eGMRES;
+    st->totres = std::sqrt(sumsq(res, n5)) / (double)N;
+}
+
+// ---- element-by-element solver (SolGMRe) on single-topology meshes ----
+// element e of EGmass is the e-th element of the reference's block order: tets (input order,
+// eid[] maps the oracle's grouped order back to it), then hexes, then wedges.
+static int ebe_nedof(const or_mesh& m) { return m.nhex ? 40 : m.nwedge ? 30 : 20; }
+
+// ElmGMRe (elmgmr.f:1-275): res, BDiag, and EGmass after bc3LHS
+void or_elmgmre(const or_common* c, const or_mesh* m, const int* eid, const double* y, const double* ac,
+                double* res, double* bdiag, double* EG, int nthreads) {
+    const size_t N = m->nshg;
+    const size_t numel = (size_t)m->nelem + m->nhex + m->nwedge;
+    const int nedof = ebe_nedof(*m);
+    std::memset(res, 0, sizeof(double) * 5 * N);
+    std::memset(bdiag, 0, sizeof(double) * 25 * N);
+    std::memset(EG, 0, sizeof(double) * numel * nedof * nedof);
+    std::vector<double> qres;
+    if (c->idiff == 1) {
+        qres.resize(12 * N);
+        reconstruct_q(*c, *m, y, qres.data());
+    }
+    const double* q = qres.empty() ? nullptr : qres.data();
+    const int ngrp = m->ngrp > 0 ? m->ngrp : 1;
+    for (int gI = 0; gI < ngrp; ++gI) {
+        const int b0 = m->ngrp > 0 ? m->grp_start[gI] : 0;
+        const int b1 = m->ngrp > 0 ? m->grp_start[gI + 1] : m->nblk;
+        parallel_for(b1 - b0, nthreads, [&](int bi) {
+            const int blk = b0 + bi;
+            for (int e = m->blk_start[blk]; e < m->blk_start[blk + 1]; ++e) {
+                const EbeStore st{EG, numel, nedof, (size_t)(eid ? eid[e] : e)};
+                one_element_lhs(*c, topo(1), *m, m->ien + 4 * (size_t)e, y, ac, res, bdiag, nullptr, nullptr,
+                                nullptr, q, &st);
+            }
+        });
+    }
+    for (int e = 0; e < m->nhex; ++e) {
+        const EbeStore st{EG, numel, nedof, (size_t)m->nelem + e};
+        one_element_lhs(*c, topo(2), *m, m->ienh + 8 * (size_t)e, y, ac, res, bdiag, nullptr, nullptr, nullptr, q,
+                        &st);
+    }
+    for (int e = 0; e < m->nwedge; ++e) {
+        const EbeStore st{EG, numel, nedof, (size_t)m->nelem + m->nhex + e};
+        one_element_lhs(*c, topo(3), *m, m->ienw + 6 * (size_t)e, y, ac, res, bdiag, nullptr, nullptr, nullptr, q,
+                        &st);
+    }
+    boundary_sweep(*c, *m, y, res);
+    or_bc3res(m, y, res, c);
+    or_bc3bdg(m, y, bdiag, c);
+}
+
+// the nodes of element e of the block order
+static const int* ebe_nodes(const or_mesh& m, const std::vector<int>& pos, size_t e, int* nshl) {
+    if (e < (size_t)m.nelem) { *nshl = 4; return m.ien + 4 * (size_t)pos[e]; }
+    e -= m.nelem;
+    if (e < (size_t)m.nhex) { *nshl = 8; return m.ienh + 8 * e; }
+    *nshl = 6;
+    return m.ienw + 6 * (e - m.nhex);
+}
+static std::vector<int> ebe_pos(const or_mesh& m, const int* eid) {
+    std::vector<int> pos(m.nelem);
+    for (int e = 0; e < m.nelem; ++e) pos[eid ? eid[e] : e] = e;
+    return pos;
+}
+
+// i3pre (i3pre.f:1-105): EGmass rows of node a <- L_a^-1 rows, then columns of node b <- U_b^-1
+void or_i3pre(const or_mesh* m, const int* eid, const double* bd, double* EG) {
+    const size_t N = m->nshg, numel = (size_t)m->nelem + m->nhex + m->nwedge;
+    const int nedof = ebe_nedof(*m);
+    const std::vector<int> pos = ebe_pos(*m, eid);
+    auto B = [&](int n, int r, int cc) { return bd[(size_t)(r + 5 * cc) * N + n]; };
+    for (size_t e = 0; e < numel; ++e) {
+        int nshl;
+        const int* ie = ebe_nodes(*m, pos, e, &nshl);
+        auto E = [&](int i, int j) -> double& { return EG[e + numel * ((size_t)i + (size_t)nedof * j)]; };
+        for (int a = 0; a < nshl; ++a) {
+            const int i = 5 * a, n = ie[a];
+            for (int j = 0; j < nedof; ++j)
+                for (int r = 1; r < 5; ++r) {
+                    double v = E(i + r, j);
+                    for (int cc = 0; cc < r; ++cc) v = v - B(n, r, cc) * E(i + cc, j);
+                    E(i + r, j) = v;
+                }
+        }
+        for (int a = 0; a < nshl; ++a) {
+            const int i = 5 * a, n = ie[a];
+            for (int j = 0; j < nedof; ++j)
+                for (int g = 0; g < 5; ++g) {
+                    double v = E(j, i + g);
+                    for (int cc = 0; cc < g; ++cc) v = v - B(n, cc, g) * E(j, i + cc);
+                    E(j, i + g) = B(n, g, g) * v;
+                }
+        }
+    }
+}
+
+// Au1GMR (au1gmr.f:1-60) with AsAuGMR (asaugmr.f) and localt (localt.f), then bc3per:
+// p <- sum_e EGmass_e p_e with the periodic gather p(iper) first
+void or_au1gmr(const or_mesh* m, const int* eid, const double* EG, double* p) {
+    const size_t N = m->nshg, numel = (size_t)m->nelem + m->nhex + m->nwedge;
+    const int nedof = ebe_nedof(*m);
+    const std::vector<int> pos = ebe_pos(*m, eid);
+    std::vector<double> pg(5 * N), q(5 * N, 0.0);
+    for (int k = 0; k < 5; ++k)
+        for (size_t n = 0; n < N; ++n) pg[k * N + n] = p[k * N + m->iper[n]];
+    for (size_t e = 0; e < numel; ++e) {
+        int nshl;
+        const int* ie = ebe_nodes(*m, pos, e, &nshl);
+        auto E = [&](int i, int j) { return EG[e + numel * ((size_t)i + (size_t)nedof * j)]; };
+        double ul[40], ub[40] = {0};
+        for (int b = 0; b < nshl; ++b)
+            for (int k = 0; k < 5; ++k) ul[5 * b + k] = pg[k * N + ie[b]];
+        for (int i = 0; i < 5 * nshl; i += 5)
+            for (int j = 0; j < 5 * nshl; j += 5)
+                for (int r = 0; r < 5; ++r)
+                    ub[i + r] = ub[i + r] + E(i + r, j) * ul[j] + E(i + r, j + 1) * ul[j + 1] +
+                                E(i + r, j + 2) * ul[j + 2] + E(i + r, j + 3) * ul[j + 3] +
+                                E(i + r, j + 4) * ul[j + 4];
+        for (int a = 0; a < nshl; ++a)
+            for (int k = 0; k < 5; ++k) q[k * N + ie[a]] = q[k * N + ie[a]] + ub[5 * a + k];
+    }
+    for (size_t j = 0; j < N; ++j)
+        if (btest(m->iBC[j], 10)) {
+            const int i = m->iper[j];
+            for (int k = 0; k < 5; ++k) {
+                q[k * N + i] = q[k * N + i] + q[k * N + j];
+                q[k * N + j] = zero;
+            }
+        }
+    std::memcpy(p, q.data(), sizeof(double) * 5 * N);
+}
+
+// SolGMRe (solgmr.f:1-245): ElmGMRe, i3LU, i3pre, GMRES with element-by-element products;
+// restarts from the true residual, convergence without the minIters test
+void or_solgmre(or_common* c, const or_mesh* m, const int* eid, const double* y, const double* ac, double* res,
+                double* bdiag, double* Dy, double* EG, or_solve_stats* st, int nthreads) {
+    const int N = m->nshg;
+    const size_t n5 = 5 * (size_t)N;
+    const int K = c->Kspace;
+    std::vector<double> temp(n5), uB(n5 * (K + 1));
+    std::vector<double> H((K + 1) * K, 0.0), eB(K + 1, 0.0), yB(K, 0.0), Rc(K, 0.0), Rs(K, 0.0);
+    auto Hm = [&](int i, int j) -> double& { return H[(size_t)(i - 1) + (size_t)(K + 1) * (j - 1)]; };
+    auto U = [&](int j) { return uB.data() + n5 * (size_t)(j - 1); };
+    or_elmgmre(c, m, eid, y, ac, res, bdiag, EG, nthreads);
+    or_i3lu(N, bdiag, nullptr, 0);
+    or_i3lu(N, bdiag, res, 1);
+    std::fill(Dy, Dy + n5, 0.0);
+    or_i3pre(m, eid, bdiag, EG);
+    std::memcpy(U(1), res, sizeof(double) * n5);
+    double unorm = std::sqrt(sumsq(res, n5));
+    st->unorm0 = unorm;
+    int iKs = 0, lGMRES = 0;
+    double echeck = 0.0;
+    if (!(unorm < 100. * c->epsM * c->epsM)) {
+        const double epsnrm = c->etol * unorm;
+        for (int mG = 1; mG <= c->nGMRES; ++mG) {
+            lGMRES = mG - 1;
+            if (lGMRES > 0) {
+                std::memcpy(temp.data(), Dy, sizeof(double) * n5);
+                or_au1gmr(m, eid, EG, temp.data());
+                for (size_t i = 0; i < n5; ++i) temp[i] = res[i] - temp[i];
+                std::memcpy(U(1), temp.data(), sizeof(double) * n5);
+                unorm = std::sqrt(sumsq(temp.data(), n5));
+            }
+            std::fill(eB.begin(), eB.end(), 0.0);
+            eB[0] = unorm;
+            for (size_t i = 0; i < n5; ++i) U(1)[i] = U(1)[i] / unorm;
+            for (int iK = 1; iK <= K; ++iK) {
+                iKs = iK;
+                std::memcpy(U(iKs + 1), U(iKs), sizeof(double) * n5);
+                or_au1gmr(m, eid, EG, U(iKs + 1));
+                double beta = 0.0;
+                for (int jK = 1; jK <= iKs + 1; ++jK) {
+                    double* w = U(iKs + 1);
+                    if (jK == 1) {
+                        beta = dot(w, U(1), n5);
+                    } else {
+                        const double* up = U(jK - 1);
+                        for (size_t i = 0; i < n5; ++i) w[i] = w[i] - beta * up[i];
+                        beta = dot(w, U(jK), n5);
+                    }
+                    Hm(jK, iKs) = beta;
+                }
+                unorm = std::sqrt(beta);
+                Hm(iKs + 1, iKs) = unorm;
+                for (size_t i = 0; i < n5; ++i) U(iKs + 1)[i] = U(iKs + 1)[i] / unorm;
+                for (int jK = 1; jK <= iKs - 1; ++jK) {
+                    const double t = Rc[jK - 1] * Hm(jK, iKs) + Rs[jK - 1] * Hm(jK + 1, iKs);
+                    Hm(jK + 1, iKs) = -Rs[jK - 1] * Hm(jK, iKs) + Rc[jK - 1] * Hm(jK + 1, iKs);
+                    Hm(jK, iKs) = t;
+                }
+                const double t = std::sqrt(Hm(iKs, iKs) * Hm(iKs, iKs) + Hm(iKs + 1, iKs) * Hm(iKs + 1, iKs));
+                Rc[iKs - 1] = Hm(iKs, iKs) / t;
+                Rs[iKs - 1] = Hm(iKs + 1, iKs) / t;
+                Hm(iKs, iKs) = t;
+                Hm(iKs + 1, iKs) = zero;
+                const double te = Rc[iKs - 1] * eB[iKs - 1] + Rs[iKs - 1] * eB[iKs];
+                eB[iKs] = -Rs[iKs - 1] * eB[iKs - 1] + Rc[iKs - 1] * eB[iKs];
+                eB[iKs - 1] = te;
+                st->ntotGM += 1;
+                echeck = std::fabs(eB[iKs]);
+                if (echeck <= epsnrm) break;
+            }
+            for (int jK = iKs; jK >= 1; --jK) {
+                yB[jK - 1] = eB[jK - 1] / Hm(jK, jK);
+                for (int lK = 1; lK <= jK - 1; ++lK) eB[lK - 1] = eB[lK - 1] - yB[jK - 1] * Hm(lK, jK);
+            }
+            for (int jK = 1; jK <= iKs; ++jK) {
+                const double* uj = U(jK);
+                for (size_t i = 0; i < n5; ++i) Dy[i] = Dy[i] + yB[jK - 1] * uj[i];
+            }
+            echeck = std::fabs(eB[iKs]);
+            if (echeck <= epsnrm) break;
+        }
+    }
+    or_i3lu(N, bdiag, Dy, 2);
+    st->iKs = iKs;
+    st->lGMRES = lGMRES;
     st->echeck = echeck;
     st->eGMRES = c->eGMRES;
     st->totres = std::sqrt(sumsq(res, n5)) / (double)N;

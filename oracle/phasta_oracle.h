@@ -141,6 +141,18 @@ void or_solgmrs(or_common* c, const or_mesh* m, const int* colm, const int* rowp
                 const double* y, const double* ac, double* res, double* bdiag, double* Dy, double* lhsK,
                 or_solve_stats* st, int nthreads);
 
+/* element-by-element solver (impl = 3x) on single-topology meshes.  EG is the reference's
+ * EGmass(numel, nedof, nedof) column-major, elements in block order (tets in input order:
+ * eid[e] = input id of the oracle's element e, NULL = identity; then hexes, wedges),
+ * nedof = 5 x (nodes per element). */
+void or_elmgmre(const or_common* c, const or_mesh* m, const int* eid, const double* y, const double* ac,
+                double* res, double* bdiag, double* EG, int nthreads);
+void or_i3pre(const or_mesh* m, const int* eid, const double* bd, double* EG);
+/* Au1GMR (au1gmr.f) then bc3per: p <- sum_e EGmass_e p_e */
+void or_au1gmr(const or_mesh* m, const int* eid, const double* EG, double* p);
+void or_solgmre(or_common* c, const or_mesh* m, const int* eid, const double* y, const double* ac, double* res,
+                double* bdiag, double* Dy, double* EG, or_solve_stats* st, int nthreads);
+
 /* itrPC.f */
 void or_itrpredict(const or_common* c, int nshg, const double* yold, const double* acold,
                    double* y, double* ac);

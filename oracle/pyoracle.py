@@ -74,6 +74,10 @@ def lib():
             "or_sparseap": ([mp, _ip, _ip, _dp, _dp], None),
             "or_solgmrs": ([cp, mp, _ip, _ip, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(OStats), C.c_int],
                            None),
+            "or_elmgmre": ([cp, mp, _ip, _dp, _dp, _dp, _dp, _dp, C.c_int], None),
+            "or_i3pre": ([mp, _ip, _dp, _dp], None),
+            "or_au1gmr": ([mp, _ip, _dp, _dp], None),
+            "or_solgmre": ([cp, mp, _ip, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(OStats), C.c_int], None),
             "or_itrpredict": ([cp, C.c_int, _dp, _dp, _dp, _dp], None),
             "or_itrcorrect": ([cp, C.c_int, _dp, _dp, _dp, _dp, _dp], None),
             "or_itrupdate": ([cp, C.c_int, _dp, _dp, _dp, _dp], None),
@@ -159,6 +163,7 @@ class Oracle:
                                        _i(grp), 1024)
             assert ng > 0
             ien = np.ascontiguousarray(ien[perm])
+            self._eid = np.ascontiguousarray(perm, dtype=np.int32)
             self._blk = np.ascontiguousarray(blk[: nb.value + 1])
             self._grp = np.ascontiguousarray(grp[: ng + 1])
             ngrp = ng
@@ -167,6 +172,7 @@ class Oracle:
             self._blk = np.minimum(np.arange(nb + 1, dtype=np.int32) * bksiz, E).astype(np.int32)
             self._grp = np.zeros(1, np.int32)
             ngrp = 0
+            self._eid = np.arange(E, dtype=np.int32)
         self._ien = ien.reshape(-1)
         self._x = case.x_ref()
         self._ienb = np.ascontiguousarray(case.ienb, dtype=np.int32).reshape(-1)
@@ -287,6 +293,39 @@ class Oracle:
         self.ntotGM = st.ntotGM
         return res, bd, Dy, lhsK, OracleStats(st.iKs, st.lGMRES, st.ntotGM, st.unorm0, st.echeck, st.eGMRES,
                                               st.totres)
+
+    # ---- element-by-element solver: EG (numel, nedof, nedof) = the reference's EGmass
+    def _eg(self):
+        n = self.case.nelem + self.case.nhex + self.case.nwedge
+        nd = 40 if self.case.nhex else 30 if self.case.nwedge else 20
+        return np.zeros((nd, nd, n))  # C order (j, i, e) = Fortran (e, i, j)
+
+    def ElmGMRe(self, y, ac):
+        res, bd, EG = self._v(), self._v(25), self._eg()
+        self.L.or_elmgmre(C.byref(self.c), C.byref(self.m), _i(self._eid), _d(y), _d(ac), _d(res), _d(bd), _d(EG),
+                          self.nthreads)
+        return res, bd, EG.transpose(2, 1, 0)
+
+    def i3pre(self, lu, EG):
+        out = np.ascontiguousarray(np.asarray(EG).transpose(2, 1, 0))
+        self.L.or_i3pre(C.byref(self.m), _i(self._eid), _d(np.ascontiguousarray(lu, dtype=np.float64)), _d(out))
+        return out.transpose(2, 1, 0)
+
+    def Au1GMR(self, EG, p):
+        p = np.array(p, dtype=np.float64)
+        eg = np.ascontiguousarray(np.asarray(EG).transpose(2, 1, 0))
+        self.L.or_au1gmr(C.byref(self.m), _i(self._eid), _d(eg), _d(p))
+        return p
+
+    def SolGMRe(self, y, ac):
+        res, bd, Dy, EG = self._v(), self._v(25), self._v(), self._eg()
+        st = OStats()
+        st.ntotGM = self.ntotGM
+        self.L.or_solgmre(C.byref(self.c), C.byref(self.m), _i(self._eid), _d(y), _d(ac), _d(res), _d(bd), _d(Dy),
+                          _d(EG), C.byref(st), self.nthreads)
+        self.ntotGM = st.ntotGM
+        return res, bd, Dy, EG.transpose(2, 1, 0), OracleStats(st.iKs, st.lGMRES, st.ntotGM, st.unorm0, st.echeck,
+                                                               st.eGMRES, st.totres)
 
     def itrPredict(self, yold, acold):
         y, ac = self._v(), self._v()

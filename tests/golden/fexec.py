@@ -752,7 +752,8 @@ class _Poison:
     def __getitem__(self, k):
         raise FortranUnsupported(f"access to an unassociated array argument ({self.what})")
 
-    __setitem__ = __getitem__
+    def __setitem__(self, k, v):
+        raise FortranUnsupported(f"store to an unassociated array argument ({self.what})")
 
 
 def _view(x, shape, wb, dtype):

@@ -29,21 +29,28 @@ DEFAULT_REF = Path("/root/reference/phSolver")
 
 # (name, case builder, parts): "elm" ElmMFG; "pieces" ItrRes, i3LU, itrBC; "solve" SolMFG;
 # "step" itrSetup and one two-iteration time step; "sparse" genadj, ElmGMRs (assembled
-# tangent lhsK), Spsi3pre, SparseAp and SolGMRs
+# tangent lhsK), Spsi3pre, SparseAp and SolGMRs; "ebe" ElmGMRe (element tangents, stored as
+# products with seeded probe vectors), i3pre, Au1GMR and SolGMRe -- on single-topology
+# meshes only: with blocks of fewer nodes than the largest element, i3pre gathers BDiag
+# through a section of its (numel, nshape, 5, 5) array into local's (npro, nshl, 25) dummy
+# (i3pre.f), which scrambles the blocks of the smaller elements
 ALL = ("elm", "pieces", "solve", "step")
 CASES = [
-    ("channel4", lambda: channel(4, ac_scale=0.05), ALL + ("sparse",)),
-    ("vortex4", lambda: vortex(4), ALL + ("sparse",)),
+    ("channel4", lambda: channel(4, ac_scale=0.05), ALL + ("sparse", "ebe")),
+    ("vortex4", lambda: vortex(4), ALL + ("sparse", "ebe")),
     ("channel3_euler", lambda: channel(3, ac_scale=0.05, navier=0), ("elm",)),
     ("channel3_galerkin", lambda: channel(3, ac_scale=0.05, ivart=1), ("elm",)),
     # Kspace 3 with two cycles: the second cycle restarts from Au2MFG's R - J Dy
     # (SolGMRs restarts from its stale first vector: its test reads lGMRES, solgmr.f:528)
-    ("channel4_restart", lambda: channel(4, ac_scale=0.05, Kspace=3, nGMRES=2), ("elm", "solve", "sparse")),
+    ("channel4_restart", lambda: channel(4, ac_scale=0.05, Kspace=3, nGMRES=2), ("elm", "solve", "sparse", "ebe")),
     # tet, hex (lcsyst 2) and wedge (lcsyst 3) blocks
     ("mixed3", lambda: mixed(3, 3, (3, 3, 2)), ALL + ("sparse",)),
     # idiff = 1: the diffusive flux reconstructed (AsIq/e3q/qpbc) and its divergence in e3LS
     ("channel4_idiff", lambda: channel(4, ac_scale=0.05, idiff=1), ALL),
     ("mixed3_idiff", lambda: mixed(3, 3, (3, 3, 2), idiff=1), ("elm", "solve")),
+    # single-topology hex and wedge meshes (periodic boxes)
+    ("hex3", lambda: mixed(0, 3, 0), ("elm", "sparse", "ebe")),
+    ("wedge3", lambda: mixed(0, 0, (3, 3, 2)), ("elm", "sparse", "ebe")),
 ]
 
 
@@ -99,6 +106,20 @@ def make(name, build, parts, ref_root):
         sres, sbd, sDy, _, st = R4.SolGMRs(y, ac, y, ac)
         out.update(sps_res=sres, sps_bd=sbd, sps_Dy=sDy, sps_iKs=np.array(st["iKs"]),
                    sps_lGMRES=np.array(st["lGMRES"]), sps_ntotGM=np.array(st["ntotGM"]))
+    if "ebe" in parts:
+        R5 = RefPhasta(case, p, ref_root)
+        eres, ebd, EG = R5.ElmGMRe(y, ac)
+        rng = np.random.default_rng(13)
+        v = rng.standard_normal(EG.shape[:2])
+        lu, _ = R5.i3LU(ebd, None, 0)
+        pre = R5.i3pre(lu, EG)
+        pv = rng.standard_normal(5 * case.nshg)
+        out.update(ebe_res=eres, ebe_bd=ebd, ebe_v=v, ebe_EGv=np.einsum("eij,ej->ei", EG, v), ebe_lu=lu,
+                   ebe_prev=np.einsum("eij,ej->ei", pre, v), ebe_p=pv, ebe_ap=R5.Au1GMR(pre, pv))
+        R6 = RefPhasta(case, p, ref_root)
+        sres, sbd, sDy, _, st = R6.SolGMRe(y, ac, y, ac)
+        out.update(ebe_sres=sres, ebe_sbd=sbd, ebe_Dy=sDy, ebe_iKs=np.array(st["iKs"]),
+                   ebe_lGMRES=np.array(st["lGMRES"]), ebe_ntotGM=np.array(st["ntotGM"]))
     path = HERE / f"ref_{name}.npz"
     np.savez_compressed(path, **out)
     print(f"{path.name}: {path.stat().st_size // 1024} KiB, nshg {case.nshg}, nelem {case.nelem}")

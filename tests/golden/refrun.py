@@ -43,6 +43,8 @@ SOURCES = [
     "compressible/elmgmr.f", "compressible/asigmr.f", "compressible/e3massl.f", "compressible/bc3lhs.f",
     "common/fillsparse.f", "common/genadj.f", "common/asadj.f", "compressible/spsi3pre.f",
     "compressible/sparseap.f", "compressible/solgmr.f",
+    # element-by-element solver: ElmGMRe, i3pre, Au1GMR/AsAuGMR/localt, SolGMRe
+    "compressible/i3pre.f", "compressible/au1gmr.f", "compressible/asaugmr.f", "compressible/localt.f",
 ]
 # rstat.f only prints statistics, and SolMFG calls it with two of its three
 # arguments (solmfg.f:367 vs rstat.f:1); its totres (rstat.f:108) is computed
@@ -98,10 +100,12 @@ class RefPhasta:
         G.numpe, G.myrank, G.master = 1, 0, 0
         G.numnp = G.nshg = N
         G.nshgt = N
-        G.numel, G.numelb = E, Eb
+        # numel counts the interior elements of every block (EGmass(numel, nedof, nedof) of SolGMRe)
+        G.numel, G.numelb = E + case.nhex + case.nwedge, Eb
         # nen is the largest element of the mesh (readnblk.f) and nedof = nflow*nshape (itrdrv.f:458)
         nenmax = max(nshl for _c, _l, nshl, _q in blocks)
         G.nen, G.ndof, G.nflow, G.nedof = nenmax, 5, 5, 5 * nenmax
+        G.nshape = nenmax  # linear basis: nshape = nen (genint.f)
         G.ndofbc, G.ndibcb, G.ndbcb = 6, 2, 6
         G.nelblk, G.nelblb = len(blocks), (1 if Eb else 0)
         # lcblk(:,iblk): iel, lelCat, lcsyst, iorder, nenl, -, mattyp, ndofl, nsymdl, nshl
@@ -323,3 +327,55 @@ class RefPhasta:
         self.P.call("sparseap", self.iper, self.ilwork, self.iBC, self.colm, self.rowp, np.asfortranarray(lhsK), pF)
         self.P.call("bc3per", self.iBC, pF, self.iper, self.ilwork, 5)
         return pF.reshape(-1, order="F")
+
+    # ---- element-by-element solver (impl = 3x): EGmass(numel, nedof, nedof) stored per element
+    def _egmass(self):
+        G = self.G
+        return np.zeros((int(G.numel), int(G.nedof), int(G.nedof)), order="F")
+
+    def ElmGMRe(self, y, ac):
+        """res, BDiag and the element tangents EGmass (after bc3LHS) of ElmGMRe (elmgmr.f:1)."""
+        N = self.N
+        G = self.G
+        G.lhs, G.iprec = 1, 1
+        EG = self._egmass()
+        res, rmes = np.zeros((N, 5), order="F"), np.zeros((N, 5), order="F")
+        bd = np.zeros((N, 5, 5), order="F")
+        self.P.call("elmgmre", _F(np.array(y), (N, 5)), _F(np.array(ac), (N, 5)), self.x, self.shp, self.shgl,
+                    self.iBC, self.BC, self.shpb, self.shglb, res, rmes, bd, self.iper, self.ilwork, EG, self.rerr)
+        G.lhs = 0
+        return res.reshape(-1, order="F"), bd.reshape(-1, order="F"), EG
+
+    def i3pre(self, lu, EG):
+        """EGmass after i3pre (i3pre.f:1) with the i3LU factors lu."""
+        N = self.N
+        bdF = _F(np.array(lu), (N, 5, 5)).copy(order="F")
+        out = np.array(EG, order="F", copy=True)
+        self.P.call("i3pre", bdF, np.zeros(1), out, self.ilwork)
+        return out
+
+    def Au1GMR(self, EG, p):
+        """The element-by-element product of Au1GMR (au1gmr.f:1), then bc3per as SolGMRe applies it."""
+        N = self.N
+        pF = _F(np.array(p), (N, 5)).copy(order="F")
+        self.P.call("au1gmr", np.asfortranarray(EG), pF, self.ilwork, self.iBC, self.iper)
+        self.P.call("bc3per", self.iBC, pF, self.iper, self.ilwork, 5)
+        return pF.reshape(-1, order="F")
+
+    def SolGMRe(self, y, ac, yold, acold):
+        N, K = self.N, self.params["Kspace"]
+        G = self.G
+        G.lhs, G.iprec = 1, 1
+        EG = self._egmass()
+        res = np.zeros((N, 5), order="F")
+        bd = np.zeros((N, 5, 5), order="F")
+        Dy = np.zeros((N, 5), order="F")
+        HBrg = np.zeros((K + 1, K), order="F")
+        eBrg, yBrg = np.zeros(K + 1), np.zeros(K)
+        Rcos, Rsin = np.zeros(K), np.zeros(K)
+        self.P.call("solgmre", _F(np.array(y), (N, 5)), _F(np.array(ac), (N, 5)), _F(np.array(yold), (N, 5)),
+                    _F(np.array(acold), (N, 5)), self.x, self.iBC, self.BC, EG, res, bd, HBrg, eBrg, yBrg, Rcos,
+                    Rsin, self.iper, self.ilwork, self.shp, self.shgl, self.shpb, self.shglb, Dy, self.rerr)
+        G.lhs = 0
+        stats = {"iKs": int(G.iks), "lGMRES": int(G.lgmres), "ntotGM": int(G.ntotgm)}
+        return res.reshape(-1, order="F"), bd.reshape(-1, order="F"), Dy.reshape(-1, order="F"), EG, stats

@@ -133,3 +133,31 @@ def test_oracle_solgmrs_matches_reference(name):
     assert rel(lhsK, d["sp_pre"].T) < 1e-12
     assert (st.iKs, st.lGMRES, st.ntotGM) == (int(d["sps_iKs"]), int(d["sps_lGMRES"]), int(d["sps_ntotGM"]))
     assert rel(Dy, d["sps_Dy"]) < 1e-9
+
+
+# ---- element-by-element solver: EGmass is stored as products with seeded probe vectors
+def _probe(EG, v):
+    return np.einsum("eij,ej->ei", EG, v)
+
+
+@pytest.mark.parametrize("name", having("ebe"))
+def test_oracle_elmgmre_i3pre_au1gmr_match_reference(name):
+    d, case, p = load(name)
+    o = pyoracle.Oracle(case, p)
+    res, bd, EG = o.ElmGMRe(d["y"], d["ac"])
+    assert rel(res, d["ebe_res"]) < 1e-12 and rel(bd, d["ebe_bd"]) < 1e-12
+    assert rel(_probe(EG, d["ebe_v"]), d["ebe_EGv"]) < 1e-12
+    pre = o.i3pre(d["ebe_lu"], EG)
+    assert rel(_probe(pre, d["ebe_v"]), d["ebe_prev"]) < 1e-12
+    # the golden product was formed from the reference's own preconditioned EGmass
+    assert rel(o.Au1GMR(pre, d["ebe_p"]), d["ebe_ap"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", having("ebe"))
+def test_oracle_solgmre_matches_reference(name):
+    d, case, p = load(name)
+    o = pyoracle.Oracle(case, p)
+    res, bd, Dy, EG, st = o.SolGMRe(d["y"], d["ac"])
+    assert rel(res, d["ebe_sres"]) < 1e-12 and rel(bd, d["ebe_sbd"]) < 1e-12
+    assert (st.iKs, st.lGMRES, st.ntotGM) == (int(d["ebe_iKs"]), int(d["ebe_lGMRES"]), int(d["ebe_ntotGM"]))
+    assert rel(Dy, d["ebe_Dy"]) < 1e-9
