@@ -50,9 +50,10 @@ enum {
 };
 
 enum { PHGPU_FP64 = 0, PHGPU_MIXED = 1 };         /* precision */
-/* Jacobian-vector product: finite-differenced (Au1MFG), linearized, or the assembled
- * tangent of the sparse solver (SolGMRs, solgmr.f:480) */
-enum { PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1, PHGPU_AP_SPARSE = 2 };
+/* Jacobian-vector product: finite-differenced (Au1MFG), linearized, the assembled tangent
+ * of the sparse solver (SolGMRs, solgmr.f:480) or the stored element tangents of the
+ * element-by-element solver (SolGMRe, solgmr.f:1) */
+enum { PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1, PHGPU_AP_SPARSE = 2, PHGPU_AP_EBE = 3 };
 enum { PHGPU_RES_FP64 = 0, PHGPU_RES_GALERKIN64 = 1, PHGPU_RES_SPLITDF = 2 }; /* outer residual in mixed precision */
 enum { PHGPU_LU_FACT = 0, PHGPU_LU_FORWARD = 1, PHGPU_LU_BACKWARD = 2, PHGPU_LU_PRODUCT = 3 };
 
@@ -77,8 +78,9 @@ typedef struct {
     /* options of this implementation */
     int precision;                   /* PHGPU_FP64: reference arithmetic; PHGPU_MIXED: FP32
                                         assembly and Ap, FP64 outer residual, dots, Givens, LU */
-    int ap_mode;                     /* PHGPU_AP_FD (Au1MFG), PHGPU_AP_LINEAR or PHGPU_AP_SPARSE
-                                        (the drivers then solve with SolGMRs, lhs = 1) */
+    int ap_mode;                     /* PHGPU_AP_FD (Au1MFG), PHGPU_AP_LINEAR, PHGPU_AP_SPARSE or
+                                        PHGPU_AP_EBE (the drivers then solve with SolGMRs or
+                                        SolGMRe, lhs = 1) */
     int outer_residual;              /* mixed precision only: PHGPU_RES_FP64 (every term FP64),
                                         PHGPU_RES_GALERKIN64 (metrics, Euler flux and time term FP64;
                                         least-squares and viscous terms FP32) or PHGPU_RES_SPLITDF
@@ -186,6 +188,25 @@ int phgpu_sparseap(phgpu_ctx* ctx, const double* lhsK, double* p);
  * (solgmr.f:528, never set by SolGMRs itself); on return, the cycles done less one. */
 int phgpu_solgmrs(phgpu_ctx* ctx, const double* y, const double* ac, int lhs, double* res,
                   double* bdiag, double* Dy, double* lhsK, phgpu_stats* st);
+
+/* ---- element-by-element solver: the reference's impl = 3x path (itrdrv.f:507-526) ----
+ * Only for meshes of one element topology (all tets, all hexes or all wedges): the
+ * reference's i3pre gathers BDiag through a section of its (numel, nshape, 5, 5) array into
+ * a (npro, nshl, 25) dummy, which scrambles the blocks of elements smaller than the largest
+ * one; mixed meshes return PHGPU_ERR_UNSUPPORTED.  EGmass is the reference's
+ * EGmass(numel, nedof, nedof) (FP64, column-major, elements in input order, nedof = 5 x
+ * nodes per element). */
+/* ElmGMRe (elmgmr.f:1) with lhs = 1, iprec = 1: res, BDiag and EGmass after bc3LHS */
+int phgpu_elmgmre(phgpu_ctx* ctx, const double* y, const double* ac, double* res, double* bdiag,
+                  double* EGmass);
+/* i3pre (i3pre.f:1) on host arrays; bdiag holds the i3LU factors */
+int phgpu_i3pre(phgpu_ctx* ctx, const double* bdiag, double* EGmass);
+/* Au1GMR (au1gmr.f:1) then bc3per (bc3per.f:1), as SolGMRe applies them: p <- sum_e EGmass_e p */
+int phgpu_au1gmr(phgpu_ctx* ctx, const double* EGmass, double* p);
+/* SolGMRe (solgmr.f:1) in the configured precision; outputs as phgpu_solmfg, plus the
+ * preconditioned EGmass (FP64 solves; may be NULL) */
+int phgpu_solgmre(phgpu_ctx* ctx, const double* y, const double* ac, double* res, double* bdiag,
+                  double* Dy, double* EGmass, phgpu_stats* st);
 
 /* device-resident state (no host traffic inside) */
 int phgpu_upload_state(phgpu_ctx* ctx, const double* y, const double* ac,

@@ -152,6 +152,7 @@ class Oracle:
         self.nthreads = nthreads
         self.nshg = case.nshg
         grouped = nthreads > 1 if grouped is None else grouped
+        grouped = grouped and case.nelem > 0  # the groups order the tet block
         ien = np.ascontiguousarray(case.ien, dtype=np.int32)
         E = ien.shape[0]
         if grouped:

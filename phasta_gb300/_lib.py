@@ -15,9 +15,9 @@ LIB_PATH = Path(__file__).resolve().parent / "libphgpu.so"
 PHGPU_OK = 0
 STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NONFINITE", 4: "SINGULAR", 5: "UNSUPPORTED", 6: "NOMEM", 7: "TOO_LARGE"}
 PHGPU_FP64, PHGPU_MIXED = 0, 1
-PHGPU_AP_FD, PHGPU_AP_LINEAR, PHGPU_AP_SPARSE = 0, 1, 2
+PHGPU_AP_FD, PHGPU_AP_LINEAR, PHGPU_AP_SPARSE, PHGPU_AP_EBE = 0, 1, 2, 3
 PHGPU_RES_FP64, PHGPU_RES_GALERKIN64, PHGPU_RES_SPLITDF = 0, 1, 2
-PHGPU_ERR_INVALID, PHGPU_ERR_TOO_LARGE = 1, 7
+PHGPU_ERR_INVALID, PHGPU_ERR_UNSUPPORTED, PHGPU_ERR_TOO_LARGE = 1, 5, 7
 PHGPU_RSTAT_NOALLOC_MAX_N = 33554432
 LU_FACT, LU_FORWARD, LU_BACKWARD, LU_PRODUCT = 0, 1, 2, 3
 
@@ -100,6 +100,10 @@ def lib():
         "phgpu_spsi3pre": ([vp, _dp, _dp], C.c_int),
         "phgpu_sparseap": ([vp, _dp, _dp], C.c_int),
         "phgpu_solgmrs": ([vp, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(Stats)], C.c_int),
+        "phgpu_elmgmre": ([vp, _dp, _dp, _dp, _dp, _dp], C.c_int),
+        "phgpu_i3pre": ([vp, _dp, _dp], C.c_int),
+        "phgpu_au1gmr": ([vp, _dp, _dp], C.c_int),
+        "phgpu_solgmre": ([vp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(Stats)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

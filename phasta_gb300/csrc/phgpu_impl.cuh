@@ -73,6 +73,15 @@ struct SparseCtx {
     double* d_lhsK = nullptr;     // 25 * nnzb, the reference's lhsK(25, nnz_tot) layout
     float* d_lhsKf = nullptr;     // FP32 tangent of the mixed-precision solve
     int have = -1;                // precision of the preconditioned tangent kept from the last lhs = 1 solve
+    // element colouring of the tet tangent (shared with the element-by-element solver)
+    bool tan_ready = false;
+    std::vector<int> torder;      // tangent position -> input tet
+    std::vector<int> h_ient;      // tets in tangent order (host copy of d_ient)
+    // element-by-element solver: per element its NEN x NEN blocks (25 values, entry (f, g) at
+    // 5 g + f), elements in tangent order (tets), d_ienh order (hexes) or d_ienw order (wedges)
+    size_t eg_blocks = 0;
+    double* d_EG = nullptr;
+    float* d_EGf = nullptr;
 };
 
 struct Ctx {
@@ -92,6 +101,7 @@ struct Ctx {
     int* d_ienh = nullptr;        // nhex*8
     int* d_ienw = nullptr;        // nwedge*6
     std::vector<int> hcol_start, wcol_start;
+    std::vector<int> horder, worder;  // colour position -> input hex / wedge
     // chunks (chunks.cu)
     int nchunk = 0, chunk_lmax = 0;
     std::vector<int> chunk_col_start;  // chunk colours
@@ -226,6 +236,12 @@ template <typename V> void scale_by(Ctx& C, V* w, const double* s, int mode, siz
 void block_adjacency(int N, const int* ien, int ne, const int* ienh, int nh, const int* ienw, int nw,
                      std::vector<int>& colm, std::vector<int>& rowp);
 int sparse_setup(Ctx& C);
+int ebe_setup(Ctx& C);    // PHGPU_ERR_UNSUPPORTED unless the mesh has one element topology
+// element tangents stored per element (ElmGMRe), bd += their diagonal blocks
+template <typename R> void launch_tangent_ebe(Ctx& C, const R* x, const R* y, R* EG, R* bd);
+template <typename R> void i3pre(Ctx& C, const R* bd, R* EG);
+// Au1GMR + bc3per: q = sum_e EG_e p(iper)
+template <typename M, typename V> void ebe_ap(Ctx& C, const M* EG, const V* p, V* q);
 template <typename R> void launch_tangent(Ctx& C, const R* x, const R* y, R* lhsK, R* bd = nullptr);
 void upload_tangent_tables(Ctx& C);
 int configure_tangent_kernels(Ctx& C);

@@ -277,11 +277,16 @@ int elmmfg64(Ctx& C, const double* y, const double* ac, double* res, double* rme
     return check(C, cudaGetLastError(), "elmmfg");
 }
 
-// the FP64 tangent of ElmGMRs (lhs = 1): lhsK, and BDiag from its diagonal blocks + bc3BDg
-int tangent64(Ctx& C, const double* y, double* lhsK, double* bd) {
-    fill0(C, lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb);
+// the FP64 tangent of ElmGMRs (lhs = 1: lhsK) or ElmGMRe (ebe: element storage), and BDiag
+// from its diagonal blocks + bc3BDg
+int tangent64(Ctx& C, const double* y, double* out, double* bd, bool ebe = false) {
     fill0(C, bd, sizeof(double) * 25 * (size_t)C.N);
-    launch_tangent<double>(C, C.d_x, y, lhsK, bd);
+    if (ebe) {
+        launch_tangent_ebe<double>(C, C.d_x, y, out, bd);
+    } else {
+        fill0(C, out, sizeof(double) * 25 * (size_t)C.sp.nnzb);
+        launch_tangent<double>(C, C.d_x, y, out, bd);
+    }
     bc3bdg<double>(C, y, bd);
     return check(C, cudaGetLastError(), "tangent");
 }
@@ -418,13 +423,27 @@ int itrfdi_dev(Ctx& C, const double* rmes, const double* ubrg) {
 template <typename V> V* sparse_lhs(Ctx& C);
 template <> double* sparse_lhs<double>(Ctx& C) { return C.sp.d_lhsK; }
 template <> float* sparse_lhs<float>(Ctx& C) { return C.sp.d_lhsKf; }
+template <typename V> V* ebe_lhs(Ctx& C);
+template <> double* ebe_lhs<double>(Ctx& C) { return C.sp.d_EG; }
+template <> float* ebe_lhs<float>(Ctx& C) { return C.sp.d_EGf; }
+
+// q = A p for the assembled (SparseAp) or element-by-element (Au1GMR) operator, then bc3per
+template <typename V>
+void assembled_ap(Ctx& C, bool ebe, const V* p, V* q) {
+    if (ebe) ebe_ap<V, V>(C, ebe_lhs<V>(C), p, q);
+    else sparse_ap<V, V>(C, sparse_lhs<V>(C), p, q);
+}
 
 // GMRES cycles on V-typed Krylov vectors; b (= L^-1 R, FP64) in d_res, output Dy (FP64, before U^-1).
 // ap_mode PHGPU_AP_SPARSE: the product is SparseAp + bc3per on the preconditioned tangent, and a
 // new cycle recomputes R - A Dy only when lgmres_common > 0 (SolGMRs, solgmr.f:526-537)
 template <typename V>
 int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
-    const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE;
+    // SolGMRe restarts from the true residual and stops without the minIters test (solgmr.f:130-210)
+    const bool ebe = C.cfg.ap_mode == PHGPU_AP_EBE;
+    const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE || ebe;
+    if (ebe) lgmres_common = 1;
+    const int min_iters = ebe ? 0 : C.cfg.minIters;
     const size_t n5 = 5 * (size_t)C.N;
     const int K = C.cfg.Kspace;
     V* U = (V*)C.d_U;
@@ -462,12 +481,12 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
         } else if (mG > 1 && sparse) {
             V* t = Uj(1);
             if constexpr (std::is_same<V, double>::value) {
-                sparse_ap<double, double>(C, C.sp.d_lhsK, C.d_Dy, t);
+                assembled_ap<double>(C, ebe, C.d_Dy, t);
                 k_axpby<<<kVG, kVT, 0, C.stream>>>(C.d_res, 1.0, t, -1.0, t, n5);
                 ++C.launches;
             } else {
                 to_f32(C, C.d_Dy, C.d_t32b, n5);
-                sparse_ap<float, float>(C, C.sp.d_lhsKf, C.d_t32b, C.d_t32);
+                assembled_ap<float>(C, ebe, C.d_t32b, C.d_t32);
                 to_f64(C, C.d_t32, C.d_t64b, n5);
                 k_axpby<<<kVG, kVT, 0, C.stream>>>(C.d_res, 1.0, C.d_t64b, -1.0, C.d_t64b, n5);
                 ++C.launches;
@@ -512,7 +531,7 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
             iKs = iK;
             V* w = Uj(iKs + 1);
             if (sparse) {
-                sparse_ap<V, V>(C, sparse_lhs<V>(C), Uj(iKs), w);
+                assembled_ap<V>(C, ebe, Uj(iKs), w);
             } else {
                 k_copy<V><<<kVG, kVT, 0, C.stream>>>(Uj(iKs), w, n5, nullptr);
                 ++C.launches;
@@ -531,7 +550,7 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
                 mgs_step<V>(C, w, up, bprev, Uj(jK), n5, Hcol + (jK - 1), nullptr);
             }
             scale_by<V>(C, w, Hcol + iKs, 1, n5, nullptr);
-            k_givens<<<1, 1, 0, C.stream>>>(s, K, iKs, C.cfg.minIters, C.d_flag);
+            k_givens<<<1, 1, 0, C.stream>>>(s, K, iKs, min_iters, C.d_flag);
             ++C.launches;
             st->ntotGM += 1;
             PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
@@ -557,8 +576,12 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
 // and the preconditioned tangent of the last lhs = 1 solve
 int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
     const size_t N = C.N, n5 = 5 * N;
-    const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE;
-    if (sparse) {
+    const bool ebe = C.cfg.ap_mode == PHGPU_AP_EBE;
+    const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE || ebe;
+    if (ebe) {
+        if (!lhs) return fail(C, PHGPU_ERR_UNSUPPORTED, "the element-by-element solver assembles on every call");
+        PH_TRY(ebe_setup(C));
+    } else if (sparse) {
         PH_TRY(sparse_setup(C));
         if (!lhs && C.sp.have != C.cfg.precision)
             return fail(C, PHGPU_ERR_INVALID, "lhs = 0 needs the tangent of an earlier lhs = 1 solve");
@@ -567,9 +590,9 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
     cudaEventRecord(C.ev[0], C.stream);
     if (C.cfg.precision == PHGPU_FP64) {
         if (sparse) {
-            // ElmGMRs: the residual, and BDiag from the tangent's diagonal blocks
+            // ElmGMRs / ElmGMRe: the residual, and BDiag from the tangent's diagonal blocks
             PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
-            if (lhs) PH_TRY(tangent64(C, C.d_y, C.sp.d_lhsK, C.d_bd));
+            if (lhs) PH_TRY(tangent64(C, C.d_y, ebe ? C.sp.d_EG : C.sp.d_lhsK, C.d_bd, ebe));
         } else {
             PH_TRY(elmmfg64(C, C.d_y, C.d_ac, C.d_res, C.d_rmes, C.d_bd, 1));
         }
@@ -598,7 +621,9 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
         }
         if (asm_bd) {
             fill0(C, C.d_bdf, sizeof(float) * 25 * N);
-            if (sparse) {
+            if (ebe) {
+                launch_tangent_ebe<float>(C, C.d_xf, C.d_yf, C.sp.d_EGf, C.d_bdf);
+            } else if (sparse) {
                 // FP32 tangent; its diagonal blocks are the block diagonal
                 fill0(C, C.sp.d_lhsKf, sizeof(float) * 25 * (size_t)C.sp.nnzb);
                 launch_tangent<float>(C, C.d_xf, C.d_yf, C.sp.d_lhsKf, C.d_bdf);
@@ -618,7 +643,10 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
     }
     lu_apply<double, double>(C, C.d_bd, C.d_res, PHGPU_LU_FORWARD);
     if (sparse) {
-        if (lhs) {
+        if (ebe) {
+            if (C.cfg.precision == PHGPU_FP64) i3pre<double>(C, C.d_bd, C.sp.d_EG);
+            else i3pre<float>(C, C.d_bdf, C.sp.d_EGf);
+        } else if (lhs) {
             if (C.cfg.precision == PHGPU_FP64) spsi3pre<double>(C, C.d_bd, C.sp.d_lhsK);
             else spsi3pre<float>(C, C.d_bdf, C.sp.d_lhsKf);
             C.sp.have = C.cfg.precision;
@@ -653,6 +681,55 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
 }
 
 int solmfg_dev(Ctx& C, phgpu_stats* st) { return solve_dev(C, st, 1, 0); }
+
+// element-by-element storage (device order, [element][a][b][25]) <-> the reference's
+// EGmass(numel, nedof, nedof), column-major, elements in input order (one topology)
+void ebe_shape(const Ctx& C, int* nen, size_t* numel, const std::vector<int>** order) {
+    if (C.E > 0) { *nen = 4; *numel = C.E; *order = &C.sp.torder; }
+    else if (C.nhex > 0) { *nen = 8; *numel = C.nhex; *order = &C.horder; }
+    else { *nen = 6; *numel = C.nwedge; *order = &C.worder; }
+}
+int ebe_download(Ctx& C, const double* d_eg, double* ref) {
+    int nen;
+    size_t numel;
+    const std::vector<int>* order;
+    ebe_shape(C, &nen, &numel, &order);
+    const int nedof = 5 * nen, NB = nen * nen;
+    std::vector<double> h(25 * C.sp.eg_blocks);
+    PH_TRY(check(C, cudaMemcpyAsync(h.data(), d_eg, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, C.stream),
+                 "download EGmass"));
+    PH_TRY(sync(C));
+    for (size_t p = 0; p < numel; ++p) {
+        const size_t e = (*order)[p];
+        for (int a = 0; a < nen; ++a)
+            for (int b = 0; b < nen; ++b)
+                for (int g = 0; g < 5; ++g)
+                    for (int f = 0; f < 5; ++f)
+                        ref[e + numel * ((size_t)(5 * a + f) + (size_t)nedof * (5 * b + g))] =
+                            h[25 * (p * NB + (size_t)a * nen + b) + 5 * g + f];
+    }
+    return PHGPU_OK;
+}
+int ebe_upload(Ctx& C, const double* ref, double* d_eg) {
+    int nen;
+    size_t numel;
+    const std::vector<int>* order;
+    ebe_shape(C, &nen, &numel, &order);
+    const int nedof = 5 * nen, NB = nen * nen;
+    std::vector<double> h(25 * C.sp.eg_blocks);
+    for (size_t p = 0; p < numel; ++p) {
+        const size_t e = (*order)[p];
+        for (int a = 0; a < nen; ++a)
+            for (int b = 0; b < nen; ++b)
+                for (int g = 0; g < 5; ++g)
+                    for (int f = 0; f < 5; ++f)
+                        h[25 * (p * NB + (size_t)a * nen + b) + 5 * g + f] =
+                            ref[e + numel * ((size_t)(5 * a + f) + (size_t)nedof * (5 * b + g))];
+    }
+    PH_TRY(check(C, cudaMemcpyAsync(d_eg, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, C.stream),
+                 "upload EGmass"));
+    return sync(C);
+}
 
 int correct_dev(Ctx& C) {
     const size_t n5 = 5 * (size_t)C.N;
@@ -748,7 +825,9 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     int rc = PHGPU_OK;
     auto T = [&](int s) { if (rc == PHGPU_OK) rc = s; };
     // colouring
-    std::vector<int> border, horder, worder;
+    std::vector<int> border;
+    std::vector<int>& horder = C.horder;
+    std::vector<int>& worder = C.worder;
     if (C.Eb > 0) T(colour(C, N, m->ienb, 4, C.Eb, border, C.bcol_start));
     if (C.nhex > 0) T(colour(C, N, m->ienh, 8, C.nhex, horder, C.hcol_start));
     if (C.nwedge > 0) T(colour(C, N, m->ienw, 6, C.nwedge, worder, C.wcol_start));
@@ -902,7 +981,7 @@ int phgpu_destroy(phgpu_ctx* h) {
                     C.d_rmes, C.d_Dy, C.d_ypre, C.d_t64, C.d_t64b, C.d_bd, C.d_yf, C.d_ylo, C.d_acf, C.d_resf, C.d_rmesf,
                     C.d_t32, C.d_t32b, C.d_bdf, C.d_qres, C.d_qresf, C.d_U, C.d_scal, C.d_part, C.d_count, C.d_flag,
                     C.sp.d_rs, C.sp.d_bcol, C.sp.d_bcolp, C.sp.d_brow, C.sp.d_ient, C.sp.d_tmap, C.sp.d_hmap,
-                    C.sp.d_wmap, C.sp.d_lhsK, C.sp.d_lhsKf};
+                    C.sp.d_wmap, C.sp.d_lhsK, C.sp.d_lhsKf, C.sp.d_EG, C.sp.d_EGf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (C.h_scal) cudaFreeHost(C.h_scal);
@@ -1154,6 +1233,80 @@ int phgpu_solgmrs(phgpu_ctx* h, const double* y, const double* ac, int lhs, doub
         PH_TRY(check(C, cudaMemcpyAsync(lhsK, C.sp.d_lhsK, sizeof(double) * 25 * (size_t)C.sp.nnzb,
                                         cudaMemcpyDeviceToHost, C.stream), "download lhsK"));
     return sync(C);
+}
+
+// the element-by-element entry points work in FP64 on the context's FP64 element storage
+static int ebe_fp64(phgpu::Ctx& C) {
+    const int prec = C.cfg.precision;
+    C.cfg.precision = PHGPU_FP64;
+    const int rc = phgpu::ebe_setup(C);
+    C.cfg.precision = prec;
+    return rc;
+}
+
+int phgpu_elmgmre(phgpu_ctx* h, const double* y, const double* ac, double* res, double* bdiag, double* EGmass) {
+    using namespace phgpu;
+    if (!h || !y || !ac || !res || !bdiag || !EGmass) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    PH_TRY(ebe_fp64(C));
+    ref_to_dev_state(C, y, C.d_t64, C.d_y);
+    ref_to_dev_state(C, ac, C.d_t64b, C.d_ac);
+    PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
+    PH_TRY(tangent64(C, C.d_y, C.sp.d_EG, C.d_bd, true));
+    dev_to_ref_res(C, C.d_res, C.d_t64, res);
+    dev_to_ref_bd(C, C.d_bd, C.d_bdstage, bdiag);
+    return ebe_download(C, C.sp.d_EG, EGmass);
+}
+
+int phgpu_i3pre(phgpu_ctx* h, const double* bdiag, double* EGmass) {
+    using namespace phgpu;
+    if (!h || !bdiag || !EGmass) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    PH_TRY(ebe_fp64(C));
+    ref_to_dev_bd(C, bdiag, C.d_bdstage, C.d_bd);
+    PH_TRY(ebe_upload(C, EGmass, C.sp.d_EG));
+    i3pre<double>(C, C.d_bd, C.sp.d_EG);
+    return ebe_download(C, C.sp.d_EG, EGmass);
+}
+
+int phgpu_au1gmr(phgpu_ctx* h, const double* EGmass, double* p) {
+    using namespace phgpu;
+    if (!h || !EGmass || !p) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    PH_TRY(ebe_fp64(C));
+    PH_TRY(ebe_upload(C, EGmass, C.sp.d_EG));
+    ref_to_dev_res(C, p, C.d_t64, C.d_t64b);
+    ebe_ap<double, double>(C, C.sp.d_EG, C.d_t64b, C.d_Dy);
+    dev_to_ref_res(C, C.d_Dy, C.d_t64, p);
+    return sync(C);
+}
+
+int phgpu_solgmre(phgpu_ctx* h, const double* y, const double* ac, double* res, double* bdiag, double* Dy,
+                  double* EGmass, phgpu_stats* st) {
+    using namespace phgpu;
+    if (!h || !y || !ac || !st) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    ref_to_dev_state(C, y, C.d_t64, C.d_y);
+    ref_to_dev_state(C, ac, C.d_t64b, C.d_ac);
+    PH_TRY(sync(C));
+    const int ntot = st->ntotGM;
+    *st = phgpu_stats{};
+    st->ntotGM = ntot;
+    const int ap = C.cfg.ap_mode;
+    C.cfg.ap_mode = PHGPU_AP_EBE;
+    const int rc = solve_dev(C, st, 1, 0);
+    C.cfg.ap_mode = ap;
+    PH_TRY(rc);
+    if (res) dev_to_ref_res(C, C.d_res, C.d_t64, res);
+    if (Dy) dev_to_ref_res(C, C.d_Dy, C.d_t64b, Dy);
+    if (bdiag) dev_to_ref_bd(C, C.d_bd, C.d_bdstage, bdiag);
+    PH_TRY(sync(C));
+    if (EGmass && C.cfg.precision == PHGPU_FP64) return ebe_download(C, C.sp.d_EG, EGmass);
+    return PHGPU_OK;
 }
 
 int phgpu_itrcorrect(phgpu_ctx* h, double* y, double* ac, const double* yold, const double* acold, const double* Dy) {

@@ -77,15 +77,11 @@ void block_map(const std::vector<int>& colm, const std::vector<int>& rowp, const
         }
 }
 
-// ---- Spsi3pre: one thread per block ----
+// L_i^-1 a U_j^-1 for one 5x5 block a (a[5 g + f] = entry (f, g)) with the i3LU factors of
+// its row node (Li) and column node (Uj), row-major: Li[5 r + c] = BDiag(i, r, c)
 template <typename R>
-__global__ void k_spsi3pre(const int* __restrict__ brow, const int* __restrict__ bcol, const R* __restrict__ bd,
-                           R* __restrict__ A, int nnzb) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nnzb) return;
-    const R* Li = bd + 25 * (size_t)brow[k];  // row-major: Li[5 r + c] = BDiag(i, r, c)
-    const R* Uj = bd + 25 * (size_t)bcol[k];
-    R* a = A + 25 * (size_t)k;                // a[5 g + f] = entry (f, g)
+__device__ __forceinline__ void precondition_block(R* __restrict__ a, const R* __restrict__ Li,
+                                                   const R* __restrict__ Uj) {
     R m[5][5];
 #pragma unroll
     for (int g = 0; g < 5; ++g)
@@ -117,6 +113,49 @@ __global__ void k_spsi3pre(const int* __restrict__ brow, const int* __restrict__
         for (int f = 0; f < 5; ++f) a[5 * g + f] = m[f][g];
 }
 
+// ---- Spsi3pre: one thread per block ----
+template <typename R>
+__global__ void k_spsi3pre(const int* __restrict__ brow, const int* __restrict__ bcol, const R* __restrict__ bd,
+                           R* __restrict__ A, int nnzb) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnzb) return;
+    precondition_block(A + 25 * (size_t)k, bd + 25 * (size_t)brow[k], bd + 25 * (size_t)bcol[k]);
+}
+
+// ---- i3pre (i3pre.f): the same transform on every block (a, b) of the stored element tangents ----
+template <typename R, int NEN>
+__global__ void k_i3pre(const int* __restrict__ ien, const R* __restrict__ bd, R* __restrict__ EG, int ne) {
+    constexpr int NB = NEN * NEN;
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)ne * NB) return;
+    const size_t e = t / NB;
+    const int ab = (int)(t - e * NB), a = ab / NEN, b = ab - NEN * (ab / NEN);
+    const int* nd = ien + (size_t)NEN * e;
+    precondition_block(EG + 25 * t, bd + 25 * (size_t)nd[a], bd + 25 * (size_t)nd[b]);
+}
+
+// ---- Au1GMR (au1gmr.f, asaugmr.f): one thread per (element, node a, equation f) ----
+// q(node a, f) += sum_b sum_g EG_e(a, b)(f, g) p(iper(node b), g); elements of one colour share no node
+template <typename M, typename V, int NEN>
+__global__ void k_ebe_ap(const int* __restrict__ ien, const M* __restrict__ EG, const int* __restrict__ iper,
+                         const V* __restrict__ p, V* __restrict__ q, int ne) {
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)ne * 5 * NEN) return;
+    const size_t e = t / (5 * NEN);
+    const int r = (int)(t - e * 5 * NEN), a = r / 5, f = r - 5 * (r / 5);
+    const int* nd = ien + (size_t)NEN * e;
+    const M* blk = EG + 25 * ((size_t)e * NEN + a) * NEN + f;
+    V acc = V(0);
+#pragma unroll
+    for (int b = 0; b < NEN; ++b) {
+        const V* pb = p + 5 * (size_t)iper[nd[b]];
+        const M* m = blk + 25 * b;
+        acc += (V)m[0] * pb[0] + (V)m[5] * pb[1] + (V)m[10] * pb[2] + (V)m[15] * pb[3] + (V)m[20] * pb[4];
+    }
+    V* o = q + 5 * (size_t)nd[a] + f;
+    *o = *o + acc;
+}
+
 // ---- SparseAp: one thread per (block row, equation) ----
 // Thread (i, f) forms q(i, f) = sum_k sum_g lhsK(k)(f, g) p(iper(col k), g) over the blocks
 // of row i: five strided values of each block (the row's segment is read in full by its
@@ -143,6 +182,26 @@ k_bsr_spmv(const int* __restrict__ rs, const int* __restrict__ bcolp, const M* _
 
 }  // namespace
 
+// the element colouring of the tet tangent, the tables and kernel attributes (both solvers)
+static int tangent_setup(Ctx& C) {
+    SparseCtx& S = C.sp;
+    if (S.tan_ready) return PHGPU_OK;
+    std::vector<int> tien(4 * (size_t)C.E);
+    if (C.E > 0) {
+        // tets: their own colouring (the chunk order of the residual kernels groups elements that share nodes)
+        const int rcc = colour(C, C.N, C.h_ien.data(), 4, C.E, S.torder, S.tcol_start);
+        if (rcc != PHGPU_OK) return rcc;
+        for (int i = 0; i < C.E; ++i)
+            for (int a = 0; a < 4; ++a) tien[4 * (size_t)i + a] = C.h_ien[4 * (size_t)S.torder[i] + a];
+    }
+    S.h_ient = tien;
+    int rc = dcopy(C, &S.d_ient, tien.data(), tien.size());
+    if (rc == PHGPU_OK) upload_tangent_tables(C);
+    if (rc == PHGPU_OK) rc = configure_tangent_kernels(C);
+    if (rc == PHGPU_OK) S.tan_ready = true;
+    return rc;
+}
+
 // the FP32 tangent is allocated the first time a mixed-precision solve needs it
 static int ensure_f32(Ctx& C) {
     SparseCtx& S = C.sp;
@@ -158,6 +217,10 @@ int sparse_setup(Ctx& C) {
     SparseCtx& S = C.sp;
     if (S.ready) return ensure_f32(C);
     const int N = C.N;
+    {
+        const int rct = tangent_setup(C);
+        if (rct != PHGPU_OK) return rct;
+    }
     block_adjacency(N, C.h_ien.data(), C.E, C.h_ienh.data(), C.nhex, C.h_ienw.data(), C.nwedge, S.colm, S.rowp);
     S.nnzb = (int)S.rowp.size();
     std::vector<int> rs(N + 1), bcol(S.nnzb), bcolp(S.nnzb), brow(S.nnzb);
@@ -173,15 +236,8 @@ int sparse_setup(Ctx& C) {
             bcol[k] = S.rowp[k] - 1;
             bcolp[k] = iper[bcol[k]];
         }
-    // tets: their own colouring (the chunk order of the residual kernels groups elements that share nodes)
-    std::vector<int> torder, tien(4 * (size_t)C.E), tmap, hmap, wmap;
-    if (C.E > 0) {
-        const int rcc = colour(C, N, C.h_ien.data(), 4, C.E, torder, S.tcol_start);
-        if (rcc != PHGPU_OK) return rcc;
-        for (int i = 0; i < C.E; ++i)
-            for (int a = 0; a < 4; ++a) tien[4 * (size_t)i + a] = C.h_ien[4 * (size_t)torder[i] + a];
-        block_map(S.colm, S.rowp, tien.data(), 4, C.E, tmap);
-    }
+    std::vector<int> tmap, hmap, wmap;
+    if (C.E > 0) block_map(S.colm, S.rowp, S.h_ient.data(), 4, C.E, tmap);
     if (C.nhex > 0) block_map(S.colm, S.rowp, C.h_ienh.data(), 8, C.nhex, hmap);
     if (C.nwedge > 0) block_map(S.colm, S.rowp, C.h_ienw.data(), 6, C.nwedge, wmap);
     int rc = PHGPU_OK;
@@ -190,15 +246,12 @@ int sparse_setup(Ctx& C) {
     T(dcopy(C, &S.d_bcol, bcol.data(), bcol.size()));
     T(dcopy(C, &S.d_bcolp, bcolp.data(), bcolp.size()));
     T(dcopy(C, &S.d_brow, brow.data(), brow.size()));
-    T(dcopy(C, &S.d_ient, tien.data(), tien.size()));
     T(dcopy(C, &S.d_tmap, tmap.data(), tmap.size()));
     T(dcopy(C, &S.d_hmap, hmap.data(), hmap.size()));
     T(dcopy(C, &S.d_wmap, wmap.data(), wmap.size()));
     if (rc == PHGPU_OK && cudaMalloc((void**)&S.d_lhsK, sizeof(double) * 25 * (size_t)std::max(S.nnzb, 1)) != cudaSuccess)
         rc = PHGPU_ERR_NOMEM;
     if (rc == PHGPU_OK) rc = ensure_f32(C);
-    if (rc == PHGPU_OK) upload_tangent_tables(C);
-    if (rc == PHGPU_OK) rc = configure_tangent_kernels(C);
     if (rc == PHGPU_OK) rc = check(C, cudaStreamSynchronize(C.stream), "sparse set-up");
     if (rc != PHGPU_OK) {
         if (C.err.empty()) C.err = "sparse set-up failed";
@@ -206,6 +259,28 @@ int sparse_setup(Ctx& C) {
     }
     S.ready = true;
     return PHGPU_OK;
+}
+
+int ebe_setup(Ctx& C) {
+    SparseCtx& S = C.sp;
+    if ((C.E > 0) + (C.nhex > 0) + (C.nwedge > 0) != 1) {
+        C.err = "the element-by-element solver needs a mesh of one element topology (i3pre.f gathers the block "
+                "diagonal through a section of the largest element's size)";
+        return PHGPU_ERR_UNSUPPORTED;
+    }
+    const int rct = tangent_setup(C);
+    if (rct != PHGPU_OK) return rct;
+    S.eg_blocks = 16 * (size_t)C.E + 64 * (size_t)C.nhex + 36 * (size_t)C.nwedge;
+    const bool f64 = C.cfg.precision == PHGPU_FP64;
+    if (f64 && !S.d_EG && cudaMalloc((void**)&S.d_EG, sizeof(double) * 25 * S.eg_blocks) != cudaSuccess) {
+        C.err = "cudaMalloc (element tangents)";
+        return PHGPU_ERR_NOMEM;
+    }
+    if (!f64 && !S.d_EGf && cudaMalloc((void**)&S.d_EGf, sizeof(float) * 25 * S.eg_blocks) != cudaSuccess) {
+        C.err = "cudaMalloc (FP32 element tangents)";
+        return PHGPU_ERR_NOMEM;
+    }
+    return check(C, cudaStreamSynchronize(C.stream), "element-by-element set-up");
 }
 
 template <typename R>
@@ -229,5 +304,63 @@ void sparse_ap(Ctx& C, const M* lhsK, const V* p, V* q) {
 }
 template void sparse_ap<double, double>(Ctx&, const double*, const double*, double*);
 template void sparse_ap<float, float>(Ctx&, const float*, const float*, float*);
+
+// the element blocks of the element-by-element storage: connectivity, colours, first block
+struct EbeBlock {
+    const int* ien;
+    const std::vector<int>* col;
+    int nen, ne;
+    size_t blk0;
+};
+static int ebe_blocks(const Ctx& C, EbeBlock* out) {
+    int n = 0;
+    if (C.E > 0) out[n++] = {C.sp.d_ient, &C.sp.tcol_start, 4, C.E, 0};
+    if (C.nhex > 0) out[n++] = {C.d_ienh, &C.hcol_start, 8, C.nhex, 16 * (size_t)C.E};
+    if (C.nwedge > 0) out[n++] = {C.d_ienw, &C.wcol_start, 6, C.nwedge, 16 * (size_t)C.E + 64 * (size_t)C.nhex};
+    return n;
+}
+
+template <typename R>
+void i3pre(Ctx& C, const R* bd, R* EG) {
+    EbeBlock b[3];
+    const int nb = ebe_blocks(C, b);
+    for (int i = 0; i < nb; ++i) {
+        const size_t nt = (size_t)b[i].ne * b[i].nen * b[i].nen;
+        const unsigned grid = (unsigned)((nt + 127) / 128);
+        R* eg = EG + 25 * b[i].blk0;
+        if (b[i].nen == 4) k_i3pre<R, 4><<<grid, 128, 0, C.stream>>>(b[i].ien, bd, eg, b[i].ne);
+        else if (b[i].nen == 8) k_i3pre<R, 8><<<grid, 128, 0, C.stream>>>(b[i].ien, bd, eg, b[i].ne);
+        else k_i3pre<R, 6><<<grid, 128, 0, C.stream>>>(b[i].ien, bd, eg, b[i].ne);
+        ++C.launches;
+    }
+}
+template void i3pre<double>(Ctx&, const double*, double*);
+template void i3pre<float>(Ctx&, const float*, float*);
+
+template <typename M, typename V>
+void ebe_ap(Ctx& C, const M* EG, const V* p, V* q) {
+    fill0(C, q, sizeof(V) * 5 * (size_t)C.N);
+    EbeBlock b[3];
+    const int nb = ebe_blocks(C, b);
+    for (int i = 0; i < nb; ++i) {
+        const int NEN = b[i].nen;
+        const std::vector<int>& col = *b[i].col;
+        for (size_t c = 0; c + 1 < col.size(); ++c) {
+            const int e0 = col[c], ne = col[c + 1] - e0;
+            if (ne <= 0) continue;
+            const size_t nt = (size_t)ne * 5 * NEN;
+            const unsigned grid = (unsigned)((nt + 159) / 160);
+            const int* ie = b[i].ien + (size_t)NEN * e0;
+            const M* eg = EG + 25 * (b[i].blk0 + (size_t)NEN * NEN * e0);
+            if (NEN == 4) k_ebe_ap<M, V, 4><<<grid, 160, 0, C.stream>>>(ie, eg, C.d_iper, p, q, ne);
+            else if (NEN == 8) k_ebe_ap<M, V, 8><<<grid, 160, 0, C.stream>>>(ie, eg, C.d_iper, p, q, ne);
+            else k_ebe_ap<M, V, 6><<<grid, 160, 0, C.stream>>>(ie, eg, C.d_iper, p, q, ne);
+            ++C.launches;
+        }
+    }
+    bc3per<V>(C, q);
+}
+template void ebe_ap<double, double>(Ctx&, const double*, const double*, double*);
+template void ebe_ap<float, float>(Ctx&, const float*, const float*, float*);
 
 }  // namespace phgpu

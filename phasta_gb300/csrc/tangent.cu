@@ -332,11 +332,20 @@ k_tangent(const int* __restrict__ ien, const int* __restrict__ bmap, int ne, con
     }
     const int ia = iBC[na], ib = iBC[nb];
     if (ia | ib) bc3lhs_block(M, ia, BC + 6 * (size_t)na, ib, BC + 6 * (size_t)nb, a == b);
-    R* o = lhsK + 25 * (size_t)bmap[(size_t)e * NB + ab];
+    if (bmap) {
+        R* o = lhsK + 25 * (size_t)bmap[(size_t)e * NB + ab];
 #pragma unroll
-    for (int g = 0; g < 5; ++g)
+        for (int g = 0; g < 5; ++g)
 #pragma unroll
-        for (int f = 0; f < 5; ++f) o[5 * g + f] += M[f][g];
+            for (int f = 0; f < 5; ++f) o[5 * g + f] += M[f][g];
+    } else {
+        // element-by-element storage (ElmGMRe): block (a, b) of element e, written once
+        R* o = lhsK + 25 * ((size_t)e * NB + ab);
+#pragma unroll
+        for (int g = 0; g < 5; ++g)
+#pragma unroll
+            for (int f = 0; f < 5; ++f) o[5 * g + f] = M[f][g];
+    }
 }
 
 template <typename R, int NEN, int TOPO>
@@ -349,8 +358,11 @@ void launch_one(Ctx& C, const int* d_ien, const int* d_map, const std::vector<in
     for (int c = 0; c < ncol; ++c) {
         const int e0 = col[c], ne = col[c + 1] - e0;
         if (ne <= 0) continue;
+        // with no block map the output is element storage, offset by the colour's first element
+        const int* map = d_map ? d_map + (size_t)NEN * NEN * e0 : nullptr;
+        R* out = d_map ? lhsK : lhsK + 25 * (size_t)NEN * NEN * e0;
         k_tangent<R, NEN, TOPO><<<(ne + EPB - 1) / EPB, kTanThreads, sm, C.stream>>>(
-            d_ien + (size_t)NEN * e0, d_map + (size_t)NEN * NEN * e0, ne, x, y, C.d_iBC, C.d_BC, lhsK, bd, P);
+            d_ien + (size_t)NEN * e0, map, ne, x, y, C.d_iBC, C.d_BC, out, bd, P);
         ++C.launches;
     }
 }
@@ -396,5 +408,18 @@ void launch_tangent(Ctx& C, const R* x, const R* y, R* lhsK, R* bd) {
 }
 template void launch_tangent<double>(Ctx&, const double*, const double*, double*, double*);
 template void launch_tangent<float>(Ctx&, const float*, const float*, float*, float*);
+
+// EG = the element tangents (after bc3LHS) stored per element; bd += their diagonal blocks
+template <typename R>
+void launch_tangent_ebe(Ctx& C, const R* x, const R* y, R* EG, R* bd) {
+    const SparseCtx& S = C.sp;
+    R* hex = EG + 25 * 16 * (size_t)C.E;
+    R* wedge = hex + 25 * 64 * (size_t)C.nhex;
+    if (C.E > 0) launch_one<R, 4, 2>(C, S.d_ient, nullptr, S.tcol_start, x, y, EG, bd);
+    if (C.nhex > 0) launch_one<R, 8, 0>(C, C.d_ienh, nullptr, C.hcol_start, x, y, hex, bd);
+    if (C.nwedge > 0) launch_one<R, 6, 1>(C, C.d_ienw, nullptr, C.wcol_start, x, y, wedge, bd);
+}
+template void launch_tangent_ebe<double>(Ctx&, const double*, const double*, double*, double*);
+template void launch_tangent_ebe<float>(Ctx&, const float*, const float*, float*, float*);
 
 }  // namespace phgpu

@@ -21,7 +21,15 @@ and the sparse solver of the reference's impl = 1x path (lhs = 1):
     SparseAp(lhsK, p)            -> lhsK p (+ bc3per)         sparseap.f:1, bc3per.f:1
     SolGMRs(y, ac, lhs)          -> res, BDiag, Dy, lhsK, st  solgmr.f:480
 
-lhsK is returned as an (nnz_tot, 25) array: row k is the reference's lhsK(:, k).
+and the element-by-element solver (impl = 3x; one element topology):
+
+    ElmGMRe(y, ac)               -> res, BDiag, EGmass        elmgmr.f:1
+    i3pre(lu, EGmass)            -> EGmass                    i3pre.f:1
+    Au1GMR(EGmass, p)            -> sum_e EGmass_e p (+bc3per) au1gmr.f:1
+    SolGMRe(y, ac)               -> res, BDiag, Dy, EGmass, st solgmr.f:1
+
+lhsK is returned as an (nnz_tot, 25) array: row k is the reference's lhsK(:, k); EGmass as
+an (numel, nedof, nedof) array view of the reference's EGmass.
 
 Every call runs on the GPU; a non-zero status from the library raises
 ``PhgpuError`` (the reference would stop in error()/tnanq).
@@ -270,6 +278,39 @@ class GpuSolver:
                                            L.dptr(lhsK), C.byref(st)))
         self.ntotGM = st.ntotGM
         return res, bd, Dy, lhsK, _stats(st)
+
+    # -- element-by-element solver (one element topology) --
+    def _eg(self):
+        c = self.case
+        n = c.nelem + c.nhex + c.nwedge
+        nd = 20 if c.nelem else 40 if c.nhex else 30
+        return np.zeros((nd, nd, n))  # C order (j, i, e): the reference's EGmass(e, i, j)
+
+    def ElmGMRe(self, y, ac):
+        res, bd, EG = self._v(), self._v(25), self._eg()
+        self._check(self.lib.phgpu_elmgmre(self.h, L.dptr(y), L.dptr(ac), L.dptr(res), L.dptr(bd), L.dptr(EG)))
+        return res, bd, EG.transpose(2, 1, 0)
+
+    def i3pre(self, lu, EG):
+        out = np.ascontiguousarray(np.asarray(EG).transpose(2, 1, 0))
+        self._check(self.lib.phgpu_i3pre(self.h, L.dptr(np.ascontiguousarray(lu, dtype=np.float64)), L.dptr(out)))
+        return out.transpose(2, 1, 0)
+
+    def Au1GMR(self, EG, p):
+        p = np.array(p, dtype=np.float64)
+        eg = np.ascontiguousarray(np.asarray(EG).transpose(2, 1, 0))
+        self._check(self.lib.phgpu_au1gmr(self.h, L.dptr(eg), L.dptr(p)))
+        return p
+
+    def SolGMRe(self, y, ac):
+        res, bd, Dy = self._v(), self._v(25), self._v()
+        EG = self._eg() if self.params.get("precision", L.PHGPU_FP64) == L.PHGPU_FP64 else None
+        st = L.Stats()
+        st.ntotGM = self.ntotGM
+        self._check(self.lib.phgpu_solgmre(self.h, L.dptr(y), L.dptr(ac), L.dptr(res), L.dptr(bd), L.dptr(Dy),
+                                           L.dptr(EG), C.byref(st)))
+        self.ntotGM = st.ntotGM
+        return res, bd, Dy, (None if EG is None else EG.transpose(2, 1, 0)), _stats(st)
 
     # -- device-resident path (benchmarks) --
     def upload(self, y=None, ac=None, yold=None, acold=None):
