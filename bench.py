@@ -232,6 +232,8 @@ def run_gpu(args, rank, world):
         result["fp64_plain"] = fp64_plain(args, case)
     if not args.skip_sparse:
         result["sparse_solver"] = sparse_solver(args)
+        if args.precision == "mixed":
+            result["ebe_solver"] = sparse_solver(args, ebe=True)
     g.close()
     return result
 
@@ -290,16 +292,17 @@ def kernel_roofline(g, case, stream, args, krylov_per_newton):
             "algorithmic_bytes": k["algorithmic_bytes"], "launch_ms": k["ms"], "sweeps": kernels}
 
 
-def sparse_solver(args):
-    """The reference's sparse solver (SolGMRs on the assembled tangent) on the same workload:
-    FP32 tangent and Krylov vectors in mixed precision, FP64 throughout otherwise."""
+def sparse_solver(args, ebe: bool = False):
+    """The reference's sparse solver (SolGMRs on the assembled tangent) or, with ebe, its
+    element-by-element solver (SolGMRe on stored element tangents) on the same workload: FP32
+    tangent and Krylov vectors in mixed precision, FP64 throughout otherwise."""
     import torch
 
     from phasta_gb300 import _lib as L
     from phasta_gb300.solver import GpuSolver
 
     case, params, y0, ac0 = make_workload(args.n, args.precision)
-    params = dict(params, ap_mode=L.PHGPU_AP_SPARSE)
+    params = dict(params, ap_mode=L.PHGPU_AP_EBE if ebe else L.PHGPU_AP_SPARSE)
     g = GpuSolver(case, params)
     stream = torch.cuda.ExternalStream(g.stream())
     g.upload(y0, ac0, y0, ac0)
@@ -318,15 +321,25 @@ def sparse_solver(args):
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / NEWTON_PER_TIMESTEP
     r_end = g.residual_norm_dev()
-    E, N, nnzb = case.nelem, case.nshg, g.nnz_tot
+    E, N = case.nelem, case.nshg
     vb = 4 if args.precision == "mixed" else 8
-    tan, spmv = (9, 10) if args.precision == "mixed" else (11, 12)
+    if ebe:
+        if args.precision != "mixed":
+            raise SystemExit("the element-by-element timing sweeps are FP32")
+        nnzb = 16 * E
+        tan, spmv = 13, 14
+        # element storage written once; the product reads it, the connectivity and the vector
+        tan_bytes = 25 * vb * nnzb + N * 8 * vb + E * 16
+        spmv_bytes = 25 * vb * nnzb + E * 16 + 2 * 5 * vb * N
+    else:
+        nnzb = g.nnz_tot
+        tan, spmv = (9, 10) if args.precision == "mixed" else (11, 12)
+        # compulsory bytes: the tangent writes lhsK once and reads x, y, connectivity and block
+        # maps; the product reads lhsK, its column list and the vector once and writes the result
+        tan_bytes = 25 * vb * nnzb + N * 8 * vb + E * (16 + 64)
+        spmv_bytes = nnzb * (25 * vb + 4) + 4 * (N + 1) + 2 * 5 * vb * N
     t_tan = _time_sweep(g, stream, tan, reps=3)
     t_spmv = _time_sweep(g, stream, spmv, reps=10)
-    # compulsory bytes: the tangent writes lhsK once and reads x, y, connectivity and block maps;
-    # the product reads lhsK, its column list and the vector once and writes the result
-    tan_bytes = 25 * vb * nnzb + N * 8 * vb + E * (16 + 64)
-    spmv_bytes = nnzb * (25 * vb + 4) + 4 * (N + 1) + 2 * 5 * vb * N
     g.close()
     return {"ms_per_newton": ms, "value": E / ms * 1e3, "krylov_iterations": iks,
             "rel_residual_after_3": r_end / r0, "nnz_blocks": nnzb,

@@ -221,7 +221,9 @@ int phgpu_residual_norm_dev(phgpu_ctx* ctx, double* rnorm);
  * diagonal + residuals, 5 FP32 copies of the state, 6 FP64-Galerkin residual, 7 double-float
  * split residual, 8 hi/lo float copies of the state, 9 FP32 assembled tangent, 10 FP32
  * block-sparse product, 11 FP64 assembled tangent, 12 FP64 block-sparse product (9-12 use the
- * sparse solver's structure; 10 and 12 multiply whatever tangent 9 and 11 left) */
+ * sparse solver's structure; 10 and 12 multiply whatever tangent 9 and 11 left), 13 FP32
+ * element tangents stored per element, 14 FP32 element-by-element product (13-14: mixed
+ * precision context, one element topology) */
 int phgpu_sweep_dev(phgpu_ctx* ctx, int which);
 
 /* Largest 5*nshg that phgpu_rstat_noalloc accepts (33,554,432 values, nshg <= 6,710,886). */

@@ -238,17 +238,19 @@ __global__ void k_lu_fact(R* __restrict__ bd, int N, int* __restrict__ flag) {
     if (bad && flag) atomicOr(flag + 1, 1);
 }
 
+// in and out may be the same array (each thread reads its node's five values before writing them)
 template <typename R, typename V>
-__global__ void k_lu_apply(const R* __restrict__ bd, V* __restrict__ r, int N, int code,
+__global__ void k_lu_apply(const R* __restrict__ bd, const V* in, V* out, int N, int code,
                            const int* __restrict__ skip) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     if (skip && *skip) return;
     const R* D = bd + 25 * (size_t)n;
-    V* v = r + 5 * (size_t)n;
+    const V* vi = in + 5 * (size_t)n;
+    V* v = out + 5 * (size_t)n;
     R x[5];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) x[k] = (R)v[k];
+    for (int k = 0; k < 5; ++k) x[k] = (R)vi[k];
     auto A = [&](int i, int j) { return D[5 * i + j]; };
     if (code == PHGPU_LU_FORWARD) {
         x[1] = x[1] - A(1, 0) * x[0];
@@ -392,15 +394,45 @@ struct DotAcc<float> {
     __device__ __forceinline__ double value() const { return df_to_double(s); }
 };
 
+// 16-byte vectors of the streaming kernels (every vector of the Krylov loop starts on a
+// 256-byte boundary); the n % W tail is handled element by element
+__device__ __forceinline__ bool al16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+template <typename V> struct Vec16;
+template <> struct Vec16<float> {
+    using T = float4;
+    static constexpr int W = 4;
+    __device__ static float at(const T& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+    __device__ static void set(T& v, int k, float x) {
+        if (k == 0) v.x = x; else if (k == 1) v.y = x; else if (k == 2) v.z = x; else v.w = x;
+    }
+};
+template <> struct Vec16<double> {
+    using T = double2;
+    static constexpr int W = 2;
+    __device__ static double at(const T& v, int k) { return k == 0 ? v.x : v.y; }
+    __device__ static void set(T& v, int k, double x) {
+        if (k == 0) v.x = x; else v.y = x;
+    }
+};
+
 template <typename V>
 __global__ void __launch_bounds__(kRedThreads)
 k_dot(const V* __restrict__ a, const V* __restrict__ b, size_t n, double* part, unsigned int* count,
       double* out, const int* __restrict__ skip) {
+    using X = Vec16<V>;
     __shared__ double sh[32];
     if (skip && *skip) return;
     DotAcc<V> acc;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        acc.add(a[i], b[i]);
+    const size_t nv = (al16(a) && al16(b)) ? n / X::W : 0, t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const typename X::T* av = reinterpret_cast<const typename X::T*>(a);
+    const typename X::T* bv = reinterpret_cast<const typename X::T*>(b);
+    for (size_t i = t0; i < nv; i += stride) {
+        const typename X::T x = av[i], y = bv[i];
+#pragma unroll
+        for (int k = 0; k < X::W; ++k) acc.add(X::at(x, k), X::at(y, k));
+    }
+    for (size_t i = X::W * nv + t0; i < n; i += stride) acc.add(a[i], b[i]);
     const double bs = block_sum(acc.value(), sh);
     __syncthreads();
     finish_reduce(bs, part, count, out, sh);
@@ -414,10 +446,30 @@ k_mgs(V* w, const V* __restrict__ up, const double* __restrict__ beta_prev, cons
     // self != 0 when uj is w itself (the last step of solmfg.f:247-267 forms w.w)
     __shared__ double sh[32];
     if (skip && *skip) return;
+    using X = Vec16<V>;
+    using T = typename X::T;
     const double bp = up ? *beta_prev : 0.0;
     const V bv = (V)bp;
     DotAcc<V> acc;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const bool vec = al16(w) && al16(up) && al16(uj);
+    const size_t nv = vec ? n / X::W : 0, t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    T* wv = reinterpret_cast<T*>(w);
+    const T* upv = reinterpret_cast<const T*>(up);
+    const T* ujv = reinterpret_cast<const T*>(uj);
+    for (size_t i = t0; i < nv; i += stride) {
+        T wi = wv[i];
+        if (up) {
+            const T ui = upv[i];
+#pragma unroll
+            for (int k = 0; k < X::W; ++k) X::set(wi, k, X::at(wi, k) - bv * X::at(ui, k));
+            wv[i] = wi;
+        }
+        const T u2 = self ? wi : ujv[i];
+#pragma unroll
+        for (int k = 0; k < X::W; ++k) acc.add(X::at(wi, k), X::at(u2, k));
+    }
+    for (size_t i = X::W * nv + t0; i < n; i += stride) {
         V wi = w[i];
         if (up) {
             wi = wi - bv * up[i];
@@ -436,10 +488,20 @@ template <typename V>
 __global__ void k_scale(V* __restrict__ w, const double* __restrict__ s, int mode, size_t n,
                         const int* __restrict__ skip) {
     if (skip && *skip) return;
+    using X = Vec16<V>;
+    using T = typename X::T;
     const double d = mode ? sqrt(*s) : *s;
     const V f = (V)(1.0 / d);
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        w[i] = w[i] * f;
+    const size_t nv = al16(w) ? n / X::W : 0, t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    T* wv = reinterpret_cast<T*>(w);
+    for (size_t i = t0; i < nv; i += stride) {
+        T x = wv[i];
+#pragma unroll
+        for (int k = 0; k < X::W; ++k) X::set(x, k, X::at(x, k) * f);
+        wv[i] = x;
+    }
+    for (size_t i = X::W * nv + t0; i < n; i += stride) w[i] = w[i] * f;
 }
 
 }  // namespace
@@ -517,9 +579,16 @@ template void lu_fact<float>(Ctx&, float*, int*);
 
 template <typename R, typename V>
 void lu_apply(Ctx& C, const R* bd, V* r, int code) {
-    k_lu_apply<R, V><<<nblocks(C.N), kT, 0, C.stream>>>(bd, r, C.N, code, nullptr);
+    k_lu_apply<R, V><<<nblocks(C.N), kT, 0, C.stream>>>(bd, r, r, C.N, code, nullptr);
     ++C.launches;
 }
+template <typename R, typename V>
+void lu_apply(Ctx& C, const R* bd, const V* in, V* out, int code) {
+    k_lu_apply<R, V><<<nblocks(C.N), kT, 0, C.stream>>>(bd, in, out, C.N, code, nullptr);
+    ++C.launches;
+}
+template void lu_apply<double, double>(Ctx&, const double*, const double*, double*, int);
+template void lu_apply<float, float>(Ctx&, const float*, const float*, float*, int);
 template void lu_apply<double, double>(Ctx&, const double*, double*, int);
 template void lu_apply<double, float>(Ctx&, const double*, float*, int);
 template void lu_apply<float, float>(Ctx&, const float*, float*, int);

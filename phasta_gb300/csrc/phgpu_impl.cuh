@@ -147,7 +147,8 @@ struct Ctx {
     double *d_res = nullptr, *d_rmes = nullptr, *d_bd = nullptr, *d_Dy = nullptr, *d_bdstage = nullptr;
     double *d_ypre = nullptr, *d_t64 = nullptr, *d_t64b = nullptr;
     float *d_resf = nullptr, *d_rmesf = nullptr, *d_bdf = nullptr, *d_t32 = nullptr, *d_t32b = nullptr;
-    void* d_U = nullptr;          // Krylov basis (Kspace+1) x 5N, double or float
+    void* d_U = nullptr;          // Krylov basis (Kspace+1) x ldU, double or float
+    size_t ldU = 0;               // 5N rounded up to 64 values: every basis vector starts on 256 bytes
     int Ucap = 0;
     double* d_scal = nullptr;     // device scalars (see Scal below)
     double* d_part = nullptr;     // reduction partials
@@ -211,6 +212,7 @@ template <typename R> void itrbc_pert(Ctx& C, R* v, bool zero_dirichlet);
 void itrbc_state(Ctx& C, double* y, double* ac, bool with_ac);
 template <typename R> void lu_fact(Ctx& C, R* bd, int* flag);
 template <typename R, typename V> void lu_apply(Ctx& C, const R* bd, V* r, int code);
+template <typename R, typename V> void lu_apply(Ctx& C, const R* bd, const V* in, V* out, int code);
 void ref_to_dev_state(Ctx& C, const double* h_ref, double* d_tmp_host_layout, double* d_out);
 void dev_to_ref_state(Ctx& C, const double* d_in, double* d_tmp, double* h_ref);
 void ref_to_dev_res(Ctx& C, const double* h_ref, double* d_tmp, double* d_out);

@@ -113,8 +113,12 @@ __global__ void k_cd_diff(const double* __restrict__ res, const double* ub1, con
 template <typename V>
 __global__ void k_copy(const V* __restrict__ a, V* __restrict__ b, size_t n, const int* skip) {
     if (skip && *skip) return;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        b[i] = a[i];
+    // 16-byte vectors when both arrays allow them, then the elements the vectors leave
+    const bool vec = (((uintptr_t)a | (uintptr_t)b) & 15) == 0;
+    const size_t W = 16 / sizeof(V), nv = vec ? n / W : 0;
+    const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = t0; i < nv; i += stride) reinterpret_cast<float4*>(b)[i] = reinterpret_cast<const float4*>(a)[i];
+    for (size_t i = W * nv + t0; i < n; i += stride) b[i] = a[i];
 }
 __global__ void k_fdi_combine(double* __restrict__ r, const double* __restrict__ rmes, double epsM, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -349,16 +353,15 @@ int au2_fd64(Ctx& C, double* out) {
     return PHGPU_OK;
 }
 
+// u_out = L^-1 J U^-1 u_in (u_in may be u_out)
 template <typename V>
-int ap_lin(Ctx& C, V* u, const int* skip);
+int ap_lin(Ctx& C, const V* u_in, V* u, const int* skip);
 
 template <>
-int ap_lin<double>(Ctx& C, double* u, const int* skip) {
+int ap_lin<double>(Ctx& C, const double* u_in, double* u, const int* skip) {
     const size_t n5 = 5 * (size_t)C.N;
     double* v = C.d_t64;
-    k_copy<double><<<kVG, kVT, 0, C.stream>>>(u, v, n5, skip);
-    ++C.launches;
-    lu_apply<double, double>(C, C.d_bd, v, PHGPU_LU_BACKWARD);
+    lu_apply<double, double>(C, C.d_bd, u_in, v, PHGPU_LU_BACKWARD);
     itrbc_pert<double>(C, v, true);
     fill0(C, u, sizeof(double) * n5);
     launch_elem_res<double>(C, RM_LIN, C.d_x, v, C.d_y, nullptr, u, 0, skip);
@@ -368,12 +371,10 @@ int ap_lin<double>(Ctx& C, double* u, const int* skip) {
 }
 
 template <>
-int ap_lin<float>(Ctx& C, float* u, const int* skip) {
+int ap_lin<float>(Ctx& C, const float* u_in, float* u, const int* skip) {
     const size_t n5 = 5 * (size_t)C.N;
     float* v = C.d_t32;
-    k_copy<float><<<kVG, kVT, 0, C.stream>>>(u, v, n5, skip);
-    ++C.launches;
-    lu_apply<float, float>(C, C.d_bdf, v, PHGPU_LU_BACKWARD);
+    lu_apply<float, float>(C, C.d_bdf, u_in, v, PHGPU_LU_BACKWARD);
     itrbc_pert<float>(C, v, true);
     fill0(C, u, sizeof(float) * n5);
     launch_elem_res<float>(C, RM_LIN, C.d_xf, v, C.d_yf, nullptr, u, 0, skip);
@@ -447,7 +448,7 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
     const size_t n5 = 5 * (size_t)C.N;
     const int K = C.cfg.Kspace;
     V* U = (V*)C.d_U;
-    auto Uj = [&](int j) { return U + (size_t)(j - 1) * n5; };  // 1-based
+    auto Uj = [&](int j) { return U + (size_t)(j - 1) * C.ldU; };  // 1-based
     double* s = C.d_scal;
     const int* done = C.d_flag;
     // ||b||
@@ -504,15 +505,13 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
                 if (C.cfg.ap_mode == PHGPU_AP_FD) {
                     PH_TRY(au2_fd64(C, t));
                 } else {
-                    k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, t, n5, nullptr);
-                    ++C.launches;
-                    PH_TRY(ap_lin<V>(C, t, nullptr));
+                    PH_TRY(ap_lin<V>(C, C.d_Dy, t, nullptr));
                     k_axpby<<<kVG, kVT, 0, C.stream>>>(C.d_res, 1.0, t, -1.0, t, n5);  // t = b - A Dy
                     ++C.launches;
                 }
             } else {
                 to_f32(C, C.d_Dy, t, n5);
-                PH_TRY(ap_lin<V>(C, t, nullptr));
+                PH_TRY(ap_lin<V>(C, t, t, nullptr));
                 to_f64(C, t, C.d_t64b, n5);
                 k_axpby<<<kVG, kVT, 0, C.stream>>>(C.d_res, 1.0, C.d_t64b, -1.0, C.d_t64b, n5);
                 ++C.launches;
@@ -532,15 +531,16 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
             V* w = Uj(iKs + 1);
             if (sparse) {
                 assembled_ap<V>(C, ebe, Uj(iKs), w);
-            } else {
-                k_copy<V><<<kVG, kVT, 0, C.stream>>>(Uj(iKs), w, n5, nullptr);
-                ++C.launches;
-                if constexpr (std::is_same<V, double>::value) {
-                    if (C.cfg.ap_mode == PHGPU_AP_FD) PH_TRY(ap_fd64(C, w, C.d_rmes, nullptr));
-                    else PH_TRY(ap_lin<V>(C, w, nullptr));
+            } else if constexpr (std::is_same<V, double>::value) {
+                if (C.cfg.ap_mode == PHGPU_AP_FD) {
+                    k_copy<V><<<kVG, kVT, 0, C.stream>>>(Uj(iKs), w, n5, nullptr);
+                    ++C.launches;
+                    PH_TRY(ap_fd64(C, w, C.d_rmes, nullptr));
                 } else {
-                    PH_TRY(ap_lin<V>(C, w, nullptr));
+                    PH_TRY(ap_lin<V>(C, Uj(iKs), w, nullptr));
                 }
+            } else {
+                PH_TRY(ap_lin<V>(C, Uj(iKs), w, nullptr));
             }
             // modified Gram-Schmidt (solmfg.f:247-267)
             double* Hcol = s + S_H + (size_t)(K + 1) * (iKs - 1);
@@ -559,7 +559,7 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
             if (C.h_flag[0]) break;
         }
         k_backsolve<<<1, 1, 0, C.stream>>>(s, K, iKs);
-        k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, U, n5, iKs, s, n5);
+        k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, U, C.ldU, iKs, s, n5);
         C.launches += 2;
         PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "echeck"));
         PH_TRY(sync(C));
@@ -911,7 +911,8 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     {
         const size_t vb = (cfg->precision == PHGPU_FP64) ? sizeof(double) : sizeof(float);
         char* p = nullptr;
-        T(dalloc(C, &p, vb * n5 * (size_t)(K + 1)));
+        C.ldU = (n5 + 63) / 64 * 64;
+        T(dalloc(C, &p, vb * C.ldU * (size_t)(K + 1)));
         C.d_U = p;
         C.Ucap = K;
     }
@@ -1433,6 +1434,14 @@ int phgpu_sweep_dev(phgpu_ctx* h, int which) {
         case 12:  // FP64 block-sparse product
             PH_TRY(sparse_setup(C));
             sparse_ap<double, double>(C, C.sp.d_lhsK, C.d_y, C.d_t64);
+            break;
+        case 13:  // FP32 element tangents stored per element (element-by-element solver)
+            PH_TRY(ebe_setup(C));
+            launch_tangent_ebe<float>(C, C.d_xf, C.d_yf, C.sp.d_EGf, nullptr);
+            break;
+        case 14:  // FP32 element-by-element product (Au1GMR + bc3per)
+            PH_TRY(ebe_setup(C));
+            ebe_ap<float, float>(C, C.sp.d_EGf, C.d_yf, C.d_t32);
             break;
         default:
             return PHGPU_ERR_INVALID;
