@@ -24,7 +24,7 @@
 
 // resident CTAs per SM of the FP32 tangent (register budget 65536 / (128 x this))
 #ifndef PHGPU_TAN32_MINB
-#define PHGPU_TAN32_MINB 6
+#define PHGPU_TAN32_MINB 7
 #endif
 
 namespace phgpu {
@@ -58,9 +58,13 @@ struct TanQp {
 template <int NEN>
 constexpr int tan_epb() { return kTanThreads / (NEN * NEN); }  // elements per CTA: tet 8, hex 2, wedge 3
 
+// per (element, point q, node a): W_q (N_a I + B_a tau) and B_a + fct N_a A0, 25 + 25 values
+constexpr int kTanDC = 50;
+
 template <typename R, int NEN>
 constexpr size_t tan_smem() {
-    return sizeof(R) * (size_t)tan_epb<NEN>() * NEN * (kTanNode + TanQp<NEN>::kN) + sizeof(int) * tan_epb<NEN>() * NEN;
+    return sizeof(R) * (size_t)tan_epb<NEN>() * NEN * (kTanNode + TanQp<NEN>::kN + NEN * kTanDC) +
+           sizeof(int) * tan_epb<NEN>() * NEN * (1 + NEN);
 }
 
 // B = sum_i s_i A_i for the direction s (e3mtrx.f closed form); Us = s . u
@@ -159,8 +163,19 @@ k_tangent(const int* __restrict__ ien, const int* __restrict__ bmap, int ne, con
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* snode = reinterpret_cast<R*>(smem_raw);                 // [EPB][NEN][kTanNode]
     R* sqp = snode + EPB * NEN * kTanNode;                     // [EPB][NEN][kN]
-    int* sid = reinterpret_cast<int*>(sqp + EPB * NEN * Q::kN);  // [EPB][NEN]
+    R* sdc = sqp + EPB * NEN * Q::kN;                          // [EPB][NEN q][NEN a][kTanDC]
+    int* sid = reinterpret_cast<int*>(sdc + EPB * NB * kTanDC);  // [EPB][NEN]
+    int* sk = sid + EPB * NEN;                                 // [EPB * NB] output block of each thread
     const int e0 = blockIdx.x * EPB;
+    // start the block's lines on their way to L2 for the read-modify-write at the end
+    if (bmap && threadIdx.x < EPB * NB && e0 + (int)threadIdx.x / NB < ne) {
+        const char* o = reinterpret_cast<const char*>(
+            lhsK + 25 * (size_t)bmap[(size_t)(e0 + threadIdx.x / NB) * NB + threadIdx.x % NB]);
+#pragma unroll
+        for (int off = 0; off < 25 * (int)sizeof(R); off += 96)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(o + off));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(o + 25 * sizeof(R) - 1));
+    }
     // stage the nodes
     for (int i = threadIdx.x; i < EPB * NEN; i += blockDim.x) {
         const int le = i / NEN, a = i % NEN, e = e0 + le;
@@ -254,61 +269,82 @@ k_tangent(const int* __restrict__ ien, const int* __restrict__ bmap, int ne, con
         os[12] = st.tau[2];
     }
     __syncthreads();
-    if (threadIdx.x >= EPB * NB) return;
+    // the two factors of every (point, node): W (N_a I + B_a tau) and B_a + fct N_a A0
+    if (threadIdx.x < EPB * NB && e0 + (int)threadIdx.x / NB < ne) {
+        const int le = threadIdx.x / NB, r = threadIdx.x % NB, q = r / NEN, a = r % NEN;
+        const R* v = sqp + Q::kN * (NEN * le + q);
+        const R w = v[Q::kW];
+        const R sa[3] = {v[Q::kShg + 3 * a], v[Q::kShg + 3 * a + 1], v[Q::kShg + 3 * a + 2]};
+        const R* st = v + Q::kS;
+        const R u[3] = {st[0], st[1], st[2]};
+        const R rho = st[3], drdp = st[4], drdT = st[5], e1p = st[6], e2p = st[7], e3p = st[8], e4p = st[9];
+        const R tk[5] = {st[10], st[11], st[11], st[11], st[12]};
+        const R Na = t_shp<R>(TOPO, q, a);
+        R Bm[5][5];
+        bmat(sa, sa[0] * u[0] + sa[1] * u[1] + sa[2] * u[2], u, rho, drdp, drdT, e2p, e3p, e4p, Bm);
+        R* o = sdc + kTanDC * ((size_t)(le * NEN + q) * NEN + a);
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) o[5 * i + k] = w * (Bm[i][k] * tk[k] + (i == k ? Na : R(0)));
+        const R fN = P.fct1 * Na;
+        Bm[0][0] += fN * drdp;
+        Bm[0][4] += fN * drdT;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            Bm[1 + j][0] += fN * drdp * u[j];
+            Bm[1 + j][1 + j] += fN * rho;
+            Bm[1 + j][4] += fN * drdT * u[j];
+            Bm[4][1 + j] += fN * rho * u[j];
+        }
+        Bm[4][0] += fN * e1p;
+        Bm[4][4] += fN * e4p;
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) o[25 + 5 * i + k] = Bm[i][k];
+    }
+    __syncthreads();
+    const bool active = threadIdx.x < EPB * NB && e0 + (int)threadIdx.x / NB < ne;
     const int le = threadIdx.x / NB, ab = threadIdx.x % NB, a = ab / NEN, b = ab % NEN;
     const int e = e0 + le;
-    if (e >= ne) return;
     R M[5][5];
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
         for (int c = 0; c < 5; ++c) M[r][c] = R(0);
 #pragma unroll 1
-    for (int q = 0; q < NEN; ++q) {
-        const R* v = sqp + Q::kN * (NEN * le + q);
-        const R w = v[Q::kW];
-        const R sa[3] = {v[Q::kShg + 3 * a], v[Q::kShg + 3 * a + 1], v[Q::kShg + 3 * a + 2]};
-        const R sb[3] = {v[Q::kShg + 3 * b], v[Q::kShg + 3 * b + 1], v[Q::kShg + 3 * b + 2]};
-        const R* s = v + Q::kS;
-        const R u[3] = {s[0], s[1], s[2]};
-        const R rho = s[3], drdp = s[4], drdT = s[5], e1p = s[6], e2p = s[7], e3p = s[8], e4p = s[9];
-        const R tk[5] = {s[10], s[11], s[11], s[11], s[12]};
-        const R Na = t_shp<R>(TOPO, q, a), Nb = t_shp<R>(TOPO, q, b);
-        const R Usa = sa[0] * u[0] + sa[1] * u[1] + sa[2] * u[2];
-        const R Usb = sb[0] * u[0] + sb[1] * u[1] + sb[2] * u[2];
-        // C = B_b + fct N_b A0
+    for (int q = 0; q < (active ? NEN : 0); ++q) {
+        // W (N_a I + B_a tau)(B_b + fct N_b A0), the factors from shared memory
+        const R* Dq = sdc + kTanDC * ((size_t)(le * NEN + q) * NEN + a);
+        const R* Cq = sdc + kTanDC * ((size_t)(le * NEN + q) * NEN + b) + 25;
         R Cm[5][5];
-        bmat(sb, Usb, u, rho, drdp, drdT, e2p, e3p, e4p, Cm);
-        const R fN = P.fct1 * Nb;
-        Cm[0][0] += fN * drdp;
-        Cm[0][4] += fN * drdT;
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            Cm[1 + j][0] += fN * drdp * u[j];
-            Cm[1 + j][1 + j] += fN * rho;
-            Cm[1 + j][4] += fN * drdT * u[j];
-            Cm[4][1 + j] += fN * rho * u[j];
-        }
-        Cm[4][0] += fN * e1p;
-        Cm[4][4] += fN * e4p;
-        // D = N_a I + B_a tau, one row at a time
-        R Ba[5][5];
-        bmat(sa, Usa, u, rho, drdp, drdT, e2p, e3p, e4p, Ba);
+        for (int k = 0; k < 5; ++k)
+#pragma unroll
+            for (int c = 0; c < 5; ++c) Cm[k][c] = Cq[5 * k + c];
 #pragma unroll
         for (int r = 0; r < 5; ++r) {
             R D[5];
 #pragma unroll
-            for (int k = 0; k < 5; ++k) D[k] = Ba[r][k] * tk[k] + (r == k ? Na : R(0));
+            for (int k = 0; k < 5; ++k) D[k] = Dq[5 * r + k];
 #pragma unroll
             for (int c = 0; c < 5; ++c) {
-                R acc = R(0);
+                R acc = M[r][c];
 #pragma unroll
                 for (int k = 0; k < 5; ++k) acc += D[k] * Cm[k][c];
-                M[r][c] += w * acc;
+                M[r][c] = acc;
             }
         }
+        const R* v = sqp + Q::kN * (NEN * le + q);
+        const R w = v[Q::kW];
         if (P.navier) {
             // K_ab = sum_ij N_a,i K_ij N_b,j
+            const R sa[3] = {v[Q::kShg + 3 * a], v[Q::kShg + 3 * a + 1], v[Q::kShg + 3 * a + 2]};
+            const R sb[3] = {v[Q::kShg + 3 * b], v[Q::kShg + 3 * b + 1], v[Q::kShg + 3 * b + 2]};
+            const R u[3] = {v[Q::kS], v[Q::kS + 1], v[Q::kS + 2]};
+            const R Usa = sa[0] * u[0] + sa[1] * u[1] + sa[2] * u[2];
+            const R Usb = sb[0] * u[0] + sb[1] * u[1] + sb[2] * u[2];
             const R sab = sa[0] * sb[0] + sa[1] * sb[1] + sa[2] * sb[2];
 #pragma unroll
             for (int m = 0; m < 3; ++m) {
@@ -320,31 +356,42 @@ k_tangent(const int* __restrict__ ien, const int* __restrict__ bmap, int ne, con
             M[4][4] += w * P.con * sab;
         }
     }
-    const int* ids = sid + NEN * le;
-    const int na = ids[a], nb = ids[b];
-    // the block diagonal is the tangent's diagonal blocks before bc3LHS (asigmr.f:92-103)
-    if (bd && a == b) {
-        R* ob = bd + 25 * (size_t)na;  // row-major BDiag(n, r, c)
+    if (active) {
+        const int* ids = sid + NEN * le;
+        const int na = ids[a], nb = ids[b];
+        // the block diagonal is the tangent's diagonal blocks before bc3LHS (asigmr.f:92-103)
+        if (bd && a == b) {
+            R* ob = bd + 25 * (size_t)na;  // row-major BDiag(n, r, c)
 #pragma unroll
-        for (int r = 0; r < 5; ++r)
+            for (int r = 0; r < 5; ++r)
 #pragma unroll
-            for (int c = 0; c < 5; ++c) ob[5 * r + c] += M[r][c];
+                for (int c = 0; c < 5; ++c) ob[5 * r + c] += M[r][c];
+        }
+        const int ia = iBC[na], ib = iBC[nb];
+        if (ia | ib) bc3lhs_block(M, ia, BC + 6 * (size_t)na, ib, BC + 6 * (size_t)nb, a == b);
     }
-    const int ia = iBC[na], ib = iBC[nb];
-    if (ia | ib) bc3lhs_block(M, ia, BC + 6 * (size_t)na, ib, BC + 6 * (size_t)nb, a == b);
-    if (bmap) {
-        R* o = lhsK + 25 * (size_t)bmap[(size_t)e * NB + ab];
+    // Stage the blocks in shared memory (over the per-point factors, now read), then move
+    // each block with 25 consecutive lanes of one warp: 4-5 sectors per block instead of one
+    // sector per value.  With a block map: add into lhsK; without: element storage.
+    __syncthreads();
+    R* sblk = sdc;  // [EPB * NB][25], entry (f, g) at 5 g + f
+    if (threadIdx.x < EPB * NB) {
+        sk[threadIdx.x] = !active ? -1 : bmap ? bmap[(size_t)e * NB + ab] : e * NB + ab;
+        if (active)
 #pragma unroll
-        for (int g = 0; g < 5; ++g)
+            for (int g = 0; g < 5; ++g)
 #pragma unroll
-            for (int f = 0; f < 5; ++f) o[5 * g + f] += M[f][g];
-    } else {
-        // element-by-element storage (ElmGMRe): block (a, b) of element e, written once
-        R* o = lhsK + 25 * ((size_t)e * NB + ab);
-#pragma unroll
-        for (int g = 0; g < 5; ++g)
-#pragma unroll
-            for (int f = 0; f < 5; ++f) o[5 * g + f] = M[f][g];
+                for (int f = 0; f < 5; ++f) sblk[25 * threadIdx.x + 5 * g + f] = M[f][g];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int j = warp; j < EPB * NB; j += nwarps) {
+        const int k = sk[j];
+        if (k < 0 || lane >= 25) continue;
+        R* o = lhsK + 25 * (size_t)k + lane;
+        const R v = sblk[25 * j + lane];
+        if (bmap) *o = *o + v;
+        else *o = v;
     }
 }
 
