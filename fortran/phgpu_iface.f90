@@ -7,7 +7,7 @@ module phgpu_iface
 
   integer(c_int), parameter :: PHGPU_OK = 0
   integer(c_int), parameter :: PHGPU_FP64 = 0, PHGPU_MIXED = 1
-  integer(c_int), parameter :: PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1, PHGPU_AP_SPARSE = 2
+  integer(c_int), parameter :: PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1, PHGPU_AP_SPARSE = 2, PHGPU_AP_EBE = 3
   integer(c_int), parameter :: PHGPU_RES_FP64 = 0, PHGPU_RES_GALERKIN64 = 1
 
   type, bind(C) :: phgpu_config
@@ -109,6 +109,31 @@ module phgpu_iface
        real(c_double), intent(in) :: y(*), ac(*)
        integer(c_int), value :: lhs
        real(c_double), intent(out) :: res(*), bdiag(*), Dy(*), lhsK(*)
+       type(phgpu_stats), intent(inout) :: st
+     end function
+     integer(c_int) function phgpu_elmgmre(ctx, y, ac, res, bdiag, EGmass) bind(C, name="phgpu_elmgmre")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: y(*), ac(*)
+       real(c_double), intent(out) :: res(*), bdiag(*), EGmass(*)
+     end function
+     integer(c_int) function phgpu_i3pre(ctx, bdiag, EGmass) bind(C, name="phgpu_i3pre")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: bdiag(*)
+       real(c_double), intent(inout) :: EGmass(*)
+     end function
+     integer(c_int) function phgpu_au1gmr(ctx, EGmass, p) bind(C, name="phgpu_au1gmr")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: EGmass(*)
+       real(c_double), intent(inout) :: p(*)
+     end function
+     integer(c_int) function phgpu_solgmre(ctx, y, ac, res, bdiag, Dy, EGmass, st) bind(C, name="phgpu_solgmre")
+       import :: c_int, c_double, c_ptr, phgpu_stats
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: y(*), ac(*)
+       real(c_double), intent(out) :: res(*), bdiag(*), Dy(*), EGmass(*)
        type(phgpu_stats), intent(inout) :: st
      end function
      type(c_ptr) function phgpu_last_error(ctx) bind(C, name="phgpu_last_error")
