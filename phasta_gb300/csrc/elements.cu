@@ -27,6 +27,9 @@
 #ifndef PHGPU_FULL32_MINB
 #define PHGPU_FULL32_MINB 3
 #endif
+#ifndef PHGPU_FULL32BD_MINB
+#define PHGPU_FULL32BD_MINB 4
+#endif
 #ifndef PHGPU_RESS_MINB
 #define PHGPU_RESS_MINB 3
 #endif
@@ -1050,7 +1053,7 @@ k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float
 // element; the quadrature-point state is evaluated by each of the four
 // threads of an element.  35 outputs: res 0-4, rmes 5-9, BDiag 10-34.
 // --------------------------------------------------------------------------
-constexpr int kFullOut = 35;
+constexpr int kFullOutAll = 35;  // res 0-4, rmes 5-9, BDiag 10-34
 constexpr int kFullSub = kChunk / 4;  // elements per sub-batch (4 threads each)
 template <typename R> constexpr int full_nsub() { return sizeof(R) == 4 ? 4 : 1; }
 
@@ -1058,51 +1061,58 @@ template <typename R> constexpr int full_nsub() { return sizeof(R) == 4 ? 4 : 1;
 // point q = a once and the four lanes exchange the point data by shuffles.
 constexpr int kQpVals = 25;  // u(3) p rho ek drdp drdT e1p e2p e3p e4p tau(3) A_i Y,i (5) A0 Y,t (5)
 
-template <typename R>
+// BD_ONLY: BDiag alone (the mixed-precision preconditioner), 25 outputs: no gradients,
+// viscous stress or residual terms, and 15 shuffled point values instead of 25
+template <typename R, bool BD_ONLY = false>
 __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R (&xl)[4][3], const R (&yl)[4][5],
                                                const R (&al)[4][5], R* __restrict__ out35,
                                                const R* divq = nullptr) {
+    constexpr int NV = BD_ONLY ? 15 : kQpVals;
     Geo<R> geo;
     geometry(xl, geo);
     R g[3][5];
-    gradients(geo, yl, g);
     Visc<R> vs;
-    if (P.navier) viscous(P, g, vs);
+    if constexpr (!BD_ONLY) {
+        gradients(geo, yl, g);
+        if (P.navier) viscous(P, g, vs);
+    }
     R s[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) s[i] = (a == 0) ? geo.shg[0][i] : (a == 1) ? geo.shg[1][i] : (a == 2) ? geo.shg[2][i] : geo.shg[3][i];
     const R ss = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
     R sv[3] = {R(0), R(0), R(0)}, sq = R(0);
-    if (P.navier) {
+    if (!BD_ONLY && P.navier) {
 #pragma unroll
         for (int j = 0; j < 3; ++j) sv[j] = s[0] * vs.t[0][j] + s[1] * vs.t[1][j] + s[2] * vs.t[2][j];
         sq = s[0] * vs.q[0] + s[1] * vs.q[1] + s[2] * vs.q[2];
     }
     // this lane's quadrature point (q = a)
-    R own[kQpVals];
+    R own[NV];
     {
         R N[4];
 #pragma unroll
         for (int n = 0; n < 4; ++n) N[n] = shp<R>(a, n);
-        R yq[5], aq[5];
+        R yq[5];
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            yq[k] = N[0] * yl[0][k] + N[1] * yl[1][k] + N[2] * yl[2][k] + N[3] * yl[3][k];
-            aq[k] = N[0] * al[0][k] + N[1] * al[1][k] + N[2] * al[2][k] + N[3] * al[3][k];
-        }
+        for (int k = 0; k < 5; ++k) yq[k] = N[0] * yl[0][k] + N[1] * yl[1][k] + N[2] * yl[2][k] + N[3] * yl[3][k];
         Qp<R> b;
         qp_state(P, yq[0], yq[1], yq[2], yq[3], yq[4], b);
         qp_tau(P, geo, b);
-        R aig[5], a0a[5];
-        ai_gi(b, g, aig);
-        a0_v(b, aq, a0a);
         own[0] = b.u[0]; own[1] = b.u[1]; own[2] = b.u[2]; own[3] = b.p; own[4] = b.rho; own[5] = b.ei + b.rk;
         own[6] = b.drdp; own[7] = b.drdT; own[8] = b.e1p; own[9] = b.e2p; own[10] = b.e3p; own[11] = b.e4p;
         own[12] = b.tau[0]; own[13] = b.tau[1]; own[14] = b.tau[2];
+        if constexpr (!BD_ONLY) {
+            R aq[5];
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            own[15 + k] = aig[k];
-            own[20 + k] = a0a[k];
+            for (int k = 0; k < 5; ++k) aq[k] = N[0] * al[0][k] + N[1] * al[1][k] + N[2] * al[2][k] + N[3] * al[3][k];
+            R aig[5], a0a[5];
+            ai_gi(b, g, aig);
+            a0_v(b, aq, a0a);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                own[15 + k] = aig[k];
+                own[20 + k] = a0a[k];
+            }
         }
     }
     R rl[5], rml[5], B_[5][5];
@@ -1118,21 +1128,12 @@ __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R 
     for (int q = 0; q < 4; ++q) {
         R v[kQpVals];
 #pragma unroll
-        for (int i = 0; i < kQpVals; ++i) v[i] = __shfl_sync(0xffffffffu, own[i], base_lane + q);
+        for (int i = 0; i < NV; ++i) v[i] = __shfl_sync(0xffffffffu, own[i], base_lane + q);
         const R Na = shp<R>(q, a);
         const R u0 = v[0], u1 = v[1], u2 = v[2], p = v[3], rho = v[4], ek = v[5];
         const R drdp = v[6], drdT = v[7], e1p = v[8], e2p = v[9], e3p = v[10], e4p = v[11];
         const R tk[5] = {v[12], v[13], v[13], v[13], v[14]};
         const R uu[3] = {u0, u1, u2};
-        R lt[5], lm[5], rm16[5];
-        const R du[5] = {rho, rho * u0, rho * u1, rho * u2, rho * ek};
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            rm16[k] = v[15 + k] + P.fct1 * du[k];
-            const R dq = (divq && k > 0) ? divq[k - 1] : R(0);  // idiff = 1 (e3ls.f:147-156)
-            lt[k] = tk[k] * (v[15 + k] + v[20 + k] - dq);
-            lm[k] = tk[k] * rm16[k];
-        }
         const R Us = s[0] * u0 + s[1] * u1 + s[2] * u2;
         R Bm[5][5];
         Bm[0][0] = drdp * Us;
@@ -1148,24 +1149,35 @@ __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R 
         }
         Bm[4][0] = e2p * Us;
         Bm[4][4] = e4p * Us;
-        R fe[5];
-        const R m = -rho * Us;
-        fe[0] = m;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) fe[1 + j] = m * uu[j] - s[j] * p + sv[j];
-        const R usv = u0 * sv[0] + u1 * sv[1] + u2 * sv[2] + sq;
-        fe[4] = m * ek - Us * p + usv;
-#pragma unroll
-        for (int r = 0; r < 5; ++r) {
-            R bt = R(0), bm = R(0);
+        if constexpr (!BD_ONLY) {
+            R lt[5], lm[5], rm16[5];
+            const R du[5] = {rho, rho * u0, rho * u1, rho * u2, rho * ek};
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
-                bt += Bm[r][k] * lt[k];
-                bm += Bm[r][k] * lm[k];
+                rm16[k] = v[15 + k] + P.fct1 * du[k];
+                const R dq = (divq && k > 0) ? divq[k - 1] : R(0);  // idiff = 1 (e3ls.f:147-156)
+                lt[k] = tk[k] * (v[15 + k] + v[20 + k] - dq);
+                lm[k] = tk[k] * rm16[k];
             }
-            const R fm = (r == 0) ? R(0) : (r == 4) ? usv : sv[r - 1];
-            rl[r] += fe[r] + bt + Na * v[20 + r];
-            rml[r] += fm + bm + Na * rm16[r];
+            R fe[5];
+            const R m = -rho * Us;
+            fe[0] = m;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) fe[1 + j] = m * uu[j] - s[j] * p + sv[j];
+            const R usv = u0 * sv[0] + u1 * sv[1] + u2 * sv[2] + sq;
+            fe[4] = m * ek - Us * p + usv;
+#pragma unroll
+            for (int r = 0; r < 5; ++r) {
+                R bt = R(0), bm = R(0);
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    bt += Bm[r][k] * lt[k];
+                    bm += Bm[r][k] * lm[k];
+                }
+                const R fm = (r == 0) ? R(0) : (r == 4) ? usv : sv[r - 1];
+                rl[r] += fe[r] + bt + Na * v[20 + r];
+                rml[r] += fm + bm + Na * rm16[r];
+            }
         }
         // BDiag: (N_a I + B_a tau)(B_a + fct N_a A0) + K_a
         const R fN = P.fct1 * Na;
@@ -1221,22 +1233,27 @@ __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R 
         }
     }
     const R w = geo.WdetJ;
+    constexpr int o0 = BD_ONLY ? 0 : 10;
+    if constexpr (!BD_ONLY) {
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-        out35[k] = w * rl[k];
-        out35[5 + k] = w * rml[k];
+        for (int k = 0; k < 5; ++k) {
+            out35[k] = w * rl[k];
+            out35[5 + k] = w * rml[k];
+        }
     }
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
-        for (int cc = 0; cc < 5; ++cc) out35[10 + 5 * r + cc] = w * B_[r][cc];
+        for (int cc = 0; cc < 5; ++cc) out35[o0 + 5 * r + cc] = w * B_[r][cc];
 }
 
-template <typename R>
-__global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? PHGPU_FULL32_MINB : 2)
+template <typename R, bool BD_ONLY>
+__global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? (BD_ONLY ? PHGPU_FULL32BD_MINB : PHGPU_FULL32_MINB) : 2)
 k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restrict__ y, const R* __restrict__ ac,
              R* __restrict__ res, R* __restrict__ rmes, R* __restrict__ bd, Phys<R> P,
              const R* __restrict__ ql = nullptr) {
+    constexpr int kFullOut = BD_ONLY ? 25 : kFullOutAll;  // values per slot: BDiag, or res rmes BDiag
+    constexpr int kBd = BD_ONLY ? 0 : 10;                    // offset of BDiag in a slot
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* sm = reinterpret_cast<R*>(smem_raw);
     const int c = chunk0 + blockIdx.x;
@@ -1288,9 +1305,9 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
             if (with_q) {
                 R divq[4];
                 tet_divq(xl, sq, nd, divq);
-                elem_full_node<R>(P, a, xl, yl, al, o35, divq);
+                elem_full_node<R, BD_ONLY>(P, a, xl, yl, al, o35, divq);
             } else {
-                elem_full_node<R>(P, a, xl, yl, al, o35);
+                elem_full_node<R, BD_ONLY>(P, a, xl, yl, al, o35);
             }
             if (valid) {
                 R* sl = slot + kFullOut * (sb * kChunk + threadIdx.x);
@@ -1313,17 +1330,17 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
                     for (int k = 0; k < kFullOut; ++k) t[k] += sl[k];
                 }
                 const size_t gn = ca.nodes[n0 + l];
-                if (res) {
+                if (!BD_ONLY && res) {
 #pragma unroll
                     for (int k = 0; k < 5; ++k) res[5 * gn + k] += t[k];
                 }
-                if (rmes) {
+                if (!BD_ONLY && rmes) {
 #pragma unroll
                     for (int k = 0; k < 5; ++k) rmes[5 * gn + k] += t[5 + k];
                 }
                 if (bd) {
 #pragma unroll
-                    for (int k = 0; k < 25; ++k) bd[25 * gn + k] += t[10 + k];
+                    for (int k = 0; k < 25; ++k) bd[25 * gn + k] += t[kBd + k];
                 }
             }
             return;
@@ -1344,17 +1361,17 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
         const size_t gn = ca.nodes[n0 + l];
         const R* ac_ = acc + kFullOut * l;
-        if (res) {
+        if (!BD_ONLY && res) {
 #pragma unroll
             for (int k = 0; k < 5; ++k) res[5 * gn + k] += ac_[k];
         }
-        if (rmes) {
+        if (!BD_ONLY && rmes) {
 #pragma unroll
             for (int k = 0; k < 5; ++k) rmes[5 * gn + k] += ac_[5 + k];
         }
         if (bd) {
 #pragma unroll
-            for (int k = 0; k < 25; ++k) bd[25 * gn + k] += ac_[10 + k];
+            for (int k = 0; k < 25; ++k) bd[25 * gn + k] += ac_[kBd + k];
         }
     }
 }
@@ -1998,10 +2015,11 @@ template <typename R>
 size_t q_smem(const Ctx& C) { return sizeof(R) * (size_t)C.chunk_lmax * 12; }
 template <typename R>
 size_t qrec_smem(const Ctx& C) { return sizeof(R) * ((size_t)C.chunk_lmax * 8 + (size_t)kChunk * 52); }
-template <typename R>
+template <typename R, bool BD_ONLY = false>
 size_t full_smem(const Ctx& C) {
     const bool single = kFullSub * full_nsub<R>() >= kChunk;
-    return sizeof(R) * ((size_t)C.chunk_lmax * (13 + (single ? 0 : kFullOut)) + (size_t)kChunk * full_nsub<R>() * kFullOut);
+    const size_t out = BD_ONLY ? 25 : kFullOutAll;
+    return sizeof(R) * ((size_t)C.chunk_lmax * (13 + (single ? 0 : out)) + (size_t)kChunk * full_nsub<R>() * out);
 }
 
 size_t resh_smem(const Ctx& C) {
@@ -2024,7 +2042,9 @@ int configure_chunk_kernels(Ctx& C) {
     T(cudaFuncSetAttribute(k_chunk_qrec<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qrec_smem<R>(C)));
     T(cudaFuncSetAttribute(k_chunk_res<R, RM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
     T(cudaFuncSetAttribute(k_chunk_res<R, RM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
-    T(cudaFuncSetAttribute(k_chunk_full<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, fs + (int)q_smem<R>(C)));
+    T(cudaFuncSetAttribute(k_chunk_full<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fs + (int)q_smem<R>(C)));
+    T(cudaFuncSetAttribute(k_chunk_full<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)full_smem<R, true>(C)));
     return rc;
 }
 int configure_element_kernels(Ctx& C) {
@@ -2133,12 +2153,18 @@ template <typename R>
 void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rmes, R* bd, const R* ql) {
     const Phys<R> P = make_phys<R>(C.cfg);
     const ChunkArgs ca = chunk_args(C);
-    const size_t sm = full_smem<R>(C) + ((ql && res) ? q_smem<R>(C) : 0);
+    // BDiag alone (the mixed-precision preconditioner) runs the kernel without the residual terms
+    const bool bd_only = !res && !rmes;
+    const size_t sm = bd_only ? full_smem<R, true>(C) : full_smem<R>(C) + ((ql && res) ? q_smem<R>(C) : 0);
     const int ncol = (int)C.chunk_col_start.size() - 1;
     for (int c = 0; c < ncol; ++c) {
         const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
         if (nc <= 0) continue;
-        k_chunk_full<R><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, ac, res, rmes, bd, P, (ql && res) ? ql : nullptr);
+        if (bd_only)
+            k_chunk_full<R, true><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, ac, nullptr, nullptr, bd, P, nullptr);
+        else
+            k_chunk_full<R, false><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, ac, res, rmes, bd, P,
+                                                               (ql && res) ? ql : nullptr);
         ++C.launches;
     }
     launch_topo<R>(C, TM_FULL, x, y, nullptr, ac, res, rmes, bd, 0, nullptr, (ql && res) ? ql : nullptr);
