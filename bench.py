@@ -10,8 +10,8 @@ time step.  Synthetic data (no mesh files exist for it).
 A "step" is one Newton iteration (one flow solve of the itrdrv multi-corrector:
 SolMFG + itrCorrect + itrBC).  Steps run in time steps of 3 iterations.
 ``value`` = elements x steps / device time, inputs resident in HBM;
-``e2e`` = the same through the host-buffer C ABI (phgpu_time_step), host<->device
-copies inside the timed region.  The state and mesh (> 300 MB) exceed the
+``e2e`` = the same through the host-buffer C ABI (phgpu_time_step) on pinned host
+buffers, host<->device copies inside the timed region.  The state and mesh (> 300 MB) exceed the
 129 MB L2, so no flush is needed between steps.
 
 ``--impl reference`` times the reference algorithm's CPU restatement (the
@@ -197,14 +197,21 @@ def run_gpu(args, rank, world):
         rn.append(st.rnorm)
     r_end = g.residual_norm_dev()
 
-    # e2e: host buffers through the reference-facing time-step call
-    yold, acold = y0.copy(), ac0.copy()
+    # e2e: pinned host buffers through the reference-facing time-step call (phgpu_time_step:
+    # H2D of yold/acold, 3 Newton iterations, D2H of y/ac/yold/acold, every time step)
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        h = t.numpy()
+        h[:] = a
+        return t, h
+    keep = [pinned(y0), pinned(ac0), pinned(y0), pinned(ac0)]
+    yold, acold, y, ac = (k[1] for k in keep)
     g.set_params(istep=0, eGMRES=0.0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ksteps = max(1, args.steps // NEWTON_PER_TIMESTEP)
     for _ in range(ksteps):
-        yold, acold, y, ac, st = g.time_step(yold, acold, NEWTON_PER_TIMESTEP)
+        st = g.time_step_into(yold, acold, y, ac, NEWTON_PER_TIMESTEP)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_steps = ksteps * NEWTON_PER_TIMESTEP

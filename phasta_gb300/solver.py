@@ -312,6 +312,16 @@ class GpuSolver:
         self.ntotGM = st.ntotGM
         return res, bd, Dy, (None if EG is None else EG.transpose(2, 1, 0)), _stats(st)
 
+    def time_step_into(self, yold, acold, y, ac, nitr: int):
+        """time_step on caller-owned arrays (float64, contiguous; pinned host memory keeps the
+        copies at the link's bandwidth): yold/acold updated in place, y/ac written."""
+        st = L.Stats()
+        st.ntotGM = self.ntotGM
+        self._check(self.lib.phgpu_time_step(self.h, L.dptr(yold), L.dptr(acold), L.dptr(y), L.dptr(ac), nitr,
+                                             C.byref(st)))
+        self.ntotGM = st.ntotGM
+        return _stats(st)
+
     # -- device-resident path (benchmarks) --
     def upload(self, y=None, ac=None, yold=None, acold=None):
         self._check(self.lib.phgpu_upload_state(self.h, L.dptr(y), L.dptr(ac), L.dptr(yold), L.dptr(acold)))
