@@ -192,16 +192,19 @@ __global__ void k_periodic_copy(const int* __restrict__ slaves, int ns, const in
 // The factorization follows i3lu.f:41-97 statement by statement, including
 // that U(4,5) is left at its input value (the reference updates every other
 // upper entry of rows 2-5 but not that one).
-template <typename R>
-__global__ void k_lu_fact(R* __restrict__ bd, int N, int* __restrict__ flag) {
+template <typename R, typename I>
+// the factors of the blocks in `in` (type I) are written to bd (type R) and, when given, to bdf
+// as floats; in may be bd or bdf (each thread reads its block before writing it)
+__global__ void k_lu_fact(const I* in, R* bd, float* bdf, int N, int* __restrict__ flag) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= N) return;
     R a[5][5];
     R* p = bd + 25 * (size_t)n;
+    const I* pi = in + 25 * (size_t)n;
 #pragma unroll
     for (int i = 0; i < 5; ++i)
 #pragma unroll
-        for (int j = 0; j < 5; ++j) a[i][j] = p[5 * i + j];
+        for (int j = 0; j < 5; ++j) a[i][j] = (R)pi[5 * i + j];
     bool bad = false;
     auto inv = [&](R v) {
         if (!(v == v) || v == R(0) || isinf(v)) bad = true;
@@ -235,6 +238,13 @@ __global__ void k_lu_fact(R* __restrict__ bd, int N, int* __restrict__ flag) {
     for (int i = 0; i < 5; ++i)
 #pragma unroll
         for (int j = 0; j < 5; ++j) p[5 * i + j] = a[i][j];
+    if (bdf) {
+        float* pf = bdf + 25 * (size_t)n;
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+#pragma unroll
+            for (int j = 0; j < 5; ++j) pf[5 * i + j] = (float)a[i][j];
+    }
     if (bad && flag) atomicOr(flag + 1, 1);
 }
 
@@ -571,11 +581,16 @@ void itrbc_state(Ctx& C, double* y, double* ac, bool with_ac) {
 
 template <typename R>
 void lu_fact(Ctx& C, R* bd, int* flag) {
-    k_lu_fact<R><<<nblocks(C.N), kT, 0, C.stream>>>(bd, C.N, flag);
+    k_lu_fact<R, R><<<nblocks(C.N), kT, 0, C.stream>>>(bd, bd, nullptr, C.N, flag);
     ++C.launches;
 }
 template void lu_fact<double>(Ctx&, double*, int*);
 template void lu_fact<float>(Ctx&, float*, int*);
+
+void lu_fact_f32(Ctx& C, float* bdf, double* bd, int* flag) {
+    k_lu_fact<double, float><<<nblocks(C.N), kT, 0, C.stream>>>(bdf, bd, bdf, C.N, flag);
+    ++C.launches;
+}
 
 template <typename R, typename V>
 void lu_apply(Ctx& C, const R* bd, V* r, int code) {

@@ -211,6 +211,8 @@ template <typename R> void bc3bdg(Ctx& C, const double* y, R* bd);
 template <typename R> void itrbc_pert(Ctx& C, R* v, bool zero_dirichlet);
 void itrbc_state(Ctx& C, double* y, double* ac, bool with_ac);
 template <typename R> void lu_fact(Ctx& C, R* bd, int* flag);
+// FP32 blocks bdf factored in FP64 into bd, and the factors rounded back into bdf (mixed precision)
+void lu_fact_f32(Ctx& C, float* bdf, double* bd, int* flag);
 template <typename R, typename V> void lu_apply(Ctx& C, const R* bd, V* r, int code);
 template <typename R, typename V> void lu_apply(Ctx& C, const R* bd, const V* in, V* out, int code);
 void ref_to_dev_state(Ctx& C, const double* h_ref, double* d_tmp_host_layout, double* d_out);

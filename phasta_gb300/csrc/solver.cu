@@ -631,15 +631,14 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
                 launch_elem_full<float>(C, C.d_xf, C.d_yf, C.d_acf, nullptr, nullptr, C.d_bdf);
             }
             bc3bdg<float>(C, C.d_y, C.d_bdf);
-            to_f64(C, C.d_bdf, C.d_bd, 25 * N);
         }
     }
     // nonlinear residual ||R|| (FP64, unpreconditioned)
     dot<double>(C, C.d_res, C.d_res, n5, S_TMP3, nullptr);
     fill0(C, C.d_flag, sizeof(int) * 2);
     if (asm_bd) {
-        lu_fact<double>(C, C.d_bd, C.d_flag);
-        if (C.cfg.precision == PHGPU_MIXED) to_f32(C, C.d_bd, C.d_bdf, 25 * N);
+        if (C.cfg.precision == PHGPU_MIXED) lu_fact_f32(C, C.d_bdf, C.d_bd, C.d_flag);
+        else lu_fact<double>(C, C.d_bd, C.d_flag);
     }
     lu_apply<double, double>(C, C.d_bd, C.d_res, PHGPU_LU_FORWARD);
     if (sparse) {
