@@ -1274,7 +1274,7 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             sy[5 * l + k] = ldg(y + 5 * (size_t)gn + k);
-            sa[5 * l + k] = ldg(ac + 5 * (size_t)gn + k);
+            if (!BD_ONLY) sa[5 * l + k] = ldg(ac + 5 * (size_t)gn + k);  // the block diagonal needs no ac
         }
         if (with_q)
             for (int k = 0; k < 12; ++k) sq[12 * l + k] = ldg(ql + 13 * (size_t)gn + k);
@@ -1299,7 +1299,12 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
 #pragma unroll
                 for (int d = 0; d < 3; ++d) xl[n][d] = sx[3 * nd[n] + d];
                 lds5(sy, nd[n], yl[n]);
-                lds5(sa, nd[n], al[n]);
+                if (BD_ONLY) {
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) al[n][k] = R(0);
+                } else {
+                    lds5(sa, nd[n], al[n]);
+                }
             }
             R o35[kFullOut];
             if (with_q) {
