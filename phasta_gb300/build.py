@@ -18,7 +18,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 LIB = PKG / "libphgpu.so"
 BUILD = PKG / "_build"
-SOURCES = ["elements.cu", "nodal.cu", "solver.cu", "chunks.cu", "noalloc.cu", "sparse.cu", "tangent.cu"]
+SOURCES = ["elements.cu", "nodal.cu", "solver.cu", "chunks.cu", "noalloc.cu", "sparse.cu", "tangent.cu", "topo_ress.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

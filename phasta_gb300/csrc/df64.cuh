@@ -77,4 +77,12 @@ __device__ __forceinline__ df64 df_rcp(df64 b) {
 
 __device__ __forceinline__ double df_to_double(df64 a) { return (double)a.hi + (double)a.lo; }
 
+// (ah + al) - (bh + bl) of two hi/lo pairs, as a double-float
+__device__ __forceinline__ df64 df_diff(float ah, float al, float bh, float bl) {
+    float s, e;
+    two_sum(ah, -bh, s, e);
+    e = __fadd_rn(e, __fsub_rn(al, bl));
+    return quick_two_sum(s, e);
+}
+
 }  // namespace phgpu

@@ -181,66 +181,6 @@ __device__ __forceinline__ void gradients(const Geo<R>& geo, const R (&v)[4][5],
                       geo.shg[3][i] * v[3][k];
 }
 
-// viscous stress (symmetric) and heat flux of a gradient field (e3visc.f:278-368)
-template <typename R>
-struct Visc {
-    R t[3][3];
-    R q[3];
-};
-template <typename R>
-__device__ __forceinline__ void viscous(const Phys<R>& P, const R (&g)[3][5], Visc<R>& v) {
-    const R divu = g[0][1] + g[1][2] + g[2][3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-#pragma unroll
-        for (int j = 0; j < 3; ++j) v.t[i][j] = P.rmu * (g[i][1 + j] + g[j][1 + i]);
-        v.t[i][i] = P.rlm * divu + R(2) * P.rmu * g[i][1 + i];
-        v.q[i] = P.con * g[i][4];
-    }
-}
-
-// sum_i A_i Y,i (e3conv.f:100-179) in closed form
-template <typename R>
-__device__ __forceinline__ void ai_gi(const Qp<R>& b, const R (&g)[3][5], R (&o)[5]) {
-    const R u0 = b.u[0], u1 = b.u[1], u2 = b.u[2];
-    const R ugp = u0 * g[0][0] + u1 * g[1][0] + u2 * g[2][0];
-    const R ugT = u0 * g[0][4] + u1 * g[1][4] + u2 * g[2][4];
-    const R divu = g[0][1] + g[1][2] + g[2][3];
-    const R c0 = b.drdp * ugp + b.rho * divu + b.drdT * ugT;
-    R adv[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) adv[d] = u0 * g[0][1 + d] + u1 * g[1][1 + d] + u2 * g[2][1 + d];
-    o[0] = c0;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) o[1 + d] = b.u[d] * c0 + g[d][0] + b.rho * adv[d];
-    o[4] = b.e2p * ugp + b.e3p * divu + b.rho * (u0 * adv[0] + u1 * adv[1] + u2 * adv[2]) + b.e4p * ugT;
-}
-
-// A0 v
-template <typename R>
-__device__ __forceinline__ void a0_v(const Qp<R>& b, const R (&v)[5], R (&o)[5]) {
-    const R s = b.drdp * v[0] + b.drdT * v[4];
-    o[0] = s;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) o[1 + j] = b.u[j] * s + b.rho * v[1 + j];
-    o[4] = b.e1p * v[0] + b.rho * (b.u[0] * v[1] + b.u[1] * v[2] + b.u[2] * v[3]) + b.e4p * v[4];
-}
-
-// F_i += A_i v for i = 0..2
-template <typename R>
-__device__ __forceinline__ void add_ai_v(const Qp<R>& b, const R (&v)[5], R (&F)[3][5]) {
-    const R s = b.drdp * v[0] + b.drdT * v[4];
-    const R t = b.e2p * v[0] + b.rho * (b.u[0] * v[1] + b.u[1] * v[2] + b.u[2] * v[3]) + b.e4p * v[4];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const R r0 = b.u[i] * s + b.rho * v[1 + i];
-        F[i][0] += r0;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) F[i][1 + j] += b.u[j] * r0 + b.rho * b.u[i] * v[1 + j] + (i == j ? v[0] : R(0));
-        F[i][4] += b.u[i] * t + b.e3p * v[1 + i];
-    }
-}
-
 template <typename R>
 __device__ __forceinline__ void load5(const R* __restrict__ a, int n, R (&o)[5]) {
     const R* p = a + 5 * (size_t)n;
@@ -801,12 +741,6 @@ struct DfConst {
 
 constexpr int kSplitSlot = 40;  // per element: 20 hi then 20 lo
 
-__device__ __forceinline__ df64 df_diff(float ah, float al, float bh, float bl) {
-    float s, e;
-    two_sum(ah, -bh, s, e);
-    e = __fadd_rn(e, __fsub_rn(al, bl));
-    return quick_two_sum(s, e);
-}
 
 template <bool WITH_Q>
 __global__ void __launch_bounds__(kChunk, PHGPU_RESS_MINB)

@@ -142,6 +142,10 @@ struct Ctx {
     float* d_ylo = nullptr;       // y - (double)d_yf, rounded to float (double-float residual)
     double* d_qres = nullptr;     // idiff = 1: reconstructed diffusive flux, 13 per node (12 + lumped mass)
     float* d_qresf = nullptr;     //   its FP32 copy for the mixed outer residual
+    // hex/wedge split residual: per (element, node, direction) I_a,i = sum_q W_q N_a,i as hi/lo
+    bool split_ready = false;
+    float2* d_Ih = nullptr;
+    float2* d_Iw = nullptr;
 
     // work arrays
     double *d_res = nullptr, *d_rmes = nullptr, *d_bd = nullptr, *d_Dy = nullptr, *d_bdstage = nullptr;
@@ -196,6 +200,9 @@ void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf
 // outer residual with no FP64 arithmetic: double-float element-constant flux + FP32 increments
 void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* acf, double* out,
                       const float* ql = nullptr);
+// the same for the hex and wedge blocks (topo_ress.cu); topo_split_setup forms I_a,i once
+int topo_split_setup(Ctx& C);
+void launch_topo_ress(Ctx& C, const float* yh, const float* ylo, const float* acf, double* out, const float* ql);
 // hex and wedge blocks; mode RM_RES/RM_MODRES/RM_LIN or 4 (ires = 3 + block diagonal)
 template <typename R>
 void launch_topo(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R* ac, R* res, R* rmes, R* bd,

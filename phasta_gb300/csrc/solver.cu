@@ -612,8 +612,14 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
             if (C.cfg.outer_residual == PHGPU_RES_SPLITDF)
                 launch_elem_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res, ql ? C.d_qresf : nullptr);
             else launch_elem_resh(C, C.d_y, C.d_ac, C.d_yf, C.d_acf, C.d_res);
-            // hex and wedge blocks: FP64 outer residual
-            launch_topo<double>(C, RM_RES, C.d_x, C.d_y, nullptr, C.d_ac, C.d_res, nullptr, nullptr, 0, nullptr, ql);
+            // hex and wedge blocks: the same split residual, or FP64 with the Galerkin64 option
+            if (C.cfg.outer_residual == PHGPU_RES_SPLITDF && (C.nhex > 0 || C.nwedge > 0)) {
+                PH_TRY(topo_split_setup(C));
+                launch_topo_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res, ql ? C.d_qresf : nullptr);
+            } else {
+                launch_topo<double>(C, RM_RES, C.d_x, C.d_y, nullptr, C.d_ac, C.d_res, nullptr, nullptr, 0, nullptr,
+                                    ql);
+            }
             if (C.Eb > 0) launch_boundary(C, C.d_y, C.d_res);
             bc3res<double>(C, C.d_res);
         } else {
@@ -981,7 +987,7 @@ int phgpu_destroy(phgpu_ctx* h) {
                     C.d_rmes, C.d_Dy, C.d_ypre, C.d_t64, C.d_t64b, C.d_bd, C.d_yf, C.d_ylo, C.d_acf, C.d_resf, C.d_rmesf,
                     C.d_t32, C.d_t32b, C.d_bdf, C.d_qres, C.d_qresf, C.d_U, C.d_scal, C.d_part, C.d_count, C.d_flag,
                     C.sp.d_rs, C.sp.d_bcol, C.sp.d_bcolp, C.sp.d_brow, C.sp.d_ient, C.sp.d_tmap, C.sp.d_hmap,
-                    C.sp.d_wmap, C.sp.d_lhsK, C.sp.d_lhsKf, C.sp.d_EG, C.sp.d_EGf};
+                    C.sp.d_wmap, C.sp.d_lhsK, C.sp.d_lhsKf, C.sp.d_EG, C.sp.d_EGf, C.d_Ih, C.d_Iw};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (C.h_scal) cudaFreeHost(C.h_scal);
@@ -1409,6 +1415,10 @@ int phgpu_sweep_dev(phgpu_ctx* h, int which) {
             break;
         case 7:  // double-float constant flux + FP32 increments (needs the hi/lo split of case 8)
             launch_elem_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res);
+            if (C.nhex > 0 || C.nwedge > 0) {
+                PH_TRY(topo_split_setup(C));
+                launch_topo_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res, nullptr);
+            }
             break;
         case 8:
             split_f32(C, C.d_y, C.d_yf, C.d_ylo, n5);

@@ -14,7 +14,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from helpers import channel, rel, vortex
+from helpers import channel, mixed, rel, vortex
 from oracle import pyoracle
 from phasta_gb300 import _lib as L
 from phasta_gb300 import mesh
@@ -232,3 +232,18 @@ def test_split_double_float_outer_residual(gpu_lib, which):
     if which != "channel_idiff":  # the FP64-Galerkin hybrid does not take idiff = 1
         rgl, _, _, sgl = GpuSolver(case, dict(base, outer_residual=L.PHGPU_RES_GALERKIN64)).SolMFG(y, ac)
         assert rel(rdf, r64) < rel(rgl, r64) / 3
+
+
+@pytest.mark.parametrize("idiff", [0, 1])
+def test_split_double_float_outer_residual_hex_wedge(gpu_lib, idiff):
+    """The split residual of the hex and wedge blocks (element-constant flux through the
+    FP64-formed integrals I_a,i = sum_q W_q N_a,i in double-float, FP32 increments) against
+    the FP64 outer residual of the same mixed solve, on disjoint tet/hex/wedge blocks with the
+    channel's perturbed free stream.  Tolerance 1e-6 relative, as for the tet channel."""
+    case, p, y, ac = mixed(6, 6, (6, 6, 3), idiff=idiff)
+    base = dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR)
+    r64, _, _, s64 = GpuSolver(case, dict(base, outer_residual=L.PHGPU_RES_FP64)).SolMFG(y, ac)
+    rdf, _, _, sdf = GpuSolver(case, dict(base, outer_residual=L.PHGPU_RES_SPLITDF)).SolMFG(y, ac)
+    assert rel(rdf, r64) < 1e-6
+    assert sdf.rnorm == pytest.approx(s64.rnorm, rel=1e-7)
+
