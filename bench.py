@@ -196,6 +196,7 @@ def run_gpu(args, rank, world):
         iks.append(st.iKs)
         rn.append(st.rnorm)
     r_end = g.residual_norm_dev()
+    y_mixed = g.download()[0]
 
     # e2e: pinned host buffers through the reference-facing time-step call (phgpu_time_step:
     # H2D of yold/acold, 3 Newton iterations, D2H of y/ac/yold/acold, every time step)
@@ -236,7 +237,9 @@ def run_gpu(args, rank, world):
         "roofline": roof, "clocks": clk.summary(),
     }
     if args.precision == "mixed" and not args.skip_fp64:
-        result["fp64_plain"] = fp64_plain(args, case)
+        result["fp64_plain"], y64 = fp64_plain(args, case)
+        # the error of the mixed-precision iterations against the FP64 ones, same start
+        result["fp64_plain"]["state_rel_diff_vs_mixed"] = float(np.linalg.norm(y_mixed - y64) / np.linalg.norm(y64))
     if not args.skip_sparse:
         result["sparse_solver"] = sparse_solver(args)
         if args.precision == "mixed":
@@ -376,10 +379,11 @@ def fp64_plain(args, case):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     r_end = g.residual_norm_dev()
+    y = g.download()[0]
     g.close()
     return {"ms_per_step": dt * 1e3 / NEWTON_PER_TIMESTEP,
             "value": case.nelem * NEWTON_PER_TIMESTEP / dt, "krylov_iterations": iks,
-            "rel_residual_after_3": r_end / r0}
+            "rel_residual_after_3": r_end / r0}, y
 
 
 def cpu_sample(n_sample: int, steps: int = 1):
