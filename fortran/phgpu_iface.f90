@@ -140,6 +140,74 @@ module phgpu_iface
        import :: c_ptr
        type(c_ptr), value :: ctx
      end function
+     ! include/phgpu_io.h: PHASTA files (strings are NUL-terminated: c_char_'...'//c_null_char)
+     integer(c_int) function phgpu_io_openfile(filename, mode, fd) bind(C, name="phgpu_io_openfile")
+       import :: c_int, c_char
+       character(kind=c_char), intent(in) :: filename(*), mode(*)
+       integer(c_int), intent(out) :: fd
+     end function
+     integer(c_int) function phgpu_io_closefile(fd, mode) bind(C, name="phgpu_io_closefile")
+       import :: c_int, c_char
+       integer(c_int), value :: fd
+       character(kind=c_char), intent(in) :: mode(*)
+     end function
+     integer(c_int) function phgpu_io_readheader(fd, key, values, nitems, datatype, iotype) &
+         bind(C, name="phgpu_io_readheader")
+       import :: c_int, c_char
+       integer(c_int), value :: fd, nitems
+       character(kind=c_char), intent(in) :: key(*), datatype(*), iotype(*)
+       integer(c_int), intent(inout) :: values(*)
+     end function
+     integer(c_int) function phgpu_io_readdatablock(fd, key, values, nitems, datatype, iotype) &
+         bind(C, name="phgpu_io_readdatablock")
+       import :: c_int, c_char, c_ptr
+       integer(c_int), value :: fd, nitems
+       character(kind=c_char), intent(in) :: key(*), datatype(*), iotype(*)
+       type(c_ptr), value :: values
+     end function
+     integer(c_int) function phgpu_io_writeheader(fd, key, values, nitems, ndata, datatype, iotype) &
+         bind(C, name="phgpu_io_writeheader")
+       import :: c_int, c_char
+       integer(c_int), value :: fd, nitems, ndata
+       character(kind=c_char), intent(in) :: key(*), datatype(*), iotype(*)
+       integer(c_int), intent(in) :: values(*)
+     end function
+     integer(c_int) function phgpu_io_writedatablock(fd, key, values, nitems, datatype, iotype) &
+         bind(C, name="phgpu_io_writedatablock")
+       import :: c_int, c_char, c_ptr
+       integer(c_int), value :: fd, nitems
+       character(kind=c_char), intent(in) :: key(*), datatype(*), iotype(*)
+       type(c_ptr), value :: values
+     end function
+     integer(c_int) function phgpu_io_write_restart(dir, rank, stepno, nshg, ndof, y, ac) &
+         bind(C, name="phgpu_io_write_restart")
+       import :: c_int, c_char, c_double
+       character(kind=c_char), intent(in) :: dir(*)
+       integer(c_int), value :: rank, stepno, nshg, ndof
+       real(c_double), intent(in) :: y(*), ac(*)
+     end function
+     integer(c_int) function phgpu_io_read_restart(dir, rank, irstart, nshg, ndof, y, ac, lstep) &
+         bind(C, name="phgpu_io_read_restart")
+       import :: c_int, c_char, c_double
+       character(kind=c_char), intent(in) :: dir(*)
+       integer(c_int), value :: rank, irstart, nshg, ndof
+       real(c_double), intent(out) :: y(*), ac(*)
+       integer(c_int), intent(out) :: lstep
+     end function
+     integer(c_int) function phgpu_io_genibc(nshg, numpbc, nBC, iBCtmp, iBC) bind(C, name="phgpu_io_genibc")
+       import :: c_int
+       integer(c_int), value :: nshg, numpbc
+       integer(c_int), intent(in) :: nBC(*), iBCtmp(*)
+       integer(c_int), intent(out) :: iBC(*)
+     end function
+     integer(c_int) function phgpu_io_genbc(nshg, numpbc, ndof, nBC, BCinp, ldbc, iBC, BC) &
+         bind(C, name="phgpu_io_genbc")
+       import :: c_int, c_double
+       integer(c_int), value :: nshg, numpbc, ndof, ldbc
+       integer(c_int), intent(in) :: nBC(*), iBC(*)
+       real(c_double), intent(in) :: BCinp(*)
+       real(c_double), intent(out) :: BC(*)
+     end function
   end interface
 
   type(c_ptr), save :: phgpu_ctx = c_null_ptr

@@ -46,7 +46,9 @@ enum {
     PHGPU_ERR_SINGULAR = 4,    /* zero or non-finite pivot in the 5x5 block LU */
     PHGPU_ERR_UNSUPPORTED = 5, /* option outside the implemented path */
     PHGPU_ERR_NOMEM = 6,       /* device allocation failed */
-    PHGPU_ERR_TOO_LARGE = 7    /* input larger than a fixed-size entry point accepts */
+    PHGPU_ERR_TOO_LARGE = 7,   /* input larger than a fixed-size entry point accepts */
+    PHGPU_ERR_IO = 8,          /* file could not be opened, read or written (phgpu_io.h) */
+    PHGPU_ERR_NOTFOUND = 9     /* header key not found in a PHASTA file (phgpu_io.h) */
 };
 
 enum { PHGPU_FP64 = 0, PHGPU_MIXED = 1 };         /* precision */

@@ -13,11 +13,13 @@ import numpy as np
 LIB_PATH = Path(__file__).resolve().parent / "libphgpu.so"
 
 PHGPU_OK = 0
-STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NONFINITE", 4: "SINGULAR", 5: "UNSUPPORTED", 6: "NOMEM", 7: "TOO_LARGE"}
+STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NONFINITE", 4: "SINGULAR", 5: "UNSUPPORTED", 6: "NOMEM", 7: "TOO_LARGE",
+          8: "IO", 9: "NOTFOUND"}
 PHGPU_FP64, PHGPU_MIXED = 0, 1
 PHGPU_AP_FD, PHGPU_AP_LINEAR, PHGPU_AP_SPARSE, PHGPU_AP_EBE = 0, 1, 2, 3
 PHGPU_RES_FP64, PHGPU_RES_GALERKIN64, PHGPU_RES_SPLITDF = 0, 1, 2
 PHGPU_ERR_INVALID, PHGPU_ERR_UNSUPPORTED, PHGPU_ERR_TOO_LARGE = 1, 5, 7
+PHGPU_ERR_IO, PHGPU_ERR_NOTFOUND = 8, 9
 PHGPU_RSTAT_NOALLOC_MAX_N = 33554432
 LU_FACT, LU_FORWARD, LU_BACKWARD, LU_PRODUCT = 0, 1, 2, 3
 
@@ -48,6 +50,15 @@ class Mesh(C.Structure):
         ("iBC", _ip), ("BC", _dp), ("iper", _ip),
         ("nhex", C.c_int), ("ienh", _ip), ("nwedge", C.c_int), ("ienw", _ip),
     ]
+
+
+class GeombcInfo(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("numnp", "nshg", "numel", "numelb", "nen", "nelblk", "nelblb", "numpbc",
+                                       "ntopsh", "nsd", "nbccols")]
+
+
+class TopBlock(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("neltp", "nenl", "ipordl", "nshl", "nshlb", "nenbl", "lcsyst", "numnbc")]
 
 
 class Stats(C.Structure):
@@ -104,6 +115,27 @@ def lib():
         "phgpu_i3pre": ([vp, _dp, _dp], C.c_int),
         "phgpu_au1gmr": ([vp, _dp, _dp], C.c_int),
         "phgpu_solgmre": ([vp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(Stats)], C.c_int),
+        # include/phgpu_io.h
+        "phgpu_io_openfile": ([C.c_char_p, C.c_char_p, _ip], C.c_int),
+        "phgpu_io_closefile": ([C.c_int, C.c_char_p], C.c_int),
+        "phgpu_io_readheader": ([C.c_int, C.c_char_p, _ip, C.c_int, C.c_char_p, C.c_char_p], C.c_int),
+        "phgpu_io_readdatablock": ([C.c_int, C.c_char_p, vp, C.c_int, C.c_char_p, C.c_char_p], C.c_int),
+        "phgpu_io_writeheader": ([C.c_int, C.c_char_p, _ip, C.c_int, C.c_int, C.c_char_p, C.c_char_p], C.c_int),
+        "phgpu_io_writedatablock": ([C.c_int, C.c_char_p, vp, C.c_int, C.c_char_p, C.c_char_p], C.c_int),
+        "phgpu_io_writestring": ([C.c_int, C.c_char_p], C.c_int),
+        "phgpu_io_togglestrictmode": ([], C.c_int),
+        "phgpu_io_last_error": ([], C.c_char_p),
+        "phgpu_io_write_restart": ([C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp], C.c_int),
+        "phgpu_io_read_restart": ([C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip], C.c_int),
+        "phgpu_io_geombc_open": ([C.c_char_p, C.c_int, C.c_int, C.POINTER(vp)], C.c_int),
+        "phgpu_io_geombc_free": ([vp], C.c_int),
+        "phgpu_io_geombc_info": ([vp, C.POINTER(GeombcInfo)], C.c_int),
+        "phgpu_io_geombc_arrays": ([vp, _dp, _ip, _ip, _dp, _ip], C.c_int),
+        "phgpu_io_geombc_interior": ([vp, C.c_int, C.POINTER(TopBlock), _ip], C.c_int),
+        "phgpu_io_geombc_boundary": ([vp, C.c_int, C.POINTER(TopBlock), _ip, _ip, _dp], C.c_int),
+        "phgpu_io_genibc": ([C.c_int, C.c_int, _ip, _ip, _ip], C.c_int),
+        "phgpu_io_genbc": ([C.c_int, C.c_int, C.c_int, _ip, _dp, C.c_int, _ip, _dp], C.c_int),
+        "phgpu_io_checkphasta": ([C.c_char_p, C.c_char_p, C.c_int, _dp, _ip], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -114,10 +146,13 @@ def lib():
 
 
 def exported_symbols() -> list[str]:
-    """Names declared in include/phgpu.h (used to check the library's exports)."""
-    hdr = (Path(__file__).resolve().parent.parent / "include" / "phgpu.h").read_text()
+    """Names declared in include/phgpu.h and include/phgpu_io.h (used to check the library's exports)."""
     import re
-    return sorted(set(re.findall(r"\b(phgpu_[a-z0-9_]+)\s*\(", hdr)))
+    inc = Path(__file__).resolve().parent.parent / "include"
+    names = set()
+    for h in ("phgpu.h", "phgpu_io.h"):
+        names |= set(re.findall(r"\b(phgpu_[a-z0-9_]+)\s*\(", (inc / h).read_text()))
+    return sorted(names)
 
 
 def dptr(a: np.ndarray | None):

@@ -1,6 +1,6 @@
 """Build the CUDA library of the hot path in place (sm_103a only).
 
-``build()`` compiles ``csrc/*.cu`` into ``phasta_gb300/libphgpu.so`` with one
+``build()`` compiles ``csrc/*.cu`` (and the host-only ``csrc/phio.cpp``) into ``phasta_gb300/libphgpu.so`` with one
 ``-gencode`` (compute_103a/sm_103a); the translation units are compiled in
 parallel and linked with the CUDA runtime.  Nothing is installed outside the
 package directory.
@@ -18,7 +18,8 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 LIB = PKG / "libphgpu.so"
 BUILD = PKG / "_build"
-SOURCES = ["elements.cu", "nodal.cu", "solver.cu", "chunks.cu", "noalloc.cu", "sparse.cu", "tangent.cu", "topo_ress.cu"]
+SOURCES = ["elements.cu", "nodal.cu", "solver.cu", "chunks.cu", "noalloc.cu", "sparse.cu", "tangent.cu", "topo_ress.cu",
+           "phio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -47,8 +48,8 @@ def _stale() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
-    deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "phgpu.h",
-                                                                  Path(__file__)]
+    deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.cpp")) + \
+        [PKG.parent / "include" / "phgpu.h", PKG.parent / "include" / "phgpu_io.h", Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps if p.exists())
 
 
