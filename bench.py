@@ -291,15 +291,24 @@ def kernel_roofline(g, case, stream, args, krylov_per_newton):
                         "achieved_gbs": algo / t / 1e9, "elements_per_s": E / t}
     dom = max(kernels, key=lambda k: kernels[k]["ms_per_newton"])
     k = kernels[dom]
-    traffic = None
+    traffic, fp32 = None, None
     tp = ROOT / "profiles" / "sweep_traffic.json"
     if tp.exists():
         d = json.loads(tp.read_text())
         if dom in d:
             traffic = d[dom]["dram_bytes_per_element"] * E
+            # the sweeps are FP32-issue bound: their executed FP32 flops (ncu instruction counts of
+            # one colour launch, per element) against the CUDA-core peak of 152 SMs x 128 lanes
+            # x 2 flops at 2070 MHz (nominal: the measured peaks cover HBM and tensor cores only)
+            f = d[dom].get("fp32_flops_per_element")
+            if f:
+                peak32 = 152 * 128 * 2 * 2.070e9 / 1e12
+                ach = f * E / (k["ms"] / 1e3) / 1e12
+                fp32 = {"flops_per_element": f, "achieved_tflops": ach, "peak_tflops": peak32,
+                        "frac": ach / peak32, "peak_source": "nominal FP32 CUDA-core peak"}
     return {"kernel": k["kernel"], "bound": "hbm", "achieved": k["achieved_gbs"], "peak": peak, "unit": "GB/s",
             "frac": k["achieved_gbs"] / peak, "peak_source": f"{src} hbm_gbs", "traffic": traffic,
-            "algorithmic_bytes": k["algorithmic_bytes"], "launch_ms": k["ms"], "sweeps": kernels}
+            "algorithmic_bytes": k["algorithmic_bytes"], "launch_ms": k["ms"], "fp32": fp32, "sweeps": kernels}
 
 
 def sparse_solver(args, ebe: bool = False):

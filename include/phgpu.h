@@ -92,7 +92,11 @@ typedef struct {
     int idiff;                       /* 0, or 1: global reconstruction of the diffusive flux
                                         (elmmfg.f:56-111) whose divergence enters the residual's
                                         least-squares term */
-    int reserved[4];
+    int no_graph;                    /* 0: each GMRES cycle of the linearized, sparse and element-by-
+                                        element solvers runs as one CUDA graph (one conditional node
+                                        per Krylov iteration, skipped once the cycle has converged);
+                                        1: launched kernel by kernel with a host check per iteration */
+    int reserved[3];
 } phgpu_config;
 
 /* Mesh and boundary-condition arrays (what the reference keeps in
@@ -140,6 +144,9 @@ const char* phgpu_last_error(phgpu_ctx* ctx);
 void* phgpu_stream(phgpu_ctx* ctx);        /* the cudaStream_t every kernel runs on */
 int phgpu_num_colors(phgpu_ctx* ctx);
 long long phgpu_kernel_launches(phgpu_ctx* ctx); /* kernels launched since create */
+/* GMRES cycles run as one CUDA graph since create (config no_graph = 0), or -1 when the
+ * graph could not be built (phgpu_last_error then gives the reason; cycles run kernel by kernel) */
+long long phgpu_graph_cycles(phgpu_ctx* ctx);
 
 /* ElmMFG: res, rmes, BDiag (BDiag only when iprec != 0) */
 int phgpu_elmmfg(phgpu_ctx* ctx, const double* y, const double* ac,

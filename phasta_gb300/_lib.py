@@ -39,7 +39,7 @@ class Config(C.Structure):
         ("etol", C.c_double), ("epsM", C.c_double), ("eGMRES", C.c_double),
         ("iter", C.c_int), ("istep", C.c_int),
         ("precision", C.c_int), ("ap_mode", C.c_int), ("outer_residual", C.c_int), ("idiff", C.c_int),
-        ("reserved", C.c_int * 4),
+        ("no_graph", C.c_int), ("reserved", C.c_int * 3),
     ]
 
 
@@ -90,6 +90,7 @@ def lib():
         "phgpu_stream": ([vp], vp),
         "phgpu_num_colors": ([vp], C.c_int),
         "phgpu_kernel_launches": ([vp], C.c_longlong),
+        "phgpu_graph_cycles": ([vp], C.c_longlong),
         "phgpu_elmmfg": ([vp, _dp, _dp, _dp, _dp, _dp, C.c_int], C.c_int),
         "phgpu_elmres": ([vp, _dp, _dp, _dp], C.c_int),
         "phgpu_itrres": ([vp, _dp, _dp, _dp, _dp], C.c_int),

@@ -84,6 +84,22 @@ struct SparseCtx {
     float* d_EGf = nullptr;
 };
 
+// The GMRES cycle as one CUDA graph: one conditional (if) node per Krylov iteration whose
+// body is that iteration's product, Gram-Schmidt and Givens kernels; the Givens kernel of
+// iteration i opens node i+1 unless the cycle has converged.  Rebuilt when the options or
+// the operator it was captured with change.
+struct CycleGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<long long> launches;  // kernels in the body of iteration i
+    phgpu_config key{};
+    int vsize = 0, min_iters = 0;
+    const void* lhs = nullptr;
+    bool disabled = false;            // a graph call failed: cycles are launched kernel by kernel
+    long long runs = 0;               // cycles run as a graph
+    std::string why;
+};
+
 struct Ctx {
     int N = 0, E = 0, Eb = 0;
     phgpu_config cfg{};
@@ -157,7 +173,8 @@ struct Ctx {
     double* d_scal = nullptr;     // device scalars (see Scal below)
     double* d_part = nullptr;     // reduction partials
     unsigned int* d_count = nullptr;
-    int* d_flag = nullptr;        // [0] converged, [1] error bits
+    int* d_flag = nullptr;        // [0] converged, [1] error bits, [2] Krylov iterations of the cycle
+    CycleGraph cyc;
     double* h_scal = nullptr;     // pinned mirror
     int* h_flag = nullptr;
 

@@ -132,8 +132,11 @@ __global__ void k_axpby(const double* __restrict__ a, double alpha, const double
         o[i] = alpha * a[i] + beta * b[i];
 }
 
-// Givens update of column iKs (solmfg.f:274-317); also sets H(iKs+1,iKs) = sqrt(beta)
-__global__ void k_givens(double* __restrict__ s, int K, int iKs, int minIters, int* __restrict__ flag) {
+// Givens update of column iKs (solmfg.f:274-317); also sets H(iKs+1,iKs) = sqrt(beta).
+// Inside a captured cycle (open_next) it opens the next iteration's conditional node
+// unless the cycle has converged or failed.
+__global__ void k_givens(double* __restrict__ s, int K, int iKs, int minIters, int* __restrict__ flag,
+                         cudaGraphConditionalHandle next, int open_next) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     if (flag[0]) return;
     auto H = [&](int i, int j) -> double& { return s[S_H + (i - 1) + (K + 1) * (j - 1)]; };
@@ -160,6 +163,8 @@ __global__ void k_givens(double* __restrict__ s, int K, int iKs, int minIters, i
     s[S_ECHECK] = echeck;
     if (!(echeck == echeck)) flag[1] |= 2;
     if (echeck <= s[S_EPSNRM] && iKs >= minIters) flag[0] = 1;
+    flag[2] = iKs;
+    if (open_next) cudaGraphSetConditional(next, (flag[0] | flag[1]) ? 0u : 1u);
 }
 
 // back substitution H y = e (solmfg.f:329-334)
@@ -211,6 +216,7 @@ __global__ void k_init_cycle(double* __restrict__ s, int K, double unorm, double
         s[S_EPSNRM] = epsnrm;
         s[S_ECHECK] = 0.0;
         flag[0] = 0;
+        flag[2] = 0;
     }
 }
 
@@ -435,6 +441,115 @@ void assembled_ap(Ctx& C, bool ebe, const V* p, V* q) {
     else sparse_ap<V, V>(C, sparse_lhs<V>(C), p, q);
 }
 
+// Krylov iteration iK of a cycle (solmfg.f:230-317): the product into u_{iK+1}, modified
+// Gram-Schmidt against u_1..u_iK, the new vector's norm and the Givens update
+template <typename V>
+int krylov_step(Ctx& C, int iK, int min_iters, bool sparse, bool ebe, cudaGraphConditionalHandle next,
+                int open_next) {
+    const size_t n5 = 5 * (size_t)C.N;
+    const int K = C.cfg.Kspace;
+    V* U = (V*)C.d_U;
+    auto Uj = [&](int j) { return U + (size_t)(j - 1) * C.ldU; };  // 1-based
+    double* s = C.d_scal;
+    V* w = Uj(iK + 1);
+    if (sparse) {
+        assembled_ap<V>(C, ebe, Uj(iK), w);
+    } else if constexpr (std::is_same<V, double>::value) {
+        if (C.cfg.ap_mode == PHGPU_AP_FD) {
+            k_copy<V><<<kVG, kVT, 0, C.stream>>>(Uj(iK), w, n5, nullptr);
+            ++C.launches;
+            PH_TRY(ap_fd64(C, w, C.d_rmes, nullptr));
+        } else {
+            PH_TRY(ap_lin<V>(C, Uj(iK), w, nullptr));
+        }
+    } else {
+        PH_TRY(ap_lin<V>(C, Uj(iK), w, nullptr));
+    }
+    // modified Gram-Schmidt (solmfg.f:247-267)
+    double* Hcol = s + S_H + (size_t)(K + 1) * (iK - 1);
+    for (int jK = 1; jK <= iK + 1; ++jK) {
+        const V* up = (jK == 1) ? nullptr : Uj(jK - 1);
+        const double* bprev = (jK == 1) ? nullptr : Hcol + (jK - 2);
+        mgs_step<V>(C, w, up, bprev, Uj(jK), n5, Hcol + (jK - 1), nullptr);
+    }
+    scale_by<V>(C, w, Hcol + iK, 1, n5, nullptr);
+    k_givens<<<1, 1, 0, C.stream>>>(s, K, iK, min_iters, C.d_flag, next, open_next);
+    ++C.launches;
+    return check(C, cudaGetLastError(), "krylov step");
+}
+
+}  // namespace
+
+void cycle_graph_free(Ctx& C) {
+    if (C.cyc.exec) cudaGraphExecDestroy(C.cyc.exec);
+    if (C.cyc.graph) cudaGraphDestroy(C.cyc.graph);
+    C.cyc.exec = nullptr;
+    C.cyc.graph = nullptr;
+}
+
+namespace {
+
+// Capture the Krylov iterations of a cycle as a graph of conditional nodes (or reuse the
+// last one): false when it cannot be built, and cycles are then launched kernel by kernel
+template <typename V>
+bool cycle_graph(Ctx& C, int min_iters, bool sparse, bool ebe) {
+    CycleGraph& G = C.cyc;
+    if (G.disabled) return false;
+    phgpu_config key = C.cfg;  // the fields the captured kernels do not read
+    key.iter = 0;
+    key.istep = 0;
+    key.eGMRES = 0.0;
+    const void* lhs = !sparse ? nullptr : ebe ? (const void*)ebe_lhs<V>(C) : (const void*)sparse_lhs<V>(C);
+    if (G.exec && G.vsize == (int)sizeof(V) && G.min_iters == min_iters && G.lhs == lhs &&
+        std::memcmp(&G.key, &key, sizeof key) == 0)
+        return true;
+    phgpu::cycle_graph_free(C);
+    const int K = C.cfg.Kspace;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    std::vector<cudaGraphConditionalHandle> h(K + 2, 0);
+    for (int i = 1; i <= K && e == cudaSuccess; ++i)
+        e = cudaGraphConditionalHandleCreate(&h[i], g, i == 1 ? 1u : 0u, cudaGraphCondAssignDefault);
+    const long long l0 = C.launches;
+    G.launches.assign(K + 1, 0);
+    cudaGraphNode_t prev = nullptr;
+    for (int i = 1; i <= K && e == cudaSuccess; ++i) {
+        cudaGraphNodeParams p{};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h[i];
+        p.conditional.type = cudaGraphCondTypeIf;
+        p.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        e = cudaGraphAddNode(&node, g, prev ? &prev : nullptr, nullptr, prev ? 1 : 0, &p);
+        if (e != cudaSuccess) break;
+        cudaGraph_t body = p.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(C.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) break;
+        const long long li = C.launches;
+        const int rc = krylov_step<V>(C, i, min_iters, sparse, ebe, h[i + 1], i < K ? 1 : 0);
+        cudaGraph_t captured = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(C.stream, &captured);
+        G.launches[i] = C.launches - li;
+        e = rc != PHGPU_OK ? cudaErrorUnknown : e2;
+        prev = node;
+    }
+    C.launches = l0;
+    G.graph = g;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&G.exec, g, 0);
+    if (e != cudaSuccess) {
+        G.why = std::string("cycle graph: ") + cudaGetErrorString(e);
+        (void)cudaGetLastError();
+        cycle_graph_free(C);
+        G.disabled = true;
+        return false;
+    }
+    G.key = key;
+    G.vsize = (int)sizeof(V);
+    G.min_iters = min_iters;
+    G.lhs = lhs;
+    return true;
+}
+
 // GMRES cycles on V-typed Krylov vectors; b (= L^-1 R, FP64) in d_res, output Dy (FP64, before U^-1).
 // ap_mode PHGPU_AP_SPARSE: the product is SparseAp + bc3per on the preconditioned tangent, and a
 // new cycle recomputes R - A Dy only when lgmres_common > 0 (SolGMRs, solgmr.f:526-537)
@@ -526,37 +641,27 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
         ++C.launches;
         // uBrg(1) /= unorm
         scale_by<V>(C, Uj(1), s + S_UNORM, 0, n5, nullptr);
-        for (int iK = 1; iK <= K; ++iK) {
-            iKs = iK;
-            V* w = Uj(iKs + 1);
-            if (sparse) {
-                assembled_ap<V>(C, ebe, Uj(iKs), w);
-            } else if constexpr (std::is_same<V, double>::value) {
-                if (C.cfg.ap_mode == PHGPU_AP_FD) {
-                    k_copy<V><<<kVG, kVT, 0, C.stream>>>(Uj(iKs), w, n5, nullptr);
-                    ++C.launches;
-                    PH_TRY(ap_fd64(C, w, C.d_rmes, nullptr));
-                } else {
-                    PH_TRY(ap_lin<V>(C, Uj(iKs), w, nullptr));
-                }
-            } else {
-                PH_TRY(ap_lin<V>(C, Uj(iKs), w, nullptr));
-            }
-            // modified Gram-Schmidt (solmfg.f:247-267)
-            double* Hcol = s + S_H + (size_t)(K + 1) * (iKs - 1);
-            for (int jK = 1; jK <= iKs + 1; ++jK) {
-                const V* up = (jK == 1) ? nullptr : Uj(jK - 1);
-                const double* bprev = (jK == 1) ? nullptr : Hcol + (jK - 2);
-                mgs_step<V>(C, w, up, bprev, Uj(jK), n5, Hcol + (jK - 1), nullptr);
-            }
-            scale_by<V>(C, w, Hcol + iKs, 1, n5, nullptr);
-            k_givens<<<1, 1, 0, C.stream>>>(s, K, iKs, min_iters, C.d_flag);
-            ++C.launches;
-            st->ntotGM += 1;
-            PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
+        // the finite-difference product reads eGMRES (changed by itrFDI) as a launch value
+        if (!C.cfg.no_graph && C.cfg.ap_mode != PHGPU_AP_FD && cycle_graph<V>(C, min_iters, sparse, ebe)) {
+            PH_TRY(check(C, cudaGraphLaunch(C.cyc.exec, C.stream), "cycle graph launch"));
+            ++C.cyc.runs;
+            PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 3, cudaMemcpyDeviceToHost, C.stream), "flag"));
             PH_TRY(sync(C));
+            iKs = C.h_flag[2];
+            if (iKs < 1 || iKs > K) return fail(C, PHGPU_ERR_CUDA, "cycle graph ran no Krylov iteration");
+            for (int i = 1; i <= iKs; ++i) C.launches += C.cyc.launches[i];
+            st->ntotGM += iKs;
             if (C.h_flag[1]) return fail(C, PHGPU_ERR_NONFINITE, "non-finite Hessenberg entry in GMRES");
-            if (C.h_flag[0]) break;
+        } else {
+            for (int iK = 1; iK <= K; ++iK) {
+                iKs = iK;
+                PH_TRY(krylov_step<V>(C, iK, min_iters, sparse, ebe, 0, 0));
+                st->ntotGM += 1;
+                PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
+                PH_TRY(sync(C));
+                if (C.h_flag[1]) return fail(C, PHGPU_ERR_NONFINITE, "non-finite Hessenberg entry in GMRES");
+                if (C.h_flag[0]) break;
+            }
         }
         k_backsolve<<<1, 1, 0, C.stream>>>(s, K, iKs);
         k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, U, C.ldU, iKs, s, n5);
@@ -924,9 +1029,9 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     T(dalloc(C, &C.d_scal, S_TOTAL));
     T(dalloc(C, &C.d_part, kRedBlocks));
     T(dalloc(C, &C.d_count, 1));
-    T(dalloc(C, &C.d_flag, 2));
+    T(dalloc(C, &C.d_flag, 4));
     if (rc == PHGPU_OK && cudaMallocHost((void**)&C.h_scal, sizeof(double) * 16) != cudaSuccess) rc = PHGPU_ERR_NOMEM;
-    if (rc == PHGPU_OK && cudaMallocHost((void**)&C.h_flag, sizeof(int) * 2) != cudaSuccess) rc = PHGPU_ERR_NOMEM;
+    if (rc == PHGPU_OK && cudaMallocHost((void**)&C.h_flag, sizeof(int) * 4) != cudaSuccess) rc = PHGPU_ERR_NOMEM;
     if (rc != PHGPU_OK) {
         phgpu_destroy(h);
         return rc;
@@ -981,6 +1086,7 @@ int phgpu_destroy(phgpu_ctx* h) {
     if (!h) return PHGPU_OK;
     Ctx& C = h->c;
     if (C.stream) cudaStreamSynchronize(C.stream);
+    phgpu::cycle_graph_free(C);
     void* ptrs[] = {C.d_ch_elem, C.d_ch_node, C.d_ch_nodes, C.d_ch_cstart, C.d_ch_csr, C.d_ch_lien,
                     C.d_bdstage, C.d_ien, C.d_ienh, C.d_ienw, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_xlo, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
                     C.d_slaves, C.d_mst, C.d_slv_start, C.d_slv, C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_res,
@@ -1019,6 +1125,15 @@ const char* phgpu_last_error(phgpu_ctx* h) { return h ? h->c.err.c_str() : "null
 void* phgpu_stream(phgpu_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
 int phgpu_num_colors(phgpu_ctx* h) { return h ? (int)h->c.chunk_col_start.size() - 1 : 0; }
 long long phgpu_kernel_launches(phgpu_ctx* h) { return h ? h->c.launches : 0; }
+
+long long phgpu_graph_cycles(phgpu_ctx* h) {
+    if (!h) return 0;
+    if (h->c.cyc.disabled) {
+        h->c.err = h->c.cyc.why;
+        return -1;
+    }
+    return h->c.cyc.runs;
+}
 
 int phgpu_elmmfg(phgpu_ctx* h, const double* y, const double* ac, double* res, double* rmes, double* bdiag,
                  int iprec) {

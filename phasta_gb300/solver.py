@@ -185,6 +185,11 @@ class GpuSolver:
     def kernel_launches(self) -> int:
         return self.lib.phgpu_kernel_launches(self.h)
 
+    @property
+    def graph_cycles(self) -> int:
+        """GMRES cycles run as one CUDA graph (-1: the graph could not be built)."""
+        return self.lib.phgpu_graph_cycles(self.h)
+
     def stream(self) -> int:
         return self.lib.phgpu_stream(self.h)
 
