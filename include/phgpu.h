@@ -96,7 +96,10 @@ typedef struct {
                                         element solvers runs as one CUDA graph (one conditional node
                                         per Krylov iteration, skipped once the cycle has converged);
                                         1: launched kernel by kernel with a host check per iteration */
-    int reserved[3];
+    int iDC;                         /* discontinuity capturing (e3dc.f): 0 off, 1 DC-mallet,
+                                        2 DC-quadratic, 3 DC-min; FP64 with the finite-difference
+                                        product (ElmMFG, ItrRes, SolMFG) */
+    int reserved[2];
 } phgpu_config;
 
 /* Mesh and boundary-condition arrays (what the reference keeps in

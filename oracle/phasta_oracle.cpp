@@ -420,6 +420,8 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             tau[2] = tau[1] / cv * c.temper;
         }
         const double tauk[5] = {tau[0], tau[1], tau[1], tau[1], tau[2]};
+        double rLyt[5];  // the least-squares residual before tau, for the DC factor (e3tau.f:183)
+        for (int k = 0; k < 5; ++k) rLyt[k] = rLyi[k];
         if (ires == 1 || ires == 3)
             for (int k = 0; k < 5; ++k) rLyi[k] = tauk[k] * rLyi[k];
         if (ires != 1)
@@ -440,6 +442,107 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
                 for (int j = 0; j < 5; ++j) s = s + A[i][row][j] * rLyi[j];
                 ri[r] = s + ri[r];
             }
+
+        // ---------------- discontinuity capturing (e3.f:217-222), iDC != 0 ----------------
+        if (c.iDC != 0) {
+            // A0DC, A0inv and dV/dY (e3mtrx.f:232-297); e3mtrx's local cv
+            const double s1 = one / (rho * rho * betaT * Tq);
+            const double cvd = cp - (alfap * alfap * Tq / rho / betaT);
+            const double A0DC[4] = {(rho * betaT) * (rho * betaT) * s1, -(rho * alfap * rho * betaT * s1), rho / Tq,
+                                    (-(rho * alfap)) * (-(rho * alfap)) * s1 + (rho * cvd / (Tq * Tq))};
+            double A0inv[15];
+            {
+                const double fact1 = one / (rho * cvd * (Tq * Tq));
+                const double d = alfap * Tq / rho / betaT;
+                const double e1bar = h - rk;
+                const double e2bar = e1bar - d;
+                const double e3bar = e2bar - cvd * Tq;
+                const double e5bar = e1bar * e1bar - 2 * e1bar * d + 2 * rk * cvd * Tq + cp * Tq / rho / betaT;
+                const double c1bar = u1 * u1 + cvd * Tq, c2bar = u2 * u2 + cvd * Tq, c3bar = u3 * u3 + cvd * Tq;
+                A0inv[0] = e5bar * fact1;
+                A0inv[1] = c1bar * fact1;
+                A0inv[2] = c2bar * fact1;
+                A0inv[3] = c3bar * fact1;
+                A0inv[4] = 1 * fact1;
+                A0inv[5] = u1 * e3bar * fact1;
+                A0inv[6] = u2 * e3bar * fact1;
+                A0inv[7] = u3 * e3bar * fact1;
+                A0inv[8] = -e2bar * fact1;
+                A0inv[9] = u1 * u2 * fact1;
+                A0inv[10] = u3 * u1 * fact1;
+                A0inv[11] = -u1 * fact1;
+                A0inv[12] = u2 * u3 * fact1;
+                A0inv[13] = -u2 * fact1;
+                A0inv[14] = -u3 * fact1;
+            }
+            double dV[15];
+            {
+                const double fact1 = 1 / Tq, fact2 = fact1 / Tq;
+                dV[0] = fact1 / rho; dV[1] = -fact1 * u1; dV[2] = fact1; dV[3] = -fact1 * u2; dV[4] = zero;
+                dV[5] = fact1; dV[6] = -fact1 * u3; dV[7] = zero; dV[8] = zero; dV[9] = fact1;
+                dV[10] = -(h - rk) * fact2; dV[11] = -fact2 * u1; dV[12] = -fact2 * u2; dV[13] = -fact2 * u3;
+                dV[14] = fact2;
+            }
+            // rTLS = (Ly - S) tau~ (Ly - S) with rLyi tau-scaled for ires 1, 3 and unscaled for
+            // ires 2; raLS = (Ly - S) A0^-1 (Ly - S) (e3tau.f:193-237)
+            const double* L = rLyi;
+            const double* T0 = rLyt;
+            const double rTLS = T0[0] * (L[0] * dV[0] + dV[1] * L[1] + dV[3] * L[2] + L[3] * dV[6] + dV[10] * L[4]) +
+                                T0[1] * (L[1] * dV[2] + L[2] * dV[4] + dV[7] * L[3] + L[4] * dV[11]) +
+                                T0[2] * (L[2] * dV[5] + dV[8] * L[3] + dV[12] * L[4]) +
+                                T0[3] * (L[3] * dV[9] + dV[13] * L[4]) + T0[4] * (dV[14] * L[4]);
+            const double raLS = two * T0[3] * T0[4] * A0inv[14] + two * T0[2] * T0[4] * A0inv[13] +
+                                two * T0[0] * T0[1] * A0inv[5] + two * T0[1] * T0[2] * A0inv[9] +
+                                two * T0[1] * T0[3] * A0inv[10] + two * T0[0] * T0[2] * A0inv[6] +
+                                two * T0[2] * T0[3] * A0inv[12] + two * T0[1] * T0[4] * A0inv[11] +
+                                two * T0[0] * T0[3] * A0inv[7] + two * T0[0] * T0[4] * A0inv[8] +
+                                T0[0] * T0[0] * A0inv[0] + T0[1] * T0[1] * A0inv[1] + T0[2] * T0[2] * A0inv[2] +
+                                T0[3] * T0[3] * A0inv[3] + T0[4] * T0[4] * A0inv[4];
+            // inverse of the tau metric, order (11, 22, 33, 12, 13, 23) (e3tau.f:241-260)
+            const double gu[6] = {gijd[0], gijd[2], gijd[5], gijd[1], gijd[3], gijd[4]};
+            const double detI = one / (gu[0] * gu[1] * gu[2] - gu[0] * gu[5] * gu[5] - gu[3] * gu[3] * gu[2] +
+                                       gu[3] * gu[4] * gu[5] * two - gu[4] * gu[4] * gu[1]);
+            const double gi[6] = {detI * (gu[1] * gu[2] - gu[5] * gu[5]), detI * (gu[0] * gu[2] - gu[4] * gu[4]),
+                                  detI * (gu[0] * gu[1] - gu[3] * gu[3]), detI * (gu[4] * gu[5] - gu[3] * gu[2]),
+                                  detI * (gu[3] * gu[5] - gu[4] * gu[1]), detI * (gu[3] * gu[4] - gu[0] * gu[5])};
+            // e3dc.f:55-240: A0 Y,j, g^ij A0 Y,j and Y,i A0DC Y,j
+            double A0g[15];
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 5; ++k)
+                    A0g[5 * j + k] = A0[k][0] * g[j][0] + A0[k][1] * g[j][1] + A0[k][2] * g[j][2] +
+                                     A0[k][3] * g[j][3] + A0[k][4] * g[j][4];
+            double gA[15];
+            for (int k = 0; k < 5; ++k) {
+                gA[k] = gi[0] * A0g[k] + gi[3] * A0g[5 + k] + gi[4] * A0g[10 + k];
+                gA[5 + k] = gi[3] * A0g[k] + gi[1] * A0g[5 + k] + gi[5] * A0g[10 + k];
+                gA[10 + k] = gi[4] * A0g[k] + gi[5] * A0g[5 + k] + gi[2] * A0g[10 + k];
+            }
+            auto yy = [&](const double* a) {
+                return A0DC[0] * (a[0] * a[0]) + two * a[0] * A0DC[1] * a[4] + A0DC[2] * (a[1] * a[1]) +
+                       A0DC[2] * (a[2] * a[2]) + A0DC[2] * (a[3] * a[3]) + A0DC[3] * (a[4] * a[4]);
+            };
+            auto yx = [&](const double* a, const double* b) {
+                return a[0] * A0DC[0] * b[0] + a[0] * A0DC[1] * b[4] + a[1] * A0DC[2] * b[1] +
+                       a[2] * A0DC[2] * b[2] + a[3] * A0DC[2] * b[3] + a[4] * A0DC[1] * b[0] + a[4] * A0DC[3] * b[4];
+            };
+            const double y1 = yy(g[0]), y2 = yy(g[1]), y3 = yy(g[2]);
+            const double y4 = yx(g[0], g[1]), y5 = yx(g[0], g[2]), y6 = yx(g[1], g[2]);
+            const double gnorm = one / (gi[0] * y1 + two * gi[3] * y4 + two * gi[4] * y5 + gi[1] * y2 +
+                                        two * gi[5] * y6 + gi[2] * y3 + c.epsM);
+            double DC = 0.0;  // ipord = 1: fact = 1
+            if (c.iDC == 1) DC = std::max(zero, std::sqrt(raLS * gnorm) - rTLS * gnorm);
+            if (c.iDC == 2) DC = two * rTLS * gnorm;
+            if (c.iDC == 3) DC = std::min(std::max(zero, std::sqrt(raLS * gnorm) - rTLS * gnorm), two * rTLS * gnorm);
+            if (ires == 1 || ires == 3) {
+                for (int r = 0; r < 15; ++r) {
+                    ri[r] = ri[r] + DC * gA[r];
+                    // the reference's update of rmi(:,11) reads rmi(:,12) (e3dc.f:366)
+                    rmi[r] = (r == 10) ? rmi[11] + DC * gA[11] : rmi[r] + DC * gA[r];
+                }
+            } else if (ires == 2) {
+                for (int r = 0; r < 15; ++r) rmi[r] = rmi[r] + DC * gA[r];
+            }
+        }
 
         // ---------------- e3massr.f:26-88 ----------------
         if (ires == 1 || ires == 3)

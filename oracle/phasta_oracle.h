@@ -40,6 +40,7 @@ typedef struct {
     double eGMRES;                    /* finite-difference interval (in/out) */
     int    iter, istep;               /* Newton iteration (1-based) and time step (0-based) */
     int    idiff;                     /* 0, or 1: global reconstruction of the diffusive flux */
+    int    iDC;                       /* discontinuity capturing: 0 off, 1 DC-mallet, 2 quadratic, 3 min */
 } or_common;
 
 typedef struct {

@@ -25,7 +25,7 @@ class Common(C.Structure):
         ("itau", C.c_int), ("ivart", C.c_int), ("iremoveStabTimeTerm", C.c_int), ("Navier", C.c_int),
         ("ipord", C.c_int), ("EntropyPressure", C.c_int), ("Kspace", C.c_int), ("nGMRES", C.c_int),
         ("minIters", C.c_int), ("etol", C.c_double), ("epsM", C.c_double), ("eGMRES", C.c_double),
-        ("iter", C.c_int), ("istep", C.c_int), ("idiff", C.c_int),
+        ("iter", C.c_int), ("istep", C.c_int), ("idiff", C.c_int), ("iDC", C.c_int),
     ]
 
 

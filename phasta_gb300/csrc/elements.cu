@@ -108,6 +108,8 @@ Phys<R> make_phys(const phgpu_config& c) {
     p.rtempcv = (R)(c.temper / cv);
     p.navier = c.Navier;
     p.supg = c.ivart >= 2;
+    p.epsM = (R)c.epsM;
+    p.idc = c.iDC;
     return p;
 }
 template Phys<double> make_phys<double>(const phgpu_config&);
@@ -252,6 +254,9 @@ __device__ __forceinline__ void elem_res(const Phys<R>& P, const R (&xl)[4][3], 
         R r16[5];
         R aig[5];
         ai_gi(b, g, aig);
+        R ly[5];  // the least-squares residual before tau (discontinuity capturing)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) ly[k] = aig[k];
         if (MODE == RM_RES) {
             // Euler flux integrated by parts (e3conv.f:72-96)
             const R ek = b.ei + b.rk;
@@ -276,6 +281,8 @@ __device__ __forceinline__ void elem_res(const Phys<R>& P, const R (&xl)[4][3], 
 #pragma unroll
                 for (int k = 0; k < 4; ++k) aig[1 + k] -= divq[k];
             }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) ly[k] = aig[k];
         } else {
 #pragma unroll
             for (int i = 0; i < 3; ++i)
@@ -319,6 +326,18 @@ __device__ __forceinline__ void elem_res(const Phys<R>& P, const R (&xl)[4][3], 
         tl[3] = b.tau[1] * aig[3];
         tl[4] = b.tau[2] * aig[4];
         add_ai_v(b, tl, F);
+        if constexpr (sizeof(R) == 8 && MODE != RM_LIN) {
+            // discontinuity capturing (e3dc.f): the residual pairs rTLS with tau L, the
+            // modified residual (ires = 2) with L itself (e3tau.f:185-205)
+            if (P.idc) {
+                R gA[3][5];
+                const R dc = dc_point(P, geo.G, b, g, ly, MODE == RM_RES ? tl : ly, gA);
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) F[i][k] += dc * gA[i][k];
+            }
+        }
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -1022,6 +1041,7 @@ __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R 
     }
     // this lane's quadrature point (q = a)
     R own[NV];
+    R odc[16];  // discontinuity capturing at this point: DC and g^ij A0 Y,j (FP64, iDC != 0)
     {
         R N[4];
 #pragma unroll
@@ -1046,6 +1066,22 @@ __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R 
             for (int k = 0; k < 5; ++k) {
                 own[15 + k] = aig[k];
                 own[20 + k] = a0a[k];
+            }
+            if constexpr (sizeof(R) == 8) {
+                if (P.idc) {
+                    const R tkk[5] = {b.tau[0], b.tau[1], b.tau[1], b.tau[1], b.tau[2]};
+                    R ly[5], lt[5], gA[3][5];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) {
+                        ly[k] = aig[k] + a0a[k] - ((divq && k > 0) ? divq[k - 1] : R(0));
+                        lt[k] = tkk[k] * ly[k];
+                    }
+                    odc[0] = dc_point(P, geo.G, b, g, ly, lt, gA);
+#pragma unroll
+                    for (int i = 0; i < 3; ++i)
+#pragma unroll
+                        for (int k = 0; k < 5; ++k) odc[1 + 5 * i + k] = gA[i][k];
+                }
             }
         }
     }
@@ -1092,6 +1128,27 @@ __device__ __forceinline__ void elem_full_node(const Phys<R>& P, int a, const R 
                 const R dq = (divq && k > 0) ? divq[k - 1] : R(0);  // idiff = 1 (e3ls.f:147-156)
                 lt[k] = tk[k] * (v[15 + k] + v[20 + k] - dq);
                 lm[k] = tk[k] * rm16[k];
+            }
+            if constexpr (sizeof(R) == 8) {
+                // discontinuity capturing: both residuals gain s_a . DC gA; the modified
+                // residual's z-flux of continuity is the reference's rmi(:,11) = rmi(:,12) +
+                // DC gA(:,12) (e3dc.f:366), the z-flux of x-momentum plus its DC part
+                if (P.idc) {
+                    R dq[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) dq[i] = __shfl_sync(0xffffffffu, odc[i], base_lane + q);
+                    const R dc = dq[0];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) {
+                        const R f = dc * (s[0] * dq[1 + k] + s[1] * dq[6 + k] + s[2] * dq[11 + k]);
+                        rl[k] += f;
+                        rml[k] += f;
+                    }
+                    const R sz = drdp * lm[0] + drdT * lm[4];
+                    const R z0 = u2 * sz + rho * lm[3];
+                    const R z1 = u0 * z0 + rho * u2 * lm[1] + (P.navier ? vs.t[2][0] : R(0));
+                    rml[0] += s[2] * (z1 + dc * dq[12] - z0 - dc * dq[11]);
+                }
             }
             R fe[5];
             const R m = -rho * Us;
@@ -1443,8 +1500,8 @@ constexpr int kTopoThreads = 128;
 enum TopoMode : int { TM_RES = RM_RES, TM_MODRES = RM_MODRES, TM_LIN = RM_LIN, TM_FULL = 4, TM_QREC = 5 };
 constexpr int kTopoNode = 25;  // staged per node: x(3) ya(5) yb(5) reconstructed flux(12)
 
-// shared values of one quadrature point
-template <int NEN>
+// shared values of one quadrature point (FP64 also holds the discontinuity-capturing terms)
+template <int NEN, bool DC = false>
 struct TopoQp {
     static constexpr int kShg = 0;                  // shg[b][i], NEN*3
     static constexpr int kW = NEN * 3;              // WdetJ
@@ -1455,7 +1512,8 @@ struct TopoQp {
     static constexpr int kVq = kVt + 9;             // heat flux (3)
     static constexpr int kDu = kVq + 3;             // conservative variables (full mode) (5)
     static constexpr int kDq = kDu + 5;             // div of the reconstructed flux (4)
-    static constexpr int kN = kDq + 4;
+    static constexpr int kDc = kDq + 4;             // DC and g^ij A0 Y,j (16, FP64)
+    static constexpr int kN = kDc + (DC ? 16 : 0);
 };
 
 template <typename R, int NEN, int TOPO, int MODE>
@@ -1464,7 +1522,7 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
        const R* __restrict__ yb, const R* __restrict__ ac, R* __restrict__ res, R* __restrict__ rmes,
        R* __restrict__ bd, Phys<R> P, int iabres, const int* __restrict__ skip, const R* __restrict__ ql) {
     if (skip && *skip) return;
-    using Q = TopoQp<NEN>;
+    using Q = TopoQp<NEN, sizeof(R) == 8>;
     constexpr int EPB = kTopoThreads / NEN;  // elements per CTA
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* sm = reinterpret_cast<R*>(smem_raw);
@@ -1639,6 +1697,28 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
         const R du[5] = {st.rho, st.rho * st.u[0], st.rho * st.u[1], st.rho * st.u[2], st.rho * (st.ei + st.rk)};
 #pragma unroll
         for (int k = 0; k < 5; ++k) o[Q::kDu + k] = du[k];
+        if constexpr (sizeof(R) == 8 && MODE != TM_LIN) {
+            // discontinuity capturing (e3dc.f): rTLS pairs the least-squares residual with its
+            // tau-scaled self for the residual, with itself for the modified residual
+            if (P.idc) {
+                R ly[5], lt[5], gA[3][5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    if (MODE == TM_MODRES) {
+                        ly[k] = aig[k];
+                        lt[k] = ly[k];
+                    } else {
+                        ly[k] = aig[k] + a0x[k] - ((with_q && k > 0) ? o[Q::kDq + k - 1] : R(0));
+                        lt[k] = (k == 0 ? st.tau[0] : k == 4 ? st.tau[2] : st.tau[1]) * ly[k];
+                    }
+                }
+                o[Q::kDc] = dc_point(P, gm.G, st, g, ly, lt, gA);
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) o[Q::kDc + 1 + 5 * i + k] = gA[i][k];
+            }
+        }
         }
     }
     __syncthreads();
@@ -1737,6 +1817,27 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
                 for (int k = 0; k < 5; ++k) bm += Bm[r][k] * lm[k];
                 const R fm = (r == 0) ? R(0) : (r == 4) ? usv : sv[r - 1];
                 rml[r] += w * (fm + bm + Na * rm16[r]);
+            }
+            if constexpr (sizeof(R) == 8 && MODE == TM_FULL) {
+                // the reference's rmi(:,11) = rmi(:,12) + DC gA(:,12) (e3dc.f:366)
+                if (P.idc) {
+                    const R* dq = v + Q::kDc;
+                    const R sz = drdp * lm[0] + drdT * lm[4];
+                    const R z0 = u2 * sz + rho * lm[3];
+                    const R z1 = u0 * z0 + rho * u2 * lm[1] + v[Q::kVt + 6];
+                    rml[0] += w * s[2] * (z1 + dq[0] * dq[12] - z0 - dq[0] * dq[11]);
+                }
+            }
+        }
+        if constexpr (sizeof(R) == 8 && MODE != TM_LIN) {
+            if (P.idc) {
+                const R* dq = v + Q::kDc;
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    const R f = w * dq[0] * (s[0] * dq[1 + k] + s[1] * dq[6 + k] + s[2] * dq[11 + k]);
+                    if (MODE == TM_RES || MODE == TM_FULL) rl[k] += f;
+                    if (MODE != TM_RES) rml[k] += f;
+                }
             }
         }
         if (MODE == TM_FULL && bd) {
@@ -1880,7 +1981,7 @@ void upload_topo_tables(Ctx& C) {
 
 template <typename R, int NEN>
 constexpr size_t topo_smem() {
-    return sizeof(R) * (size_t)(kTopoThreads / NEN) * NEN * (kTopoNode + TopoQp<NEN>::kN);
+    return sizeof(R) * (size_t)(kTopoThreads / NEN) * NEN * (kTopoNode + TopoQp<NEN, sizeof(R) == 8>::kN);
 }
 
 template <typename R, int NEN, int TOPO>

@@ -31,7 +31,9 @@ struct Phys {
     R dts2;              // (2*dtsfct*Dtgl)^2  (0 if the time term is removed)
     R fmu2;              // 36*mu^2
     R taucfct, rtempcv;  // tau_C scale, temper/cv
+    R epsM;              // sqrt(machine epsilon): the DC factor's guard (e3dc.f:260)
     int navier, supg;
+    int idc;             // discontinuity capturing (FP64 residual kernels only)
 };
 
 // quadrature/shape tables for linear tets (host-computed, read-only in constant memory)

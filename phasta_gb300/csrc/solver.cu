@@ -691,6 +691,10 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
         if (!lhs && C.sp.have != C.cfg.precision)
             return fail(C, PHGPU_ERR_INVALID, "lhs = 0 needs the tangent of an earlier lhs = 1 solve");
     }
+    // discontinuity capturing is in the FP64 residual kernels; the linearized and assembled
+    // products do not carry it
+    if (C.cfg.iDC != 0 && (C.cfg.precision != PHGPU_FP64 || C.cfg.ap_mode != PHGPU_AP_FD))
+        return fail(C, PHGPU_ERR_UNSUPPORTED, "iDC != 0 needs FP64 with the finite-difference product");
     const bool asm_bd = !sparse || lhs;
     cudaEventRecord(C.ev[0], C.stream);
     if (C.cfg.precision == PHGPU_FP64) {
@@ -901,6 +905,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     if (cfg->Kspace < 1 || cfg->Kspace > kMaxK || cfg->nGMRES < 1) return PHGPU_ERR_INVALID;
     if (cfg->itau != 0 || cfg->ipord != 1 || cfg->EntropyPressure != 0) return PHGPU_ERR_UNSUPPORTED;
     if (cfg->idiff != 0 && cfg->idiff != 1) return PHGPU_ERR_UNSUPPORTED;
+    if (cfg->iDC < 0 || cfg->iDC > 3) return PHGPU_ERR_INVALID;
     phgpu_ctx* h = new (std::nothrow) phgpu_ctx();
     if (!h) return PHGPU_ERR_NOMEM;
     Ctx& C = h->c;
@@ -1110,6 +1115,7 @@ int phgpu_set_config(phgpu_ctx* h, const phgpu_config* cfg) {
     if (cfg->Kspace < 1 || cfg->Kspace > h->c.Ucap || cfg->nGMRES < 1) return PHGPU_ERR_INVALID;
     if (cfg->itau != 0 || cfg->ipord != 1 || cfg->EntropyPressure != 0) return PHGPU_ERR_UNSUPPORTED;
     if (cfg->idiff != 0 && cfg->idiff != 1) return PHGPU_ERR_UNSUPPORTED;
+    if (cfg->iDC < 0 || cfg->iDC > 3) return PHGPU_ERR_INVALID;
     const bool was64 = h->c.cfg.precision == PHGPU_FP64;
     const bool is64 = cfg->precision == PHGPU_FP64;
     if (was64 != is64 && !was64) return PHGPU_ERR_UNSUPPORTED;  // basis was allocated as FP32

@@ -8,7 +8,7 @@ itrPredict, itrCorrect and itrUpdate of the reference compute for the seeded
 inputs, which are stored beside the outputs; for the sparse solver (lhs = 1)
 also genadj, ElmGMRs, Spsi3pre, SparseAp (with bc3per) and SolGMRs.
 
-    python tests/golden/make_ref_golden.py [reference phSolver directory]
+    python tests/golden/make_ref_golden.py [reference phSolver directory] [case names]
 """
 from __future__ import annotations
 
@@ -50,6 +50,11 @@ CASES = [
     ("mixed3_idiff", lambda: mixed(3, 3, (3, 3, 2), idiff=1), ("elm", "solve")),
     # single-topology hex and wedge meshes (periodic boxes)
     ("hex3", lambda: mixed(0, 3, 0), ("elm", "sparse", "ebe")),
+    # discontinuity capturing: DC-mallet, DC-quadratic and DC-min (e3dc.f) on the matrix-free path
+    ("channel4_dc1", lambda: channel(4, ac_scale=0.05, sigma=0.05, iDC=1), ("elm", "pieces", "solve")),
+    ("channel4_dc2", lambda: channel(4, ac_scale=0.05, sigma=0.05, iDC=2), ("elm", "pieces")),
+    ("channel4_dc3", lambda: channel(4, ac_scale=0.05, sigma=0.05, iDC=3), ("elm", "pieces")),
+    ("mixed3_dc1", lambda: mixed(3, 3, (3, 3, 2), sigma=0.05, iDC=1), ("elm", "pieces")),
     ("wedge3", lambda: mixed(0, 0, (3, 3, 2)), ("elm", "sparse", "ebe")),
 ]
 
@@ -129,8 +134,10 @@ def main():
     ref_root = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REF
     if not (ref_root / "compressible" / "e3.f").exists():
         raise SystemExit(f"reference sources not found under {ref_root}")
+    only = set(sys.argv[2:])
     for name, build, parts in CASES:
-        make(name, build, parts, ref_root)
+        if not only or name in only:
+            make(name, build, parts, ref_root)
 
 
 if __name__ == "__main__":

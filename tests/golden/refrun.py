@@ -45,6 +45,8 @@ SOURCES = [
     "compressible/sparseap.f", "compressible/solgmr.f",
     # element-by-element solver: ElmGMRe, i3pre, Au1GMR/AsAuGMR/localt, SolGMRe
     "compressible/i3pre.f", "compressible/au1gmr.f", "compressible/asaugmr.f", "compressible/localt.f",
+    # discontinuity capturing (iDC = 1, 2, 3)
+    "compressible/e3dc.f",
 ]
 # rstat.f only prints statistics, and SolMFG calls it with two of its three
 # arguments (solmfg.f:367 vs rstat.f:1); its totres (rstat.f:108) is computed
@@ -128,7 +130,7 @@ class RefPhasta:
         G.dtgl, G.almi, G.alfi, G.gami = p["Dtgl"], p["almi"], p["alfi"], p["gami"]
         G.lhs, G.itau, G.ipord, G.idiff, G.isurf = 0, p["itau"], p["ipord"], p.get("idiff", 0), 0
         G.dtsfct, G.taucfct, G.temper = p["dtsfct"], p["taucfct"], p["temper"]
-        G.ivart, G.navier, G.jactyp, G.idc = p["ivart"], p["Navier"], 0, 0
+        G.ivart, G.navier, G.jactyp, G.idc = p["ivart"], p["Navier"], 0, p.get("iDC", 0)
         G.iremovestabtimeterm, G.entropypressure = p["iremoveStabTimeTerm"], p["EntropyPressure"]
         G.idflx = 12 if p.get("idiff", 0) >= 1 else 0  # (nflow-1)*nsd, solmfg.f:61-63
         G.kspace, G.ngmres, G.miniters = p["Kspace"], p["nGMRES"], p["minIters"]

@@ -247,3 +247,35 @@ def test_split_double_float_outer_residual_hex_wedge(gpu_lib, idiff):
     assert rel(rdf, r64) < 1e-6
     assert sdf.rnorm == pytest.approx(s64.rnorm, rel=1e-7)
 
+
+
+@pytest.mark.parametrize("iDC", [1, 2, 3])
+@pytest.mark.parametrize("make", [lambda iDC: channel(10, ac_scale=0.05, sigma=0.05, iDC=iDC),
+                                  lambda iDC: mixed(3, 3, (3, 3, 2), sigma=0.05, iDC=iDC)],
+                         ids=["channel10", "mixed3"])
+def test_discontinuity_capturing_fp64(gpu_lib, make, iDC):
+    """iDC = 1, 2, 3 (e3dc.f) in the FP64 element routines: ElmMFG's res, rmes (with the
+    reference's rmi(:,11) line) and BDiag, ItrRes's modified residual, within 1e-10 of the
+    oracle; the DC term itself is non-trivial (the residual moves against iDC = 0)."""
+    case, p, y, ac = make(iDC)
+    g, o = GpuSolver(case, p), pyoracle.Oracle(case, p)
+    r, m, b = g.ElmMFG(y, ac)
+    ro, mo, bo = o.ElmMFG(y, ac)
+    assert rel(r, ro) < 1e-10 and rel(m, mo) < 1e-10 and rel(b, bo) < 1e-10
+    g0 = GpuSolver(case, dict(p, iDC=0))
+    r0, m0, _b0 = g0.ElmMFG(y, ac)
+    assert rel(r, r0) > 1e-6 and rel(m, m0) > 1e-6
+    rng = np.random.default_rng(5)
+    yp = y * (1.0 + 1e-3 * rng.standard_normal(y.shape))
+    base = rng.standard_normal(y.shape)
+    assert rel(g.ItrRes(yp, y, ac, base), o.ItrRes(yp, y, ac, base)) < 1e-10
+    g.close()
+    g0.close()
+
+
+def test_discontinuity_capturing_needs_fp64_fd(gpu_lib):
+    case, p, y, ac = channel(6, iDC=1, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR)
+    g = GpuSolver(case, p)
+    with pytest.raises(PhgpuError) as e:
+        g.SolMFG(y, ac)
+    assert e.value.code == L.PHGPU_ERR_UNSUPPORTED

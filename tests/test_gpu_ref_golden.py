@@ -83,7 +83,9 @@ def test_gpu_solmfg_matches_reference(gpu_lib, name):
     assert st.iKs == int(d["sol_iKs"]) and st.lGMRES == int(d["sol_lGMRES"])
     assert st.ntotGM == int(d["sol_ntotGM"])
     assert abs(st.eGMRES / float(d["sol_eGMRES"]) - 1.0) < 1e-2
-    assert rel(Dy, d["sol_Dy"]) < 1e-5
+    # with discontinuity capturing the reference's own finite-difference interval is ~2e-12,
+    # and two FP64 evaluations of that solve agree to ~2e-3 (see the oracle's golden test)
+    assert rel(Dy, d["sol_Dy"]) < (1e-2 if p.get("iDC", 0) else 1e-5)
 
 
 @pytest.mark.parametrize("name", having("step"))

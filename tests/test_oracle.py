@@ -22,13 +22,26 @@ def test_tables_match_reference_c_sources():
         assert np.array_equal(np.array(g[k]), t[k]), k
 
 
-def test_uniform_freestream_has_zero_residual():
-    case, p, y, ac = channel(8, sigma=0.0)
+@pytest.mark.parametrize("iDC", [0, 1, 2, 3])
+def test_uniform_freestream_has_zero_residual(iDC):
+    case, p, y, ac = channel(8, sigma=0.0, iDC=iDC)
     o = pyoracle.Oracle(case, p)
     res, rmes, bd = o.ElmMFG(y, ac)
-    # flux magnitudes are O(p) ~ 8: a free stream is an exact solution
+    # flux magnitudes are O(p) ~ 8: a free stream is an exact solution (the DC factor of
+    # zero gradients and residuals is zero: raLS = rTLS = 0, gnorm = 1/epsM)
     assert np.abs(res).max() < 1e-12
     assert np.isfinite(bd).all()
+
+
+def test_discontinuity_capturing_leaves_bdiag():
+    """The matrix-free block diagonal has no DC term (e3bdg.f takes no DC stiffness); the
+    residual does."""
+    case, p, y, ac = channel(6, sigma=0.05, ac_scale=0.05)
+    r0, _m0, b0 = pyoracle.Oracle(case, p).ElmMFG(y, ac)
+    for iDC in (1, 2, 3):
+        r, _m, b = pyoracle.Oracle(case, dict(p, iDC=iDC)).ElmMFG(y, ac)
+        assert np.array_equal(b, b0)
+        assert np.linalg.norm(r - r0) > 1e-8 * np.linalg.norm(r0)
 
 
 def test_periodic_vortex_runs_and_is_finite():

@@ -45,7 +45,9 @@ def load(name):
     assert np.array_equal(d["ien"], case.ien.astype(np.int32)), "mesh generator changed"
     assert np.array_equal(d["x"], case.x_ref())
     assert np.array_equal(d["y"], y) and np.array_equal(d["ac"], ac), "seeded state changed"
-    assert json.loads(str(d["params"])) == json.loads(json.dumps(p, sort_keys=True))
+    stored = json.loads(str(d["params"]))
+    stored.setdefault("iDC", 0)  # fixtures written before the option hold no key for it (it was off)
+    assert stored == json.loads(json.dumps(p, sort_keys=True))
     return d, case, p
 
 
@@ -82,7 +84,16 @@ def test_oracle_solmfg_matches_reference(name):
     assert st.iKs == int(d["sol_iKs"]) and st.lGMRES == int(d["sol_lGMRES"])
     assert st.ntotGM == int(d["sol_ntotGM"])
     assert abs(st.eGMRES / float(d["sol_eGMRES"]) - 1.0) < 1e-2
-    assert rel(Dy, d["sol_Dy"]) < 1e-5
+    if p.get("iDC", 0):
+        # With discontinuity capturing itrFDI sets eGMRES = 2.4e-12 in this case (the
+        # reference's ElmMFG rmes also differs from ItrRes's modified residual by e3dc.f:366,
+        # rmi(:,11) = rmi(:,12) + ...), so the products (Rmod - rmes)/eGMRES amplify rounding
+        # by ~1e4 and two FP64 evaluations of the same solve agree to ~2e-3 (measured, also
+        # with the reference's own eGMRES); the element routines and the Krylov counts are
+        # the sharp checks of this case.
+        assert rel(Dy, d["sol_Dy"]) < 1e-2
+    else:
+        assert rel(Dy, d["sol_Dy"]) < 1e-5
 
 
 @pytest.mark.parametrize("name", having("step"))
