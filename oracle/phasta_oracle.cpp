@@ -405,7 +405,30 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             gijd[5] = dxidx[0][2] * t1 + dxidx[1][2] * t2 + dxidx[2][2] * t3;
         }
         double tau[3];
-        {
+        if (c.itau == 1) {
+            // Diagonal-Franca (e3tau.f:54-139), iremoveStabTimeTerm = 0, ipord = 1
+            double fact = gijd[0] * gijd[2] * gijd[5] - gijd[0] * gijd[4] * gijd[4] - gijd[2] * gijd[3] * gijd[3] -
+                          gijd[5] * gijd[1] * gijd[1] + gijd[1] * gijd[3] * gijd[4] * two;
+            double uh1 = u1 * u1 * (gijd[2] * gijd[5] - gijd[4] * gijd[4]) +
+                         u2 * u2 * (gijd[0] * gijd[5] - gijd[3] * gijd[3]) +
+                         u3 * u3 * (gijd[0] * gijd[2] - gijd[1] * gijd[1]) +
+                         two * (u1 * u2 * (gijd[3] * gijd[4] - gijd[1] * gijd[5]) +
+                                u1 * u3 * (gijd[1] * gijd[4] - gijd[3] * gijd[2]) +
+                                u2 * u3 * (gijd[3] * gijd[1] - gijd[0] * gijd[4]));
+            uh1 = two * std::sqrt(uh1 / fact);
+            double h2o2u = u1 * u1 * gijd[0] + u2 * u2 * gijd[2] + u3 * u3 * gijd[5] +
+                           (u1 * u2 * gijd[1] + u1 * u3 * gijd[3] + u2 * u3 * gijd[4]) * two + 1.0e-15;
+            h2o2u = one / std::sqrt(h2o2u);
+            fact = pt5 * rho * uh1 / rmu;
+            tau[0] = pt5 * uh1 * std::min(one, fact) * c.taucfct;
+            const double dts = one / (c.Dtgl * c.dtsfct);
+            tau[1] = std::min(dts, h2o2u);
+            tau[1] = tau[1] / rho;
+            tau[2] = tau[1] / cv;
+            fact = h2o2u * h2o2u * rk * pt66 / rmu;
+            tau[1] = std::min(tau[1], fact);
+            tau[2] = std::min(tau[2], fact * rmu / con) * c.temper;
+        } else {
             const double fff = 36.0;  // ipord == 1
             const double dts = (c.iremoveStabTimeTerm == 1) ? zero : c.dtsfct * c.Dtgl;
             double t2 = rho * rho * ((two * dts) * (two * dts) +

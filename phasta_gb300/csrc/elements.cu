@@ -110,6 +110,10 @@ Phys<R> make_phys(const phgpu_config& c) {
     p.supg = c.ivart >= 2;
     p.epsM = (R)c.epsM;
     p.idc = c.iDC;
+    p.itau = c.itau;
+    p.rdts = (R)(1.0 / (c.Dtgl * c.dtsfct));
+    p.celt = (R)(2.0 / 3.0);
+    p.temper = (R)c.temper;
     return p;
 }
 template Phys<double> make_phys<double>(const phgpu_config&);

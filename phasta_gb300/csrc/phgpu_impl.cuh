@@ -32,8 +32,10 @@ struct Phys {
     R fmu2;              // 36*mu^2
     R taucfct, rtempcv;  // tau_C scale, temper/cv
     R epsM;              // sqrt(machine epsilon): the DC factor's guard (e3dc.f:260)
+    R rdts, celt, temper;  // itau = 1: 1/(Dtgl dtsfct), the diffusive correction 2/3, temper
     int navier, supg;
     int idc;             // discontinuity capturing (FP64 residual kernels only)
+    int itau;            // 0 Diagonal-Shakib, 1 Diagonal-Franca (FP64 kernels only)
 };
 
 // quadrature/shape tables for linear tets (host-computed, read-only in constant memory)

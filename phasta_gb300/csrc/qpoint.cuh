@@ -51,11 +51,33 @@ __device__ __forceinline__ void qp_state(const Phys<R>& P, R p, R u0, R u1, R u2
     b.e4p = b.drdT * hk + b.rho * P.cp;
 }
 
-// diagonal tau (e3tau.f:140-181, itau = 0)
+// diagonal tau: itau = 0 (Shakib, e3tau.f:140-181) or, in FP64, itau = 1 (Franca's tau with
+// the cell Reynolds number and a diffusive limit, e3tau.f:54-139)
 template <typename R>
 __device__ __forceinline__ void qp_tau(const Phys<R>& P, const Geo<R>& geo, Qp<R>& b) {
     const R* G = geo.G;
     const R u0 = b.u[0], u1 = b.u[1], u2 = b.u[2];
+    if constexpr (sizeof(R) == 8) {
+        if (P.itau == 1) {
+            const R det = G[0] * G[2] * G[5] - G[0] * G[4] * G[4] - G[2] * G[3] * G[3] - G[5] * G[1] * G[1] +
+                          R(2) * G[1] * G[3] * G[4];
+            const R uau = u0 * u0 * (G[2] * G[5] - G[4] * G[4]) + u1 * u1 * (G[0] * G[5] - G[3] * G[3]) +
+                          u2 * u2 * (G[0] * G[2] - G[1] * G[1]) +
+                          R(2) * (u0 * u1 * (G[3] * G[4] - G[1] * G[5]) + u0 * u2 * (G[1] * G[4] - G[3] * G[2]) +
+                                  u1 * u2 * (G[3] * G[1] - G[0] * G[4]));
+            const R uh1 = R(2) * sqrt(uau / det);  // |u| h_1
+            const R h2o2u = R(1) / sqrt(u0 * u0 * G[0] + u1 * u1 * G[2] + u2 * u2 * G[5] +
+                                        R(2) * (u0 * u1 * G[1] + u0 * u2 * G[3] + u1 * u2 * G[4]) + R(1e-15));
+            const R reh = R(0.5) * b.rho * uh1 / P.rmu;  // cell Reynolds number
+            b.tau[0] = R(0.5) * uh1 * fmin(R(1), reh) * P.taucfct;
+            const R t1 = fmin(P.rdts, h2o2u) / b.rho;
+            const R t2 = t1 / P.cv;
+            const R fd = h2o2u * h2o2u * b.rk * P.celt / P.rmu;
+            b.tau[1] = fmin(t1, fd);
+            b.tau[2] = fmin(t2, fd * P.rmu / P.con) * P.temper;
+            return;
+        }
+    }
     const R uGu = u0 * (u0 * G[0] + R(2) * (u1 * G[1] + u2 * G[3])) + u1 * (u1 * G[2] + R(2) * u2 * G[4]) +
                   u2 * u2 * G[5];
     const R t2 = b.rho * b.rho * (P.dts2 + uGu) + P.fmu2 * geo.GG;

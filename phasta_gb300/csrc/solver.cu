@@ -903,7 +903,11 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
         return PHGPU_ERR_INVALID;
     if (m->nbelem < 0 || (m->nbelem > 0 && !m->ienb)) return PHGPU_ERR_INVALID;
     if (cfg->Kspace < 1 || cfg->Kspace > kMaxK || cfg->nGMRES < 1) return PHGPU_ERR_INVALID;
-    if (cfg->itau != 0 || cfg->ipord != 1 || cfg->EntropyPressure != 0) return PHGPU_ERR_UNSUPPORTED;
+    if ((cfg->itau != 0 && cfg->itau != 1) || cfg->ipord != 1 || cfg->EntropyPressure != 0) return PHGPU_ERR_UNSUPPORTED;
+    // itau = 1 (Diagonal-Franca) is in the FP64 kernels; the reference leaves its momentum tau
+    // unset when the stabilization time term is removed (e3tau.f:107-111)
+    if (cfg->itau == 1 && (cfg->precision != PHGPU_FP64 || cfg->iremoveStabTimeTerm != 0 || !(cfg->rmu > 0.0)))
+        return PHGPU_ERR_UNSUPPORTED;
     if (cfg->idiff != 0 && cfg->idiff != 1) return PHGPU_ERR_UNSUPPORTED;
     if (cfg->iDC < 0 || cfg->iDC > 3) return PHGPU_ERR_INVALID;
     phgpu_ctx* h = new (std::nothrow) phgpu_ctx();
@@ -1113,7 +1117,11 @@ int phgpu_destroy(phgpu_ctx* h) {
 int phgpu_set_config(phgpu_ctx* h, const phgpu_config* cfg) {
     if (!h || !cfg) return PHGPU_ERR_INVALID;
     if (cfg->Kspace < 1 || cfg->Kspace > h->c.Ucap || cfg->nGMRES < 1) return PHGPU_ERR_INVALID;
-    if (cfg->itau != 0 || cfg->ipord != 1 || cfg->EntropyPressure != 0) return PHGPU_ERR_UNSUPPORTED;
+    if ((cfg->itau != 0 && cfg->itau != 1) || cfg->ipord != 1 || cfg->EntropyPressure != 0) return PHGPU_ERR_UNSUPPORTED;
+    // itau = 1 (Diagonal-Franca) is in the FP64 kernels; the reference leaves its momentum tau
+    // unset when the stabilization time term is removed (e3tau.f:107-111)
+    if (cfg->itau == 1 && (cfg->precision != PHGPU_FP64 || cfg->iremoveStabTimeTerm != 0 || !(cfg->rmu > 0.0)))
+        return PHGPU_ERR_UNSUPPORTED;
     if (cfg->idiff != 0 && cfg->idiff != 1) return PHGPU_ERR_UNSUPPORTED;
     if (cfg->iDC < 0 || cfg->iDC > 3) return PHGPU_ERR_INVALID;
     const bool was64 = h->c.cfg.precision == PHGPU_FP64;

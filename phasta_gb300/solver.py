@@ -54,10 +54,10 @@ class PhgpuError(RuntimeError):
 def make_params(mu: float, dt: float, rho_inf: float = 0.5, Kspace: int = 10, etol: float = 1e-3,
                 minIters: int = 1, nGMRES: int = 1, pr: float = 0.72, precision: int = L.PHGPU_FP64,
                 ap_mode: int = L.PHGPU_AP_FD, navier: int = 1, ivart: int = 2,
-                outer_residual: int = L.PHGPU_RES_FP64, idiff: int = 0, iDC: int = 0) -> dict:
+                outer_residual: int = L.PHGPU_RES_FP64, idiff: int = 0, iDC: int = 0, itau: int = 0) -> dict:
     """The COMMON-block values of the hot path (input.config defaults otherwise)."""
     p = {"Rgas": rgas(), "gamma": GAMMA, "gamma1": GAMMA1, "pr": pr, "rmu": mu,
-         "dtsfct": 1.0, "taucfct": 1.0, "temper": 1.0, "itau": 0, "ivart": ivart,
+         "dtsfct": 1.0, "taucfct": 1.0, "temper": 1.0, "itau": itau, "ivart": ivart,
          "iremoveStabTimeTerm": 0, "Navier": navier, "ipord": 1, "EntropyPressure": 0,
          "Kspace": Kspace, "nGMRES": nGMRES, "minIters": minIters, "etol": etol,
          "epsM": float(np.sqrt(np.finfo(np.float64).eps)), "eGMRES": 0.0, "iter": 1, "istep": 0,

@@ -55,6 +55,9 @@ CASES = [
     ("channel4_dc2", lambda: channel(4, ac_scale=0.05, sigma=0.05, iDC=2), ("elm", "pieces")),
     ("channel4_dc3", lambda: channel(4, ac_scale=0.05, sigma=0.05, iDC=3), ("elm", "pieces")),
     ("mixed3_dc1", lambda: mixed(3, 3, (3, 3, 2), sigma=0.05, iDC=1), ("elm", "pieces")),
+    # itau = 1: Diagonal-Franca tau (e3tau.f:54-139), matrix-free and assembled solvers
+    ("channel4_tau1", lambda: channel(4, ac_scale=0.05, itau=1), ("elm", "pieces", "solve", "sparse")),
+    ("mixed3_tau1", lambda: mixed(3, 3, (3, 3, 2), itau=1), ("elm", "pieces")),
     ("wedge3", lambda: mixed(0, 0, (3, 3, 2)), ("elm", "sparse", "ebe")),
 ]
 

@@ -279,3 +279,28 @@ def test_discontinuity_capturing_needs_fp64_fd(gpu_lib):
     with pytest.raises(PhgpuError) as e:
         g.SolMFG(y, ac)
     assert e.value.code == L.PHGPU_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("make", [lambda: channel(10, ac_scale=0.05, itau=1),
+                                  lambda: mixed(3, 3, (3, 3, 2), itau=1)], ids=["channel10", "mixed3"])
+def test_franca_tau_fp64(gpu_lib, make):
+    """itau = 1 (Diagonal-Franca tau, e3tau.f:54-139) in the FP64 kernels: ElmMFG, ItrRes and
+    the assembled tangent within 1e-10 / 1e-12 of the oracle, and a SolMFG with the same Krylov
+    count; the tau differs from itau = 0 (the residual moves)."""
+    case, p, y, ac = make()
+    g, o = GpuSolver(case, p), pyoracle.Oracle(case, p)
+    r, m, b = g.ElmMFG(y, ac)
+    ro, mo, bo = o.ElmMFG(y, ac)
+    assert rel(r, ro) < 1e-10 and rel(m, mo) < 1e-10 and rel(b, bo) < 1e-10
+    r0, _m0, _b0 = GpuSolver(case, dict(p, itau=0)).ElmMFG(y, ac)
+    assert rel(r, r0) > 1e-6
+    rng = np.random.default_rng(5)
+    yp = y * (1.0 + 1e-3 * rng.standard_normal(y.shape))
+    base = rng.standard_normal(y.shape)
+    assert rel(g.ItrRes(yp, y, ac, base), o.ItrRes(yp, y, ac, base)) < 1e-10
+    res, bd, Dy, st = g.SolMFG(y, ac)
+    ores, obd, oDy, ost = o.SolMFG(y, ac)
+    assert st.iKs == ost.iKs and rel(Dy, oDy) < 1e-6
+    _gres, _gbd, lhsK = g.ElmGMRs(y, ac)
+    _ores, _obd, olhsK = o.ElmGMRs(y, ac)
+    assert rel(lhsK, olhsK) < 1e-12

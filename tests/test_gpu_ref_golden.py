@@ -20,7 +20,7 @@ import pytest
 
 from helpers import rel
 from phasta_gb300 import _lib as L
-from phasta_gb300.solver import GpuSolver
+from phasta_gb300.solver import GpuSolver, PhgpuError
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 sys.path.insert(0, str(GOLDEN))
@@ -56,6 +56,11 @@ def test_gpu_elmmfg_fp64_matches_reference(gpu_lib, name):
 def test_gpu_mixed_bdiag_matches_reference(gpu_lib, name):
     d, case, p = load(name)
     p = dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR)
+    if p["itau"] == 1:  # Diagonal-Franca tau is computed by the FP64 kernels only
+        with pytest.raises(PhgpuError) as e:
+            GpuSolver(case, p)
+        assert e.value.code == L.PHGPU_ERR_UNSUPPORTED
+        return
     g = GpuSolver(case, p)
     r, m, b = g.ElmMFG(d["y"], d["ac"])
     assert rel(b, d["elm_bd"]) < 1e-5
