@@ -20,7 +20,7 @@ module phgpu_iface
      integer(c_int) :: iter, istep
      integer(c_int) :: precision, ap_mode, outer_residual
      integer(c_int) :: idiff         ! 0 or 1 (global diffusive-flux reconstruction)
-     integer(c_int) :: no_graph, iDC, reserved(2)
+     integer(c_int) :: no_graph, iDC, no_pipe, reserved(1)
   end type
 
   type, bind(C) :: phgpu_mesh

@@ -99,7 +99,10 @@ typedef struct {
     int iDC;                         /* discontinuity capturing (e3dc.f): 0 off, 1 DC-mallet,
                                         2 DC-quadratic, 3 DC-min; FP64 with the finite-difference
                                         product (ElmMFG, ItrRes, SolMFG) */
-    int reserved[2];
+    int no_pipe;                     /* 0: the FP32 linearized product runs as a persistent kernel
+                                        that stages the next mesh chunk with cp.async while it
+                                        computes the current one; 1: one CTA per chunk */
+    int reserved[1];
 } phgpu_config;
 
 /* Mesh and boundary-condition arrays (what the reference keeps in

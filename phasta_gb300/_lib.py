@@ -39,7 +39,7 @@ class Config(C.Structure):
         ("etol", C.c_double), ("epsM", C.c_double), ("eGMRES", C.c_double),
         ("iter", C.c_int), ("istep", C.c_int),
         ("precision", C.c_int), ("ap_mode", C.c_int), ("outer_residual", C.c_int), ("idiff", C.c_int),
-        ("no_graph", C.c_int), ("iDC", C.c_int), ("reserved", C.c_int * 2),
+        ("no_graph", C.c_int), ("iDC", C.c_int), ("no_pipe", C.c_int), ("reserved", C.c_int * 1),
     ]
 
 

@@ -16,6 +16,9 @@
 //  * the weights of e3wmlt.f are applied once per element after the
 //    quadrature sum (WdetJ is the same at every point of a linear tet).
 // Results agree with the statement-by-statement restatement to rounding.
+#include <algorithm>
+#include <type_traits>
+
 #include "phgpu_impl.cuh"
 #include "df64.cuh"
 #include "qpoint.cuh"
@@ -447,6 +450,105 @@ k_chunk_res(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restri
 #pragma unroll
         for (int k = 0; k < 5; ++k) og[k] += acc[k];
     }
+}
+
+// --------------------------------------------------------------------------
+// FP32 linearized product (RM_LIN) over the chunks of one colour, software-pipelined: each
+// CTA walks chunks chunk0 + blockIdx.x, + gridDim.x, ... and stages the next chunk's nodal
+// data (coordinates, direction, base state and the product's current values) into the other
+// half of a double buffer with cp.async while it computes the current one.  Chunks of one
+// colour share no node, so prefetching the product's values of a later chunk is safe.  The
+// arithmetic and the summation order are those of k_chunk_res<float, RM_LIN>.
+// --------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+constexpr int kLinNode = 18;  // staged per node: x(3) direction(5) base state(5) product(5)
+
+__global__ void __launch_bounds__(kChunk, PHGPU_RES32_MINB)
+k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x, const float* __restrict__ ya,
+                 const float* __restrict__ yb, float* __restrict__ out, Phys<float> P, int lmax) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sm = reinterpret_cast<float*>(smem_raw);
+    const int per = kLinNode * lmax;
+    float* slot = sm + 2 * per;
+    auto stage = [&](int c, float* b) {
+        const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+        float* sx = b;
+        float* sa = sx + 3 * lmax;
+        float* sb = sa + 5 * lmax;
+        float* so = sb + 5 * lmax;
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            const size_t gn = (size_t)ca.nodes[n0 + l];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) cp_async4(sx + 3 * l + d, x + 3 * gn + d);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                cp_async4(sa + 5 * l + k, ya + 5 * gn + k);
+                cp_async4(sb + 5 * l + k, yb + 5 * gn + k);
+                cp_async4(so + 5 * l + k, out + 5 * gn + k);
+            }
+        }
+    };
+    const int cend = chunk0 + nch;
+    int c = chunk0 + blockIdx.x;
+    if (c < cend) stage(c, sm);
+    cp_async_commit();
+    for (int it = 0; c < cend; c += gridDim.x, ++it) {
+        float* cur = sm + (it & 1) * per;
+        const int cn = c + gridDim.x;
+        if (cn < cend) stage(cn, sm + ((it + 1) & 1) * per);
+        cp_async_commit();
+        cp_async_wait<1>();
+        __syncthreads();
+        const float* sx = cur;
+        const float* sa = sx + 3 * lmax;
+        const float* sb = sa + 5 * lmax;
+        const float* so = sb + 5 * lmax;
+        const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
+        const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+        if ((int)threadIdx.x < ne) {
+            const ushort4 ln = ca.lien[e0 + threadIdx.x];
+            const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
+            float xl[4][3], va[4][5], vb[4][5];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) xl[a][d] = sx[3 * nd[a] + d];
+                lds5(sa, nd[a], va[a]);
+                lds5(sb, nd[a], vb[a]);
+            }
+            float o[4][5];
+            elem_res<float, RM_LIN>(P, xl, va, vb, o);
+            float* sl = slot + 20 * threadIdx.x;
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int k = 0; k < 5; ++k) sl[5 * a + k] = o[a][k];
+        }
+        __syncthreads();
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+            const int s0 = ca.cstart[n0 + l], s1 = ca.cstart[n0 + l + 1];
+            for (int s = s0; s < s1; ++s) {
+                const float* sl = slot + 5 * (int)ca.csr[s];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) acc[k] += sl[k];
+            }
+            float* og = out + 5 * (size_t)ca.nodes[n0 + l];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) og[k] = so[5 * l + k] + acc[k];
+        }
+        __syncthreads();
+    }
+    cp_async_wait<0>();
 }
 
 // --------------------------------------------------------------------------
@@ -2054,6 +2156,9 @@ static ChunkArgs chunk_args(const Ctx& C) {
 
 template <typename R>
 size_t res_smem(const Ctx& C) { return sizeof(R) * ((size_t)C.chunk_lmax * 13 + (size_t)kChunk * 20); }
+size_t lin_pipe_smem(const Ctx& C) {
+    return sizeof(float) * (2 * (size_t)C.chunk_lmax * kLinNode + (size_t)kChunk * 20);
+}
 // extra shared memory of the reconstructed flux (idiff = 1): 12 per chunk node
 template <typename R>
 size_t q_smem(const Ctx& C) { return sizeof(R) * (size_t)C.chunk_lmax * 12; }
@@ -2109,6 +2214,21 @@ int configure_element_kernels(Ctx& C) {
         rc = check(C, cudaFuncSetAttribute(k_chunk_ress<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)(ress_smem(C) + q_smem<float>(C))),
                    "cudaFuncSetAttribute");
+    if (rc == PHGPU_OK)
+        rc = check(C, cudaFuncSetAttribute(k_chunk_lin_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)lin_pipe_smem(C)),
+                   "cudaFuncSetAttribute");
+    if (rc == PHGPU_OK) {
+        // persistent grid of the pipelined linearized product: every resident CTA slot
+        int dev = 0, nsm = 0, per_sm = 0;
+        rc = check(C, cudaGetDevice(&dev), "cudaGetDevice");
+        if (rc == PHGPU_OK) rc = check(C, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+        if (rc == PHGPU_OK)
+            rc = check(C, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chunk_lin_pipe, kChunk,
+                                                                       lin_pipe_smem(C)),
+                       "occupancy");
+        C.lin_pipe_grid = std::max(1, nsm * per_sm);
+    }
     if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 8, 0>(C);
     if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 6, 1>(C);
     if (rc == PHGPU_OK) rc = configure_topo_kernels<float, 8, 0>(C);
@@ -2130,7 +2250,13 @@ void launch_elem_res(Ctx& C, int mode, const R* x, const R* ya, const R* yb, con
             k_chunk_res<R, RM_RES><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip, ql);
         else if (mode == RM_MODRES)
             k_chunk_res<R, RM_MODRES><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
-        else
+        else if constexpr (std::is_same<R, float>::value) {
+            if (!C.cfg.no_pipe && !skip && !iabres)
+                k_chunk_lin_pipe<<<std::min(nc, C.lin_pipe_grid), kChunk, lin_pipe_smem(C), C.stream>>>(
+                    ca, c0, nc, x, ya, yb, out, P, C.chunk_lmax);
+            else
+                k_chunk_res<R, RM_LIN><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
+        } else
             k_chunk_res<R, RM_LIN><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
         ++C.launches;
     }

@@ -179,6 +179,7 @@ struct Ctx {
     unsigned int* d_count = nullptr;
     int* d_flag = nullptr;        // [0] converged, [1] error bits, [2] Krylov iterations of the cycle
     CycleGraph cyc;
+    int lin_pipe_grid = 1;        // its CTAs per colour launch (resident slots)
     double* h_scal = nullptr;     // pinned mirror
     int* h_flag = nullptr;
 

@@ -1529,6 +1529,13 @@ int phgpu_sweep_dev(phgpu_ctx* h, int which) {
         case 2:  // FP32 linearized product in direction y
             launch_elem_res<float>(C, RM_LIN, C.d_xf, C.d_yf, C.d_yf, nullptr, C.d_t32, 0, nullptr);
             break;
+        case 15: {  // the same product with one CTA per chunk (no cp.async pipeline)
+            const int keep = C.cfg.no_pipe;
+            C.cfg.no_pipe = 1;
+            launch_elem_res<float>(C, RM_LIN, C.d_xf, C.d_yf, C.d_yf, nullptr, C.d_t32, 0, nullptr);
+            C.cfg.no_pipe = keep;
+            break;
+        }
         case 3:  // FP32 block diagonal
             launch_elem_full<float>(C, C.d_xf, C.d_yf, C.d_acf, nullptr, nullptr, C.d_bdf);
             break;

@@ -304,3 +304,21 @@ def test_franca_tau_fp64(gpu_lib, make):
     _gres, _gbd, lhsK = g.ElmGMRs(y, ac)
     _ores, _obd, olhsK = o.ElmGMRs(y, ac)
     assert rel(lhsK, olhsK) < 1e-12
+
+
+@pytest.mark.parametrize("n", [10, 64])
+def test_pipelined_linearized_product_is_the_per_chunk_kernel(gpu_lib, n):
+    """The persistent cp.async-pipelined FP32 linearized product (config no_pipe = 0) against
+    one CTA per chunk (no_pipe = 1): the same arithmetic and summation order, so a mixed-
+    precision time step is bitwise the same.  At 64^3 x 6 the colours hold more chunks than
+    the persistent grid, so CTAs walk several chunks through both halves of the buffer."""
+    case, p, y, ac = channel(n, ac_scale=0.05, Kspace=6)
+    p = dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR)
+    out = []
+    for no_pipe in (0, 1):
+        g = GpuSolver(case, dict(p, no_pipe=no_pipe))
+        _yo, _ao, y1, a1, st = g.time_step(y, ac, nitr=1)
+        out.append((y1, a1, st.iKs))
+        g.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
