@@ -176,6 +176,12 @@ int build_chunks(Ctx& C, const int* ien, const double* x_ref) {
             C.err = "chunk construction produced an out-of-range chunk";
             return PHGPU_ERR_INVALID;
         }
+        // each element corner is in one slot list: chunk k's lists start at 4 * elem_start[k]
+        // (the pipelined linearized product copies them from there)
+        if (cstart[node_start[k]] != 4 * elem_start[k] || cstart[node_start[k + 1]] != 4 * elem_start[k + 1]) {
+            C.err = "chunk construction produced misplaced slot lists";
+            return PHGPU_ERR_INVALID;
+        }
         for (int i = elem_start[k]; i < elem_start[k + 1]; ++i) {
             const ushort4 u = lien[i];
             if (u.x >= nn || u.y >= nn || u.z >= nn || u.w >= nn) {

@@ -472,19 +472,38 @@ __device__ __forceinline__ void cp_async_wait() {
 
 constexpr int kLinNode = 18;  // staged per node: x(3) direction(5) base state(5) product(5)
 
+// words of one pipeline stage: node data, then (8-byte aligned) the chunk's local
+// connectivity (ushort4 per element), its slot lists (ushort) and their offsets (int)
+__host__ __device__ constexpr int lin_stage_words(int lmax) {
+    return ((kLinNode * lmax + 1) & ~1) + 2 * kChunk + 2 * kChunk + lmax + 1 + 1;
+}
+
 __global__ void __launch_bounds__(kChunk, PHGPU_RES32_MINB)
 k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x, const float* __restrict__ ya,
                  const float* __restrict__ yb, float* __restrict__ out, Phys<float> P, int lmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sm = reinterpret_cast<float*>(smem_raw);
-    const int per = kLinNode * lmax;
+    const int per = (lin_stage_words(lmax) + 1) & ~1;
+    const int lie_off = (kLinNode * lmax + 1) & ~1;  // even: ushort4 rows 8-byte aligned
     float* slot = sm + 2 * per;
     auto stage = [&](int c, float* b) {
         const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+        const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
         float* sx = b;
         float* sa = sx + 3 * lmax;
         float* sb = sa + 5 * lmax;
         float* so = sb + 5 * lmax;
+        float* sl = b + lie_off;                 // ne ushort4 (2 words each)
+        float* sc = sl + 2 * kChunk;             // 4 ne ushort slot ids (2 per word)
+        float* st = sc + 2 * kChunk;             // nn + 1 offsets
+        // the slot lists of chunk c start at 4 * elem_start[c] (each element corner once)
+        const unsigned* csr_w = reinterpret_cast<const unsigned*>(ca.csr) + 2 * (size_t)e0;
+        for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+            const unsigned s8 = (unsigned)__cvta_generic_to_shared(sl + 2 * i);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s8), "l"(ca.lien + e0 + i) : "memory");
+        }
+        for (int w = threadIdx.x; w < 2 * ne; w += blockDim.x) cp_async4(sc + w, csr_w + w);
+        for (int l = threadIdx.x; l <= nn; l += blockDim.x) cp_async4(st + l, ca.cstart + n0 + l);
         for (int l = threadIdx.x; l < nn; l += blockDim.x) {
             const size_t gn = (size_t)ca.nodes[n0 + l];
 #pragma unroll
@@ -512,10 +531,13 @@ k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x,
         const float* sa = sx + 3 * lmax;
         const float* sb = sa + 5 * lmax;
         const float* so = sb + 5 * lmax;
+        const ushort4* slie = reinterpret_cast<const ushort4*>(cur + lie_off);
+        const unsigned short* scsr = reinterpret_cast<const unsigned short*>(cur + lie_off + 2 * kChunk);
+        const int* scst = reinterpret_cast<const int*>(cur + lie_off + 4 * kChunk);
         const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
         const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
         if ((int)threadIdx.x < ne) {
-            const ushort4 ln = ca.lien[e0 + threadIdx.x];
+            const ushort4 ln = slie[threadIdx.x];
             const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
             float xl[4][3], va[4][5], vb[4][5];
 #pragma unroll
@@ -534,11 +556,12 @@ k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x,
                 for (int k = 0; k < 5; ++k) sl[5 * a + k] = o[a][k];
         }
         __syncthreads();
+        const int sbase = 4 * e0;
         for (int l = threadIdx.x; l < nn; l += blockDim.x) {
             float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-            const int s0 = ca.cstart[n0 + l], s1 = ca.cstart[n0 + l + 1];
+            const int s0 = scst[l] - sbase, s1 = scst[l + 1] - sbase;
             for (int s = s0; s < s1; ++s) {
-                const float* sl = slot + 5 * (int)ca.csr[s];
+                const float* sl = slot + 5 * (int)scsr[s];
 #pragma unroll
                 for (int k = 0; k < 5; ++k) acc[k] += sl[k];
             }
@@ -2157,7 +2180,7 @@ static ChunkArgs chunk_args(const Ctx& C) {
 template <typename R>
 size_t res_smem(const Ctx& C) { return sizeof(R) * ((size_t)C.chunk_lmax * 13 + (size_t)kChunk * 20); }
 size_t lin_pipe_smem(const Ctx& C) {
-    return sizeof(float) * (2 * (size_t)C.chunk_lmax * kLinNode + (size_t)kChunk * 20);
+    return sizeof(float) * (2 * (size_t)((lin_stage_words(C.chunk_lmax) + 1) & ~1) + (size_t)kChunk * 20);
 }
 // extra shared memory of the reconstructed flux (idiff = 1): 12 per chunk node
 template <typename R>
