@@ -472,23 +472,41 @@ __device__ __forceinline__ void cp_async_wait() {
 
 constexpr int kLinNode = 18;  // staged per node: x(3) direction(5) base state(5) product(5)
 
-// words of one pipeline stage: node data, then (8-byte aligned) the chunk's local
-// connectivity (ushort4 per element), its slot lists (ushort) and their offsets (int)
+// words of one data stage: node data, then (8-byte aligned) the chunk's local connectivity
+// (ushort4 per element), its slot lists (ushort) and their offsets (int)
 __host__ __device__ constexpr int lin_stage_words(int lmax) {
-    return ((kLinNode * lmax + 1) & ~1) + 2 * kChunk + 2 * kChunk + lmax + 1 + 1;
+    return ((((kLinNode * lmax + 1) & ~1) + 4 * kChunk + lmax + 2) + 1) & ~1;
 }
+// words of one node-id stage: e0, ne, n0, nn, then the chunk's global node ids
+__host__ __device__ constexpr int lin_id_words(int lmax) { return 4 + lmax; }
 
 __global__ void __launch_bounds__(kChunk, PHGPU_RES32_MINB)
 k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x, const float* __restrict__ ya,
                  const float* __restrict__ yb, float* __restrict__ out, Phys<float> P, int lmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sm = reinterpret_cast<float*>(smem_raw);
-    const int per = (lin_stage_words(lmax) + 1) & ~1;
+    const int per = lin_stage_words(lmax);
     const int lie_off = (kLinNode * lmax + 1) & ~1;  // even: ushort4 rows 8-byte aligned
-    float* slot = sm + 2 * per;
-    auto stage = [&](int c, float* b) {
+    int* ids = reinterpret_cast<int*>(sm + 2 * per);  // 3 x lin_id_words
+    const int idw = lin_id_words(lmax);
+    float* slot = sm + 2 * per + 3 * idw;
+    // node ids of chunk c (and its element and node ranges) into id stage ib
+    auto stage_ids = [&](int c, int ib) {
+        int* h = ids + ib * idw;
         const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
-        const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
+        if (threadIdx.x == 0) {
+            const int e0 = ca.elem[c];
+            h[0] = e0;
+            h[1] = ca.elem[c + 1] - e0;
+            h[2] = n0;
+            h[3] = nn;
+        }
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) cp_async4(h + 4 + l, ca.nodes + n0 + l);
+    };
+    // nodal data, connectivity and slot lists of the chunk whose ids are in stage ib
+    auto stage_data = [&](int ib, float* b) {
+        const int* h = ids + ib * idw;
+        const int e0 = h[0], ne = h[1], n0 = h[2], nn = h[3];
         float* sx = b;
         float* sa = sx + 3 * lmax;
         float* sb = sa + 5 * lmax;
@@ -496,7 +514,7 @@ k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x,
         float* sl = b + lie_off;                 // ne ushort4 (2 words each)
         float* sc = sl + 2 * kChunk;             // 4 ne ushort slot ids (2 per word)
         float* st = sc + 2 * kChunk;             // nn + 1 offsets
-        // the slot lists of chunk c start at 4 * elem_start[c] (each element corner once)
+        // the slot lists of a chunk start at 4 * its first element (each element corner once)
         const unsigned* csr_w = reinterpret_cast<const unsigned*>(ca.csr) + 2 * (size_t)e0;
         for (int i = threadIdx.x; i < ne; i += blockDim.x) {
             const unsigned s8 = (unsigned)__cvta_generic_to_shared(sl + 2 * i);
@@ -505,7 +523,7 @@ k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x,
         for (int w = threadIdx.x; w < 2 * ne; w += blockDim.x) cp_async4(sc + w, csr_w + w);
         for (int l = threadIdx.x; l <= nn; l += blockDim.x) cp_async4(st + l, ca.cstart + n0 + l);
         for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-            const size_t gn = (size_t)ca.nodes[n0 + l];
+            const size_t gn = (size_t)h[4 + l];
 #pragma unroll
             for (int d = 0; d < 3; ++d) cp_async4(sx + 3 * l + d, x + 3 * gn + d);
 #pragma unroll
@@ -516,17 +534,27 @@ k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x,
             }
         }
     };
-    const int cend = chunk0 + nch;
+    const int cend = chunk0 + nch, G = gridDim.x;
     int c = chunk0 + blockIdx.x;
-    if (c < cend) stage(c, sm);
+    if (c >= cend) return;
+    // prologue: ids of the first chunk, then its data and the ids of the next
+    stage_ids(c, 0);
     cp_async_commit();
-    for (int it = 0; c < cend; c += gridDim.x, ++it) {
-        float* cur = sm + (it & 1) * per;
-        const int cn = c + gridDim.x;
-        if (cn < cend) stage(cn, sm + ((it + 1) & 1) * per);
-        cp_async_commit();
-        cp_async_wait<1>();
+    cp_async_wait<0>();
+    __syncthreads();
+    stage_data(0, sm);
+    if (c + G < cend) stage_ids(c + G, 1);
+    cp_async_commit();
+    for (int it = 0; c < cend; c += G, ++it) {
+        cp_async_wait<0>();  // data of chunk c, ids of chunk c + G
         __syncthreads();
+        const int cn = c + G;
+        if (cn < cend) stage_data((it + 1) % 3, sm + ((it + 1) & 1) * per);
+        if (cn + G < cend) stage_ids(cn + G, (it + 2) % 3);
+        cp_async_commit();
+        const float* cur = sm + (it & 1) * per;
+        const int* h = ids + (it % 3) * idw;
+        const int e0 = h[0], ne = h[1], nn = h[3];
         const float* sx = cur;
         const float* sa = sx + 3 * lmax;
         const float* sb = sa + 5 * lmax;
@@ -534,8 +562,6 @@ k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x,
         const ushort4* slie = reinterpret_cast<const ushort4*>(cur + lie_off);
         const unsigned short* scsr = reinterpret_cast<const unsigned short*>(cur + lie_off + 2 * kChunk);
         const int* scst = reinterpret_cast<const int*>(cur + lie_off + 4 * kChunk);
-        const int e0 = ca.elem[c], ne = ca.elem[c + 1] - e0;
-        const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
         if ((int)threadIdx.x < ne) {
             const ushort4 ln = slie[threadIdx.x];
             const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
@@ -565,7 +591,7 @@ k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x,
 #pragma unroll
                 for (int k = 0; k < 5; ++k) acc[k] += sl[k];
             }
-            float* og = out + 5 * (size_t)ca.nodes[n0 + l];
+            float* og = out + 5 * (size_t)h[4 + l];
 #pragma unroll
             for (int k = 0; k < 5; ++k) og[k] = so[5 * l + k] + acc[k];
         }
@@ -2180,7 +2206,8 @@ static ChunkArgs chunk_args(const Ctx& C) {
 template <typename R>
 size_t res_smem(const Ctx& C) { return sizeof(R) * ((size_t)C.chunk_lmax * 13 + (size_t)kChunk * 20); }
 size_t lin_pipe_smem(const Ctx& C) {
-    return sizeof(float) * (2 * (size_t)((lin_stage_words(C.chunk_lmax) + 1) & ~1) + (size_t)kChunk * 20);
+    return sizeof(float) * (2 * (size_t)lin_stage_words(C.chunk_lmax) + 3 * (size_t)lin_id_words(C.chunk_lmax) +
+                            (size_t)kChunk * 20);
 }
 // extra shared memory of the reconstructed flux (idiff = 1): 12 per chunk node
 template <typename R>
