@@ -291,6 +291,7 @@ def kernel_roofline(g, case, stream, args, krylov_per_newton):
                         "achieved_gbs": algo / t / 1e9, "elements_per_s": E / t}
     # the linearized product with one CTA per chunk, for comparison with the pipelined kernel
     kernels["lin"]["per_chunk_kernel_ms"] = _time_sweep(g, stream, 15) * 1e3
+    kernels["ress"]["per_chunk_kernel_ms"] = _time_sweep(g, stream, 16) * 1e3
     dom = max(kernels, key=lambda k: kernels[k]["ms_per_newton"])
     k = kernels[dom]
     traffic, fp32 = None, None

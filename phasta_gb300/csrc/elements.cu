@@ -916,6 +916,200 @@ struct DfConst {
 constexpr int kSplitSlot = 40;  // per element: 20 hi then 20 lo
 
 
+// one element of the split outer residual: its four nodal contributions as double-float
+// hi/lo pairs in its slot sl (kSplitSlot floats), from the chunk's staged node data
+template <bool WITH_Q>
+__device__ __forceinline__ void ress_element(const ushort4 ln, const float* __restrict__ sxh,
+                                             const float* __restrict__ sxl, const float* __restrict__ syh,
+                                             const float* __restrict__ syl, const float* __restrict__ sa,
+                                             const float* __restrict__ sq, float* __restrict__ sl,
+                                             const Phys<float>& Pf, const DfConst& K) {
+    const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
+    float o32[4][5];
+    {
+        float xl[4][3], yl[4][5], al[4][5], dl[3][5];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) xl[a][d] = sxh[3 * nd[a] + d];
+            lds5(syh, nd[a], yl[a]);
+            lds5(sa, nd[a], al[a]);
+        }
+        // increments from local node 3, from the hi and lo parts
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                dl[a][k] = (yl[a][k] - yl[3][k]) + (syl[5 * nd[a] + k] - syl[5 * nd[3] + k]);
+        Geo<float> geo;
+        geometry(xl, geo);
+        // gradients from the increments (sum_a shg_a = 0): differences of nearby nodal
+        // values keep their own FP32 accuracy instead of that of the values
+        float g[3][5];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                g[i][k] = geo.shg[0][i] * dl[0][k] + geo.shg[1][i] * dl[1][k] + geo.shg[2][i] * dl[2][k];
+        Visc<float> vs;
+        if (Pf.navier) viscous(Pf, g, vs);
+        float divq[4] = {0.f, 0.f, 0.f, 0.f};  // idiff = 1 (e3ivar.f:374-395)
+        if (WITH_Q) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float acc = 0.f;
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    const float* q = sq + 12 * nd[a];
+                    acc += geo.shg[a][0] * q[k] + geo.shg[a][1] * q[4 + k] + geo.shg[a][2] * q[8 + k];
+                }
+                divq[k] = acc;
+            }
+        }
+        const float pr = yl[3][0], Tr = yl[3][4];
+        const float ur[3] = {yl[3][1], yl[3][2], yl[3][3]};
+        const float rhor = pr * Pf.rRgas / Tr;
+        const float mr[3] = {rhor * ur[0], rhor * ur[1], rhor * ur[2]};
+        float S32[3][5], T32[4][5];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) S32[i][k] = 0.f;
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) T32[a][k] = 0.f;
+#pragma unroll 1
+        for (int q = 0; q < 4; ++q) {
+            float N[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) N[a] = shp<float>(q, a);
+            float bq[5], aq[5], dq[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                bq[k] = N[0] * yl[0][k] + N[1] * yl[1][k] + N[2] * yl[2][k] + N[3] * yl[3][k];
+                aq[k] = N[0] * al[0][k] + N[1] * al[1][k] + N[2] * al[2][k] + N[3] * al[3][k];
+                dq[k] = N[0] * dl[0][k] + N[1] * dl[1][k] + N[2] * dl[2][k];
+            }
+            Qp<float> b;
+            qp_state(Pf, bq[0], bq[1], bq[2], bq[3], bq[4], b);
+            qp_tau(Pf, geo, b);
+            float aig[5], a0a[5];
+            ai_gi(b, g, aig);
+            a0_v(b, aq, a0a);
+            float tl[5];
+            tl[0] = b.tau[0] * (aig[0] + a0a[0]);
+            tl[1] = b.tau[1] * (aig[1] + a0a[1] - divq[0]);
+            tl[2] = b.tau[1] * (aig[2] + a0a[2] - divq[1]);
+            tl[3] = b.tau[1] * (aig[3] + a0a[3] - divq[2]);
+            tl[4] = b.tau[2] * (aig[4] + a0a[4] - divq[3]);
+            float F[3][5];
+            // Euler-flux increment F(y_q) - F(y_r) (flux sign of e3conv.f:72-96)
+            const float drho = (dq[0] * Tr - pr * dq[4]) * Pf.rRgas / (Tr * b.T);
+            const float dek = Pf.cv * dq[4] + (ur[0] * dq[1] + ur[1] * dq[2] + ur[2] * dq[3]) +
+                              0.5f * (dq[1] * dq[1] + dq[2] * dq[2] + dq[3] * dq[3]);
+            const float ek = b.ei + b.rk;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float dm = drho * b.u[i] + rhor * dq[1 + i];
+                F[i][0] = -dm;
+#pragma unroll
+                for (int j = 0; j < 3; ++j) F[i][1 + j] = -(dm * b.u[j] + mr[i] * dq[1 + j]) - (i == j ? dq[0] : 0.f);
+                F[i][4] = -(dm * ek + mr[i] * dek) - (dq[1 + i] * b.p + ur[i] * dq[0]);
+            }
+            if (Pf.navier) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) F[i][1 + j] += vs.t[i][j];
+                    F[i][4] += b.u[0] * vs.t[i][0] + b.u[1] * vs.t[i][1] + b.u[2] * vs.t[i][2] + vs.q[i];
+                }
+            }
+            add_ai_v(b, tl, F);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 5; ++k) S32[i][k] += F[i][k];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int k = 0; k < 5; ++k) T32[a][k] += N[a] * a0a[k];
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                o32[a][k] = geo.WdetJ * (geo.shg[a][0] * S32[0][k] + geo.shg[a][1] * S32[1][k] +
+                                         geo.shg[a][2] * S32[2][k] + T32[a][k]);
+    }
+    // ---- element-constant flux F(y_r) (double-float) ----
+    const int r = nd[3];
+    const df64 p = df_make(syh[5 * r + 0], syl[5 * r + 0]);
+    const df64 u[3] = {df_make(syh[5 * r + 1], syl[5 * r + 1]), df_make(syh[5 * r + 2], syl[5 * r + 2]),
+                       df_make(syh[5 * r + 3], syl[5 * r + 3])};
+    const df64 T = df_make(syh[5 * r + 4], syl[5 * r + 4]);
+    const df64 rho = df_mul(p, df_mul(df_make(K.rRgas_hi, K.rRgas_lo), df_rcp(T)));
+    df64 rk = df_add(df_add(df_mul(u[0], u[0]), df_mul(u[1], u[1])), df_mul(u[2], u[2]));
+    rk.hi *= 0.5f;
+    rk.lo *= 0.5f;
+    const df64 ek = df_add(df_mul(df_make(K.cv_hi, K.cv_lo), T), rk);
+    df64 F[3][5];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const df64 m = df_mul(rho, u[i]);
+        F[i][0] = df_neg(m);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            F[i][1 + j] = df_neg(df_mul(m, u[j]));
+            if (i == j) F[i][1 + j] = df_sub(F[i][1 + j], p);
+        }
+        F[i][4] = df_neg(df_add(df_mul(m, ek), df_mul(u[i], p)));
+    }
+    // cofactors of the edge matrix d'[i][j] = x_j,i - x_3,i (the geometry() layout)
+    df64 d[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            d[i][j] = df_diff(sxh[3 * nd[j] + i], sxl[3 * nd[j] + i], sxh[3 * r + i], sxl[3 * r + i]);
+    auto minor2 = [](df64 a, df64 b, df64 c2, df64 e) { return df_sub(df_mul(a, b), df_mul(c2, e)); };
+    df64 cof[3][3];
+    cof[0][0] = minor2(d[1][1], d[2][2], d[2][1], d[1][2]);
+    cof[0][1] = minor2(d[2][1], d[0][2], d[0][1], d[2][2]);
+    cof[0][2] = minor2(d[0][1], d[1][2], d[0][2], d[1][1]);
+    cof[1][0] = minor2(d[1][2], d[2][0], d[1][0], d[2][2]);
+    cof[1][1] = minor2(d[0][0], d[2][2], d[2][0], d[0][2]);
+    cof[1][2] = minor2(d[1][0], d[0][2], d[0][0], d[1][2]);
+    cof[2][0] = minor2(d[1][0], d[2][1], d[1][1], d[2][0]);
+    cof[2][1] = minor2(d[2][0], d[0][1], d[0][0], d[2][1]);
+    cof[2][2] = minor2(d[0][0], d[1][1], d[0][1], d[1][0]);
+    const df64 wq = df_make(K.wq_hi, K.wq_lo);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) cof[a][i] = df_mul(cof[a][i], wq);
+    df64 s3[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) s3[k] = df_make(0.f, 0.f);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const df64 g64 = df_add(df_add(df_mul(cof[a][0], F[0][k]), df_mul(cof[a][1], F[1][k])),
+                                    df_mul(cof[a][2], F[2][k]));
+            s3[k] = df_add(s3[k], g64);
+            const df64 v = df_add(g64, o32[a][k]);
+            sl[5 * a + k] = v.hi;
+            sl[20 + 5 * a + k] = v.lo;
+        }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const df64 v = df_add(df_neg(s3[k]), o32[3][k]);  // shg_3 = -(shg_0 + shg_1 + shg_2)
+        sl[15 + k] = v.hi;
+        sl[35 + k] = v.lo;
+    }
+}
+
 template <bool WITH_Q>
 __global__ void __launch_bounds__(kChunk, PHGPU_RESS_MINB)
 k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float* __restrict__ xlo,
@@ -950,194 +1144,9 @@ k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float
             for (int k = 0; k < 12; ++k) sq[12 * l + k] = __ldg(ql + 13 * gn + k);
     }
     __syncthreads();
-    if ((int)threadIdx.x < ne) {
-        const ushort4 ln = ca.lien[e0 + threadIdx.x];
-        const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
-        float o32[4][5];
-        {
-            float xl[4][3], yl[4][5], al[4][5], dl[3][5];
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-#pragma unroll
-                for (int d = 0; d < 3; ++d) xl[a][d] = sxh[3 * nd[a] + d];
-                lds5(syh, nd[a], yl[a]);
-                lds5(sa, nd[a], al[a]);
-            }
-            // increments from local node 3, from the hi and lo parts
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-                for (int k = 0; k < 5; ++k)
-                    dl[a][k] = (yl[a][k] - yl[3][k]) + (syl[5 * nd[a] + k] - syl[5 * nd[3] + k]);
-            Geo<float> geo;
-            geometry(xl, geo);
-            // gradients from the increments (sum_a shg_a = 0): differences of nearby nodal
-            // values keep their own FP32 accuracy instead of that of the values
-            float g[3][5];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int k = 0; k < 5; ++k)
-                    g[i][k] = geo.shg[0][i] * dl[0][k] + geo.shg[1][i] * dl[1][k] + geo.shg[2][i] * dl[2][k];
-            Visc<float> vs;
-            if (Pf.navier) viscous(Pf, g, vs);
-            float divq[4] = {0.f, 0.f, 0.f, 0.f};  // idiff = 1 (e3ivar.f:374-395)
-            if (WITH_Q) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    float acc = 0.f;
-#pragma unroll
-                    for (int a = 0; a < 4; ++a) {
-                        const float* q = sq + 12 * nd[a];
-                        acc += geo.shg[a][0] * q[k] + geo.shg[a][1] * q[4 + k] + geo.shg[a][2] * q[8 + k];
-                    }
-                    divq[k] = acc;
-                }
-            }
-            const float pr = yl[3][0], Tr = yl[3][4];
-            const float ur[3] = {yl[3][1], yl[3][2], yl[3][3]};
-            const float rhor = pr * Pf.rRgas / Tr;
-            const float mr[3] = {rhor * ur[0], rhor * ur[1], rhor * ur[2]};
-            float S32[3][5], T32[4][5];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int k = 0; k < 5; ++k) S32[i][k] = 0.f;
-#pragma unroll
-            for (int a = 0; a < 4; ++a)
-#pragma unroll
-                for (int k = 0; k < 5; ++k) T32[a][k] = 0.f;
-#pragma unroll 1
-            for (int q = 0; q < 4; ++q) {
-                float N[4];
-#pragma unroll
-                for (int a = 0; a < 4; ++a) N[a] = shp<float>(q, a);
-                float bq[5], aq[5], dq[5];
-#pragma unroll
-                for (int k = 0; k < 5; ++k) {
-                    bq[k] = N[0] * yl[0][k] + N[1] * yl[1][k] + N[2] * yl[2][k] + N[3] * yl[3][k];
-                    aq[k] = N[0] * al[0][k] + N[1] * al[1][k] + N[2] * al[2][k] + N[3] * al[3][k];
-                    dq[k] = N[0] * dl[0][k] + N[1] * dl[1][k] + N[2] * dl[2][k];
-                }
-                Qp<float> b;
-                qp_state(Pf, bq[0], bq[1], bq[2], bq[3], bq[4], b);
-                qp_tau(Pf, geo, b);
-                float aig[5], a0a[5];
-                ai_gi(b, g, aig);
-                a0_v(b, aq, a0a);
-                float tl[5];
-                tl[0] = b.tau[0] * (aig[0] + a0a[0]);
-                tl[1] = b.tau[1] * (aig[1] + a0a[1] - divq[0]);
-                tl[2] = b.tau[1] * (aig[2] + a0a[2] - divq[1]);
-                tl[3] = b.tau[1] * (aig[3] + a0a[3] - divq[2]);
-                tl[4] = b.tau[2] * (aig[4] + a0a[4] - divq[3]);
-                float F[3][5];
-                // Euler-flux increment F(y_q) - F(y_r) (flux sign of e3conv.f:72-96)
-                const float drho = (dq[0] * Tr - pr * dq[4]) * Pf.rRgas / (Tr * b.T);
-                const float dek = Pf.cv * dq[4] + (ur[0] * dq[1] + ur[1] * dq[2] + ur[2] * dq[3]) +
-                                  0.5f * (dq[1] * dq[1] + dq[2] * dq[2] + dq[3] * dq[3]);
-                const float ek = b.ei + b.rk;
-#pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    const float dm = drho * b.u[i] + rhor * dq[1 + i];
-                    F[i][0] = -dm;
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) F[i][1 + j] = -(dm * b.u[j] + mr[i] * dq[1 + j]) - (i == j ? dq[0] : 0.f);
-                    F[i][4] = -(dm * ek + mr[i] * dek) - (dq[1 + i] * b.p + ur[i] * dq[0]);
-                }
-                if (Pf.navier) {
-#pragma unroll
-                    for (int i = 0; i < 3; ++i) {
-#pragma unroll
-                        for (int j = 0; j < 3; ++j) F[i][1 + j] += vs.t[i][j];
-                        F[i][4] += b.u[0] * vs.t[i][0] + b.u[1] * vs.t[i][1] + b.u[2] * vs.t[i][2] + vs.q[i];
-                    }
-                }
-                add_ai_v(b, tl, F);
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) S32[i][k] += F[i][k];
-#pragma unroll
-                for (int a = 0; a < 4; ++a)
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) T32[a][k] += N[a] * a0a[k];
-            }
-#pragma unroll
-            for (int a = 0; a < 4; ++a)
-#pragma unroll
-                for (int k = 0; k < 5; ++k)
-                    o32[a][k] = geo.WdetJ * (geo.shg[a][0] * S32[0][k] + geo.shg[a][1] * S32[1][k] +
-                                             geo.shg[a][2] * S32[2][k] + T32[a][k]);
-        }
-        // ---- element-constant flux F(y_r) (double-float) ----
-        const int r = nd[3];
-        const df64 p = df_make(syh[5 * r + 0], syl[5 * r + 0]);
-        const df64 u[3] = {df_make(syh[5 * r + 1], syl[5 * r + 1]), df_make(syh[5 * r + 2], syl[5 * r + 2]),
-                           df_make(syh[5 * r + 3], syl[5 * r + 3])};
-        const df64 T = df_make(syh[5 * r + 4], syl[5 * r + 4]);
-        const df64 rho = df_mul(p, df_mul(df_make(K.rRgas_hi, K.rRgas_lo), df_rcp(T)));
-        df64 rk = df_add(df_add(df_mul(u[0], u[0]), df_mul(u[1], u[1])), df_mul(u[2], u[2]));
-        rk.hi *= 0.5f;
-        rk.lo *= 0.5f;
-        const df64 ek = df_add(df_mul(df_make(K.cv_hi, K.cv_lo), T), rk);
-        df64 F[3][5];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            const df64 m = df_mul(rho, u[i]);
-            F[i][0] = df_neg(m);
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                F[i][1 + j] = df_neg(df_mul(m, u[j]));
-                if (i == j) F[i][1 + j] = df_sub(F[i][1 + j], p);
-            }
-            F[i][4] = df_neg(df_add(df_mul(m, ek), df_mul(u[i], p)));
-        }
-        // cofactors of the edge matrix d'[i][j] = x_j,i - x_3,i (the geometry() layout)
-        df64 d[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-                d[i][j] = df_diff(sxh[3 * nd[j] + i], sxl[3 * nd[j] + i], sxh[3 * r + i], sxl[3 * r + i]);
-        auto minor2 = [](df64 a, df64 b, df64 c2, df64 e) { return df_sub(df_mul(a, b), df_mul(c2, e)); };
-        df64 cof[3][3];
-        cof[0][0] = minor2(d[1][1], d[2][2], d[2][1], d[1][2]);
-        cof[0][1] = minor2(d[2][1], d[0][2], d[0][1], d[2][2]);
-        cof[0][2] = minor2(d[0][1], d[1][2], d[0][2], d[1][1]);
-        cof[1][0] = minor2(d[1][2], d[2][0], d[1][0], d[2][2]);
-        cof[1][1] = minor2(d[0][0], d[2][2], d[2][0], d[0][2]);
-        cof[1][2] = minor2(d[1][0], d[0][2], d[0][0], d[1][2]);
-        cof[2][0] = minor2(d[1][0], d[2][1], d[1][1], d[2][0]);
-        cof[2][1] = minor2(d[2][0], d[0][1], d[0][0], d[2][1]);
-        cof[2][2] = minor2(d[0][0], d[1][1], d[0][1], d[1][0]);
-        const df64 wq = df_make(K.wq_hi, K.wq_lo);
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int i = 0; i < 3; ++i) cof[a][i] = df_mul(cof[a][i], wq);
-        float* sl = slot + kSplitSlot * threadIdx.x;
-        df64 s3[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) s3[k] = df_make(0.f, 0.f);
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int k = 0; k < 5; ++k) {
-                const df64 g64 = df_add(df_add(df_mul(cof[a][0], F[0][k]), df_mul(cof[a][1], F[1][k])),
-                                        df_mul(cof[a][2], F[2][k]));
-                s3[k] = df_add(s3[k], g64);
-                const df64 v = df_add(g64, o32[a][k]);
-                sl[5 * a + k] = v.hi;
-                sl[20 + 5 * a + k] = v.lo;
-            }
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const df64 v = df_add(df_neg(s3[k]), o32[3][k]);  // shg_3 = -(shg_0 + shg_1 + shg_2)
-            sl[15 + k] = v.hi;
-            sl[35 + k] = v.lo;
-        }
-    }
+    if ((int)threadIdx.x < ne)
+        ress_element<WITH_Q>(ca.lien[e0 + threadIdx.x], sxh, sxl, syh, syl, sa, sq, slot + kSplitSlot * threadIdx.x,
+                             Pf, K);
     __syncthreads();
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
         df64 acc[5];
@@ -1154,6 +1163,136 @@ k_chunk_ress(ChunkArgs ca, int chunk0, const float* __restrict__ xh, const float
 #pragma unroll
         for (int k = 0; k < 5; ++k) og[k] += df_to_double(acc[k]);
     }
+}
+
+// The split outer residual over the chunks of one colour, pipelined like k_chunk_lin_pipe:
+// node ids two chunks ahead, the nodal data (hi/lo coordinates and state, FP32 ac, the
+// reconstructed flux, the residual's current FP64 values), connectivity and slot lists one
+// chunk ahead, by cp.async; arithmetic and summation order of k_chunk_ress.
+constexpr int kRessNode = 21;  // staged floats per node: x hi/lo (6), y hi/lo (10), ac (5)
+
+__host__ __device__ constexpr int ress_stage_words(int lmax, bool with_q) {
+    // FP64 product values first (8-byte aligned), then the float data, then the indices
+    return ((((10 * lmax + kRessNode * lmax + (with_q ? 12 * lmax : 0) + 1) & ~1) + 4 * kChunk + lmax + 2) + 1) & ~1;
+}
+
+template <bool WITH_Q>
+__global__ void __launch_bounds__(kChunk, PHGPU_RESS_MINB)
+k_chunk_ress_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ xh, const float* __restrict__ xlo,
+                  const float* __restrict__ yh, const float* __restrict__ ylo, const float* __restrict__ acf,
+                  double* __restrict__ out, Phys<float> Pf, DfConst K, const float* __restrict__ ql, int lmax) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sm = reinterpret_cast<float*>(smem_raw);
+    const int per = ress_stage_words(lmax, WITH_Q);
+    const int fw = 10 * lmax;                                   // floats start after the doubles
+    const int lie_off = (fw + kRessNode * lmax + (WITH_Q ? 12 * lmax : 0) + 1) & ~1;
+    int* ids = reinterpret_cast<int*>(sm + 2 * per);
+    const int idw = lin_id_words(lmax);
+    float* slot = sm + 2 * per + 3 * idw;
+    auto stage_ids = [&](int c, int ib) {
+        int* h = ids + ib * idw;
+        const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
+        if (threadIdx.x == 0) {
+            const int e0 = ca.elem[c];
+            h[0] = e0;
+            h[1] = ca.elem[c + 1] - e0;
+            h[2] = n0;
+            h[3] = nn;
+        }
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) cp_async4(h + 4 + l, ca.nodes + n0 + l);
+    };
+    auto stage_data = [&](int ib, float* b) {
+        const int* h = ids + ib * idw;
+        const int e0 = h[0], ne = h[1], n0 = h[2], nn = h[3];
+        double* so = reinterpret_cast<double*>(b);
+        float* sxh = b + fw;
+        float* sxl = sxh + 3 * lmax;
+        float* syh = sxl + 3 * lmax;
+        float* syl = syh + 5 * lmax;
+        float* sa = syl + 5 * lmax;
+        float* sq = sa + 5 * lmax;
+        float* sl = b + lie_off;
+        float* sc = sl + 2 * kChunk;
+        float* st = sc + 2 * kChunk;
+        const unsigned* csr_w = reinterpret_cast<const unsigned*>(ca.csr) + 2 * (size_t)e0;
+        for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+            const unsigned s8 = (unsigned)__cvta_generic_to_shared(sl + 2 * i);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s8), "l"(ca.lien + e0 + i) : "memory");
+        }
+        for (int w = threadIdx.x; w < 2 * ne; w += blockDim.x) cp_async4(sc + w, csr_w + w);
+        for (int l = threadIdx.x; l <= nn; l += blockDim.x) cp_async4(st + l, ca.cstart + n0 + l);
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            const size_t gn = (size_t)h[4 + l];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                cp_async4(sxh + 3 * l + d, xh + 3 * gn + d);
+                cp_async4(sxl + 3 * l + d, xlo + 3 * gn + d);
+            }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                cp_async4(syh + 5 * l + k, yh + 5 * gn + k);
+                cp_async4(syl + 5 * l + k, ylo + 5 * gn + k);
+                cp_async4(sa + 5 * l + k, acf + 5 * gn + k);
+                const unsigned s8 = (unsigned)__cvta_generic_to_shared(so + 5 * l + k);
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s8), "l"(out + 5 * gn + k) : "memory");
+            }
+            if (WITH_Q)
+                for (int k = 0; k < 12; ++k) cp_async4(sq + 12 * l + k, ql + 13 * gn + k);
+        }
+    };
+    const int cend = chunk0 + nch, G = gridDim.x;
+    int c = chunk0 + blockIdx.x;
+    if (c >= cend) return;
+    stage_ids(c, 0);
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    stage_data(0, sm);
+    if (c + G < cend) stage_ids(c + G, 1);
+    cp_async_commit();
+    for (int it = 0; c < cend; c += G, ++it) {
+        cp_async_wait<0>();
+        __syncthreads();
+        const int cn = c + G;
+        if (cn < cend) stage_data((it + 1) % 3, sm + ((it + 1) & 1) * per);
+        if (cn + G < cend) stage_ids(cn + G, (it + 2) % 3);
+        cp_async_commit();
+        const float* cur = sm + (it & 1) * per;
+        const int* h = ids + (it % 3) * idw;
+        const int e0 = h[0], ne = h[1], nn = h[3];
+        const double* so = reinterpret_cast<const double*>(cur);
+        const float* sxh = cur + fw;
+        const float* sxl = sxh + 3 * lmax;
+        const float* syh = sxl + 3 * lmax;
+        const float* syl = syh + 5 * lmax;
+        const float* sa = syl + 5 * lmax;
+        const float* sq = sa + 5 * lmax;
+        const ushort4* slie = reinterpret_cast<const ushort4*>(cur + lie_off);
+        const unsigned short* scsr = reinterpret_cast<const unsigned short*>(cur + lie_off + 2 * kChunk);
+        const int* scst = reinterpret_cast<const int*>(cur + lie_off + 4 * kChunk);
+        if ((int)threadIdx.x < ne)
+            ress_element<WITH_Q>(slie[threadIdx.x], sxh, sxl, syh, syl, sa, sq, slot + kSplitSlot * threadIdx.x, Pf,
+                                 K);
+        __syncthreads();
+        const int sbase = 4 * e0;
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            df64 acc[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) acc[k] = df_make(0.f, 0.f);
+            const int s0 = scst[l] - sbase, s1 = scst[l + 1] - sbase;
+            for (int s = s0; s < s1; ++s) {
+                const int sid = (int)scsr[s];
+                const float* sl = slot + kSplitSlot * (sid >> 2) + 5 * (sid & 3);
+#pragma unroll
+                for (int k = 0; k < 5; ++k) acc[k] = df_add(acc[k], df_make(sl[k], sl[20 + k]));
+            }
+            double* og = out + 5 * (size_t)h[4 + l];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) og[k] = so[5 * l + k] + df_to_double(acc[k]);
+        }
+        __syncthreads();
+    }
+    cp_async_wait<0>();
 }
 
 // --------------------------------------------------------------------------
@@ -2205,6 +2344,10 @@ static ChunkArgs chunk_args(const Ctx& C) {
 
 template <typename R>
 size_t res_smem(const Ctx& C) { return sizeof(R) * ((size_t)C.chunk_lmax * 13 + (size_t)kChunk * 20); }
+size_t ress_pipe_smem(const Ctx& C, bool with_q) {
+    return sizeof(float) * (2 * (size_t)ress_stage_words(C.chunk_lmax, with_q) + 3 * (size_t)lin_id_words(C.chunk_lmax) +
+                            (size_t)kChunk * kSplitSlot);
+}
 size_t lin_pipe_smem(const Ctx& C) {
     return sizeof(float) * (2 * (size_t)lin_stage_words(C.chunk_lmax) + 3 * (size_t)lin_id_words(C.chunk_lmax) +
                             (size_t)kChunk * 20);
@@ -2278,6 +2421,16 @@ int configure_element_kernels(Ctx& C) {
                                                                        lin_pipe_smem(C)),
                        "occupancy");
         C.lin_pipe_grid = std::max(1, nsm * per_sm);
+        for (int q = 0; q < 2 && rc == PHGPU_OK; ++q)
+            rc = check(C, cudaFuncSetAttribute(q ? k_chunk_ress_pipe<true> : k_chunk_ress_pipe<false>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)ress_pipe_smem(C, q == 1)),
+                       "cudaFuncSetAttribute");
+        if (rc == PHGPU_OK)
+            rc = check(C, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chunk_ress_pipe<false>, kChunk,
+                                                                       ress_pipe_smem(C, false)),
+                       "occupancy");
+        C.ress_pipe_grid = std::max(1, nsm * per_sm);
     }
     if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 8, 0>(C);
     if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 6, 1>(C);
@@ -2363,8 +2516,19 @@ void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* ac
     for (int c = 0; c < ncol; ++c) {
         const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
         if (nc <= 0) continue;
-        if (ql) k_chunk_ress<true><<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql);
-        else k_chunk_ress<false><<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql);
+        if (!C.cfg.no_pipe) {
+            const int g = std::min(nc, C.ress_pipe_grid);
+            if (ql)
+                k_chunk_ress_pipe<true><<<g, kChunk, ress_pipe_smem(C, true), C.stream>>>(
+                    ca, c0, nc, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql, C.chunk_lmax);
+            else
+                k_chunk_ress_pipe<false><<<g, kChunk, ress_pipe_smem(C, false), C.stream>>>(
+                    ca, c0, nc, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql, C.chunk_lmax);
+        } else if (ql) {
+            k_chunk_ress<true><<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql);
+        } else {
+            k_chunk_ress<false><<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql);
+        }
         ++C.launches;
     }
 }

@@ -180,6 +180,7 @@ struct Ctx {
     int* d_flag = nullptr;        // [0] converged, [1] error bits, [2] Krylov iterations of the cycle
     CycleGraph cyc;
     int lin_pipe_grid = 1;        // its CTAs per colour launch (resident slots)
+    int ress_pipe_grid = 1;       // the same for the pipelined split outer residual
     double* h_scal = nullptr;     // pinned mirror
     int* h_flag = nullptr;
 

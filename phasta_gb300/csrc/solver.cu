@@ -1549,6 +1549,13 @@ int phgpu_sweep_dev(phgpu_ctx* h, int which) {
         case 6:  // FP64-Galerkin / FP32-stabilization residual
             launch_elem_resh(C, C.d_y, C.d_ac, C.d_yf, C.d_acf, C.d_res);
             break;
+        case 16: {  // the tets' split residual with one CTA per chunk (no cp.async pipeline)
+            const int keep = C.cfg.no_pipe;
+            C.cfg.no_pipe = 1;
+            launch_elem_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res);
+            C.cfg.no_pipe = keep;
+            break;
+        }
         case 7:  // double-float constant flux + FP32 increments (needs the hi/lo split of case 8)
             launch_elem_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_res);
             if (C.nhex > 0 || C.nwedge > 0) {

@@ -306,14 +306,15 @@ def test_franca_tau_fp64(gpu_lib, make):
     assert rel(lhsK, olhsK) < 1e-12
 
 
-@pytest.mark.parametrize("n", [10, 64])
-def test_pipelined_linearized_product_is_the_per_chunk_kernel(gpu_lib, n):
-    """The persistent cp.async-pipelined FP32 linearized product (config no_pipe = 0) against
-    one CTA per chunk (no_pipe = 1): the same arithmetic and summation order, so a mixed-
-    precision time step is bitwise the same.  At 64^3 x 6 the colours hold more chunks than
-    the persistent grid, so CTAs walk several chunks through both halves of the buffer."""
-    case, p, y, ac = channel(n, ac_scale=0.05, Kspace=6)
-    p = dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR)
+@pytest.mark.parametrize("n,idiff", [(10, 0), (64, 0), (12, 1)])
+def test_pipelined_linearized_product_is_the_per_chunk_kernel(gpu_lib, n, idiff):
+    """The persistent cp.async-pipelined FP32 linearized product and split outer residual
+    (config no_pipe = 0) against one CTA per chunk (no_pipe = 1): the same arithmetic and
+    summation order, so a mixed-precision time step is bitwise the same.  At 64^3 x 6 the
+    colours hold more chunks than the persistent grid, so CTAs walk several chunks through
+    both halves of the buffers; idiff = 1 stages the reconstructed flux as well."""
+    case, p, y, ac = channel(n, ac_scale=0.05, Kspace=6, idiff=idiff)
+    p = dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR, outer_residual=L.PHGPU_RES_SPLITDF)
     out = []
     for no_pipe in (0, 1):
         g = GpuSolver(case, dict(p, no_pipe=no_pipe))
