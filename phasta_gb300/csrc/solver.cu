@@ -168,8 +168,10 @@ __global__ void k_givens(double* __restrict__ s, int K, int iKs, int minIters, i
 }
 
 // back substitution H y = e (solmfg.f:329-334)
-__global__ void k_backsolve(double* __restrict__ s, int K, int iKs) {
+// (iks_dev: the iteration count a captured cycle left on the device, read in place of iKs)
+__global__ void k_backsolve(double* __restrict__ s, int K, int iKs, const int* __restrict__ iks_dev) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (iks_dev) iKs = min(max(*iks_dev, 0), K);
     auto H = [&](int i, int j) -> double { return s[S_H + (i - 1) + (K + 1) * (j - 1)]; };
     double* eB = s + S_EB;
     double* yB = s + S_YB;
@@ -183,7 +185,8 @@ __global__ void k_backsolve(double* __restrict__ s, int K, int iKs) {
 // runs in double-float (coefficients split once per block), then one FP64 add per entry.
 template <typename V>
 __global__ void k_update_dy(double* __restrict__ Dy, const V* __restrict__ U, size_t ld, int iKs,
-                            const double* __restrict__ s, size_t n) {
+                            const double* __restrict__ s, size_t n, const int* __restrict__ iks_dev) {
+    if (iks_dev) iKs = min(max(*iks_dev, 0), kMaxK);
     const double* yB = s + S_YB;
     if constexpr (std::is_same<V, float>::value) {
         __shared__ float ch[kMaxK], cl[kMaxK];
@@ -554,7 +557,7 @@ bool cycle_graph(Ctx& C, int min_iters, bool sparse, bool ebe) {
 // ap_mode PHGPU_AP_SPARSE: the product is SparseAp + bc3per on the preconditioned tangent, and a
 // new cycle recomputes R - A Dy only when lgmres_common > 0 (SolGMRs, solgmr.f:526-537)
 template <typename V>
-int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
+int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = false) {
     // SolGMRe restarts from the true residual and stops without the minIters test (solgmr.f:130-210)
     const bool ebe = C.cfg.ap_mode == PHGPU_AP_EBE;
     const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE || ebe;
@@ -566,10 +569,12 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
     auto Uj = [&](int j) { return U + (size_t)(j - 1) * C.ldU; };  // 1-based
     double* s = C.d_scal;
     const int* done = C.d_flag;
-    // ||b||
-    dot<double>(C, C.d_res, C.d_res, n5, S_TMP0, nullptr);
-    PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "unorm"));
-    PH_TRY(sync(C));
+    // ||b|| (already read with the assembly's status when unorm_ready)
+    if (!unorm_ready) {
+        dot<double>(C, C.d_res, C.d_res, n5, S_TMP0, nullptr);
+        PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "unorm"));
+        PH_TRY(sync(C));
+    }
     double unorm = std::sqrt(C.h_scal[S_TMP0]);
     st->unorm0 = unorm;
     st->totres = unorm / (double)C.N;
@@ -645,13 +650,22 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
         if (!C.cfg.no_graph && C.cfg.ap_mode != PHGPU_AP_FD && cycle_graph<V>(C, min_iters, sparse, ebe)) {
             PH_TRY(check(C, cudaGraphLaunch(C.cyc.exec, C.stream), "cycle graph launch"));
             ++C.cyc.runs;
+            // back substitution and update with the iteration count the graph left in flag[2],
+            // then one host read of the flags and the final residual estimate
+            k_backsolve<<<1, 1, 0, C.stream>>>(s, K, 0, C.d_flag + 2);
+            k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, U, C.ldU, 0, s, n5, C.d_flag + 2);
+            C.launches += 2;
             PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 3, cudaMemcpyDeviceToHost, C.stream), "flag"));
+            PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "echeck"));
             PH_TRY(sync(C));
             iKs = C.h_flag[2];
             if (iKs < 1 || iKs > K) return fail(C, PHGPU_ERR_CUDA, "cycle graph ran no Krylov iteration");
             for (int i = 1; i <= iKs; ++i) C.launches += C.cyc.launches[i];
             st->ntotGM += iKs;
             if (C.h_flag[1]) return fail(C, PHGPU_ERR_NONFINITE, "non-finite Hessenberg entry in GMRES");
+            st->echeck = C.h_scal[S_ECHECK];
+            if (C.h_scal[S_ECHECK] <= epsnrm) break;
+            continue;
         } else {
             for (int iK = 1; iK <= K; ++iK) {
                 iKs = iK;
@@ -663,8 +677,8 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0) {
                 if (C.h_flag[0]) break;
             }
         }
-        k_backsolve<<<1, 1, 0, C.stream>>>(s, K, iKs);
-        k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, U, C.ldU, iKs, s, n5);
+        k_backsolve<<<1, 1, 0, C.stream>>>(s, K, iKs, nullptr);
+        k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, U, C.ldU, iKs, s, n5, nullptr);
         C.launches += 2;
         PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "echeck"));
         PH_TRY(sync(C));
@@ -772,15 +786,17 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
         ++C.launches;
         lu_apply<double, double>(C, C.d_bd, C.d_ypre, PHGPU_LU_PRODUCT);
     }
+    // ||L^-1 R|| for GMRES, read with the LU status and ||R|| in one host round trip
+    dot<double>(C, C.d_res, C.d_res, n5, S_TMP0, nullptr);
     PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
-    PH_TRY(check(C, cudaMemcpyAsync(C.h_scal + 8, C.d_scal + S_TMP3, sizeof(double), cudaMemcpyDeviceToHost, C.stream), "rn"));
+    PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, C.d_scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "rn"));
     PH_TRY(sync(C));
-    st->rnorm = std::sqrt(C.h_scal[8]);
+    st->rnorm = std::sqrt(C.h_scal[S_TMP3]);
     if (C.h_flag[1]) return fail(C, PHGPU_ERR_SINGULAR, "zero or non-finite pivot in the block-diagonal LU");
     cudaEventRecord(C.ev[1], C.stream);
     int rc;
-    if (C.cfg.precision == PHGPU_FP64) rc = gmres<double>(C, st, lgmres_common);
-    else rc = gmres<float>(C, st, lgmres_common);
+    if (C.cfg.precision == PHGPU_FP64) rc = gmres<double>(C, st, lgmres_common, true);
+    else rc = gmres<float>(C, st, lgmres_common, true);
     if (rc != PHGPU_OK) return rc;
     lu_apply<double, double>(C, C.d_bd, C.d_Dy, PHGPU_LU_BACKWARD);
     cudaEventRecord(C.ev[2], C.stream);
