@@ -1552,6 +1552,16 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
     constexpr bool single = kFullSub * full_nsub<R>() >= kChunk;
     R* acc = sq + (with_q ? 12 * nn : 0);         // nn x 35 (multi-round only)
     R* slot = acc + (single ? 0 : kFullOut * nn); // (kChunk * nsub) x 35
+    // the connectivity of this thread's tet in each sub-batch of the first round, and its
+    // node's slot-list bounds, loaded before the staging so that their latency overlaps it
+    ushort4 lnp[4];
+#pragma unroll
+    for (int sb = 0; sb < 4; ++sb) {
+        const int el = min(sb * kFullSub + (int)(threadIdx.x >> 2), ne - 1);
+        if (sb < full_nsub<R>()) lnp[sb] = ca.lien[e0 + el];
+    }
+    const int cs_own0 = (int)threadIdx.x < nn ? ca.cstart[n0 + threadIdx.x] : 0;
+    const int cs_own1 = (int)threadIdx.x < nn ? ca.cstart[n0 + threadIdx.x + 1] : 0;
     for (int l = threadIdx.x; l < nn; l += blockDim.x) {
         const int gn = ca.nodes[n0 + l];
 #pragma unroll
@@ -1576,7 +1586,8 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
             const int el_raw = b0 + sb * kFullSub + (threadIdx.x >> 2), a = threadIdx.x & 3;
             const bool valid = el_raw < ne;
             const int el = valid ? el_raw : ne - 1;  // every lane takes part in the shuffles
-            const ushort4 ln = ca.lien[e0 + el];
+            const ushort4 ln = b0 > 0 ? ca.lien[e0 + el]
+                               : sb == 0 ? lnp[0] : sb == 1 ? lnp[1] : sb == 2 ? lnp[2] : lnp[3];
             const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
             R xl[4][3], yl[4][5], al[4][5];
 #pragma unroll
@@ -1610,7 +1621,8 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
         if (kFullSub * nsub >= kChunk) {
             // single round: sum the slots straight into the global arrays
             for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-                const int s0 = ca.cstart[n0 + l], s1 = ca.cstart[n0 + l + 1];
+                const bool own = l == (int)threadIdx.x;
+                const int s0 = own ? cs_own0 : ca.cstart[n0 + l], s1 = own ? cs_own1 : ca.cstart[n0 + l + 1];
                 R t[kFullOut];
 #pragma unroll
                 for (int k = 0; k < kFullOut; ++k) t[k] = R(0);
