@@ -268,10 +268,11 @@ def _time_sweep(g, stream, which, reps=10):
 #   full: FP32 block diagonal (BDiag-only variant), reads y, x (f32), writes BDiag (25 f32)
 #   lin:  FP32 linearized product, reads the direction, base state, x (f32), reads and writes the product
 SWEEPS = {
-    "ress": (7, "k_chunk_ress (double-float constant flux + FP32 increment residual)",
+    "ress": (7, "k_chunk_ress_pipe (double-float constant flux + FP32 increment residual, cp.async-pipelined)",
              lambda E, N: 16 * E + N * (40 + 40 + 24 + 40)),
     "full": (3, "k_chunk_full<float, true> (FP32 block diagonal)", lambda E, N: 16 * E + N * (20 + 12 + 100)),
-    "lin": (2, "k_chunk_res<float, RM_LIN> (FP32 linearized Ap sweep)", lambda E, N: 16 * E + N * (20 + 20 + 12 + 40)),
+    "lin": (2, "k_chunk_lin_pipe (FP32 linearized Ap sweep, cp.async-pipelined)",
+            lambda E, N: 16 * E + N * (20 + 20 + 12 + 40)),
 }
 
 
