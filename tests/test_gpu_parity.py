@@ -323,3 +323,26 @@ def test_pipelined_linearized_product_is_the_per_chunk_kernel(gpu_lib, n, idiff)
         g.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
     assert out[0][2] == out[1][2]
+
+
+def test_time_step_on_pinned_host_buffers(gpu_lib):
+    """The host-buffer time step on page-locked arrays (the e2e path of the bench) is bitwise
+    the one on pageable arrays."""
+    torch = pytest.importorskip("torch")
+    case, p, y, ac = channel(8, ac_scale=0.05, Kspace=10)
+    g = GpuSolver(case, p)
+    yo1, ao1, y1, a1, _st = g.time_step(y, ac, nitr=2)
+    g.close()
+
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        t.numpy()[:] = a.reshape(-1)
+        return t, t.numpy()
+
+    keep = [pinned(y), pinned(ac), pinned(np.zeros_like(y)), pinned(np.zeros_like(ac))]
+    yo, ao, y2, a2 = (k[1] for k in keep)
+    g2 = GpuSolver(case, p)
+    g2.time_step_into(yo, ao, y2, a2, nitr=2)
+    g2.close()
+    assert np.array_equal(y2, y1.reshape(-1)) and np.array_equal(a2, a1.reshape(-1))
+    assert np.array_equal(yo, yo1.reshape(-1)) and np.array_equal(ao, ao1.reshape(-1))
