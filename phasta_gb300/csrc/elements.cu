@@ -36,6 +36,9 @@
 #ifndef PHGPU_RESS_MINB
 #define PHGPU_RESS_MINB 3
 #endif
+#ifndef PHGPU_LINPIPE_MINB
+#define PHGPU_LINPIPE_MINB 4
+#endif
 #ifndef PHGPU_RES_QUNROLL
 #define PHGPU_RES_QUNROLL 1
 #endif
@@ -480,7 +483,7 @@ __host__ __device__ constexpr int lin_stage_words(int lmax) {
 // words of one node-id stage: e0, ne, n0, nn, then the chunk's global node ids
 __host__ __device__ constexpr int lin_id_words(int lmax) { return 4 + lmax; }
 
-__global__ void __launch_bounds__(kChunk, PHGPU_RES32_MINB)
+__global__ void __launch_bounds__(kChunk, PHGPU_LINPIPE_MINB)
 k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x, const float* __restrict__ ya,
                  const float* __restrict__ yb, float* __restrict__ out, Phys<float> P, int lmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
