@@ -8,7 +8,8 @@ module phgpu_iface
   integer(c_int), parameter :: PHGPU_OK = 0
   integer(c_int), parameter :: PHGPU_FP64 = 0, PHGPU_MIXED = 1
   integer(c_int), parameter :: PHGPU_AP_FD = 0, PHGPU_AP_LINEAR = 1, PHGPU_AP_SPARSE = 2, PHGPU_AP_EBE = 3
-  integer(c_int), parameter :: PHGPU_RES_FP64 = 0, PHGPU_RES_GALERKIN64 = 1
+  integer(c_int), parameter :: PHGPU_RES_FP64 = 0, PHGPU_RES_GALERKIN64 = 1, PHGPU_RES_SPLITDF = 2
+  integer(c_int), parameter :: PHGPU_PRECOND_BDIAG = 0, PHGPU_PRECOND_LEARNED = 1
 
   type, bind(C) :: phgpu_config
      real(c_double) :: Rgas, gamma, gamma1, pr, rmu
@@ -20,7 +21,7 @@ module phgpu_iface
      integer(c_int) :: iter, istep
      integer(c_int) :: precision, ap_mode, outer_residual
      integer(c_int) :: idiff         ! 0 or 1 (global diffusive-flux reconstruction)
-     integer(c_int) :: no_graph, iDC, no_pipe, reserved(1)
+     integer(c_int) :: no_graph, iDC, no_pipe, precond
   end type
 
   type, bind(C) :: phgpu_mesh
@@ -37,6 +38,7 @@ module phgpu_iface
   type, bind(C) :: phgpu_stats
      integer(c_int) :: iKs, lGMRES, ntotGM, status
      real(c_double) :: unorm0, echeck, eGMRES, totres, rnorm, t_assembly_ms, t_gmres_ms
+     integer(c_int) :: net_its, net_fallback
   end type
 
   interface

@@ -102,8 +102,13 @@ typedef struct {
     int no_pipe;                     /* 0: the FP32 linearized product runs as a persistent kernel
                                         that stages the next mesh chunk with cp.async while it
                                         computes the current one; 1: one CTA per chunk */
-    int reserved[1];
+    int precond;                     /* PHGPU_PRECOND_BDIAG: the reference's block-diagonal LU
+                                        (i3lu.f); PHGPU_PRECOND_LEARNED: in addition the learned
+                                        network as the right preconditioner of flexible GMRES
+                                        (mixed precision, linearized product; see phgpu_net_*) */
 } phgpu_config;
+
+enum { PHGPU_PRECOND_BDIAG = 0, PHGPU_PRECOND_LEARNED = 1 };
 
 /* Mesh and boundary-condition arrays (what the reference keeps in
  * pointer_data mien/mienb/miBCB/mBCB and in iBC/BC/iper). */
@@ -137,7 +142,20 @@ typedef struct {
     double totres;        /* rstat measure: sqrt(sum res^2)/nshg of L^-1 R */
     double rnorm;         /* unpreconditioned FP64 ||R|| after BCs (nonlinear residual) */
     double t_assembly_ms, t_gmres_ms; /* device time of the phases, if timing is on */
+    int net_its;          /* Krylov iterations of the learned flexible-GMRES cycle (0: none ran) */
+    int net_fallback;     /* PHGPU_NET_*: how the solve used the learned preconditioner */
 } phgpu_stats;
+
+/* phgpu_stats.net_fallback */
+enum {
+    PHGPU_NET_USED = 0,      /* the learned cycle converged with fewer iterations than the last
+                                block-diagonal solve */
+    PHGPU_NET_FELL_BACK = 1, /* it did not (or produced a non-finite value): block-diagonal GMRES
+                                cycles finished the solve from where it stopped */
+    PHGPU_NET_PLAIN = 2      /* block-diagonal GMRES only: precond = BDIAG, no weights, the
+                                reference count of a first solve, or the network switched off
+                                after two failures in a row */
+};
 
 typedef struct phgpu_ctx phgpu_ctx;
 
@@ -153,6 +171,10 @@ long long phgpu_kernel_launches(phgpu_ctx* ctx); /* kernels launched since creat
 /* GMRES cycles run as one CUDA graph since create (config no_graph = 0), or -1 when the
  * graph could not be built (phgpu_last_error then gives the reason; cycles run kernel by kernel) */
 long long phgpu_graph_cycles(phgpu_ctx* ctx);
+
+/* new values BC(nshg, 6) of the Dirichlet constraints (the iBC bits of phgpu_create stay): the
+ * reference passes BC to every ElmMFG/SolMFG call (elmmfg.f:1-5, solmfg.f:1-7) */
+int phgpu_set_bc(phgpu_ctx* ctx, const double* BC);
 
 /* ElmMFG: res, rmes, BDiag (BDiag only when iprec != 0) */
 int phgpu_elmmfg(phgpu_ctx* ctx, const double* y, const double* ac,
@@ -240,6 +262,61 @@ int phgpu_residual_norm_dev(phgpu_ctx* ctx, double* rnorm);
  * element tangents stored per element, 14 FP32 element-by-element product (13-14: mixed
  * precision context, one element topology) */
 int phgpu_sweep_dev(phgpu_ctx* ctx, int which);
+
+/* ---- learned preconditioner (no counterpart in the reference) --------------------------
+ * A message-passing network over the mesh edges maps a Krylov vector v of the block-diagonal
+ * preconditioned operator L^-1 J U^-1 (the operator SolMFG's loop multiplies by, au1mfg.f:57-83)
+ * to z = P(v) ~ (L^-1 J U^-1)^-1 v; with precond = PHGPU_PRECOND_LEARNED the GMRES cycle of
+ * solmfg.f:221-340 becomes flexible GMRES whose Krylov iteration j multiplies z_j = P(v_j) and
+ * whose solution is sum_j y_j z_j.  The block-diagonal GMRES of the reference is the fallback:
+ * the first solve of a context runs it to set the reference iteration count; later solves cap
+ * the learned cycle one iteration below that count and, when it does not converge (or is not
+ * finite), finish with block-diagonal cycles from where it stopped; two failures in a row switch
+ * the network off until new weights are set.  The network: encoder 48 -> 64, three edge
+ * message-passing layers (hidden width 64), decoder 64 -> 5; BF16 GEMM operands with FP32
+ * accumulation on the tensor cores, FP32 master weights.  Input per node: the direction (5), the
+ * node's factored BDiag block (25, over their RMS), its state (5) and an active flag.
+ * Weights are one FP32 array of PHGPU_NET_NPARAM values in this order (row-major matrices):
+ *   W_e[64][48] b_e[64], then per layer l = 0..2: W_p[64][64] W_q[64][64] b_m[64] C[64][3]
+ *   W_u[64][128] b_u[64], then W_d[5][64] b_d[5] alpha[5] beta[5]
+ * (alpha, beta: per-dof input and output scales, set from the training pairs).
+ * Host vectors v, t, z use the layout of res (nshg, 5). */
+#define PHGPU_NET_NPARAM 53583
+#define PHGPU_NET_NTRAIN 53573   /* trained values: all but alpha and beta */
+typedef struct {
+    int epochs;                      /* passes over the collected pairs */
+    int npairs;                      /* pairs used (<= collected; 0: all) */
+    float lr, beta1, beta2, eps;     /* Adam */
+    float clip;                      /* global gradient-norm clip (0: none) */
+    unsigned seed;                   /* pair order of each epoch */
+    int renormalize;                 /* 1: set alpha and beta from the pairs first */
+} phgpu_net_train_config;
+typedef struct {
+    double loss_first, loss_last;    /* mean loss of the first and of the last epoch */
+    double ms;                       /* device time of the training */
+    long long steps;
+} phgpu_net_train_stats;
+/* weights (copied); resets the fallback state */
+int phgpu_net_set_weights(phgpu_ctx* ctx, const float* w, int n);
+int phgpu_net_get_weights(phgpu_ctx* ctx, float* w, int n);
+/* the edge graph: nstart (nshg+1), nbr (room for cap; 26-bit neighbour | shift code << 26,
+ * code bits 2d..2d+1 = 1: +L_d, 2: -L_d), geo = {L_x, L_y, L_z, 1/hbar}; *nnz = edges */
+int phgpu_net_graph(phgpu_ctx* ctx, int* nstart, unsigned* nbr, long long cap, long long* nnz, float* geo);
+/* context features of the resident state and FP32 factored BDiag (after a mixed-precision
+ * solve): out (nshg, 32) as floats, may be NULL (computes them only) */
+int phgpu_net_features(phgpu_ctx* ctx, float* out);
+/* z = P(v) with the current features; hidden (4 x nshg x 64: h0..h3) and out (nshg x 8,
+ * decoder outputs) may be NULL */
+int phgpu_net_apply(phgpu_ctx* ctx, const double* v, double* z, float* hidden, float* out);
+/* training loss and gradient (PHGPU_NET_NPARAM floats, alpha/beta entries 0) of one pair */
+int phgpu_net_loss_grad(phgpu_ctx* ctx, const double* v, const double* t, double* loss, float* grad);
+/* training pairs: room for cap pairs (frees the old set) */
+int phgpu_net_pairs(phgpu_ctx* ctx, int cap);
+/* after a mixed-precision block-diagonal solve (phgpu_solmfg): store pair `slot` from its
+ * solution w = U Dy: v = A~ w / ||A~ w||, t = w / ||A~ w||, and the current features */
+int phgpu_net_collect(phgpu_ctx* ctx, int slot);
+/* Adam over the collected pairs, one pair per step, on the GPU */
+int phgpu_net_train(phgpu_ctx* ctx, const phgpu_net_train_config* cfg, phgpu_net_train_stats* out);
 
 /* Largest 5*nshg that phgpu_rstat_noalloc accepts (33,554,432 values, nshg <= 6,710,886). */
 #define PHGPU_RSTAT_NOALLOC_MAX_N 33554432

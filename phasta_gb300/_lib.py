@@ -21,10 +21,14 @@ PHGPU_RES_FP64, PHGPU_RES_GALERKIN64, PHGPU_RES_SPLITDF = 0, 1, 2
 PHGPU_ERR_INVALID, PHGPU_ERR_UNSUPPORTED, PHGPU_ERR_TOO_LARGE = 1, 5, 7
 PHGPU_ERR_IO, PHGPU_ERR_NOTFOUND = 8, 9
 PHGPU_RSTAT_NOALLOC_MAX_N = 33554432
+PHGPU_PRECOND_BDIAG, PHGPU_PRECOND_LEARNED = 0, 1
+PHGPU_NET_USED, PHGPU_NET_FELL_BACK, PHGPU_NET_PLAIN = 0, 1, 2
+PHGPU_NET_NPARAM, PHGPU_NET_NTRAIN = 53583, 53573
 LU_FACT, LU_FORWARD, LU_BACKWARD, LU_PRODUCT = 0, 1, 2, 3
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
+_fp = C.POINTER(C.c_float)
 
 
 class Config(C.Structure):
@@ -39,7 +43,7 @@ class Config(C.Structure):
         ("etol", C.c_double), ("epsM", C.c_double), ("eGMRES", C.c_double),
         ("iter", C.c_int), ("istep", C.c_int),
         ("precision", C.c_int), ("ap_mode", C.c_int), ("outer_residual", C.c_int), ("idiff", C.c_int),
-        ("no_graph", C.c_int), ("iDC", C.c_int), ("no_pipe", C.c_int), ("reserved", C.c_int * 1),
+        ("no_graph", C.c_int), ("iDC", C.c_int), ("no_pipe", C.c_int), ("precond", C.c_int),
     ]
 
 
@@ -66,7 +70,19 @@ class Stats(C.Structure):
         ("iKs", C.c_int), ("lGMRES", C.c_int), ("ntotGM", C.c_int), ("status", C.c_int),
         ("unorm0", C.c_double), ("echeck", C.c_double), ("eGMRES", C.c_double), ("totres", C.c_double),
         ("rnorm", C.c_double), ("t_assembly_ms", C.c_double), ("t_gmres_ms", C.c_double),
+        ("net_its", C.c_int), ("net_fallback", C.c_int),
     ]
+
+
+class NetTrainConfig(C.Structure):
+    _fields_ = [("epochs", C.c_int), ("npairs", C.c_int), ("lr", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("eps", C.c_float), ("clip", C.c_float), ("seed", C.c_uint),
+                ("renormalize", C.c_int)]
+
+
+class NetTrainStats(C.Structure):
+    _fields_ = [("loss_first", C.c_double), ("loss_last", C.c_double), ("ms", C.c_double),
+                ("steps", C.c_longlong)]
 
 
 _lib = None
@@ -116,6 +132,16 @@ def lib():
         "phgpu_i3pre": ([vp, _dp, _dp], C.c_int),
         "phgpu_au1gmr": ([vp, _dp, _dp], C.c_int),
         "phgpu_solgmre": ([vp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(Stats)], C.c_int),
+        "phgpu_set_bc": ([vp, _dp], C.c_int),
+        "phgpu_net_set_weights": ([vp, _fp, C.c_int], C.c_int),
+        "phgpu_net_get_weights": ([vp, _fp, C.c_int], C.c_int),
+        "phgpu_net_graph": ([vp, _ip, C.POINTER(C.c_uint), C.c_longlong, C.POINTER(C.c_longlong), _fp], C.c_int),
+        "phgpu_net_features": ([vp, _fp], C.c_int),
+        "phgpu_net_apply": ([vp, _dp, _dp, _fp, _fp], C.c_int),
+        "phgpu_net_loss_grad": ([vp, _dp, _dp, _dp, _fp], C.c_int),
+        "phgpu_net_pairs": ([vp, C.c_int], C.c_int),
+        "phgpu_net_collect": ([vp, C.c_int], C.c_int),
+        "phgpu_net_train": ([vp, C.POINTER(NetTrainConfig), C.POINTER(NetTrainStats)], C.c_int),
         # include/phgpu_io.h
         "phgpu_io_openfile": ([C.c_char_p, C.c_char_p, _ip], C.c_int),
         "phgpu_io_closefile": ([C.c_int, C.c_char_p], C.c_int),
@@ -161,6 +187,13 @@ def dptr(a: np.ndarray | None):
         return None
     assert a.dtype == np.float64 and a.flags.c_contiguous, "expected a contiguous float64 array"
     return a.ctypes.data_as(_dp)
+
+
+def fptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous, "expected a contiguous float32 array"
+    return a.ctypes.data_as(_fp)
 
 
 def iptr(a: np.ndarray | None):

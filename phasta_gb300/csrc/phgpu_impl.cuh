@@ -7,6 +7,7 @@
 //                  of one colour share a stored node, so scatters are plain
 //                  read-modify-writes, deterministic and atomic-free)
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <string>
@@ -104,6 +105,60 @@ struct CycleGraph {
     std::string why;
 };
 
+// The learned right preconditioner of flexible GMRES (learn.cu): the mesh-edge graph of the
+// message-passing network, its weights, per-solve context features, activation buffers,
+// the preconditioned Krylov basis Z, the training set and the fallback state.
+struct NetTrain {
+    int cap = 0, npairs = 0;              // training pairs allocated / collected
+    float* d_pv = nullptr;                // cap x 5N: input directions v (unit norm)
+    float* d_pt = nullptr;                // cap x 5N: targets t
+    __nv_bfloat16* d_pctx = nullptr;      // cap x 32N: context features of each pair
+    // activations kept by the training forward for the backward
+    __nv_bfloat16* d_hs = nullptr;        // 4 x 64N: h0..h3
+    __nv_bfloat16* d_ps = nullptr;        // 3 x 64N: P of each layer
+    __nv_bfloat16* d_as = nullptr;        // 3 x 64N: aggregated messages
+    float* d_qs = nullptr;                // 3 x 64N: Q of each layer
+    float* d_us = nullptr;                // 3 x 64N: update pre-activations
+    float* d_out = nullptr;               // 8N: decoder outputs
+    float* d_dh = nullptr;                // 64N: gradient of the hidden state
+    float* d_dms = nullptr;               // 64N: gradient of the mean message
+    __nv_bfloat16* d_dqp = nullptr;       // 128N: gradients of Q and P (bf16 GEMM operands)
+    float* d_part = nullptr;              // grid x (NPARAM + 1) per-CTA partial gradients and loss
+    float* d_grad = nullptr;              // NPARAM
+    float* d_m = nullptr;                 // Adam moments
+    float* d_v = nullptr;
+    double* d_scal = nullptr;             // [0] grad norm^2, [1..] per-step losses
+    int scal_cap = 0;
+    int grid = 0;                         // CTAs of the training kernels
+    long long step = 0;                   // Adam steps taken
+};
+struct NetCtx {
+    bool graph = false;
+    long long nnz = 0;
+    int* d_nstart = nullptr;              // N+1 CSR row starts
+    unsigned* d_nbr = nullptr;            // neighbour | periodic shift code << 26
+    unsigned char* d_act = nullptr;       // 1: node the network corrects
+    int nact = 0;
+    float L[3] = {0.f, 0.f, 0.f};         // periods of the translational periodicity
+    float rh = 1.f;                       // 1 / mean edge length
+    double hbar = 1.0;
+    float* d_w = nullptr;                 // FP32 master weights (NPARAM)
+    bool have_w = false;
+    __nv_bfloat16* d_ctx = nullptr;       // 32N context features of the current solve
+    float* d_stat = nullptr;              // normalisation of the context features
+    double* d_spart = nullptr;            // their partial sums
+    __nv_bfloat16* d_h = nullptr;         // 64N hidden state (inference, updated in place)
+    __nv_bfloat16* d_P0 = nullptr;        // 64N message projections (ping-pong)
+    __nv_bfloat16* d_P1 = nullptr;
+    float* d_Z = nullptr;                 // Kspace x ldU preconditioned Krylov vectors
+    int grid_enc = 1, grid_mp = 1;        // persistent grids of the inference kernels
+    // fallback: Krylov iterations of the last block-diagonal solve (-1: none yet), consecutive
+    // learned cycles that did not converge within fewer iterations, and the switch they throw
+    int its_ref = -1, fails = 0;
+    bool disabled = false;
+    NetTrain tr;
+};
+
 struct Ctx {
     int N = 0, E = 0, Eb = 0;
     phgpu_config cfg{};
@@ -179,6 +234,8 @@ struct Ctx {
     unsigned int* d_count = nullptr;
     int* d_flag = nullptr;        // [0] converged, [1] error bits, [2] Krylov iterations of the cycle
     CycleGraph cyc;
+    CycleGraph cyc_net;           // the learned preconditioner's flexible GMRES cycle
+    NetCtx net;
     int lin_pipe_grid = 1;        // its CTAs per colour launch (resident slots)
     int ress_pipe_grid = 1;       // the same for the pipelined split outer residual
     double* h_scal = nullptr;     // pinned mirror
@@ -287,5 +344,19 @@ template <typename M, typename V> void sparse_ap(Ctx& C, const M* lhsK, const V*
 int colour(Ctx& C, int n_nodes, const int* ien, int nen, int ne, std::vector<int>& order, std::vector<int>& start);
 
 int check(Ctx& C, cudaError_t e, const char* what);
+int fail(Ctx& C, int code, const std::string& msg);
+
+// ---- learned preconditioner (learn.cu) ----
+int net_setup(Ctx& C);                      // graph, buffers and the Z basis (first use)
+int net_prepare(Ctx& C);                    // context features of the current state and FP32 LU factors
+void net_apply(Ctx& C, const float* v, float* z);   // z = P(v), four kernels, graph-capturable
+void net_free(Ctx& C);
+// training pair `slot`: v = Aw / ||Aw||, t = w / ||Aw|| (||Aw||^2 at nrm2 on the device), current features
+int net_store_pair(Ctx& C, int slot, const float* Aw, const float* w, const double* nrm2);
+bool net_usable(const Ctx& C);              // graph and weights present
 
 }  // namespace phgpu
+
+struct phgpu_ctx {
+    phgpu::Ctx c;
+};

@@ -21,6 +21,11 @@ int check(Ctx& C, cudaError_t e, const char* what) {
     return PHGPU_ERR_CUDA;
 }
 
+int fail(Ctx& C, int code, const std::string& msg) {
+    C.err = msg;
+    return code;
+}
+
 namespace {
 
 #define PH_TRY(x)                          \
@@ -28,11 +33,6 @@ namespace {
         int _s = (x);                      \
         if (_s != PHGPU_OK) return _s;     \
     } while (0)
-
-int fail(Ctx& C, int code, const std::string& msg) {
-    C.err = msg;
-    return code;
-}
 
 template <typename T>
 int dalloc(Ctx& C, T** p, size_t n) {
@@ -136,7 +136,7 @@ __global__ void k_axpby(const double* __restrict__ a, double alpha, const double
 // Inside a captured cycle (open_next) it opens the next iteration's conditional node
 // unless the cycle has converged or failed.
 __global__ void k_givens(double* __restrict__ s, int K, int iKs, int minIters, int* __restrict__ flag,
-                         cudaGraphConditionalHandle next, int open_next) {
+                         cudaGraphConditionalHandle next, int open_next, int capped) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     if (flag[0]) return;
     auto H = [&](int i, int j) -> double& { return s[S_H + (i - 1) + (K + 1) * (j - 1)]; };
@@ -164,7 +164,10 @@ __global__ void k_givens(double* __restrict__ s, int K, int iKs, int minIters, i
     if (!(echeck == echeck)) flag[1] |= 2;
     if (echeck <= s[S_EPSNRM] && iKs >= minIters) flag[0] = 1;
     flag[2] = iKs;
-    if (open_next) cudaGraphSetConditional(next, (flag[0] | flag[1]) ? 0u : 1u);
+    // capped: a learned flexible-GMRES cycle stops at flag[3] iterations (then block-diagonal
+    // cycles take over)
+    const bool stop = (flag[0] | flag[1]) || (capped && iKs >= flag[3]);
+    if (open_next) cudaGraphSetConditional(next, stop ? 0u : 1u);
 }
 
 // back substitution H y = e (solmfg.f:329-334)
@@ -184,9 +187,9 @@ __global__ void k_backsolve(double* __restrict__ s, int K, int iKs, const int* _
 // Dy = Dy + sum_j yBrg(j) u_j (solmfg.f:338-340).  FP32 Krylov vectors: the sum over j
 // runs in double-float (coefficients split once per block), then one FP64 add per entry.
 template <typename V>
-__global__ void k_update_dy(double* __restrict__ Dy, const V* __restrict__ U, size_t ld, int iKs,
+__global__ void k_update_dy(double* __restrict__ Dy, const V* __restrict__ U, size_t ld, int iKs, int K,
                             const double* __restrict__ s, size_t n, const int* __restrict__ iks_dev) {
-    if (iks_dev) iKs = min(max(*iks_dev, 0), kMaxK);
+    if (iks_dev) iKs = min(max(*iks_dev, 0), K);
     const double* yB = s + S_YB;
     if constexpr (std::is_same<V, float>::value) {
         __shared__ float ch[kMaxK], cl[kMaxK];
@@ -209,7 +212,7 @@ __global__ void k_update_dy(double* __restrict__ Dy, const V* __restrict__ U, si
     }
 }
 
-__global__ void k_init_cycle(double* __restrict__ s, int K, double unorm, double epsnrm, int* flag) {
+__global__ void k_init_cycle(double* __restrict__ s, int K, double unorm, double epsnrm, int* flag, int cap) {
     const int t = threadIdx.x;
     for (int i = t; i < K + 1; i += blockDim.x) s[S_EB + i] = 0.0;
     for (int i = t; i < (K + 1) * K; i += blockDim.x) s[S_H + i] = 0.0;
@@ -220,6 +223,7 @@ __global__ void k_init_cycle(double* __restrict__ s, int K, double unorm, double
         s[S_ECHECK] = 0.0;
         flag[0] = 0;
         flag[2] = 0;
+        flag[3] = cap;
     }
 }
 
@@ -448,14 +452,23 @@ void assembled_ap(Ctx& C, bool ebe, const V* p, V* q) {
 // Gram-Schmidt against u_1..u_iK, the new vector's norm and the Givens update
 template <typename V>
 int krylov_step(Ctx& C, int iK, int min_iters, bool sparse, bool ebe, cudaGraphConditionalHandle next,
-                int open_next) {
+                int open_next, bool learned = false) {
     const size_t n5 = 5 * (size_t)C.N;
     const int K = C.cfg.Kspace;
     V* U = (V*)C.d_U;
     auto Uj = [&](int j) { return U + (size_t)(j - 1) * C.ldU; };  // 1-based
     double* s = C.d_scal;
     V* w = Uj(iK + 1);
-    if (sparse) {
+    if constexpr (std::is_same<V, float>::value) {
+        if (learned) {
+            // flexible GMRES: z_iK = P(u_iK) kept for the solution, w = A~ z_iK
+            float* z = C.net.d_Z + (size_t)(iK - 1) * C.ldU;
+            net_apply(C, Uj(iK), z);
+            PH_TRY(ap_lin<V>(C, z, w, nullptr));
+        }
+    }
+    if (learned) {
+    } else if (sparse) {
         assembled_ap<V>(C, ebe, Uj(iK), w);
     } else if constexpr (std::is_same<V, double>::value) {
         if (C.cfg.ap_mode == PHGPU_AP_FD) {
@@ -476,18 +489,22 @@ int krylov_step(Ctx& C, int iK, int min_iters, bool sparse, bool ebe, cudaGraphC
         mgs_step<V>(C, w, up, bprev, Uj(jK), n5, Hcol + (jK - 1), nullptr);
     }
     scale_by<V>(C, w, Hcol + iK, 1, n5, nullptr);
-    k_givens<<<1, 1, 0, C.stream>>>(s, K, iK, min_iters, C.d_flag, next, open_next);
+    k_givens<<<1, 1, 0, C.stream>>>(s, K, iK, min_iters, C.d_flag, next, open_next, learned ? 1 : 0);
     ++C.launches;
     return check(C, cudaGetLastError(), "krylov step");
 }
 
 }  // namespace
 
+void cycle_graph_free(CycleGraph& G) {
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    if (G.graph) cudaGraphDestroy(G.graph);
+    G.exec = nullptr;
+    G.graph = nullptr;
+}
 void cycle_graph_free(Ctx& C) {
-    if (C.cyc.exec) cudaGraphExecDestroy(C.cyc.exec);
-    if (C.cyc.graph) cudaGraphDestroy(C.cyc.graph);
-    C.cyc.exec = nullptr;
-    C.cyc.graph = nullptr;
+    cycle_graph_free(C.cyc);
+    cycle_graph_free(C.cyc_net);
 }
 
 namespace {
@@ -495,8 +512,8 @@ namespace {
 // Capture the Krylov iterations of a cycle as a graph of conditional nodes (or reuse the
 // last one): false when it cannot be built, and cycles are then launched kernel by kernel
 template <typename V>
-bool cycle_graph(Ctx& C, int min_iters, bool sparse, bool ebe) {
-    CycleGraph& G = C.cyc;
+bool cycle_graph(Ctx& C, int min_iters, bool sparse, bool ebe, bool learned = false) {
+    CycleGraph& G = learned ? C.cyc_net : C.cyc;
     if (G.disabled) return false;
     phgpu_config key = C.cfg;  // the fields the captured kernels do not read
     key.iter = 0;
@@ -506,7 +523,7 @@ bool cycle_graph(Ctx& C, int min_iters, bool sparse, bool ebe) {
     if (G.exec && G.vsize == (int)sizeof(V) && G.min_iters == min_iters && G.lhs == lhs &&
         std::memcmp(&G.key, &key, sizeof key) == 0)
         return true;
-    phgpu::cycle_graph_free(C);
+    phgpu::cycle_graph_free(G);
     const int K = C.cfg.Kspace;
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaGraphCreate(&g, 0);
@@ -529,7 +546,7 @@ bool cycle_graph(Ctx& C, int min_iters, bool sparse, bool ebe) {
         e = cudaStreamBeginCaptureToGraph(C.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
         if (e != cudaSuccess) break;
         const long long li = C.launches;
-        const int rc = krylov_step<V>(C, i, min_iters, sparse, ebe, h[i + 1], i < K ? 1 : 0);
+        const int rc = krylov_step<V>(C, i, min_iters, sparse, ebe, h[i + 1], i < K ? 1 : 0, learned);
         cudaGraph_t captured = nullptr;
         const cudaError_t e2 = cudaStreamEndCapture(C.stream, &captured);
         G.launches[i] = C.launches - li;
@@ -542,7 +559,7 @@ bool cycle_graph(Ctx& C, int min_iters, bool sparse, bool ebe) {
     if (e != cudaSuccess) {
         G.why = std::string("cycle graph: ") + cudaGetErrorString(e);
         (void)cudaGetLastError();
-        cycle_graph_free(C);
+        cycle_graph_free(G);
         G.disabled = true;
         return false;
     }
@@ -581,6 +598,8 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
     fill0(C, C.d_Dy, sizeof(double) * n5);
     st->iKs = 0;
     st->lGMRES = 0;
+    st->net_its = 0;
+    st->net_fallback = PHGPU_NET_PLAIN;
     if (!std::isfinite(unorm)) return fail(C, PHGPU_ERR_NONFINITE, "non-finite residual (tnanq)");
     if (unorm < 100. * C.cfg.epsM * C.cfg.epsM) return PHGPU_OK;
     const double epsnrm = C.cfg.etol * unorm;
@@ -592,8 +611,23 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
     } else {
         to_f32(C, C.d_res, Uj(1), n5);
     }
+    // learned preconditioner: the first cycle is flexible GMRES with the network, capped one
+    // iteration below the last block-diagonal solve; if it does not converge, nGMRES
+    // block-diagonal cycles continue from its solution
+    const bool want_net = std::is_same<V, float>::value && C.cfg.precond == PHGPU_PRECOND_LEARNED && !sparse;
+    bool use_net = false;
+    int cap = K;
+    if (want_net && net_usable(C) && !C.net.disabled && C.net.its_ref >= 2) {
+        use_net = true;
+        cap = std::min(K, C.net.its_ref - 1);
+        PH_TRY(net_prepare(C));
+    }
+    const int ncycles = C.cfg.nGMRES + (use_net ? 1 : 0);
+    int its_plain = 0;
+    bool net_ok = false;
     int iKs = 0;
-    for (int mG = 1; mG <= C.cfg.nGMRES; ++mG) {
+    for (int mG = 1; mG <= ncycles; ++mG) {
+        const bool learned = use_net && mG == 1;
         st->lGMRES = mG - 1;
         if (mG > 1 && sparse && lgmres_common <= 0) {
             // SolGMRs tests the COMMON lGMRES, which it never sets (solgmr.f:528): the cycle
@@ -642,50 +676,83 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
             PH_TRY(sync(C));
             unorm = std::sqrt(C.h_scal[S_TMP0]);
         }
-        k_init_cycle<<<1, 256, 0, C.stream>>>(s, K, unorm, epsnrm, C.d_flag);
+        k_init_cycle<<<1, 256, 0, C.stream>>>(s, K, unorm, epsnrm, C.d_flag, cap);
         ++C.launches;
         // uBrg(1) /= unorm
         scale_by<V>(C, Uj(1), s + S_UNORM, 0, n5, nullptr);
+        // the solution is sum_j y_j u_j, or sum_j y_j z_j in a learned (flexible) cycle
+        const V* basis = U;
+        if constexpr (std::is_same<V, float>::value)
+            if (learned) basis = C.net.d_Z;
+        bool nonfinite = false;
         // the finite-difference product reads eGMRES (changed by itrFDI) as a launch value
-        if (!C.cfg.no_graph && C.cfg.ap_mode != PHGPU_AP_FD && cycle_graph<V>(C, min_iters, sparse, ebe)) {
-            PH_TRY(check(C, cudaGraphLaunch(C.cyc.exec, C.stream), "cycle graph launch"));
-            ++C.cyc.runs;
+        if (!C.cfg.no_graph && C.cfg.ap_mode != PHGPU_AP_FD && cycle_graph<V>(C, min_iters, sparse, ebe, learned)) {
+            CycleGraph& G = learned ? C.cyc_net : C.cyc;
+            PH_TRY(check(C, cudaGraphLaunch(G.exec, C.stream), "cycle graph launch"));
+            ++G.runs;
             // back substitution and update with the iteration count the graph left in flag[2],
             // then one host read of the flags and the final residual estimate
             k_backsolve<<<1, 1, 0, C.stream>>>(s, K, 0, C.d_flag + 2);
-            k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, U, C.ldU, 0, s, n5, C.d_flag + 2);
+            k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, basis, C.ldU, 0, K, s, n5, C.d_flag + 2);
             C.launches += 2;
             PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 3, cudaMemcpyDeviceToHost, C.stream), "flag"));
             PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "echeck"));
             PH_TRY(sync(C));
             iKs = C.h_flag[2];
             if (iKs < 1 || iKs > K) return fail(C, PHGPU_ERR_CUDA, "cycle graph ran no Krylov iteration");
-            for (int i = 1; i <= iKs; ++i) C.launches += C.cyc.launches[i];
+            for (int i = 1; i <= iKs; ++i) C.launches += G.launches[i];
             st->ntotGM += iKs;
-            if (C.h_flag[1]) return fail(C, PHGPU_ERR_NONFINITE, "non-finite Hessenberg entry in GMRES");
-            st->echeck = C.h_scal[S_ECHECK];
-            if (C.h_scal[S_ECHECK] <= epsnrm) break;
-            continue;
+            nonfinite = C.h_flag[1] != 0;
         } else {
             for (int iK = 1; iK <= K; ++iK) {
                 iKs = iK;
-                PH_TRY(krylov_step<V>(C, iK, min_iters, sparse, ebe, 0, 0));
+                PH_TRY(krylov_step<V>(C, iK, min_iters, sparse, ebe, 0, 0, learned));
                 st->ntotGM += 1;
                 PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
                 PH_TRY(sync(C));
-                if (C.h_flag[1]) return fail(C, PHGPU_ERR_NONFINITE, "non-finite Hessenberg entry in GMRES");
-                if (C.h_flag[0]) break;
+                if (C.h_flag[1]) {
+                    nonfinite = true;
+                    break;
+                }
+                if (C.h_flag[0] || (learned && iK >= cap)) break;
+            }
+            if (!nonfinite) {
+                k_backsolve<<<1, 1, 0, C.stream>>>(s, K, iKs, nullptr);
+                k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, basis, C.ldU, iKs, K, s, n5, nullptr);
+                C.launches += 2;
+                PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "echeck"));
+                PH_TRY(sync(C));
             }
         }
-        k_backsolve<<<1, 1, 0, C.stream>>>(s, K, iKs, nullptr);
-        k_update_dy<V><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, U, C.ldU, iKs, s, n5, nullptr);
-        C.launches += 2;
-        PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, s, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "echeck"));
-        PH_TRY(sync(C));
+        if (nonfinite) {
+            if (!learned) return fail(C, PHGPU_ERR_NONFINITE, "non-finite Hessenberg entry in GMRES");
+            // the network gave a non-finite direction: drop the cycle, block-diagonal GMRES from Dy = 0
+            fill0(C, C.d_Dy, sizeof(double) * n5);
+            st->net_its = iKs;
+            continue;
+        }
         st->echeck = C.h_scal[S_ECHECK];
-        if (C.h_scal[S_ECHECK] <= epsnrm) break;
+        const bool converged = C.h_scal[S_ECHECK] <= epsnrm;
+        if (learned) {
+            st->net_its = iKs;
+            net_ok = converged;
+        } else {
+            its_plain += iKs;
+        }
+        if (converged) break;
     }
     st->iKs = iKs;
+    if (use_net) {
+        st->net_fallback = net_ok ? PHGPU_NET_USED : PHGPU_NET_FELL_BACK;
+        if (net_ok) {
+            C.net.fails = 0;
+        } else if (++C.net.fails >= 2) {
+            C.net.disabled = true;
+        }
+    } else if (want_net) {
+        // a block-diagonal solve with the learned preconditioner selected: its count is the reference
+        C.net.its_ref = its_plain;
+    }
     (void)done;
     return PHGPU_OK;
 }
@@ -709,6 +776,8 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
     // products do not carry it
     if (C.cfg.iDC != 0 && (C.cfg.precision != PHGPU_FP64 || C.cfg.ap_mode != PHGPU_AP_FD))
         return fail(C, PHGPU_ERR_UNSUPPORTED, "iDC != 0 needs FP64 with the finite-difference product");
+    if (C.cfg.precond == PHGPU_PRECOND_LEARNED && (C.cfg.precision != PHGPU_MIXED || C.cfg.ap_mode != PHGPU_AP_LINEAR))
+        return fail(C, PHGPU_ERR_UNSUPPORTED, "the learned preconditioner needs mixed precision with the linearized product");
     const bool asm_bd = !sparse || lhs;
     cudaEventRecord(C.ev[0], C.stream);
     if (C.cfg.precision == PHGPU_FP64) {
@@ -902,10 +971,6 @@ int time_step_dev(Ctx& C, int nitr, phgpu_stats* st) {
 // ============================================================================
 using phgpu::Ctx;
 
-struct phgpu_ctx {
-    Ctx c;
-};
-
 extern "C" {
 
 int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) {
@@ -926,6 +991,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
         return PHGPU_ERR_UNSUPPORTED;
     if (cfg->idiff != 0 && cfg->idiff != 1) return PHGPU_ERR_UNSUPPORTED;
     if (cfg->iDC < 0 || cfg->iDC > 3) return PHGPU_ERR_INVALID;
+    if (cfg->precond != PHGPU_PRECOND_BDIAG && cfg->precond != PHGPU_PRECOND_LEARNED) return PHGPU_ERR_INVALID;
     phgpu_ctx* h = new (std::nothrow) phgpu_ctx();
     if (!h) return PHGPU_ERR_NOMEM;
     Ctx& C = h->c;
@@ -1112,6 +1178,7 @@ int phgpu_destroy(phgpu_ctx* h) {
     Ctx& C = h->c;
     if (C.stream) cudaStreamSynchronize(C.stream);
     phgpu::cycle_graph_free(C);
+    phgpu::net_free(C);
     void* ptrs[] = {C.d_ch_elem, C.d_ch_node, C.d_ch_nodes, C.d_ch_cstart, C.d_ch_csr, C.d_ch_lien,
                     C.d_bdstage, C.d_ien, C.d_ienh, C.d_ienw, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_xlo, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
                     C.d_slaves, C.d_mst, C.d_slv_start, C.d_slv, C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_res,
@@ -1140,6 +1207,7 @@ int phgpu_set_config(phgpu_ctx* h, const phgpu_config* cfg) {
         return PHGPU_ERR_UNSUPPORTED;
     if (cfg->idiff != 0 && cfg->idiff != 1) return PHGPU_ERR_UNSUPPORTED;
     if (cfg->iDC < 0 || cfg->iDC > 3) return PHGPU_ERR_INVALID;
+    if (cfg->precond != PHGPU_PRECOND_BDIAG && cfg->precond != PHGPU_PRECOND_LEARNED) return PHGPU_ERR_INVALID;
     const bool was64 = h->c.cfg.precision == PHGPU_FP64;
     const bool is64 = cfg->precision == PHGPU_FP64;
     if (was64 != is64 && !was64) return PHGPU_ERR_UNSUPPORTED;  // basis was allocated as FP32
@@ -1279,6 +1347,42 @@ int phgpu_solmfg(phgpu_ctx* h, const double* y, const double* ac, double* res, d
         return sync(C);
     }
     return PHGPU_OK;
+}
+
+int phgpu_set_bc(phgpu_ctx* h, const double* BC) {
+    using namespace phgpu;
+    if (!h || !BC) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    const int N = C.N;
+    std::vector<double> bc(6 * (size_t)N);
+    for (int n = 0; n < N; ++n)
+        for (int k = 0; k < 6; ++k) bc[6 * (size_t)n + k] = BC[(size_t)k * N + n];
+    PH_TRY(check(C, cudaMemcpyAsync(C.d_BC, bc.data(), sizeof(double) * bc.size(), cudaMemcpyHostToDevice, C.stream), "BC"));
+    return sync(C);
+}
+
+int phgpu_net_collect(phgpu_ctx* h, int slot) {
+    using namespace phgpu;
+    if (!h) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    if (C.cfg.precision != PHGPU_MIXED || C.cfg.ap_mode != PHGPU_AP_LINEAR)
+        return fail(C, PHGPU_ERR_UNSUPPORTED, "training pairs come from a mixed-precision solve with the linearized product");
+    if (slot < 0 || slot >= C.net.tr.cap) return fail(C, PHGPU_ERR_INVALID, "pair slot outside the allocated training set");
+    const size_t n5 = 5 * (size_t)C.N;
+    // features of the solve's state and factors, then w = U Dy (the Krylov-space solution)
+    PH_TRY(net_prepare(C));
+    k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, C.d_t64, n5, nullptr);
+    ++C.launches;
+    lu_apply<double, double>(C, C.d_bd, C.d_t64, PHGPU_LU_PRODUCT);
+    to_f32(C, C.d_t64, C.d_t32b, n5);
+    // A~ w with the operator the Krylov loop multiplies by
+    float* Aw = (float*)C.d_U;
+    PH_TRY(ap_lin<float>(C, C.d_t32b, Aw, nullptr));
+    dot<float>(C, Aw, Aw, n5, S_TMP0, nullptr);
+    PH_TRY(net_store_pair(C, slot, Aw, C.d_t32b, C.d_scal + S_TMP0));
+    return sync(C);
 }
 
 int phgpu_genadj(const phgpu_mesh* m, int nnz, int* colm, int* rowp, int* icnt) {

@@ -1,0 +1,139 @@
+"""Training and evaluation of the learned right preconditioner (flexible GMRES).
+
+The preconditioner has no counterpart in the reference: PHASTA's matrix-free GMRES
+(solmfg.f:221-340) is preconditioned by the 5x5 block-diagonal LU of i3lu.f alone.  Here a
+message-passing network over the mesh edges maps a Krylov vector v of the block-diagonal
+preconditioned operator A~ = L^-1 J U^-1 to z ~ A~^-1 v; ``precond = PHGPU_PRECOND_LEARNED``
+makes the GMRES cycle flexible with z_j = P(v_j), and the block-diagonal method stays the
+fallback (include/phgpu.h describes the policy).
+
+Everything numerical runs on the GPU in libphgpu.so (csrc/learn.cu): the network's forward
+and backward kernels (BF16 tensor-core GEMMs, FP32 accumulation), the Adam update and the
+pair collection.  This module chooses the training states, drives the plain solver that
+produces the pairs, and calls the training entry point.
+
+Training pairs (v, t) come from block-diagonal solves of seeded perturbed states: w = U Dy is
+the solve's Krylov-space solution, v = A~ w / ||A~ w||, t = w / ||A~ w|| (so A~ t = v exactly).
+The states follow the learned-preconditioner workload's recipe: uniform flow along x plus
+seeded Gaussian noise of sigma 0.5-5% of the free stream, Mach 0.1-0.6, half of them with
+random-phase Fourier velocity modes on top; each state gives the pairs of the three Newton
+iterations of one time step.  The network is local (three edge hops) and its inputs are
+normalised, so pairs from a small mesh train the operator of the large one.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from . import mesh
+
+H, F_IN, NL, NOUT = 64, 48, 3, 5
+
+
+def param_offsets() -> dict:
+    """Offsets of the flat weight array (include/phgpu.h)."""
+    lay = [("W_e", (H, F_IN)), ("b_e", (H,))]
+    for l in range(NL):
+        lay += [(f"W_p{l}", (H, H)), (f"W_q{l}", (H, H)), (f"b_m{l}", (H,)), (f"C{l}", (H, 3)),
+                (f"W_u{l}", (H, 2 * H)), (f"b_u{l}", (H,))]
+    lay += [("W_d", (NOUT, H)), ("b_d", (NOUT,)), ("alpha", (NOUT,)), ("beta", (NOUT,))]
+    out, o = {}, 0
+    for n, s in lay:
+        out[n] = (o, s)
+        o += int(np.prod(s))
+    assert o == L.PHGPU_NET_NPARAM
+    return out
+
+
+def init_weights(seed: int = 1) -> np.ndarray:
+    """He-scaled normal GEMM weights, zero biases and a zero decoder: the untrained network is the
+    identity, i.e. flexible GMRES starts as the plain block-diagonal method."""
+    g = np.random.default_rng(seed)
+    w = np.zeros(L.PHGPU_NET_NPARAM, np.float32)
+    for n, (o, s) in param_offsets().items():
+        size = int(np.prod(s))
+        if n.startswith("W_") and n != "W_d":
+            scale = math.sqrt(2.0 / s[1]) * (0.5 if n.startswith("W_u") else 1.0)
+            w[o:o + size] = (g.standard_normal(size) * scale).astype(np.float32)
+        elif n.startswith("C"):
+            w[o:o + size] = (0.5 * g.standard_normal(size)).astype(np.float32)
+        elif n in ("alpha", "beta"):
+            w[o:o + size] = 1.0
+    return w
+
+
+def channel_bc(case: mesh.Case, mach: float) -> np.ndarray:
+    """BC(nshg, 6) of the channel's Dirichlet inflow for the free stream at ``mach``."""
+    fs = mesh.freestream(mach)
+    BC = np.array(case.BC, dtype=np.float64, copy=True)
+    t = ((case.iBC >> 1) & 1) == 1
+    v = ((case.iBC >> 3) & 7) == 7
+    BC[1, t] = fs["T"]
+    BC[2, v], BC[3, v], BC[4, v] = fs["u"], 0.0, 0.0
+    return BC
+
+
+@dataclass
+class PairRecipe:
+    sigma: tuple = (0.005, 0.05)     # log-uniform noise level (fraction of the free stream)
+    mach: tuple = (0.1, 0.6)         # uniform Mach number
+    re: float = 1000.0
+    fourier: float = 0.5             # share of states with Fourier velocity modes on top
+    newton: int = 3                  # pairs per state (Newton iterations of one time step)
+
+
+def state(case: mesh.Case, k: int, seed: int, recipe: PairRecipe):
+    """Seeded training state k: (mach, y)."""
+    g = np.random.default_rng([seed, k])
+    mach = float(g.uniform(*recipe.mach))
+    sigma = float(math.exp(g.uniform(math.log(recipe.sigma[0]), math.log(recipe.sigma[1]))))
+    y = mesh.uniform_state(case, mach, sigma=sigma, seed=int(g.integers(1, 2 ** 31)))
+    if g.uniform() < recipe.fourier:
+        amp = float(g.uniform(0.1, 0.3))
+        yf = mesh.fourier_state(case, mach, kmax=4, seed=int(g.integers(1, 2 ** 31)))
+        y = y.reshape(5, -1).copy()
+        y[:3] += amp * yf.reshape(5, -1)[:3]
+        y = mesh.apply_bc_state(case, y.reshape(-1))
+    return mach, y
+
+
+def collect_pairs(g, case: mesh.Case, n_pairs: int, seed: int = 1, recipe: PairRecipe | None = None) -> dict:
+    """Fill the context's training set with n_pairs pairs from block-diagonal solves (the GpuSolver
+    ``g`` must be mixed precision with the linearized product on the channel mesh ``case``)."""
+    recipe = recipe or PairRecipe()
+    g.set_params(precond=L.PHGPU_PRECOND_BDIAG)
+    g.net_pairs(n_pairs)
+    slot, k, its = 0, 0, []
+    t0 = time.perf_counter()
+    while slot < n_pairs:
+        mach, y0 = state(case, k, seed, recipe)
+        dt = mesh.cfl_dt(case, mach)
+        g.set_bc(channel_bc(case, mach))
+        g.set_params(rmu=1.0 / recipe.re, istep=1, eGMRES=0.0, **mesh.time_params(0.5, dt))
+        y, ac = y0, np.zeros_like(y0)
+        ac0 = np.zeros_like(y0)
+        for it in range(1, recipe.newton + 1):
+            if slot >= n_pairs:
+                break
+            g.set_params(iter=it)
+            _, _, Dy, st = g.SolMFG(y, ac)
+            g.net_collect(slot)
+            its.append(st.iKs)
+            slot += 1
+            y, ac = g.itrCorrect(y, ac, y0, ac0, Dy)
+        k += 1
+    return {"pairs": n_pairs, "states": k, "krylov_iterations_mean": float(np.mean(its)),
+            "seconds": time.perf_counter() - t0}
+
+
+def train(g, case: mesh.Case, n_pairs: int = 2000, epochs: int = 8, lr: float = 1e-3, seed: int = 1,
+          recipe: PairRecipe | None = None, weights: np.ndarray | None = None) -> tuple[np.ndarray, dict]:
+    """Collect pairs and train on the GPU; returns (weights, report)."""
+    rep = {"collect": collect_pairs(g, case, n_pairs, seed, recipe)}
+    g.net_set_weights(init_weights(seed) if weights is None else weights)
+    rep["train"] = g.net_train(epochs, lr=lr, seed=seed)
+    return g.net_get_weights(), rep

@@ -306,6 +306,36 @@ def vortex_state(case: Case, mach: float = 0.1, noise: float = 1e-3, seed: int =
     return apply_bc_state(case, y.reshape(-1))
 
 
+def fourier_state(case: Case, mach: float, kmax: int = 8, nmodes: int = 24, noise: float = 0.0,
+                  seed: int = 20261203, lengths=None) -> np.ndarray:
+    """Random-phase Fourier velocity modes: u(x) = sum_m a_m cos(2 pi k_m . x / L + phi_m) with
+    integer wave vectors 1 <= |k_m|_inf <= kmax and amplitudes a_m perpendicular to k_m
+    (divergence-free), scaled so that max |u| over the nodes is 1; p and T of the free stream at
+    ``mach`` (so max |u| / c = mach), plus ``noise`` x seeded Gaussian noise."""
+    fs = freestream(mach)
+    g = np.random.default_rng(seed)
+    L = np.asarray(lengths if lengths is not None else case.meta.get("lengths", (1.0, 1.0, 1.0)), dtype=np.float64)
+    x = case.x
+    u = np.zeros((case.nshg, 3))
+    for _ in range(nmodes):
+        k = np.zeros(3)
+        while not np.any(k):
+            k = g.integers(-kmax, kmax + 1, size=3).astype(np.float64)
+        a = g.standard_normal(3)
+        a -= k * (a @ k) / (k @ k)
+        a /= np.linalg.norm(a) * np.sqrt(k @ k)  # energy falling with |k|
+        phi = g.uniform(0.0, 2.0 * np.pi)
+        u += np.cos(2.0 * np.pi * (x / L) @ k + phi)[:, None] * a[None, :]
+    u /= np.abs(np.linalg.norm(u, axis=1)).max()
+    y = np.empty((5, case.nshg))
+    y[0], y[1], y[2] = u[:, 0], u[:, 1], u[:, 2]
+    y[3], y[4] = fs["p"], fs["T"]
+    if noise > 0:
+        z = _noise(seed + 1, case.nshg)
+        y += noise * np.array([1.0, 1.0, 1.0, fs["p"], fs["T"]])[:, None] * z
+    return apply_bc_state(case, y.reshape(-1))
+
+
 def apply_bc_state(case: Case, y: np.ndarray) -> np.ndarray:
     """itrBC for Dirichlet T/velocity and the periodic master->slave copy (itrbc.f:54-176)."""
     y = y.reshape(5, case.nshg).copy()

@@ -54,7 +54,8 @@ class PhgpuError(RuntimeError):
 def make_params(mu: float, dt: float, rho_inf: float = 0.5, Kspace: int = 10, etol: float = 1e-3,
                 minIters: int = 1, nGMRES: int = 1, pr: float = 0.72, precision: int = L.PHGPU_FP64,
                 ap_mode: int = L.PHGPU_AP_FD, navier: int = 1, ivart: int = 2,
-                outer_residual: int = L.PHGPU_RES_FP64, idiff: int = 0, iDC: int = 0, itau: int = 0) -> dict:
+                outer_residual: int = L.PHGPU_RES_FP64, idiff: int = 0, iDC: int = 0, itau: int = 0,
+                precond: int = L.PHGPU_PRECOND_BDIAG) -> dict:
     """The COMMON-block values of the hot path (input.config defaults otherwise)."""
     p = {"Rgas": rgas(), "gamma": GAMMA, "gamma1": GAMMA1, "pr": pr, "rmu": mu,
          "dtsfct": 1.0, "taucfct": 1.0, "temper": 1.0, "itau": itau, "ivart": ivart,
@@ -62,7 +63,7 @@ def make_params(mu: float, dt: float, rho_inf: float = 0.5, Kspace: int = 10, et
          "Kspace": Kspace, "nGMRES": nGMRES, "minIters": minIters, "etol": etol,
          "epsM": float(np.sqrt(np.finfo(np.float64).eps)), "eGMRES": 0.0, "iter": 1, "istep": 0,
          "precision": precision, "ap_mode": ap_mode, "outer_residual": outer_residual, "idiff": idiff,
-         "iDC": iDC}
+         "iDC": iDC, "precond": precond}
     p.update(time_params(rho_inf, dt))
     return p
 
@@ -87,11 +88,13 @@ class SolveStats:
     rnorm: float
     t_assembly_ms: float
     t_gmres_ms: float
+    net_its: int = 0
+    net_fallback: int = L.PHGPU_NET_PLAIN
 
 
 def _stats(s: L.Stats) -> SolveStats:
     return SolveStats(s.iKs, s.lGMRES, s.ntotGM, s.unorm0, s.echeck, s.eGMRES, s.totres, s.rnorm,
-                      s.t_assembly_ms, s.t_gmres_ms)
+                      s.t_assembly_ms, s.t_gmres_ms, s.net_its, s.net_fallback)
 
 
 class _MeshArrays:
@@ -173,7 +176,7 @@ class GpuSolver:
     def get_params(self) -> dict:
         c = L.Config()
         self._check(self.lib.phgpu_get_config(self.h, C.byref(c)))
-        return {name: getattr(c, name) for name, _ in L.Config._fields_ if name != "reserved"}
+        return {name: getattr(c, name) for name, _ in L.Config._fields_}
 
     def _v(self, k: int = 5) -> np.ndarray:
         return np.zeros(k * self.nshg, dtype=np.float64)
@@ -350,6 +353,68 @@ class GpuSolver:
         self._check(self.lib.phgpu_time_step_dev(self.h, nitr, C.byref(st)))
         self.ntotGM = st.ntotGM
         return _stats(st)
+
+    def set_bc(self, BC):
+        """New Dirichlet values BC(nshg, 6) (the reference passes BC to every ElmMFG/SolMFG call)."""
+        bc = np.ascontiguousarray(BC, dtype=np.float64).reshape(-1)
+        self._check(self.lib.phgpu_set_bc(self.h, L.dptr(bc)))
+
+    # -- learned preconditioner (flexible GMRES with a message-passing network; no reference
+    #    counterpart: the reference's preconditioner is the block-diagonal LU of i3lu.f) --
+    def net_set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._check(self.lib.phgpu_net_set_weights(self.h, L.fptr(w), w.size))
+
+    def net_get_weights(self) -> np.ndarray:
+        w = np.zeros(L.PHGPU_NET_NPARAM, np.float32)
+        self._check(self.lib.phgpu_net_get_weights(self.h, L.fptr(w), w.size))
+        return w
+
+    def net_graph(self):
+        """(nstart (nshg+1), nbr (nnz, neighbour | shift code << 26), geo [Lx, Ly, Lz, 1/hbar])."""
+        nnz = C.c_longlong()
+        geo = np.zeros(4, np.float32)
+        self._check(self.lib.phgpu_net_graph(self.h, None, None, 0, C.byref(nnz), L.fptr(geo)))
+        nstart = np.zeros(self.nshg + 1, np.int32)
+        nbr = np.zeros(max(nnz.value, 1), np.uint32)
+        self._check(self.lib.phgpu_net_graph(self.h, L.iptr(nstart), nbr.ctypes.data_as(C.POINTER(C.c_uint)),
+                                             nbr.size, C.byref(nnz), L.fptr(geo)))
+        return nstart, nbr[: nnz.value], geo
+
+    def net_features(self) -> np.ndarray:
+        out = np.zeros((self.nshg, 32), np.float32)
+        self._check(self.lib.phgpu_net_features(self.h, L.fptr(out)))
+        return out
+
+    def net_apply(self, v, hidden: bool = False):
+        """z = P(v) (res layout); with hidden, also h0..h3 (4, nshg, 64) and the decoder outputs (nshg, 8)."""
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        z = np.zeros_like(v)
+        hb = np.zeros((4, self.nshg, 64), np.float32) if hidden else None
+        ob = np.zeros((self.nshg, 8), np.float32) if hidden else None
+        self._check(self.lib.phgpu_net_apply(self.h, L.dptr(v), L.dptr(z), L.fptr(hb), L.fptr(ob)))
+        return (z, hb, ob) if hidden else z
+
+    def net_loss_grad(self, v, t):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        loss = C.c_double()
+        grad = np.zeros(L.PHGPU_NET_NPARAM, np.float32)
+        self._check(self.lib.phgpu_net_loss_grad(self.h, L.dptr(v), L.dptr(t), C.byref(loss), L.fptr(grad)))
+        return loss.value, grad
+
+    def net_pairs(self, cap: int):
+        self._check(self.lib.phgpu_net_pairs(self.h, cap))
+
+    def net_collect(self, slot: int):
+        self._check(self.lib.phgpu_net_collect(self.h, slot))
+
+    def net_train(self, epochs: int, lr: float = 1e-3, npairs: int = 0, clip: float = 1.0, seed: int = 1,
+                  renormalize: bool = True, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8) -> dict:
+        cfg = L.NetTrainConfig(epochs, npairs, lr, beta1, beta2, eps, clip, seed, 1 if renormalize else 0)
+        st = L.NetTrainStats()
+        self._check(self.lib.phgpu_net_train(self.h, C.byref(cfg), C.byref(st)))
+        return {"loss_first": st.loss_first, "loss_last": st.loss_last, "ms": st.ms, "steps": st.steps}
 
     def residual_norm_dev(self) -> float:
         r = C.c_double()

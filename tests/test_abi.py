@@ -28,7 +28,29 @@ def test_create_rejects_invalid_arguments_before_touching_the_device(gpu_lib):
     assert gpu_lib.phgpu_last_error(None) == b"null context"
 
 
-def test_struct_sizes_match_header():
-    # phgpu_config: 12 doubles, 9 ints, 3 doubles, 2 ints, 2 ints + 6 reserved (packed by the C ABI rules)
-    assert C.sizeof(L.Config) % 8 == 0
-    assert C.sizeof(L.Stats) == 4 * 4 + 7 * 8
+def test_struct_layouts_match_the_header_as_gcc_lays_them_out(tmp_path):
+    """Every struct of include/phgpu.h: sizeof and the offset of every field as gcc computes them
+    (tests/abi/layout.c), against the ctypes declarations."""
+    import json
+    from pathlib import Path
+    src = Path(__file__).resolve().parent / "abi" / "layout.c"
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-o", str(exe), str(src)], check=True)
+    got = json.loads(subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout)
+    for cname, ct in (("phgpu_config", L.Config), ("phgpu_mesh", L.Mesh), ("phgpu_stats", L.Stats),
+                      ("phgpu_net_train_config", L.NetTrainConfig), ("phgpu_net_train_stats", L.NetTrainStats)):
+        c = got[cname]
+        assert c["__size"] == C.sizeof(ct), cname
+        fields = [f[0] for f in ct._fields_]
+        assert sorted(fields) == sorted(k for k in c if k != "__size"), cname
+        for f in fields:
+            assert getattr(ct, f).offset == c[f], (cname, f)
+    k = got["constants"]
+    assert k["PHGPU_NET_NPARAM"] == L.PHGPU_NET_NPARAM and k["PHGPU_NET_NTRAIN"] == L.PHGPU_NET_NTRAIN
+    assert k["PHGPU_RSTAT_NOALLOC_MAX_N"] == L.PHGPU_RSTAT_NOALLOC_MAX_N
+    assert k["PHGPU_PRECOND_LEARNED"] == L.PHGPU_PRECOND_LEARNED and k["PHGPU_NET_PLAIN"] == L.PHGPU_NET_PLAIN
+
+
+def test_network_parameter_layout_matches_the_oracle():
+    from oracle import net_oracle as no
+    assert no.NPARAM == L.PHGPU_NET_NPARAM and no.NTRAIN == L.PHGPU_NET_NTRAIN

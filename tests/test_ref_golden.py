@@ -47,6 +47,7 @@ def load(name):
     assert np.array_equal(d["y"], y) and np.array_equal(d["ac"], ac), "seeded state changed"
     stored = json.loads(str(d["params"]))
     stored.setdefault("iDC", 0)  # fixtures written before the option hold no key for it (it was off)
+    stored.setdefault("precond", 0)  # likewise: the block-diagonal preconditioner of the reference
     assert stored == json.loads(json.dumps(p, sort_keys=True))
     return d, case, p
 
