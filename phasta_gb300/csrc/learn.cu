@@ -1278,9 +1278,7 @@ void forward(Ctx& C, const float* v, float* z, const bf16* ctx, bool train) {
     NetCtx& T = C.net;
     NetTrain& R = T.tr;
     const size_t HNs = (size_t)C.N * H;
-    const int nslab = (C.N + 15) / 16;
-    const int sms = num_sms();
-    const int genc = std::max(1, std::min((nslab + 7) / 8, 2 * sms));
+    const int genc = T.grid_mp;
     Fwd a{};
     a.w = T.d_w;
     a.v = v;
@@ -1420,6 +1418,11 @@ int net_setup(Ctx& C) {
         NT_TRY(nalloc(C, &T.d_P1, HNs));
     }
     if (!T.d_Z && C.cfg.precision == PHGPU_MIXED) NT_TRY(nalloc(C, &T.d_Z, C.ldU * (size_t)C.Ucap));
+    // persistent grid of the forward kernels: two CTAs per SM (shared memory and 128 registers
+    // allow two), 8 slabs of 16 nodes per CTA pass
+    const int nslab = (C.N + 15) / 16;
+    T.grid_mp = std::max(1, std::min((nslab + 7) / 8, 2 * num_sms()));
+    T.grid_enc = T.grid_mp;
     return PHGPU_OK;
 }
 

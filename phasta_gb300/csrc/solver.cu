@@ -728,6 +728,7 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
             if (!learned) return fail(C, PHGPU_ERR_NONFINITE, "non-finite Hessenberg entry in GMRES");
             // the network gave a non-finite direction: drop the cycle, block-diagonal GMRES from Dy = 0
             fill0(C, C.d_Dy, sizeof(double) * n5);
+            fill0(C, C.d_flag + 1, sizeof(int));
             st->net_its = iKs;
             continue;
         }
