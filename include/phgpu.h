@@ -148,8 +148,8 @@ typedef struct {
 
 /* phgpu_stats.net_fallback */
 enum {
-    PHGPU_NET_USED = 0,      /* the learned cycle converged with fewer iterations than the last
-                                block-diagonal solve */
+    PHGPU_NET_USED = 0,      /* the learned cycle converged with fewer iterations, and in less
+                                device time, than the reference block-diagonal solve needed */
     PHGPU_NET_FELL_BACK = 1, /* it did not (or produced a non-finite value): block-diagonal GMRES
                                 cycles finished the solve from where it stopped */
     PHGPU_NET_PLAIN = 2      /* block-diagonal GMRES only: precond = BDIAG, no weights, the
@@ -260,7 +260,8 @@ int phgpu_residual_norm_dev(phgpu_ctx* ctx, double* rnorm);
  * block-sparse product, 11 FP64 assembled tangent, 12 FP64 block-sparse product (9-12 use the
  * sparse solver's structure; 10 and 12 multiply whatever tangent 9 and 11 left), 13 FP32
  * element tangents stored per element, 14 FP32 element-by-element product (13-14: mixed
- * precision context, one element topology) */
+ * precision context, one element topology), 17 one application of the learned preconditioner
+ * (weights set, after a mixed-precision solve), 18 its context features */
 int phgpu_sweep_dev(phgpu_ctx* ctx, int which);
 
 /* ---- learned preconditioner (no counterpart in the reference) --------------------------
@@ -269,10 +270,12 @@ int phgpu_sweep_dev(phgpu_ctx* ctx, int which);
  * to z = P(v) ~ (L^-1 J U^-1)^-1 v; with precond = PHGPU_PRECOND_LEARNED the GMRES cycle of
  * solmfg.f:221-340 becomes flexible GMRES whose Krylov iteration j multiplies z_j = P(v_j) and
  * whose solution is sum_j y_j z_j.  The block-diagonal GMRES of the reference is the fallback:
- * the first solve of a context runs it to set the reference iteration count; later solves cap
- * the learned cycle one iteration below that count and, when it does not converge (or is not
- * finite), finish with block-diagonal cycles from where it stopped; two failures in a row switch
- * the network off until new weights are set.  The network: encoder 48 -> 64, three edge
+ * the first solve of a context (and the first after new weights) runs it to set the reference:
+ * its Krylov iterations and its device time per iteration.  Later solves cap the learned cycle one
+ * iteration below that count; a learned cycle fails when it does not converge within the cap,
+ * is not finite, or takes longer on the device than the reference iterations it replaces.  A
+ * failed cycle is finished by block-diagonal cycles from where it stopped (nGMRES more cycles);
+ * two failures in a row switch the network off until new weights are set.  The network: encoder 48 -> 64, three edge
  * message-passing layers (hidden width 64), decoder 64 -> 5; BF16 GEMM operands with FP32
  * accumulation on the tensor cores, FP32 master weights.  Input per node: the direction (5), the
  * node's factored BDiag block (25, over their RMS), its state (5) and an active flag.
@@ -312,9 +315,11 @@ int phgpu_net_apply(phgpu_ctx* ctx, const double* v, double* z, float* hidden, f
 int phgpu_net_loss_grad(phgpu_ctx* ctx, const double* v, const double* t, double* loss, float* grad);
 /* training pairs: room for cap pairs (frees the old set) */
 int phgpu_net_pairs(phgpu_ctx* ctx, int cap);
-/* after a mixed-precision block-diagonal solve (phgpu_solmfg): store pair `slot` from its
- * solution w = U Dy: v = A~ w / ||A~ w||, t = w / ||A~ w||, and the current features */
-int phgpu_net_collect(phgpu_ctx* ctx, int slot);
+/* after a mixed-precision block-diagonal solve (phgpu_solmfg): store pair `slot` from u = the
+ * solve's Krylov-space solution U Dy (which = 0) or Krylov vector u_which of its last cycle
+ * (1 <= which <= the cycle's iterations + 1): v = A~ u / ||A~ u||, t = u / ||A~ u|| (A~ t = v
+ * exactly), with the current context features */
+int phgpu_net_collect(phgpu_ctx* ctx, int slot, int which);
 /* Adam over the collected pairs, one pair per step, on the GPU */
 int phgpu_net_train(phgpu_ctx* ctx, const phgpu_net_train_config* cfg, phgpu_net_train_stats* out);
 

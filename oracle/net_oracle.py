@@ -15,7 +15,7 @@ here and implemented by the kernels:
            edges), mapped to periodic masters (iper); per directed edge
            i -> j the edge vector e_ij = (x_b - x_a) / hbar of the element
            edge it came from (periodic wrap kept), hbar the mean edge length
-  input    x_i = [ s alpha_d v_i,d (5) | ctx_i (32) | 0 (11) ]        bf16
+  input    x_i = [ ctx_i (32) | s alpha_d v_i,d (5) | 0 (11) ]        bf16
            s = sqrt(5 nshg) (v has unit 2-norm, so s v_i is O(1) per node)
            ctx_i = 25 entries of node i's factored BDiag block over their
            RMS, 10 (p/pbar - 1), u/cbar, v/cbar, w/cbar, 10 (T/Tbar - 1),
@@ -49,7 +49,7 @@ import math
 import numpy as np
 
 H = 64          # hidden width
-F_IN = 48       # input features (5 direction + 32 context + 11 zero)
+F_IN = 48       # input features (32 context + 5 direction + 11 zero)
 F_CTX = 32
 NL = 3          # message-passing layers
 NOUT = 5
@@ -238,8 +238,8 @@ def forward(w, g: Graph, v: np.ndarray, ctx: np.ndarray, act: np.ndarray, emulat
     N = v.shape[0]
     s = math.sqrt(5.0 * N)
     x = np.zeros((N, F_IN))
-    x[:, :5] = r(s * v * Wg["alpha"][None, :])
-    x[:, 5:5 + F_CTX] = ctx
+    x[:, :F_CTX] = ctx
+    x[:, F_CTX:F_CTX + 5] = r(s * v * Wg["alpha"][None, :])
     pre_e = x @ Wg["W_e"].T + Wg["b_e"]
     h = r(_relu(pre_e))
     cache = {"x": x, "h": [h], "P": [], "Q": [], "a": [], "u": [], "pre": [], "s": s, "W": Wg}

@@ -140,7 +140,7 @@ def lib():
         "phgpu_net_apply": ([vp, _dp, _dp, _fp, _fp], C.c_int),
         "phgpu_net_loss_grad": ([vp, _dp, _dp, _dp, _fp], C.c_int),
         "phgpu_net_pairs": ([vp, C.c_int], C.c_int),
-        "phgpu_net_collect": ([vp, C.c_int], C.c_int),
+        "phgpu_net_collect": ([vp, C.c_int, C.c_int], C.c_int),
         "phgpu_net_train": ([vp, C.POINTER(NetTrainConfig), C.POINTER(NetTrainStats)], C.c_int),
         # include/phgpu_io.h
         "phgpu_io_openfile": ([C.c_char_p, C.c_char_p, _ip], C.c_int),

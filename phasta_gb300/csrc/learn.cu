@@ -5,7 +5,7 @@
 // by the 5x5 block-diagonal LU alone; that method stays the fallback (solver.cu).
 //
 // Network (the oracle restates it as test infrastructure, oracle/net_oracle.py):
-//   x_i  = [bf16(s alpha_d v_i,d) (5) | ctx_i (32) | 0 (11)],  s = sqrt(5 nshg)
+//   x_i  = [ctx_i (32) | bf16(s alpha_d v_i,d) (5) | 0 (11)],  s = sqrt(5 nshg)
 //   h0   = bf16(relu(W_e x + b_e))
 //   per layer: P = bf16(W_p h), Q = W_q h + b_m, m_ij = relu(Q_i + P_j + C e_ij),
 //              a_i = bf16(mean_j m_ij), h' = bf16(h + relu(W_u [h; a] + b_u))
@@ -154,6 +154,17 @@ __device__ __forceinline__ int edge_vec(const Geo& G, float xi0, float xi1, floa
     e[2] = __fmul_rn(__fadd_rn(__fsub_rn(xj2, xi2), s2), G.rh);
     return j;
 }
+// the same from coordinates already loaded (x.w unused)
+__device__ __forceinline__ void edge_vec4(const Geo& G, const float4& xi, const float4& xj, unsigned nb, float* e) {
+    const unsigned code = nb >> SHIFT;
+    const unsigned c0 = code & 3, c1 = (code >> 2) & 3, c2 = (code >> 4) & 3;
+    const float s0 = c0 == 1 ? G.L0 : (c0 == 2 ? -G.L0 : 0.f);
+    const float s1 = c1 == 1 ? G.L1 : (c1 == 2 ? -G.L1 : 0.f);
+    const float s2 = c2 == 1 ? G.L2 : (c2 == 2 ? -G.L2 : 0.f);
+    e[0] = __fmul_rn(__fadd_rn(__fsub_rn(xj.x, xi.x), s0), G.rh);
+    e[1] = __fmul_rn(__fadd_rn(__fsub_rn(xj.y, xi.y), s1), G.rh);
+    e[2] = __fmul_rn(__fadd_rn(__fsub_rn(xj.z, xi.z), s2), G.rh);
+}
 // message pre-activation Q_i + P_j + C e (one rounding sequence for the forward and backward)
 __device__ __forceinline__ float edge_pre(float q, float p, float c0, float c1, float c2, const float* e) {
     return __fadd_rn(__fadd_rn(q, p), __fmaf_rn(c2, e[2], __fmaf_rn(c1, e[1], __fmul_rn(c0, e[0]))));
@@ -164,8 +175,8 @@ __device__ __forceinline__ float bfhi(uint32_t u) { return __uint_as_float(u & 0
 
 // input feature f of node n (the encoder's x, rebuilt identically by the backward)
 __device__ __forceinline__ float feat(const float* v, const bf16* ctx, const float* alpha, float s, int n, int f) {
-    if (f < NOUT) return __fmul_rn(__fmul_rn(s, v[5 * (size_t)n + f]), alpha[f]);
-    if (f < NOUT + FCTX) return __bfloat162float(ctx[(size_t)FCTX * n + (f - NOUT)]);
+    if (f < FCTX) return __bfloat162float(ctx[(size_t)FCTX * n + f]);
+    if (f < FCTX + NOUT) return __fmul_rn(__fmul_rn(s, v[5 * (size_t)n + (f - FCTX)]), alpha[f - FCTX]);
     return 0.f;
 }
 
@@ -270,6 +281,7 @@ struct Fwd {
     const bf16* ctx;           // [N][32]
     const unsigned char* act;  // [N]
     Geo G;
+    const float4* x4;          // [N] coordinates padded to 16 bytes (the same FP32 values as G.xf)
     const bf16* h_in;
     bf16* h_out;
     const bf16* P_in;
@@ -303,8 +315,17 @@ __global__ void __launch_bounds__(256, 2) k_net_enc(Fwd a) {
     const int N = a.G.N, nslab = (N + 15) / 16;
     for (int slab = blockIdx.x * 8 + warp; slab < nslab; slab += gridDim.x * 8) {
         const int n0 = slab * 16;
-        for (int idx = lane; idx < 16 * (LD48 / 2); idx += 32) {
-            const int r = idx / (LD48 / 2), f = 2 * (idx - r * (LD48 / 2)), n = n0 + r;
+        // context features: 4 x 16 bytes per node
+#pragma unroll
+        for (int it = 0; it < 2; ++it) {
+            const int idx = it * 32 + lane, r = idx >> 2, q = idx & 3, n = n0 + r;
+            uint4 u = make_uint4(0, 0, 0, 0);
+            if (n < N) u = __ldg(reinterpret_cast<const uint4*>(a.ctx + (size_t)FCTX * n) + q);
+            *reinterpret_cast<uint4*>(sx + r * LD48 + 8 * q) = u;
+        }
+        // direction (5) and zeros (columns 37..55) as bf16 pairs from column 32
+        for (int idx = lane; idx < 16 * 12; idx += 32) {
+            const int r = idx / 12, f = FCTX + 2 * (idx - r * 12), n = n0 + r;
             float x0 = 0.f, x1 = 0.f;
             if (n < N) {
                 x0 = feat(a.v, a.ctx, sal, a.s, n, f);
@@ -342,53 +363,50 @@ __global__ void __launch_bounds__(256, 2) k_net_enc(Fwd a) {
     }
 }
 
+constexpr int kEdgeCap = 16 * LD64 / 2;  // CSR entries of a slab that fit in the h area (576)
 constexpr int kMpSmemW = (64 * LD64 + 64 * LD128 + 64 * LD64) * 2 + (64 + 64 + 192 + 8 + 8) * 4;
 constexpr int kMpSmemWarp = (16 * LD64 + 16 * LD64) * 2 + 16 * LDQ * 4;
 constexpr int kMpSmem = kMpSmemW + 8 * kMpSmemWarp;
 
-// mean of relu(Q_i + P_j + C e_ij) over the neighbours of node n, for the 8 channels
-// [8 chunk, 8 chunk + 8) of this lane; lanes 8 slot + chunk take neighbours slot, slot + 4, ...
-__device__ __forceinline__ void aggregate(const Geo& G, const bf16* __restrict__ P, int n, const float* q,
-                                          const float (*cw)[3], int slot, float* acc, int& deg) {
-    const int beg = __ldg(G.nstart + n), end = __ldg(G.nstart + n + 1);
-    deg = end - beg;
-    const float xi0 = __ldg(G.xf + 3 * (size_t)n), xi1 = __ldg(G.xf + 3 * (size_t)n + 1),
-                xi2 = __ldg(G.xf + 3 * (size_t)n + 2);
-    const int chunk = (threadIdx.x & 31) & 7;
+// Sum over the neighbours of node n (edges [beg, end), their entries from the staged slab
+// segment eb when given) of relu(Q_i + P_j + C e_ij), for the 8 channels [8 chunk, 8 chunk + 8)
+// of this lane, in edge order; the gathers of eight edges are in flight at once.
+constexpr int kAggU = 6;
+__device__ __forceinline__ void aggregate(const Geo& G, const float4* __restrict__ x4, const bf16* __restrict__ P,
+                                          int n, int beg, int end, const unsigned* eb, int eb0, const float* q,
+                                          const float (*cw)[3], int chunk, float* acc) {
+    const float4 xi = __ldg(x4 + n);
 #pragma unroll
     for (int c = 0; c < 8; ++c) acc[c] = 0.f;
-    for (int kb = beg; kb < end; kb += 16) {
-        unsigned nb[4];
-        uint4 pv[4];
-        bool ok[4];
+    for (int kb = beg; kb < end; kb += kAggU) {
+        unsigned nb[kAggU];
+        uint4 pv[kAggU];
+        float4 xj[kAggU];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int k = kb + slot + 4 * r;
-            ok[r] = k < end;
-            nb[r] = ok[r] ? __ldg(G.nbr + k) : 0u;
+        for (int u = 0; u < kAggU; ++u) {
+            const int k = kb + u;
+            nb[u] = k < end ? (eb ? eb[k - eb0] : __ldg(G.nbr + k)) : 0u;
         }
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            pv[r] = make_uint4(0, 0, 0, 0);
-            if (ok[r]) pv[r] = __ldg(reinterpret_cast<const uint4*>(P + (size_t)(nb[r] & NBMASK) * H + 8 * chunk));
+        for (int u = 0; u < kAggU; ++u) {
+            if (kb + u < end) {
+                const int j = (int)(nb[u] & NBMASK);
+                pv[u] = __ldg(reinterpret_cast<const uint4*>(P + (size_t)j * H + 8 * chunk));
+                xj[u] = __ldg(x4 + j);
+            }
         }
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            if (!ok[r]) continue;
+        for (int u = 0; u < kAggU; ++u) {
+            if (kb + u >= end) break;
             float e[3];
-            edge_vec(G, xi0, xi1, xi2, nb[r], e);
-            const uint32_t pw[4] = {pv[r].x, pv[r].y, pv[r].z, pv[r].w};
+            edge_vec4(G, xi, xj[u], nb[u], e);
+            const uint32_t pw[4] = {pv[u].x, pv[u].y, pv[u].z, pv[u].w};
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
                 const float p = (c & 1) ? bfhi(pw[c >> 1]) : bflo(pw[c >> 1]);
                 acc[c] += fmaxf(edge_pre(q[c], p, cw[c][0], cw[c][1], cw[c][2], e), 0.f);
             }
         }
-    }
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 8);
-        acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
     }
 }
 
@@ -454,23 +472,32 @@ __global__ void __launch_bounds__(256, 2) k_net_mp(Fwd a) {
             }
         }
         __syncwarp();
-        // mean message of every node of the slab
-        for (int r = 0; r < 16; ++r) {
-            const int n = n0 + r;
+        // the slab's CSR segment into the h area (free until h is loaded again below)
+        const int st = lane <= 16 ? __ldg(a.G.nstart + min(n0 + lane, N)) : 0;
+        const int sb = __shfl_sync(0xffffffffu, st, 0), se = __shfl_sync(0xffffffffu, st, 16);
+        unsigned* eb = reinterpret_cast<unsigned*>(sh);
+        const bool staged = se - sb <= kEdgeCap;
+        if (staged)
+            for (int k = lane; k < se - sb; k += 32) eb[k] = __ldg(a.G.nbr + sb + k);
+        __syncwarp();
+        // mean message of every node of the slab, four nodes at a time (lanes 8 slot + chunk)
+        for (int it = 0; it < 4; ++it) {
+            const int r = 4 * it + slot, n = n0 + r;
+            const int beg = __shfl_sync(0xffffffffu, st, r), end = __shfl_sync(0xffffffffu, st, r + 1);
+            const int deg = n < N ? end - beg : 0;
             float acc[8];
-            int deg = 0;
             if (n < N) {
                 float q[8];
                 const float4 qa = *reinterpret_cast<const float4*>(sQ + r * LDQ + 8 * chunk);
                 const float4 qb = *reinterpret_cast<const float4*>(sQ + r * LDQ + 8 * chunk + 4);
                 q[0] = qa.x; q[1] = qa.y; q[2] = qa.z; q[3] = qa.w;
                 q[4] = qb.x; q[5] = qb.y; q[6] = qb.z; q[7] = qb.w;
-                aggregate(a.G, a.P_in, n, q, cw, slot, acc, deg);
+                aggregate(a.G, a.x4, a.P_in, n, beg, end, staged ? eb : nullptr, sb, q, cw, chunk, acc);
             } else {
 #pragma unroll
                 for (int c = 0; c < 8; ++c) acc[c] = 0.f;
             }
-            if (slot == 0) {
+            {
                 float m[8];
 #pragma unroll
                 for (int c = 0; c < 8; ++c) m[c] = deg > 0 ? __fdiv_rn(acc[c], (float)deg) : 0.f;
@@ -484,6 +511,8 @@ __global__ void __launch_bounds__(256, 2) k_net_mp(Fwd a) {
                 *reinterpret_cast<uint4*>(sa + r * LD64 + 8 * chunk) = u;
             }
         }
+        __syncwarp();
+        load_slab(sh, LD64, a.h_in, n0, N);
         __syncwarp();
         if (TRAIN) store_slab(a.a_st, sa, LD64, n0, N);
         // h' = h + relu(W_u [h; a] + b_u), in place
@@ -1232,6 +1261,13 @@ int build_graph(Ctx& C) {
     NT_TRY(nalloc(C, &T.d_nstart, (size_t)N + 1));
     NT_TRY(nalloc(C, &T.d_nbr, (size_t)std::max<long long>(w, 1)));
     NT_TRY(nalloc(C, &T.d_act, (size_t)N));
+    {
+        std::vector<float4> x4(N);
+        for (int n = 0; n < N; ++n)
+            x4[n] = make_float4((float)x[3 * (size_t)n], (float)x[3 * (size_t)n + 1], (float)x[3 * (size_t)n + 2], 0.f);
+        NT_TRY(nalloc(C, &T.d_x4, (size_t)N));
+        NT_TRY(check(C, cudaMemcpy(T.d_x4, x4.data(), sizeof(float4) * N, cudaMemcpyHostToDevice), "graph"));
+    }
     NT_TRY(check(C, cudaMemcpy(T.d_nstart, nstart.data(), sizeof(int) * nstart.size(), cudaMemcpyHostToDevice), "graph"));
     if (w > 0) NT_TRY(check(C, cudaMemcpy(T.d_nbr, ent.data(), sizeof(unsigned) * w, cudaMemcpyHostToDevice), "graph"));
     NT_TRY(check(C, cudaMemcpy(T.d_act, act.data(), N, cudaMemcpyHostToDevice), "graph"));
@@ -1286,6 +1322,7 @@ void forward(Ctx& C, const float* v, float* z, const bf16* ctx, bool train) {
     a.ctx = ctx;
     a.act = T.d_act;
     a.G = geo(C);
+    a.x4 = T.d_x4;
     a.s = (float)std::sqrt(5.0 * C.N);
     a.h_out = train ? R.d_hs : T.d_h;
     a.P_out = train ? R.d_ps : T.d_P0;
@@ -1418,6 +1455,10 @@ int net_setup(Ctx& C) {
         NT_TRY(nalloc(C, &T.d_P1, HNs));
     }
     if (!T.d_Z && C.cfg.precision == PHGPU_MIXED) NT_TRY(nalloc(C, &T.d_Z, C.ldU * (size_t)C.Ucap));
+    if (!T.ev0) {
+        NT_TRY(check(C, cudaEventCreate(&T.ev0), "event"));
+        NT_TRY(check(C, cudaEventCreate(&T.ev1), "event"));
+    }
     // persistent grid of the forward kernels: two CTAs per SM (shared memory and 128 registers
     // allow two), 8 slabs of 16 nodes per CTA pass
     const int nslab = (C.N + 15) / 16;
@@ -1453,11 +1494,13 @@ int net_store_pair(Ctx& C, int slot, const float* Aw, const float* w, const doub
 void net_free(Ctx& C) {
     NetCtx& T = C.net;
     NetTrain& R = T.tr;
-    void* ptrs[] = {T.d_nstart, T.d_nbr, T.d_act, T.d_w, T.d_ctx, T.d_stat, T.d_spart, T.d_h, T.d_P0, T.d_P1, T.d_Z,
+    void* ptrs[] = {T.d_nstart, T.d_nbr, T.d_act, T.d_x4, T.d_w, T.d_ctx, T.d_stat, T.d_spart, T.d_h, T.d_P0, T.d_P1, T.d_Z,
                     R.d_pv, R.d_pt, R.d_pctx, R.d_hs, R.d_ps, R.d_as, R.d_qs, R.d_us, R.d_out, R.d_dh, R.d_dms,
                     R.d_dqp, R.d_part, R.d_grad, R.d_m, R.d_v, R.d_scal};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (T.ev0) cudaEventDestroy(T.ev0);
+    if (T.ev1) cudaEventDestroy(T.ev1);
     T = NetCtx{};
 }
 

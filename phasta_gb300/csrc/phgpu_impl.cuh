@@ -138,6 +138,7 @@ struct NetCtx {
     int* d_nstart = nullptr;              // N+1 CSR row starts
     unsigned* d_nbr = nullptr;            // neighbour | periodic shift code << 26
     unsigned char* d_act = nullptr;       // 1: node the network corrects
+    float4* d_x4 = nullptr;               // coordinates (FP32, padded to 16 bytes)
     int nact = 0;
     float L[3] = {0.f, 0.f, 0.f};         // periods of the translational periodicity
     float rh = 1.f;                       // 1 / mean edge length
@@ -156,6 +157,9 @@ struct NetCtx {
     // learned cycles that did not converge within fewer iterations, and the switch they throw
     int its_ref = -1, fails = 0;
     bool disabled = false;
+    double ms_ref_iter = 0.0;             // device time per Krylov iteration of that solve
+    double ms_last = 0.0;                 // device time of the last learned cycle
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     NetTrain tr;
 };
 

@@ -625,6 +625,9 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
     const int ncycles = C.cfg.nGMRES + (use_net ? 1 : 0);
     int its_plain = 0;
     bool net_ok = false;
+    // device time of the cycles: a learned cycle must beat the block-diagonal iterations it replaces
+    const bool timed = want_net && C.net.ev0;
+    if (timed) cudaEventRecord(C.net.ev0, C.stream);
     int iKs = 0;
     for (int mG = 1; mG <= ncycles; ++mG) {
         const bool learned = use_net && mG == 1;
@@ -736,7 +739,15 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
         const bool converged = C.h_scal[S_ECHECK] <= epsnrm;
         if (learned) {
             st->net_its = iKs;
-            net_ok = converged;
+            float ms = 0.f;
+            if (timed) {
+                cudaEventRecord(C.net.ev1, C.stream);
+                cudaEventSynchronize(C.net.ev1);
+                cudaEventElapsedTime(&ms, C.net.ev0, C.net.ev1);
+            }
+            C.net.ms_last = ms;
+            // converged, and faster than the block-diagonal iterations it replaces
+            net_ok = converged && (!timed || C.net.ms_ref_iter <= 0.0 || ms < C.net.its_ref * C.net.ms_ref_iter);
         } else {
             its_plain += iKs;
         }
@@ -751,8 +762,16 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
             C.net.disabled = true;
         }
     } else if (want_net) {
-        // a block-diagonal solve with the learned preconditioner selected: its count is the reference
+        // a block-diagonal solve with the learned preconditioner selected: its count and its time
+        // per iteration are the reference
         C.net.its_ref = its_plain;
+        float ms = 0.f;
+        if (timed) {
+            cudaEventRecord(C.net.ev1, C.stream);
+            cudaEventSynchronize(C.net.ev1);
+            cudaEventElapsedTime(&ms, C.net.ev0, C.net.ev1);
+        }
+        C.net.ms_ref_iter = its_plain > 0 ? ms / its_plain : 0.0;
     }
     (void)done;
     return PHGPU_OK;
@@ -1363,7 +1382,7 @@ int phgpu_set_bc(phgpu_ctx* h, const double* BC) {
     return sync(C);
 }
 
-int phgpu_net_collect(phgpu_ctx* h, int slot) {
+int phgpu_net_collect(phgpu_ctx* h, int slot, int which) {
     using namespace phgpu;
     if (!h) return PHGPU_ERR_INVALID;
     Ctx& C = h->c;
@@ -1371,18 +1390,28 @@ int phgpu_net_collect(phgpu_ctx* h, int slot) {
     if (C.cfg.precision != PHGPU_MIXED || C.cfg.ap_mode != PHGPU_AP_LINEAR)
         return fail(C, PHGPU_ERR_UNSUPPORTED, "training pairs come from a mixed-precision solve with the linearized product");
     if (slot < 0 || slot >= C.net.tr.cap) return fail(C, PHGPU_ERR_INVALID, "pair slot outside the allocated training set");
+    if (which < 0 || which > C.cfg.Kspace) return fail(C, PHGPU_ERR_INVALID, "which: 0 (solution) or a Krylov vector 1..Kspace");
     const size_t n5 = 5 * (size_t)C.N;
-    // features of the solve's state and factors, then w = U Dy (the Krylov-space solution)
+    // features of the solve's state and factors
+    PH_TRY(net_setup(C));
     PH_TRY(net_prepare(C));
-    k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, C.d_t64, n5, nullptr);
-    ++C.launches;
-    lu_apply<double, double>(C, C.d_bd, C.d_t64, PHGPU_LU_PRODUCT);
-    to_f32(C, C.d_t64, C.d_t32b, n5);
-    // A~ w with the operator the Krylov loop multiplies by
-    float* Aw = (float*)C.d_U;
-    PH_TRY(ap_lin<float>(C, C.d_t32b, Aw, nullptr));
-    dot<float>(C, Aw, Aw, n5, S_TMP0, nullptr);
-    PH_TRY(net_store_pair(C, slot, Aw, C.d_t32b, C.d_scal + S_TMP0));
+    float* u = C.d_t32b;
+    if (which == 0) {
+        // w = U Dy, the Krylov-space solution
+        k_copy<double><<<kVG, kVT, 0, C.stream>>>(C.d_Dy, C.d_t64, n5, nullptr);
+        ++C.launches;
+        lu_apply<double, double>(C, C.d_bd, C.d_t64, PHGPU_LU_PRODUCT);
+        to_f32(C, C.d_t64, u, n5);
+    } else {
+        // Krylov vector u_which of the solve's last cycle
+        k_copy<float><<<kVG, kVT, 0, C.stream>>>((const float*)C.d_U + (size_t)(which - 1) * C.ldU, u, n5, nullptr);
+        ++C.launches;
+    }
+    // A~ u with the operator the Krylov loop multiplies by
+    float* Au = C.net.d_Z;
+    PH_TRY(ap_lin<float>(C, u, Au, nullptr));
+    dot<float>(C, Au, Au, n5, S_TMP0, nullptr);
+    PH_TRY(net_store_pair(C, slot, Au, u, C.d_scal + S_TMP0));
     return sync(C);
 }
 
@@ -1666,6 +1695,14 @@ int phgpu_sweep_dev(phgpu_ctx* h, int which) {
         case 5:
             to_f32(C, C.d_y, C.d_yf, n5);
             to_f32(C, C.d_ac, C.d_acf, n5);
+            break;
+        case 17:  // one application of the learned preconditioner (needs weights and a solve's features)
+            if (!net_usable(C) || !C.net.d_Z) return fail(C, PHGPU_ERR_INVALID, "no network weights or features");
+            net_apply(C, C.d_yf, C.net.d_Z);
+            break;
+        case 18:  // the learned preconditioner's context features
+            if (!C.net.d_ctx) return fail(C, PHGPU_ERR_INVALID, "network not set up");
+            PH_TRY(net_prepare(C));
             break;
         case 6:  // FP64-Galerkin / FP32-stabilization residual
             launch_elem_resh(C, C.d_y, C.d_ac, C.d_yf, C.d_acf, C.d_res);

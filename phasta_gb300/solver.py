@@ -406,8 +406,9 @@ class GpuSolver:
     def net_pairs(self, cap: int):
         self._check(self.lib.phgpu_net_pairs(self.h, cap))
 
-    def net_collect(self, slot: int):
-        self._check(self.lib.phgpu_net_collect(self.h, slot))
+    def net_collect(self, slot: int, which: int = 0):
+        """Training pair from the last solve: its solution (which = 0) or Krylov vector ``which``."""
+        self._check(self.lib.phgpu_net_collect(self.h, slot, which))
 
     def net_train(self, epochs: int, lr: float = 1e-3, npairs: int = 0, clip: float = 1.0, seed: int = 1,
                   renormalize: bool = True, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8) -> dict:

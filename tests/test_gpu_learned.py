@@ -226,7 +226,8 @@ def test_learned_cycle_graph_equals_launched_cycle(gpu_lib):
         if no_graph == 0:
             assert g.graph_cycles >= 1
     (d0, s0), (d1, s1) = out
-    assert s0.net_its == s1.net_its and s0.iKs == s1.iKs and s0.net_fallback == s1.net_fallback
+    # the same cycles in the same order (whether the cycle counts as a gain is a timing verdict)
+    assert s0.net_its == s1.net_its and s0.iKs == s1.iKs
     assert np.array_equal(d0, d1)
 
 
