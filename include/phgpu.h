@@ -305,6 +305,9 @@ int phgpu_net_get_weights(phgpu_ctx* ctx, float* w, int n);
 /* the edge graph: nstart (nshg+1), nbr (room for cap; 26-bit neighbour | shift code << 26,
  * code bits 2d..2d+1 = 1: +L_d, 2: -L_d), geo = {L_x, L_y, L_z, 1/hbar}; *nnz = edges */
 int phgpu_net_graph(phgpu_ctx* ctx, int* nstart, unsigned* nbr, long long cap, long long* nnz, float* geo);
+/* solves with precond = PHGPU_PRECOND_LEARNED since create, by outcome: counts[0] learned
+ * cycle used, [1] fell back, [2] block-diagonal only; counts[3] = 1 while the network is off */
+int phgpu_net_usage(phgpu_ctx* ctx, long long* counts);
 /* context features of the resident state and FP32 factored BDiag (after a mixed-precision
  * solve): out (nshg, 32) as floats, may be NULL (computes them only) */
 int phgpu_net_features(phgpu_ctx* ctx, float* out);

@@ -137,6 +137,7 @@ def lib():
         "phgpu_net_get_weights": ([vp, _fp, C.c_int], C.c_int),
         "phgpu_net_graph": ([vp, _ip, C.POINTER(C.c_uint), C.c_longlong, C.POINTER(C.c_longlong), _fp], C.c_int),
         "phgpu_net_features": ([vp, _fp], C.c_int),
+        "phgpu_net_usage": ([vp, C.POINTER(C.c_longlong)], C.c_int),
         "phgpu_net_apply": ([vp, _dp, _dp, _fp, _fp], C.c_int),
         "phgpu_net_loss_grad": ([vp, _dp, _dp, _dp, _fp], C.c_int),
         "phgpu_net_pairs": ([vp, C.c_int], C.c_int),

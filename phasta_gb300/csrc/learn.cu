@@ -1589,6 +1589,16 @@ int phgpu_net_graph(phgpu_ctx* h, int* nstart, unsigned* nbr, long long cap, lon
     return PHGPU_OK;
 }
 
+int phgpu_net_usage(phgpu_ctx* h, long long* counts) {
+    if (!h || !counts) return PHGPU_ERR_INVALID;
+    const phgpu::NetCtx& T = h->c.net;
+    counts[0] = T.n_used;
+    counts[1] = T.n_fell_back;
+    counts[2] = T.n_plain;
+    counts[3] = T.disabled ? 1 : 0;
+    return PHGPU_OK;
+}
+
 int phgpu_net_features(phgpu_ctx* h, float* out) {
     if (!h) return PHGPU_ERR_INVALID;
     Ctx& C = h->c;

@@ -159,6 +159,7 @@ struct NetCtx {
     bool disabled = false;
     double ms_ref_iter = 0.0;             // device time per Krylov iteration of that solve
     double ms_last = 0.0;                 // device time of the last learned cycle
+    long long n_used = 0, n_fell_back = 0, n_plain = 0;  // solves with precond = LEARNED, by outcome
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     NetTrain tr;
 };

@@ -754,6 +754,7 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
         if (converged) break;
     }
     st->iKs = iKs;
+    if (want_net) ++(use_net ? (net_ok ? C.net.n_used : C.net.n_fell_back) : C.net.n_plain);
     if (use_net) {
         st->net_fallback = net_ok ? PHGPU_NET_USED : PHGPU_NET_FELL_BACK;
         if (net_ok) {

@@ -381,6 +381,12 @@ class GpuSolver:
                                              nbr.size, C.byref(nnz), L.fptr(geo)))
         return nstart, nbr[: nnz.value], geo
 
+    def net_usage(self) -> dict:
+        """Solves with the learned preconditioner selected, by outcome, and whether it is switched off."""
+        c = (C.c_longlong * 4)()
+        self._check(self.lib.phgpu_net_usage(self.h, c))
+        return {"used": c[0], "fell_back": c[1], "plain": c[2], "off": bool(c[3])}
+
     def net_features(self) -> np.ndarray:
         out = np.zeros((self.nshg, 32), np.float32)
         self._check(self.lib.phgpu_net_features(self.h, L.fptr(out)))
