@@ -186,7 +186,8 @@ int phgpu_itrres(phgpu_ctx* ctx, const double* yp, const double* yc, const doubl
                  double* rmes);
 /* i3LU on host arrays */
 int phgpu_i3lu(phgpu_ctx* ctx, double* bdiag, double* r, int code);
-/* SolMFG: outputs res = L^-1 R, bdiag = LU factors, Dy */
+/* SolMFG: outputs res = L^-1 R, bdiag = LU factors, Dy (undefined when the status is
+ * PHGPU_ERR_NONFINITE: a GMRES cycle run as a CUDA graph updates Dy before the host sees the flag) */
 int phgpu_solmfg(phgpu_ctx* ctx, const double* y, const double* ac,
                  double* res, double* bdiag, double* Dy, phgpu_stats* st);
 /* itrCorrect + itrBC on host arrays */
@@ -343,7 +344,10 @@ int phgpu_net_train(phgpu_ctx* ctx, const phgpu_net_train_config* cfg, phgpu_net
  * it calls no cudaMalloc, cudaFree or other allocating routine.
  *   - The first call on a device looks up that array's device address
  *     (cudaGetSymbolAddress, with that device current) and caches it; make
- *     that first call before any stream capture.
+ *     that first call before any stream capture.  A cudaDeviceReset of that
+ *     device invalidates the cached address: do not call this entry point on
+ *     it again in the same process after a reset.
+ *   - `stream` must belong to the current device (PHGPU_ERR_INVALID otherwise).
  *   - Returns PHGPU_ERR_TOO_LARGE when 5*nshg > PHGPU_RSTAT_NOALLOC_MAX_N,
  *     PHGPU_ERR_INVALID for null pointers or nshg <= 0, PHGPU_ERR_CUDA when
  *     the address look-up or the launch fails.

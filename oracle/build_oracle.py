@@ -19,7 +19,8 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "libphoracle.so"
 REF_DIR = HERE / "_ref"
 REF_LIB = REF_DIR / "libphref_shape.so"
-REFERENCE = Path(os.environ.get("PHASTA_REFERENCE", "/root/reference"))
+# the reference tree: $PHASTA_REFERENCE, else a directory "reference" beside the repository
+REFERENCE = Path(os.environ.get("PHASTA_REFERENCE", str(HERE.parent.parent / "reference")))
 
 
 def _run(cmd):

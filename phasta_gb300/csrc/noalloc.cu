@@ -103,6 +103,10 @@ extern "C" int phgpu_rstat_noalloc(const double* res, int nshg, double* totres, 
         scratch = g_scratch_ptr[dev];
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the scratch array looked up above belongs to the current device: a stream of another device
+    // would run the kernel there on this device's address
+    int sdev = dev;
+    if (s && cudaStreamGetDevice(s, &sdev) == cudaSuccess && sdev != dev) return PHGPU_ERR_INVALID;
     // the completion counter must start at zero; the partials are all rewritten
     if (cudaMemsetAsync(scratch + kMaxBlocks, 0, sizeof(unsigned long long), s) != cudaSuccess)
         return PHGPU_ERR_CUDA;

@@ -207,6 +207,32 @@ def train_default(out=None, **over) -> dict:
     return {"recipe": cfg, **rep, "file": str(out)}
 
 
+def probe(n: int, reps: int = 3, weights=None) -> dict:
+    """Set the network up on the n^3 x 6 decaying-vortex mesh, run one mixed-precision Newton
+    iteration (its features), then apply the network ``reps`` times and one linearized product
+    (phgpu_sweep_dev 17 and 2): the timing probe the kernel profiles are taken on."""
+    import time as _t
+    from .solver import GpuSolver, make_params
+    case, ph = mesh.periodic_vortex_case(n)
+    p = make_params(ph["mu"], ph["dt"], Kspace=20, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR,
+                    outer_residual=L.PHGPU_RES_SPLITDF, precond=L.PHGPU_PRECOND_LEARNED)
+    g = GpuSolver(case, p)
+    g.net_set_weights(load_weights(weights))
+    y = mesh.vortex_state(case)
+    g.upload(y, np.zeros_like(y), y, np.zeros_like(y))
+    g.newton_dev()
+    g.net_features()
+    g.sweep_dev(5)
+    t0 = _t.perf_counter()
+    for _ in range(reps):
+        g.sweep_dev(17)
+    g.sweep_dev(2)
+    g.download()
+    out = {"n": n, "nodes": case.nshg, "edges": int(len(g.net_graph()[1])), "seconds": _t.perf_counter() - t0}
+    g.close()
+    return out
+
+
 if __name__ == "__main__":
     import argparse
     import json
@@ -217,5 +243,9 @@ if __name__ == "__main__":
     ap.add_argument("--pairs", type=int, default=DEFAULT_RECIPE["pairs"])
     ap.add_argument("--epochs", type=int, default=DEFAULT_RECIPE["epochs"])
     ap.add_argument("--seed", type=int, default=DEFAULT_RECIPE["seed"])
+    ap.add_argument("--probe", type=int, default=0, help="time the trained network on an N^3 x 6 vortex mesh instead")
     a = ap.parse_args()
-    print(json.dumps(train_default(a.out, kind=a.kind, n=a.n, pairs=a.pairs, epochs=a.epochs, seed=a.seed)))
+    if a.probe:
+        print(json.dumps(probe(a.probe)))
+    else:
+        print(json.dumps(train_default(a.out, kind=a.kind, n=a.n, pairs=a.pairs, epochs=a.epochs, seed=a.seed)))

@@ -18,6 +18,7 @@ with the vector order flipped (a zero pivot entry, genbc1.f:70-76).
 from __future__ import annotations
 
 import sys
+import os
 from pathlib import Path
 
 import numpy as np
@@ -27,7 +28,8 @@ sys.path[:0] = [str(HERE)]
 
 import fexec  # noqa: E402
 
-DEFAULT_REF = Path("/root/reference/phSolver")
+# the reference tree: $PHASTA_REFERENCE, else a directory "reference" beside the repository
+DEFAULT_REF = Path(os.environ.get("PHASTA_REFERENCE", str(Path(__file__).resolve().parents[3] / "reference"))) / "phSolver"
 
 
 def inputs(seed=20261204):

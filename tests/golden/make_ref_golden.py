@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import json
 import sys
+import os
 from pathlib import Path
 
 import numpy as np
@@ -25,7 +26,8 @@ sys.path[:0] = [str(HERE), str(ROOT), str(ROOT / "tests")]
 from helpers import channel, mixed, vortex  # noqa: E402
 from refrun import RefPhasta  # noqa: E402
 
-DEFAULT_REF = Path("/root/reference/phSolver")
+# the reference tree: $PHASTA_REFERENCE, else a directory "reference" beside the repository
+DEFAULT_REF = Path(os.environ.get("PHASTA_REFERENCE", str(Path(__file__).resolve().parents[3] / "reference"))) / "phSolver"
 
 # (name, case builder, parts): "elm" ElmMFG; "pieces" ItrRes, i3LU, itrBC; "solve" SolMFG;
 # "step" itrSetup and one two-iteration time step; "sparse" genadj, ElmGMRs (assembled
