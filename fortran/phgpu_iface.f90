@@ -1,6 +1,8 @@
 ! phgpu_iface.f90 -- ISO_C_BINDING interface of include/phgpu.h for a PHASTA
-! build (compressible solver).  Compiled only by a Fortran compiler; the
-! wrappers keep the argument lists of the routines they replace.
+! build (compressible solver): the structs and the bind(C) interfaces of the
+! phgpu_* entry points.  The drop-in replacements of the reference routines,
+! with their own names and argument lists, are in phgpu_shims.f (they use
+! this module).  Compiled only by a Fortran compiler.
 module phgpu_iface
   use iso_c_binding
   implicit none
@@ -52,6 +54,21 @@ module phgpu_iface
        import :: c_int, c_ptr, phgpu_config
        type(c_ptr), value :: ctx
        type(phgpu_config), intent(in) :: cfg
+     end function
+     integer(c_int) function phgpu_destroy(ctx) bind(C, name="phgpu_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function phgpu_set_bc(ctx, BC) bind(C, name="phgpu_set_bc")
+       import :: c_int, c_double, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: BC(*)
+     end function
+     integer(c_int) function phgpu_net_set_weights(ctx, w, n) bind(C, name="phgpu_net_set_weights")
+       import :: c_int, c_float, c_ptr
+       type(c_ptr), value :: ctx
+       real(c_float), intent(in) :: w(*)
+       integer(c_int), value :: n
      end function
      integer(c_int) function phgpu_elmmfg(ctx, y, ac, res, rmes, bdiag, iprec) bind(C, name="phgpu_elmmfg")
        import :: c_int, c_double, c_ptr
