@@ -237,6 +237,52 @@ def wedge_box(n, lengths=(1.0, 1.0, 1.0)) -> Case:
                 meta={"n": n, "lengths": lengths, "periodic": (True, True, True)})
 
 
+def layered(nxy: int, n_hex: int, n_wedge: int, n_tet: int, lengths=(1.0, 1.0, 1.0)) -> Case:
+    """One connected, fully periodic box of nxy x nxy x (n_hex + n_wedge + n_tet) cells whose z
+    layers are, from z = 0 up, hexes, then prisms (two per cell, triangles in the xy planes,
+    the x = y diagonal), then Kuhn tets (six per cell).  Neighbouring layers share their
+    interface nodes: the prisms' top triangles are faces of the tets above (the Kuhn split cuts
+    the horizontal cell faces along the same diagonal), the hexes' top quads carry the prisms'
+    bottom triangles, and the periodic wrap in z joins the tets' top to the hexes' bottom.
+    Node ids follow one (nxy+1)^2 (nz+1) lattice, periodic slaves stored."""
+    nz = n_hex + n_wedge + n_tet
+    n = (nxy, nxy, nz)
+    x, iper, iBC, nid = _grid(n, lengths, (True, True, True))
+    ii, jj = (a.reshape(-1) for a in np.meshgrid(np.arange(nxy), np.arange(nxy), indexing="ij"))
+    corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    hexes, prisms, tets = [], [], []
+    tris = ([(0, 0), (1, 0), (1, 1)], [(0, 0), (1, 1), (0, 1)])
+    for k in range(nz):
+        kk = np.full_like(ii, k)
+        if k < n_hex:
+            hexes.append(np.stack([nid(ii + a, jj + b, kk + c) for a, b, c in corners], axis=1))
+        elif k < n_hex + n_wedge:
+            layer = []
+            for tri in tris:
+                bot = [nid(ii + a, jj + b, kk) for a, b in tri]
+                top = [nid(ii + a, jj + b, kk + 1) for a, b in tri]
+                layer.append(np.stack(bot + top, axis=1))
+            prisms.append(np.stack(layer, axis=1).reshape(-1, 6))
+        else:
+            cell = []
+            for perm in itertools.permutations(range(3)):
+                off = [0, 0, 0]
+                verts = [nid(ii, jj, kk)]
+                for ax in perm:
+                    off[ax] += 1
+                    verts.append(nid(ii + off[0], jj + off[1], kk + off[2]))
+                cell.append(np.stack(verts, axis=1))
+            tets.append(np.stack(cell, axis=1).reshape(-1, 4))
+    cat = lambda lst, w: np.concatenate(lst).astype(np.int32) if lst else np.zeros((0, w), np.int32)  # noqa: E731
+    ien = _orient(cat(tets, 4), x).astype(np.int32) if tets else np.zeros((0, 4), np.int32)
+    h = min(lengths[0] / nxy, lengths[1] / nxy, lengths[2] / nz)
+    return Case(nshg=x.shape[0], x=x, ien=ien, ienb=np.zeros((0, 4), np.int32), iBCB=np.zeros((0, 2), np.int32),
+                BCB=np.zeros((0, 3, 6)), iBC=iBC, BC=np.zeros((6, x.shape[0])), iper=iper, h=h,
+                ienh=cat(hexes, 8), ienw=cat(prisms, 6),
+                meta={"n": n, "lengths": lengths, "periodic": (True, True, True),
+                      "layers": (n_hex, n_wedge, n_tet)})
+
+
 def concat(*cases: Case) -> Case:
     """Disjoint union of meshes (node numbers of each part offset by the nodes before it)."""
     off = 0
@@ -381,6 +427,15 @@ def periodic_vortex_case(n: int, mach: float = 0.1, re: float = 1600.0):
     case = box(n, lengths=(L, L, L), periodic=(True, True, True), inflow=None)
     fs = freestream(mach)
     mu = fs["rho"] * 1.0 * 1.0 / re
+    dt = cfl_dt(case, mach)
+    return case, {"mach": mach, "re": re, "mu": mu, "dt": dt, "fs": fs}
+
+
+def layered_case(nxy: int, n_hex: int, n_wedge: int, n_tet: int, mach: float = 0.3, re: float = 1000.0):
+    """The connected mixed-topology box of ``layered`` with the channel's physics."""
+    case = layered(nxy, n_hex, n_wedge, n_tet)
+    fs = freestream(mach)
+    mu = fs["rho"] * fs["u"] * 1.0 / re
     dt = cfl_dt(case, mach)
     return case, {"mach": mach, "re": re, "mu": mu, "dt": dt, "fs": fs}
 

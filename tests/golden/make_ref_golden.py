@@ -23,7 +23,7 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 sys.path[:0] = [str(HERE), str(ROOT), str(ROOT / "tests")]
 
-from helpers import channel, mixed, vortex  # noqa: E402
+from helpers import channel, layered, mixed, vortex  # noqa: E402
 from refrun import RefPhasta  # noqa: E402
 
 # the reference tree: $PHASTA_REFERENCE, else a directory "reference" beside the repository
@@ -61,6 +61,10 @@ CASES = [
     ("channel4_tau1", lambda: channel(4, ac_scale=0.05, itau=1), ("elm", "pieces", "solve", "sparse")),
     ("mixed3_tau1", lambda: mixed(3, 3, (3, 3, 2), itau=1), ("elm", "pieces")),
     ("wedge3", lambda: mixed(0, 0, (3, 3, 2)), ("elm", "sparse", "ebe")),
+    # one connected mesh whose hex, prism and tet layers share their interface nodes: every
+    # interface node sums contributions of two element topologies
+    ("layered3", lambda: layered(3, (2, 1, 2)), ALL + ("sparse",)),
+    ("layered3_idiff", lambda: layered(3, (1, 1, 1), idiff=1), ("elm", "solve")),
 ]
 
 
