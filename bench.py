@@ -318,10 +318,45 @@ def run_gpu(args, rank, world):
         result["speedup_vs_plain_fp64"] = result["plain_fp64"]["ms_per_step"] / (ms / args.steps)
     if not args.skip_channel:
         result["channel"] = channel_object(args, weights)
+    if not args.skip_mixed:
+        result["mixed_topology"] = mixed_topology_object(args)
     if not args.skip_sparse:
         result["sparse_solver"] = sparse_solver(args)
         result["ebe_solver"] = sparse_solver(args, ebe=True)
     return result
+
+
+def mixed_topology_object(args):
+    """The mixed-topology workload: one connected periodic box of 80 x 80 cells in x, y whose z
+    layers are 80 of hexes (512,000), 4 of prisms (51,200) and 52 of Kuhn tets (1,996,800),
+    sharing their interface nodes; random-phase Fourier velocity modes (k <= 8) at Mach 0.35 with
+    0.1% noise; mixed precision, block-diagonal GMRES, 10 time steps x 3 Newton iterations."""
+    import torch
+
+    from phasta_gb300 import _lib as L
+    from phasta_gb300 import mesh
+    from phasta_gb300.solver import GpuSolver, make_params
+    n = args.mixed_n
+    lay = (n, max(1, n // 20), max(1, (13 * n) // 20))
+    case, ph = mesh.layered_case(n, *lay, mach=0.35)
+    p = make_params(ph["mu"], ph["dt"], rho_inf=0.5, Kspace=20, etol=1e-3, precision=L.PHGPU_MIXED,
+                    ap_mode=L.PHGPU_AP_LINEAR, outer_residual=L.PHGPU_RES_SPLITDF)
+    y0 = mesh.fourier_state(case, 0.35, kmax=8, noise=1e-3)
+    ac0 = np.zeros_like(y0)
+    g = GpuSolver(case, p)
+    s = torch.cuda.ExternalStream(g.stream())
+    g.upload(y0, ac0, y0, ac0)
+    g.time_step_dev(NEWTON_PER_TIMESTEP)
+    steps = 10 * NEWTON_PER_TIMESTEP
+    t = run_newton(g, case, y0, ac0, steps, s)
+    conv, _ = convergence(g, y0, ac0)
+    E = case.nelem + case.nhex + case.nwedge
+    g.close()
+    return {"workload": f"connected periodic box {n}x{n}x{sum(lay)} cells: {case.nhex} hexes, {case.nwedge} prisms, "
+                        f"{case.nelem} tets sharing interface nodes; Fourier modes k<=8 Mach 0.35; 10 time steps x 3 "
+                        f"Newton", "elements": E, "nodes": case.nshg, "value": E * steps / (t["ms"] / 1e3),
+            "unit": "elements/s", "ms_per_step": t["ms"] / steps, "gpu_launches": t["launches"], **conv,
+            "launch": "tets: persistent pipelined kernel per colour; hexes and prisms: one launch per colour"}
 
 
 def channel_object(args, weights):
@@ -578,6 +613,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-channel", action="store_true")
+    ap.add_argument("--skip-mixed", action="store_true")
+    ap.add_argument("--mixed-n", type=int, default=80)
     ap.add_argument("--skip-sparse", action="store_true", help="leave out the assembled-tangent solver lines")
     args = ap.parse_args()
     rank, world, _ = _dist()

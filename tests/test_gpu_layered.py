@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(scope="module")
 def lay(gpu_lib):
-    case, p, y, ac = layered(8, (3, 2, 3))
+    case, p, y, ac = layered(8, (3, 2, 3), Kspace=20)
     return case, p, y, ac, GpuSolver(case, p), pyoracle.Oracle(case, p, nthreads=4)
 
 
