@@ -171,6 +171,16 @@ long long phgpu_kernel_launches(phgpu_ctx* ctx); /* kernels launched since creat
 /* GMRES cycles run as one CUDA graph since create (config no_graph = 0), or -1 when the
  * graph could not be built (phgpu_last_error then gives the reason; cycles run kernel by kernel) */
 long long phgpu_graph_cycles(phgpu_ctx* ctx);
+/* time steps run as one CUDA graph since create, or -1 when the graph could not be built
+ * (phgpu_last_error gives the reason; steps are then launched kernel by kernel).  With
+ * no_graph = 0, phgpu_time_step(_dev) of the mixed-precision block-diagonal matrix-free solver
+ * with nGMRES = 1 and nitr <= 16 runs itrPredict, the nitr Newton iterations (assembly, LU,
+ * the GMRES cycle as conditional nodes opened from the device, back substitution, itrCorrect,
+ * itrBC) and itrUpdate as one graph with one host read of the statistics: the same kernels in
+ * the same order as kernel by kernel, so the state is bitwise the same; phgpu_stats then has
+ * no phase timings (t_assembly_ms = t_gmres_ms = 0), and after a SINGULAR or NONFINITE status
+ * the state of that step is undefined. */
+long long phgpu_step_graphs(phgpu_ctx* ctx);
 
 /* new values BC(nshg, 6) of the Dirichlet constraints (the iBC bits of phgpu_create stay): the
  * reference passes BC to every ElmMFG/SolMFG call (elmmfg.f:1-5, solmfg.f:1-7) */

@@ -107,6 +107,7 @@ def lib():
         "phgpu_num_colors": ([vp], C.c_int),
         "phgpu_kernel_launches": ([vp], C.c_longlong),
         "phgpu_graph_cycles": ([vp], C.c_longlong),
+        "phgpu_step_graphs": ([vp], C.c_longlong),
         "phgpu_elmmfg": ([vp, _dp, _dp, _dp, _dp, _dp, C.c_int], C.c_int),
         "phgpu_elmres": ([vp, _dp, _dp, _dp], C.c_int),
         "phgpu_itrres": ([vp, _dp, _dp, _dp, _dp], C.c_int),

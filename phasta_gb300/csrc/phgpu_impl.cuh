@@ -105,6 +105,26 @@ struct CycleGraph {
     std::string why;
 };
 
+// A whole time step (itrPredict + itrBC, nitr Newton iterations, itrUpdate + itrBC) as one CUDA
+// graph, for the mixed-precision block-diagonal matrix-free solve with one GMRES cycle: the
+// assembly, the LU, the cycle (one conditional node per Krylov iteration, opened from the
+// device) and the update are launched from the graph; the norms and the cycle's decisions stay
+// on the device, and the statistics of every Newton iteration come back in one read.
+struct StepGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    phgpu_config key{};
+    int nitr = 0;
+    long long fixed_launches = 0;     // kernels outside the Krylov iterations
+    long long body_launches = 0;      // kernels of one Krylov iteration
+    bool disabled = false;
+    std::string why;
+    long long runs = 0;
+    cudaStream_t aux = nullptr;       // the stream the Krylov iteration bodies are captured on
+    double* d_stats = nullptr;        // per Newton iteration (8 values, see k_step_record)
+};
+constexpr int kStepGraphMaxNitr = 16;
+
 // The learned right preconditioner of flexible GMRES (learn.cu): the mesh-edge graph of the
 // message-passing network, its weights, per-solve context features, activation buffers,
 // the preconditioned Krylov basis Z, the training set and the fallback state.
@@ -240,6 +260,7 @@ struct Ctx {
     int* d_flag = nullptr;        // [0] converged, [1] error bits, [2] Krylov iterations of the cycle
     CycleGraph cyc;
     CycleGraph cyc_net;           // the learned preconditioner's flexible GMRES cycle
+    StepGraph stepg;              // the whole time step
     NetCtx net;
     int lin_pipe_grid = 1;        // its CTAs per colour launch (resident slots)
     int ress_pipe_grid = 1;       // the same for the pipelined split outer residual

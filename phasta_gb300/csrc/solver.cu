@@ -227,6 +227,45 @@ __global__ void k_init_cycle(double* __restrict__ s, int K, double unorm, double
     }
 }
 
+// k_init_cycle with the norm on the device: unorm = ||L^-1 R|| from S_TMP0, epsnrm = etol unorm
+// (solmfg.f:161); opens the cycle's first Krylov iteration unless the norm is below the
+// early-exit bound (solmfg.f:158), not finite, or the LU reported a pivot failure
+__global__ void k_init_cycle_dev(double* __restrict__ s, int K, double etol, double tiny, int* flag,
+                                 cudaGraphConditionalHandle first) {
+    const int t = threadIdx.x;
+    const double unorm = sqrt(s[S_TMP0]);
+    for (int i = t; i < K + 1; i += blockDim.x) s[S_EB + i] = 0.0;
+    for (int i = t; i < (K + 1) * K; i += blockDim.x) s[S_H + i] = 0.0;
+    if (t == 0) {
+        s[S_EB] = unorm;
+        s[S_UNORM] = unorm;
+        s[S_EPSNRM] = etol * unorm;
+        s[S_ECHECK] = 0.0;
+        flag[0] = 0;
+        flag[2] = 0;
+        flag[3] = K;
+        const bool finite = unorm == unorm && unorm <= 1.7976931348623157e308;
+        if (!finite) flag[1] |= 2;
+        cudaGraphSetConditional(first, (finite && !(unorm < tiny) && flag[1] == 0) ? 1u : 0u);
+    }
+}
+
+// statistics of one Newton iteration of the step graph: [0] ||R||^2, [1] ||L^-1 R||^2, [2] the
+// final |eBrg| of the cycle, [3] its Krylov iterations, [4] the LU status, [5] the error bits
+// after the cycle
+__global__ void k_step_record(const double* __restrict__ s, const int* __restrict__ flag, double* out, int phase) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (phase == 0) {
+        out[0] = s[S_TMP3];
+        out[1] = s[S_TMP0];
+        out[4] = flag[1];
+    } else {
+        out[2] = s[S_ECHECK];
+        out[3] = flag[2];
+        out[5] = flag[1];
+    }
+}
+
 // itrCorrect (itrPC.f:128-148) in the device's local dof order
 __global__ void k_correct(double* __restrict__ y, double* __restrict__ ac, const double* __restrict__ yold,
                           const double* __restrict__ acold, const double* __restrict__ Dy, double fct1,
@@ -778,29 +817,11 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
     return PHGPU_OK;
 }
 
-// SolMFG (solmfg.f) or, with ap_mode PHGPU_AP_SPARSE, SolGMRs (solgmr.f:480): lhs = 1 forms
-// BDiag and the tangent (iprec = lhs, itrdrv.f:456-457); lhs = 0 reuses the factored BDiag
-// and the preconditioned tangent of the last lhs = 1 solve
-int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
+// The assembly part of SolMFG / SolGMRs / SolGMRe on resident data, launches only (no host
+// round trip): residual R (d_res), ||R||^2 (S_TMP3), BDiag and its LU factors (status in flag[1]),
+// L^-1 R in d_res and ||L^-1 R||^2 (S_TMP0); for the matrix-free solver also ypre = U y.
+int assemble_and_factor(Ctx& C, int lhs, bool asm_bd, bool sparse, bool ebe) {
     const size_t N = C.N, n5 = 5 * N;
-    const bool ebe = C.cfg.ap_mode == PHGPU_AP_EBE;
-    const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE || ebe;
-    if (ebe) {
-        if (!lhs) return fail(C, PHGPU_ERR_UNSUPPORTED, "the element-by-element solver assembles on every call");
-        PH_TRY(ebe_setup(C));
-    } else if (sparse) {
-        PH_TRY(sparse_setup(C));
-        if (!lhs && C.sp.have != C.cfg.precision)
-            return fail(C, PHGPU_ERR_INVALID, "lhs = 0 needs the tangent of an earlier lhs = 1 solve");
-    }
-    // discontinuity capturing is in the FP64 residual kernels; the linearized and assembled
-    // products do not carry it
-    if (C.cfg.iDC != 0 && (C.cfg.precision != PHGPU_FP64 || C.cfg.ap_mode != PHGPU_AP_FD))
-        return fail(C, PHGPU_ERR_UNSUPPORTED, "iDC != 0 needs FP64 with the finite-difference product");
-    if (C.cfg.precond == PHGPU_PRECOND_LEARNED && (C.cfg.precision != PHGPU_MIXED || C.cfg.ap_mode != PHGPU_AP_LINEAR))
-        return fail(C, PHGPU_ERR_UNSUPPORTED, "the learned preconditioner needs mixed precision with the linearized product");
-    const bool asm_bd = !sparse || lhs;
-    cudaEventRecord(C.ev[0], C.stream);
     if (C.cfg.precision == PHGPU_FP64) {
         if (sparse) {
             // ElmGMRs / ElmGMRe: the residual, and BDiag from the tangent's diagonal blocks
@@ -876,8 +897,35 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
         ++C.launches;
         lu_apply<double, double>(C, C.d_bd, C.d_ypre, PHGPU_LU_PRODUCT);
     }
-    // ||L^-1 R|| for GMRES, read with the LU status and ||R|| in one host round trip
+    // ||L^-1 R|| for GMRES
     dot<double>(C, C.d_res, C.d_res, n5, S_TMP0, nullptr);
+    return PHGPU_OK;
+}
+
+// SolMFG (solmfg.f) or, with ap_mode PHGPU_AP_SPARSE, SolGMRs (solgmr.f:480): lhs = 1 forms
+// BDiag and the tangent (iprec = lhs, itrdrv.f:456-457); lhs = 0 reuses the factored BDiag
+// and the preconditioned tangent of the last lhs = 1 solve
+int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
+    const size_t N = C.N, n5 = 5 * N;
+    const bool ebe = C.cfg.ap_mode == PHGPU_AP_EBE;
+    const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE || ebe;
+    if (ebe) {
+        if (!lhs) return fail(C, PHGPU_ERR_UNSUPPORTED, "the element-by-element solver assembles on every call");
+        PH_TRY(ebe_setup(C));
+    } else if (sparse) {
+        PH_TRY(sparse_setup(C));
+        if (!lhs && C.sp.have != C.cfg.precision)
+            return fail(C, PHGPU_ERR_INVALID, "lhs = 0 needs the tangent of an earlier lhs = 1 solve");
+    }
+    // discontinuity capturing is in the FP64 residual kernels; the linearized and assembled
+    // products do not carry it
+    if (C.cfg.iDC != 0 && (C.cfg.precision != PHGPU_FP64 || C.cfg.ap_mode != PHGPU_AP_FD))
+        return fail(C, PHGPU_ERR_UNSUPPORTED, "iDC != 0 needs FP64 with the finite-difference product");
+    if (C.cfg.precond == PHGPU_PRECOND_LEARNED && (C.cfg.precision != PHGPU_MIXED || C.cfg.ap_mode != PHGPU_AP_LINEAR))
+        return fail(C, PHGPU_ERR_UNSUPPORTED, "the learned preconditioner needs mixed precision with the linearized product");
+    const bool asm_bd = !sparse || lhs;
+    cudaEventRecord(C.ev[0], C.stream);
+    PH_TRY(assemble_and_factor(C, lhs, asm_bd, sparse, ebe));
     PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
     PH_TRY(check(C, cudaMemcpyAsync(C.h_scal, C.d_scal, sizeof(double) * 8, cudaMemcpyDeviceToHost, C.stream), "rn"));
     PH_TRY(sync(C));
@@ -967,7 +1015,196 @@ int newton_dev(Ctx& C, phgpu_stats* st) {
     return PHGPU_OK;
 }
 
+// ---------------------------------------------------------------------------
+// the whole time step as one CUDA graph (StepGraph)
+// ---------------------------------------------------------------------------
+bool step_graph_eligible(const Ctx& C, int nitr) {
+    const phgpu_config& c = C.cfg;
+    return !c.no_graph && c.precision == PHGPU_MIXED && c.ap_mode == PHGPU_AP_LINEAR &&
+           c.precond == PHGPU_PRECOND_BDIAG && c.nGMRES == 1 && c.iDC == 0 && nitr >= 1 &&
+           nitr <= kStepGraphMaxNitr && !C.stepg.disabled;
+}
+
+void step_graph_free(StepGraph& G) {
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    if (G.graph) cudaGraphDestroy(G.graph);
+    G.exec = nullptr;
+    G.graph = nullptr;
+}
+
+// Capture itrPredict + itrBC, nitr Newton iterations (assembly and LU, one GMRES cycle whose Krylov
+// iterations are conditional nodes, back substitution, update, U^-1, itrCorrect + itrBC) and
+// itrUpdate + itrBC: the kernels of time_step_dev in the same order with the same arguments,
+// the cycle's norms read on the device instead of on the host.
+int step_graph_build(Ctx& C, int nitr) {
+    StepGraph& G = C.stepg;
+    const size_t n5 = 5 * (size_t)C.N;
+    const int K = C.cfg.Kspace;
+    if (!G.d_stats && cudaMalloc((void**)&G.d_stats, sizeof(double) * 8 * kStepGraphMaxNitr) != cudaSuccess)
+        return fail(C, PHGPU_ERR_NOMEM, "step graph statistics");
+    if (!G.aux) PH_TRY(check(C, cudaStreamCreateWithFlags(&G.aux, cudaStreamNonBlocking), "step graph stream"));
+    // host set-up the assembly does on its first call, outside the capture
+    if (C.cfg.outer_residual == PHGPU_RES_SPLITDF && (C.nhex > 0 || C.nwedge > 0)) PH_TRY(topo_split_setup(C));
+    PH_TRY(sync(C));
+    step_graph_free(G);
+    float* U = (float*)C.d_U;
+    auto Uj = [&](int j) { return U + (size_t)(j - 1) * C.ldU; };
+    double* s = C.d_scal;
+    const phgpu_config c = C.cfg;
+    const double tiny = 100. * c.epsM * c.epsM;
+    cudaStream_t st0 = C.stream;
+    const long long l0 = C.launches;
+    long long body = 0;
+    int rc = PHGPU_OK;
+    cudaError_t e = cudaStreamBeginCapture(st0, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+        k_predict<<<kVG, kVT, 0, st0>>>(C.d_yold, C.d_acold, C.d_y, C.d_ac, 1.0 - c.almi / c.gami, n5);
+        ++C.launches;
+        itrbc_state(C, C.d_y, C.d_ac, true);
+        for (int it = 1; it <= nitr && rc == PHGPU_OK && e == cudaSuccess; ++it) {
+            double* out = G.d_stats + 8 * (it - 1);
+            rc = assemble_and_factor(C, 1, true, false, false);
+            if (rc != PHGPU_OK) break;
+            k_step_record<<<1, 1, 0, st0>>>(s, C.d_flag, out, 0);
+            ++C.launches;
+            fill0(C, C.d_Dy, sizeof(double) * n5);
+            to_f32(C, C.d_res, Uj(1), n5);
+            cudaStreamCaptureStatus cs;
+            cudaGraph_t g = nullptr;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t nd = 0;
+            e = cudaStreamGetCaptureInfo(st0, &cs, nullptr, &g, &deps, nullptr, &nd);
+            std::vector<cudaGraphConditionalHandle> h(K + 2, 0);
+            for (int i = 1; i <= K && e == cudaSuccess; ++i)
+                e = cudaGraphConditionalHandleCreate(&h[i], g, 0u, cudaGraphCondAssignDefault);
+            if (e != cudaSuccess) break;
+            k_init_cycle_dev<<<1, 256, 0, st0>>>(s, K, c.etol, tiny, C.d_flag, h[1]);
+            ++C.launches;
+            scale_by<float>(C, Uj(1), s + S_UNORM, 0, n5, nullptr);
+            e = cudaStreamGetCaptureInfo(st0, &cs, nullptr, &g, &deps, nullptr, &nd);
+            if (e != cudaSuccess) break;
+            std::vector<cudaGraphNode_t> prev(deps, deps + nd);
+            cudaGraphNode_t node = nullptr;
+            for (int i = 1; i <= K && e == cudaSuccess && rc == PHGPU_OK; ++i) {
+                cudaGraphNodeParams p{};
+                p.type = cudaGraphNodeTypeConditional;
+                p.conditional.handle = h[i];
+                p.conditional.type = cudaGraphCondTypeIf;
+                p.conditional.size = 1;
+                e = cudaGraphAddNode(&node, g, prev.data(), nullptr, prev.size(), &p);
+                if (e != cudaSuccess) break;
+                cudaGraph_t bodyg = p.conditional.phGraph_out[0];
+                e = cudaStreamBeginCaptureToGraph(G.aux, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+                if (e != cudaSuccess) break;
+                C.stream = G.aux;
+                const long long lb = C.launches;
+                rc = krylov_step<float>(C, i, c.minIters, false, false, h[i + 1], i < K ? 1 : 0, false);
+                C.stream = st0;
+                body = C.launches - lb;
+                C.launches = lb;
+                cudaGraph_t captured = nullptr;
+                const cudaError_t e2 = cudaStreamEndCapture(G.aux, &captured);
+                if (e2 != cudaSuccess) e = e2;
+                prev.assign(1, node);
+            }
+            if (e != cudaSuccess || rc != PHGPU_OK) break;
+            e = cudaStreamUpdateCaptureDependencies(st0, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+            if (e != cudaSuccess) break;
+            k_backsolve<<<1, 1, 0, st0>>>(s, K, 0, C.d_flag + 2);
+            k_update_dy<float><<<kVG, kVT, 0, st0>>>(C.d_Dy, U, C.ldU, 0, K, s, n5, C.d_flag + 2);
+            k_step_record<<<1, 1, 0, st0>>>(s, C.d_flag, out, 1);
+            C.launches += 3;
+            lu_apply<double, double>(C, C.d_bd, C.d_Dy, PHGPU_LU_BACKWARD);
+            rc = correct_dev(C);
+        }
+        if (e == cudaSuccess && rc == PHGPU_OK) {
+            k_update<<<kVG, kVT, 0, st0>>>(C.d_yold, C.d_acold, C.d_y, C.d_ac, 1.0 / c.almi, 1.0 / c.alfi, n5);
+            ++C.launches;
+            itrbc_state(C, C.d_yold, C.d_acold, true);
+        }
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e3 = cudaStreamEndCapture(st0, &graph);
+        if (e == cudaSuccess) e = e3;
+        G.graph = graph;
+    }
+    C.stream = st0;
+    G.fixed_launches = C.launches - l0;
+    G.body_launches = body;
+    C.launches = l0;
+    if (e == cudaSuccess && rc == PHGPU_OK) e = cudaGraphInstantiate(&G.exec, G.graph, 0);
+    if (e != cudaSuccess || rc != PHGPU_OK) {
+        (void)cudaGetLastError();
+        step_graph_free(G);
+        if (rc != PHGPU_OK) return rc;
+        G.why = std::string("step graph: ") + cudaGetErrorString(e);
+        G.disabled = true;
+        return PHGPU_ERR_CUDA;
+    }
+    G.key = c;
+    G.key.iter = G.key.istep = 0;
+    G.key.eGMRES = 0.0;
+    G.nitr = nitr;
+    return PHGPU_OK;
+}
+
+// one time step through the graph; *used = false when the graph could not be built (the caller
+// then launches the step kernel by kernel)
+int step_graph_run(Ctx& C, int nitr, phgpu_stats* st, bool* used) {
+    StepGraph& G = C.stepg;
+    *used = false;
+    phgpu_config key = C.cfg;
+    key.iter = key.istep = 0;
+    key.eGMRES = 0.0;
+    if (!G.exec || G.nitr != nitr || std::memcmp(&G.key, &key, sizeof key) != 0) {
+        const int rc = step_graph_build(C, nitr);
+        if (rc != PHGPU_OK) {
+            if (G.disabled) {
+                C.err.clear();
+                return PHGPU_OK;
+            }
+            return rc;
+        }
+    }
+    PH_TRY(check(C, cudaGraphLaunch(G.exec, C.stream), "step graph launch"));
+    *used = true;
+    ++G.runs;
+    double out[8 * kStepGraphMaxNitr];
+    PH_TRY(check(C, cudaMemcpyAsync(out, G.d_stats, sizeof(double) * 8 * nitr, cudaMemcpyDeviceToHost, C.stream),
+                 "step statistics"));
+    PH_TRY(sync(C));
+    long long iks_tot = 0;
+    for (int it = 0; it < nitr; ++it) {
+        const double* o = out + 8 * it;
+        if (o[4] != 0.0) return fail(C, PHGPU_ERR_SINGULAR, "zero or non-finite pivot in the block-diagonal LU");
+        if (((int)o[5]) & 2) return fail(C, PHGPU_ERR_NONFINITE, "non-finite value in GMRES");
+        iks_tot += (long long)o[3];
+    }
+    const double* o = out + 8 * (nitr - 1);
+    st->iKs = (int)o[3];
+    st->lGMRES = 0;
+    st->ntotGM += (int)iks_tot;
+    st->unorm0 = std::sqrt(o[1]);
+    st->totres = st->unorm0 / (double)C.N;
+    st->echeck = o[2];
+    st->rnorm = std::sqrt(o[0]);
+    st->eGMRES = C.cfg.eGMRES;
+    st->t_assembly_ms = st->t_gmres_ms = 0.0;
+    st->net_its = 0;
+    st->net_fallback = PHGPU_NET_PLAIN;
+    st->status = PHGPU_OK;
+    C.launches += G.fixed_launches + iks_tot * G.body_launches;
+    C.cyc.runs += nitr;  // each Newton iteration's GMRES cycle ran as (part of) a graph
+    C.cfg.iter = nitr;
+    C.cfg.istep += 1;
+    return PHGPU_OK;
+}
+
 int time_step_dev(Ctx& C, int nitr, phgpu_stats* st) {
+    if (step_graph_eligible(C, nitr)) {
+        bool used = false;
+        PH_TRY(step_graph_run(C, nitr, st, &used));
+        if (used) return PHGPU_OK;
+    }
     const size_t n5 = 5 * (size_t)C.N;
     const phgpu_config& c = C.cfg;
     k_predict<<<kVG, kVT, 0, C.stream>>>(C.d_yold, C.d_acold, C.d_y, C.d_ac, 1.0 - c.almi / c.gami, n5);
@@ -1200,6 +1437,10 @@ int phgpu_destroy(phgpu_ctx* h) {
     if (C.stream) cudaStreamSynchronize(C.stream);
     phgpu::cycle_graph_free(C);
     phgpu::net_free(C);
+    if (C.stepg.exec) cudaGraphExecDestroy(C.stepg.exec);
+    if (C.stepg.graph) cudaGraphDestroy(C.stepg.graph);
+    if (C.stepg.d_stats) cudaFree(C.stepg.d_stats);
+    if (C.stepg.aux) cudaStreamDestroy(C.stepg.aux);
     void* ptrs[] = {C.d_ch_elem, C.d_ch_node, C.d_ch_nodes, C.d_ch_cstart, C.d_ch_csr, C.d_ch_lien,
                     C.d_bdstage, C.d_ien, C.d_ienh, C.d_ienw, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_xlo, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
                     C.d_slaves, C.d_mst, C.d_slv_start, C.d_slv, C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_res,
@@ -1244,6 +1485,15 @@ const char* phgpu_last_error(phgpu_ctx* h) { return h ? h->c.err.c_str() : "null
 void* phgpu_stream(phgpu_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
 int phgpu_num_colors(phgpu_ctx* h) { return h ? (int)h->c.chunk_col_start.size() - 1 : 0; }
 long long phgpu_kernel_launches(phgpu_ctx* h) { return h ? h->c.launches : 0; }
+
+long long phgpu_step_graphs(phgpu_ctx* h) {
+    if (!h) return 0;
+    if (h->c.stepg.disabled) {
+        h->c.err = h->c.stepg.why;
+        return -1;
+    }
+    return h->c.stepg.runs;
+}
 
 long long phgpu_graph_cycles(phgpu_ctx* h) {
     if (!h) return 0;

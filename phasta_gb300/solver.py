@@ -194,6 +194,11 @@ class GpuSolver:
         """GMRES cycles run as one CUDA graph (-1: the graph could not be built)."""
         return self.lib.phgpu_graph_cycles(self.h)
 
+    @property
+    def step_graphs(self) -> int:
+        """Time steps run as one CUDA graph (-1: the graph could not be built)."""
+        return self.lib.phgpu_step_graphs(self.h)
+
     def stream(self) -> int:
         return self.lib.phgpu_stream(self.h)
 
