@@ -192,19 +192,29 @@ __global__ void k_periodic_copy(const int* __restrict__ slaves, int ns, const in
 // The factorization follows i3lu.f:41-97 statement by statement, including
 // that U(4,5) is left at its input value (the reference updates every other
 // upper entry of rows 2-5 but not that one).
+// The factors of the blocks in `in` (type I) are written to bd (type R) and, when given, to bdf
+// as floats; in may be bd or bdf.  The block's 25 x kLuT values are staged through one shared
+// buffer in both directions (read in, factored in registers, written back), so the global reads
+// and writes are contiguous (one thread per node would read and write at a stride of 25
+// values); the arithmetic per node is unchanged.
+constexpr int kLuT = 128;
 template <typename R, typename I>
-// the factors of the blocks in `in` (type I) are written to bd (type R) and, when given, to bdf
-// as floats; in may be bd or bdf (each thread reads its block before writing it)
-__global__ void k_lu_fact(const I* in, R* bd, float* bdf, int N, int* __restrict__ flag) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
+__global__ void __launch_bounds__(kLuT) k_lu_fact(const I* in, R* bd, float* bdf, int N, int* __restrict__ flag) {
+    __shared__ __align__(16) unsigned char s_buf[25 * kLuT * 8];
+    I* s_in = reinterpret_cast<I*>(s_buf);
+    R* s_out = reinterpret_cast<R*>(s_buf);
+    const int n0 = blockIdx.x * kLuT, t = threadIdx.x;
+    const int nb = min(kLuT, N - n0);
+    const size_t base = 25 * (size_t)n0;
+    for (int k = t; k < 25 * nb; k += kLuT) s_in[k] = in[base + k];
+    __syncthreads();
+    const int n = n0 + t;
     R a[5][5];
-    R* p = bd + 25 * (size_t)n;
-    const I* pi = in + 25 * (size_t)n;
 #pragma unroll
     for (int i = 0; i < 5; ++i)
 #pragma unroll
-        for (int j = 0; j < 5; ++j) a[i][j] = (R)pi[5 * i + j];
+        for (int j = 0; j < 5; ++j) a[i][j] = t < nb ? (R)s_in[25 * t + 5 * i + j] : (i == j ? R(1) : R(0));
+    __syncthreads();
     bool bad = false;
     auto inv = [&](R v) {
         if (!(v == v) || v == R(0) || isinf(v)) bad = true;
@@ -237,15 +247,14 @@ __global__ void k_lu_fact(const I* in, R* bd, float* bdf, int N, int* __restrict
 #pragma unroll
     for (int i = 0; i < 5; ++i)
 #pragma unroll
-        for (int j = 0; j < 5; ++j) p[5 * i + j] = a[i][j];
-    if (bdf) {
-        float* pf = bdf + 25 * (size_t)n;
-#pragma unroll
-        for (int i = 0; i < 5; ++i)
-#pragma unroll
-            for (int j = 0; j < 5; ++j) pf[5 * i + j] = (float)a[i][j];
+        for (int j = 0; j < 5; ++j) s_out[25 * t + 5 * i + j] = a[i][j];
+    __syncthreads();
+    for (int k = t; k < 25 * nb; k += kLuT) {
+        const R v = s_out[k];
+        bd[base + k] = v;
+        if (bdf) bdf[base + k] = (float)v;
     }
-    if (bad && flag) atomicOr(flag + 1, 1);
+    if (bad && flag && n < N) atomicOr(flag + 1, 1);
 }
 
 // in and out may be the same array (each thread reads its node's five values before writing them)
@@ -581,14 +590,14 @@ void itrbc_state(Ctx& C, double* y, double* ac, bool with_ac) {
 
 template <typename R>
 void lu_fact(Ctx& C, R* bd, int* flag) {
-    k_lu_fact<R, R><<<nblocks(C.N), kT, 0, C.stream>>>(bd, bd, nullptr, C.N, flag);
+    k_lu_fact<R, R><<<(C.N + kLuT - 1) / kLuT, kLuT, 0, C.stream>>>(bd, bd, nullptr, C.N, flag);
     ++C.launches;
 }
 template void lu_fact<double>(Ctx&, double*, int*);
 template void lu_fact<float>(Ctx&, float*, int*);
 
 void lu_fact_f32(Ctx& C, float* bdf, double* bd, int* flag) {
-    k_lu_fact<double, float><<<nblocks(C.N), kT, 0, C.stream>>>(bdf, bd, bdf, C.N, flag);
+    k_lu_fact<double, float><<<(C.N + kLuT - 1) / kLuT, kLuT, 0, C.stream>>>(bdf, bd, bdf, C.N, flag);
     ++C.launches;
 }
 

@@ -116,7 +116,7 @@ struct StepGraph {
     phgpu_config key{};
     int nitr = 0;
     long long fixed_launches = 0;     // kernels outside the Krylov iterations
-    long long body_launches = 0;      // kernels of one Krylov iteration
+    std::vector<long long> body_launches;  // kernels of Krylov iteration i (1-based)
     bool disabled = false;
     std::string why;
     long long runs = 0;

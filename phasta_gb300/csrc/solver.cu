@@ -1054,7 +1054,7 @@ int step_graph_build(Ctx& C, int nitr) {
     const double tiny = 100. * c.epsM * c.epsM;
     cudaStream_t st0 = C.stream;
     const long long l0 = C.launches;
-    long long body = 0;
+    std::vector<long long> body(K + 1, 0);
     int rc = PHGPU_OK;
     cudaError_t e = cudaStreamBeginCapture(st0, cudaStreamCaptureModeRelaxed);
     if (e == cudaSuccess) {
@@ -1100,7 +1100,7 @@ int step_graph_build(Ctx& C, int nitr) {
                 const long long lb = C.launches;
                 rc = krylov_step<float>(C, i, c.minIters, false, false, h[i + 1], i < K ? 1 : 0, false);
                 C.stream = st0;
-                body = C.launches - lb;
+                body[i] = C.launches - lb;
                 C.launches = lb;
                 cudaGraph_t captured = nullptr;
                 const cudaError_t e2 = cudaStreamEndCapture(G.aux, &captured);
@@ -1132,6 +1132,7 @@ int step_graph_build(Ctx& C, int nitr) {
     G.body_launches = body;
     C.launches = l0;
     if (e == cudaSuccess && rc == PHGPU_OK) e = cudaGraphInstantiate(&G.exec, G.graph, 0);
+    // fixed part: everything but the Krylov iteration bodies (they were taken out as captured)
     if (e != cudaSuccess || rc != PHGPU_OK) {
         (void)cudaGetLastError();
         step_graph_free(G);
@@ -1172,12 +1173,14 @@ int step_graph_run(Ctx& C, int nitr, phgpu_stats* st, bool* used) {
     PH_TRY(check(C, cudaMemcpyAsync(out, G.d_stats, sizeof(double) * 8 * nitr, cudaMemcpyDeviceToHost, C.stream),
                  "step statistics"));
     PH_TRY(sync(C));
-    long long iks_tot = 0;
+    long long iks_tot = 0, body = 0;
     for (int it = 0; it < nitr; ++it) {
         const double* o = out + 8 * it;
         if (o[4] != 0.0) return fail(C, PHGPU_ERR_SINGULAR, "zero or non-finite pivot in the block-diagonal LU");
         if (((int)o[5]) & 2) return fail(C, PHGPU_ERR_NONFINITE, "non-finite value in GMRES");
-        iks_tot += (long long)o[3];
+        const int iks = (int)o[3];
+        iks_tot += iks;
+        for (int i = 1; i <= iks && i < (int)G.body_launches.size(); ++i) body += G.body_launches[i];
     }
     const double* o = out + 8 * (nitr - 1);
     st->iKs = (int)o[3];
@@ -1192,7 +1195,7 @@ int step_graph_run(Ctx& C, int nitr, phgpu_stats* st, bool* used) {
     st->net_its = 0;
     st->net_fallback = PHGPU_NET_PLAIN;
     st->status = PHGPU_OK;
-    C.launches += G.fixed_launches + iks_tot * G.body_launches;
+    C.launches += G.fixed_launches + body;
     C.cyc.runs += nitr;  // each Newton iteration's GMRES cycle ran as (part of) a graph
     C.cfg.iter = nitr;
     C.cfg.istep += 1;
