@@ -173,34 +173,70 @@ const Topo& topo(int lcsyst) {
 // e3.f for one element (lhs = 0, idiff = 0, iLES = iRANS = iLSet = 0, iDC = 0,
 // no body force, ipord = 1, itau = 0)
 // ---------------------------------------------------------------------------
-void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const double (*yl)[5],
-                const double (*ycl)[5], const double (*acl)[5], const double (*xl)[3],
-                double (*rl)[5], double (*rml)[5], double (*bdl)[5][5], const double (*ql)[12] = nullptr,
-                double* EG = nullptr) {
+// ---------------------------------------------------------------------------
+// e3 (e3.f and the routines it calls) for one element, generic in the scalar type: R = double is
+// the oracle; R = Flop counts the floating-point operations of the reference formulation
+// (or_e3_flops).  sqrt, max and min go through these overloads.
+// ---------------------------------------------------------------------------
+inline double osqrt(double x) { return std::sqrt(x); }
+inline double omax(double a, double b) { return std::max(a, b); }
+inline double omin(double a, double b) { return std::min(a, b); }
+
+// counting scalar: every +, -, *, / and sqrt of two operands counts one operation
+struct Flop {
+    double v = 0.0;
+    Flop() = default;
+    Flop(double x) : v(x) {}  // NOLINT: constants and table values enter the arithmetic
+};
+thread_local long long g_flops = 0;
+inline Flop operator+(Flop a, Flop b) { ++g_flops; return Flop(a.v + b.v); }
+inline Flop operator-(Flop a, Flop b) { ++g_flops; return Flop(a.v - b.v); }
+inline Flop operator*(Flop a, Flop b) { ++g_flops; return Flop(a.v * b.v); }
+inline Flop operator/(Flop a, Flop b) { ++g_flops; return Flop(a.v / b.v); }
+inline Flop operator-(Flop a) { return Flop(-a.v); }
+inline Flop& operator+=(Flop& a, Flop b) { a = a + b; return a; }
+inline Flop& operator-=(Flop& a, Flop b) { a = a - b; return a; }
+inline Flop& operator*=(Flop& a, Flop b) { a = a * b; return a; }
+inline Flop& operator/=(Flop& a, Flop b) { a = a / b; return a; }
+inline bool operator<(Flop a, Flop b) { return a.v < b.v; }
+inline bool operator>(Flop a, Flop b) { return a.v > b.v; }
+inline bool operator<=(Flop a, Flop b) { return a.v <= b.v; }
+inline bool operator>=(Flop a, Flop b) { return a.v >= b.v; }
+inline bool operator==(Flop a, Flop b) { return a.v == b.v; }
+inline bool operator!=(Flop a, Flop b) { return a.v != b.v; }
+inline Flop osqrt(Flop x) { ++g_flops; return Flop(std::sqrt(x.v)); }
+inline Flop omax(Flop a, Flop b) { return Flop(std::max(a.v, b.v)); }
+inline Flop omin(Flop a, Flop b) { return Flop(std::min(a.v, b.v)); }
+
+template <class R>
+void e3_element_t(const or_common& c, const Topo& tp, int ires, int iprec, const R (*yl)[5],
+                const R (*ycl)[5], const R (*acl)[5], const R (*xl)[3],
+                R (*rl)[5], R (*rml)[5], R (*bdl)[5][5], const R (*ql)[12],
+                R* EG) {
     const int nshl = tp.nshl, nenl = tp.nshl, ngauss = tp.ngauss;
-    const double Rgas = c.Rgas, gamma = c.gamma, gamma1 = c.gamma1;
+    const R Rgas = c.Rgas, gamma = c.gamma, gamma1 = c.gamma1;
 
     for (int intp = 0; intp < ngauss; ++intp) {
         if (tp.Qwt[intp] == zero) continue;  // e3.f:110
         const double* shape = tp.shp[intp];
         const double (*shgl)[8] = tp.shgl[intp];
-        double ri[20] = {0}, rmi[20] = {0};
+        R ri[20] = {0}, rmi[20] = {0};
 
         // ---------------- e3ivar.f:96-156 ----------------
-        double dui[5] = {0, 0, 0, 0, 0};
+        R dui[5] = {0, 0, 0, 0, 0};
         for (int n = 0; n < nshl; ++n)
             for (int k = 0; k < 5; ++k) dui[k] = dui[k] + shape[n] * yl[n][k];
-        double rk = pt5 * (dui[1] * dui[1] + dui[2] * dui[2] + dui[3] * dui[3]);
+        R rk = pt5 * (dui[1] * dui[1] + dui[2] * dui[2] + dui[3] * dui[3]);
         {   // getthm ithm=6 (getthm.f:103-148): pres=dui(1), T=dui(5)
-            double rho6 = dui[0] / (Rgas * dui[4]);
-            double ei6 = dui[4] * (Rgas / gamma1);
+            R rho6 = dui[0] / (Rgas * dui[4]);
+            R ei6 = dui[4] * (Rgas / gamma1);
             dui[0] = rho6;
             dui[1] = rho6 * dui[1];
             dui[2] = rho6 * dui[2];
             dui[3] = rho6 * dui[3];
             dui[4] = rho6 * (ei6 + rk);
         }
-        double pres = 0, u1 = 0, u2 = 0, u3 = 0, Tq = 0;
+        R pres = 0, u1 = 0, u2 = 0, u3 = 0, Tq = 0;
         for (int n = 0; n < nshl; ++n) {
             pres = pres + shape[n] * ycl[n][0];
             u1 = u1 + shape[n] * ycl[n][1];
@@ -208,37 +244,37 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             u3 = u3 + shape[n] * ycl[n][3];
             Tq = Tq + shape[n] * ycl[n][4];
         }
-        double aci[5] = {0, 0, 0, 0, 0};
+        R aci[5] = {0, 0, 0, 0, 0};
         for (int n = 0; n < nshl; ++n)
             for (int k = 0; k < 5; ++k) aci[k] = aci[k] + shape[n] * acl[n][k];
         rk = pt5 * (u1 * u1 + u2 * u2 + u3 * u3);
         // getthm ithm=7 (getthm.f:111, 148, 157-171)
-        const double rho = pres / (Rgas * Tq);
-        const double ei = Tq * (Rgas / gamma1);
-        const double h = Tq * (Rgas * gamma / gamma1);
-        const double cv = Rgas / gamma1;
-        const double cp = Rgas * gamma / gamma1;
-        const double alfap = one / Tq;
-        const double betaT = one / pres;
+        const R rho = pres / (Rgas * Tq);
+        const R ei = Tq * (Rgas / gamma1);
+        const R h = Tq * (Rgas * gamma / gamma1);
+        const R cv = Rgas / gamma1;
+        const R cp = Rgas * gamma / gamma1;
+        const R alfap = one / Tq;
+        const R betaT = one / pres;
         // getDiff (getdiff.f:127, 164, 171, 258-261): constant mu, Stokes, no eddy viscosity
-        double rmu = c.rmu;
-        double rlm = -pt66 * rmu;
-        double con = rmu * cp / c.pr;
-        const double xmut = 0.0;
+        R rmu = c.rmu;
+        R rlm = -pt66 * rmu;
+        R con = rmu * cp / c.pr;
+        const R xmut = 0.0;
         rlm = rlm - pt66 * xmut;
         rmu = rmu + xmut;
-        const double rlm2mu = rlm + two * rmu;
+        const R rlm2mu = rlm + two * rmu;
         con = con + xmut * cp / c.pr;
         // e3metric (e3metric.f:22-77)
-        double dxdxi[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        R dxdxi[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         for (int n = 0; n < nenl; ++n)
             for (int i = 0; i < 3; ++i)
                 for (int j = 0; j < 3; ++j) dxdxi[i][j] = dxdxi[i][j] + xl[n][i] * shgl[j][n];
-        double dxidx[3][3];
+        R dxidx[3][3];
         dxidx[0][0] = dxdxi[1][1] * dxdxi[2][2] - dxdxi[2][1] * dxdxi[1][2];
         dxidx[0][1] = dxdxi[2][1] * dxdxi[0][2] - dxdxi[0][1] * dxdxi[2][2];
         dxidx[0][2] = dxdxi[0][1] * dxdxi[1][2] - dxdxi[0][2] * dxdxi[1][1];
-        const double tmp = one / (dxidx[0][0] * dxdxi[0][0] + dxidx[0][1] * dxdxi[1][0] +
+        const R tmp = one / (dxidx[0][0] * dxdxi[0][0] + dxidx[0][1] * dxdxi[1][0] +
                                   dxidx[0][2] * dxdxi[2][0]);
         dxidx[0][0] = dxidx[0][0] * tmp;
         dxidx[0][1] = dxidx[0][1] * tmp;
@@ -249,33 +285,33 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
         dxidx[2][0] = (dxdxi[1][0] * dxdxi[2][1] - dxdxi[1][1] * dxdxi[2][0]) * tmp;
         dxidx[2][1] = (dxdxi[2][0] * dxdxi[0][1] - dxdxi[0][0] * dxdxi[2][1]) * tmp;
         dxidx[2][2] = (dxdxi[0][0] * dxdxi[1][1] - dxdxi[0][1] * dxdxi[1][0]) * tmp;
-        const double WdetJ = tp.Qwt[intp] / tmp;
-        double shg[8][3];
+        const R WdetJ = tp.Qwt[intp] / tmp;
+        R shg[8][3];
         for (int n = 0; n < nshl; ++n)
             for (int i = 0; i < 3; ++i)
                 shg[n][i] = shgl[0][n] * dxidx[0][i] + shgl[1][n] * dxidx[1][i] +
                             shgl[2][n] * dxidx[2][i];
         // global gradients of the (perturbed) yl (e3ivar.f:259-334)
-        double g[3][5] = {{0}};
+        R g[3][5] = {{0}};
         for (int n = 0; n < nshl; ++n)
             for (int i = 0; i < 3; ++i)
                 for (int k = 0; k < 5; ++k) g[i][k] = g[i][k] + shg[n][i] * yl[n][k];
 
         // ---------------- e3mtrx.f:79-224 ----------------
-        double A0[5][5] = {{0}}, A[3][5][5] = {{{0}}};
-        const double drdp = rho * betaT;
-        const double drdT = -rho * alfap;
+        R A0[5][5] = {{0}}, A[3][5][5] = {{{0}}};
+        const R drdp = rho * betaT;
+        const R drdT = -rho * alfap;
         A0[4][0] = drdp * (h + rk) - alfap * Tq;
-        const double e2p = A0[4][0] + one;
-        const double e3p = rho * (h + rk);
-        const double e4p = drdT * (h + rk) + rho * cp;
+        const R e2p = A0[4][0] + one;
+        const R e3p = rho * (h + rk);
+        const R e4p = drdT * (h + rk) + rho * cp;
         A0[0][0] = drdp;
         A0[0][4] = drdT;
         A0[1][0] = drdp * u1; A0[1][1] = rho; A0[1][4] = drdT * u1;
         A0[2][0] = drdp * u2; A0[2][2] = rho; A0[2][4] = drdT * u2;
         A0[3][0] = drdp * u3; A0[3][3] = rho; A0[3][4] = drdT * u3;
         A0[4][1] = rho * u1; A0[4][2] = rho * u2; A0[4][3] = rho * u3; A0[4][4] = e4p;
-        double (*A1)[5] = A[0], (*A2)[5] = A[1], (*A3)[5] = A[2];
+        R (*A1)[5] = A[0], (*A2)[5] = A[1], (*A3)[5] = A[2];
         A1[0][0] = drdp * u1; A1[0][1] = rho; A1[0][4] = drdT * u1;
         A1[1][0] = drdp * u1 * u1 + 1; A1[1][1] = two * rho * u1; A1[1][4] = drdT * u1 * u1;
         A1[2][0] = drdp * u1 * u2; A1[2][1] = rho * u2; A1[2][2] = rho * u1; A1[2][4] = drdT * u1 * u2;
@@ -313,9 +349,9 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             ri[13] = (-u3) * rho * u3 - pres;
             ri[14] = (-u3) * rho * (ei + rk) - u3 * pres;
         }
-        double rLyi[5];
+        R rLyi[5];
         for (int k = 0; k < 5; ++k) {
-            double s = 0.0;
+            R s = 0.0;
             for (int i = 0; i < 3; ++i)
                 for (int j = 0; j < 5; ++j) s = s + A[i][k][j] * g[i][j];
             rLyi[k] = s;
@@ -325,9 +361,9 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
 
         // ---------------- e3visc.f:278-368 (Navier == 1, rlsli == 0) ----------------
         if (c.Navier == 1) {
-            const double (*g1)[5] = &g[0], (*g2)[5] = &g[1], (*g3)[5] = &g[2];
+            const R (*g1)[5] = &g[0], (*g2)[5] = &g[1], (*g3)[5] = &g[2];
             (void)g1; (void)g2; (void)g3;
-            const double* G1 = g[0]; const double* G2 = g[1]; const double* G3 = g[2];
+            const R* G1 = g[0]; const R* G2 = g[1]; const R* G3 = g[2];
             rmi[1] = rlm2mu * G1[1] + rlm * G2[2] + rlm * G3[3] - 0.0;
             rmi[2] = rmu * G1[2] + rmu * G2[1] - 0.0;
             rmi[3] = rmu * G1[3] + rmu * G3[1] - 0.0;
@@ -352,20 +388,20 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
         }
 
         // ---------------- e3ls.f:96-143 ----------------
-        const double fct1 = c.almi / c.gami / c.alfi * c.Dtgl;
-        double rLymi[5] = {0, 0, 0, 0, 0};
+        const R fct1 = c.almi / c.gami / c.alfi * c.Dtgl;
+        R rLymi[5] = {0, 0, 0, 0, 0};
         if (ires != 1)
             for (int k = 0; k < 5; ++k) rLymi[k] = rLyi[k] + fct1 * dui[k];
         if (ires == 1 || ires == 3)
             for (int k = 0; k < 5; ++k) {
-                double s = rLyi[k];
+                R s = rLyi[k];
                 for (int j = 0; j < 5; ++j) s = s + A0[k][j] * aci[j];
                 rLyi[k] = s;
             }
         // idiff >= 1: divergence of the reconstructed diffusive flux (e3ivar.f:363-395),
         // subtracted from the least-squares term (e3ls.f:147-156)
         if (ql && c.idiff >= 1 && (ires == 1 || ires == 3)) {
-            double divqi[4] = {0, 0, 0, 0};
+            R divqi[4] = {0, 0, 0, 0};
             for (int n = 0; n < nshl; ++n)
                 for (int k = 0; k < 4; ++k)
                     divqi[k] = divqi[k] + shg[n][0] * ql[n][k] + shg[n][1] * ql[n][4 + k] + shg[n][2] * ql[n][8 + k];
@@ -373,7 +409,7 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
         }
 
         // ---------------- e3tau.f:140-181 (itau = 0) + e3gijd (e3tau.f:1397-1508) ----------------
-        double gijd[6];
+        R gijd[6];
         if (tp.lcsyst >= 2) {
             // hexes and wedges: dxidx^T dxidx (e3tau.f:1408-1425)
             auto col = [&](int i, int j) {
@@ -386,8 +422,8 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             gijd[4] = col(1, 2);
             gijd[5] = col(2, 2);
         } else {
-            const double c1 = 1.259921049894873e+00, c2 = 6.299605249474365e-01;
-            double t1, t2, t3;
+            const R c1 = 1.259921049894873e+00, c2 = 6.299605249474365e-01;
+            R t1, t2, t3;
             t1 = c1 * dxidx[0][0] + c2 * (dxidx[1][0] + dxidx[2][0]);
             t2 = c1 * dxidx[1][0] + c2 * (dxidx[0][0] + dxidx[2][0]);
             t3 = c1 * dxidx[2][0] + c2 * (dxidx[0][0] + dxidx[1][0]);
@@ -404,46 +440,46 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             gijd[4] = dxidx[0][1] * t1 + dxidx[1][1] * t2 + dxidx[2][1] * t3;
             gijd[5] = dxidx[0][2] * t1 + dxidx[1][2] * t2 + dxidx[2][2] * t3;
         }
-        double tau[3];
+        R tau[3];
         if (c.itau == 1) {
             // Diagonal-Franca (e3tau.f:54-139), iremoveStabTimeTerm = 0, ipord = 1
-            double fact = gijd[0] * gijd[2] * gijd[5] - gijd[0] * gijd[4] * gijd[4] - gijd[2] * gijd[3] * gijd[3] -
+            R fact = gijd[0] * gijd[2] * gijd[5] - gijd[0] * gijd[4] * gijd[4] - gijd[2] * gijd[3] * gijd[3] -
                           gijd[5] * gijd[1] * gijd[1] + gijd[1] * gijd[3] * gijd[4] * two;
-            double uh1 = u1 * u1 * (gijd[2] * gijd[5] - gijd[4] * gijd[4]) +
+            R uh1 = u1 * u1 * (gijd[2] * gijd[5] - gijd[4] * gijd[4]) +
                          u2 * u2 * (gijd[0] * gijd[5] - gijd[3] * gijd[3]) +
                          u3 * u3 * (gijd[0] * gijd[2] - gijd[1] * gijd[1]) +
                          two * (u1 * u2 * (gijd[3] * gijd[4] - gijd[1] * gijd[5]) +
                                 u1 * u3 * (gijd[1] * gijd[4] - gijd[3] * gijd[2]) +
                                 u2 * u3 * (gijd[3] * gijd[1] - gijd[0] * gijd[4]));
-            uh1 = two * std::sqrt(uh1 / fact);
-            double h2o2u = u1 * u1 * gijd[0] + u2 * u2 * gijd[2] + u3 * u3 * gijd[5] +
+            uh1 = two * osqrt(uh1 / fact);
+            R h2o2u = u1 * u1 * gijd[0] + u2 * u2 * gijd[2] + u3 * u3 * gijd[5] +
                            (u1 * u2 * gijd[1] + u1 * u3 * gijd[3] + u2 * u3 * gijd[4]) * two + 1.0e-15;
-            h2o2u = one / std::sqrt(h2o2u);
+            h2o2u = one / osqrt(h2o2u);
             fact = pt5 * rho * uh1 / rmu;
-            tau[0] = pt5 * uh1 * std::min(one, fact) * c.taucfct;
-            const double dts = one / (c.Dtgl * c.dtsfct);
-            tau[1] = std::min(dts, h2o2u);
+            tau[0] = pt5 * uh1 * omin(one, fact) * c.taucfct;
+            const R dts = one / (c.Dtgl * c.dtsfct);
+            tau[1] = omin(dts, h2o2u);
             tau[1] = tau[1] / rho;
             tau[2] = tau[1] / cv;
             fact = h2o2u * h2o2u * rk * pt66 / rmu;
-            tau[1] = std::min(tau[1], fact);
-            tau[2] = std::min(tau[2], fact * rmu / con) * c.temper;
+            tau[1] = omin(tau[1], fact);
+            tau[2] = omin(tau[2], fact * rmu / con) * c.temper;
         } else {
-            const double fff = 36.0;  // ipord == 1
-            const double dts = (c.iremoveStabTimeTerm == 1) ? zero : c.dtsfct * c.Dtgl;
-            double t2 = rho * rho * ((two * dts) * (two * dts) +
+            const R fff = 36.0;  // ipord == 1
+            const R dts = (c.iremoveStabTimeTerm == 1) ? zero : c.dtsfct * c.Dtgl;
+            R t2 = rho * rho * ((two * dts) * (two * dts) +
                                      (u1 * (u1 * gijd[0] + two * (u2 * gijd[1] + u3 * gijd[3])) +
                                       u2 * (u2 * gijd[2] + two * u3 * gijd[4]) + u3 * u3 * gijd[5])) +
                         fff * (rmu * rmu) *
                             (gijd[0] * gijd[0] + gijd[2] * gijd[2] + gijd[5] * gijd[5] +
                              two * (gijd[1] * gijd[1] + gijd[3] * gijd[3] + gijd[4] * gijd[4]));
-            const double fact = std::sqrt(t2);
+            const R fact = osqrt(t2);
             tau[0] = pt125 * fact / (rho * (gijd[0] + gijd[2] + gijd[5])) * c.taucfct;
             tau[1] = one / fact;
             tau[2] = tau[1] / cv * c.temper;
         }
-        const double tauk[5] = {tau[0], tau[1], tau[1], tau[1], tau[2]};
-        double rLyt[5];  // the least-squares residual before tau, for the DC factor (e3tau.f:183)
+        const R tauk[5] = {tau[0], tau[1], tau[1], tau[1], tau[2]};
+        R rLyt[5];  // the least-squares residual before tau, for the DC factor (e3tau.f:183)
         for (int k = 0; k < 5; ++k) rLyt[k] = rLyi[k];
         if (ires == 1 || ires == 3)
             for (int k = 0; k < 5; ++k) rLyi[k] = tauk[k] * rLyi[k];
@@ -454,14 +490,14 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
         if (ires != 1)
             for (int r = 0; r < 15; ++r) {
                 const int i = r / 5, row = r % 5;
-                double s = 0.0;
+                R s = 0.0;
                 for (int j = 0; j < 5; ++j) s = s + A[i][row][j] * rLymi[j];
                 rmi[r] = s + rmi[r];
             }
         if (ires == 1 || ires == 3)
             for (int r = 0; r < 15; ++r) {
                 const int i = r / 5, row = r % 5;
-                double s = 0.0;
+                R s = 0.0;
                 for (int j = 0; j < 5; ++j) s = s + A[i][row][j] * rLyi[j];
                 ri[r] = s + ri[r];
             }
@@ -469,19 +505,19 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
         // ---------------- discontinuity capturing (e3.f:217-222), iDC != 0 ----------------
         if (c.iDC != 0) {
             // A0DC, A0inv and dV/dY (e3mtrx.f:232-297); e3mtrx's local cv
-            const double s1 = one / (rho * rho * betaT * Tq);
-            const double cvd = cp - (alfap * alfap * Tq / rho / betaT);
-            const double A0DC[4] = {(rho * betaT) * (rho * betaT) * s1, -(rho * alfap * rho * betaT * s1), rho / Tq,
+            const R s1 = one / (rho * rho * betaT * Tq);
+            const R cvd = cp - (alfap * alfap * Tq / rho / betaT);
+            const R A0DC[4] = {(rho * betaT) * (rho * betaT) * s1, -(rho * alfap * rho * betaT * s1), rho / Tq,
                                     (-(rho * alfap)) * (-(rho * alfap)) * s1 + (rho * cvd / (Tq * Tq))};
-            double A0inv[15];
+            R A0inv[15];
             {
-                const double fact1 = one / (rho * cvd * (Tq * Tq));
-                const double d = alfap * Tq / rho / betaT;
-                const double e1bar = h - rk;
-                const double e2bar = e1bar - d;
-                const double e3bar = e2bar - cvd * Tq;
-                const double e5bar = e1bar * e1bar - 2 * e1bar * d + 2 * rk * cvd * Tq + cp * Tq / rho / betaT;
-                const double c1bar = u1 * u1 + cvd * Tq, c2bar = u2 * u2 + cvd * Tq, c3bar = u3 * u3 + cvd * Tq;
+                const R fact1 = one / (rho * cvd * (Tq * Tq));
+                const R d = alfap * Tq / rho / betaT;
+                const R e1bar = h - rk;
+                const R e2bar = e1bar - d;
+                const R e3bar = e2bar - cvd * Tq;
+                const R e5bar = e1bar * e1bar - 2 * e1bar * d + 2 * rk * cvd * Tq + cp * Tq / rho / betaT;
+                const R c1bar = u1 * u1 + cvd * Tq, c2bar = u2 * u2 + cvd * Tq, c3bar = u3 * u3 + cvd * Tq;
                 A0inv[0] = e5bar * fact1;
                 A0inv[1] = c1bar * fact1;
                 A0inv[2] = c2bar * fact1;
@@ -498,9 +534,9 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
                 A0inv[13] = -u2 * fact1;
                 A0inv[14] = -u3 * fact1;
             }
-            double dV[15];
+            R dV[15];
             {
-                const double fact1 = 1 / Tq, fact2 = fact1 / Tq;
+                const R fact1 = 1 / Tq, fact2 = fact1 / Tq;
                 dV[0] = fact1 / rho; dV[1] = -fact1 * u1; dV[2] = fact1; dV[3] = -fact1 * u2; dV[4] = zero;
                 dV[5] = fact1; dV[6] = -fact1 * u3; dV[7] = zero; dV[8] = zero; dV[9] = fact1;
                 dV[10] = -(h - rk) * fact2; dV[11] = -fact2 * u1; dV[12] = -fact2 * u2; dV[13] = -fact2 * u3;
@@ -508,13 +544,13 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             }
             // rTLS = (Ly - S) tau~ (Ly - S) with rLyi tau-scaled for ires 1, 3 and unscaled for
             // ires 2; raLS = (Ly - S) A0^-1 (Ly - S) (e3tau.f:193-237)
-            const double* L = rLyi;
-            const double* T0 = rLyt;
-            const double rTLS = T0[0] * (L[0] * dV[0] + dV[1] * L[1] + dV[3] * L[2] + L[3] * dV[6] + dV[10] * L[4]) +
+            const R* L = rLyi;
+            const R* T0 = rLyt;
+            const R rTLS = T0[0] * (L[0] * dV[0] + dV[1] * L[1] + dV[3] * L[2] + L[3] * dV[6] + dV[10] * L[4]) +
                                 T0[1] * (L[1] * dV[2] + L[2] * dV[4] + dV[7] * L[3] + L[4] * dV[11]) +
                                 T0[2] * (L[2] * dV[5] + dV[8] * L[3] + dV[12] * L[4]) +
                                 T0[3] * (L[3] * dV[9] + dV[13] * L[4]) + T0[4] * (dV[14] * L[4]);
-            const double raLS = two * T0[3] * T0[4] * A0inv[14] + two * T0[2] * T0[4] * A0inv[13] +
+            const R raLS = two * T0[3] * T0[4] * A0inv[14] + two * T0[2] * T0[4] * A0inv[13] +
                                 two * T0[0] * T0[1] * A0inv[5] + two * T0[1] * T0[2] * A0inv[9] +
                                 two * T0[1] * T0[3] * A0inv[10] + two * T0[0] * T0[2] * A0inv[6] +
                                 two * T0[2] * T0[3] * A0inv[12] + two * T0[1] * T0[4] * A0inv[11] +
@@ -522,40 +558,40 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
                                 T0[0] * T0[0] * A0inv[0] + T0[1] * T0[1] * A0inv[1] + T0[2] * T0[2] * A0inv[2] +
                                 T0[3] * T0[3] * A0inv[3] + T0[4] * T0[4] * A0inv[4];
             // inverse of the tau metric, order (11, 22, 33, 12, 13, 23) (e3tau.f:241-260)
-            const double gu[6] = {gijd[0], gijd[2], gijd[5], gijd[1], gijd[3], gijd[4]};
-            const double detI = one / (gu[0] * gu[1] * gu[2] - gu[0] * gu[5] * gu[5] - gu[3] * gu[3] * gu[2] +
+            const R gu[6] = {gijd[0], gijd[2], gijd[5], gijd[1], gijd[3], gijd[4]};
+            const R detI = one / (gu[0] * gu[1] * gu[2] - gu[0] * gu[5] * gu[5] - gu[3] * gu[3] * gu[2] +
                                        gu[3] * gu[4] * gu[5] * two - gu[4] * gu[4] * gu[1]);
-            const double gi[6] = {detI * (gu[1] * gu[2] - gu[5] * gu[5]), detI * (gu[0] * gu[2] - gu[4] * gu[4]),
+            const R gi[6] = {detI * (gu[1] * gu[2] - gu[5] * gu[5]), detI * (gu[0] * gu[2] - gu[4] * gu[4]),
                                   detI * (gu[0] * gu[1] - gu[3] * gu[3]), detI * (gu[4] * gu[5] - gu[3] * gu[2]),
                                   detI * (gu[3] * gu[5] - gu[4] * gu[1]), detI * (gu[3] * gu[4] - gu[0] * gu[5])};
             // e3dc.f:55-240: A0 Y,j, g^ij A0 Y,j and Y,i A0DC Y,j
-            double A0g[15];
+            R A0g[15];
             for (int j = 0; j < 3; ++j)
                 for (int k = 0; k < 5; ++k)
                     A0g[5 * j + k] = A0[k][0] * g[j][0] + A0[k][1] * g[j][1] + A0[k][2] * g[j][2] +
                                      A0[k][3] * g[j][3] + A0[k][4] * g[j][4];
-            double gA[15];
+            R gA[15];
             for (int k = 0; k < 5; ++k) {
                 gA[k] = gi[0] * A0g[k] + gi[3] * A0g[5 + k] + gi[4] * A0g[10 + k];
                 gA[5 + k] = gi[3] * A0g[k] + gi[1] * A0g[5 + k] + gi[5] * A0g[10 + k];
                 gA[10 + k] = gi[4] * A0g[k] + gi[5] * A0g[5 + k] + gi[2] * A0g[10 + k];
             }
-            auto yy = [&](const double* a) {
+            auto yy = [&](const R* a) {
                 return A0DC[0] * (a[0] * a[0]) + two * a[0] * A0DC[1] * a[4] + A0DC[2] * (a[1] * a[1]) +
                        A0DC[2] * (a[2] * a[2]) + A0DC[2] * (a[3] * a[3]) + A0DC[3] * (a[4] * a[4]);
             };
-            auto yx = [&](const double* a, const double* b) {
+            auto yx = [&](const R* a, const R* b) {
                 return a[0] * A0DC[0] * b[0] + a[0] * A0DC[1] * b[4] + a[1] * A0DC[2] * b[1] +
                        a[2] * A0DC[2] * b[2] + a[3] * A0DC[2] * b[3] + a[4] * A0DC[1] * b[0] + a[4] * A0DC[3] * b[4];
             };
-            const double y1 = yy(g[0]), y2 = yy(g[1]), y3 = yy(g[2]);
-            const double y4 = yx(g[0], g[1]), y5 = yx(g[0], g[2]), y6 = yx(g[1], g[2]);
-            const double gnorm = one / (gi[0] * y1 + two * gi[3] * y4 + two * gi[4] * y5 + gi[1] * y2 +
+            const R y1 = yy(g[0]), y2 = yy(g[1]), y3 = yy(g[2]);
+            const R y4 = yx(g[0], g[1]), y5 = yx(g[0], g[2]), y6 = yx(g[1], g[2]);
+            const R gnorm = one / (gi[0] * y1 + two * gi[3] * y4 + two * gi[4] * y5 + gi[1] * y2 +
                                         two * gi[5] * y6 + gi[2] * y3 + c.epsM);
-            double DC = 0.0;  // ipord = 1: fact = 1
-            if (c.iDC == 1) DC = std::max(zero, std::sqrt(raLS * gnorm) - rTLS * gnorm);
+            R DC = 0.0;  // ipord = 1: fact = 1
+            if (c.iDC == 1) DC = omax(zero, osqrt(raLS * gnorm) - rTLS * gnorm);
             if (c.iDC == 2) DC = two * rTLS * gnorm;
-            if (c.iDC == 3) DC = std::min(std::max(zero, std::sqrt(raLS * gnorm) - rTLS * gnorm), two * rTLS * gnorm);
+            if (c.iDC == 3) DC = omin(omax(zero, osqrt(raLS * gnorm) - rTLS * gnorm), two * rTLS * gnorm);
             if (ires == 1 || ires == 3) {
                 for (int r = 0; r < 15; ++r) {
                     ri[r] = ri[r] + DC * gA[r];
@@ -570,7 +606,7 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
         // ---------------- e3massr.f:26-88 ----------------
         if (ires == 1 || ires == 3)
             for (int k = 0; k < 5; ++k) {
-                double s = ri[15 + k];
+                R s = ri[15 + k];
                 for (int j = 0; j < 5; ++j) s = s + A0[k][j] * aci[j];
                 ri[15 + k] = s;
             }
@@ -580,11 +616,11 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
         // ---------------- lhs = 1: element tangent EG[nedof][nedof], nedof = 5 nshl ----------------
         if (EG) {
             const int nedof = 5 * nshl;
-            auto E = [&](int r, int cc) -> double& { return EG[(size_t)r * nedof + cc]; };
+            auto E = [&](int r, int cc) -> R& { return EG[(size_t)r * nedof + cc]; };
             // e3conv.f:186-260: N_a (A_i N_b,i)
             for (int j = 0; j < nshl; ++j) {
-                const double f1 = WdetJ * shg[j][0], f2 = WdetJ * shg[j][1], f3 = WdetJ * shg[j][2];
-                double AiNbi[5][5];
+                const R f1 = WdetJ * shg[j][0], f2 = WdetJ * shg[j][1], f3 = WdetJ * shg[j][2];
+                R AiNbi[5][5];
                 for (int r = 0; r < 5; ++r)
                     for (int cc = 0; cc < 5; ++cc) AiNbi[r][cc] = f1 * A1[r][cc] + f2 * A2[r][cc] + f3 * A3[r][cc];
                 for (int i = 0; i < nshl; ++i)
@@ -592,16 +628,16 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
                         for (int r = 0; r < 5; ++r) E(5 * i + r, 5 * j + cc) = E(5 * i + r, 5 * j + cc) + shape[i] * AiNbi[r][cc];
             }
             // stiff(15,15): e3visc.f:65-127 (diffusivity K_ij), then e3ls.f:464-702 (A_i tau A_j)
-            double stiff[15][15] = {{0}};
+            R stiff[15][15] = {{0}};
             if (c.Navier == 1) {
-                const double uu[3] = {u1, u2, u3};
+                const R uu[3] = {u1, u2, u3};
                 for (int i = 0; i < 3; ++i)
                     for (int j = 0; j < 3; ++j) {
-                        double (*K)[15] = stiff;
+                        R (*K)[15] = stiff;
                         const int ri = 5 * i, cj = 5 * j;
                         for (int m = 0; m < 3; ++m)
                             for (int n = 0; n < 3; ++n) {
-                                double v = 0.0;
+                                R v = 0.0;
                                 if (i == j && m == n) v = (m == i) ? rlm2mu : rmu;
                                 else if (i != j && m == i && n == j) v = rlm;
                                 else if (i != j && m == j && n == i) v = rmu;
@@ -609,7 +645,7 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
                             }
                         // energy row: u_m times the momentum rows
                         for (int n = 0; n < 3; ++n) {
-                            double v = 0.0;
+                            R v = 0.0;
                             if (i == j) v = ((n == i) ? rlm2mu : rmu) * uu[n];
                             else if (n == j) v = rlm * uu[i];
                             else if (n == i) v = rmu * uu[j];
@@ -618,9 +654,9 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
                         if (i == j) K[ri + 4][cj + 4] = con;
                     }
             }
-            double AtA0[3][5][5];
+            R AtA0[3][5][5];
             for (int i = 0; i < 3; ++i) {
-                double Atau[5][5];
+                R Atau[5][5];
                 for (int r = 0; r < 5; ++r)
                     for (int k = 0; k < 5; ++k) Atau[r][k] = A[i][r][k] * tauk[k];
                 for (int cc = 0; cc < 5; ++cc)
@@ -637,30 +673,30 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             }
             // e3ls.f:703-766: least-squares time term N_a,i A_i tau A0 N_b
             for (int i = 0; i < nshl; ++i) {
-                double At[5][5];
+                R At[5][5];
                 for (int r = 0; r < 5; ++r)
                     for (int cc = 0; cc < 5; ++cc)
                         At[r][cc] = shg[i][0] * AtA0[0][r][cc] + shg[i][1] * AtA0[1][r][cc] + shg[i][2] * AtA0[2][r][cc];
                 for (int j = 0; j < nshl; ++j) {
-                    const double fact = shape[j] * WdetJ * c.almi / c.gami / c.alfi * c.Dtgl;
+                    const R fact = shape[j] * WdetJ * c.almi / c.gami / c.alfi * c.Dtgl;
                     for (int r = 0; r < 5; ++r)
                         for (int cc = 0; cc < 5; ++cc) E(5 * i + r, 5 * j + cc) = E(5 * i + r, 5 * j + cc) + fact * At[r][cc];
                 }
             }
             // e3massl.f:1-75 (bcool = 0): N_a N_b fct A0
             {
-                const double temp = WdetJ * c.almi / c.gami / c.alfi * c.Dtgl;
+                const R temp = WdetJ * c.almi / c.gami / c.alfi * c.Dtgl;
                 for (int j = 0; j < nshl; ++j)
                     for (int i = 0; i < nshl; ++i) {
-                        const double f = (shape[i] * shape[j]) * (temp + 0.0);
+                        const R f = (shape[i] * shape[j]) * (temp + 0.0);
                         for (int cc = 0; cc < 5; ++cc)
                             for (int r = 0; r < 5; ++r) E(5 * i + r, 5 * j + cc) = E(5 * i + r, 5 * j + cc) + f * A0[r][cc];
                     }
             }
             // e3wmlt.f (lhs part): N_a,i stiff_ij N_b,j
             for (int j = 0; j < nshl; ++j) {
-                const double g1 = WdetJ * shg[j][0], g2 = WdetJ * shg[j][1], g3 = WdetJ * shg[j][2];
-                double st[3][5][5];
+                const R g1 = WdetJ * shg[j][0], g2 = WdetJ * shg[j][1], g3 = WdetJ * shg[j][2];
+                R st[3][5][5];
                 for (int cc = 0; cc < 5; ++cc)
                     for (int r = 0; r < 5; ++r)
                         for (int b = 0; b < 3; ++b)
@@ -678,7 +714,7 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
         if (iprec == 1 && bdl && !EG) {
             // convective, non-integrated-by-parts: N_b A_i N_b,i  (e3bdg.f:37-189)
             for (int j = 0; j < nshl; ++j) {
-                const double t = shape[j] * WdetJ;
+                const R t = shape[j] * WdetJ;
                 for (int r = 0; r < 5; ++r)
                     for (int cc = 0; cc < 5; ++cc)
                         bdl[j][r][cc] = bdl[j][r][cc] +
@@ -687,19 +723,19 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             }
             // mass (e3bdg.f:219-246), bcool = 0
             {
-                const double ff = c.almi / c.gami / c.alfi;
-                const double t = WdetJ * (c.Dtgl * ff + 0.0);
+                const R ff = c.almi / c.gami / c.alfi;
+                const R t = WdetJ * (c.Dtgl * ff + 0.0);
                 for (int j = 0; j < nshl; ++j) {
-                    const double t2 = (shape[j] * shape[j]) * t;
+                    const R t2 = (shape[j] * shape[j]) * t;
                     for (int r = 0; r < 5; ++r)
                         for (int cc = 0; cc < 5; ++cc) bdl[j][r][cc] = bdl[j][r][cc] + t2 * A0[r][cc];
                 }
             }
             // least-squares time term N_a,i A_i tau A0 (e3bdg.f:254-342)
             if (c.ivart >= 2) {
-                double AtA0[3][5][5];
+                R AtA0[3][5][5];
                 for (int i = 0; i < 3; ++i) {
-                    double Atau[5][5];
+                    R Atau[5][5];
                     for (int r = 0; r < 5; ++r)
                         for (int k = 0; k < 5; ++k) Atau[r][k] = A[i][r][k] * tauk[k];
                     for (int cc = 0; cc < 5; ++cc)
@@ -709,7 +745,7 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
                                              Atau[r][4] * A0[4][cc];
                 }
                 for (int a = 0; a < nshl; ++a) {
-                    const double t1 = shape[a] * WdetJ * c.almi / c.gami / c.alfi * c.Dtgl;
+                    const R t1 = shape[a] * WdetJ * c.almi / c.gami / c.alfi * c.Dtgl;
                     for (int r = 0; r < 5; ++r)
                         for (int cc = 0; cc < 5; ++cc)
                             bdl[a][r][cc] = bdl[a][r][cc] +
@@ -721,9 +757,9 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             const int blocks[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
             for (int b = 0; b < 6; ++b) {
                 const int p = blocks[b][0], q = blocks[b][1];
-                const double (*Ap)[5] = A[p];
-                const double (*Aq)[5] = A[q];
-                double M[5][5];
+                const R (*Ap)[5] = A[p];
+                const R (*Aq)[5] = A[q];
+                R M[5][5];
                 if (c.ivart >= 2) {
                     for (int r = 0; r < 5; ++r)
                         for (int cc = 0; cc < 5; ++cc) {
@@ -744,15 +780,15 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
                     std::memset(M, 0, sizeof(M));
                 }
                 if (c.Navier == 1) {
-                    const double uu[3] = {u1, u2, u3};
+                    const R uu[3] = {u1, u2, u3};
                     if (p == q) {
                         // diagonal: rlm2mu on the p-th momentum row, rmu on the others
                         for (int d = 0; d < 3; ++d) {
-                            const double coef = (d == p) ? rlm2mu : rmu;
+                            const R coef = (d == p) ? rlm2mu : rmu;
                             M[1 + d][1 + d] = M[1 + d][1 + d] + coef;
                         }
                         for (int d = 0; d < 3; ++d) {
-                            const double coef = (d == p) ? rlm2mu : rmu;
+                            const R coef = (d == p) ? rlm2mu : rmu;
                             M[4][1 + d] = M[4][1 + d] + coef * uu[d];
                         }
                         M[4][4] = M[4][4] + con;
@@ -765,7 +801,7 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
                     }
                 }
                 for (int j = 0; j < nshl; ++j) {
-                    const double t = WdetJ * shg[j][p] * shg[j][q];
+                    const R t = WdetJ * shg[j][p] * shg[j][q];
                     for (int r = 0; r < 5; ++r)
                         for (int cc = 0; cc < 5; ++cc) bdl[j][r][cc] = bdl[j][r][cc] + t * M[r][cc];
                 }
@@ -787,6 +823,13 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
             for (int i = 0; i < nshl; ++i)
                 for (int k = 0; k < 5; ++k) rl[i][k] = rl[i][k] + shape[i] * WdetJ * ri[15 + k];
     }
+}
+
+void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const double (*yl)[5],
+                const double (*ycl)[5], const double (*acl)[5], const double (*xl)[3],
+                double (*rl)[5], double (*rml)[5], double (*bdl)[5][5], const double (*ql)[12] = nullptr,
+                double* EG = nullptr) {
+    e3_element_t<double>(c, tp, ires, iprec, yl, ycl, acl, xl, rl, rml, bdl, ql, EG);
 }
 
 // ---------------------------------------------------------------------------
@@ -2378,3 +2421,36 @@ void or_itrupdate(const or_common* c, int N, double* yold, double* acold, const 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// floating-point operations of the reference formulation of e3 for one element (the counting
+// scalar through the same statements as the oracle), and the element's outputs for a check
+// ---------------------------------------------------------------------------
+extern "C" long long or_e3_flops(const or_common* c, int lcsyst, int ires, int iprec, const double* yl,
+                                 const double* ycl, const double* acl, const double* xl, double* rl,
+                                 double* rml, double* bdl) {
+    const Topo& tp = topo(lcsyst);
+    const int n = tp.nshl;
+    std::vector<Flop> y(5 * n), yc(5 * n), a(5 * n), x(3 * n), r(5 * n), rm(5 * n), bd(25 * n);
+    for (int i = 0; i < 5 * n; ++i) {
+        y[i] = yl[i];
+        yc[i] = ycl[i];
+        a[i] = acl[i];
+        r[i] = rl[i];
+        rm[i] = rml[i];
+    }
+    for (int i = 0; i < 3 * n; ++i) x[i] = xl[i];
+    for (int i = 0; i < 25 * n; ++i) bd[i] = bdl ? bdl[i] : 0.0;
+    g_flops = 0;
+    e3_element_t<Flop>(*c, tp, ires, iprec, (const Flop (*)[5])y.data(), (const Flop (*)[5])yc.data(),
+                       (const Flop (*)[5])a.data(), (const Flop (*)[3])x.data(), (Flop (*)[5])r.data(),
+                       (Flop (*)[5])rm.data(), iprec ? (Flop (*)[5][5])bd.data() : nullptr, nullptr, nullptr);
+    const long long nf = g_flops;
+    for (int i = 0; i < 5 * n; ++i) {
+        rl[i] = r[i].v;
+        rml[i] = rm[i].v;
+    }
+    if (bdl)
+        for (int i = 0; i < 25 * n; ++i) bdl[i] = bd[i].v;
+    return nf;
+}
