@@ -174,6 +174,7 @@ long long phgpu_graph_cycles(phgpu_ctx* ctx);
 /* time steps run as one CUDA graph since create, or -1 when the graph could not be built
  * (phgpu_last_error gives the reason; steps are then launched kernel by kernel).  With
  * no_graph = 0, phgpu_time_step(_dev) of the mixed-precision block-diagonal matrix-free solver
+ * (also with precond = PHGPU_PRECOND_LEARNED while the network is off or has no weights)
  * with nGMRES = 1 and nitr <= 16 runs itrPredict, the nitr Newton iterations (assembly, LU,
  * the GMRES cycle as conditional nodes opened from the device, back substitution, itrCorrect,
  * itrBC) and itrUpdate as one graph with one host read of the statistics: the same kernels in

@@ -1018,11 +1018,14 @@ int newton_dev(Ctx& C, phgpu_stats* st) {
 // ---------------------------------------------------------------------------
 // the whole time step as one CUDA graph (StepGraph)
 // ---------------------------------------------------------------------------
+// (with the learned preconditioner selected, once it is switched off -- or has no weights --
+// every solve is block-diagonal, and the step graph applies as well)
 bool step_graph_eligible(const Ctx& C, int nitr) {
     const phgpu_config& c = C.cfg;
-    return !c.no_graph && c.precision == PHGPU_MIXED && c.ap_mode == PHGPU_AP_LINEAR &&
-           c.precond == PHGPU_PRECOND_BDIAG && c.nGMRES == 1 && c.iDC == 0 && nitr >= 1 &&
-           nitr <= kStepGraphMaxNitr && !C.stepg.disabled;
+    const bool plain = c.precond == PHGPU_PRECOND_BDIAG ||
+                       (c.precond == PHGPU_PRECOND_LEARNED && (C.net.disabled || !net_usable(C)));
+    return !c.no_graph && c.precision == PHGPU_MIXED && c.ap_mode == PHGPU_AP_LINEAR && plain &&
+           c.nGMRES == 1 && c.iDC == 0 && nitr >= 1 && nitr <= kStepGraphMaxNitr && !C.stepg.disabled;
 }
 
 void step_graph_free(StepGraph& G) {
@@ -1197,6 +1200,7 @@ int step_graph_run(Ctx& C, int nitr, phgpu_stats* st, bool* used) {
     st->status = PHGPU_OK;
     C.launches += G.fixed_launches + body;
     C.cyc.runs += nitr;  // each Newton iteration's GMRES cycle ran as (part of) a graph
+    if (C.cfg.precond == PHGPU_PRECOND_LEARNED) C.net.n_plain += nitr;
     C.cfg.iter = nitr;
     C.cfg.istep += 1;
     return PHGPU_OK;
