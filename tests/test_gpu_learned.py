@@ -189,6 +189,11 @@ def test_identity_network_falls_back_and_still_converges(gpu_lib):
         assert st.echeck <= p["etol"] * st.unorm0 * (1 + 1e-12), st
         seen.append(st.net_fallback)
     assert seen == [L.PHGPU_NET_PLAIN, L.PHGPU_NET_FELL_BACK, L.PHGPU_NET_FELL_BACK, L.PHGPU_NET_PLAIN]
+    u = g.net_usage()
+    assert u["off"] and u["fell_back"] == 2 and u["plain"] == 2
+    # with the network off, a time step is block-diagonal and runs as one CUDA graph
+    g.time_step(y, ac, 3)
+    assert g.step_graphs == 1 and g.net_usage()["plain"] == 5
 
 
 def test_nonfinite_network_output_falls_back(gpu_lib):
