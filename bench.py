@@ -276,6 +276,7 @@ def run_gpu(args, rank, world):
            "h2d_bytes_per_step": int(2 * 5 * case.nshg * 8 / NEWTON_PER_TIMESTEP),
            "d2h_bytes_per_step": int(4 * 5 * case.nshg * 8 / NEWTON_PER_TIMESTEP)}
     roof = kernel_roofline(g, case, stream, sum(conv["krylov_iterations"]) / NEWTON_PER_TIMESTEP)
+    tuning = g.tuning()
     g.close()
     del g
 
@@ -309,6 +310,9 @@ def run_gpu(args, rank, world):
         "newton": conv, "learned_usage": usage, "plain_mixed": plain_mixed,
         "speedup_vs_plain_mixed": plain_mixed["ms_per_step"] / (ms / args.steps),
         "roofline": roof, "clocks": t["clocks"],
+        "sweep_tuning": {"lin_minb": tuning["lin_minb"], "ress_minb": tuning["ress_minb"], "how": tuning["how"],
+                         "lin_ms": {str(k): v for k, v in tuning["lin_ms"].items()},
+                         "ress_ms": {str(k): v for k, v in tuning["ress_ms"].items()}},
     }
     result["state_rel_diff_learned_vs_plain_mixed"] = float(np.linalg.norm(y_learned - y_plain) /
                                                             np.linalg.norm(y_plain))

@@ -183,6 +183,20 @@ long long phgpu_graph_cycles(phgpu_ctx* ctx);
  * the state of that step is undefined. */
 long long phgpu_step_graphs(phgpu_ctx* ctx);
 
+/* Autotuned register/occupancy variants of the two pipelined element sweeps of the mixed-precision
+ * matrix-free solver: the linearized product (compiled for at least 3 or 4 resident CTAs per SM)
+ * and the double-float split outer residual (2, 3 or 4).  Before its first mixed-precision
+ * linearized solve or graph-captured time step, a context times each variant on its own mesh
+ * and state (a warm-up and three timed sweeps each, CUDA events) and keeps the fastest; the
+ * variants compute the same values, so the choice changes no result.
+ * phgpu_set_tuning forces a choice (lin_minb 3 or 4, ress_minb 2, 3 or 4), or with (0, 0)
+ * returns to the compiled-in defaults and tunes again at the next solve.
+ * phgpu_tuning gives the current choice and, in ms[5], the mean time of each variant in ms
+ * (linearized product 3, 4; split residual 2, 3, 4; -1 when not timed); it returns 0 while
+ * untuned, 1 when tuned, 2 when forced. */
+int phgpu_set_tuning(phgpu_ctx* ctx, int lin_minb, int ress_minb);
+int phgpu_tuning(phgpu_ctx* ctx, int* lin_minb, int* ress_minb, double* ms);
+
 /* new values BC(nshg, 6) of the Dirichlet constraints (the iBC bits of phgpu_create stay): the
  * reference passes BC to every ElmMFG/SolMFG call (elmmfg.f:1-5, solmfg.f:1-7) */
 int phgpu_set_bc(phgpu_ctx* ctx, const double* BC);

@@ -483,7 +483,8 @@ __host__ __device__ constexpr int lin_stage_words(int lmax) {
 // words of one node-id stage: e0, ne, n0, nn, then the chunk's global node ids
 __host__ __device__ constexpr int lin_id_words(int lmax) { return 4 + lmax; }
 
-__global__ void __launch_bounds__(kChunk, PHGPU_LINPIPE_MINB)
+template <int MINB>
+__global__ void __launch_bounds__(kChunk, MINB)
 k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x, const float* __restrict__ ya,
                  const float* __restrict__ yb, float* __restrict__ out, Phys<float> P, int lmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1179,8 +1180,8 @@ __host__ __device__ constexpr int ress_stage_words(int lmax, bool with_q) {
     return ((((10 * lmax + kRessNode * lmax + (with_q ? 12 * lmax : 0) + 1) & ~1) + 4 * kChunk + lmax + 2) + 1) & ~1;
 }
 
-template <bool WITH_Q>
-__global__ void __launch_bounds__(kChunk, PHGPU_RESS_MINB)
+template <bool WITH_Q, int MINB>
+__global__ void __launch_bounds__(kChunk, MINB)
 k_chunk_ress_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ xh, const float* __restrict__ xlo,
                   const float* __restrict__ yh, const float* __restrict__ ylo, const float* __restrict__ acf,
                   double* __restrict__ out, Phys<float> Pf, DfConst K, const float* __restrict__ ql, int lmax) {
@@ -2422,30 +2423,30 @@ int configure_element_kernels(Ctx& C) {
         rc = check(C, cudaFuncSetAttribute(k_chunk_ress<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)(ress_smem(C) + q_smem<float>(C))),
                    "cudaFuncSetAttribute");
-    if (rc == PHGPU_OK)
-        rc = check(C, cudaFuncSetAttribute(k_chunk_lin_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)lin_pipe_smem(C)),
-                   "cudaFuncSetAttribute");
     if (rc == PHGPU_OK) {
-        // persistent grid of the pipelined linearized product: every resident CTA slot
-        int dev = 0, nsm = 0, per_sm = 0;
+        // persistent grids of the pipelined sweeps: every resident CTA slot of each variant
+        int dev = 0, nsm = 0;
         rc = check(C, cudaGetDevice(&dev), "cudaGetDevice");
         if (rc == PHGPU_OK) rc = check(C, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
-        if (rc == PHGPU_OK)
-            rc = check(C, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chunk_lin_pipe, kChunk,
-                                                                       lin_pipe_smem(C)),
-                       "occupancy");
-        C.lin_pipe_grid = std::max(1, nsm * per_sm);
-        for (int q = 0; q < 2 && rc == PHGPU_OK; ++q)
-            rc = check(C, cudaFuncSetAttribute(q ? k_chunk_ress_pipe<true> : k_chunk_ress_pipe<false>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)ress_pipe_smem(C, q == 1)),
-                       "cudaFuncSetAttribute");
-        if (rc == PHGPU_OK)
-            rc = check(C, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chunk_ress_pipe<false>, kChunk,
-                                                                       ress_pipe_smem(C, false)),
-                       "occupancy");
-        C.ress_pipe_grid = std::max(1, nsm * per_sm);
+        auto grid_of = [&](const void* f, size_t smem, int* grid) {
+            int per_sm = 0;
+            if (rc == PHGPU_OK)
+                rc = check(C, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                           "cudaFuncSetAttribute");
+            if (rc == PHGPU_OK)
+                rc = check(C, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, kChunk, smem), "occupancy");
+            *grid = std::max(1, nsm * per_sm);
+        };
+        grid_of((const void*)k_chunk_lin_pipe<3>, lin_pipe_smem(C), &C.lin_grids[0]);
+        grid_of((const void*)k_chunk_lin_pipe<4>, lin_pipe_smem(C), &C.lin_grids[1]);
+        int g2 = 0;
+        grid_of((const void*)k_chunk_ress_pipe<false, 2>, ress_pipe_smem(C, false), &C.ress_grids[0]);
+        grid_of((const void*)k_chunk_ress_pipe<false, 3>, ress_pipe_smem(C, false), &C.ress_grids[1]);
+        grid_of((const void*)k_chunk_ress_pipe<false, 4>, ress_pipe_smem(C, false), &C.ress_grids[2]);
+        grid_of((const void*)k_chunk_ress_pipe<true, 2>, ress_pipe_smem(C, true), &g2);
+        grid_of((const void*)k_chunk_ress_pipe<true, 3>, ress_pipe_smem(C, true), &g2);
+        grid_of((const void*)k_chunk_ress_pipe<true, 4>, ress_pipe_smem(C, true), &g2);
+        if (rc == PHGPU_OK) select_sweep_variants(C, PHGPU_LINPIPE_MINB, PHGPU_RESS_MINB);
     }
     if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 8, 0>(C);
     if (rc == PHGPU_OK) rc = configure_topo_kernels<double, 6, 1>(C);
@@ -2469,10 +2470,15 @@ void launch_elem_res(Ctx& C, int mode, const R* x, const R* ya, const R* yb, con
         else if (mode == RM_MODRES)
             k_chunk_res<R, RM_MODRES><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
         else if constexpr (std::is_same<R, float>::value) {
-            if (!C.cfg.no_pipe && !skip && !iabres)
-                k_chunk_lin_pipe<<<std::min(nc, C.lin_pipe_grid), kChunk, lin_pipe_smem(C), C.stream>>>(
-                    ca, c0, nc, x, ya, yb, out, P, C.chunk_lmax);
-            else
+            if (!C.cfg.no_pipe && !skip && !iabres) {
+                const int g = std::min(nc, C.lin_pipe_grid);
+                if (C.lin_minb == 3)
+                    k_chunk_lin_pipe<3><<<g, kChunk, lin_pipe_smem(C), C.stream>>>(ca, c0, nc, x, ya, yb, out, P,
+                                                                                   C.chunk_lmax);
+                else
+                    k_chunk_lin_pipe<4><<<g, kChunk, lin_pipe_smem(C), C.stream>>>(ca, c0, nc, x, ya, yb, out, P,
+                                                                                   C.chunk_lmax);
+            } else
                 k_chunk_res<R, RM_LIN><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
         } else
             k_chunk_res<R, RM_LIN><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
@@ -2505,6 +2511,68 @@ void launch_qrec(Ctx& C, const R* x, const R* y, R* out) {
 template void launch_qrec<double>(Ctx&, const double*, const double*, double*);
 template void launch_qrec<float>(Ctx&, const float*, const float*, float*);
 
+// ---------------------------------------------------------------------------
+// autotuner of the two pipelined sweeps' register/occupancy variants
+// ---------------------------------------------------------------------------
+// (0 selects the compiled-in default of each)
+void select_sweep_variants(Ctx& C, int lin_minb, int ress_minb) {
+    static_assert(PHGPU_LINPIPE_MINB >= 3 && PHGPU_LINPIPE_MINB <= 4, "linearized-product variants are 3 and 4");
+    static_assert(PHGPU_RESS_MINB >= 2 && PHGPU_RESS_MINB <= 4, "split-residual variants are 2, 3 and 4");
+    C.lin_minb = (lin_minb == 3 || lin_minb == 4) ? lin_minb : PHGPU_LINPIPE_MINB;
+    C.ress_minb = (ress_minb >= 2 && ress_minb <= 4) ? ress_minb : PHGPU_RESS_MINB;
+    C.lin_pipe_grid = C.lin_grids[C.lin_minb - 3];
+    C.ress_pipe_grid = C.ress_grids[C.ress_minb - 2];
+}
+
+// Each candidate runs once to warm up, then three times between CUDA events, on the context's own
+// mesh and state (the FP32 split of y and ac, which the next assembly writes again; direction =
+// the state for the linearized product; outputs to scratch); the fastest of each sweep is kept.
+// The variants run the same code with different register budgets, so the results do not depend
+// on the choice.  The split residual is tuned only when it is the outer residual in use.
+int autotune_sweeps(Ctx& C) {
+    if (C.tuned || C.tune_forced || C.cfg.no_pipe || C.E == 0) return PHGPU_OK;
+    const size_t n5 = 5 * (size_t)C.N;
+    const long long l0 = C.launches;
+    split_f32(C, C.d_y, C.d_yf, C.d_ylo, n5);
+    to_f32(C, C.d_ac, C.d_acf, n5);
+    cudaEvent_t e0 = C.ev[2], e1 = C.ev[3];
+    auto time_it = [&](auto&& fn) {
+        fn();
+        cudaEventRecord(e0, C.stream);
+        for (int r = 0; r < 3; ++r) fn();
+        cudaEventRecord(e1, C.stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return (double)ms / 3.0;
+    };
+    const int keep_r = C.ress_minb;
+    double best = 1e300;
+    int best_l = C.lin_minb;
+    for (int m = 3; m <= 4; ++m) {
+        select_sweep_variants(C, m, keep_r);
+        const double t = time_it([&] {
+            launch_elem_res<float>(C, RM_LIN, C.d_xf, C.d_yf, C.d_yf, nullptr, C.d_t32, 0, nullptr);
+        });
+        C.tune_ms[m - 3] = t;
+        if (t < best) { best = t; best_l = m; }
+    }
+    int best_r = keep_r;
+    if (C.cfg.outer_residual == PHGPU_RES_SPLITDF) {
+        best = 1e300;
+        for (int m = 2; m <= 4; ++m) {
+            select_sweep_variants(C, best_l, m);
+            const double t = time_it([&] { launch_elem_ress(C, C.d_yf, C.d_ylo, C.d_acf, C.d_t64, nullptr); });
+            C.tune_ms[2 + m - 2] = t;
+            if (t < best) { best = t; best_r = m; }
+        }
+    }
+    C.launches = l0;  // tuning launches are not part of the solve
+    select_sweep_variants(C, best_l, best_r);
+    C.tuned = true;
+    return check(C, cudaGetLastError(), "autotune");
+}
+
 void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf, const float* acf, double* out) {
     const Phys<double> P = make_phys<double>(C.cfg);
     const Phys<float> Pf = make_phys<float>(C.cfg);
@@ -2533,12 +2601,19 @@ void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* ac
         if (nc <= 0) continue;
         if (!C.cfg.no_pipe) {
             const int g = std::min(nc, C.ress_pipe_grid);
-            if (ql)
-                k_chunk_ress_pipe<true><<<g, kChunk, ress_pipe_smem(C, true), C.stream>>>(
-                    ca, c0, nc, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql, C.chunk_lmax);
-            else
-                k_chunk_ress_pipe<false><<<g, kChunk, ress_pipe_smem(C, false), C.stream>>>(
-                    ca, c0, nc, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql, C.chunk_lmax);
+            const size_t smp = ress_pipe_smem(C, ql != nullptr);
+#define PH_RESS(Q, M) k_chunk_ress_pipe<Q, M><<<g, kChunk, smp, C.stream>>>(ca, c0, nc, C.d_xf, C.d_xlo, yh, ylo, \
+                                                                          acf, out, Pf, K, ql, C.chunk_lmax)
+            if (ql) {
+                if (C.ress_minb == 2) PH_RESS(true, 2);
+                else if (C.ress_minb == 4) PH_RESS(true, 4);
+                else PH_RESS(true, 3);
+            } else {
+                if (C.ress_minb == 2) PH_RESS(false, 2);
+                else if (C.ress_minb == 4) PH_RESS(false, 4);
+                else PH_RESS(false, 3);
+            }
+#undef PH_RESS
         } else if (ql) {
             k_chunk_ress<true><<<nc, kChunk, sm, C.stream>>>(ca, c0, C.d_xf, C.d_xlo, yh, ylo, acf, out, Pf, K, ql);
         } else {

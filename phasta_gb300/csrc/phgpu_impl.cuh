@@ -99,6 +99,7 @@ struct CycleGraph {
     std::vector<long long> launches;  // kernels in the body of iteration i
     phgpu_config key{};
     int vsize = 0, min_iters = 0;
+    int lin_minb = 0;                 // the linearized-product variant fixed in the graph
     const void* lhs = nullptr;
     bool disabled = false;            // a graph call failed: cycles are launched kernel by kernel
     long long runs = 0;               // cycles run as a graph
@@ -115,6 +116,7 @@ struct StepGraph {
     cudaGraphExec_t exec = nullptr;
     phgpu_config key{};
     int nitr = 0;
+    int lin_minb = 0, ress_minb = 0;  // the sweep variants fixed in the graph
     long long fixed_launches = 0;     // kernels outside the Krylov iterations
     std::vector<long long> body_launches;  // kernels of Krylov iteration i (1-based)
     bool disabled = false;
@@ -262,8 +264,16 @@ struct Ctx {
     CycleGraph cyc_net;           // the learned preconditioner's flexible GMRES cycle
     StepGraph stepg;              // the whole time step
     NetCtx net;
-    int lin_pipe_grid = 1;        // its CTAs per colour launch (resident slots)
+    int lin_pipe_grid = 1;        // its CTAs per colour launch (resident slots) of the chosen variant
     int ress_pipe_grid = 1;       // the same for the pipelined split outer residual
+    // autotuned register/occupancy variants of the two pipelined sweeps (elements.cu): the
+    // minimum CTAs per SM each is compiled for (linearized product 3 or 4, split residual 2, 3
+    // or 4), their resident grids, the device time each took when tuned (ms, -1 untimed), and
+    // whether they were chosen by timing (tuned) or forced (phgpu_set_tuning)
+    int lin_minb = 4, ress_minb = 3;
+    int lin_grids[2] = {1, 1}, ress_grids[3] = {1, 1, 1};
+    double tune_ms[5] = {-1, -1, -1, -1, -1};
+    bool tuned = false, tune_forced = false;
     double* h_scal = nullptr;     // pinned mirror
     int* h_flag = nullptr;
 
@@ -316,6 +326,10 @@ void launch_topo(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R
 void upload_tables(Ctx& C);
 int build_chunks(Ctx& C, const int* ien, const double* x_ref);
 int configure_element_kernels(Ctx& C);
+// time the variants of the pipelined linearized product and split residual on the resident
+// FP32 state (d_yf, d_ylo, d_acf) and keep the fastest of each (no-op once tuned or forced)
+int autotune_sweeps(Ctx& C);
+void select_sweep_variants(Ctx& C, int lin_minb, int ress_minb);
 
 // ---- nodal kernels (nodal.cu) ----
 template <typename R> void bc3res(Ctx& C, R* r);

@@ -559,7 +559,7 @@ bool cycle_graph(Ctx& C, int min_iters, bool sparse, bool ebe, bool learned = fa
     key.istep = 0;
     key.eGMRES = 0.0;
     const void* lhs = !sparse ? nullptr : ebe ? (const void*)ebe_lhs<V>(C) : (const void*)sparse_lhs<V>(C);
-    if (G.exec && G.vsize == (int)sizeof(V) && G.min_iters == min_iters && G.lhs == lhs &&
+    if (G.exec && G.vsize == (int)sizeof(V) && G.min_iters == min_iters && G.lhs == lhs && G.lin_minb == C.lin_minb &&
         std::memcmp(&G.key, &key, sizeof key) == 0)
         return true;
     phgpu::cycle_graph_free(G);
@@ -605,6 +605,7 @@ bool cycle_graph(Ctx& C, int min_iters, bool sparse, bool ebe, bool learned = fa
     G.key = key;
     G.vsize = (int)sizeof(V);
     G.min_iters = min_iters;
+    G.lin_minb = C.lin_minb;
     G.lhs = lhs;
     return true;
 }
@@ -924,6 +925,7 @@ int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
     if (C.cfg.precond == PHGPU_PRECOND_LEARNED && (C.cfg.precision != PHGPU_MIXED || C.cfg.ap_mode != PHGPU_AP_LINEAR))
         return fail(C, PHGPU_ERR_UNSUPPORTED, "the learned preconditioner needs mixed precision with the linearized product");
     const bool asm_bd = !sparse || lhs;
+    if (C.cfg.precision == PHGPU_MIXED && C.cfg.ap_mode == PHGPU_AP_LINEAR) PH_TRY(autotune_sweeps(C));
     cudaEventRecord(C.ev[0], C.stream);
     PH_TRY(assemble_and_factor(C, lhs, asm_bd, sparse, ebe));
     PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
@@ -1148,6 +1150,8 @@ int step_graph_build(Ctx& C, int nitr) {
     G.key.iter = G.key.istep = 0;
     G.key.eGMRES = 0.0;
     G.nitr = nitr;
+    G.lin_minb = C.lin_minb;
+    G.ress_minb = C.ress_minb;
     return PHGPU_OK;
 }
 
@@ -1159,7 +1163,8 @@ int step_graph_run(Ctx& C, int nitr, phgpu_stats* st, bool* used) {
     phgpu_config key = C.cfg;
     key.iter = key.istep = 0;
     key.eGMRES = 0.0;
-    if (!G.exec || G.nitr != nitr || std::memcmp(&G.key, &key, sizeof key) != 0) {
+    if (!G.exec || G.nitr != nitr || G.lin_minb != C.lin_minb || G.ress_minb != C.ress_minb ||
+        std::memcmp(&G.key, &key, sizeof key) != 0) {
         const int rc = step_graph_build(C, nitr);
         if (rc != PHGPU_OK) {
             if (G.disabled) {
@@ -1209,6 +1214,7 @@ int step_graph_run(Ctx& C, int nitr, phgpu_stats* st, bool* used) {
 int time_step_dev(Ctx& C, int nitr, phgpu_stats* st) {
     if (step_graph_eligible(C, nitr)) {
         bool used = false;
+        PH_TRY(autotune_sweeps(C));  // before the kernels are fixed in the graph
         PH_TRY(step_graph_run(C, nitr, st, &used));
         if (used) return PHGPU_OK;
     }
@@ -1492,6 +1498,33 @@ const char* phgpu_last_error(phgpu_ctx* h) { return h ? h->c.err.c_str() : "null
 void* phgpu_stream(phgpu_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
 int phgpu_num_colors(phgpu_ctx* h) { return h ? (int)h->c.chunk_col_start.size() - 1 : 0; }
 long long phgpu_kernel_launches(phgpu_ctx* h) { return h ? h->c.launches : 0; }
+
+int phgpu_set_tuning(phgpu_ctx* h, int lin_minb, int ress_minb) {
+    if (!h) return PHGPU_ERR_INVALID;
+    Ctx& C = h->c;
+    C.err.clear();
+    if (lin_minb == 0 && ress_minb == 0) {
+        C.tune_forced = false;
+        C.tuned = false;
+        for (double& t : C.tune_ms) t = -1.0;
+        phgpu::select_sweep_variants(C, 0, 0);
+        return PHGPU_OK;
+    }
+    if (lin_minb < 3 || lin_minb > 4 || ress_minb < 2 || ress_minb > 4)
+        return phgpu::fail(C, PHGPU_ERR_INVALID, "sweep variants: lin_minb 3 or 4, ress_minb 2, 3 or 4");
+    C.tune_forced = true;
+    phgpu::select_sweep_variants(C, lin_minb, ress_minb);
+    return PHGPU_OK;
+}
+
+int phgpu_tuning(phgpu_ctx* h, int* lin_minb, int* ress_minb, double* ms) {
+    if (!h) return PHGPU_ERR_INVALID;
+    const Ctx& C = h->c;
+    if (lin_minb) *lin_minb = C.lin_minb;
+    if (ress_minb) *ress_minb = C.ress_minb;
+    if (ms) for (int i = 0; i < 5; ++i) ms[i] = C.tune_ms[i];
+    return C.tune_forced ? 2 : C.tuned ? 1 : 0;
+}
 
 long long phgpu_step_graphs(phgpu_ctx* h) {
     if (!h) return 0;

@@ -199,6 +199,20 @@ class GpuSolver:
         """Time steps run as one CUDA graph (-1: the graph could not be built)."""
         return self.lib.phgpu_step_graphs(self.h)
 
+    def set_tuning(self, lin_minb: int = 0, ress_minb: int = 0) -> None:
+        """Force the pipelined sweeps' variants (minimum CTAs per SM: linearized product 3 or 4,
+        split residual 2, 3 or 4), or with (0, 0) return to autotuning at the next solve."""
+        self._check(self.lib.phgpu_set_tuning(self.h, int(lin_minb), int(ress_minb)))
+
+    def tuning(self) -> dict:
+        """The sweep variants in use, how they were chosen and each variant's tuned time (ms)."""
+        lm, rm = C.c_int(0), C.c_int(0)
+        ms = np.zeros(5)
+        state = self.lib.phgpu_tuning(self.h, C.byref(lm), C.byref(rm), L.dptr(ms))
+        how = {0: "default", 1: "tuned", 2: "forced"}[state]
+        return {"lin_minb": lm.value, "ress_minb": rm.value, "how": how,
+                "lin_ms": {3: ms[0], 4: ms[1]}, "ress_ms": {2: ms[2], 3: ms[3], 4: ms[4]}}
+
     def stream(self) -> int:
         return self.lib.phgpu_stream(self.h)
 
