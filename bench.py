@@ -324,6 +324,8 @@ def run_gpu(args, rank, world):
         result["channel"] = channel_object(args, weights)
     if not args.skip_mixed:
         result["mixed_topology"] = mixed_topology_object(args)
+    if not args.skip_order:
+        result["node_order"] = node_order_object(args)
     if not args.skip_sparse:
         result["sparse_solver"] = sparse_solver(args)
         result["ebe_solver"] = sparse_solver(args, ebe=True)
@@ -361,6 +363,39 @@ def mixed_topology_object(args):
                         f"Newton", "elements": E, "nodes": case.nshg, "value": E * steps / (t["ms"] / 1e3),
             "unit": "elements/s", "ms_per_step": t["ms"] / steps, "gpu_launches": t["launches"], **conv,
             "launch": "tets: persistent pipelined kernel per colour; hexes and prisms: one launch per colour"}
+
+
+def node_order_object(args):
+    """The channel at --order-n^3 x 6 (mixed precision, block-diagonal GMRES) with its nodes in
+    generation order, shuffled at random, and shuffled then renumbered by reverse Cuthill-McKee
+    (phgpu_rcm_order): ms per Newton iteration over 2 time steps x 3 Newton iterations each."""
+    import torch
+
+    from phasta_gb300 import _lib as L
+    from phasta_gb300 import mesh
+    from phasta_gb300.solver import GpuSolver, rcm_order
+    n = args.order_n
+    case, params, y0, ac0 = make_workload(n, "mixed", "channel", precond=L.PHGPU_PRECOND_BDIAG)
+    shuf = np.random.default_rng(20261204).permutation(case.nshg)
+    sh = mesh.renumber(case, shuf)
+    t0 = time.perf_counter()
+    perm, bw_shuf, bw_rcm = rcm_order(sh)
+    t_rcm = time.perf_counter() - t0
+    _, bw_gen, _ = rcm_order(case)
+    ys, acs = mesh.renumber_field(y0, shuf, 5), mesh.renumber_field(ac0, shuf, 5)
+    out = {"workload": WORKLOADS["channel"].format(n=n), "rcm_host_s": t_rcm}
+    for name, m, y, ac, bw in (("generated", case, y0, ac0, bw_gen), ("shuffled", sh, ys, acs, bw_shuf),
+                               ("rcm_of_shuffled", mesh.renumber(sh, perm), mesh.renumber_field(ys, perm, 5),
+                                mesh.renumber_field(acs, perm, 5), bw_rcm)):
+        g = GpuSolver(m, params)
+        s = torch.cuda.ExternalStream(g.stream())
+        g.upload(y, ac, y, ac)
+        g.time_step_dev(NEWTON_PER_TIMESTEP)
+        steps = 2 * NEWTON_PER_TIMESTEP
+        t = run_newton(g, m, y, ac, steps, s)
+        out[name] = {"ms_per_step": t["ms"] / steps, "bandwidth": int(bw)}
+        g.close()
+    return out
 
 
 def channel_object(args, weights):
@@ -634,6 +669,8 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-channel", action="store_true")
     ap.add_argument("--skip-mixed", action="store_true")
+    ap.add_argument("--skip-order", action="store_true", help="leave out the node-order (RCM) object")
+    ap.add_argument("--order-n", type=int, default=96)
     ap.add_argument("--mixed-n", type=int, default=80)
     ap.add_argument("--skip-sparse", action="store_true", help="leave out the assembled-tangent solver lines")
     args = ap.parse_args()

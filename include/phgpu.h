@@ -159,6 +159,15 @@ enum {
 
 typedef struct phgpu_ctx phgpu_ctx;
 
+/* Reverse Cuthill-McKee order of the mesh's nodes (host only, no device needed): new_of_old[n]
+ * is node n's number in the new order.  Nodes are adjacent when they share an interior element;
+ * a periodic slave is adjacent to its master.  The caller renumbers its arrays with it before
+ * phgpu_create (PHASTA's pre-processor does this before the solver reads the mesh); the optional
+ * outputs give the graph's bandwidth max |i - j| over adjacent nodes before and after.
+ * Deterministic (ties broken by node number); PHGPU_ERR_INVALID on a bad mesh. */
+int phgpu_rcm_order(const phgpu_mesh* mesh, int* new_of_old, long long* bandwidth_before,
+                    long long* bandwidth_after);
+
 /* set-up: copies the mesh to the device, colours the elements; one GPU, one stream */
 int phgpu_create(const phgpu_mesh* mesh, const phgpu_config* cfg, phgpu_ctx** out);
 int phgpu_destroy(phgpu_ctx* ctx);

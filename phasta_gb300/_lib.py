@@ -108,6 +108,8 @@ def lib():
         "phgpu_kernel_launches": ([vp], C.c_longlong),
         "phgpu_graph_cycles": ([vp], C.c_longlong),
         "phgpu_step_graphs": ([vp], C.c_longlong),
+        "phgpu_rcm_order": ([C.POINTER(Mesh), C.POINTER(C.c_int), C.POINTER(C.c_longlong),
+                             C.POINTER(C.c_longlong)], C.c_int),
         "phgpu_set_tuning": ([vp, C.c_int, C.c_int], C.c_int),
         "phgpu_tuning": ([vp, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp], C.c_int),
         "phgpu_elmmfg": ([vp, _dp, _dp, _dp, _dp, _dp, C.c_int], C.c_int),

@@ -1,6 +1,6 @@
 """Build the CUDA library of the hot path in place (sm_103a only).
 
-``build()`` compiles ``csrc/*.cu`` (and the host-only ``csrc/phio.cpp``) into ``phasta_gb300/libphgpu.so`` with one
+``build()`` compiles ``csrc/*.cu`` (and the host-only ``csrc/phio.cpp``, ``csrc/reorder.cpp``) into ``phasta_gb300/libphgpu.so`` with one
 ``-gencode`` (compute_103a/sm_103a); the translation units are compiled in
 parallel and linked with the CUDA runtime.  Nothing is installed outside the
 package directory.
@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 LIB = PKG / "libphgpu.so"
 BUILD = PKG / "_build"
 SOURCES = ["elements.cu", "nodal.cu", "solver.cu", "chunks.cu", "noalloc.cu", "sparse.cu", "tangent.cu", "topo_ress.cu",
-           "learn.cu", "phio.cpp"]
+           "learn.cu", "phio.cpp", "reorder.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

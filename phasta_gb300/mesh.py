@@ -306,6 +306,29 @@ def concat(*cases: Case) -> Case:
                 ienw=cat["ienw"].astype(np.int32), meta={"parts": [c.meta for c in cases]})
 
 
+def renumber(case: Case, new_of_old: np.ndarray) -> Case:
+    """The same mesh with node n renamed new_of_old[n] (elements, faces and their order unchanged)."""
+    p = np.asarray(new_of_old, dtype=np.int64)
+    N = case.nshg
+    if p.shape != (N,) or not np.array_equal(np.sort(p), np.arange(N)):
+        raise ValueError("new_of_old must be a permutation of the nodes")
+    old_of_new = np.empty(N, np.int64)
+    old_of_new[p] = np.arange(N)
+    return Case(nshg=N, x=np.ascontiguousarray(case.x[old_of_new]), ien=p[case.ien].astype(np.int32),
+                ienb=p[case.ienb].astype(np.int32), iBCB=case.iBCB.copy(), BCB=case.BCB.copy(),
+                iBC=case.iBC[old_of_new].astype(np.int32), BC=np.ascontiguousarray(case.BC[:, old_of_new]),
+                iper=p[case.iper[old_of_new]].astype(np.int32), h=case.h, meta=dict(case.meta),
+                ienh=p[case.ienh].astype(np.int32), ienw=p[case.ienw].astype(np.int32))
+
+
+def renumber_field(v: np.ndarray, new_of_old: np.ndarray, ncomp: int) -> np.ndarray:
+    """A nodal field in the reference's column-major (nshg, ncomp) layout, renumbered."""
+    p = np.asarray(new_of_old, dtype=np.int64)
+    old_of_new = np.empty_like(p)
+    old_of_new[p] = np.arange(p.size)
+    return np.ascontiguousarray(np.asarray(v).reshape(ncomp, -1)[:, old_of_new]).reshape(-1)
+
+
 # ---------------------------------------------------------------------------
 # seeded states (counter-based: the value of (node, dof) does not depend on
 # the mesh size or traversal order)

@@ -132,6 +132,19 @@ def genadj(case: Case, nnz: int = 40):
     return colm, rowp[: icnt.value].copy()
 
 
+def rcm_order(case: Case) -> tuple[np.ndarray, int, int]:
+    """Reverse Cuthill-McKee node order (phgpu_rcm_order, host only): new_of_old and the graph's
+    bandwidth before and after; apply it with mesh.renumber / mesh.renumber_field."""
+    lib = L.lib()
+    ma = _MeshArrays(case)
+    p = np.zeros(case.nshg, np.int32)
+    b0, b1 = C.c_longlong(), C.c_longlong()
+    rc = lib.phgpu_rcm_order(C.byref(ma.m), L.iptr(p), C.byref(b0), C.byref(b1))
+    if rc != 0:
+        raise PhgpuError(rc, "rcm_order: invalid mesh")
+    return p, b0.value, b1.value
+
+
 class GpuSolver:
     def __init__(self, case: Case, params: dict):
         self.lib = L.lib()
