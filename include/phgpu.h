@@ -196,8 +196,11 @@ long long phgpu_step_graphs(phgpu_ctx* ctx);
  * matrix-free solver: the linearized product (compiled for at least 3 or 4 resident CTAs per SM)
  * and the double-float split outer residual (2, 3 or 4).  Before its first mixed-precision
  * linearized solve or graph-captured time step, a context times each variant on its own mesh
- * and state (a warm-up and three timed sweeps each, CUDA events) and keeps the fastest; the
- * variants compute the same values, so the choice changes no result.
+ * and state (a warm-up and three timed sweeps each, CUDA events) and keeps the fastest when it
+ * beats the compiled-in default by more than 3%, for the context's lifetime.  The variants are
+ * the same arithmetic compiled under different register budgets: each is deterministic, and
+ * they agree with one another to FP32 rounding (the compiler may fuse multiplies and adds
+ * differently), not bit for bit.
  * phgpu_set_tuning forces a choice (lin_minb 3 or 4, ress_minb 2, 3 or 4), or with (0, 0)
  * returns to the compiled-in defaults and tunes again at the next solve.
  * phgpu_tuning gives the current choice and, in ms[5], the mean time of each variant in ms

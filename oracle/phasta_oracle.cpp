@@ -169,6 +169,110 @@ const Topo& topo(int lcsyst) {
     return t[lcsyst - 1];
 }
 
+// boundary element topologies (genint.f, genshpb.f; elmmfg.f:171-188 turns a wedge block's
+// lcsyst 3 into nenbl, so 3 is the triangle face and 4 the quadrilateral face), linear basis
+struct BTopo {
+    int lcsyst, nshl, nshlb, ngaussb;
+    int lnode[4];          // face nodes, 0-based, getbnodes order (hierarchic.f:90-165)
+    double shpb[4][8];     // [q][a]
+    double shglb[4][3][8]; // [q][i][a]
+    double Qwtb[4];
+};
+
+// the linear hex and wedge shapes of make_topo at one parent point
+void hex_shape(const double par[3], double N[8], double dN[3][8]) {
+    const double sgn[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                              {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+    for (int a = 0; a < 8; ++a) {
+        const double f[3] = {(1.0 + sgn[a][0] * par[0]) / 2.0, (1.0 + sgn[a][1] * par[1]) / 2.0,
+                             (1.0 + sgn[a][2] * par[2]) / 2.0};
+        N[a] = f[0] * f[1] * f[2];
+        dN[0][a] = sgn[a][0] / 2.0 * f[1] * f[2];
+        dN[1][a] = f[0] * sgn[a][1] / 2.0 * f[2];
+        dN[2][a] = f[0] * f[1] * sgn[a][2] / 2.0;
+    }
+}
+void wedge_shape(double r, double s2, double z, double N[8], double dN[3][8]) {
+    const double L[3] = {1.0 - r - s2, r, s2};
+    const double dLr[3] = {-1.0, 1.0, 0.0}, dLs[3] = {-1.0, 0.0, 1.0};
+    for (int a = 0; a < 6; ++a) {
+        const int v = a % 3;
+        const double zs = a < 3 ? -1.0 : 1.0;
+        const double fz = (1.0 + zs * z) / 2.0;
+        N[a] = L[v] * fz;
+        dN[0][a] = dLr[v] * fz / 2.0;
+        dN[1][a] = dLs[v] * fz / 2.0;
+        dN[2][a] = L[v] * zs / 2.0;
+    }
+}
+
+BTopo make_btopo(int lcsyst) {
+    BTopo t{};
+    t.lcsyst = lcsyst;
+    if (lcsyst == 1) {
+        // the tet's 3-point triangle rule on face (0,1,2) (genint.f:61-75, genshpb.f)
+        const Tables& T = tables();
+        t.nshl = 4;
+        t.nshlb = 3;
+        t.ngaussb = 3;
+        for (int n = 0; n < 3; ++n) t.lnode[n] = n;
+        for (int q = 0; q < 3; ++q) {
+            t.Qwtb[q] = T.Qwtb[q];
+            for (int a = 0; a < 4; ++a) {
+                t.shpb[q][a] = T.shpb[q][a];
+                for (int i = 0; i < 3; ++i) t.shglb[q][i][a] = T.shglb[q][i][a];
+            }
+        }
+    } else if (lcsyst == 2) {
+        // symquad.c rule 2: (xi, eta) = (-+1/sqrt(3)) with xi fastest on zeta = -1, weights 1
+        // (genint.f:140-142, no scaling)
+        const double g = 0.577350269189626;
+        t.nshl = 8;
+        t.nshlb = 4;
+        t.ngaussb = 4;
+        for (int n = 0; n < 4; ++n) t.lnode[n] = n;
+        for (int q = 0; q < 4; ++q) {
+            const double par[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, -1.0};
+            t.Qwtb[q] = 1.0;
+            hex_shape(par, t.shpb[q], t.shglb[q]);
+        }
+    } else if (lcsyst == 3) {
+        // symtri.c 3-point rule with its last point moved first (genint.f:325-332): (1/6, 1/6),
+        // (2/3, 1/6), (1/6, 2/3) on zeta = -1, weights 0.333333333333333
+        const double P3 = 0.166666666666667, P4 = 0.666666666666667;
+        const double tri[3][2] = {{P3, P3}, {P4, P3}, {P3, P4}};
+        t.nshl = 6;
+        t.nshlb = 3;
+        t.ngaussb = 3;
+        for (int n = 0; n < 3; ++n) t.lnode[n] = n;
+        for (int q = 0; q < 3; ++q) {
+            t.Qwtb[q] = 0.333333333333333;
+            wedge_shape(tri[q][0], tri[q][1], -1.0, t.shpb[q], t.shglb[q]);
+        }
+    } else {
+        // symquadw.c rule 2: r = 0.211324865405187, 0.788675134594813 (r fastest), s = 0,
+        // zeta = -+0.577350269189626, weights 1 (genint.f:340-343); face nodes 1, 4, 5, 2
+        const double r[2] = {0.211324865405187, 0.788675134594813}, g = 0.577350269189626;
+        t.nshl = 6;
+        t.nshlb = 4;
+        t.ngaussb = 4;
+        t.lnode[0] = 0;
+        t.lnode[1] = 3;
+        t.lnode[2] = 4;
+        t.lnode[3] = 1;
+        for (int q = 0; q < 4; ++q) {
+            t.Qwtb[q] = 1.0;
+            wedge_shape(r[q & 1], 0.0, (q & 2) ? g : -g, t.shpb[q], t.shglb[q]);
+        }
+    }
+    return t;
+}
+
+const BTopo& btopo(int lcsyst) {
+    static const BTopo t[4] = {make_btopo(1), make_btopo(2), make_btopo(3), make_btopo(4)};
+    return t[lcsyst - 1];
+}
+
 // ---------------------------------------------------------------------------
 // e3.f for one element (lhs = 0, idiff = 0, iLES = iRANS = iLSet = 0, iDC = 0,
 // no body force, ipord = 1, itau = 0)
@@ -833,25 +937,28 @@ void e3_element(const or_common& c, const Topo& tp, int ires, int iprec, const d
 }
 
 // ---------------------------------------------------------------------------
-// e3b.f + e3bvar.f for one boundary tet (face = local nodes 0,1,2), ires 1/3
+// e3b.f + e3bvar.f for one boundary element of topology bt (ires 1/3): the state at a point
+// from the face nodes, the metric and gradients from all nodes, the normal by e3bvar.f:156-176
+// and the weight by e3bvar.f:184-197 for each boundary topology
 // ---------------------------------------------------------------------------
-void e3b_element(const or_common& c, const double (*yl)[5], int iBCB, const double (*BCB)[6],
+void e3b_element(const or_common& c, const BTopo& bt, const double (*yl)[5], int iBCB, const double (*BCB)[6],
                  const double (*xlb)[3], double (*rl)[5]) {
-    const Tables& T = tables();
     const double Rgas = c.Rgas, gamma = c.gamma, gamma1 = c.gamma1;
-    const int nshlb = 3, nshl = 4, nenl = 4;
-    for (int intp = 0; intp < 3; ++intp) {
-        if (T.Qwtb[intp] == zero) continue;
-        const double* shpb = T.shpb[intp];
-        const double (*shglb)[4] = T.shglb[intp];
+    const int nshlb = bt.nshlb, nshl = bt.nshl, nenl = bt.nshl;
+    const int* lnode = bt.lnode;
+    for (int intp = 0; intp < bt.ngaussb; ++intp) {
+        if (bt.Qwtb[intp] == zero) continue;
+        const double* shpb = bt.shpb[intp];
+        const double (*shglb)[8] = bt.shglb[intp];
         // e3bvar.f:100-121
         double pres = 0, u1 = 0, u2 = 0, u3 = 0, Tq = 0;
         for (int n = 0; n < nshlb; ++n) {
-            pres = pres + shpb[n] * yl[n][0];
-            u1 = u1 + shpb[n] * yl[n][1];
-            u2 = u2 + shpb[n] * yl[n][2];
-            u3 = u3 + shpb[n] * yl[n][3];
-            Tq = Tq + shpb[n] * yl[n][4];
+            const int l = lnode[n];
+            pres = pres + shpb[l] * yl[l][0];
+            u1 = u1 + shpb[l] * yl[l][1];
+            u2 = u2 + shpb[l] * yl[l][2];
+            u3 = u3 + shpb[l] * yl[l][3];
+            Tq = Tq + shpb[l] * yl[l][4];
         }
         const double rk = pt5 * (u1 * u1 + u2 * u2 + u3 * u3);
         const double rho = pres / (Rgas * Tq);
@@ -862,14 +969,30 @@ void e3b_element(const or_common& c, const double (*yl)[5], int iBCB, const doub
         for (int n = 0; n < nenl; ++n)
             for (int i = 0; i < 3; ++i)
                 for (int j = 0; j < 3; ++j) dx[i][j] = dx[i][j] + xlb[n][i] * shglb[j][n];
-        double v1[3], v2[3];
-        for (int i = 0; i < 3; ++i) { v1[i] = xlb[1][i] - xlb[0][i]; v2[i] = xlb[2][i] - xlb[0][i]; }
-        const double t1 = v1[1] * v2[2] - v2[1] * v1[2];
-        const double t2 = v2[0] * v1[2] - v1[0] * v2[2];
-        const double t3 = v1[0] * v2[1] - v2[0] * v1[1];
+        double t1, t2, t3;
+        if (bt.lcsyst == 4) {
+            t1 = dx[1][0] * dx[2][2] - dx[1][2] * dx[2][0];
+            t2 = dx[2][0] * dx[0][2] - dx[2][2] * dx[0][0];
+            t3 = dx[0][0] * dx[1][2] - dx[0][2] * dx[1][0];
+        } else {
+            double v1[3], v2[3];
+            for (int i = 0; i < 3; ++i) { v1[i] = xlb[1][i] - xlb[0][i]; v2[i] = xlb[2][i] - xlb[0][i]; }
+            if (bt.lcsyst == 1) {
+                t1 = v1[1] * v2[2] - v2[1] * v1[2];
+                t2 = v2[0] * v1[2] - v1[0] * v2[2];
+                t3 = v1[0] * v2[1] - v2[0] * v1[1];
+            } else {
+                t1 = -v1[1] * v2[2] + v2[1] * v1[2];
+                t2 = -v2[0] * v1[2] + v1[0] * v2[2];
+                t3 = -v1[0] * v2[1] + v2[0] * v1[1];
+            }
+        }
         double temp = one / std::sqrt(t1 * t1 + t2 * t2 + t3 * t3);
         const double bn[3] = {t1 * temp, t2 * temp, t3 * temp};
-        const double WdetJb = T.Qwtb[intp] / (four * temp);
+        double WdetJb;
+        if (bt.lcsyst == 3) WdetJb = (one - bt.Qwtb[intp]) / (four * temp);
+        else if (bt.lcsyst == 4) WdetJb = bt.Qwtb[intp] / temp;
+        else WdetJb = bt.Qwtb[intp] / (four * temp);
         double g[3][5] = {{0}};
         if (c.Navier == 1) {
             double di[3][3];
@@ -896,16 +1019,16 @@ void e3b_element(const or_common& c, const double (*yl)[5], int iBCB, const doub
         }
         double rou = 0, p = 0;
         for (int n = 0; n < nshlb; ++n) {
-            rou = rou + shpb[n] * BCB[n][0];
-            p = p + shpb[n] * BCB[n][1];
+            rou = rou + shpb[lnode[n]] * BCB[n][0];
+            p = p + shpb[lnode[n]] * BCB[n][1];
         }
         double Fv2 = 0, Fv3 = 0, Fv4 = 0, Fh5 = 0;
         if (c.Navier == 1)
             for (int n = 0; n < nshlb; ++n) {
-                Fv2 = Fv2 + shpb[n] * BCB[n][2];
-                Fv3 = Fv3 + shpb[n] * BCB[n][3];
-                Fv4 = Fv4 + shpb[n] * BCB[n][4];
-                Fh5 = Fh5 + shpb[n] * BCB[n][5];
+                Fv2 = Fv2 + shpb[lnode[n]] * BCB[n][2];
+                Fv3 = Fv3 + shpb[lnode[n]] * BCB[n][3];
+                Fv4 = Fv4 + shpb[lnode[n]] * BCB[n][4];
+                Fh5 = Fh5 + shpb[lnode[n]] * BCB[n][5];
             }
         // e3b.f:134-166
         double un;
@@ -946,12 +1069,13 @@ void e3b_element(const or_common& c, const double (*yl)[5], int iBCB, const doub
         }
         // e3b.f:224-241
         for (int n = 0; n < nshlb; ++n) {
-            const double w = WdetJb * shpb[n];
-            rl[n][0] = rl[n][0] + w * F1;
-            rl[n][1] = rl[n][1] + w * F2;
-            rl[n][2] = rl[n][2] + w * F3;
-            rl[n][3] = rl[n][3] + w * F4;
-            rl[n][4] = rl[n][4] + w * F5;
+            const int l = lnode[n];
+            const double w = WdetJb * shpb[l];
+            rl[l][0] = rl[l][0] + w * F1;
+            rl[l][1] = rl[l][1] + w * F2;
+            rl[l][2] = rl[l][2] + w * F3;
+            rl[l][3] = rl[l][3] + w * F4;
+            rl[l][4] = rl[l][4] + w * F5;
         }
     }
 }
@@ -1168,9 +1292,29 @@ void boundary_sweep(const or_common& c, const or_mesh& m, const double* y, doubl
         for (int n = 0; n < 3; ++n)
             for (int k = 0; k < 6; ++k) bcb[n][k] = m.BCB ? m.BCB[(e * 3 + n) * 6 + k] : 0.0;
         double rl[4][5] = {{0}};
-        e3b_element(c, yl, m.iBCB ? m.iBCB[2 * e] : 0, bcb, xl, rl);
+        e3b_element(c, btopo(1), yl, m.iBCB ? m.iBCB[2 * e] : 0, bcb, xl, rl);
         for (int k = 0; k < 5; ++k)
             for (int a = 0; a < 4; ++a) res[k * (size_t)nshg + ie[a]] += rl[a][k];
+    }
+    // boundary hex and wedge blocks (elmmfg.f:171-211)
+    for (int b = 0; b < m.nbblk; ++b) {
+        const or_bnd_block& B = m.bblk[b];
+        const BTopo& bt = btopo(B.lcsyst);
+        for (int e = 0; e < B.nelem; ++e) {
+            const int* ie = B.ien + (size_t)bt.nshl * e;
+            double yl[8][5], xl[8][3];
+            for (int a = 0; a < bt.nshl; ++a) {
+                gather_y(y, nshg, ie[a], yl[a]);
+                gather_x(m.x, nshg, ie[a], xl[a]);
+            }
+            double bcb[4][6];
+            for (int n = 0; n < bt.nshlb; ++n)
+                for (int k = 0; k < 6; ++k) bcb[n][k] = B.BCB ? B.BCB[((size_t)e * bt.nshlb + n) * 6 + k] : 0.0;
+            double rl[8][5] = {{0}};
+            e3b_element(c, bt, yl, B.iBCB ? B.iBCB[2 * e] : 0, bcb, xl, rl);
+            for (int k = 0; k < 5; ++k)
+                for (int a = 0; a < bt.nshl; ++a) res[k * (size_t)nshg + ie[a]] += rl[a][k];
+        }
     }
 }
 
@@ -1425,8 +1569,24 @@ void or_e3_topo(const or_common* c, int lcsyst, int ires, int iprec, const doubl
 void or_e3b(const or_common* c, int ires, const double* yl, const int* iBCB, const double* BCB,
             const double* xlb, double* rl) {
     if (ires == 1 || ires == 3)
-        e3b_element(*c, (const double (*)[5])yl, iBCB ? iBCB[0] : 0, (const double (*)[6])BCB,
+        e3b_element(*c, btopo(1), (const double (*)[5])yl, iBCB ? iBCB[0] : 0, (const double (*)[6])BCB,
                     (const double (*)[3])xlb, (double (*)[5])rl);
+}
+
+void or_btopo_tables(int lcsyst, double shpb[32], double shglb[96], double Qwtb[4], int* nshl, int* nshlb,
+                     int* ngaussb, int lnode[4]) {
+    const BTopo& t = btopo(lcsyst);
+    *nshl = t.nshl;
+    *nshlb = t.nshlb;
+    *ngaussb = t.ngaussb;
+    for (int n = 0; n < 4; ++n) lnode[n] = n < t.nshlb ? t.lnode[n] : -1;
+    for (int q = 0; q < t.ngaussb; ++q) {
+        Qwtb[q] = t.Qwtb[q];
+        for (int a = 0; a < t.nshl; ++a) {
+            shpb[q * t.nshl + a] = t.shpb[q][a];
+            for (int i = 0; i < 3; ++i) shglb[(q * 3 + i) * t.nshl + a] = t.shglb[q][i][a];
+        }
+    }
 }
 
 // bc3res.f:23-160 (single rank)

@@ -43,6 +43,17 @@ typedef struct {
     int    iDC;                       /* discontinuity capturing: 0 off, 1 DC-mallet, 2 quadratic, 3 min */
 } or_common;
 
+/* a block of boundary hexes or wedges (genbkb.f blocks; elmmfg.f:171-211): lcsyst 2 the hex with
+ * its zeta = -1 quadrilateral face, 3 the wedge with its zeta = -1 triangle, 4 the wedge with its
+ * s = 0 quadrilateral (face nodes 1, 4, 5, 2 in getbnodes' order, hierarchic.f:161-164) */
+typedef struct {
+    int lcsyst;
+    int nelem;
+    const int* ien;           /* nelem*nshl (8 for lcsyst 2, else 6) */
+    const int* iBCB;          /* nelem*2 */
+    const double* BCB;        /* nelem*nshlb*6 : BCB[(e*nshlb + n)*6 + k] */
+} or_bnd_block;
+
 typedef struct {
     int nshg;                 /* number of (stored) nodes */
     int nelem;                /* interior tets */
@@ -63,6 +74,8 @@ typedef struct {
     const int* ienh;          /* nhex*8, reference local node order */
     int nwedge;               /* interior linear wedges (lcsyst 3) */
     const int* ienw;          /* nwedge*6 */
+    int nbblk;                /* blocks of boundary hexes and wedges */
+    const or_bnd_block* bblk;
 } or_mesh;
 
 typedef struct {
@@ -88,6 +101,12 @@ void or_tet_tables(double shp[16], double shgl[48], double Qwt[4],
 void or_e3(const or_common* c, int ires, int iprec,
            const double* yl, const double* ycl, const double* acl,
            const double* xl, double* rl, double* rml, double* bdl);
+
+/* boundary quadrature/shape tables (genint.f, genshpb.f) of boundary topology lcsyst 2, 3 or 4:
+ * shpb[q*nshl+a], shglb[(q*3+i)*nshl+a], Qwtb[q]; nshl, nshlb, ngaussb and the face nodes lnode
+ * (0-based, getbnodes order) */
+void or_btopo_tables(int lcsyst, double shpb[32], double shglb[96], double Qwtb[4], int* nshl, int* nshlb,
+                     int* ngaussb, int lnode[4]);
 
 /* quadrature/shape tables of topology lcsyst (1 tet, 2 hex, 3 wedge):
  * shp[q*nshl+a], shgl[(q*3+i)*nshl+a], Qwt[q] */

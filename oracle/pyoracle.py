@@ -29,12 +29,17 @@ class Common(C.Structure):
     ]
 
 
+class OBnd(C.Structure):
+    _fields_ = [("lcsyst", C.c_int), ("nelem", C.c_int), ("ien", _ip), ("iBCB", _ip), ("BCB", _dp)]
+
+
 class OMesh(C.Structure):
     _fields_ = [
         ("nshg", C.c_int), ("nelem", C.c_int), ("ien", _ip), ("nblk", C.c_int), ("blk_start", _ip),
         ("ngrp", C.c_int), ("grp_start", _ip), ("x", _dp), ("nbelem", C.c_int), ("ienb", _ip),
         ("iBCB", _ip), ("BCB", _dp), ("iBC", _ip), ("BC", _dp), ("iper", _ip),
         ("nhex", C.c_int), ("ienh", _ip), ("nwedge", C.c_int), ("ienw", _ip),
+        ("nbblk", C.c_int), ("bblk", C.POINTER(OBnd)),
     ]
 
 
@@ -57,6 +62,8 @@ def lib():
             "or_make_groups": ([C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, _ip, _ip, C.c_int], C.c_int),
             "or_tet_tables": ([_dp] * 6, None),
             "or_topo_tables": ([C.c_int, _dp, _dp, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int)], None),
+            "or_btopo_tables": ([C.c_int, _dp, _dp, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_int), _ip], None),
             "or_e3": ([cp, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp], None),
             "or_e3b": ([cp, C.c_int, _dp, _ip, _dp, _dp, _dp], None),
             "or_elmmfg": ([cp, mp, _dp, _dp, _dp, _dp, _dp, C.c_int, C.c_int], None),
@@ -184,10 +191,16 @@ class Oracle:
         self._iper = np.ascontiguousarray(case.iper, dtype=np.int32)
         self._ienh = np.ascontiguousarray(getattr(case, "ienh", np.zeros((0, 8))), dtype=np.int32).reshape(-1)
         self._ienw = np.ascontiguousarray(getattr(case, "ienw", np.zeros((0, 6))), dtype=np.int32).reshape(-1)
+        bnd = getattr(case, "bnd", [])
+        self._bnd_arrays = [(np.ascontiguousarray(b.ien, dtype=np.int32).reshape(-1),
+                             np.ascontiguousarray(b.iBCB, dtype=np.int32).reshape(-1),
+                             np.ascontiguousarray(b.BCB, dtype=np.float64).reshape(-1)) for b in bnd]
+        self._bblk = (OBnd * max(1, len(bnd)))(*[OBnd(b.lcsyst, b.ien.shape[0], _i(a[0]), _i(a[1]), _d(a[2]))
+                                                 for b, a in zip(bnd, self._bnd_arrays)])
         self.m = OMesh(self.nshg, E, _i(self._ien), len(self._blk) - 1, _i(self._blk), ngrp, _i(self._grp),
                        _d(self._x), case.nbelem, _i(self._ienb), _i(self._iBCB), _d(self._BCB), _i(self._iBC),
                        _d(self._BC), _i(self._iper), len(self._ienh) // 8, _i(self._ienh), len(self._ienw) // 6,
-                       _i(self._ienw))
+                       _i(self._ienw), len(bnd), self._bblk)
         self.c = common(self.params)
         self.ntotGM = 0
 
@@ -361,6 +374,19 @@ class Oracle:
         yold, acold = self.itrUpdate(yold, acold, y, ac)
         self.set_params(istep=self.params["istep"] + 1)
         return yold, acold, y, ac, stats
+
+
+def btopo_tables(lcsyst: int) -> dict:
+    """Boundary quadrature/shape tables of boundary topology lcsyst (2 hex, 3 wedge triangle face,
+    4 wedge quadrilateral face): shpb[q][a], shglb[q][i][a], Qwtb[q], lnode (0-based face nodes)."""
+    L = lib()
+    shp, shgl, qwt = np.zeros(32), np.zeros(96), np.zeros(4)
+    nshl, nshlb, ng = C.c_int(), C.c_int(), C.c_int()
+    ln = np.zeros(4, np.int32)
+    L.or_btopo_tables(lcsyst, _d(shp), _d(shgl), _d(qwt), C.byref(nshl), C.byref(nshlb), C.byref(ng), _i(ln))
+    n, q = nshl.value, ng.value
+    return {"shpb": shp[: q * n].reshape(q, n), "shglb": shgl[: 3 * q * n].reshape(q, 3, n), "Qwtb": qwt[:q],
+            "lnode": ln[: nshlb.value].copy()}
 
 
 def topo_tables(lcsyst: int) -> dict:

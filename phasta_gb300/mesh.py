@@ -41,6 +41,34 @@ def rgas() -> float:
 
 
 @dataclass
+class BndBlock:
+    """A block of boundary hexes or wedges (the reference's boundary element blocks of lcsyst
+    2, 3 and 4, genbkb.f): the whole element in its local node order with the boundary face
+    where the reference's boundary routines look for it (hex: the zeta = -1 face, nodes 1-4;
+    wedge, lcsyst 3: the zeta = -1 triangle, nodes 1-3; wedge, lcsyst 4: the s = 0 quadrilateral,
+    nodes 1, 4, 5, 2 as getbnodes lists them, hierarchic.f:161-164), its BC codes and values per
+    face node in getbnodes' order."""
+    lcsyst: int              # 2 hex/quad face, 3 wedge/triangle face, 4 wedge/quad face
+    ien: np.ndarray          # (n, nshl) int32
+    iBCB: np.ndarray         # (n, 2) int32
+    BCB: np.ndarray          # (n, nshlb, 6) float64
+
+    @property
+    def nshl(self) -> int:
+        return 8 if self.lcsyst == 2 else 6
+
+    @property
+    def nshlb(self) -> int:
+        return 3 if self.lcsyst == 3 else 4
+
+
+def bnd_block(lcsyst: int, ien) -> BndBlock:
+    ien = np.ascontiguousarray(ien, dtype=np.int32)
+    nb = 3 if lcsyst == 3 else 4
+    return BndBlock(lcsyst, ien, np.zeros((ien.shape[0], 2), np.int32), np.zeros((ien.shape[0], nb, 6)))
+
+
+@dataclass
 class Case:
     """A mesh with its boundary conditions (0-based, reference layouts)."""
     nshg: int
@@ -57,6 +85,8 @@ class Case:
     # further interior blocks (linear hexes and wedges, the reference's lcsyst 2 and 3)
     ienh: np.ndarray = field(default_factory=lambda: np.zeros((0, 8), np.int32))
     ienw: np.ndarray = field(default_factory=lambda: np.zeros((0, 6), np.int32))
+    # boundary hexes and wedges, one block per boundary element topology
+    bnd: list = field(default_factory=list)
 
     @property
     def nhex(self) -> int:
@@ -143,32 +173,66 @@ def box(n: int | tuple[int, int, int], lengths=(1.0, 1.0, 1.0), periodic=(False,
     iBC = np.zeros(nshg, dtype=np.int32)
     iBC[iper != idx] |= 1 << 10
     BC = np.zeros((6, nshg), dtype=np.float64)
-    if inflow is not None and not periodic[0]:
-        m = i == 0
-        iBC[m] |= (1 << 1) | (7 << 3)
-        BC[1, m] = inflow["T"]
-        BC[2, m], BC[3, m], BC[4, m] = inflow["u"]
-
-    ienb = np.zeros((0, 4), dtype=np.int32)
-    if boundary_faces and not periodic[0]:
-        xs = x[:, 0]
-        blist = []
-        for plane in (0.0, lengths[0]):
-            on = np.isclose(xs[ien], plane)
-            sel = np.where(on.sum(axis=1) == 3)[0]
-            for e in sel:
-                face = [ien[e, a] for a in range(4) if on[e, a]]
-                inner = [ien[e, a] for a in range(4) if not on[e, a]]
-                blist.append(face + inner)
-        if blist:
-            ienb = _orient(np.array(blist, dtype=np.int64), x)
-            # orientation swaps nodes 0/1 only, so the face stays first
-            ienb = ienb.astype(np.int32)
+    if not periodic[0]:
+        _inflow(x, iBC, BC, inflow)
+    ienb = _tet_x_faces(x, ien, lengths[0]) if boundary_faces and not periodic[0] else np.zeros((0, 4), np.int32)
     nb = ienb.shape[0]
     h = min(lengths[d] / n[d] for d in range(3))
     return Case(nshg=nshg, x=x, ien=ien, ienb=ienb, iBCB=np.zeros((nb, 2), np.int32),
                 BCB=np.zeros((nb, 3, 6), np.float64), iBC=iBC, BC=BC, iper=iper, h=h,
                 meta={"n": n, "lengths": lengths, "periodic": periodic})
+
+
+def _inflow(x, iBC, BC, inflow):
+    """Dirichlet velocity and temperature (iBC bits 1, 3, 4, 5) on the x = 0 nodes."""
+    if inflow is None:
+        return
+    m = np.isclose(x[:, 0], 0.0)
+    iBC[m] |= (1 << 1) | (7 << 3)
+    BC[1, m] = inflow["T"]
+    BC[2, m], BC[3, m], BC[4, m] = inflow["u"]
+
+
+def _tet_x_faces(x, ien, lx):
+    """Boundary tets of the x = 0 and x = lx planes, face nodes first (orientation swaps nodes
+    0/1 only, so the face stays first)."""
+    if ien.shape[0] == 0:
+        return np.zeros((0, 4), np.int32)
+    xs = x[:, 0]
+    blist = []
+    for plane in (0.0, lx):
+        on = np.isclose(xs[ien], plane)
+        sel = np.where(on.sum(axis=1) == 3)[0]
+        for e in sel:
+            face = [ien[e, a] for a in range(4) if on[e, a]]
+            inner = [ien[e, a] for a in range(4) if not on[e, a]]
+            blist.append(face + inner)
+    if not blist:
+        return np.zeros((0, 4), np.int32)
+    return _orient(np.array(blist, dtype=np.int64), x).astype(np.int32)
+
+
+def _hex_x_faces(nid, nx, j, k):
+    """Boundary hexes of the cells (0, j, k) and (nx-1, j, k): each a right-handed hex whose
+    zeta = -1 face lies on x = 0 (xi, eta, zeta along +y, +z, +x) or on x = lx (xi, eta, zeta
+    along +z, +y, -x), so -(v1 x v2) of face nodes 1-3 is the outward normal (e3bvar.f:174-176)."""
+    lo = [nid(0, j + b, k + c) for b, c in ((0, 0), (1, 0), (1, 1), (0, 1))]
+    lo += [nid(1, j + b, k + c) for b, c in ((0, 0), (1, 0), (1, 1), (0, 1))]
+    hi = [nid(nx, j + b, k + c) for c, b in ((0, 0), (1, 0), (1, 1), (0, 1))]
+    hi += [nid(nx - 1, j + b, k + c) for c, b in ((0, 0), (1, 0), (1, 1), (0, 1))]
+    return np.concatenate([np.stack(lo, axis=1), np.stack(hi, axis=1)])
+
+
+def _wedge_x_faces(nid, nx, j, k):
+    """Boundary prisms (triangles in the xy planes, the x = y diagonal) of the cells (0, j, k) and
+    (nx-1, j, k), each with its x-plane quadrilateral as the s = 0 face (nodes 1, 2, 4, 5): the
+    triangle turned cyclically so that its edge 1-2 lies on the plane; dx/dr x dx/dzeta then points
+    out of the domain (e3bvar.f:160-164)."""
+    lo = [(0, 1), (0, 0), (1, 1)]   # the cell's (0,0),(1,1),(0,1) prism turned
+    hi = [(1, 0), (1, 1), (0, 0)]   # the cell's (0,0),(1,0),(1,1) prism turned
+    a = [nid(0 + p, j + q, k) for p, q in lo] + [nid(0 + p, j + q, k + 1) for p, q in lo]
+    b = [nid(nx - 1 + p, j + q, k) for p, q in hi] + [nid(nx - 1 + p, j + q, k + 1) for p, q in hi]
+    return np.concatenate([np.stack(a, axis=1), np.stack(b, axis=1)])
 
 
 def _grid(n, lengths, periodic):
@@ -194,34 +258,46 @@ def _grid(n, lengths, periodic):
     return x, iper, iBC, (lambda a, b, c: a + npts[0] * (b + npts[1] * c))
 
 
-def hex_box(n, lengths=(1.0, 1.0, 1.0)) -> Case:
-    """Fully periodic box of n^3 linear hexes.
+def hex_box(n, lengths=(1.0, 1.0, 1.0), periodic=(True, True, True), inflow=None) -> Case:
+    """Box of n^3 linear hexes, periodic in y and z and, by default, in x.
 
     Local node order of the reference's hex (HexShapeAndDrv in newshape.cc): parent
     (xi, eta, zeta) corners (-,-,-), (+,-,-), (+,+,-), (-,+,-), then the same at zeta = +1;
-    xi, eta, zeta run along x, y, z."""
+    xi, eta, zeta run along x, y, z.  With x not periodic the x = 0 and x = lx faces are
+    boundary hexes (lcsyst 2), natural fluxes, and ``inflow`` = dict(T=..., u=(u,v,w)) makes
+    x = 0 a Dirichlet inflow."""
     if isinstance(n, int):
         n = (n, n, n)
-    x, iper, iBC, nid = _grid(n, lengths, (True, True, True))
+    x, iper, iBC, nid = _grid(n, lengths, periodic)
     ii, jj, kk = (a.reshape(-1) for a in np.meshgrid(*(np.arange(m) for m in n), indexing="ij"))
     corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
     ienh = np.stack([nid(ii + a, jj + b, kk + c) for a, b, c in corners], axis=1).astype(np.int32)
     h = min(lengths[d] / n[d] for d in range(3))
+    BC = np.zeros((6, x.shape[0]))
+    bnd = []
+    if not periodic[0]:
+        _inflow(x, iBC, BC, inflow)
+        j2, k2 = (a.reshape(-1) for a in np.meshgrid(np.arange(n[1]), np.arange(n[2]), indexing="ij"))
+        bnd.append(bnd_block(2, _hex_x_faces(nid, n[0], j2, k2)))
     return Case(nshg=x.shape[0], x=x, ien=np.zeros((0, 4), np.int32), ienb=np.zeros((0, 4), np.int32),
                 iBCB=np.zeros((0, 2), np.int32), BCB=np.zeros((0, 3, 6)), iBC=iBC,
-                BC=np.zeros((6, x.shape[0])), iper=iper, h=h, ienh=ienh,
-                meta={"n": n, "lengths": lengths, "periodic": (True, True, True)})
+                BC=BC, iper=iper, h=h, ienh=ienh, bnd=bnd,
+                meta={"n": n, "lengths": lengths, "periodic": tuple(periodic)})
 
 
-def wedge_box(n, lengths=(1.0, 1.0, 1.0)) -> Case:
-    """Fully periodic box of n^3 cubes, each split along its x = y diagonal into two prisms
-    with triangles in the xy planes.
+def wedge_box(n, lengths=(1.0, 1.0, 1.0), periodic=(True, True, True), inflow=None) -> Case:
+    """Box of n^3 cubes, each split along its x = y diagonal into two prisms with triangles in
+    the xy planes; periodic in y and, by default, in x and z.
 
     Local node order of the reference's wedge (WedgeShapeAndDrv): the triangle at
-    zeta = -1 with parent (r, s) = (0, 0), (1, 0), (0, 1), then the triangle at zeta = +1."""
+    zeta = -1 with parent (r, s) = (0, 0), (1, 0), (0, 1), then the triangle at zeta = +1.
+    With x not periodic the x-plane faces are boundary prisms with a quadrilateral face
+    (lcsyst 4); with z not periodic the z-plane faces are boundary prisms with a triangle face
+    (lcsyst 3; at z = lz the prism is listed from its top triangle down, the triangle reversed,
+    so that the face is its zeta = -1 triangle)."""
     if isinstance(n, int):
         n = (n, n, n)
-    x, iper, iBC, nid = _grid(n, lengths, (True, True, True))
+    x, iper, iBC, nid = _grid(n, lengths, periodic)
     ii, jj, kk = (a.reshape(-1) for a in np.meshgrid(*(np.arange(m) for m in n), indexing="ij"))
     tris = ([(0, 0), (1, 0), (1, 1)], [(0, 0), (1, 1), (0, 1)])  # counter-clockwise seen from +z
     prisms = []
@@ -231,23 +307,43 @@ def wedge_box(n, lengths=(1.0, 1.0, 1.0)) -> Case:
         prisms.append(np.stack(bot + top, axis=1))
     ienw = np.stack(prisms, axis=1).reshape(-1, 6).astype(np.int32)
     h = min(lengths[d] / n[d] for d in range(3))
+    BC = np.zeros((6, x.shape[0]))
+    bnd = []
+    if not periodic[2]:
+        i2, j2 = (a.reshape(-1) for a in np.meshgrid(np.arange(n[0]), np.arange(n[1]), indexing="ij"))
+        faces = []
+        for tri in tris:
+            faces.append(np.stack([nid(i2 + a, j2 + b, 0) for a, b in tri] +
+                                  [nid(i2 + a, j2 + b, 1) for a, b in tri], axis=1))
+            rev = [tri[0], tri[2], tri[1]]
+            faces.append(np.stack([nid(i2 + a, j2 + b, n[2]) for a, b in rev] +
+                                  [nid(i2 + a, j2 + b, n[2] - 1) for a, b in rev], axis=1))
+        bnd.append(bnd_block(3, np.concatenate(faces)))
+    if not periodic[0]:
+        _inflow(x, iBC, BC, inflow)
+        j2, k2 = (a.reshape(-1) for a in np.meshgrid(np.arange(n[1]), np.arange(n[2]), indexing="ij"))
+        bnd.append(bnd_block(4, _wedge_x_faces(nid, n[0], j2, k2)))
     return Case(nshg=x.shape[0], x=x, ien=np.zeros((0, 4), np.int32), ienb=np.zeros((0, 4), np.int32),
                 iBCB=np.zeros((0, 2), np.int32), BCB=np.zeros((0, 3, 6)), iBC=iBC,
-                BC=np.zeros((6, x.shape[0])), iper=iper, h=h, ienw=ienw,
-                meta={"n": n, "lengths": lengths, "periodic": (True, True, True)})
+                BC=BC, iper=iper, h=h, ienw=ienw, bnd=bnd,
+                meta={"n": n, "lengths": lengths, "periodic": tuple(periodic)})
 
 
-def layered(nxy: int, n_hex: int, n_wedge: int, n_tet: int, lengths=(1.0, 1.0, 1.0)) -> Case:
+def layered(nxy: int, n_hex: int, n_wedge: int, n_tet: int, lengths=(1.0, 1.0, 1.0), periodic_x: bool = True,
+            inflow=None) -> Case:
     """One connected, fully periodic box of nxy x nxy x (n_hex + n_wedge + n_tet) cells whose z
     layers are, from z = 0 up, hexes, then prisms (two per cell, triangles in the xy planes,
     the x = y diagonal), then Kuhn tets (six per cell).  Neighbouring layers share their
     interface nodes: the prisms' top triangles are faces of the tets above (the Kuhn split cuts
     the horizontal cell faces along the same diagonal), the hexes' top quads carry the prisms'
     bottom triangles, and the periodic wrap in z joins the tets' top to the hexes' bottom.
-    Node ids follow one (nxy+1)^2 (nz+1) lattice, periodic slaves stored."""
+    Node ids follow one (nxy+1)^2 (nz+1) lattice, periodic slaves stored.  With ``periodic_x``
+    False the x = 0 and x = lx planes are boundaries of all three layers: boundary tets
+    (triangle faces), boundary hexes (lcsyst 2) and boundary prisms with a quadrilateral face
+    (lcsyst 4), natural fluxes, and ``inflow`` makes x = 0 a Dirichlet inflow."""
     nz = n_hex + n_wedge + n_tet
     n = (nxy, nxy, nz)
-    x, iper, iBC, nid = _grid(n, lengths, (True, True, True))
+    x, iper, iBC, nid = _grid(n, lengths, (periodic_x, True, True))
     ii, jj = (a.reshape(-1) for a in np.meshgrid(np.arange(nxy), np.arange(nxy), indexing="ij"))
     corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
     hexes, prisms, tets = [], [], []
@@ -276,10 +372,21 @@ def layered(nxy: int, n_hex: int, n_wedge: int, n_tet: int, lengths=(1.0, 1.0, 1
     cat = lambda lst, w: np.concatenate(lst).astype(np.int32) if lst else np.zeros((0, w), np.int32)  # noqa: E731
     ien = _orient(cat(tets, 4), x).astype(np.int32) if tets else np.zeros((0, 4), np.int32)
     h = min(lengths[0] / nxy, lengths[1] / nxy, lengths[2] / nz)
-    return Case(nshg=x.shape[0], x=x, ien=ien, ienb=np.zeros((0, 4), np.int32), iBCB=np.zeros((0, 2), np.int32),
-                BCB=np.zeros((0, 3, 6)), iBC=iBC, BC=np.zeros((6, x.shape[0])), iper=iper, h=h,
-                ienh=cat(hexes, 8), ienw=cat(prisms, 6),
-                meta={"n": n, "lengths": lengths, "periodic": (True, True, True),
+    BC = np.zeros((6, x.shape[0]))
+    bnd, ienb = [], np.zeros((0, 4), np.int32)
+    if not periodic_x:
+        _inflow(x, iBC, BC, inflow)
+        ienb = _tet_x_faces(x, ien, lengths[0])
+        jj1 = np.arange(nxy)
+        for lcsyst, k0, k1, fn in ((2, 0, n_hex, _hex_x_faces), (4, n_hex, n_hex + n_wedge, _wedge_x_faces)):
+            if k1 > k0:
+                j2, k2 = (a.reshape(-1) for a in np.meshgrid(jj1, np.arange(k0, k1), indexing="ij"))
+                bnd.append(bnd_block(lcsyst, fn(nid, nxy, j2, k2)))
+    nb = ienb.shape[0]
+    return Case(nshg=x.shape[0], x=x, ien=ien, ienb=ienb, iBCB=np.zeros((nb, 2), np.int32),
+                BCB=np.zeros((nb, 3, 6)), iBC=iBC, BC=BC, iper=iper, h=h,
+                ienh=cat(hexes, 8), ienw=cat(prisms, 6), bnd=bnd,
+                meta={"n": n, "lengths": lengths, "periodic": (periodic_x, True, True),
                       "layers": (n_hex, n_wedge, n_tet)})
 
 
@@ -300,10 +407,17 @@ def concat(*cases: Case) -> Case:
         parts["ienw"].append(c.ienw + off)
         off += c.nshg
     cat = {k: np.concatenate(v, axis=(1 if k == "BC" else 0)) for k, v in parts.items()}
+    bnd, boff = {}, 0
+    for c in cases:
+        for b in c.bnd:
+            bnd.setdefault(b.lcsyst, []).append(BndBlock(b.lcsyst, b.ien + boff, b.iBCB, b.BCB))
+        boff += c.nshg
+    bnd = [BndBlock(l, np.concatenate([b.ien for b in v]).astype(np.int32), np.concatenate([b.iBCB for b in v]),
+                    np.concatenate([b.BCB for b in v])) for l, v in sorted(bnd.items())]
     return Case(nshg=off, x=cat["x"], ien=cat["ien"].astype(np.int32), ienb=cat["ienb"].astype(np.int32),
                 iBCB=cat["iBCB"].astype(np.int32), BCB=cat["BCB"], iBC=cat["iBC"].astype(np.int32), BC=cat["BC"],
                 iper=cat["iper"].astype(np.int32), h=min(c.h for c in cases), ienh=cat["ienh"].astype(np.int32),
-                ienw=cat["ienw"].astype(np.int32), meta={"parts": [c.meta for c in cases]})
+                ienw=cat["ienw"].astype(np.int32), meta={"parts": [c.meta for c in cases]}, bnd=bnd)
 
 
 def renumber(case: Case, new_of_old: np.ndarray) -> Case:
@@ -318,7 +432,8 @@ def renumber(case: Case, new_of_old: np.ndarray) -> Case:
                 ienb=p[case.ienb].astype(np.int32), iBCB=case.iBCB.copy(), BCB=case.BCB.copy(),
                 iBC=case.iBC[old_of_new].astype(np.int32), BC=np.ascontiguousarray(case.BC[:, old_of_new]),
                 iper=p[case.iper[old_of_new]].astype(np.int32), h=case.h, meta=dict(case.meta),
-                ienh=p[case.ienh].astype(np.int32), ienw=p[case.ienw].astype(np.int32))
+                ienh=p[case.ienh].astype(np.int32), ienw=p[case.ienw].astype(np.int32),
+                bnd=[BndBlock(b.lcsyst, p[b.ien].astype(np.int32), b.iBCB.copy(), b.BCB.copy()) for b in case.bnd])
 
 
 def renumber_field(v: np.ndarray, new_of_old: np.ndarray, ncomp: int) -> np.ndarray:

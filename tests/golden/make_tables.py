@@ -76,7 +76,31 @@ def main():
             qwt.append(wt[q])
             pts.append([pt[4 * q + k] for k in range(4)])
         topo[name] = {"shp": shp, "shgl": shgl, "Qwt": qwt, "Qpt": pts}
-    topo["source"] = "reference symhex.c, symwdg.c, shphex.c, shp6w.c -> newshape.cc; genint.f, genshp.f"
+    # boundary elements (genint.f:119-142, 302-345; genshpb.f; shapes unscaled): lcsyst 2, the hex
+    # with its zeta = -1 quadrilateral face (symquad.c); lcsyst 3, the wedge with its triangle
+    # face (symtri.c, the last point moved first, zeta = -1, weights in symtri's order);
+    # lcsyst 4, the wedge with a quadrilateral face (symquadw.c)
+    def bnd(rule, shape, nq, nen, reorder_tri=False):
+        n = C.c_int(nq)
+        pt, wt = (D * (4 * nq))(), (D * nq)()
+        rule(C.byref(n), pt, wt, C.byref(err))
+        pts = [[pt[4 * q + k] for k in range(4)] for q in range(nq)]
+        if reorder_tri:
+            pts = [pts[nq - 1]] + pts[: nq - 1]
+            pts = [[p[0], p[1], -1.0, -1.0] for p in pts]
+        shpb, shglb = [], []
+        for q in range(nq):
+            par = (D * 3)(*pts[q][:3])
+            N, dN = (D * nen)(), (D * (3 * nen))()
+            shape(C.byref(C.c_int(1)), par, N, dN)
+            shpb.append([N[a] for a in range(nen)])
+            shglb.append([[dN[3 * a + i] for a in range(nen)] for i in range(3)])
+        return {"shpb": shpb, "shglb": shglb, "Qwtb": [wt[q] for q in range(nq)], "Qptb": pts}
+    topo["hex_quad_b"] = bnd(L.symquad_, L.shphex_, 4, 8)
+    topo["wedge_tri_b"] = bnd(L.symtri_, L.shp6w_, 3, 6, reorder_tri=True)
+    topo["wedge_quad_b"] = bnd(L.symquadw_, L.shp6w_, 4, 6)
+    topo["source"] = ("reference symhex.c, symwdg.c, symquad.c, symtri.c, symquadw.c, shphex.c, shp6w.c -> "
+                      "newshape.cc; genint.f, genshp.f, genshpb.f")
     p2 = Path(__file__).resolve().parent / "topo_tables.json"
     p2.write_text(json.dumps(topo, indent=1))
     print(p2)

@@ -318,6 +318,8 @@ def test_pipelined_linearized_product_is_the_per_chunk_kernel(gpu_lib, n, idiff)
     out = []
     for no_pipe in (0, 1):
         g = GpuSolver(case, dict(p, no_pipe=no_pipe))
+        # the pipelined variants compiled for the per-chunk kernels' occupancy (4 and 3 CTAs/SM)
+        g.set_tuning(4, 3)
         _yo, _ao, y1, a1, st = g.time_step(y, ac, nitr=1)
         out.append((y1, a1, st.iKs))
         g.close()

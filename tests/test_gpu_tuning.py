@@ -1,15 +1,18 @@
 """Autotuned variants of the pipelined element sweeps (phgpu_set_tuning / phgpu_tuning).
 
 The linearized product is compiled for at least 3 or 4 resident CTAs per SM, the double-float
-split residual for 2, 3 or 4: the same code under different register budgets.  A context times
-them on its own mesh before its first mixed-precision matrix-free solve and keeps the fastest;
-every forced choice must give bit for bit the same time steps."""
+split residual for 2, 3 or 4: the same source under different register budgets.  A context
+times them on its own mesh before its first mixed-precision matrix-free solve and keeps the
+fastest when it beats the compiled-in default by more than 3%.  Each variant is deterministic;
+the compiler may fuse multiplies and adds differently under each budget, so variants agree with
+one another to FP32 rounding, which the Newton iterations then carry at the level of the
+nonlinear residual they leave."""
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
-from helpers import channel
+from helpers import channel, rel
 from phasta_gb300 import _lib as L
 from phasta_gb300.solver import GpuSolver
 
@@ -31,7 +34,7 @@ def _run(case, p, y, ac, force=None, nsteps=2):
 
 
 @pytest.mark.parametrize("no_graph", [0, 1], ids=["step-graph", "launched"])
-def test_forced_variants_give_bitwise_the_same_steps(no_graph):
+def test_each_variant_is_deterministic_and_variants_agree(no_graph):
     case, p, y, ac = channel(10, ac_scale=0.05, Kspace=20)
     p = dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR, outer_residual=L.PHGPU_RES_SPLITDF,
              no_graph=no_graph)
@@ -39,15 +42,22 @@ def test_forced_variants_give_bitwise_the_same_steps(no_graph):
     assert tun["how"] == "tuned"
     assert tun["lin_minb"] in (3, 4) and tun["ress_minb"] in (2, 3, 4)
     assert all(t > 0 for t in tun["lin_ms"].values()) and all(t > 0 for t in tun["ress_ms"].values())
-    # the chosen variant is the fastest one timed
-    assert tun["lin_ms"][tun["lin_minb"]] == min(tun["lin_ms"].values())
-    assert tun["ress_ms"][tun["ress_minb"]] == min(tun["ress_ms"].values())
-    for force in [(3, 2), (4, 4), (3, 3), (4, 2)]:
-        got, t2, l2 = _run(case, p, y, ac, force=force)
+    # a variant other than the default (4, 3) only when it was more than 3% faster
+    for key, default in (("lin", 4), ("ress", 3)):
+        chosen = tun[f"{key}_minb"]
+        ms = tun[f"{key}_ms"]
+        assert chosen == default or ms[chosen] < 0.97 * ms[default]
+    for force in [(3, 2), (4, 4), (3, 3), (4, 3)]:
+        a, t2, l2 = _run(case, p, y, ac, force=force)
+        b, _t3, _l3 = _run(case, p, y, ac, force=force)
         assert t2["how"] == "forced" and (t2["lin_minb"], t2["ress_minb"]) == force
         assert l2 == launches  # tuning launches are not counted
-        for (ya, aa, ka, na), (yb, ab, kb, nb) in zip(ref, got):
+        for (ya, aa, ka, na), (yb, ab, kb, nb) in zip(a, b):
             assert np.array_equal(ya, yb) and np.array_equal(aa, ab) and ka == kb and na == nb
+        # against the tuned run: FP32 rounding carried through two time steps of two Newton
+        # iterations (Krylov tolerance 1e-3)
+        for (ya, aa, *_), (yr, ar, *_) in zip(a, ref):
+            assert rel(ya, yr) <= 1e-6 and rel(aa, ar) <= 1e-4
 
 
 def test_set_tuning_checks_its_arguments_and_resets():

@@ -234,3 +234,50 @@ def test_hex_and_wedge_tables_match_reference_c_sources():
         t = pyoracle.topo_tables(lcsyst)
         for k in ("shp", "shgl", "Qwt"):
             assert np.array_equal(t[k], np.array(d[name][k])), (name, k)
+
+
+def test_boundary_hex_and_wedge_tables_match_reference_c_sources():
+    """Oracle restatement of the boundary rules (symquad.c, symtri.c reordered, symquadw.c) and shapes
+    at their points vs tests/golden/topo_tables.json, and the face nodes of getbnodes."""
+    import json
+    d = json.loads((Path(__file__).resolve().parent / "golden" / "topo_tables.json").read_text())
+    for name, lcsyst, lnode in (("hex_quad_b", 2, [0, 1, 2, 3]), ("wedge_tri_b", 3, [0, 1, 2]),
+                                ("wedge_quad_b", 4, [0, 3, 4, 1])):
+        t = pyoracle.btopo_tables(lcsyst)
+        for k in ("shpb", "shglb", "Qwtb"):
+            assert np.array_equal(t[k], np.array(d[name][k])), (name, k)
+        assert t["lnode"].tolist() == lnode
+        # the face nodes carry the whole shape at every boundary point
+        assert np.allclose(t["shpb"][:, lnode].sum(axis=1), 1.0, rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("which", ["hex", "wedge"])
+def test_boundary_faces_integrate_to_the_face_area(which):
+    """A uniform pressure, zero velocity, no viscosity: each boundary face adds p n dA to the momentum
+    residual, so the x-momentum over the inflow and outflow faces sums to -p A and +p A."""
+    from phasta_gb300 import mesh
+    from phasta_gb300.solver import make_params
+    case = (mesh.hex_box(3, periodic=(False, True, True)) if which == "hex"
+            else mesh.wedge_box(3, periodic=(False, True, False)))
+    p = make_params(0.0, 1.0, navier=0)
+    y = np.zeros(5 * case.nshg)
+    y[3 * case.nshg:4 * case.nshg] = 2.5       # p
+    y[4 * case.nshg:] = 300.0                  # T
+    o = pyoracle.Oracle(case, p)
+    import ctypes as C
+    res = np.zeros(5 * case.nshg)
+    o.L.or_elmres(C.byref(o.c), C.byref(o.m), pyoracle._d(y), pyoracle._d(np.zeros_like(y)), pyoracle._d(res), 0)
+    import dataclasses
+    interior = pyoracle.Oracle(dataclasses.replace(case, bnd=[]), p)
+    res0 = np.zeros(5 * case.nshg)
+    o.L.or_elmres(C.byref(interior.c), C.byref(interior.m), pyoracle._d(y), pyoracle._d(np.zeros_like(y)),
+                  pyoracle._d(res0), 0)
+    fx = (res - res0).reshape(5, -1)[1]       # x-momentum (local dof 2 = u-row) of the faces
+    x = case.x[:, 0]
+    assert abs(fx[np.isclose(x, 0.0)].sum() + 2.5) < 1e-12
+    assert abs(fx[np.isclose(x, 1.0)].sum() - 2.5) < 1e-12
+    if which == "wedge":  # the triangle faces (lcsyst 3) on z = 0 and z = 1
+        fz = (res - res0).reshape(5, -1)[3]
+        z = case.x[:, 2]
+        assert abs(fz[np.isclose(z, 0.0)].sum() + 2.5) < 1e-12
+        assert abs(fz[np.isclose(z, 1.0)].sum() - 2.5) < 1e-12
