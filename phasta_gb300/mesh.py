@@ -560,6 +560,25 @@ def channel_case(n: int, mach: float = 0.3, re: float = 1000.0):
     return case, {"mach": mach, "re": re, "mu": mu, "dt": dt, "fs": fs}
 
 
+def channel_hex_case(n, mach: float = 0.3, re: float = 1000.0):
+    """The channel on n^3 hexes: periodic y/z, Dirichlet inflow at x = 0, natural outflow at
+    x = 1 through boundary hexes (lcsyst 2)."""
+    fs = freestream(mach)
+    case = hex_box(n, periodic=(False, True, True), inflow={"T": fs["T"], "u": (fs["u"], 0.0, 0.0)})
+    mu = fs["rho"] * fs["u"] * 1.0 / re
+    return case, {"mach": mach, "re": re, "mu": mu, "dt": cfl_dt(case, mach), "fs": fs}
+
+
+def channel_wedge_case(n, mach: float = 0.3, re: float = 1000.0):
+    """The channel on prisms: periodic y, Dirichlet inflow at x = 0 and natural outflow at x = 1
+    through quadrilateral faces (lcsyst 4), natural walls at z = 0 and z = 1 through triangle
+    faces (lcsyst 3)."""
+    fs = freestream(mach)
+    case = wedge_box(n, periodic=(False, True, False), inflow={"T": fs["T"], "u": (fs["u"], 0.0, 0.0)})
+    mu = fs["rho"] * fs["u"] * 1.0 / re
+    return case, {"mach": mach, "re": re, "mu": mu, "dt": cfl_dt(case, mach), "fs": fs}
+
+
 def periodic_vortex_case(n: int, mach: float = 0.1, re: float = 1600.0):
     L = 2.0 * math.pi
     case = box(n, lengths=(L, L, L), periodic=(True, True, True), inflow=None)
@@ -569,10 +588,14 @@ def periodic_vortex_case(n: int, mach: float = 0.1, re: float = 1600.0):
     return case, {"mach": mach, "re": re, "mu": mu, "dt": dt, "fs": fs}
 
 
-def layered_case(nxy: int, n_hex: int, n_wedge: int, n_tet: int, mach: float = 0.3, re: float = 1000.0):
-    """The connected mixed-topology box of ``layered`` with the channel's physics."""
-    case = layered(nxy, n_hex, n_wedge, n_tet)
+def layered_case(nxy: int, n_hex: int, n_wedge: int, n_tet: int, mach: float = 0.3, re: float = 1000.0,
+                 periodic_x: bool = True):
+    """The connected mixed-topology box of ``layered`` with the channel's physics; with
+    ``periodic_x`` False a Dirichlet inflow at x = 0 and natural outflow at x = 1 through
+    boundary tets, hexes and prisms."""
     fs = freestream(mach)
+    case = layered(nxy, n_hex, n_wedge, n_tet, periodic_x=periodic_x,
+                   inflow=None if periodic_x else {"T": fs["T"], "u": (fs["u"], 0.0, 0.0)})
     mu = fs["rho"] * fs["u"] * 1.0 / re
     dt = cfl_dt(case, mach)
     return case, {"mach": mach, "re": re, "mu": mu, "dt": dt, "fs": fs}

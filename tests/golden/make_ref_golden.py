@@ -23,7 +23,7 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 sys.path[:0] = [str(HERE), str(ROOT), str(ROOT / "tests")]
 
-from helpers import channel, layered, mixed, vortex  # noqa: E402
+from helpers import channel, hexchannel, layered, mixed, vortex, wedgechannel  # noqa: E402
 from refrun import RefPhasta  # noqa: E402
 
 # the reference tree: $PHASTA_REFERENCE, else a directory "reference" beside the repository
@@ -65,6 +65,12 @@ CASES = [
     # interface node sums contributions of two element topologies
     ("layered3", lambda: layered(3, (2, 1, 2)), ALL + ("sparse",)),
     ("layered3_idiff", lambda: layered(3, (1, 1, 1), idiff=1), ("elm", "solve")),
+    # boundary hexes and wedges (AsBMFG/e3b with lcsyst 2, 3 and 4): inflow and outflow through
+    # hex faces; through prism quadrilaterals, with prism triangles on the z walls; and the
+    # connected layered mesh with tet, hex and prism faces on its inflow and outflow planes
+    ("hexchannel3", lambda: hexchannel(3), ALL + ("sparse",)),
+    ("wedgechannel3", lambda: wedgechannel((3, 3, 2)), ("elm", "pieces", "solve")),
+    ("layered3_open", lambda: layered(3, (2, 1, 2), periodic_x=False), ALL + ("sparse",)),
 ]
 
 

@@ -84,14 +84,24 @@ class RefPhasta:
         blocks = [(case.ien, 1, 4, 4), (getattr(case, "ienh", np.zeros((0, 8))), 2, 8, 8),
                   (getattr(case, "ienw", np.zeros((0, 6))), 3, 6, 6)]
         blocks = [b for b in blocks if len(b[0])]
-        ienb = np.asfortranarray(case.ienb.astype(np.int64) + 1)
+        # boundary blocks (genbkb.f): the boundary tets, then each block of boundary hexes and
+        # wedges as (connectivity, lcblkb lcsyst, nshl, nenbl, iBCB, BCB)
+        bblocks = []
+        if Eb:
+            bblocks.append((case.ienb, 1, 4, 3, case.iBCB, case.BCB))
+        for b in getattr(case, "bnd", []):
+            bblocks.append((b.ien, 2 if b.lcsyst == 2 else 3, b.nshl, b.nshlb, b.iBCB, b.BCB))
         P.module("pointer_data", {
             "mien": [_Obj(np.asfortranarray(np.asarray(b[0]).astype(np.int64) + 1)) for b in blocks],
             "mmat": [_Obj(np.ones(len(b[0]), np.int64)) for b in blocks],
             "mxmudmi": [_Obj(np.zeros((len(b[0]), b[3]), order="F")) for b in blocks],
-            "mienb": [_Obj(ienb)], "mmatb": [_Obj(np.ones(max(Eb, 1), np.int64))],
-            "mibcb": [_Obj(np.asfortranarray(case.iBCB.astype(np.int64)))],
-            "mbcb": [_Obj(np.asfortranarray(case.BCB))]})
+            "mienb": [_Obj(np.asfortranarray(np.asarray(b[0]).astype(np.int64) + 1)) for b in bblocks] or
+                     [_Obj(np.zeros((1, 4), np.int64, order="F"))],
+            "mmatb": [_Obj(np.ones(len(b[0]), np.int64)) for b in bblocks] or [_Obj(np.ones(1, np.int64))],
+            "mibcb": [_Obj(np.asfortranarray(np.asarray(b[4]).astype(np.int64))) for b in bblocks] or
+                     [_Obj(np.zeros((1, 2), np.int64, order="F"))],
+            "mbcb": [_Obj(np.asfortranarray(np.asarray(b[5], dtype=np.float64))) for b in bblocks] or
+                    [_Obj(np.zeros((1, 3, 6), order="F"))]})
         for m in MODULES:
             P.module(m, {})
         P.function("elmmfg")  # declares the COMMON blocks of common.h
@@ -103,13 +113,13 @@ class RefPhasta:
         G.numnp = G.nshg = N
         G.nshgt = N
         # numel counts the interior elements of every block (EGmass(numel, nedof, nedof) of SolGMRe)
-        G.numel, G.numelb = E + case.nhex + case.nwedge, Eb
+        G.numel, G.numelb = E + case.nhex + case.nwedge, sum(len(b[0]) for b in bblocks)
         # nen is the largest element of the mesh (readnblk.f) and nedof = nflow*nshape (itrdrv.f:458)
         nenmax = max(nshl for _c, _l, nshl, _q in blocks)
         G.nen, G.ndof, G.nflow, G.nedof = nenmax, 5, 5, 5 * nenmax
         G.nshape = nenmax  # linear basis: nshape = nen (genint.f)
         G.ndofbc, G.ndibcb, G.ndbcb = 6, 2, 6
-        G.nelblk, G.nelblb = len(blocks), (1 if Eb else 0)
+        G.nelblk, G.nelblb = len(blocks), len(bblocks)
         # lcblk(:,iblk): iel, lelCat, lcsyst, iorder, nenl, -, mattyp, ndofl, nsymdl, nshl
         iel = 1
         for ib, (con, lcsyst, nshl, _nq) in enumerate(blocks):
@@ -117,14 +127,21 @@ class RefPhasta:
             iel += len(con)
         G.lcblk[0, len(blocks)] = iel
         # lcblkb(:,iblk): iel, lelCat, lcsyst, iorder, nenl, nenbl, mattyp, ndofl, nshl, nshlb
-        G.lcblkb[:, 0] = [1, 1, 1, 1, 4, 3, 1, 5, 4, 3]
-        G.lcblkb[0, 1] = Eb + 1
+        iel = 1
+        for ib, (con, lcsyst, nshl, nenbl, _ib, _b) in enumerate(bblocks):
+            G.lcblkb[:, ib] = [iel, lcsyst, lcsyst, 1, nshl, nenbl, 1, 5, nshl, nenbl]
+            iel += len(con)
+        G.lcblkb[0, len(bblocks)] = iel
         G.nint[0], G.nintb[0] = 4, 3
         G.nint[1], G.nint[2] = 8, 6
+        G.nintb[1], G.nintb[2], G.nintb[3] = 4, 3, 4   # genint.f: quad 2x2, wedge triangle 3, wedge quad 4
         G.qwt[0, :4] = T["Qwt"]
         G.qwt[1, :8] = TT["hex"]["Qwt"]
         G.qwt[2, :6] = TT["wedge"]["Qwt"]
         G.qwtb[0, :3] = T["Qwtb"]
+        G.qwtb[1, :4] = TT["hex_quad_b"]["Qwtb"]
+        G.qwtb[2, :3] = TT["wedge_tri_b"]["Qwtb"]
+        G.qwtb[3, :4] = TT["wedge_quad_b"]["Qwtb"]
         G.datmat[0, 1, 0] = p["rmu"]
         G.pr, G.rgas, G.gamma, G.gamma1 = p["pr"], p["Rgas"], p["gamma"], p["gamma1"]
         G.dtgl, G.almi, G.alfi, G.gami = p["Dtgl"], p["almi"], p["alfi"], p["gami"]
@@ -157,6 +174,12 @@ class RefPhasta:
             for q in range(nq):
                 self.shp[top, :nen, q] = TT[name]["shp"][q]
                 self.shgl[top, :, :nen, q] = TT[name]["shgl"][q]
+        # genshpb.f: shpb(lcsyst, :, q) for the boundary topologies 2, 3 and 4
+        for top, (name, nq, nen) in ((1, ("hex_quad_b", 4, 8)), (2, ("wedge_tri_b", 3, 6)),
+                                     (3, ("wedge_quad_b", 4, 6))):
+            for q in range(nq):
+                self.shpb[top, :nen, q] = TT[name]["shpb"][q]
+                self.shglb[top, :, :nen, q] = TT[name]["shglb"][q]
         self.iBC = case.iBC.astype(np.int64)
         self.BC = np.asfortranarray(case.BC.T)
         self.iper = case.iper.astype(np.int64) + 1

@@ -47,9 +47,10 @@ def mixed(n_tet=3, n_hex=3, n_wedge=(3, 3, 2), mach=0.3, sigma=0.01, seed=202612
     return case, p, y, ac
 
 
-def layered(nxy=3, layers=(2, 1, 2), mach=0.3, sigma=0.02, seed=20261203, ac_scale=0.05, **kw):
-    """One connected periodic box whose hex, prism and tet layers share their interface nodes."""
-    case, ph = mesh.layered_case(nxy, *layers, mach=mach)
+def layered(nxy=3, layers=(2, 1, 2), mach=0.3, sigma=0.02, seed=20261203, ac_scale=0.05, periodic_x=True, **kw):
+    """One connected box whose hex, prism and tet layers share their interface nodes (periodic, or
+    with inflow and outflow faces in x)."""
+    case, ph = mesh.layered_case(nxy, *layers, mach=mach, periodic_x=periodic_x)
     p = make_params(ph["mu"], ph["dt"], **kw)
     y = mesh.uniform_state(case, mach, sigma=sigma, seed=seed)
     ac = np.zeros_like(y)
@@ -58,3 +59,26 @@ def layered(nxy=3, layers=(2, 1, 2), mach=0.3, sigma=0.02, seed=20261203, ac_sca
         ac = ac_scale * g.standard_normal(y.shape) * np.repeat(np.abs(y.reshape(5, -1)).mean(axis=1), case.nshg)
         ac = np.ascontiguousarray(ac.reshape(5, -1)[:, case.iper]).reshape(-1)
     return case, p, y, ac
+
+
+def _perturbed(case, ph, mach, sigma, seed, ac_scale, **kw):
+    p = make_params(ph["mu"], ph["dt"], **kw)
+    y = mesh.uniform_state(case, mach, sigma=sigma, seed=seed)
+    ac = np.zeros_like(y)
+    if ac_scale:
+        g = np.random.default_rng(seed + 1)
+        ac = ac_scale * g.standard_normal(y.shape) * np.repeat(np.abs(y.reshape(5, -1)).mean(axis=1), case.nshg)
+        ac = np.ascontiguousarray(ac.reshape(5, -1)[:, case.iper]).reshape(-1)
+    return case, p, y, ac
+
+
+def hexchannel(n=3, mach=0.3, sigma=0.01, seed=20261203, ac_scale=0.05, **kw):
+    """The channel on hexes: inflow and outflow through boundary hexes."""
+    case, ph = mesh.channel_hex_case(n, mach=mach)
+    return _perturbed(case, ph, mach, sigma, seed, ac_scale, **kw)
+
+
+def wedgechannel(n=(3, 3, 2), mach=0.3, sigma=0.01, seed=20261203, ac_scale=0.05, **kw):
+    """The channel on prisms: quadrilateral inflow/outflow faces, triangle wall faces."""
+    case, ph = mesh.channel_wedge_case(n, mach=mach)
+    return _perturbed(case, ph, mach, sigma, seed, ac_scale, **kw)
