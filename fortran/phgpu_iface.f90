@@ -26,6 +26,12 @@ module phgpu_iface
      integer(c_int) :: no_graph, iDC, no_pipe, precond
   end type
 
+  ! a block of boundary hexes (lcsyst 2) or wedges (3: triangle face, 4: quadrilateral face)
+  type, bind(C) :: phgpu_bnd_block
+     integer(c_int) :: lcsyst, nelem
+     type(c_ptr)    :: ien, iBCB, BCB
+  end type
+
   type, bind(C) :: phgpu_mesh
      integer(c_int) :: nshg, nelem
      type(c_ptr)    :: ien, x
@@ -35,6 +41,8 @@ module phgpu_iface
      type(c_ptr)    :: ienh
      integer(c_int) :: nwedge        ! blocks with lcsyst 3 (nshl = 6)
      type(c_ptr)    :: ienw
+     integer(c_int) :: nbblk         ! boundary hex and wedge blocks
+     type(c_ptr)    :: bblk          ! nbblk phgpu_bnd_block
   end type
 
   type, bind(C) :: phgpu_stats

@@ -39,6 +39,10 @@ c
         integer(c_int), allocatable, target, save :: ienw(:), ienb(:)
         integer(c_int), allocatable, target, save :: ibcbc(:)
         real(c_double), allocatable, target, save :: bcbc(:)
+c.... boundary hex and wedge blocks: the phgpu_bnd_block list and its arrays
+        type(phgpu_bnd_block), allocatable, target, save :: bblks(:)
+        integer(c_int), allocatable, target, save :: ienbt(:), ibcbt(:)
+        real(c_double), allocatable, target, save :: bcbt(:)
         end module
 c
 c.... options of the GPU path (call before the first solve)
@@ -69,6 +73,7 @@ c
         integer(c_int) :: rc
         integer(c_int), allocatable, target :: iperc(:)
         integer nt, nh, nw, nb, ib, i, j, k, ie
+        integer nbl, nbt, nbi, nbc, nsl, nsb
 c
         if (numpe .gt. 1) call error ('phgpushm', 'numpe   ', numpe)
         if (matflg(2,1) .ne. 0) call error ('phgpushm', 'matflg2 ',
@@ -162,15 +167,17 @@ c.... boundary tets (face first), their iBCB and BCB
 c
           nb = 0
           do ib = 1, nelblb
-            if (lcblkb(3,ib) .ne. 1) call error ('phgpushm', 'bndtopo ',
-     &                                           lcblkb(3,ib))
-            nb = nb + lcblkb(1,ib+1) - lcblkb(1,ib)
+            if (lcblkb(3,ib) .lt. 1 .or. lcblkb(3,ib) .gt. 3)
+     &        call error ('phgpushm', 'bndtopo ', lcblkb(3,ib))
+            if (lcblkb(3,ib) .eq. 1)
+     &        nb = nb + lcblkb(1,ib+1) - lcblkb(1,ib)
           enddo
           allocate (ienb(max(1,4*nb)), ibcbc(max(1,2*nb)))
           allocate (bcbc(max(1,18*nb)))
           bcbc = 0d0
           nb = 0
           do ib = 1, nelblb
+            if (lcblkb(3,ib) .ne. 1) cycle
             do ie = 1, lcblkb(1,ib+1) - lcblkb(1,ib)
               do j = 1, 4
                 ienb(4*nb+j) = abs(mienb(ib)%p(ie,j)) - 1
@@ -205,6 +212,64 @@ c.... periodic masters 0-based (phgpu_create copies what it keeps)
           m%ienh = c_loc(ienh)
           m%nwedge = nw
           m%ienw = c_loc(ienw)
+c
+c.... boundary hex and wedge blocks, one phgpu_bnd_block each: lcsyst 2
+c     for hexes, and for wedges the face's node count nenbl as
+c     elmmfg.f:187 turns it into the lcsyst of the boundary rule (3
+c     triangle, 4 quadrilateral); nshl = lcblkb(9,:), nshlb = lcblkb(10,:)
+c
+          nbl = 0
+          nbt = 0
+          nbi = 0
+          nbc = 0
+          do ib = 1, nelblb
+            if (lcblkb(3,ib) .eq. 1) cycle
+            i = lcblkb(1,ib+1) - lcblkb(1,ib)
+            nbl = nbl + 1
+            nbt = nbt + i*lcblkb(9,ib)
+            nbi = nbi + 2*i
+            nbc = nbc + 6*i*lcblkb(10,ib)
+          enddo
+          allocate (bblks(max(1,nbl)), ienbt(max(1,nbt)))
+          allocate (ibcbt(max(1,nbi)), bcbt(max(1,nbc)))
+          bcbt = 0d0
+          nbl = 0
+          nbt = 0
+          nbi = 0
+          nbc = 0
+          do ib = 1, nelblb
+            if (lcblkb(3,ib) .eq. 1) cycle
+            i = lcblkb(1,ib+1) - lcblkb(1,ib)
+            nsl = lcblkb(9,ib)
+            nsb = lcblkb(10,ib)
+            nbl = nbl + 1
+            if (lcblkb(3,ib) .eq. 2) then
+              bblks(nbl)%lcsyst = 2
+            else
+              bblks(nbl)%lcsyst = lcblkb(6,ib)
+            endif
+            bblks(nbl)%nelem = i
+            bblks(nbl)%ien = c_loc(ienbt(nbt+1))
+            bblks(nbl)%iBCB = c_loc(ibcbt(nbi+1))
+            bblks(nbl)%BCB = c_loc(bcbt(nbc+1))
+            do ie = 1, i
+              do j = 1, nsl
+                ienbt(nbt+j) = abs(mienb(ib)%p(ie,j)) - 1
+              enddo
+              ibcbt(nbi+1) = miBCB(ib)%p(ie,1)
+              ibcbt(nbi+2) = miBCB(ib)%p(ie,2)
+              do j = 1, nsb
+                do k = 1, min(6, ndBCB)
+                  bcbt(nbc + 6*(j-1) + k) = mBCB(ib)%p(ie,j,k)
+                enddo
+              enddo
+              nbt = nbt + nsl
+              nbi = nbi + 2
+              nbc = nbc + 6*nsb
+            enddo
+          enddo
+          m%nbblk = nbl
+          m%bblk = c_loc(bblks)
           rc = phgpu_create (m, cfg, hctx)
           deallocate (iperc)
           if (rc .ne. PHGPU_OK) call error ('phgpushm', 'create  ', rc)

@@ -112,6 +112,23 @@ enum { PHGPU_PRECOND_BDIAG = 0, PHGPU_PRECOND_LEARNED = 1 };
 
 /* Mesh and boundary-condition arrays (what the reference keeps in
  * pointer_data mien/mienb/miBCB/mBCB and in iBC/BC/iper). */
+/* A block of boundary hexes or wedges (the reference's boundary element blocks of lcsyst 2, 3
+ * and 4, genbkb.f; handled by AsBMFG/e3b, elmmfg.f:171-211): each element whole, in the
+ * reference's local node order, with its boundary face where getbnodes (hierarchic.f:90-165)
+ * looks for it:
+ *   lcsyst 2  hex, the zeta = -1 quadrilateral: nodes 0-3 (nshl 8, nshlb 4)
+ *   lcsyst 3  wedge, the zeta = -1 triangle: nodes 0-2 (nshl 6, nshlb 3)
+ *   lcsyst 4  wedge, the s = 0 quadrilateral: nodes 0, 3, 4, 1 (nshl 6, nshlb 4)
+ * BC values come per face node in that order.  The face's normal is the reference's: for
+ * lcsyst 2 and 3, -(x1 - x0) x (x2 - x0); for lcsyst 4, dx/dr x dx/dzeta at each point. */
+typedef struct {
+    int lcsyst;
+    int nelem;
+    const int* ien;       /* nelem*nshl, element-major */
+    const int* iBCB;      /* nelem*2: (flux bits, surface id) */
+    const double* BCB;    /* nelem*nshlb*6: BCB[(e*nshlb + n)*6 + k] */
+} phgpu_bnd_block;
+
 typedef struct {
     int nshg;             /* nodes (periodic slaves are stored, as in the reference) */
     int nelem;            /* interior linear tets (lcsyst 1) */
@@ -129,6 +146,9 @@ typedef struct {
     const int* ienh;      /* nhex*8 */
     int nwedge;           /* wedges */
     const int* ienw;      /* nwedge*6 */
+    /* boundary hexes and wedges (the boundary tets are nbelem/ienb above) */
+    int nbblk;
+    const phgpu_bnd_block* bblk;
 } phgpu_mesh;
 
 typedef struct {

@@ -47,12 +47,17 @@ class Config(C.Structure):
     ]
 
 
+class BndBlock(C.Structure):
+    _fields_ = [("lcsyst", C.c_int), ("nelem", C.c_int), ("ien", _ip), ("iBCB", _ip), ("BCB", _dp)]
+
+
 class Mesh(C.Structure):
     _fields_ = [
         ("nshg", C.c_int), ("nelem", C.c_int), ("ien", _ip), ("x", _dp),
         ("nbelem", C.c_int), ("ienb", _ip), ("iBCB", _ip), ("BCB", _dp),
         ("iBC", _ip), ("BC", _dp), ("iper", _ip),
         ("nhex", C.c_int), ("ienh", _ip), ("nwedge", C.c_int), ("ienw", _ip),
+        ("nbblk", C.c_int), ("bblk", C.POINTER(BndBlock)),
     ]
 
 

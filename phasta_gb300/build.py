@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 LIB = PKG / "libphgpu.so"
 BUILD = PKG / "_build"
 SOURCES = ["elements.cu", "nodal.cu", "solver.cu", "chunks.cu", "noalloc.cu", "sparse.cu", "tangent.cu", "topo_ress.cu",
-           "learn.cu", "phio.cpp", "reorder.cpp"]
+           "learn.cu", "boundary.cu", "phio.cpp", "reorder.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

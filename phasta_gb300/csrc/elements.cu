@@ -2666,6 +2666,7 @@ void launch_boundary(Ctx& C, const double* y, double* res) {
                                                    C.d_x, y, res, P);
         ++C.launches;
     }
+    launch_bnd_blocks(C, y, res);
 }
 
 }  // namespace phgpu

@@ -111,6 +111,15 @@ struct CycleGraph {
 // assembly, the LU, the cycle (one conditional node per Krylov iteration, opened from the
 // device) and the update are launched from the graph; the norms and the cycle's decisions stay
 // on the device, and the statistics of every Newton iteration come back in one read.
+// a block of boundary hexes or wedges on the device, its elements in colour order
+struct BndBlockDev {
+    int lcsyst = 0, nelem = 0, nshl = 0, nshlb = 0;
+    int* d_ien = nullptr;      // nelem*nshl
+    int* d_ibcb = nullptr;     // nelem*2
+    double* d_bcb = nullptr;   // nelem*nshlb*6
+    std::vector<int> col_start;
+};
+
 struct StepGraph {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -197,6 +206,7 @@ struct Ctx {
     // element colouring
     std::vector<int> col_start;   // ncol+1 (interior)
     std::vector<int> bcol_start;  // boundary
+    std::vector<BndBlockDev> bblk;  // boundary hexes and wedges (boundary.cu)
     int4* d_ien = nullptr;        // E (chunk order)
     // hex and wedge blocks (colour order)
     int nhex = 0, nwedge = 0;
@@ -311,7 +321,11 @@ template <typename R>
 void launch_qrec(Ctx& C, const R* x, const R* y, R* out);
 template <typename R>
 void qpbc(Ctx& C, R* q13);
-void launch_boundary(Ctx& C, const double* y, double* res);
+void launch_boundary(Ctx& C, const double* y, double* res);  // tets, then the hex and wedge blocks
+int bnd_setup(Ctx& C, const phgpu_mesh* m);                    // boundary.cu
+void bnd_free(Ctx& C);
+void launch_bnd_blocks(Ctx& C, const double* y, double* res);
+inline bool has_boundary(const Ctx& C) { return C.Eb > 0 || !C.bblk.empty(); }
 void launch_elem_resh(Ctx& C, const double* y, const double* ac, const float* yf, const float* acf, double* out);
 // outer residual with no FP64 arithmetic: double-float element-constant flux + FP32 increments
 void launch_elem_ress(Ctx& C, const float* yh, const float* ylo, const float* acf, double* out,

@@ -309,7 +309,7 @@ int elmres64(Ctx& C, const double* y, const double* ac, double* res) {
     const double* ql = reconstruct_q(C, y);
     fill0(C, res, sizeof(double) * 5 * (size_t)C.N);
     launch_elem_res<double>(C, RM_RES, C.d_x, y, nullptr, ac, res, 0, nullptr, ql);
-    if (C.Eb > 0) launch_boundary(C, y, res);
+    if (has_boundary(C)) launch_boundary(C, y, res);
     bc3res<double>(C, res);
     return check(C, cudaGetLastError(), "elmres");
 }
@@ -326,7 +326,7 @@ int elmmfg64(Ctx& C, const double* y, const double* ac, double* res, double* rme
         launch_elem_res<double>(C, RM_RES, C.d_x, y, nullptr, ac, res, 0, nullptr, ql);
         launch_elem_res<double>(C, RM_MODRES, C.d_x, y, y, ac, rmes, 0, nullptr);
     }
-    if (C.Eb > 0) launch_boundary(C, y, res);
+    if (has_boundary(C)) launch_boundary(C, y, res);
     bc3res<double>(C, res);
     bc3res<double>(C, rmes);
     if (iprec) bc3bdg<double>(C, y, bd);
@@ -855,7 +855,7 @@ int assemble_and_factor(Ctx& C, int lhs, bool asm_bd, bool sparse, bool ebe) {
                 launch_topo<double>(C, RM_RES, C.d_x, C.d_y, nullptr, C.d_ac, C.d_res, nullptr, nullptr, 0, nullptr,
                                     ql);
             }
-            if (C.Eb > 0) launch_boundary(C, C.d_y, C.d_res);
+            if (has_boundary(C)) launch_boundary(C, C.d_y, C.d_res);
             bc3res<double>(C, C.d_res);
         } else {
             PH_TRY(elmres64(C, C.d_y, C.d_ac, C.d_res));
@@ -1304,6 +1304,8 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     if (C.nhex > 0) T(colour(C, N, m->ienh, 8, C.nhex, horder, C.hcol_start));
     if (C.nwedge > 0) T(colour(C, N, m->ienw, 6, C.nwedge, worder, C.wcol_start));
     if (rc != PHGPU_OK) { phgpu_destroy(h); return rc; }
+    T(bnd_setup(C, m));
+    if (rc != PHGPU_OK) { phgpu_destroy(h); return rc; }
     if (C.E > 0) T(build_chunks(C, m->ien, m->x));
     C.h_ien.assign(m->ien, m->ien + 4 * (size_t)C.E);
     if (rc == PHGPU_OK) T(configure_element_kernels(C));
@@ -1450,6 +1452,7 @@ int phgpu_destroy(phgpu_ctx* h) {
     if (C.stream) cudaStreamSynchronize(C.stream);
     phgpu::cycle_graph_free(C);
     phgpu::net_free(C);
+    phgpu::bnd_free(C);
     if (C.stepg.exec) cudaGraphExecDestroy(C.stepg.exec);
     if (C.stepg.graph) cudaGraphDestroy(C.stepg.graph);
     if (C.stepg.d_stats) cudaFree(C.stepg.d_stats);

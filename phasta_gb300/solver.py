@@ -112,11 +112,18 @@ class _MeshArrays:
         self.ienh = np.ascontiguousarray(case.ienh, dtype=np.int32).reshape(-1)
         self.ienw = np.ascontiguousarray(case.ienw, dtype=np.int32).reshape(-1)
         nb = case.nbelem
+        bnd = getattr(case, "bnd", [])
+        self.bnd = [(np.ascontiguousarray(b.ien, dtype=np.int32).reshape(-1),
+                     np.ascontiguousarray(b.iBCB, dtype=np.int32).reshape(-1),
+                     np.ascontiguousarray(b.BCB, dtype=np.float64).reshape(-1)) for b in bnd]
+        self.bblk = (L.BndBlock * max(1, len(bnd)))(
+            *[L.BndBlock(b.lcsyst, b.ien.shape[0], L.iptr(a[0]), L.iptr(a[1]), L.dptr(a[2]))
+              for b, a in zip(bnd, self.bnd)])
         self.m = L.Mesh(case.nshg, case.nelem, L.iptr(self.ien) if case.nelem else None, L.dptr(self.x), nb,
                         L.iptr(self.ienb) if nb else None, L.iptr(self.iBCB) if nb else None,
                         L.dptr(self.BCB) if nb else None, L.iptr(self.iBC), L.dptr(self.BC), L.iptr(self.iper),
                         case.nhex, L.iptr(self.ienh) if case.nhex else None, case.nwedge,
-                        L.iptr(self.ienw) if case.nwedge else None)
+                        L.iptr(self.ienw) if case.nwedge else None, len(bnd), self.bblk if bnd else None)
 
 
 def genadj(case: Case, nnz: int = 40):

@@ -26,6 +26,11 @@ int main(void) {
     F(phgpu_mesh, nshg); F(phgpu_mesh, nelem); F(phgpu_mesh, ien); F(phgpu_mesh, x); F(phgpu_mesh, nbelem);
     F(phgpu_mesh, ienb); F(phgpu_mesh, iBCB); F(phgpu_mesh, BCB); F(phgpu_mesh, iBC); F(phgpu_mesh, BC);
     F(phgpu_mesh, iper); F(phgpu_mesh, nhex); F(phgpu_mesh, ienh); F(phgpu_mesh, nwedge); F(phgpu_mesh, ienw);
+    F(phgpu_mesh, nbblk); F(phgpu_mesh, bblk);
+    printf("}, \"phgpu_bnd_block\": {\"__size\": %zu, ", sizeof(phgpu_bnd_block));
+    first = 0;
+    F(phgpu_bnd_block, lcsyst); F(phgpu_bnd_block, nelem); F(phgpu_bnd_block, ien); F(phgpu_bnd_block, iBCB);
+    F(phgpu_bnd_block, BCB);
     printf("}, \"phgpu_stats\": {\"__size\": %zu, ", sizeof(phgpu_stats));
     first = 0;
     F(phgpu_stats, iKs); F(phgpu_stats, lGMRES); F(phgpu_stats, ntotGM); F(phgpu_stats, status);

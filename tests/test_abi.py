@@ -37,7 +37,8 @@ def test_struct_layouts_match_the_header_as_gcc_lays_them_out(tmp_path):
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-o", str(exe), str(src)], check=True)
     got = json.loads(subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout)
-    for cname, ct in (("phgpu_config", L.Config), ("phgpu_mesh", L.Mesh), ("phgpu_stats", L.Stats),
+    for cname, ct in (("phgpu_config", L.Config), ("phgpu_mesh", L.Mesh), ("phgpu_bnd_block", L.BndBlock),
+                      ("phgpu_stats", L.Stats),
                       ("phgpu_net_train_config", L.NetTrainConfig), ("phgpu_net_train_stats", L.NetTrainStats)):
         c = got[cname]
         assert c["__size"] == C.sizeof(ct), cname

@@ -67,13 +67,13 @@ def test_finite_difference_solver_keeps_the_launched_cycle():
     assert runs == 0
 
 
-@pytest.mark.parametrize("which", ["channel", "layered", "channel_idiff"])
+@pytest.mark.parametrize("which", ["channel", "layered", "layered_open", "channel_idiff"])
 def test_step_graph_is_bitwise_the_launched_time_step(which):
     """Whole time steps (predictor, 3 Newton iterations, update) as one graph: the state, the
     iteration counts and the statistics equal the kernel-by-kernel time steps."""
     from helpers import layered
-    if which == "layered":
-        case, p, y, ac = layered(6, (2, 1, 3), Kspace=20)
+    if which.startswith("layered"):
+        case, p, y, ac = layered(6, (2, 1, 3), Kspace=20, periodic_x=which == "layered")
     else:
         case, p, y, ac = channel(10, ac_scale=0.05, Kspace=20, idiff=1 if which == "channel_idiff" else 0)
     p = dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR, outer_residual=L.PHGPU_RES_SPLITDF)

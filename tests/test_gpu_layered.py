@@ -1,7 +1,8 @@
 """GPU parity on one connected mesh whose element topologies share nodes.
 
 The layered box (phasta_gb300.mesh.layered) stacks hexes, prisms and Kuhn tets in z on one
-node lattice, fully periodic: every node of a layer interface sums the contributions of two
+node lattice, fully periodic or open in x (inflow and outflow faces of all three topologies):
+every node of a layer interface sums the contributions of two
 element topologies (hex/prism, prism/tet and, through the periodic wrap, tet/hex), in the order
 the GPU's colour launches give them.  Tolerances as in test_gpu_parity.py: FP64 residuals and
 block diagonal 1e-10 against the oracle (and on the interface nodes alone), FP32 block diagonal
@@ -21,9 +22,13 @@ from phasta_gb300.solver import GpuSolver, make_params
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def lay(gpu_lib):
-    case, p, y, ac = layered(8, (3, 2, 3), Kspace=20)
+@pytest.fixture(scope="module", params=[True, False], ids=["periodic", "open"])
+def lay(request, gpu_lib):
+    """The layered box, fully periodic or with a Dirichlet inflow at x = 0 and outflow at x = 1
+    through boundary tets, hexes (lcsyst 2) and prisms (lcsyst 4)."""
+    case, p, y, ac = layered(8, (3, 2, 3), Kspace=20, periodic_x=request.param)
+    if not request.param:
+        assert case.nbelem > 0 and sorted(b.lcsyst for b in case.bnd) == [2, 4]
     return case, p, y, ac, GpuSolver(case, p), pyoracle.Oracle(case, p, nthreads=4)
 
 
