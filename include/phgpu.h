@@ -217,12 +217,14 @@ long long phgpu_step_graphs(phgpu_ctx* ctx);
  * and the double-float split outer residual (2, 3 or 4).  Before its first mixed-precision
  * linearized solve or graph-captured time step, a context times each variant on its own mesh
  * and state (a warm-up and three timed sweeps each, CUDA events) and keeps the fastest when it
- * beats the compiled-in default by more than 3%, for the context's lifetime.  The variants are
+ * beats the compiled-in default by more than 5%, for the context's lifetime; on a mesh whose
+ * default linearized product takes less than 0.5 ms the defaults stay untimed beyond it.  The variants are
  * the same arithmetic compiled under different register budgets: each is deterministic, and
  * they agree with one another to FP32 rounding (the compiler may fuse multiplies and adds
  * differently), not bit for bit.
  * phgpu_set_tuning forces a choice (lin_minb 3 or 4, ress_minb 2, 3 or 4), or with (0, 0)
- * returns to the compiled-in defaults and tunes again at the next solve.
+ * returns to the compiled-in defaults and tunes again at the next solve, or with (-1, -1) does
+ * so timing every variant whatever the mesh size.
  * phgpu_tuning gives the current choice and, in ms[5], the mean time of each variant in ms
  * (linearized product 3, 4; split residual 2, 3, 4; -1 when not timed); it returns 0 while
  * untuned, 1 when tuned, 2 when forced. */

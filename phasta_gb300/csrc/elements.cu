@@ -2530,9 +2530,12 @@ void select_sweep_variants(Ctx& C, int lin_minb, int ress_minb) {
 // default only when it is more than kTuneGain faster: the variants are the same source under
 // different register budgets, and the compiler may contract multiplies and adds differently
 // under each, so their results agree to FP32 rounding but not bit for bit; the margin keeps
-// the choice (and so the results) from flipping with timing noise.  The choice holds for the
+// the choice (and so the results) from flipping with timing noise.  On a mesh whose default
+// linearized product takes less than kTuneMinMs the timings are mostly noise and the defaults
+// stay (unless tuning is forced with phgpu_set_tuning(-1, -1)).  The choice holds for the
 // context's lifetime.  The split residual is tuned only when it is the outer residual in use.
-constexpr double kTuneGain = 0.03;
+constexpr double kTuneGain = 0.05;
+constexpr double kTuneMinMs = 0.5;
 int autotune_sweeps(Ctx& C) {
     if (C.tuned || C.tune_forced || C.cfg.no_pipe || C.E == 0) return PHGPU_OK;
     const size_t n5 = 5 * (size_t)C.N;
@@ -2559,12 +2562,21 @@ int autotune_sweeps(Ctx& C) {
             if (ms[m - lo] < ms[best - lo]) best = m;
         return ms[best - lo] < (1.0 - kTuneGain) * ms[def - lo] ? best : def;
     };
-    for (int m = 3; m <= 4; ++m) {
+    auto time_lin = [&](int m) {
         select_sweep_variants(C, m, def_r);
         C.tune_ms[m - 3] = time_it([&] {
             launch_elem_res<float>(C, RM_LIN, C.d_xf, C.d_yf, C.d_yf, nullptr, C.d_t32, 0, nullptr);
         });
+    };
+    time_lin(def_l);
+    if (!C.tune_always && C.tune_ms[def_l - 3] < kTuneMinMs) {
+        C.launches = l0;
+        select_sweep_variants(C, def_l, def_r);
+        C.tuned = true;
+        return check(C, cudaGetLastError(), "autotune");
     }
+    for (int m = 3; m <= 4; ++m)
+        if (m != def_l) time_lin(m);
     const int best_l = pick(C.tune_ms, 3, 4, def_l);
     int best_r = def_r;
     if (C.cfg.outer_residual == PHGPU_RES_SPLITDF) {

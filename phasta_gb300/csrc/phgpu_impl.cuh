@@ -283,7 +283,7 @@ struct Ctx {
     int lin_minb = 4, ress_minb = 3;
     int lin_grids[2] = {1, 1}, ress_grids[3] = {1, 1, 1};
     double tune_ms[5] = {-1, -1, -1, -1, -1};
-    bool tuned = false, tune_forced = false;
+    bool tuned = false, tune_forced = false, tune_always = false;
     double* h_scal = nullptr;     // pinned mirror
     int* h_flag = nullptr;
 

@@ -1506,9 +1506,10 @@ int phgpu_set_tuning(phgpu_ctx* h, int lin_minb, int ress_minb) {
     if (!h) return PHGPU_ERR_INVALID;
     Ctx& C = h->c;
     C.err.clear();
-    if (lin_minb == 0 && ress_minb == 0) {
+    if ((lin_minb == 0 && ress_minb == 0) || (lin_minb == -1 && ress_minb == -1)) {
         C.tune_forced = false;
         C.tuned = false;
+        C.tune_always = lin_minb == -1;
         for (double& t : C.tune_ms) t = -1.0;
         phgpu::select_sweep_variants(C, 0, 0);
         return PHGPU_OK;

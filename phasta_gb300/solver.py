@@ -221,7 +221,8 @@ class GpuSolver:
 
     def set_tuning(self, lin_minb: int = 0, ress_minb: int = 0) -> None:
         """Force the pipelined sweeps' variants (minimum CTAs per SM: linearized product 3 or 4,
-        split residual 2, 3 or 4), or with (0, 0) return to autotuning at the next solve."""
+        split residual 2, 3 or 4), or with (0, 0) return to autotuning at the next solve, or with
+        (-1, -1) autotune timing every variant whatever the mesh size."""
         self._check(self.lib.phgpu_set_tuning(self.h, int(lin_minb), int(ress_minb)))
 
     def tuning(self) -> dict:

@@ -3,10 +3,11 @@
 The linearized product is compiled for at least 3 or 4 resident CTAs per SM, the double-float
 split residual for 2, 3 or 4: the same source under different register budgets.  A context
 times them on its own mesh before its first mixed-precision matrix-free solve and keeps the
-fastest when it beats the compiled-in default by more than 3%.  Each variant is deterministic;
-the compiler may fuse multiplies and adds differently under each budget, so variants agree with
-one another to FP32 rounding, which the Newton iterations then carry at the level of the
-nonlinear residual they leave."""
+fastest when it beats the compiled-in default by more than 5% (on meshes whose default
+linearized product takes at least 0.5 ms; these tests force tuning on small meshes).  Each
+variant is deterministic; the compiler may fuse multiplies and adds differently under each
+budget, so variants agree with one another to FP32 rounding, which the Newton iterations then
+carry at the level of the nonlinear residual they leave."""
 from __future__ import annotations
 
 import numpy as np
@@ -38,15 +39,15 @@ def test_each_variant_is_deterministic_and_variants_agree(no_graph):
     case, p, y, ac = channel(10, ac_scale=0.05, Kspace=20)
     p = dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR, outer_residual=L.PHGPU_RES_SPLITDF,
              no_graph=no_graph)
-    ref, tun, launches = _run(case, p, y, ac)
+    ref, tun, launches = _run(case, p, y, ac, force=(-1, -1))
     assert tun["how"] == "tuned"
     assert tun["lin_minb"] in (3, 4) and tun["ress_minb"] in (2, 3, 4)
     assert all(t > 0 for t in tun["lin_ms"].values()) and all(t > 0 for t in tun["ress_ms"].values())
-    # a variant other than the default (4, 3) only when it was more than 3% faster
+    # a variant other than the default (4, 3) only when it was more than 5% faster
     for key, default in (("lin", 4), ("ress", 3)):
         chosen = tun[f"{key}_minb"]
         ms = tun[f"{key}_ms"]
-        assert chosen == default or ms[chosen] < 0.97 * ms[default]
+        assert chosen == default or ms[chosen] < 0.95 * ms[default]
     for force in [(3, 2), (4, 4), (3, 3), (4, 3)]:
         a, t2, l2 = _run(case, p, y, ac, force=force)
         b, _t3, _l3 = _run(case, p, y, ac, force=force)
@@ -75,7 +76,13 @@ def test_set_tuning_checks_its_arguments_and_resets():
         assert g.tuning()["how"] == "default"
         g.time_step(y, ac, nitr=1)
         t = g.tuning()
-        assert t["how"] == "tuned"
+        # a small mesh: the default timed once, the defaults kept
+        assert t["how"] == "tuned" and (t["lin_minb"], t["ress_minb"]) == (4, 3)
+        assert t["lin_ms"][4] > 0 and t["lin_ms"][3] < 0 and all(v < 0 for v in t["ress_ms"].values())
+        g.set_tuning(-1, -1)
+        g.time_step(y, ac, nitr=1)
+        t = g.tuning()
+        assert t["how"] == "tuned" and all(v > 0 for v in t["lin_ms"].values())
         # the split residual is timed only when it is the outer residual in use
         split = p.get("outer_residual", 0) == L.PHGPU_RES_SPLITDF
         assert all((v > 0) == split for v in t["ress_ms"].values())
