@@ -214,6 +214,40 @@ int build_chunks(Ctx& C, const int* ien, const double* x_ref) {
     T(up(&C.d_ch_csr, csr));
     T(up(&C.d_ch_lien, lien));
     T(up(&C.d_ien, ien_c));
+    // per-chunk records for the bulk copies (16-byte aligned parts, sizes multiples of 16 bytes)
+    std::vector<int> rec_off(nch + 1, 0);
+    size_t words = 0;
+    int rec_max = 0;
+    for (int k = 0; k < nch; ++k) {
+        const int ne = elem_start[k + 1] - elem_start[k], nn = node_start[k + 1] - node_start[k];
+        const int w = chunk_record_words(ne, nn);
+        rec_max = std::max(rec_max, 4 * w);
+        words += (size_t)w;
+        if (words / 4 > (size_t)INT32_MAX) {
+            C.err = "chunk records exceed 2^31 16-byte units";
+            return PHGPU_ERR_TOO_LARGE;
+        }
+        rec_off[k + 1] = (int)(words / 4);
+    }
+    std::vector<uint32_t> rec(std::max<size_t>(words, 4), 0u);
+    for (int k = 0; k < nch; ++k) {
+        const int e0 = elem_start[k], ne = elem_start[k + 1] - e0;
+        const int n0 = node_start[k], nn = node_start[k + 1] - n0;
+        uint32_t* r = rec.data() + 4 * (size_t)rec_off[k];
+        r[0] = (uint32_t)e0;
+        r[1] = (uint32_t)ne;
+        r[2] = (uint32_t)n0;
+        r[3] = (uint32_t)nn;
+        for (int l = 0; l < nn; ++l) r[rec_ids_off() + l] = (uint32_t)nodes[n0 + l];
+        std::memcpy(r + rec_lien_off(nn), lien.data() + e0, sizeof(ushort4) * ne);
+        std::memcpy(r + rec_csr_off(ne, nn), csr.data() + 4 * (size_t)e0, sizeof(uint16_t) * 4 * ne);
+        for (int l = 0; l <= nn; ++l) r[rec_cst_off(ne, nn) + l] = (uint32_t)(cstart[n0 + l] - 4 * e0);
+    }
+    C.chunk_rec_max = rec_max;
+    std::vector<uint4> rec4(rec.size() / 4);
+    std::memcpy(rec4.data(), rec.data(), sizeof(uint4) * rec4.size());
+    T(up(&C.d_ch_rec, rec4));
+    T(up(&C.d_ch_rec_off, rec_off));
     return rc;
 }
 

@@ -456,12 +456,7 @@ k_chunk_res(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restri
 }
 
 // --------------------------------------------------------------------------
-// FP32 linearized product (RM_LIN) over the chunks of one colour, software-pipelined: each
-// CTA walks chunks chunk0 + blockIdx.x, + gridDim.x, ... and stages the next chunk's nodal
-// data (coordinates, direction, base state and the product's current values) into the other
-// half of a double buffer with cp.async while it computes the current one.  Chunks of one
-// colour share no node, so prefetching the product's values of a later chunk is safe.  The
-// arithmetic and the summation order are those of k_chunk_res<float, RM_LIN>.
+// persistent, software-pipelined sweeps over the chunks of one colour (cp.async staging)
 // --------------------------------------------------------------------------
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -473,109 +468,167 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-constexpr int kLinNode = 18;  // staged per node: x(3) direction(5) base state(5) product(5)
-
-// words of one data stage: node data, then (8-byte aligned) the chunk's local connectivity
-// (ushort4 per element), its slot lists (ushort) and their offsets (int)
-__host__ __device__ constexpr int lin_stage_words(int lmax) {
-    return ((((kLinNode * lmax + 1) & ~1) + 4 * kChunk + lmax + 2) + 1) & ~1;
-}
-// words of one node-id stage: e0, ne, n0, nn, then the chunk's global node ids
+// words of a node-id stage of the pipelined split residual: e0, ne, n0, nn, then the chunk's
+// global node ids
 __host__ __device__ constexpr int lin_id_words(int lmax) { return 4 + lmax; }
 
+// --- bulk copies (cp.async.bulk, completion on an mbarrier) ---
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+// one contiguous copy global -> shared: both addresses 16-byte aligned, size a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// a wait that gives up: false after kMbarTries unsuccessful tries (each may suspend the thread
+// for a short, hardware-chosen time), so that a copy that never completes cannot hang the GPU
+constexpr int kMbarTries = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    for (int i = 0; i < kMbarTries; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+
+// floats of one node-data stage of the pipelined linearized product: the packed base state
+// and coordinates (8 per node, 16-byte aligned), the direction (5) and the product (5)
+__host__ __device__ constexpr int lin_data_words(int lmax) { return (18 * lmax + 3) & ~3; }
+
+// The FP32 linearized product over the chunks of one colour, software-pipelined: each CTA
+// walks chunks chunk0 + blockIdx.x, + gridDim.x, ...  Per chunk, one thread moves the chunk's
+// record (header, node ids, connectivity, slot lists, slot offsets: contiguous, 16-byte aligned,
+// chunks.cu) into shared memory with one bulk copy two chunks ahead, completion signalled on an
+// mbarrier; one chunk ahead every thread gathers the chunk's node data with cp.async (the packed
+// base state and coordinates as two 16-byte copies, the direction and the product's current
+// values as 4-byte ones) into the other half of a double buffer, while the current chunk is
+// computed.  Chunks of one colour share no node, so prefetching the product's values of a later
+// chunk is safe.  The arithmetic and the summation order are those of k_chunk_res<float, RM_LIN>.
+// If a bulk copy does not complete within the wait limit, the CTA sets bit 8 of *err and returns.
 template <int MINB>
 __global__ void __launch_bounds__(kChunk, MINB)
-k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x, const float* __restrict__ ya,
-                 const float* __restrict__ yb, float* __restrict__ out, Phys<float> P, int lmax) {
+k_chunk_lin_pipe(const uint4* __restrict__ rec, const int* __restrict__ rec_off, int chunk0, int nch,
+                 const float4* __restrict__ xb, const float* __restrict__ ya, float* __restrict__ out, Phys<float> P,
+                 int lmax, int rec_bytes, int* __restrict__ err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float* sm = reinterpret_cast<float*>(smem_raw);
-    const int per = lin_stage_words(lmax);
-    const int lie_off = (kLinNode * lmax + 1) & ~1;  // even: ushort4 rows 8-byte aligned
-    int* ids = reinterpret_cast<int*>(sm + 2 * per);  // 3 x lin_id_words
-    const int idw = lin_id_words(lmax);
-    float* slot = sm + 2 * per + 3 * idw;
-    // node ids of chunk c (and its element and node ranges) into id stage ib
-    auto stage_ids = [&](int c, int ib) {
-        int* h = ids + ib * idw;
-        const int n0 = ca.node[c], nn = ca.node[c + 1] - n0;
-        if (threadIdx.x == 0) {
-            const int e0 = ca.elem[c];
-            h[0] = e0;
-            h[1] = ca.elem[c + 1] - e0;
-            h[2] = n0;
-            h[3] = nn;
-        }
-        for (int l = threadIdx.x; l < nn; l += blockDim.x) cp_async4(h + 4 + l, ca.nodes + n0 + l);
+    unsigned char* R = smem_raw;                                   // 3 record stages of rec_bytes
+    float* D = reinterpret_cast<float*>(smem_raw + 3 * (size_t)rec_bytes);  // 2 node-data stages
+    const int dw = lin_data_words(lmax);
+    float* slot = D + 2 * dw;                                      // 20 per element
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(slot + 20 * kChunk);
+    __shared__ int s_abort;
+    const int cend = chunk0 + nch, G = gridDim.x;
+    int c = chunk0 + blockIdx.x;
+    if (c >= cend) return;
+    auto issue = [&](int chunk, int st) {  // thread 0: the record of chunk into stage st
+        const unsigned bytes = 16u * (unsigned)(rec_off[chunk + 1] - rec_off[chunk]);
+        mbar_expect_tx(&bar[st], bytes);
+        bulk_g2s(R + (size_t)st * rec_bytes, rec + rec_off[chunk], bytes, &bar[st]);
     };
-    // nodal data, connectivity and slot lists of the chunk whose ids are in stage ib
-    auto stage_data = [&](int ib, float* b) {
-        const int* h = ids + ib * idw;
-        const int e0 = h[0], ne = h[1], n0 = h[2], nn = h[3];
-        float* sx = b;
-        float* sa = sx + 3 * lmax;
-        float* sb = sa + 5 * lmax;
-        float* so = sb + 5 * lmax;
-        float* sl = b + lie_off;                 // ne ushort4 (2 words each)
-        float* sc = sl + 2 * kChunk;             // 4 ne ushort slot ids (2 per word)
-        float* st = sc + 2 * kChunk;             // nn + 1 offsets
-        // the slot lists of a chunk start at 4 * its first element (each element corner once)
-        const unsigned* csr_w = reinterpret_cast<const unsigned*>(ca.csr) + 2 * (size_t)e0;
-        for (int i = threadIdx.x; i < ne; i += blockDim.x) {
-            const unsigned s8 = (unsigned)__cvta_generic_to_shared(sl + 2 * i);
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s8), "l"(ca.lien + e0 + i) : "memory");
-        }
-        for (int w = threadIdx.x; w < 2 * ne; w += blockDim.x) cp_async4(sc + w, csr_w + w);
-        for (int l = threadIdx.x; l <= nn; l += blockDim.x) cp_async4(st + l, ca.cstart + n0 + l);
+    auto record = [&](int st) { return reinterpret_cast<const int*>(R + (size_t)st * rec_bytes); };
+    // node data of the chunk whose record is in stage st, into data stage b
+    auto stage_data = [&](int st, float* b) {
+        const int* h = record(st);
+        const int nn = h[3];
+        const int* ids = h + rec_ids_off();
+        float* sxb = b;
+        float* sa = sxb + 8 * lmax;
+        float* so = sa + 5 * lmax;
         for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-            const size_t gn = (size_t)h[4 + l];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) cp_async4(sx + 3 * l + d, x + 3 * gn + d);
+            const size_t gn = (size_t)ids[l];
+            cp_async16(sxb + 8 * l, xb + 2 * gn);
+            cp_async16(sxb + 8 * l + 4, xb + 2 * gn + 1);
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
                 cp_async4(sa + 5 * l + k, ya + 5 * gn + k);
-                cp_async4(sb + 5 * l + k, yb + 5 * gn + k);
                 cp_async4(so + 5 * l + k, out + 5 * gn + k);
             }
         }
     };
-    const int cend = chunk0 + nch, G = gridDim.x;
-    int c = chunk0 + blockIdx.x;
-    if (c >= cend) return;
-    // prologue: ids of the first chunk, then its data and the ids of the next
-    stage_ids(c, 0);
-    cp_async_commit();
-    cp_async_wait<0>();
+    // every thread reaches this with the same ok: a failed wait ends the CTA after a second
+    // bounded wait for the copy it was waiting on
+    auto aborted = [&](bool ok, int st, unsigned parity) {
+        if (!ok) s_abort = 1;
+        __syncthreads();
+        if (!s_abort) return false;
+        if (threadIdx.x == 0) atomicOr(err, 8);
+        (void)mbar_wait(&bar[st], parity);
+        return true;
+    };
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        for (int i = 0; i < 3; ++i) mbar_init(&bar[i], 1);
+    }
     __syncthreads();
-    stage_data(0, sm);
-    if (c + G < cend) stage_ids(c + G, 1);
+    if (threadIdx.x == 0) {
+        issue(c, 0);
+        if (c + G < cend) issue(c + G, 1);
+    }
+    if (aborted(mbar_wait(&bar[0], 0), 0, 0)) {
+        if (c + G < cend) (void)mbar_wait(&bar[1], 0);  // the other copy in flight
+        return;
+    }
+    stage_data(0, D);
     cp_async_commit();
     for (int it = 0; c < cend; c += G, ++it) {
-        cp_async_wait<0>();  // data of chunk c, ids of chunk c + G
-        __syncthreads();
         const int cn = c + G;
-        if (cn < cend) stage_data((it + 1) % 3, sm + ((it + 1) & 1) * per);
-        if (cn + G < cend) stage_ids(cn + G, (it + 2) % 3);
+        const int sn = (it + 1) % 3;
+        const unsigned pn = (unsigned)(((it + 1) / 3) & 1);
+        cp_async_wait<0>();  // node data of chunk c
+        const bool ok = cn < cend ? mbar_wait(&bar[sn], pn) : true;  // record of chunk cn
+        if (aborted(ok, sn, pn)) return;
+        if (cn < cend) stage_data(sn, D + ((it + 1) & 1) * dw);
+        if (threadIdx.x == 0 && cn + G < cend) {
+            fence_proxy_async();  // the stage's last readers finished at the barrier above
+            issue(cn + G, (it + 2) % 3);
+        }
         cp_async_commit();
-        const float* cur = sm + (it & 1) * per;
-        const int* h = ids + (it % 3) * idw;
-        const int e0 = h[0], ne = h[1], nn = h[3];
-        const float* sx = cur;
-        const float* sa = sx + 3 * lmax;
-        const float* sb = sa + 5 * lmax;
-        const float* so = sb + 5 * lmax;
-        const ushort4* slie = reinterpret_cast<const ushort4*>(cur + lie_off);
-        const unsigned short* scsr = reinterpret_cast<const unsigned short*>(cur + lie_off + 2 * kChunk);
-        const int* scst = reinterpret_cast<const int*>(cur + lie_off + 4 * kChunk);
+        const int* h = record(it % 3);
+        const int ne = h[1], nn = h[3];
+        const int* ids = h + rec_ids_off();
+        const ushort4* slie = reinterpret_cast<const ushort4*>(h + rec_lien_off(nn));
+        const unsigned short* scsr = reinterpret_cast<const unsigned short*>(h + rec_csr_off(ne, nn));
+        const int* scst = h + rec_cst_off(ne, nn);
+        const float* cur = D + (it & 1) * dw;
+        const float* sxb = cur;
+        const float* sa = sxb + 8 * lmax;
+        const float* so = sa + 5 * lmax;
         if ((int)threadIdx.x < ne) {
             const ushort4 ln = slie[threadIdx.x];
             const int nd[4] = {ln.x, ln.y, ln.z, ln.w};
             float xl[4][3], va[4][5], vb[4][5];
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
-#pragma unroll
-                for (int d = 0; d < 3; ++d) xl[a][d] = sx[3 * nd[a] + d];
+                const float4 p0 = *reinterpret_cast<const float4*>(sxb + 8 * nd[a]);
+                const float4 p1 = *reinterpret_cast<const float4*>(sxb + 8 * nd[a] + 4);
+                vb[a][0] = p0.x;
+                vb[a][1] = p0.y;
+                vb[a][2] = p0.z;
+                vb[a][3] = p0.w;
+                vb[a][4] = p1.x;
+                xl[a][0] = p1.y;
+                xl[a][1] = p1.z;
+                xl[a][2] = p1.w;
                 lds5(sa, nd[a], va[a]);
-                lds5(sb, nd[a], vb[a]);
             }
             float o[4][5];
             elem_res<float, RM_LIN>(P, xl, va, vb, o);
@@ -586,22 +639,32 @@ k_chunk_lin_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x,
                 for (int k = 0; k < 5; ++k) sl[5 * a + k] = o[a][k];
         }
         __syncthreads();
-        const int sbase = 4 * e0;
         for (int l = threadIdx.x; l < nn; l += blockDim.x) {
             float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-            const int s0 = scst[l] - sbase, s1 = scst[l + 1] - sbase;
+            const int s0 = scst[l], s1 = scst[l + 1];
             for (int s = s0; s < s1; ++s) {
                 const float* sl = slot + 5 * (int)scsr[s];
 #pragma unroll
                 for (int k = 0; k < 5; ++k) acc[k] += sl[k];
             }
-            float* og = out + 5 * (size_t)h[4 + l];
+            float* og = out + 5 * (size_t)ids[l];
 #pragma unroll
             for (int k = 0; k < 5; ++k) og[k] = so[5 * l + k] + acc[k];
         }
         __syncthreads();
     }
     cp_async_wait<0>();
+}
+
+// the FP32 base state and the coordinates packed per node: (yb0, yb1, yb2, yb3), (yb4, x0, x1, x2)
+__global__ void k_pack_xb(const float* __restrict__ xf, const float* __restrict__ yf, float4* __restrict__ xb,
+                          int N) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+        const float* y = yf + 5 * (size_t)n;
+        const float* x = xf + 3 * (size_t)n;
+        xb[2 * (size_t)n] = make_float4(y[0], y[1], y[2], y[3]);
+        xb[2 * (size_t)n + 1] = make_float4(y[4], x[0], x[1], x[2]);
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -2365,8 +2428,9 @@ size_t ress_pipe_smem(const Ctx& C, bool with_q) {
                             (size_t)kChunk * kSplitSlot);
 }
 size_t lin_pipe_smem(const Ctx& C) {
-    return sizeof(float) * (2 * (size_t)lin_stage_words(C.chunk_lmax) + 3 * (size_t)lin_id_words(C.chunk_lmax) +
-                            (size_t)kChunk * 20);
+    // 3 record stages, 2 node-data stages, the element slots, 3 mbarriers
+    return 3 * (size_t)C.chunk_rec_max + sizeof(float) * (2 * (size_t)lin_data_words(C.chunk_lmax) + (size_t)kChunk * 20) +
+           4 * sizeof(unsigned long long);
 }
 // extra shared memory of the reconstructed flux (idiff = 1): 12 per chunk node
 template <typename R>
@@ -2470,14 +2534,17 @@ void launch_elem_res(Ctx& C, int mode, const R* x, const R* ya, const R* yb, con
         else if (mode == RM_MODRES)
             k_chunk_res<R, RM_MODRES><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
         else if constexpr (std::is_same<R, float>::value) {
-            if (!C.cfg.no_pipe && !skip && !iabres) {
+            // the pipelined kernel reads the base state from the packed records of d_yf
+            if (!C.cfg.no_pipe && !skip && !iabres && (const void*)yb == (const void*)C.d_yf) {
                 const int g = std::min(nc, C.lin_pipe_grid);
+                const float4* xbp = C.d_xbf;
+                int* err = C.d_flag + 1;
                 if (C.lin_minb == 3)
-                    k_chunk_lin_pipe<3><<<g, kChunk, lin_pipe_smem(C), C.stream>>>(ca, c0, nc, x, ya, yb, out, P,
-                                                                                   C.chunk_lmax);
+                    k_chunk_lin_pipe<3><<<g, kChunk, lin_pipe_smem(C), C.stream>>>(
+                        C.d_ch_rec, C.d_ch_rec_off, c0, nc, xbp, ya, out, P, C.chunk_lmax, C.chunk_rec_max, err);
                 else
-                    k_chunk_lin_pipe<4><<<g, kChunk, lin_pipe_smem(C), C.stream>>>(ca, c0, nc, x, ya, yb, out, P,
-                                                                                   C.chunk_lmax);
+                    k_chunk_lin_pipe<4><<<g, kChunk, lin_pipe_smem(C), C.stream>>>(
+                        C.d_ch_rec, C.d_ch_rec_off, c0, nc, xbp, ya, out, P, C.chunk_lmax, C.chunk_rec_max, err);
             } else
                 k_chunk_res<R, RM_LIN><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, ya, yb, ac, out, P, iabres, skip);
         } else
@@ -2511,6 +2578,13 @@ void launch_qrec(Ctx& C, const R* x, const R* y, R* out) {
 template void launch_qrec<double>(Ctx&, const double*, const double*, double*);
 template void launch_qrec<float>(Ctx&, const float*, const float*, float*);
 
+void pack_xb(Ctx& C) {
+    if (C.E == 0) return;
+    const int blocks = (int)std::min<size_t>(((size_t)C.N + 255) / 256, 8192);
+    k_pack_xb<<<blocks, 256, 0, C.stream>>>(C.d_xf, C.d_yf, C.d_xbf, C.N);
+    ++C.launches;
+}
+
 // ---------------------------------------------------------------------------
 // autotuner of the two pipelined sweeps' register/occupancy variants
 // ---------------------------------------------------------------------------
@@ -2541,6 +2615,7 @@ int autotune_sweeps(Ctx& C) {
     const size_t n5 = 5 * (size_t)C.N;
     const long long l0 = C.launches;
     split_f32(C, C.d_y, C.d_yf, C.d_ylo, n5);
+    pack_xb(C);
     to_f32(C, C.d_ac, C.d_acf, n5);
     cudaEvent_t e0 = C.ev[2], e1 = C.ev[3];
     auto time_it = [&](auto&& fn) {
@@ -2573,6 +2648,12 @@ int autotune_sweeps(Ctx& C) {
         C.launches = l0;
         select_sweep_variants(C, def_l, def_r);
         C.tuned = true;
+        int f = 0;
+        if (check(C, cudaMemcpyAsync(&f, C.d_flag + 1, sizeof(int), cudaMemcpyDeviceToHost, C.stream), "autotune") !=
+                PHGPU_OK ||
+            check(C, cudaStreamSynchronize(C.stream), "autotune") != PHGPU_OK)
+            return PHGPU_ERR_CUDA;
+        if (f & kPipeCopyFailed) return fail(C, PHGPU_ERR_CUDA, kPipeCopyMsg);
         return check(C, cudaGetLastError(), "autotune");
     }
     for (int m = 3; m <= 4; ++m)
@@ -2589,6 +2670,12 @@ int autotune_sweeps(Ctx& C) {
     C.launches = l0;  // tuning launches are not part of the solve
     select_sweep_variants(C, best_l, best_r);
     C.tuned = true;
+    int f = 0;
+    if (check(C, cudaMemcpyAsync(&f, C.d_flag + 1, sizeof(int), cudaMemcpyDeviceToHost, C.stream), "autotune") !=
+            PHGPU_OK ||
+        check(C, cudaStreamSynchronize(C.stream), "autotune") != PHGPU_OK)
+        return PHGPU_ERR_CUDA;
+    if (f & kPipeCopyFailed) return fail(C, PHGPU_ERR_CUDA, kPipeCopyMsg);
     return check(C, cudaGetLastError(), "autotune");
 }
 

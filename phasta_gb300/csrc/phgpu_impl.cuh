@@ -223,6 +223,14 @@ struct Ctx {
     int* d_ch_cstart = nullptr;   // slot-list offsets (+1)
     unsigned short* d_ch_csr = nullptr;
     ushort4* d_ch_lien = nullptr;
+    // one 16-byte aligned record per chunk for the bulk copies of the pipelined linearized
+    // product (chunk_record_words): header, node ids, connectivity, slot lists, slot offsets
+    uint4* d_ch_rec = nullptr;
+    int* d_ch_rec_off = nullptr;  // nchunk+1, in 16-byte units
+    int chunk_rec_max = 0;        // largest record, bytes
+    // the FP32 base state and coordinates packed per node (yb0..yb4, x0, x1, x2): two 16-byte
+    // copies per node instead of eight 4-byte ones; rebuilt whenever d_yf is written
+    float4* d_xbf = nullptr;
     int4* d_ienb = nullptr;       // Eb (face nodes first)
     int* d_iBCB = nullptr;        // Eb
     double* d_BCB = nullptr;      // Eb*18  [e][n][6]
@@ -339,6 +347,20 @@ void launch_topo(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R
                  int iabres, const int* skip, const R* ql = nullptr);
 void upload_tables(Ctx& C);
 int build_chunks(Ctx& C, const int* ien, const double* x_ref);
+// 4-byte words of a chunk record of ne elements and nn nodes, and the word offsets of its parts:
+// header {e0, ne, n0, nn}; node ids (nn); connectivity (ne ushort4); slot lists (4 ne ushort);
+// slot-list offsets relative to the chunk's first slot (nn + 1) -- each part padded to 16 bytes
+__host__ __device__ constexpr int rec_pad4(int w) { return (w + 3) & ~3; }
+__host__ __device__ constexpr int rec_ids_off() { return 4; }
+__host__ __device__ constexpr int rec_lien_off(int nn) { return 4 + rec_pad4(nn); }
+__host__ __device__ constexpr int rec_csr_off(int ne, int nn) { return rec_lien_off(nn) + rec_pad4(2 * ne); }
+__host__ __device__ constexpr int rec_cst_off(int ne, int nn) { return rec_csr_off(ne, nn) + rec_pad4(2 * ne); }
+__host__ __device__ constexpr int chunk_record_words(int ne, int nn) { return rec_cst_off(ne, nn) + rec_pad4(nn + 1); }
+// write the FP32 base state d_yf into the packed node records d_xbf (after every write of d_yf)
+void pack_xb(Ctx& C);
+// bit of flag[1] that the pipelined linearized product sets when a bulk copy did not complete
+constexpr int kPipeCopyFailed = 8;
+constexpr const char* kPipeCopyMsg = "pipelined linearized product: a bulk copy did not complete in time";
 int configure_element_kernels(Ctx& C);
 // time the variants of the pipelined linearized product and split residual on the resident
 // FP32 state (d_yf, d_ylo, d_acf) and keep the fastest of each (no-op once tuned or forced)

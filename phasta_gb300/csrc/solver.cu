@@ -745,6 +745,7 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
             if (iKs < 1 || iKs > K) return fail(C, PHGPU_ERR_CUDA, "cycle graph ran no Krylov iteration");
             for (int i = 1; i <= iKs; ++i) C.launches += G.launches[i];
             st->ntotGM += iKs;
+            if (C.h_flag[1] & kPipeCopyFailed) return fail(C, PHGPU_ERR_CUDA, kPipeCopyMsg);
             nonfinite = C.h_flag[1] != 0;
         } else {
             for (int iK = 1; iK <= K; ++iK) {
@@ -753,6 +754,7 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
                 st->ntotGM += 1;
                 PH_TRY(check(C, cudaMemcpyAsync(C.h_flag, C.d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, C.stream), "flag"));
                 PH_TRY(sync(C));
+                if (C.h_flag[1] & kPipeCopyFailed) return fail(C, PHGPU_ERR_CUDA, kPipeCopyMsg);
                 if (C.h_flag[1]) {
                     nonfinite = true;
                     break;
@@ -837,6 +839,7 @@ int assemble_and_factor(Ctx& C, int lhs, bool asm_bd, bool sparse, bool ebe) {
         // outer residual (FP64, or FP64 Galerkin + FP32 stabilization); FP32 block-diagonal tangent
         if (C.cfg.outer_residual == PHGPU_RES_SPLITDF) split_f32(C, C.d_y, C.d_yf, C.d_ylo, n5);
         else to_f32(C, C.d_y, C.d_yf, n5);
+        pack_xb(C);
         to_f32(C, C.d_ac, C.d_acf, n5);
         if (C.cfg.outer_residual == PHGPU_RES_GALERKIN64 || C.cfg.outer_residual == PHGPU_RES_SPLITDF) {
             if (C.cfg.idiff == 1 && C.cfg.outer_residual == PHGPU_RES_GALERKIN64)
@@ -1185,6 +1188,7 @@ int step_graph_run(Ctx& C, int nitr, phgpu_stats* st, bool* used) {
     for (int it = 0; it < nitr; ++it) {
         const double* o = out + 8 * it;
         if (o[4] != 0.0) return fail(C, PHGPU_ERR_SINGULAR, "zero or non-finite pivot in the block-diagonal LU");
+        if (((int)o[5]) & kPipeCopyFailed) return fail(C, PHGPU_ERR_CUDA, kPipeCopyMsg);
         if (((int)o[5]) & 2) return fail(C, PHGPU_ERR_NONFINITE, "non-finite value in GMRES");
         const int iks = (int)o[3];
         iks_tot += iks;
@@ -1365,6 +1369,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     T(dalloc(C, &C.d_ienw, 6 * (size_t)std::max(C.nwedge, 1)));
     T(dalloc(C, &C.d_x, 3 * (size_t)N));
     T(dalloc(C, &C.d_xf, 3 * (size_t)N));
+    T(dalloc(C, &C.d_xbf, 2 * (size_t)N));
     T(dalloc(C, &C.d_xlo, 3 * (size_t)N));
     T(dalloc(C, &C.d_iBC, N));
     T(dalloc(C, &C.d_BC, 6 * (size_t)N));
@@ -1458,6 +1463,7 @@ int phgpu_destroy(phgpu_ctx* h) {
     if (C.stepg.d_stats) cudaFree(C.stepg.d_stats);
     if (C.stepg.aux) cudaStreamDestroy(C.stepg.aux);
     void* ptrs[] = {C.d_ch_elem, C.d_ch_node, C.d_ch_nodes, C.d_ch_cstart, C.d_ch_csr, C.d_ch_lien,
+                    C.d_ch_rec, C.d_ch_rec_off, C.d_xbf,
                     C.d_bdstage, C.d_ien, C.d_ienh, C.d_ienw, C.d_ienb, C.d_iBCB, C.d_BCB, C.d_x, C.d_xf, C.d_xlo, C.d_iBC, C.d_BC, C.d_iper, C.d_bcn,
                     C.d_slaves, C.d_mst, C.d_slv_start, C.d_slv, C.d_y, C.d_ac, C.d_yold, C.d_acold, C.d_res,
                     C.d_rmes, C.d_Dy, C.d_ypre, C.d_t64, C.d_t64b, C.d_bd, C.d_yf, C.d_ylo, C.d_acf, C.d_resf, C.d_rmesf,
@@ -1989,6 +1995,7 @@ int phgpu_sweep_dev(phgpu_ctx* h, int which) {
             break;
         case 5:
             to_f32(C, C.d_y, C.d_yf, n5);
+            pack_xb(C);
             to_f32(C, C.d_ac, C.d_acf, n5);
             break;
         case 17:  // one application of the learned preconditioner (needs weights and a solve's features)
@@ -2018,6 +2025,7 @@ int phgpu_sweep_dev(phgpu_ctx* h, int which) {
             break;
         case 8:
             split_f32(C, C.d_y, C.d_yf, C.d_ylo, n5);
+            pack_xb(C);
             to_f32(C, C.d_ac, C.d_acf, n5);
             break;
         case 9:   // FP32 assembled tangent (zero fill + element sweep)
