@@ -332,6 +332,32 @@ def run_gpu(args, rank, world):
     return result
 
 
+def launch_list_steps(args):
+    """Two time steps of the block-diagonal mixed-precision form, launched kernel by kernel (config
+    no_graph = 1: the same kernels as the step graph) after one time step of warm-up."""
+    import torch
+
+    from phasta_gb300 import _lib as L
+    from phasta_gb300 import build
+    from phasta_gb300.solver import GpuSolver
+    build.build()
+    case, params, y0, ac0 = make_workload(args.n, "mixed", args.workload, precond=L.PHGPU_PRECOND_BDIAG)
+    g = GpuSolver(case, dict(params, no_graph=1))
+    g.upload(y0, ac0, y0, ac0)
+    g.time_step_dev(NEWTON_PER_TIMESTEP)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    iks = []
+    for _ in range(2):
+        iks.append(g.time_step_dev(NEWTON_PER_TIMESTEP).iKs)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / (2 * NEWTON_PER_TIMESTEP) * 1e3
+    out = {"workload": WORKLOADS[args.workload].format(n=args.n), "ms_per_newton_wall": ms, "last_iKs": iks,
+           "tuning": {k: v for k, v in g.tuning().items() if k in ("lin_minb", "ress_minb", "how")}}
+    g.close()
+    return out
+
+
 def mixed_topology_object(args):
     """The mixed-topology workload: one connected periodic box of 80 x 80 cells in x, y whose z
     layers are 80 of hexes (512,000), 4 of prisms (51,200) and 52 of Kuhn tets (1,996,800),
@@ -673,8 +699,15 @@ def main():
     ap.add_argument("--order-n", type=int, default=96)
     ap.add_argument("--mixed-n", type=int, default=80)
     ap.add_argument("--skip-sparse", action="store_true", help="leave out the assembled-tangent solver lines")
+    ap.add_argument("--launch-list", action="store_true",
+                    help="only run 2 time steps (after one of warm-up) of the block-diagonal mixed form of --workload "
+                         "at --n, kernel by kernel (for an ncu launch list: kernels inside captured graphs are not "
+                         "listed), and print ms per Newton iteration")
     args = ap.parse_args()
     rank, world, _ = _dist()
+    if args.launch_list:
+        print(json.dumps(launch_list_steps(args)))
+        return
     if args.impl == "reference":
         out = run_reference(args)
         if out is not None:

@@ -477,6 +477,9 @@ __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)_
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
+// makes the initialised mbarriers visible to the async proxy (the bulk-copy unit that completes
+// them) before their first use
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
 __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
@@ -577,6 +580,7 @@ k_chunk_lin_pipe(const uint4* __restrict__ rec, const int* __restrict__ rec_off,
     if (threadIdx.x == 0) {
         s_abort = 0;
         for (int i = 0; i < 3; ++i) mbar_init(&bar[i], 1);
+        fence_mbar_init();
     }
     __syncthreads();
     if (threadIdx.x == 0) {
