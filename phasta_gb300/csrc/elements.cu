@@ -2618,6 +2618,10 @@ int autotune_sweeps(Ctx& C) {
     if (C.tuned || C.tune_forced || C.cfg.no_pipe || C.E == 0) return PHGPU_OK;
     const size_t n5 = 5 * (size_t)C.N;
     const long long l0 = C.launches;
+    // flag[1] collects the sweeps' bulk-copy status over the timing runs (the assembly after
+    // the tuner clears the flags again)
+    if (check(C, cudaMemsetAsync(C.d_flag + 1, 0, sizeof(int), C.stream), "autotune") != PHGPU_OK)
+        return PHGPU_ERR_CUDA;
     split_f32(C, C.d_y, C.d_yf, C.d_ylo, n5);
     pack_xb(C);
     to_f32(C, C.d_ac, C.d_acf, n5);

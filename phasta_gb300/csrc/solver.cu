@@ -1399,6 +1399,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     T(dalloc(C, &C.d_part, kRedBlocks));
     T(dalloc(C, &C.d_count, 1));
     T(dalloc(C, &C.d_flag, 4));
+    if (rc == PHGPU_OK) T(check(C, cudaMemsetAsync(C.d_flag, 0, sizeof(int) * 4, C.stream), "clear flags"));
     if (rc == PHGPU_OK && cudaMallocHost((void**)&C.h_scal, sizeof(double) * 16) != cudaSuccess) rc = PHGPU_ERR_NOMEM;
     if (rc == PHGPU_OK && cudaMallocHost((void**)&C.h_flag, sizeof(int) * 4) != cudaSuccess) rc = PHGPU_ERR_NOMEM;
     if (rc != PHGPU_OK) {
