@@ -174,7 +174,7 @@ enum {
                                 cycles finished the solve from where it stopped */
     PHGPU_NET_PLAIN = 2      /* block-diagonal GMRES only: precond = BDIAG, no weights, the
                                 reference count of a first solve, or the network switched off
-                                after two failures in a row */
+                                after two failures in a row (or one more than twice as slow) */
 };
 
 typedef struct phgpu_ctx phgpu_ctx;
@@ -335,7 +335,9 @@ int phgpu_sweep_dev(phgpu_ctx* ctx, int which);
  * iteration below that count; a learned cycle fails when it does not converge within the cap,
  * is not finite, or takes longer on the device than the reference iterations it replaces.  A
  * failed cycle is finished by block-diagonal cycles from where it stopped (nGMRES more cycles);
- * two failures in a row switch the network off until new weights are set.  The network: encoder 48 -> 64, three edge
+ * two failures in a row, or one learned cycle that takes more than twice the time of the
+ * reference iterations it replaces, switch the network off until new weights are set.  The
+ * network: encoder 48 -> 64, three edge
  * message-passing layers (hidden width 64), decoder 64 -> 5; BF16 GEMM operands with FP32
  * accumulation on the tensor cores, FP32 master weights.  Input per node: the direction (5), the
  * node's factored BDiag block (25, over their RMS), its state (5) and an active flag.

@@ -799,9 +799,13 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
     if (want_net) ++(use_net ? (net_ok ? C.net.n_used : C.net.n_fell_back) : C.net.n_plain);
     if (use_net) {
         st->net_fallback = net_ok ? PHGPU_NET_USED : PHGPU_NET_FELL_BACK;
+        // off after two failed learned cycles in a row, or at once after one that took more
+        // than twice the time of the block-diagonal iterations it was to replace
+        const bool much_slower = timed && C.net.ms_ref_iter > 0.0 &&
+                                 C.net.ms_last > 2.0 * C.net.its_ref * C.net.ms_ref_iter;
         if (net_ok) {
             C.net.fails = 0;
-        } else if (++C.net.fails >= 2) {
+        } else if (much_slower || ++C.net.fails >= 2) {
             C.net.disabled = true;
         }
     } else if (want_net) {

@@ -177,7 +177,9 @@ def _solve(g, y, ac):
 
 def test_identity_network_falls_back_and_still_converges(gpu_lib):
     """A network that does nothing (zero decoder) cannot converge below the block-diagonal count:
-    the solve falls back, converges anyway, and two such failures switch the network off."""
+    the solve falls back, converges anyway, and the network is switched off after two such
+    failures, or after the first when that learned cycle took more than twice the time of the
+    block-diagonal iterations it was to replace."""
     case, ph = mesh.channel_case(8)
     g, p = _mixed(case, ph, precond=L.PHGPU_PRECOND_LEARNED)
     y = mesh.uniform_state(case, 0.3, sigma=0.02)
@@ -188,12 +190,14 @@ def test_identity_network_falls_back_and_still_converges(gpu_lib):
         Dy, st = _solve(g, y, ac)
         assert st.echeck <= p["etol"] * st.unorm0 * (1 + 1e-12), st
         seen.append(st.net_fallback)
-    assert seen == [L.PHGPU_NET_PLAIN, L.PHGPU_NET_FELL_BACK, L.PHGPU_NET_FELL_BACK, L.PHGPU_NET_PLAIN]
+    assert seen in ([L.PHGPU_NET_PLAIN, L.PHGPU_NET_FELL_BACK, L.PHGPU_NET_FELL_BACK, L.PHGPU_NET_PLAIN],
+                    [L.PHGPU_NET_PLAIN, L.PHGPU_NET_FELL_BACK, L.PHGPU_NET_PLAIN, L.PHGPU_NET_PLAIN]), seen
     u = g.net_usage()
-    assert u["off"] and u["fell_back"] == 2 and u["plain"] == 2
+    nfb = seen.count(L.PHGPU_NET_FELL_BACK)
+    assert u["off"] and u["fell_back"] == nfb and u["plain"] == 4 - nfb
     # with the network off, a time step is block-diagonal and runs as one CUDA graph
     g.time_step(y, ac, 3)
-    assert g.step_graphs == 1 and g.net_usage()["plain"] == 5
+    assert g.step_graphs == 1 and g.net_usage()["plain"] == 7 - nfb
 
 
 def test_nonfinite_network_output_falls_back(gpu_lib):
