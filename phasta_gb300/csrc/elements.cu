@@ -1607,7 +1607,7 @@ template <typename R, bool BD_ONLY>
 __global__ void __launch_bounds__(kChunk, sizeof(R) == 4 ? (BD_ONLY ? PHGPU_FULL32BD_MINB : PHGPU_FULL32_MINB) : 2)
 k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restrict__ y, const R* __restrict__ ac,
              R* __restrict__ res, R* __restrict__ rmes, R* __restrict__ bd, Phys<R> P,
-             const R* __restrict__ ql = nullptr) {
+             const R* __restrict__ ql = nullptr, const float4* __restrict__ xb = nullptr) {
     constexpr int kFullOut = BD_ONLY ? 25 : kFullOutAll;  // values per slot: BDiag, or res rmes BDiag
     constexpr int kBd = BD_ONLY ? 0 : 10;                    // offset of BDiag in a slot
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1633,18 +1633,39 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
     }
     const int cs_own0 = (int)threadIdx.x < nn ? ca.cstart[n0 + threadIdx.x] : 0;
     const int cs_own1 = (int)threadIdx.x < nn ? ca.cstart[n0 + threadIdx.x + 1] : 0;
-    for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-        const int gn = ca.nodes[n0 + l];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) sx[3 * l + d] = ldg(x + 3 * (size_t)gn + d);
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            sy[5 * l + k] = ldg(y + 5 * (size_t)gn + k);
-            if (!BD_ONLY) sa[5 * l + k] = ldg(ac + 5 * (size_t)gn + k);  // the block diagonal needs no ac
+    // FP32 block diagonal alone: the state and coordinates packed per node (yb0..yb4, x0, x1,
+    // x2) when given, two 16-byte loads per node
+    bool packed = false;
+    if constexpr (BD_ONLY && sizeof(R) == 4) {
+        if (xb) {
+            packed = true;
+            for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+                const size_t gn = (size_t)ca.nodes[n0 + l];
+                const float4 p0 = __ldg(xb + 2 * gn), p1 = __ldg(xb + 2 * gn + 1);
+                sy[5 * l + 0] = p0.x;
+                sy[5 * l + 1] = p0.y;
+                sy[5 * l + 2] = p0.z;
+                sy[5 * l + 3] = p0.w;
+                sy[5 * l + 4] = p1.x;
+                sx[3 * l + 0] = p1.y;
+                sx[3 * l + 1] = p1.z;
+                sx[3 * l + 2] = p1.w;
+            }
         }
-        if (with_q)
-            for (int k = 0; k < 12; ++k) sq[12 * l + k] = ldg(ql + 13 * (size_t)gn + k);
     }
+    if (!packed)
+        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
+            const int gn = ca.nodes[n0 + l];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) sx[3 * l + d] = ldg(x + 3 * (size_t)gn + d);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                sy[5 * l + k] = ldg(y + 5 * (size_t)gn + k);
+                if (!BD_ONLY) sa[5 * l + k] = ldg(ac + 5 * (size_t)gn + k);  // the block diagonal needs no ac
+            }
+            if (with_q)
+                for (int k = 0; k < 12; ++k) sq[12 * l + k] = ldg(ql + 13 * (size_t)gn + k);
+        }
     if (!single)
         for (int i = threadIdx.x; i < kFullOut * nn; i += blockDim.x) acc[i] = R(0);
     // FP32: the whole chunk is computed before one accumulation round;
@@ -2744,12 +2765,16 @@ void launch_elem_full(Ctx& C, const R* x, const R* y, const R* ac, R* res, R* rm
     // BDiag alone (the mixed-precision preconditioner) runs the kernel without the residual terms
     const bool bd_only = !res && !rmes;
     const size_t sm = bd_only ? full_smem<R, true>(C) : full_smem<R>(C) + ((ql && res) ? q_smem<R>(C) : 0);
+    // the packed FP32 node records hold exactly this x and y
+    const float4* xb_packed = (sizeof(R) == 4 && (const void*)x == (const void*)C.d_xf &&
+                               (const void*)y == (const void*)C.d_yf) ? C.d_xbf : nullptr;
     const int ncol = (int)C.chunk_col_start.size() - 1;
     for (int c = 0; c < ncol; ++c) {
         const int c0 = C.chunk_col_start[c], nc = C.chunk_col_start[c + 1] - c0;
         if (nc <= 0) continue;
         if (bd_only)
-            k_chunk_full<R, true><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, ac, nullptr, nullptr, bd, P, nullptr);
+            k_chunk_full<R, true><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, ac, nullptr, nullptr, bd, P, nullptr,
+                                                              xb_packed);
         else
             k_chunk_full<R, false><<<nc, kChunk, sm, C.stream>>>(ca, c0, x, y, ac, res, rmes, bd, P,
                                                                (ql && res) ? ql : nullptr);
