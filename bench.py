@@ -132,6 +132,8 @@ def replica_throughput(local_ms: float, elements: int, steps: int, device: str =
 WORKLOADS = {
     "vortex": "periodic decaying vortex {n}^3x6 tets Mach0.1 Re1600 +0.1% noise, Kspace20 tol1e-3, 3 Newton/step",
     "channel": "channel {n}^3x6 tets Mach0.3 Re1000, Kspace20 tol1e-3, 3 Newton/step",
+    "layered": "connected periodic box {n}x{n}x(n + n/20 + 13n/20) cells of hexes, prisms and tets, Fourier modes "
+               "k<=8 Mach 0.35, Kspace20 tol1e-3, 3 Newton/step",
 }
 
 
@@ -143,6 +145,9 @@ def make_workload(n: int, precision: str, kind: str = "channel", precond: int = 
     if kind == "vortex":
         case, ph = mesh.periodic_vortex_case(n, mach=0.1, re=1600.0)
         y0 = mesh.vortex_state(case, mach=0.1, noise=1e-3)
+    elif kind == "layered":
+        case, ph = mesh.layered_case(n, n, max(1, n // 20), max(1, (13 * n) // 20), mach=0.35)
+        y0 = mesh.fourier_state(case, 0.35, kmax=8, noise=1e-3)
     else:
         case, ph = mesh.channel_case(n, mach=0.3, re=1000.0)
         y0 = mesh.uniform_state(case, 0.3, sigma=0.01)
@@ -686,7 +691,7 @@ def main():
     ap.add_argument("--steps", type=int, default=60, help="Newton iterations timed (20 time steps x 3)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "channel"])
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "channel", "layered"])
     ap.add_argument("--n", type=int, default=192)
     ap.add_argument("--channel-n", type=int, default=128)
     ap.add_argument("--weights", default=None, help="learned preconditioner weights (default: the committed file)")
