@@ -31,8 +31,10 @@ def nvcc() -> str:
 
 
 def _flags() -> list[str]:
+    # PHGPU_NVCC_FLAGS: extra flags, e.g. -DPHGPU_TOPO_LEAN_MINB=5 to compile another occupancy variant
+    extra = os.environ.get("PHGPU_NVCC_FLAGS", "").split()
     return ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
-                   "--expt-relaxed-constexpr"]
+                   "--expt-relaxed-constexpr", *extra]
 
 
 def _compile(src: str) -> Path:

@@ -1897,9 +1897,16 @@ template <> __device__ __forceinline__ float tqwt<float>(int t, int q) { return 
 constexpr int kTopoThreads = 128;
 enum TopoMode : int { TM_RES = RM_RES, TM_MODRES = RM_MODRES, TM_LIN = RM_LIN, TM_FULL = 4, TM_QREC = 5 };
 constexpr int kTopoNode = 25;  // staged per node: x(3) ya(5) yb(5) reconstructed flux(12)
+// the FP32 linearized and modified residuals read no reconstructed flux, no conservative
+// variables and no DC terms: a lean layout (13 values per node, the point values up to kDu)
+// lets a fifth CTA per SM fit in shared memory
+template <typename R, int MODE>
+constexpr bool topo_lean() { return sizeof(R) == 4 && (MODE == RM_LIN || MODE == RM_MODRES); }
+template <typename R, int MODE>
+constexpr int topo_node() { return topo_lean<R, MODE>() ? 13 : kTopoNode; }
 
 // shared values of one quadrature point (FP64 also holds the discontinuity-capturing terms)
-template <int NEN, bool DC = false>
+template <int NEN, bool DC = false, bool LEAN = false>
 struct TopoQp {
     static constexpr int kShg = 0;                  // shg[b][i], NEN*3
     static constexpr int kW = NEN * 3;              // WdetJ
@@ -1911,29 +1918,38 @@ struct TopoQp {
     static constexpr int kDu = kVq + 3;             // conservative variables (full mode) (5)
     static constexpr int kDq = kDu + 5;             // div of the reconstructed flux (4)
     static constexpr int kDc = kDq + 4;             // DC and g^ij A0 Y,j (16, FP64)
-    static constexpr int kN = kDc + (DC ? 16 : 0);
+    static constexpr int kN = LEAN ? kDu : kDc + (DC ? 16 : 0);
 };
 
+// resident CTAs per SM the lean variants are compiled for (their shared memory allows 6)
+#ifndef PHGPU_TOPO_LEAN_MINB
+#define PHGPU_TOPO_LEAN_MINB 6
+#endif
+template <typename R, int MODE>
+constexpr int topo_minb() { return topo_lean<R, MODE>() ? PHGPU_TOPO_LEAN_MINB : 1; }
+
 template <typename R, int NEN, int TOPO, int MODE>
-__global__ void __launch_bounds__(kTopoThreads)
+__global__ void __launch_bounds__(kTopoThreads, topo_minb<R, MODE>())
 k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __restrict__ ya,
        const R* __restrict__ yb, const R* __restrict__ ac, R* __restrict__ res, R* __restrict__ rmes,
        R* __restrict__ bd, Phys<R> P, int iabres, const int* __restrict__ skip, const R* __restrict__ ql) {
     if (skip && *skip) return;
-    using Q = TopoQp<NEN, sizeof(R) == 8>;
+    constexpr bool LEAN = topo_lean<R, MODE>();
+    constexpr int NS = topo_node<R, MODE>();  // staged values per node
+    using Q = TopoQp<NEN, sizeof(R) == 8, LEAN>;
     constexpr int EPB = kTopoThreads / NEN;  // elements per CTA
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R* sm = reinterpret_cast<R*>(smem_raw);
     const int le = threadIdx.x / NEN, a = threadIdx.x % NEN;
     const int e = blockIdx.x * EPB + le;
     const bool active = le < EPB && e < ne;
-    R* sx = sm + (size_t)le * NEN * kTopoNode;
-    R* sq = sm + (size_t)EPB * NEN * kTopoNode + (size_t)le * NEN * Q::kN;
+    R* sx = sm + (size_t)le * NEN * NS;
+    R* sq = sm + (size_t)EPB * NEN * NS + (size_t)le * NEN * Q::kN;
     const bool with_q = (MODE == TM_RES || MODE == TM_FULL) && ql != nullptr;
     int node = 0;
     if (active) {
         node = ien[(size_t)e * NEN + a];
-        R* s = sx + kTopoNode * a;
+        R* s = sx + NS * a;
 #pragma unroll
         for (int d = 0; d < 3; ++d) s[d] = ldg(x + 3 * (size_t)node + d);
         const R* bsrc = (MODE == TM_RES || MODE == TM_FULL) ? ac : yb;
@@ -1956,7 +1972,7 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
             for (int j = 0; j < 3; ++j) {
                 R acc = R(0);
 #pragma unroll
-                for (int b = 0; b < NEN; ++b) acc += sx[kTopoNode * b + i] * tshgl<R>(TOPO, q, j, b);
+                for (int b = 0; b < NEN; ++b) acc += sx[NS * b + i] * tshgl<R>(TOPO, q, j, b);
                 dxdxi[i][j] = acc;
             }
         R di[3][3];
@@ -1994,7 +2010,7 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
                 o[Q::kShg + 3 * b + i] = sh[i];
             }
             const R Nb = tshp<R>(TOPO, q, b);
-            const R* s = sx + kTopoNode * b;
+            const R* s = sx + NS * b;
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
                 const R va = s[3 + k];
@@ -2092,9 +2108,11 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
             for (int j = 0; j < 3; ++j) o[Q::kVt + 3 * i + j] = vs.t[i][j];
             o[Q::kVq + i] = vs.q[i];
         }
-        const R du[5] = {st.rho, st.rho * st.u[0], st.rho * st.u[1], st.rho * st.u[2], st.rho * (st.ei + st.rk)};
+        if constexpr (!LEAN) {
+            const R du[5] = {st.rho, st.rho * st.u[0], st.rho * st.u[1], st.rho * st.u[2], st.rho * (st.ei + st.rk)};
 #pragma unroll
-        for (int k = 0; k < 5; ++k) o[Q::kDu + k] = du[k];
+            for (int k = 0; k < 5; ++k) o[Q::kDu + k] = du[k];
+        }
         if constexpr (sizeof(R) == 8 && MODE != TM_LIN) {
             // discontinuity capturing (e3dc.f): rTLS pairs the least-squares residual with its
             // tau-scaled self for the residual, with itself for the modified residual
@@ -2377,21 +2395,26 @@ void upload_topo_tables(Ctx& C) {
     check(C, cudaMemcpyToSymbolAsync(c_topof, tf, sizeof(tf), 0, cudaMemcpyHostToDevice, C.stream), "upload tables");
 }
 
-template <typename R, int NEN>
+template <typename R, int NEN, int MODE>
 constexpr size_t topo_smem() {
-    return sizeof(R) * (size_t)(kTopoThreads / NEN) * NEN * (kTopoNode + TopoQp<NEN, sizeof(R) == 8>::kN);
+    return sizeof(R) * (size_t)(kTopoThreads / NEN) * NEN *
+           (topo_node<R, MODE>() + TopoQp<NEN, sizeof(R) == 8, topo_lean<R, MODE>()>::kN);
 }
 
 template <typename R, int NEN, int TOPO>
 int configure_topo_kernels(Ctx& C) {
-    const int sm = (int)topo_smem<R, NEN>();
     int rc = PHGPU_OK;
     auto T = [&](cudaError_t e) { if (rc == PHGPU_OK) rc = check(C, e, "cudaFuncSetAttribute"); };
-    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_QREC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)topo_smem<R, NEN, TM_RES>()));
+    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)topo_smem<R, NEN, TM_MODRES>()));
+    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)topo_smem<R, NEN, TM_LIN>()));
+    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)topo_smem<R, NEN, TM_FULL>()));
+    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_QREC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)topo_smem<R, NEN, TM_QREC>()));
     return rc;
 }
 
@@ -2401,7 +2424,6 @@ static void launch_topo_one(Ctx& C, int mode, const int* d_ien, const std::vecto
                             const int* skip, const R* ql) {
     const Phys<R> P = make_phys<R>(C.cfg);
     constexpr int EPB = kTopoThreads / NEN;
-    const size_t sm = topo_smem<R, NEN>();
     const int ncol = (int)col.size() - 1;
     for (int c = 0; c < ncol; ++c) {
         const int e0 = col[c], ne = col[c + 1] - e0;
@@ -2410,19 +2432,19 @@ static void launch_topo_one(Ctx& C, int mode, const int* d_ien, const std::vecto
         const int* ie = d_ien + (size_t)NEN * e0;
         switch (mode) {
             case TM_RES:
-                k_topo<R, NEN, TOPO, TM_RES><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
+                k_topo<R, NEN, TOPO, TM_RES><<<grid, kTopoThreads, topo_smem<R, NEN, TM_RES>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
                 break;
             case TM_MODRES:
-                k_topo<R, NEN, TOPO, TM_MODRES><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
+                k_topo<R, NEN, TOPO, TM_MODRES><<<grid, kTopoThreads, topo_smem<R, NEN, TM_MODRES>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
                 break;
             case TM_LIN:
-                k_topo<R, NEN, TOPO, TM_LIN><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
+                k_topo<R, NEN, TOPO, TM_LIN><<<grid, kTopoThreads, topo_smem<R, NEN, TM_LIN>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
                 break;
             case TM_QREC:
-                k_topo<R, NEN, TOPO, TM_QREC><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
+                k_topo<R, NEN, TOPO, TM_QREC><<<grid, kTopoThreads, topo_smem<R, NEN, TM_QREC>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
                 break;
             default:
-                k_topo<R, NEN, TOPO, TM_FULL><<<grid, kTopoThreads, sm, C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
+                k_topo<R, NEN, TOPO, TM_FULL><<<grid, kTopoThreads, topo_smem<R, NEN, TM_FULL>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
                 break;
         }
         ++C.launches;
