@@ -1921,9 +1921,12 @@ struct TopoQp {
     static constexpr int kN = LEAN ? kDu : kDc + (DC ? 16 : 0);
 };
 
-// resident CTAs per SM the lean variants are compiled for (their shared memory allows 6)
+// resident CTAs per SM the lean variants are compiled for: their shared memory allows 6, which
+// costs spills (80 registers); at 5 (96 registers, no spill) the mixed-topology Newton iteration
+// takes 14.46 ms against 14.95 at 6, 15.06 uncapped (104 registers, 4 CTAs) and 14.78 with the
+// full layout
 #ifndef PHGPU_TOPO_LEAN_MINB
-#define PHGPU_TOPO_LEAN_MINB 6
+#define PHGPU_TOPO_LEAN_MINB 5
 #endif
 template <typename R, int MODE>
 constexpr int topo_minb() { return topo_lean<R, MODE>() ? PHGPU_TOPO_LEAN_MINB : 1; }
