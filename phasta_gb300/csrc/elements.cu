@@ -1935,7 +1935,8 @@ template <typename R, int NEN, int TOPO, int MODE>
 __global__ void __launch_bounds__(kTopoThreads, topo_minb<R, MODE>())
 k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __restrict__ ya,
        const R* __restrict__ yb, const R* __restrict__ ac, R* __restrict__ res, R* __restrict__ rmes,
-       R* __restrict__ bd, Phys<R> P, int iabres, const int* __restrict__ skip, const R* __restrict__ ql) {
+       R* __restrict__ bd, Phys<R> P, int iabres, const int* __restrict__ skip, const R* __restrict__ ql,
+       const float4* __restrict__ xbp = nullptr) {
     if (skip && *skip) return;
     constexpr bool LEAN = topo_lean<R, MODE>();
     constexpr int NS = topo_node<R, MODE>();  // staged values per node
@@ -1953,13 +1954,31 @@ k_topo(const int* __restrict__ ien, int ne, const R* __restrict__ x, const R* __
     if (active) {
         node = ien[(size_t)e * NEN + a];
         R* s = sx + NS * a;
+        bool packed = false;
+        if constexpr (LEAN) {
+            if (xbp) {
+                // the FP32 base state and coordinates packed per node: two 16-byte loads
+                const float4 p0 = __ldg(xbp + 2 * (size_t)node), p1 = __ldg(xbp + 2 * (size_t)node + 1);
+                s[8] = p0.x;
+                s[9] = p0.y;
+                s[10] = p0.z;
+                s[11] = p0.w;
+                s[12] = p1.x;
+                s[0] = p1.y;
+                s[1] = p1.z;
+                s[2] = p1.w;
+                packed = true;
+            }
+        }
+        if (!packed) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) s[d] = ldg(x + 3 * (size_t)node + d);
+            for (int d = 0; d < 3; ++d) s[d] = ldg(x + 3 * (size_t)node + d);
+        }
         const R* bsrc = (MODE == TM_RES || MODE == TM_FULL) ? ac : yb;
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             s[3 + k] = ldg(ya + 5 * (size_t)node + k);
-            if (MODE != TM_QREC) s[8 + k] = ldg(bsrc + 5 * (size_t)node + k);
+            if (MODE != TM_QREC && !packed) s[8 + k] = ldg(bsrc + 5 * (size_t)node + k);
         }
         if (with_q)
             for (int k = 0; k < 12; ++k) s[13 + k] = ldg(ql + 13 * (size_t)node + k);
@@ -2428,6 +2447,9 @@ static void launch_topo_one(Ctx& C, int mode, const int* d_ien, const std::vecto
     const Phys<R> P = make_phys<R>(C.cfg);
     constexpr int EPB = kTopoThreads / NEN;
     const int ncol = (int)col.size() - 1;
+    // the packed FP32 node records hold exactly this x and base state
+    const float4* xbp = (sizeof(R) == 4 && (const void*)x == (const void*)C.d_xf && (const void*)yb == (const void*)C.d_yf)
+                            ? C.d_xbf : nullptr;
     for (int c = 0; c < ncol; ++c) {
         const int e0 = col[c], ne = col[c + 1] - e0;
         if (ne <= 0) continue;
@@ -2438,10 +2460,10 @@ static void launch_topo_one(Ctx& C, int mode, const int* d_ien, const std::vecto
                 k_topo<R, NEN, TOPO, TM_RES><<<grid, kTopoThreads, topo_smem<R, NEN, TM_RES>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
                 break;
             case TM_MODRES:
-                k_topo<R, NEN, TOPO, TM_MODRES><<<grid, kTopoThreads, topo_smem<R, NEN, TM_MODRES>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
+                k_topo<R, NEN, TOPO, TM_MODRES><<<grid, kTopoThreads, topo_smem<R, NEN, TM_MODRES>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql, xbp);
                 break;
             case TM_LIN:
-                k_topo<R, NEN, TOPO, TM_LIN><<<grid, kTopoThreads, topo_smem<R, NEN, TM_LIN>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
+                k_topo<R, NEN, TOPO, TM_LIN><<<grid, kTopoThreads, topo_smem<R, NEN, TM_LIN>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql, xbp);
                 break;
             case TM_QREC:
                 k_topo<R, NEN, TOPO, TM_QREC><<<grid, kTopoThreads, topo_smem<R, NEN, TM_QREC>(), C.stream>>>(ie, ne, x, ya, yb, ac, res, rmes, bd, P, iabres, skip, ql);
