@@ -2651,7 +2651,8 @@ template void launch_qrec<double>(Ctx&, const double*, const double*, double*);
 template void launch_qrec<float>(Ctx&, const float*, const float*, float*);
 
 void pack_xb(Ctx& C) {
-    if (C.E == 0) return;
+    // every topology's FP32 products read the packed records, so pack on every mesh
+    if (C.N == 0) return;
     const int blocks = (int)std::min<size_t>(((size_t)C.N + 255) / 256, 8192);
     k_pack_xb<<<blocks, 256, 0, C.stream>>>(C.d_xf, C.d_yf, C.d_xbf, C.N);
     ++C.launches;

@@ -249,6 +249,26 @@ def test_split_double_float_outer_residual_hex_wedge(gpu_lib, idiff):
 
 
 
+@pytest.mark.parametrize("which", ["hex", "wedge"])
+def test_mixed_newton_on_tet_free_meshes(gpu_lib, which):
+    """Meshes with no tets (the channel on hexes, the channel on prisms with triangle walls): the
+    FP32 products of the hexes and prisms read the packed node records that every write of the
+    FP32 state refreshes.  A mixed-precision Newton step against the oracle's FP64 one: the
+    update within 10 x the Krylov tolerance, the residual no larger than the oracle's plus that."""
+    from helpers import hexchannel, wedgechannel
+    case, p, y, ac = hexchannel(6) if which == "hex" else wedgechannel((6, 6, 4))
+    p = dict(p, Kspace=20)
+    o = pyoracle.Oracle(case, p)
+    r0 = np.linalg.norm(o.ElmRes(y, ac))
+    gm = GpuSolver(case, dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR,
+                              outer_residual=L.PHGPU_RES_SPLITDF))
+    y1, a1, st = gm.newton(y, ac, y, ac)
+    yo, ao, so, _ = o.newton(y, ac, y, ac)
+    assert st.echeck <= p["etol"] * st.unorm0
+    assert rel(y1 - y, yo - y) < 10 * p["etol"]
+    assert np.linalg.norm(o.ElmRes(y1, a1)) < np.linalg.norm(o.ElmRes(yo, ao)) + 10 * p["etol"] * r0
+
+
 @pytest.mark.parametrize("iDC", [1, 2, 3])
 @pytest.mark.parametrize("make", [lambda iDC: channel(10, ac_scale=0.05, sigma=0.05, iDC=iDC),
                                   lambda iDC: mixed(3, 3, (3, 3, 2), sigma=0.05, iDC=iDC)],
