@@ -24,7 +24,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _lib as L
-from .mesh import Case
+from .mesh import BndBlock, Case
 
 LCSYST = {1: "tetrahedron", 2: "hexahedron", 3: "wedge"}
 
@@ -205,8 +205,10 @@ def _min_edge(x, blocks):
 
 
 def read_case(dirname, rank: int = 0) -> Case:
-    """geombc.dat.<rank+1> as a ``mesh.Case``: linear tets, hexes and wedges; tet
-    boundary elements with their face first (0-based connectivity)."""
+    """geombc.dat.<rank+1> as a ``mesh.Case``: linear tets, hexes and wedges; boundary tets with
+    their face first, and boundary hexes and wedges as ``mesh.BndBlock``s (a wedge block's
+    boundary rule follows its face's node count, 3 or 4, as elmmfg.f:187 does; 0-based
+    connectivity)."""
     g = read_geombc(dirname, rank)
     ien = {1: [], 2: [], 3: []}
     for t, e in g["interior"]:
@@ -214,21 +216,30 @@ def read_case(dirname, rank: int = 0) -> Case:
             raise PhastaIOError(L.PHGPU_ERR_UNSUPPORTED,
                                 f"interior block lcsyst {t['lcsyst']}, order {t['ipordl']}, nshl {t['nshl']}")
         ien[t["lcsyst"]].append(np.abs(e) - 1)
-    ienb, ibcb, bcb = [], [], []
+    ienb, ibcb, bcb, bnd = [], [], [], {}
     for t, e, codes, vals in g["boundary"]:
-        if t["lcsyst"] != 1 or t["nshl"] != 4 or t["nshlb"] != 3:
-            raise PhastaIOError(L.PHGPU_ERR_UNSUPPORTED, f"boundary block lcsyst {t['lcsyst']} (tet faces only)")
-        ienb.append(np.abs(e) - 1)
-        ibcb.append(codes)
-        bcb.append(vals)
+        shape = (t["lcsyst"], t["nshl"], t["nshlb"])
+        if t["ipordl"] != 1 or shape not in ((1, 4, 3), (2, 8, 4), (3, 6, 3), (3, 6, 4)):
+            raise PhastaIOError(L.PHGPU_ERR_UNSUPPORTED, f"boundary block lcsyst {t['lcsyst']}, nshl {t['nshl']}, "
+                                                         f"nshlb {t['nshlb']}, order {t['ipordl']}")
+        if t["lcsyst"] == 1:
+            ienb.append(np.abs(e) - 1)
+            ibcb.append(codes)
+            bcb.append(vals)
+        else:
+            lc = 2 if t["lcsyst"] == 2 else (3 if t["nshlb"] == 3 else 4)
+            bnd.setdefault(lc, []).append((np.abs(e) - 1, codes, vals))
     iBC, BC = boundary_conditions(g["nBC"], g["iBCtmp"], g["BCinp"])
     x = np.ascontiguousarray(g["x"])
     cat = lambda parts, n: (np.concatenate(parts) if parts else np.zeros((0, n))).astype(np.int32)  # noqa: E731
     tets, hexes, wedges = cat(ien[1], 4), cat(ien[2], 8), cat(ien[3], 6)
+    bblocks = [BndBlock(lc, np.concatenate([b[0] for b in v]).astype(np.int32),
+                        np.concatenate([b[1] for b in v]).astype(np.int32), np.concatenate([b[2] for b in v]))
+               for lc, v in sorted(bnd.items())]
     return Case(nshg=g["info"]["nshg"], x=x, ien=tets, ienb=cat(ienb, 4), iBCB=cat(ibcb, 2),
                 BCB=(np.concatenate(bcb) if bcb else np.zeros((0, 3, 6))), iBC=iBC, BC=BC,
                 iper=(g["iper"] - 1).astype(np.int32), h=_min_edge(x, [tets, hexes, wedges]),
-                meta={"source": str(dirname)}, ienh=hexes, ienw=wedges)
+                meta={"source": str(dirname)}, ienh=hexes, ienw=wedges, bnd=bblocks)
 
 
 def _bcinp(case: Case):
@@ -272,9 +283,10 @@ def write_case(case: Case, dirname, rank: int = 0) -> Path:
         f.write("byteorder magic number", [362436], [362436], "integer")
         counts = [("number of nodes", case.nshg), ("number of modes", case.nshg),
                   ("number of interior elements", sum(len(e) for e, _ in blocks)),
-                  ("number of boundary elements", case.nbelem), ("maximum number of element nodes", nen),
+                  ("number of boundary elements", case.nbelem + sum(len(b.ien) for b in case.bnd)),
+                  ("maximum number of element nodes", nen),
                   ("number of interior tpblocks", len(blocks)),
-                  ("number of boundary tpblocks", 1 if case.nbelem else 0),
+                  ("number of boundary tpblocks", (1 if case.nbelem else 0) + len(case.bnd)),
                   ("number of nodes with Dirichlet BCs", len(codes)), ("number of shape functions", nen)]
         for k, v in counts:
             f.writeheader(k, [v], 0, "integer")
@@ -292,4 +304,14 @@ def write_case(case: Case, dirname, rank: int = 0) -> Path:
             f.write("connectivity boundary linear tetrahedron", h, (np.asarray(case.ienb, np.int32) + 1).T, "integer")
             f.write("nbc codes linear tetrahedron", h, np.asarray(case.iBCB, np.int32).T, "integer")
             f.write("nbc values linear tetrahedron", h, np.asarray(case.BCB)[:, 0, :].T, "double")
+        # boundary hexes and wedges: header (neltp, nenl, ipordl, nshl, nshlb, nenbl, lcsyst, numnbc), the
+        # lcsyst of the element topology (a wedge block's face size tells its boundary rule)
+        for b in case.bnd:
+            ne, nshl, nb = len(b.ien), b.nshl, b.nshlb
+            lc = 2 if b.lcsyst == 2 else 3
+            h = [ne, nshl, 1, nshl, nb, nb, lc, 6]
+            name = LCSYST[lc]
+            f.write(f"connectivity boundary linear {name}", h, (np.asarray(b.ien, np.int32) + 1).T, "integer")
+            f.write(f"nbc codes linear {name}", h, np.asarray(b.iBCB, np.int32).T, "integer")
+            f.write(f"nbc values linear {name}", h, np.asarray(b.BCB)[:, 0, :].T, "double")
     return path

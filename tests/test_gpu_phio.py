@@ -10,7 +10,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from helpers import channel, mixed
+from helpers import channel, layered, mixed
 from phasta_gb300 import _lib as L
 from phasta_gb300 import phio
 from phasta_gb300.solver import GpuSolver
@@ -34,7 +34,8 @@ def _run(case, p, y, ac, out, steps=2):
     (lambda: channel(8, ac_scale=0.05, Kspace=10), L.PHGPU_FP64),
     (lambda: channel(8, ac_scale=0.05, Kspace=10), L.PHGPU_MIXED),
     (lambda: mixed(3, 3, (3, 3, 2), Kspace=10), L.PHGPU_MIXED),
-], ids=["channel8-fp64", "channel8-mixed", "mixed3-mixed"])
+    (lambda: layered(4, (2, 1, 2), periodic_x=False, Kspace=10), L.PHGPU_MIXED),
+], ids=["channel8-fp64", "channel8-mixed", "mixed3-mixed", "layered-open-mixed"])
 def test_run_from_phasta_files(tmp_path, make, precision):
     case, p, y, ac = make()
     p = dict(p, precision=precision, ap_mode=L.PHGPU_AP_LINEAR if precision == L.PHGPU_MIXED else L.PHGPU_AP_FD)

@@ -212,6 +212,10 @@ def _same_case(a, b):
     for k in ("x", "ien", "ienb", "iBCB", "BCB", "iBC", "BC", "iper", "ienh", "ienw"):
         assert np.array_equal(np.asarray(getattr(a, k)), np.asarray(getattr(b, k))), k
     assert a.h == pytest.approx(b.h, rel=1e-12)
+    assert [blk.lcsyst for blk in a.bnd] == [blk.lcsyst for blk in b.bnd]
+    for x, y in zip(a.bnd, b.bnd):
+        for k in ("ien", "iBCB", "BCB"):
+            assert np.array_equal(getattr(x, k), getattr(y, k)), (x.lcsyst, k)
 
 
 @pytest.mark.parametrize("make", [lambda: channel(4, ac_scale=0.05), lambda: mixed(3, 3, (3, 3, 2))],
@@ -236,6 +240,25 @@ def test_geombc_round_trip(tmp_path, make):
     (tmp_path / "o" / "geombc.dat.1").write_bytes(
         O.geombc_bytes(case.x, interior, nBC, codes, rows, case.iper + 1, boundary))
     _same_case(case, phio.read_case(tmp_path / "o"))
+
+
+@pytest.mark.parametrize("which", ["layered_open", "wedge_channel"])
+def test_geombc_round_trip_with_boundary_hexes_and_wedges(tmp_path, which):
+    """Boundary blocks of hexes (lcsyst 2) and of wedges with triangle or quadrilateral faces
+    (lcsyst 3 with nenbl 3 or 4) through the file: the wedge block's face size selects its
+    boundary rule on reading; BC codes and values per element, spread over the face nodes."""
+    from helpers import layered, wedgechannel
+    case = layered(4, (2, 1, 2), periodic_x=False)[0] if which == "layered_open" else wedgechannel((3, 3, 2))[0]
+    rng = np.random.default_rng(9)
+    for b in case.bnd:
+        n = len(b.ien)
+        b.iBCB = np.stack([np.full(n, 3), np.arange(n) % 4], axis=1).astype(np.int32)  # mass flux and pressure set
+        vals = np.zeros((n, 6))
+        vals[:, :2] = rng.standard_normal((n, 2))
+        b.BCB = np.repeat(vals[:, None, :], b.nshlb, axis=1)
+    phio.write_case(case, tmp_path)
+    back = phio.read_case(tmp_path)
+    _same_case(case, back)
 
 
 def test_geombc_boundary_values_are_masked_by_flux_codes(tmp_path):
