@@ -1346,20 +1346,19 @@ k_chunk_ress_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x
                                  K);
         __syncthreads();
         const int sbase = 4 * e0;
-        for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-            df64 acc[5];
-#pragma unroll
-            for (int k = 0; k < 5; ++k) acc[k] = df_make(0.f, 0.f);
+        // one thread per (chunk node, component), the node's slots in ascending order: the
+        // double-float sums are spread over all four warps (one thread per node left three
+        // quarters of the CTA waiting at the barrier)
+        for (int p = threadIdx.x; p < 5 * nn; p += blockDim.x) {
+            const int l = p / 5, k = p - 5 * l;
+            df64 acc = df_make(0.f, 0.f);
             const int s0 = scst[l] - sbase, s1 = scst[l + 1] - sbase;
             for (int s = s0; s < s1; ++s) {
                 const int sid = (int)scsr[s];
-                const float* sl = slot + kSplitSlot * (sid >> 2) + 5 * (sid & 3);
-#pragma unroll
-                for (int k = 0; k < 5; ++k) acc[k] = df_add(acc[k], df_make(sl[k], sl[20 + k]));
+                const float* sl = slot + kSplitSlot * (sid >> 2) + 5 * (sid & 3) + k;
+                acc = df_add(acc, df_make(sl[0], sl[20]));
             }
-            double* og = out + 5 * (size_t)h[4 + l];
-#pragma unroll
-            for (int k = 0; k < 5; ++k) og[k] = so[5 * l + k] + df_to_double(acc[k]);
+            out[5 * (size_t)h[4 + l] + k] = so[p] + df_to_double(acc);
         }
         __syncthreads();
     }
@@ -1623,16 +1622,14 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
     constexpr bool single = kFullSub * full_nsub<R>() >= kChunk;
     R* acc = sq + (with_q ? 12 * nn : 0);         // nn x 35 (multi-round only)
     R* slot = acc + (single ? 0 : kFullOut * nn); // (kChunk * nsub) x 35
-    // the connectivity of this thread's tet in each sub-batch of the first round, and its
-    // node's slot-list bounds, loaded before the staging so that their latency overlaps it
+    // the connectivity of this thread's tet in each sub-batch of the first round, loaded
+    // before the staging so that its latency overlaps it
     ushort4 lnp[4];
 #pragma unroll
     for (int sb = 0; sb < 4; ++sb) {
         const int el = min(sb * kFullSub + (int)(threadIdx.x >> 2), ne - 1);
         if (sb < full_nsub<R>()) lnp[sb] = ca.lien[e0 + el];
     }
-    const int cs_own0 = (int)threadIdx.x < nn ? ca.cstart[n0 + threadIdx.x] : 0;
-    const int cs_own1 = (int)threadIdx.x < nn ? ca.cstart[n0 + threadIdx.x + 1] : 0;
     // FP32 block diagonal alone: the state and coordinates packed per node (yb0..yb4, x0, x1,
     // x2) when given, two 16-byte loads per node
     bool packed = false;
@@ -1711,30 +1708,27 @@ k_chunk_full(ChunkArgs ca, int chunk0, const R* __restrict__ x, const R* __restr
         __syncthreads();
         const int lo = 4 * b0, hi = 4 * (b0 + kFullSub * nsub);
         if (kFullSub * nsub >= kChunk) {
-            // single round: sum the slots straight into the global arrays
-            for (int l = threadIdx.x; l < nn; l += blockDim.x) {
-                const bool own = l == (int)threadIdx.x;
-                const int s0 = own ? cs_own0 : ca.cstart[n0 + l], s1 = own ? cs_own1 : ca.cstart[n0 + l + 1];
-                R t[kFullOut];
-#pragma unroll
-                for (int k = 0; k < kFullOut; ++k) t[k] = R(0);
+            // single round: one thread per (chunk node, row of five slot values), the node's
+            // slots in ascending order, straight into the global arrays (one thread per node left
+            // most of the CTA waiting while 25 or 35 sums per node ran)
+            constexpr int NR = kFullOut / 5;
+            for (int p = threadIdx.x; p < NR * nn; p += blockDim.x) {
+                const int l = p / NR, r = p - NR * l;
+                const int s0 = ca.cstart[n0 + l], s1 = ca.cstart[n0 + l + 1];
+                R t[5] = {R(0), R(0), R(0), R(0), R(0)};
                 for (int s = s0; s < s1; ++s) {
-                    const R* sl = slot + kFullOut * (int)ca.csr[s];
+                    const R* sl = slot + kFullOut * (int)ca.csr[s] + 5 * r;
 #pragma unroll
-                    for (int k = 0; k < kFullOut; ++k) t[k] += sl[k];
+                    for (int k = 0; k < 5; ++k) t[k] += sl[k];
                 }
                 const size_t gn = ca.nodes[n0 + l];
-                if (!BD_ONLY && res) {
+                R* dst;
+                if (!BD_ONLY && r == 0) dst = res ? res + 5 * gn : nullptr;
+                else if (!BD_ONLY && r == 1) dst = rmes ? rmes + 5 * gn : nullptr;
+                else dst = bd ? bd + 25 * gn + 5 * (r - kBd / 5) : nullptr;
+                if (dst) {
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) res[5 * gn + k] += t[k];
-                }
-                if (!BD_ONLY && rmes) {
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) rmes[5 * gn + k] += t[5 + k];
-                }
-                if (bd) {
-#pragma unroll
-                    for (int k = 0; k < 25; ++k) bd[25 * gn + k] += t[kBd + k];
+                    for (int k = 0; k < 5; ++k) dst[k] += t[k];
                 }
             }
             return;
