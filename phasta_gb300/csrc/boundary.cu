@@ -270,10 +270,12 @@ int balloc(Ctx& C, T** p, size_t n) {
 int bnd_setup(Ctx& C, const phgpu_mesh* m) {
     if (m->nbblk <= 0) return PHGPU_OK;
     if (!m->bblk) return fail(C, PHGPU_ERR_INVALID, "nbblk > 0 with no boundary blocks");
-    static BndTab host[3];
-    bnd_tables_host(host);
-    BD_TRY(check(C, cudaMemcpyToSymbolAsync(c_btab, host, sizeof(host), 0, cudaMemcpyHostToDevice, C.stream),
+    std::vector<BndTab> host(3);
+    bnd_tables_host(host.data());
+    BD_TRY(check(C, cudaMemcpyToSymbolAsync(c_btab, host.data(), sizeof(BndTab) * 3, 0, cudaMemcpyHostToDevice,
+                                            C.stream),
                  "boundary tables"));
+    BD_TRY(check(C, cudaStreamSynchronize(C.stream), "boundary tables"));  // the source is a local
     for (int b = 0; b < m->nbblk; ++b) {
         const phgpu_bnd_block& B = m->bblk[b];
         if (B.lcsyst < 2 || B.lcsyst > 4 || B.nelem < 0 || (B.nelem > 0 && (!B.ien || !B.iBCB || !B.BCB)))

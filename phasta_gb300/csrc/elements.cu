@@ -51,12 +51,12 @@ __constant__ TetTables c_tab;
 __constant__ float c_shpf[4][4];   // single-precision copies (no conversions in FP32 kernels)
 __constant__ float c_qwtf;
 
-void upload_topo_tables(Ctx& C);
+int upload_topo_tables(Ctx& C);
 
 // tet point weight: symtet.c's 1/4 scaled by 4/3 (genint.f:72)
 constexpr double kTetQwt = (4.0 / 3.0) * 0.25;
 
-void upload_tables(Ctx& C) {
+int upload_tables(Ctx& C) {
     TetTables t;
     // symtet.c 4-point rule (barycentric (a,b,b,b) permutations), genint.f:72 Qwt *= 4/3
     const double a4 = 0.5854101966249685, b4 = 0.1381966011250150;
@@ -78,18 +78,22 @@ void upload_tables(Ctx& C) {
         t.shpb[q][3] = 1.0 - ptb[q][0] - ptb[q][1] - ptb[q][2];
         t.Qwtb[q] = 2.0 * A;
     }
-    check(C, cudaMemcpyToSymbolAsync(c_tab, &t, sizeof(t), 0, cudaMemcpyHostToDevice, C.stream),
-          "upload tables");
+    int rc = check(C, cudaMemcpyToSymbolAsync(c_tab, &t, sizeof(t), 0, cudaMemcpyHostToDevice, C.stream),
+                   "upload tables");
     float sf[4][4];
     for (int q = 0; q < 4; ++q)
         for (int a = 0; a < 4; ++a) sf[q][a] = (float)t.shp[q][a];
-    check(C, cudaMemcpyToSymbolAsync(c_shpf, sf, sizeof(sf), 0, cudaMemcpyHostToDevice, C.stream),
-          "upload tables");
-    static float qf;
-    qf = (float)t.Qwt[0];
-    check(C, cudaMemcpyToSymbolAsync(c_qwtf, &qf, sizeof(qf), 0, cudaMemcpyHostToDevice, C.stream),
-          "upload tables");
-    upload_topo_tables(C);
+    if (rc == PHGPU_OK)
+        rc = check(C, cudaMemcpyToSymbolAsync(c_shpf, sf, sizeof(sf), 0, cudaMemcpyHostToDevice, C.stream),
+                   "upload tables");
+    const float qf = (float)t.Qwt[0];
+    if (rc == PHGPU_OK)
+        rc = check(C, cudaMemcpyToSymbolAsync(c_qwtf, &qf, sizeof(qf), 0, cudaMemcpyHostToDevice, C.stream),
+                   "upload tables");
+    if (rc == PHGPU_OK) rc = upload_topo_tables(C);
+    // the sources are this function's locals
+    if (rc == PHGPU_OK) rc = check(C, cudaStreamSynchronize(C.stream), "upload tables");
+    return rc;
 }
 
 template <typename R>
@@ -2392,11 +2396,11 @@ void topo_tables_host(TopoTabD* t) {
     }
 }
 
-void upload_topo_tables(Ctx& C) {
+int upload_topo_tables(Ctx& C) {
     TopoTabD t[3];
     topo_tables_host(t);
-    static TopoTabD td[2];
-    static TopoTabF tf[2];
+    std::vector<TopoTabD> td(2);
+    std::vector<TopoTabF> tf(2);
     for (int k = 0; k < 2; ++k) {
         td[k] = t[k];
         for (int q = 0; q < 8; ++q) {
@@ -2407,8 +2411,15 @@ void upload_topo_tables(Ctx& C) {
             }
         }
     }
-    check(C, cudaMemcpyToSymbolAsync(c_topo, td, sizeof(td), 0, cudaMemcpyHostToDevice, C.stream), "upload tables");
-    check(C, cudaMemcpyToSymbolAsync(c_topof, tf, sizeof(tf), 0, cudaMemcpyHostToDevice, C.stream), "upload tables");
+    int rc = check(C, cudaMemcpyToSymbolAsync(c_topo, td.data(), sizeof(TopoTabD) * 2, 0, cudaMemcpyHostToDevice,
+                                              C.stream),
+                   "upload tables");
+    if (rc == PHGPU_OK)
+        rc = check(C, cudaMemcpyToSymbolAsync(c_topof, tf.data(), sizeof(TopoTabF) * 2, 0, cudaMemcpyHostToDevice,
+                                              C.stream),
+                   "upload tables");
+    if (rc == PHGPU_OK) rc = check(C, cudaStreamSynchronize(C.stream), "upload tables");
+    return rc;
 }
 
 template <typename R, int NEN, int MODE>

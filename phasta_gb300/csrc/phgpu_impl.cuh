@@ -345,7 +345,7 @@ void launch_topo_ress(Ctx& C, const float* yh, const float* ylo, const float* ac
 template <typename R>
 void launch_topo(Ctx& C, int mode, const R* x, const R* ya, const R* yb, const R* ac, R* res, R* rmes, R* bd,
                  int iabres, const int* skip, const R* ql = nullptr);
-void upload_tables(Ctx& C);
+int upload_tables(Ctx& C);
 int build_chunks(Ctx& C, const int* ien, const double* x_ref);
 // 4-byte words of a chunk record of ne elements and nn nodes, and the word offsets of its parts:
 // header {e0, ne, n0, nn}; node ids (nn); connectivity (ne ushort4); slot lists (4 ne ushort);
@@ -410,7 +410,7 @@ template <typename R> void i3pre(Ctx& C, const R* bd, R* EG);
 // Au1GMR + bc3per: q = sum_e EG_e p(iper)
 template <typename M, typename V> void ebe_ap(Ctx& C, const M* EG, const V* p, V* q);
 template <typename R> void launch_tangent(Ctx& C, const R* x, const R* y, R* lhsK, R* bd = nullptr);
-void upload_tangent_tables(Ctx& C);
+int upload_tangent_tables(Ctx& C);
 int configure_tangent_kernels(Ctx& C);
 // Spsi3pre: lhsK <- L_i^-1 lhsK U_j^-1 with the i3LU factors bd (device layouts)
 template <typename R> void spsi3pre(Ctx& C, const R* bd, R* lhsK);

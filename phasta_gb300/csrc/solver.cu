@@ -1446,7 +1446,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     T(check(C, cudaMemsetAsync(C.d_scal, 0, sizeof(double) * S_TOTAL, C.stream), "memset"));
     for (double* p : {C.d_y, C.d_ac, C.d_yold, C.d_acold})
         T(check(C, cudaMemsetAsync(p, 0, sizeof(double) * n5, C.stream), "memset"));
-    upload_tables(C);
+    T(upload_tables(C));
     T(sync(C));
     if (rc != PHGPU_OK) {
         phgpu_destroy(h);

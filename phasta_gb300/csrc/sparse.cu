@@ -196,7 +196,7 @@ static int tangent_setup(Ctx& C) {
     }
     S.h_ient = tien;
     int rc = dcopy(C, &S.d_ient, tien.data(), tien.size());
-    if (rc == PHGPU_OK) upload_tangent_tables(C);
+    if (rc == PHGPU_OK) rc = upload_tangent_tables(C);
     if (rc == PHGPU_OK) rc = configure_tangent_kernels(C);
     if (rc == PHGPU_OK) S.tan_ready = true;
     return rc;

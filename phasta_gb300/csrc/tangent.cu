@@ -416,10 +416,10 @@ void launch_one(Ctx& C, const int* d_ien, const int* d_map, const std::vector<in
 
 }  // namespace
 
-void upload_tangent_tables(Ctx& C) {
-    static TopoTabD td[3];
-    static TopoTabF tf[3];
-    topo_tables_host(td);
+int upload_tangent_tables(Ctx& C) {
+    std::vector<TopoTabD> td(3);
+    std::vector<TopoTabF> tf(3);
+    topo_tables_host(td.data());
     for (int k = 0; k < 3; ++k)
         for (int q = 0; q < 8; ++q) {
             tf[k].qwt[q] = (float)td[k].qwt[q];
@@ -428,8 +428,16 @@ void upload_tangent_tables(Ctx& C) {
                 for (int i = 0; i < 3; ++i) tf[k].shgl[q][i][a] = (float)td[k].shgl[q][i][a];
             }
         }
-    check(C, cudaMemcpyToSymbolAsync(c_tt, td, sizeof(td), 0, cudaMemcpyHostToDevice, C.stream), "tangent tables");
-    check(C, cudaMemcpyToSymbolAsync(c_ttf, tf, sizeof(tf), 0, cudaMemcpyHostToDevice, C.stream), "tangent tables");
+    int rc = check(C, cudaMemcpyToSymbolAsync(c_tt, td.data(), sizeof(TopoTabD) * 3, 0, cudaMemcpyHostToDevice,
+                                              C.stream),
+                   "tangent tables");
+    if (rc == PHGPU_OK)
+        rc = check(C, cudaMemcpyToSymbolAsync(c_ttf, tf.data(), sizeof(TopoTabF) * 3, 0, cudaMemcpyHostToDevice,
+                                              C.stream),
+                   "tangent tables");
+    // the sources are this function's locals
+    if (rc == PHGPU_OK) rc = check(C, cudaStreamSynchronize(C.stream), "tangent tables");
+    return rc;
 }
 
 int configure_tangent_kernels(Ctx& C) {

@@ -307,7 +307,7 @@ int topo_split_setup(Ctx& C) {
     if (C.split_ready || (C.nhex == 0 && C.nwedge == 0)) return PHGPU_OK;
     TopoTabD td[3];
     topo_tables_host(td);
-    static TopoTabF tf[2];
+    std::vector<TopoTabF> tf(2);
     for (int k = 0; k < 2; ++k)
         for (int q = 0; q < 8; ++q) {
             tf[k].qwt[q] = (float)td[k].qwt[q];
@@ -316,8 +316,10 @@ int topo_split_setup(Ctx& C) {
                 for (int i = 0; i < 3; ++i) tf[k].shgl[q][i][a] = (float)td[k].shgl[q][i][a];
             }
         }
-    int rc = check(C, cudaMemcpyToSymbolAsync(c_trf, tf, sizeof(tf), 0, cudaMemcpyHostToDevice, C.stream),
+    int rc = check(C, cudaMemcpyToSymbolAsync(c_trf, tf.data(), sizeof(TopoTabF) * 2, 0, cudaMemcpyHostToDevice,
+                                              C.stream),
                    "split-residual tables");
+    if (rc == PHGPU_OK) rc = check(C, cudaStreamSynchronize(C.stream), "split-residual tables");  // a local source
     if (rc != PHGPU_OK) return rc;
     std::vector<double> x(3 * (size_t)C.N);
     rc = check(C, cudaMemcpy(x.data(), C.d_x, sizeof(double) * x.size(), cudaMemcpyDeviceToHost), "download x");
