@@ -659,7 +659,8 @@ k_chunk_lin_pipe(const uint4* __restrict__ rec, const int* __restrict__ rec_off,
 #pragma unroll
             for (int k = 0; k < 5; ++k) og[k] = so[5 * l + k] + acc[k];
         }
-        __syncthreads();
+        // no barrier here: the next iteration's first barrier precedes every write of the slots,
+        // of this data stage and of this record stage
     }
     cp_async_wait<0>();
 }
@@ -1364,7 +1365,8 @@ k_chunk_ress_pipe(ChunkArgs ca, int chunk0, int nch, const float* __restrict__ x
             }
             out[5 * (size_t)h[4 + l] + k] = so[p] + df_to_double(acc);
         }
-        __syncthreads();
+        // no barrier here: the next iteration's first barrier precedes every write of the slots,
+        // of this data stage and of this id stage
     }
     cp_async_wait<0>();
 }
