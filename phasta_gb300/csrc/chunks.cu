@@ -203,7 +203,7 @@ int build_chunks(Ctx& C, const int* ien, const double* x_ref) {
         using T = typename std::remove_reference<decltype(v)>::type::value_type;
         cudaError_t e = cudaMalloc((void**)d, sizeof(T) * std::max<size_t>(v.size(), 1));
         if (e != cudaSuccess) return check(C, e, "cudaMalloc chunks");
-        return check(C, cudaMemcpy(*d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice), "upload chunks");
+        return h2d(C, *d, v.data(), sizeof(T) * v.size(), "upload chunks");
     };
     int rc = PHGPU_OK;
     auto T = [&](int s) { if (rc == PHGPU_OK) rc = s; };

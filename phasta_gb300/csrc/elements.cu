@@ -2434,15 +2434,15 @@ template <typename R, int NEN, int TOPO>
 int configure_topo_kernels(Ctx& C) {
     int rc = PHGPU_OK;
     auto T = [&](cudaError_t e) { if (rc == PHGPU_OK) rc = check(C, e, "cudaFuncSetAttribute"); };
-    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    T(smem_attr(k_topo<R, NEN, TOPO, TM_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)topo_smem<R, NEN, TM_RES>()));
-    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    T(smem_attr(k_topo<R, NEN, TOPO, TM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)topo_smem<R, NEN, TM_MODRES>()));
-    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    T(smem_attr(k_topo<R, NEN, TOPO, TM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)topo_smem<R, NEN, TM_LIN>()));
-    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    T(smem_attr(k_topo<R, NEN, TOPO, TM_FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)topo_smem<R, NEN, TM_FULL>()));
-    T(cudaFuncSetAttribute(k_topo<R, NEN, TOPO, TM_QREC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    T(smem_attr(k_topo<R, NEN, TOPO, TM_QREC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)topo_smem<R, NEN, TM_QREC>()));
     return rc;
 }
@@ -2538,13 +2538,13 @@ int configure_chunk_kernels(Ctx& C) {
     const int rs = (int)res_smem<R>(C), fs = (int)full_smem<R>(C);
     int rc = PHGPU_OK;
     auto T = [&](cudaError_t e) { if (rc == PHGPU_OK) rc = check(C, e, "cudaFuncSetAttribute"); };
-    T(cudaFuncSetAttribute(k_chunk_res<R, RM_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    T(smem_attr(k_chunk_res<R, RM_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            rs + (int)q_smem<R>(C)));
-    T(cudaFuncSetAttribute(k_chunk_qrec<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qrec_smem<R>(C)));
-    T(cudaFuncSetAttribute(k_chunk_res<R, RM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
-    T(cudaFuncSetAttribute(k_chunk_res<R, RM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
-    T(cudaFuncSetAttribute(k_chunk_full<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fs + (int)q_smem<R>(C)));
-    T(cudaFuncSetAttribute(k_chunk_full<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    T(smem_attr(k_chunk_qrec<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qrec_smem<R>(C)));
+    T(smem_attr(k_chunk_res<R, RM_MODRES>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
+    T(smem_attr(k_chunk_res<R, RM_LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs));
+    T(smem_attr(k_chunk_full<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fs + (int)q_smem<R>(C)));
+    T(smem_attr(k_chunk_full<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)full_smem<R, true>(C)));
     return rc;
 }
@@ -2556,14 +2556,14 @@ int configure_element_kernels(Ctx& C) {
     int rc = configure_chunk_kernels<double>(C);
     if (rc == PHGPU_OK) rc = configure_chunk_kernels<float>(C);
     if (rc == PHGPU_OK)
-        rc = check(C, cudaFuncSetAttribute(k_chunk_resh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)resh_smem(C)),
+        rc = check(C, smem_attr(k_chunk_resh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)resh_smem(C)),
                    "cudaFuncSetAttribute");
     if (rc == PHGPU_OK)
-        rc = check(C, cudaFuncSetAttribute(k_chunk_ress<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        rc = check(C, smem_attr(k_chunk_ress<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)ress_smem(C)),
                    "cudaFuncSetAttribute");
     if (rc == PHGPU_OK)
-        rc = check(C, cudaFuncSetAttribute(k_chunk_ress<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        rc = check(C, smem_attr(k_chunk_ress<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)(ress_smem(C) + q_smem<float>(C))),
                    "cudaFuncSetAttribute");
     if (rc == PHGPU_OK) {
@@ -2574,7 +2574,7 @@ int configure_element_kernels(Ctx& C) {
         auto grid_of = [&](const void* f, size_t smem, int* grid) {
             int per_sm = 0;
             if (rc == PHGPU_OK)
-                rc = check(C, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                rc = check(C, smem_attr(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                            "cudaFuncSetAttribute");
             if (rc == PHGPU_OK)
                 rc = check(C, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, kChunk, smem), "occupancy");

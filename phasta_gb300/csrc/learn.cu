@@ -1153,9 +1153,9 @@ int build_graph(Ctx& C) {
     if (N >= (1 << SHIFT)) return fail(C, PHGPU_ERR_UNSUPPORTED, "learned preconditioner: more than 2^26 nodes");
     std::vector<double> x(3 * (size_t)N);
     std::vector<int> iper(N), iBC(N);
-    NT_TRY(check(C, cudaMemcpy(x.data(), C.d_x, sizeof(double) * x.size(), cudaMemcpyDeviceToHost), "graph: x"));
-    NT_TRY(check(C, cudaMemcpy(iper.data(), C.d_iper, sizeof(int) * N, cudaMemcpyDeviceToHost), "graph: iper"));
-    NT_TRY(check(C, cudaMemcpy(iBC.data(), C.d_iBC, sizeof(int) * N, cudaMemcpyDeviceToHost), "graph: iBC"));
+    NT_TRY(d2h(C, x.data(), C.d_x, sizeof(double) * x.size(), "graph: x"));
+    NT_TRY(d2h(C, iper.data(), C.d_iper, sizeof(int) * N, "graph: iper"));
+    NT_TRY(d2h(C, iBC.data(), C.d_iBC, sizeof(int) * N, "graph: iBC"));
     struct Blk {
         const int* ien;
         size_t ne;
@@ -1266,11 +1266,11 @@ int build_graph(Ctx& C) {
         for (int n = 0; n < N; ++n)
             x4[n] = make_float4((float)x[3 * (size_t)n], (float)x[3 * (size_t)n + 1], (float)x[3 * (size_t)n + 2], 0.f);
         NT_TRY(nalloc(C, &T.d_x4, (size_t)N));
-        NT_TRY(check(C, cudaMemcpy(T.d_x4, x4.data(), sizeof(float4) * N, cudaMemcpyHostToDevice), "graph"));
+        NT_TRY(h2d(C, T.d_x4, x4.data(), sizeof(float4) * N, "graph"));
     }
-    NT_TRY(check(C, cudaMemcpy(T.d_nstart, nstart.data(), sizeof(int) * nstart.size(), cudaMemcpyHostToDevice), "graph"));
-    if (w > 0) NT_TRY(check(C, cudaMemcpy(T.d_nbr, ent.data(), sizeof(unsigned) * w, cudaMemcpyHostToDevice), "graph"));
-    NT_TRY(check(C, cudaMemcpy(T.d_act, act.data(), N, cudaMemcpyHostToDevice), "graph"));
+    NT_TRY(h2d(C, T.d_nstart, nstart.data(), sizeof(int) * nstart.size(), "graph"));
+    if (w > 0) NT_TRY(h2d(C, T.d_nbr, ent.data(), sizeof(unsigned) * w, "graph"));
+    NT_TRY(h2d(C, T.d_act, act.data(), N, "graph"));
     T.graph = true;
     return PHGPU_OK;
 }
@@ -1294,18 +1294,18 @@ int num_sms() {
     return sms > 0 ? sms : 152;
 }
 
-bool g_attr_done = false;
+// once per context (function attributes belong to the device the context runs on)
 int set_attrs(Ctx& C) {
-    if (g_attr_done) return PHGPU_OK;
-    NT_TRY(check(C, cudaFuncSetAttribute(k_net_enc, cudaFuncAttributeMaxDynamicSharedMemorySize, kEncSmem), "attr"));
-    NT_TRY(check(C, cudaFuncSetAttribute(k_net_mp<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMpSmem), "attr"));
-    NT_TRY(check(C, cudaFuncSetAttribute(k_net_mp<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMpSmem), "attr"));
-    NT_TRY(check(C, cudaFuncSetAttribute(k_net_mp<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMpSmem), "attr"));
-    NT_TRY(check(C, cudaFuncSetAttribute(k_net_mp<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMpSmem), "attr"));
-    NT_TRY(check(C, cudaFuncSetAttribute(k_bwd_top, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopSmem), "attr"));
-    NT_TRY(check(C, cudaFuncSetAttribute(k_bwd_node<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNodeSmem), "attr"));
-    NT_TRY(check(C, cudaFuncSetAttribute(k_bwd_node<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNodeSmem), "attr"));
-    g_attr_done = true;
+    if (C.net.attrs_set) return PHGPU_OK;
+    NT_TRY(check(C, smem_attr(k_net_enc, cudaFuncAttributeMaxDynamicSharedMemorySize, kEncSmem), "attr"));
+    NT_TRY(check(C, smem_attr(k_net_mp<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMpSmem), "attr"));
+    NT_TRY(check(C, smem_attr(k_net_mp<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMpSmem), "attr"));
+    NT_TRY(check(C, smem_attr(k_net_mp<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMpSmem), "attr"));
+    NT_TRY(check(C, smem_attr(k_net_mp<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMpSmem), "attr"));
+    NT_TRY(check(C, smem_attr(k_bwd_top, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopSmem), "attr"));
+    NT_TRY(check(C, smem_attr(k_bwd_node<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNodeSmem), "attr"));
+    NT_TRY(check(C, smem_attr(k_bwd_node<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNodeSmem), "attr"));
+    C.net.attrs_set = true;
     return PHGPU_OK;
 }
 
@@ -1373,12 +1373,12 @@ int train_alloc(Ctx& C) {
     const int ntile = (C.N + TILE - 1) / TILE;
     R.grid = std::max(1, std::min(ntile, num_sms()));
     NT_TRY(nalloc(C, &R.d_part, (size_t)R.grid * PSTRIDE));
-    NT_TRY(check(C, cudaMemset(R.d_part, 0, sizeof(float) * (size_t)R.grid * PSTRIDE), "memset"));
+    NT_TRY(dzero(C, R.d_part, sizeof(float) * (size_t)R.grid * PSTRIDE, "memset"));
     NT_TRY(nalloc(C, &R.d_grad, NPARAM));
     NT_TRY(nalloc(C, &R.d_m, NPARAM));
     NT_TRY(nalloc(C, &R.d_v, NPARAM));
-    NT_TRY(check(C, cudaMemset(R.d_m, 0, sizeof(float) * NPARAM), "memset"));
-    NT_TRY(check(C, cudaMemset(R.d_v, 0, sizeof(float) * NPARAM), "memset"));
+    NT_TRY(dzero(C, R.d_m, sizeof(float) * NPARAM, "memset"));
+    NT_TRY(dzero(C, R.d_v, sizeof(float) * NPARAM, "memset"));
     return PHGPU_OK;
 }
 
@@ -1444,7 +1444,7 @@ int net_setup(Ctx& C) {
     const size_t HNs = (size_t)C.N * H;
     if (!T.d_w) {
         NT_TRY(nalloc(C, &T.d_w, NPARAM));
-        NT_TRY(check(C, cudaMemset(T.d_w, 0, sizeof(float) * NPARAM), "memset"));
+        NT_TRY(dzero(C, T.d_w, sizeof(float) * NPARAM, "memset"));
     }
     if (!T.d_ctx) {
         NT_TRY(nalloc(C, &T.d_ctx, (size_t)FCTX * C.N));
@@ -1524,12 +1524,12 @@ int upload_vec(Ctx& C, const double* h, float* d) {
     std::vector<float> t(5 * (size_t)N);
     for (int n = 0; n < N; ++n)
         for (int k = 0; k < 5; ++k) t[5 * (size_t)n + k] = (float)h[(size_t)k * N + n];
-    return phgpu::check(C, cudaMemcpy(d, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice), "upload vector");
+    return phgpu::h2d(C, d, t.data(), sizeof(float) * t.size(), "upload vector");
 }
 int download_vec(Ctx& C, const float* d, double* h) {
     const int N = C.N;
     std::vector<float> t(5 * (size_t)N);
-    NT_TRY(phgpu::check(C, cudaMemcpy(t.data(), d, sizeof(float) * t.size(), cudaMemcpyDeviceToHost), "download vector"));
+    NT_TRY(phgpu::d2h(C, t.data(), d, sizeof(float) * t.size(), "download vector"));
     for (int n = 0; n < N; ++n)
         for (int k = 0; k < 5; ++k) h[(size_t)k * N + n] = t[5 * (size_t)n + k];
     return PHGPU_OK;
@@ -1581,10 +1581,10 @@ int phgpu_net_graph(phgpu_ctx* h, int* nstart, unsigned* nbr, long long cap, lon
         geo[3] = C.net.rh;
     }
     if (nstart)
-        NT_TRY(phgpu::check(C, cudaMemcpy(nstart, C.net.d_nstart, sizeof(int) * ((size_t)C.N + 1), cudaMemcpyDeviceToHost), "graph"));
+        NT_TRY(phgpu::d2h(C, nstart, C.net.d_nstart, sizeof(int) * ((size_t)C.N + 1), "graph"));
     if (nbr) {
         if (cap < C.net.nnz) return phgpu::fail(C, PHGPU_ERR_TOO_LARGE, "phgpu_net_graph: nbr holds fewer than nnz entries");
-        NT_TRY(phgpu::check(C, cudaMemcpy(nbr, C.net.d_nbr, sizeof(unsigned) * C.net.nnz, cudaMemcpyDeviceToHost), "graph"));
+        NT_TRY(phgpu::d2h(C, nbr, C.net.d_nbr, sizeof(unsigned) * C.net.nnz, "graph"));
     }
     return PHGPU_OK;
 }
@@ -1608,7 +1608,7 @@ int phgpu_net_features(phgpu_ctx* h, float* out) {
     NT_TRY(sync_net(C));
     if (out) {
         std::vector<__nv_bfloat16> t((size_t)phgpu::netk::FCTX * C.N);
-        NT_TRY(phgpu::check(C, cudaMemcpy(t.data(), C.net.d_ctx, sizeof(__nv_bfloat16) * t.size(), cudaMemcpyDeviceToHost), "features"));
+        NT_TRY(phgpu::d2h(C, t.data(), C.net.d_ctx, sizeof(__nv_bfloat16) * t.size(), "features"));
         for (size_t i = 0; i < t.size(); ++i) out[i] = __bfloat162float(t[i]);
     }
     return PHGPU_OK;
@@ -1631,10 +1631,10 @@ int phgpu_net_apply(phgpu_ctx* h, const double* v, double* z, float* hidden, flo
     const size_t HNs = (size_t)C.N * H;
     if (hidden) {
         std::vector<__nv_bfloat16> t(4 * HNs);
-        NT_TRY(phgpu::check(C, cudaMemcpy(t.data(), C.net.tr.d_hs, sizeof(__nv_bfloat16) * t.size(), cudaMemcpyDeviceToHost), "hidden"));
+        NT_TRY(phgpu::d2h(C, t.data(), C.net.tr.d_hs, sizeof(__nv_bfloat16) * t.size(), "hidden"));
         for (size_t i = 0; i < t.size(); ++i) hidden[i] = __bfloat162float(t[i]);
     }
-    if (out) NT_TRY(phgpu::check(C, cudaMemcpy(out, C.net.tr.d_out, sizeof(float) * 8 * (size_t)C.N, cudaMemcpyDeviceToHost), "out"));
+    if (out) NT_TRY(phgpu::d2h(C, out, C.net.tr.d_out, sizeof(float) * 8 * (size_t)C.N, "out"));
     return PHGPU_OK;
 }
 
@@ -1654,9 +1654,9 @@ int phgpu_net_loss_grad(phgpu_ctx* h, const double* v, const double* t, double* 
     phgpu::backward(C, C.d_t32, C.d_t32b, C.net.d_ctx, C.net.tr.d_scal + 1);
     NT_TRY(sync_net(C));
     double l = 0.0;
-    NT_TRY(phgpu::check(C, cudaMemcpy(&l, C.net.tr.d_scal + 1, sizeof(double), cudaMemcpyDeviceToHost), "loss"));
+    NT_TRY(phgpu::d2h(C, &l, C.net.tr.d_scal + 1, sizeof(double), "loss"));
     if (loss) *loss = l / std::max(5.0 * C.net.nact, 1.0);
-    if (grad) NT_TRY(phgpu::check(C, cudaMemcpy(grad, C.net.tr.d_grad, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost), "grad"));
+    if (grad) NT_TRY(phgpu::d2h(C, grad, C.net.tr.d_grad, sizeof(float) * NPARAM, "grad"));
     return PHGPU_OK;
 }
 
@@ -1745,7 +1745,7 @@ int phgpu_net_train(phgpu_ctx* h, const phgpu_net_train_config* cfg, phgpu_net_t
     cudaEventRecord(e1, C.stream);
     NT_TRY(sync_net(C));
     std::vector<double> losses((size_t)nsteps);
-    NT_TRY(phgpu::check(C, cudaMemcpy(losses.data(), R.d_scal + 1, sizeof(double) * nsteps, cudaMemcpyDeviceToHost), "losses"));
+    NT_TRY(phgpu::d2h(C, losses.data(), R.d_scal + 1, sizeof(double) * nsteps, "losses"));
     const double nm = std::max(5.0 * T.nact, 1.0);
     if (out) {
         double f = 0.0, l = 0.0;

@@ -165,6 +165,7 @@ struct NetTrain {
 };
 struct NetCtx {
     bool graph = false;
+    bool attrs_set = false;               // the kernels' shared-memory limits, on this context's device
     long long nnz = 0;
     int* d_nstart = nullptr;              // N+1 CSR row starts
     unsigned* d_nbr = nullptr;            // neighbour | periodic shift code << 26
@@ -421,6 +422,30 @@ int colour(Ctx& C, int n_nodes, const int* ien, int nen, int ne, std::vector<int
 
 int check(Ctx& C, cudaError_t e, const char* what);
 int fail(Ctx& C, int code, const std::string& msg);
+// The dynamic shared memory a kernel may be launched with.  Function attributes belong to the
+// process (per device), not to a context, so a context never lowers one to its own mesh's need
+// (another context's launches would then fail): every call checks the need against the
+// device's opt-in limit less the kernel's static shared memory and sets the attribute to that
+// limit.  Occupancy follows the shared memory of each launch, not this attribute.
+template <typename F>
+inline cudaError_t smem_attr(F f, cudaFuncAttribute attr, int need) {
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, f);
+    if (e != cudaSuccess) return e;
+    const int limit = optin - (int)fa.sharedSizeBytes;
+    if (need > limit) return cudaErrorInvalidValue;
+    return cudaFuncSetAttribute(f, attr, limit);
+}
+// host <-> device copies and clears of a context, all on its own stream (ordered after the
+// context's kernels; never the legacy stream, which neither orders against a non-blocking
+// stream nor may synchronise while another thread captures a graph): the copies are complete
+// on return, the clear is ordered before the context's next work
+int h2d(Ctx& C, void* dst, const void* src, size_t bytes, const char* what);
+int d2h(Ctx& C, void* dst, const void* src, size_t bytes, const char* what);
+int dzero(Ctx& C, void* dst, size_t bytes, const char* what);
 
 // ---- learned preconditioner (learn.cu) ----
 int net_setup(Ctx& C);                      // graph, buffers and the Z basis (first use)

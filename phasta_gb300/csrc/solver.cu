@@ -27,6 +27,34 @@ int fail(Ctx& C, int code, const std::string& msg) {
 }
 
 namespace {
+// a synchronous copy cannot be part of a graph: every host set-up runs before a capture starts
+int not_capturing(Ctx& C, const char* what) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(C.stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+        return fail(C, PHGPU_ERR_CUDA, std::string(what) + ": host copy while the stream is captured");
+    return PHGPU_OK;
+}
+}  // namespace
+
+int h2d(Ctx& C, void* dst, const void* src, size_t bytes, const char* what) {
+    if (bytes == 0) return PHGPU_OK;
+    int rc = not_capturing(C, what);
+    if (rc == PHGPU_OK) rc = check(C, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, C.stream), what);
+    return rc != PHGPU_OK ? rc : check(C, cudaStreamSynchronize(C.stream), what);
+}
+
+int d2h(Ctx& C, void* dst, const void* src, size_t bytes, const char* what) {
+    if (bytes == 0) return PHGPU_OK;
+    int rc = not_capturing(C, what);
+    if (rc == PHGPU_OK) rc = check(C, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, C.stream), what);
+    return rc != PHGPU_OK ? rc : check(C, cudaStreamSynchronize(C.stream), what);
+}
+
+int dzero(Ctx& C, void* dst, size_t bytes, const char* what) {
+    return bytes == 0 ? PHGPU_OK : check(C, cudaMemsetAsync(dst, 0, bytes, C.stream), what);
+}
+
+namespace {
 
 #define PH_TRY(x)                          \
     do {                                   \
@@ -1410,8 +1438,9 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
         phgpu_destroy(h);
         return rc;
     }
+    // on the context's stream; the host vectors stay alive until the stream synchronisation below
     auto up = [&](void* d, const void* s, size_t bytes) {
-        T(check(C, cudaMemcpy(d, s, bytes, cudaMemcpyHostToDevice), "upload mesh"));
+        if (bytes) T(check(C, cudaMemcpyAsync(d, s, bytes, cudaMemcpyHostToDevice, C.stream), "upload mesh"));
     };
     up(C.d_ienb, ienb.data(), sizeof(int4) * ienb.size());
     if (C.nhex > 0) {
@@ -1441,7 +1470,7 @@ int phgpu_create(const phgpu_mesh* m, const phgpu_config* cfg, phgpu_ctx** out) 
     if (C.nmaster) up(C.d_mst, mst.data(), sizeof(int) * C.nmaster);
     up(C.d_slv_start, sstart.data(), sizeof(int) * sstart.size());
     if (C.nslave) up(C.d_slv, slv.data(), sizeof(int) * C.nslave);
-    T(check(C, cudaDeviceSynchronize(), "upload mesh"));
+    T(check(C, cudaStreamSynchronize(C.stream), "upload mesh"));
     T(check(C, cudaMemsetAsync(C.d_count, 0, sizeof(unsigned int), C.stream), "memset"));
     T(check(C, cudaMemsetAsync(C.d_scal, 0, sizeof(double) * S_TOTAL, C.stream), "memset"));
     for (double* p : {C.d_y, C.d_ac, C.d_yold, C.d_acold})

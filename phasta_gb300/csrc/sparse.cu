@@ -58,7 +58,7 @@ int dcopy(Ctx& C, T** d, const T* h, size_t n) {
         return PHGPU_ERR_NOMEM;
     }
     if (n == 0) return PHGPU_OK;
-    return check(C, cudaMemcpy(*d, h, sizeof(T) * n, cudaMemcpyHostToDevice), "upload sparse structure");
+    return h2d(C, *d, h, sizeof(T) * n, "upload sparse structure");
 }
 
 // block index of (element, a, b) for every element of a block (element-major, a-major)
@@ -226,7 +226,7 @@ int sparse_setup(Ctx& C) {
     std::vector<int> rs(N + 1), bcol(S.nnzb), bcolp(S.nnzb), brow(S.nnzb);
     std::vector<int> iper(N);
     {
-        const int rci = check(C, cudaMemcpy(iper.data(), C.d_iper, sizeof(int) * N, cudaMemcpyDeviceToHost), "download iper");
+        const int rci = d2h(C, iper.data(), C.d_iper, sizeof(int) * N, "download iper");
         if (rci != PHGPU_OK) return rci;
     }
     for (int n = 0; n <= N; ++n) rs[n] = S.colm[n] - 1;

@@ -443,12 +443,12 @@ int upload_tangent_tables(Ctx& C) {
 int configure_tangent_kernels(Ctx& C) {
     int rc = PHGPU_OK;
     auto T = [&](cudaError_t e) { if (rc == PHGPU_OK) rc = check(C, e, "cudaFuncSetAttribute"); };
-    T(cudaFuncSetAttribute(k_tangent<double, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<double, 4>()));
-    T(cudaFuncSetAttribute(k_tangent<double, 8, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<double, 8>()));
-    T(cudaFuncSetAttribute(k_tangent<double, 6, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<double, 6>()));
-    T(cudaFuncSetAttribute(k_tangent<float, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<float, 4>()));
-    T(cudaFuncSetAttribute(k_tangent<float, 8, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<float, 8>()));
-    T(cudaFuncSetAttribute(k_tangent<float, 6, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<float, 6>()));
+    T(smem_attr(k_tangent<double, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<double, 4>()));
+    T(smem_attr(k_tangent<double, 8, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<double, 8>()));
+    T(smem_attr(k_tangent<double, 6, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<double, 6>()));
+    T(smem_attr(k_tangent<float, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<float, 4>()));
+    T(smem_attr(k_tangent<float, 8, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<float, 8>()));
+    T(smem_attr(k_tangent<float, 6, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tan_smem<float, 6>()));
     return rc;
 }
 

@@ -322,7 +322,7 @@ int topo_split_setup(Ctx& C) {
     if (rc == PHGPU_OK) rc = check(C, cudaStreamSynchronize(C.stream), "split-residual tables");  // a local source
     if (rc != PHGPU_OK) return rc;
     std::vector<double> x(3 * (size_t)C.N);
-    rc = check(C, cudaMemcpy(x.data(), C.d_x, sizeof(double) * x.size(), cudaMemcpyDeviceToHost), "download x");
+    rc = d2h(C, x.data(), C.d_x, sizeof(double) * x.size(), "download x");
     if (rc != PHGPU_OK) return rc;
     std::vector<float2> Ih, Iw;
     if (C.nhex > 0) flux_integrals(td[0], 8, x, C.h_ienh, C.nhex, Ih);
@@ -334,8 +334,7 @@ int topo_split_setup(Ctx& C) {
             return PHGPU_ERR_NOMEM;
         }
         if (!pr->empty()) {
-            rc = check(C, cudaMemcpy(*d, pr->data(), sizeof(float2) * pr->size(), cudaMemcpyHostToDevice),
-                       "upload flux integrals");
+            rc = h2d(C, *d, pr->data(), sizeof(float2) * pr->size(), "upload flux integrals");
             if (rc != PHGPU_OK) return rc;
         }
     }
@@ -360,10 +359,10 @@ void launch_topo_ress(Ctx& C, const float* yh, const float* ylo, const float* ac
 int configure_topo_ress(Ctx& C) {
     int rc = PHGPU_OK;
     auto T = [&](cudaError_t e) { if (rc == PHGPU_OK) rc = check(C, e, "cudaFuncSetAttribute"); };
-    T(cudaFuncSetAttribute(k_topo_ress<8, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem<8, false>()));
-    T(cudaFuncSetAttribute(k_topo_ress<8, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem<8, true>()));
-    T(cudaFuncSetAttribute(k_topo_ress<6, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem<6, false>()));
-    T(cudaFuncSetAttribute(k_topo_ress<6, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem<6, true>()));
+    T(smem_attr(k_topo_ress<8, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem<8, false>()));
+    T(smem_attr(k_topo_ress<8, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem<8, true>()));
+    T(smem_attr(k_topo_ress<6, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem<6, false>()));
+    T(smem_attr(k_topo_ress<6, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem<6, true>()));
     return rc;
 }
 
