@@ -476,17 +476,40 @@ k_mgs(V* w, const V* __restrict__ up, const double* __restrict__ beta_prev, cons
     T* wv = reinterpret_cast<T*>(w);
     const T* upv = reinterpret_cast<const T*>(up);
     const T* ujv = reinterpret_cast<const T*>(uj);
-    for (size_t i = t0; i < nv; i += stride) {
-        T wi = wv[i];
+    // one element of this thread's stride: update w, add its product to the dot
+    auto step = [&](size_t i, T wi, const T& ui, const T& ji) {
         if (up) {
-            const T ui = upv[i];
 #pragma unroll
             for (int k = 0; k < X::W; ++k) X::set(wi, k, X::at(wi, k) - bv * X::at(ui, k));
             wv[i] = wi;
         }
-        const T u2 = self ? wi : ujv[i];
+        const T u2 = self ? wi : ji;
 #pragma unroll
         for (int k = 0; k < X::W; ++k) acc.add(X::at(wi, k), X::at(u2, k));
+    };
+    // two strides per pass, every load of both issued before the first store (the store to w
+    // would otherwise hold back the next loads); the order of the updates and of the dot's
+    // additions is the one-stride loop's
+    size_t i = t0;
+    for (; i + stride < nv; i += 2 * stride) {
+        const T wa = wv[i], wb = wv[i + stride];
+        T ua{}, ub{}, ja{}, jb{};
+        if (up) {
+            ua = upv[i];
+            ub = upv[i + stride];
+        }
+        if (!self) {
+            ja = ujv[i];
+            jb = ujv[i + stride];
+        }
+        step(i, wa, ua, ja);
+        step(i + stride, wb, ub, jb);
+    }
+    for (; i < nv; i += stride) {
+        T ui{}, ji{};
+        if (up) ui = upv[i];
+        if (!self) ji = ujv[i];
+        step(i, wv[i], ui, ji);
     }
     for (size_t i = X::W * nv + t0; i < n; i += stride) {
         V wi = w[i];
