@@ -346,10 +346,29 @@ __global__ void k_bd_out(const double* __restrict__ b, double* __restrict__ a, i
 #pragma unroll
         for (int j = 0; j < 5; ++j) a[(size_t)(i + 5 * j) * N + n] = b[25 * (size_t)n + 5 * i + j];
 }
+// four entries per thread and pass when both arrays start on 16-byte boundaries (16-byte
+// loads or stores on each side), element by element for the rest
 template <typename A, typename B>
 __global__ void k_convert(const A* __restrict__ a, B* __restrict__ b, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        b[i] = (B)a[i];
+    const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    const size_t n4 = (((uintptr_t)a | (uintptr_t)b) & 15) == 0 ? n / 4 : 0;
+    for (size_t i = t0; i < n4; i += stride) {
+        A v[4];
+        if constexpr (sizeof(A) == 8) {
+            const double2 p = reinterpret_cast<const double2*>(a)[2 * i], q = reinterpret_cast<const double2*>(a)[2 * i + 1];
+            v[0] = p.x; v[1] = p.y; v[2] = q.x; v[3] = q.y;
+        } else {
+            const float4 p = reinterpret_cast<const float4*>(a)[i];
+            v[0] = p.x; v[1] = p.y; v[2] = p.z; v[3] = p.w;
+        }
+        if constexpr (sizeof(B) == 8) {
+            reinterpret_cast<double2*>(b)[2 * i] = make_double2((B)v[0], (B)v[1]);
+            reinterpret_cast<double2*>(b)[2 * i + 1] = make_double2((B)v[2], (B)v[3]);
+        } else {
+            reinterpret_cast<float4*>(b)[i] = make_float4((B)v[0], (B)v[1], (B)v[2], (B)v[3]);
+        }
+    }
+    for (size_t i = 4 * n4 + t0; i < n; i += stride) b[i] = (B)a[i];
 }
 
 // ---------------- reductions (FP64 accumulation, fixed grid => deterministic) ----------------
@@ -675,7 +694,22 @@ void to_f32(Ctx& C, const double* a, float* b, size_t n) {
     ++C.launches;
 }
 __global__ void k_split(const double* __restrict__ a, float* __restrict__ hi, float* __restrict__ lo, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    // four entries per thread and pass with 16-byte loads and stores when all three arrays allow
+    const size_t n4 = (((uintptr_t)a | (uintptr_t)hi | (uintptr_t)lo) & 15) == 0 ? n / 4 : 0;
+    for (size_t i = t0; i < n4; i += stride) {
+        const double2 p = reinterpret_cast<const double2*>(a)[2 * i], q = reinterpret_cast<const double2*>(a)[2 * i + 1];
+        const double v[4] = {p.x, p.y, q.x, q.y};
+        float h[4], l[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            h[k] = (float)v[k];
+            l[k] = (float)(v[k] - (double)h[k]);
+        }
+        reinterpret_cast<float4*>(hi)[i] = make_float4(h[0], h[1], h[2], h[3]);
+        reinterpret_cast<float4*>(lo)[i] = make_float4(l[0], l[1], l[2], l[3]);
+    }
+    for (size_t i = 4 * n4 + t0; i < n; i += stride) {
         const double v = a[i];
         const float h = (float)v;
         hi[i] = h;

@@ -226,7 +226,33 @@ __global__ void k_update_dy(double* __restrict__ Dy, const V* __restrict__ U, si
             cl[j] = (float)(yB[j] - (double)ch[j]);
         }
         __syncthreads();
-        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+        // four entries per thread and pass: 16-byte loads of every basis row and of Dy (the rows
+        // start on 256-byte boundaries); each entry's sum over j in the same order as one at a time
+        const size_t n4 = ((reinterpret_cast<uintptr_t>(U) & 15) == 0 && ld % 4 == 0 &&
+                           (reinterpret_cast<uintptr_t>(Dy) & 15) == 0)
+                              ? n / 4
+                              : 0;
+        for (size_t i4 = t0; i4 < n4; i4 += stride) {
+            df64 acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+            for (int j = 0; j < iKs; ++j) {
+                const float4 u = *reinterpret_cast<const float4*>(U + (size_t)j * ld + 4 * i4);
+                const df64 c = df_make(ch[j], cl[j]);
+                acc[0] = df_add(acc[0], df_mul(c, u.x));
+                acc[1] = df_add(acc[1], df_mul(c, u.y));
+                acc[2] = df_add(acc[2], df_mul(c, u.z));
+                acc[3] = df_add(acc[3], df_mul(c, u.w));
+            }
+            double2* d = reinterpret_cast<double2*>(Dy + 4 * i4);
+            double2 d0 = d[0], d1 = d[1];
+            d0.x = d0.x + df_to_double(acc[0]);
+            d0.y = d0.y + df_to_double(acc[1]);
+            d1.x = d1.x + df_to_double(acc[2]);
+            d1.y = d1.y + df_to_double(acc[3]);
+            d[0] = d0;
+            d[1] = d1;
+        }
+        for (size_t i = 4 * n4 + t0; i < n; i += stride) {
             df64 acc{0.f, 0.f};
             for (int j = 0; j < iKs; ++j) acc = df_add(acc, df_mul(df_make(ch[j], cl[j]), U[(size_t)j * ld + i]));
             Dy[i] = Dy[i] + df_to_double(acc);
