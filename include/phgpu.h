@@ -418,6 +418,14 @@ int phgpu_net_train(phgpu_ctx* ctx, const phgpu_net_train_config* cfg, phgpu_net
  *     counter itself, so no zeroing is required of the caller. */
 int phgpu_rstat_noalloc(const double* res, int nshg, double* totres, void* stream);
 
+/* Self-test of the bounded wait that guards every bulk copy of the pipelined sweeps (no context
+ * needed; current device): one CTA arms an mbarrier that expects two arrivals, gives it one, and
+ * waits at most `tries` times (1 .. 524,288, the sweeps' own limit: about 2 s, at about 4 us per
+ * try on a GB300); *status receives 8 when the
+ * wait gave up (the value a sweep sets in its error word before it ends), 0 if the phase
+ * completed.  PHGPU_ERR_INVALID for a null status or tries out of range. */
+int phgpu_selftest_wait_limit(int tries, int* status);
+
 #ifdef __cplusplus
 }
 #endif

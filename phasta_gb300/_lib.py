@@ -132,6 +132,7 @@ def lib():
         "phgpu_residual_norm_dev": ([vp, _dp], C.c_int),
         "phgpu_sweep_dev": ([vp, C.c_int], C.c_int),
         "phgpu_rstat_noalloc": ([vp, C.c_int, vp, vp], C.c_int),
+        "phgpu_selftest_wait_limit": ([C.c_int, _ip], C.c_int),
         "phgpu_genadj": ([C.POINTER(Mesh), C.c_int, _ip, _ip, C.POINTER(C.c_int)], C.c_int),
         "phgpu_nnz_tot": ([vp, C.POINTER(C.c_int)], C.c_int),
         "phgpu_elmgmrs": ([vp, _dp, _dp, _dp, _dp, _dp], C.c_int),

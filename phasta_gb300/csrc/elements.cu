@@ -506,11 +506,29 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
 }
 // a wait that gives up: false after kMbarTries unsuccessful tries (each may suspend the thread
 // for a short, hardware-chosen time), so that a copy that never completes cannot hang the GPU
-constexpr int kMbarTries = 1 << 22;
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-    for (int i = 0; i < kMbarTries; ++i)
+constexpr int kMbarTries = kMbarTriesMax;
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int tries = kMbarTries) {
+    for (int i = 0; i < tries; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+// self-test of the bounded wait: an mbarrier that expects two arrivals and gets one never
+// completes its phase, so mbar_wait gives up after `tries` tries; status[0] is then the bit a
+// sweep sets when its bulk copy does not complete
+__global__ void k_wait_limit_probe(int tries, int* status) {
+    __shared__ unsigned long long bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 2);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive(&bar);
+        status[0] = mbar_wait(&bar, 0, tries) ? 0 : kPipeCopyFailed;
+    }
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -2856,4 +2874,24 @@ void launch_boundary(Ctx& C, const double* y, double* res) {
     launch_bnd_blocks(C, y, res);
 }
 
+// the bounded mbarrier wait of the pipelined sweeps, made to run out (k_wait_limit_probe)
+int selftest_wait_limit(int tries, int* status) {
+    int* d = nullptr;
+    cudaError_t e = cudaMalloc((void**)&d, sizeof(int));
+    if (e != cudaSuccess) return PHGPU_ERR_NOMEM;
+    e = cudaMemset(d, 0xff, sizeof(int));
+    if (e == cudaSuccess) {
+        k_wait_limit_probe<<<1, 32>>>(tries, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(status, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? PHGPU_OK : PHGPU_ERR_CUDA;
+}
+
 }  // namespace phgpu
+
+extern "C" int phgpu_selftest_wait_limit(int tries, int* status) {
+    if (!status || tries < 1 || tries > phgpu::kMbarTriesMax) return PHGPU_ERR_INVALID;
+    return phgpu::selftest_wait_limit(tries, status);
+}

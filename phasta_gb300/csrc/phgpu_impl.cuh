@@ -361,6 +361,7 @@ __host__ __device__ constexpr int chunk_record_words(int ne, int nn) { return re
 void pack_xb(Ctx& C);
 // bit of flag[1] that the pipelined linearized product sets when a bulk copy did not complete
 constexpr int kPipeCopyFailed = 8;
+constexpr int kMbarTriesMax = 1 << 19;  // tries of a bounded mbarrier wait before it gives up (~2 s)
 constexpr const char* kPipeCopyMsg = "pipelined linearized product: a bulk copy did not complete in time";
 int configure_element_kernels(Ctx& C);
 // time the variants of the pipelined linearized product and split residual on the resident

@@ -28,6 +28,14 @@ def test_create_rejects_invalid_arguments_before_touching_the_device(gpu_lib):
     assert gpu_lib.phgpu_last_error(None) == b"null context"
 
 
+def test_wait_self_test_rejects_bad_arguments_before_touching_the_device(gpu_lib):
+    st = C.c_int(-1)
+    assert gpu_lib.phgpu_selftest_wait_limit(0, C.byref(st)) == L.PHGPU_ERR_INVALID
+    assert gpu_lib.phgpu_selftest_wait_limit((1 << 19) + 1, C.byref(st)) == L.PHGPU_ERR_INVALID
+    assert gpu_lib.phgpu_selftest_wait_limit(16, None) == L.PHGPU_ERR_INVALID
+    assert st.value == -1
+
+
 def test_struct_layouts_match_the_header_as_gcc_lays_them_out(tmp_path):
     """Every struct of include/phgpu.h: sizeof and the offset of every field as gcc computes them
     (tests/abi/layout.c), against the ctypes declarations."""

@@ -9,10 +9,14 @@ run after the device is set up.
 * Boundary hex and wedge blocks are checked when the context uploads them: a topology other
   than lcsyst 2, 3, 4 or connectivity outside the nodes is PHGPU_ERR_INVALID, and the failed
   create leaves no context behind.
+* The bounded mbarrier wait that guards the pipelined sweeps' bulk copies, made to run out on a
+  phase that can never complete: it gives up and reports the sweeps' copy-failure value, and
+  the device stays usable.
 """
 from __future__ import annotations
 
 import copy
+import ctypes as C
 
 import numpy as np
 import pytest
@@ -86,6 +90,33 @@ def test_boundary_blocks_are_checked(gpu_lib, which):
     assert e.value.code == L.PHGPU_ERR_INVALID
 
     # the context still works after the failed creates
+    g, o = GpuSolver(case, p), pyoracle.Oracle(case, p)
+    try:
+        assert rel(g.ElmRes(y, ac), o.ElmRes(y, ac)) < 1e-10
+    finally:
+        g.close()
+
+
+def test_bounded_wait_runs_out_and_reports(gpu_lib):
+    """phgpu_selftest_wait_limit: one CTA arms an mbarrier for two arrivals, gives it one and
+    waits through mbar_wait, the wait of every bulk copy of the pipelined sweeps, with a small
+    try limit: the wait gives up and the status is 8, the value a sweep writes to its error word
+    before its CTA ends (the solve then returns PHGPU_ERR_CUDA)."""
+    import time
+    per_try = []
+    for tries in (1, 64, 1024):
+        st = C.c_int(-1)
+        t0 = time.perf_counter()
+        assert gpu_lib.phgpu_selftest_wait_limit(tries, C.byref(st)) == 0
+        dt = time.perf_counter() - t0
+        assert st.value == 8
+        per_try.append(dt / tries)
+    # each try suspends the thread for at most a hardware-chosen time: the sweeps' 2^19 tries
+    # must end within seconds
+    print(f"bounded wait: {1e6 * per_try[-1]:.2f} us per try, 2^19 tries ~ {per_try[-1] * 524288:.1f} s")
+    assert per_try[-1] * 524288 < 10.0
+    # the device and the library are usable afterwards
+    case, p, y, ac = channel(4)
     g, o = GpuSolver(case, p), pyoracle.Oracle(case, p)
     try:
         assert rel(g.ElmRes(y, ac), o.ElmRes(y, ac)) < 1e-10
