@@ -2709,6 +2709,7 @@ void select_sweep_variants(Ctx& C, int lin_minb, int ress_minb) {
 constexpr double kTuneGain = 0.05;
 constexpr double kTuneMinMs = 0.5;
 int autotune_sweeps(Ctx& C) {
+    Range nv("phgpu: sweep autotuner");
     if (C.tuned || C.tune_forced || C.cfg.no_pipe || C.E == 0) return PHGPU_OK;
     const size_t n5 = 5 * (size_t)C.N;
     const long long l0 = C.launches;

@@ -13,6 +13,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/phgpu.h"
 
 namespace phgpu {
@@ -421,6 +423,13 @@ template <typename M, typename V> void sparse_ap(Ctx& C, const M* lhsK, const V*
 // greedy first-fit element colouring (solver.cu)
 int colour(Ctx& C, int n_nodes, const int* ien, int nen, int ne, std::vector<int>& order, std::vector<int>& start);
 
+// a named range on the NVTX timeline of a profiler (host-side phases; no cost without a tool)
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
 int check(Ctx& C, cudaError_t e, const char* what);
 int fail(Ctx& C, int code, const std::string& msg);
 // The dynamic shared memory a kernel may be launched with.  Function attributes belong to the

@@ -669,6 +669,7 @@ bool cycle_graph(Ctx& C, int min_iters, bool sparse, bool ebe, bool learned = fa
 // new cycle recomputes R - A Dy only when lgmres_common > 0 (SolGMRs, solgmr.f:526-537)
 template <typename V>
 int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = false) {
+    Range nv("phgpu: GMRES cycles");
     // SolGMRe restarts from the true residual and stops without the minIters test (solgmr.f:130-210)
     const bool ebe = C.cfg.ap_mode == PHGPU_AP_EBE;
     const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE || ebe;
@@ -882,6 +883,7 @@ int gmres(Ctx& C, phgpu_stats* st, int lgmres_common = 0, bool unorm_ready = fal
 // round trip): residual R (d_res), ||R||^2 (S_TMP3), BDiag and its LU factors (status in flag[1]),
 // L^-1 R in d_res and ||L^-1 R||^2 (S_TMP0); for the matrix-free solver also ypre = U y.
 int assemble_and_factor(Ctx& C, int lhs, bool asm_bd, bool sparse, bool ebe) {
+    Range nv("phgpu: assembly and block LU");
     const size_t N = C.N, n5 = 5 * N;
     if (C.cfg.precision == PHGPU_FP64) {
         if (sparse) {
@@ -968,6 +970,7 @@ int assemble_and_factor(Ctx& C, int lhs, bool asm_bd, bool sparse, bool ebe) {
 // BDiag and the tangent (iprec = lhs, itrdrv.f:456-457); lhs = 0 reuses the factored BDiag
 // and the preconditioned tangent of the last lhs = 1 solve
 int solve_dev(Ctx& C, phgpu_stats* st, int lhs, int lgmres_common) {
+    Range nv("phgpu: flow solve");
     const size_t N = C.N, n5 = 5 * N;
     const bool ebe = C.cfg.ap_mode == PHGPU_AP_EBE;
     const bool sparse = C.cfg.ap_mode == PHGPU_AP_SPARSE || ebe;
@@ -1103,6 +1106,7 @@ void step_graph_free(StepGraph& G) {
 // itrUpdate + itrBC: the kernels of time_step_dev in the same order with the same arguments,
 // the cycle's norms read on the device instead of on the host.
 int step_graph_build(Ctx& C, int nitr) {
+    Range nv("phgpu: step graph capture");
     StepGraph& G = C.stepg;
     const size_t n5 = 5 * (size_t)C.N;
     const int K = C.cfg.Kspace;
@@ -1219,6 +1223,7 @@ int step_graph_build(Ctx& C, int nitr) {
 // one time step through the graph; *used = false when the graph could not be built (the caller
 // then launches the step kernel by kernel)
 int step_graph_run(Ctx& C, int nitr, phgpu_stats* st, bool* used) {
+    Range nv("phgpu: time step (graph)");
     StepGraph& G = C.stepg;
     *used = false;
     phgpu_config key = C.cfg;
@@ -1274,6 +1279,7 @@ int step_graph_run(Ctx& C, int nitr, phgpu_stats* st, bool* used) {
 }
 
 int time_step_dev(Ctx& C, int nitr, phgpu_stats* st) {
+    Range nv("phgpu: time step");
     if (step_graph_eligible(C, nitr)) {
         bool used = false;
         PH_TRY(autotune_sweeps(C));  // before the kernels are fixed in the graph

@@ -51,3 +51,38 @@ def test_run_from_phasta_files(tmp_path, make, precision):
     assert np.all(np.isfinite(ya)) and not np.array_equal(ya, y)
     m, n, ok = phio.checkphasta(tmp_path / "a", tmp_path / "b", 0.0)
     assert n == 2 and m == 0.0 and ok
+
+
+@pytest.mark.parametrize("make", [
+    lambda: channel(8, ac_scale=0.05, Kspace=10),
+    lambda: layered(4, (2, 1, 2), periodic_x=False, Kspace=10),
+], ids=["channel8", "layered-open"])
+def test_checkpoint_and_resume_is_bitwise_the_uninterrupted_run(tmp_path, make):
+    """checkpoint (restar('out ') of yold/acold after itrUpdate) at step 2 of a four-step run; a
+    new context started from that restart file (restar('in  ')) runs steps 3 and 4: bitwise the
+    uninterrupted run's state.  Mixed precision with the linearized product: the restart's
+    state is all that a time step carries from one step to the next."""
+    case, p, y, ac = make()
+    p = dict(p, precision=L.PHGPU_MIXED, ap_mode=L.PHGPU_AP_LINEAR, outer_residual=L.PHGPU_RES_SPLITDF)
+    ck = tmp_path / "ck"
+    ck.mkdir()
+    g = GpuSolver(case, p)
+    try:
+        g.set_tuning(4, 3)
+        for step in range(1, 5):
+            _yo, _ao, y, ac, _st = g.time_step(y, ac, nitr=2)
+            if step == 2:
+                phio.write_restart(ck, 2, y.reshape(5, -1), ac.reshape(5, -1))
+    finally:
+        g.close()
+    yr, acr, lstep = phio.read_restart(ck, 2, case.nshg)
+    assert lstep == 2
+    yr, acr = yr.reshape(-1), acr.reshape(-1)
+    g2 = GpuSolver(case, p)
+    try:
+        g2.set_tuning(4, 3)
+        for _ in range(2):
+            _yo, _ao, yr, acr, _st = g2.time_step(yr, acr, nitr=2)
+    finally:
+        g2.close()
+    assert np.array_equal(yr, y) and np.array_equal(acr, ac)
