@@ -15,6 +15,8 @@
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <queue>
+#include <tuple>
 #include <type_traits>
 
 #include "phgpu_impl.cuh"
@@ -107,29 +109,81 @@ int build_chunks(Ctx& C, const int* ien, const double* x_ref) {
         for (int l = 0; l < nn; ++l) local[tmp[l]] = -1;
     }
     cnode_start[nch] = (int)cnodes.size();
-    // greedy colouring of chunks (shared nodes conflict)
-    std::vector<uint64_t> m0(N, 0), m1(N, 0);
-    std::vector<int> ccol(nch);
-    int ncol = 0;
+    // DSatur colouring of the chunks (chunks that share a node conflict; Brelaz 1979): the chunk
+    // with the most distinct colours among its neighbours next, ties by degree, then by chunk
+    // number; each takes the smallest free colour.  Fewer and more even colours than first fit
+    // in Morton order (13 against 17 at 64^3 x 6, the smallest colour 74 chunks against 1), so
+    // fewer launches and tails per sweep; deterministic.
+    std::vector<int> nch_start(N + 1, 0);
+    for (int j = 0; j < cnode_start[nch]; ++j) nch_start[cnodes[j] + 1]++;
+    for (int n = 0; n < N; ++n) nch_start[n + 1] += nch_start[n];
+    std::vector<int> nch_list(cnode_start[nch]);
+    {
+        std::vector<int> pos(nch_start.begin(), nch_start.end() - 1);
+        for (int c = 0; c < nch; ++c)
+            for (int j = cnode_start[c]; j < cnode_start[c + 1]; ++j) nch_list[pos[cnodes[j]]++] = c;
+    }
+    std::vector<int64_t> adj_start(nch + 1, 0);
+    std::vector<int> adj;
+    adj.reserve((size_t)nch * 32);
     for (int c = 0; c < nch; ++c) {
-        uint64_t f0 = 0, f1 = 0;
+        const size_t b0 = adj.size();
         for (int j = cnode_start[c]; j < cnode_start[c + 1]; ++j) {
-            f0 |= m0[cnodes[j]];
-            f1 |= m1[cnodes[j]];
+            const int n = cnodes[j];
+            for (int k = nch_start[n]; k < nch_start[n + 1]; ++k)
+                if (nch_list[k] != c) adj.push_back(nch_list[k]);
         }
+        std::sort(adj.begin() + b0, adj.end());
+        adj.erase(std::unique(adj.begin() + b0, adj.end()), adj.end());
+        adj_start[c + 1] = (int64_t)adj.size();
+    }
+    std::vector<int> ccol(nch, -1), sat(nch, 0);
+    std::vector<uint64_t> u0(nch, 0), u1(nch, 0);  // colours taken by a chunk's neighbours
+    // (saturation, degree, -chunk): the largest first
+    std::priority_queue<std::tuple<int, int, int>> pq;
+    for (int c = 0; c < nch; ++c) pq.emplace(0, (int)(adj_start[c + 1] - adj_start[c]), -c);
+    int ncol = 0;
+    while (!pq.empty()) {
+        const auto [sc, dc, nc] = pq.top();
+        pq.pop();
+        const int c = -nc;
+        if (ccol[c] >= 0 || sc != sat[c]) continue;  // done, or an outdated entry
         int col;
-        if (~f0) col = __builtin_ctzll(~f0);
-        else if (~f1) col = 64 + __builtin_ctzll(~f1);
+        if (~u0[c]) col = __builtin_ctzll(~u0[c]);
+        else if (~u1[c]) col = 64 + __builtin_ctzll(~u1[c]);
         else {
             C.err = "chunk colouring needs more than 128 colours";
             return PHGPU_ERR_UNSUPPORTED;
         }
         ccol[c] = col;
         ncol = std::max(ncol, col + 1);
-        for (int j = cnode_start[c]; j < cnode_start[c + 1]; ++j) {
-            if (col < 64) m0[cnodes[j]] |= 1ull << col;
-            else m1[cnodes[j]] |= 1ull << (col - 64);
+        for (int64_t k = adj_start[c]; k < adj_start[c + 1]; ++k) {
+            const int o = adj[k];
+            if (ccol[o] >= 0) continue;
+            uint64_t& w = col < 64 ? u0[o] : u1[o];
+            const uint64_t bit = 1ull << (col & 63);
+            if (w & bit) continue;
+            w |= bit;
+            ++sat[o];
+            pq.emplace(sat[o], (int)(adj_start[o + 1] - adj_start[o]), -o);
         }
+        (void)dc;
+    }
+    // no two chunks of a colour share a node: their node sums run concurrently without atomics
+    {
+        std::vector<int> last(N, -1);
+        std::vector<int> by_col(nch);
+        std::iota(by_col.begin(), by_col.end(), 0);
+        std::stable_sort(by_col.begin(), by_col.end(), [&](int x, int y) { return ccol[x] < ccol[y]; });
+        for (int c : by_col)
+            for (int j = cnode_start[c]; j < cnode_start[c + 1]; ++j) {
+                const int n = cnodes[j];
+                if (last[n] == ccol[c]) {
+                    C.err = "chunk colouring put two chunks that share a node in one colour";
+                    return PHGPU_ERR_INVALID;
+                }
+                last[n] = ccol[c];
+            }
     }
     // chunks sorted by colour (stable), elements follow their chunk
     std::vector<int> corder(nch);
